@@ -1,0 +1,371 @@
+"""Benchmark: j3d ray-cast frames of the 28.09M-triangle torus at 1920x1080.
+
+One step = one frame (primary ray + closest hit + G-buffer record + shadow ray
++ plain matcap shading, j3d's view::render_scene) for each of 32 seeded
+cameras. `value` = Mrays/s (primary + shadow rays) with the mesh, BVH and
+canvas resident in HBM; `e2e` = the same through the C-ABI per frame
+including the device->host copies of the G-buffer and RGBA image into
+pinned host memory (the arrays j3d's view reads back every frame).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
+
+--impl reference times the CPU path on the host cores (the oracle port of
+j3d's canvas + qbvh, all threads) on a bounded sample of the same frames.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+W_, H_ = 1920, 1080
+N_CAMERAS = 32
+NODE_BYTES = 128      # one BVH4 node: 4 child AABBs (96 B) + 4 refs, padded
+TRI_BYTES = 48        # 12 B index triple + 36 B of vertices per tested triangle
+RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+class CpuRenderer:
+    """The oracle (port of j3d's CPU path: canvas::update_canvas + canvas_to_image
+    over a 4-wide binned-SAH BVH, row-parallel like pooled_parallel_for) on the
+    same mesh and cameras, timed on a bounded sample of rows."""
+
+    def __init__(self, wl, n_threads: int):
+        import oracle.oracle as O
+        from j3d_gb300 import scene as S
+        self.O, self.wl, self.n_threads = O, wl, n_threads
+        self.m = O.Mesh(wl.vertices, wl.triangles, 4, n_threads)
+        self.I16 = np.eye(4, dtype=np.float32).reshape(16)
+        mn, mx, self.diag = O.prepare_scene([(self.m.min_bb, self.m.max_bb)], [self.I16])
+        _, _, self.piv = O.unzoom(mn, mx, self.diag)
+        self.cam = O.camera_with_focal(S.lib().j3dg_focal_for_vfov(60.0, 0.768))
+        self.Pi = O.invert_projection_matrix(O.make_projection_matrix(self.cam, wl.width, wl.height))
+        self.st = O.settings(shadow=True, edges=False)
+        self.mc, self.cav = O.make_matcap(0)
+
+    def sample(self, cams, budget_s: float):
+        """Bands of 8 whole rows every 72 rows of each camera's frame until the
+        time budget is spent. Returns (rays, seconds, node_visits, tri_tests, rows)."""
+        O, wl = self.O, self.wl
+        rays = visits = tests = rows_done = 0
+        secs = 0.0
+        for c in cams:
+            pose = wl.poses[c]
+            v = O.view(pose, O.invert_orthonormal(pose), self.piv, self.diag, self.Pi, self.cam.near_clipping_plane)
+            pix = O.fresh_pixels(wl.width, wl.height)
+            for y0 in range(0, wl.height, 72):
+                y1 = min(wl.height - 1, y0 + 7)
+                t0 = time.perf_counter()
+                s = O.update_canvas(pix, [(self.m, self.I16, 1)], v, self.st, rect=(0, y0, wl.width - 1, y1),
+                                    n_threads=self.n_threads)
+                band = np.ascontiguousarray(pix[y0:y1 + 1])
+                im = np.zeros(band.shape, np.uint32)
+                O.canvas_to_image(band, im, v, self.st, self.mc, self.cav)
+                secs += time.perf_counter() - t0
+                rays += s.rays
+                visits += s.node_visits
+                tests += s.tri_tests
+                rows_done += y1 - y0 + 1
+                if secs > budget_s:
+                    return rays, secs, visits, tests, rows_done
+        return rays, secs, visits, tests, rows_done
+
+
+def run_reference(args):
+    """CPU arm: the oracle port of j3d's renderer on all host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle.oracle as O
+    from j3d_gb300 import build as B, workloads as Wk
+    B.build()
+    O.build()
+    wl = Wk.config1(N_CAMERAS, W_, H_)
+    n_threads = os.cpu_count() or 1
+    cpu = CpuRenderer(wl, n_threads)
+    per_step = max(2.0, min(15.0, args.cpu_total / max(1, args.warmup + args.steps)))
+    vals = []
+    total_rays = 0
+    for i in range(args.warmup + args.steps):
+        r = cpu.sample((i % N_CAMERAS,), per_step)
+        if i >= args.warmup:
+            vals.append(r[0] / r[1] / 1e6)
+            total_rays += r[0]
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded displaced torus, no dataset)", "config": CONFIG,
+            "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": n_threads, "kind": "port",
+                             "sample": f"per step ~{per_step:.1f} s of bands of 8 rows every 72 rows of one "
+                                       f"camera's 1920x1080 frame (primary + shadow + shading), {total_rays} rays "
+                                       "timed; the reference itself cannot be built (jtk absent, SSE-only canvas)"},
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "bvh_build_s": round(cpu.m.build_seconds, 3)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+METRIC = "Mrays/s & frame ms, 28M-tri mesh @1080p, 1 GB300, learned vs plain vs CPU qbvh (plain GPU path)"
+CONFIG = {"workload": "torus R=1 r=0.35 5300x2650 grid, 28,090,000 tris / 14,045,000 verts, 32 cameras r 2.5-4, "
+                      "1920x1080, primary + shadow, plain red-wax matcap", "cameras": N_CAMERAS,
+          "resolution": [W_, H_], "l2": "inputs larger than L2 (BVH + leaf triangles ~1.9 GB)"}
+
+
+def run_own(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from j3d_gb300 import (Canvas, Context, Matcap, Mesh, Scene, build as B, camera_for_vfov, settings,
+                           workloads as Wk)
+    B.build()
+    wl = Wk.config1(N_CAMERAS, W_, H_)
+    ctx = Context(local)
+    t0 = time.perf_counter()
+    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    build_wall = time.perf_counter() - t0
+    info = mesh.info()
+    # a second build with warm allocator gives the steady build time
+    mesh2 = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    build_ms = mesh2.info().build_ms
+    mesh2.close()
+    sc = Scene()
+    sc.add_object(mesh)
+    sc.prepare_scene()
+    sc.unzoom()
+    cv = Canvas(ctx, W_, H_)
+    cv.set_camera(camera_for_vfov(60.0))
+    cv.set_background_color()
+    cv.update_settings(settings(shadow=True, edges=False))
+    mc = Matcap.make(ctx, 0)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    # rays per frame (primary + shadow) and the GPU's own traversal counters
+    prim = W_ * H_
+    shadow_rays = []
+    ctx.set_counting(True)
+    for p in wl.poses:
+        sc.set_pose(p)
+        cv.render_frame(sc, mc)
+        px = cv.get_pixels()
+        shadow_rays.append(int((px["object_id"] != 0xFFFFFFFF).sum()))
+    gvis, gtests = ctx.read_counters(reset=True)
+    ctx.set_counting(False)
+    rays_per_step = prim * N_CAMERAS + sum(shadow_rays)
+
+    def step():
+        for p in wl.poses:
+            sc.set_pose(p)
+            cv.render_frame(sc, mc)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ctx.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        torch.distributed.barrier()
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    clk = clocks.stop()
+    value = rays_per_step * ws / (ms / 1e3) / 1e6
+
+    # per-frame kernel time (one k_render launch per frame in plain mode)
+    fe0 = [torch.cuda.Event(enable_timing=True) for _ in wl.poses]
+    fe1 = [torch.cuda.Event(enable_timing=True) for _ in wl.poses]
+    for i, p in enumerate(wl.poses):
+        sc.set_pose(p)
+        fe0[i].record(stream)
+        cv.render_frame(sc, mc)
+        fe1[i].record(stream)
+    ctx.synchronize()
+    frame_ms = [a.elapsed_time(b) for a, b in zip(fe0, fe1)]
+
+    # end to end through the C-ABI: render + G-buffer and image into pinned host memory
+    hp = torch.empty(H_ * W_ * 32, dtype=torch.uint8, pin_memory=True)
+    hi = torch.empty(H_ * W_ * 4, dtype=torch.uint8, pin_memory=True)
+    from j3d_gb300 import _ffi
+    for p in wl.poses[:2]:
+        sc.set_pose(p)
+        cv.render_frame(sc, mc)
+        _ffi.lib().j3dg_canvas_get_pixels(cv.h, hp.data_ptr())
+        _ffi.lib().j3dg_canvas_get_image(cv.h, hi.data_ptr())
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for p in wl.poses:
+            sc.set_pose(p)
+            cv.render_frame(sc, mc)
+            assert _ffi.lib().j3dg_canvas_get_pixels(cv.h, hp.data_ptr()) == 0
+            assert _ffi.lib().j3dg_canvas_get_image(cv.h, hi.data_ptr()) == 0
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = rays_per_step / e2e_s / 1e6
+    # host -> device per frame: the FrameParams kernel argument block (the
+    # instance table is unchanged between frames and not re-sent)
+    h2d = N_CAMERAS * 512
+    d2h = N_CAMERAS * (H_ * W_ * 36)
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # CPU baseline (oracle port) on a bounded sample; also gives the
+    # algorithmic bytes per ray of the 4-wide SAH BVH
+    cpu = None
+    if not args.no_cpu:
+        import oracle.oracle as O
+        O.build()
+        n_threads = os.cpu_count() or 1
+        cr = CpuRenderer(wl, n_threads)
+        r = cr.sample((0, 1), args.cpu_budget)
+        cpu = (r[0], r[1], r[2], r[3], cr.m.build_seconds, r[4], n_threads)
+    peak, peak_kind = peaks()
+    if cpu:
+        node_per_ray = cpu[2] / cpu[0]
+        tri_per_ray = cpu[3] / cpu[0]
+    else:
+        node_per_ray = gvis / rays_per_step
+        tri_per_ray = gtests / rays_per_step
+    alg_bytes = prim * N_CAMERAS * RECORD_BYTES + rays_per_step * (node_per_ray * NODE_BYTES + tri_per_ray * TRI_BYTES)
+    kernel_ms_step = float(np.sum(frame_ms))
+    achieved = alg_bytes / (kernel_ms_step / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced torus, no dataset)",
+        "config": dict(CONFIG, parallelism="replicas" if ws > 1 else "single GPU",
+                       frame_ms_mean=round(ms / N_CAMERAS, 4), frame_ms_p50=round(float(np.median(frame_ms)), 4),
+                       rays_per_step=rays_per_step, shadow_ray_fraction=round(sum(shadow_rays) / (prim * N_CAMERAS), 4),
+                       bvh_build_ms=round(build_ms, 3), bvh_first_build_wall_s=round(build_wall, 3),
+                       bvh_nodes=info.n_nodes, bvh_depth=info.max_depth, leaf_size=args.leaf,
+                       mesh_device_bytes=int(info.device_bytes),
+                       bvh_build_mtris_per_s=round(28_090_000 / (build_ms / 1e3) / 1e6, 1),
+                       gpu_node_visits_per_ray=round(gvis / rays_per_step, 3),
+                       gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "k_render", "peak_kind": peak_kind,
+                     "bytes_per_ray": round(alg_bytes / rays_per_step, 1),
+                     "node_visits_per_ray": round(node_per_ray, 3), "tri_tests_per_ray": round(tri_per_ray, 3),
+                     "per_ray_model": "36 B per primary ray + node_visits*128 B + tri_tests*48 B (oracle BVH4 SAH)"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": N_CAMERAS * args.steps,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = {"value": round(cpu[0] / cpu[1] / 1e6, 4), "unit": "Mrays/s", "cores": cpu[6],
+                                "kind": "port",
+                                "sample": f"{cpu[5]} rows of the 1920x1080 frames of cameras 0-1 (bands of 8 rows every "
+                                          f"72), {cpu[0]} rays in {cpu[1]:.1f} s; oracle BVH build {cpu[4]:.2f} s"}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="own", choices=["own", "reference"])
+    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
+    ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_own(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

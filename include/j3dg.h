@@ -1,0 +1,284 @@
+/*
+ * j3dg.h -- C-ABI of libj3dgpu.so, the GB300 (sm_103a) implementation of
+ * j3d's ray-cast rendering hot path.
+ *
+ * The reference has no FFI for this path: its boundary is the in-process C++
+ * API of jtk::qbvh (built at scene.cpp:23, queried at canvas.cpp:762,786,854
+ * and vox.cpp:307,333) and, above it, class canvas (canvas.h:27-101) driven by
+ * view::render_scene (view.cpp:421-430). Every entry point below names the
+ * reference call it replaces. All entry points:
+ *   - are extern "C", take plain pointers and sizes, never throw;
+ *   - return j3dg_status (J3DG_OK == 0); j3dg_last_error() gives the text;
+ *   - accept host or device pointers for bulk arrays (detected per call) --
+ *     device pointers must live on the context's device;
+ *   - run on the context's single CUDA stream. A context, and everything made
+ *     from it, must not be used from two threads at once (j3d serialises the
+ *     same calls behind view::_mut, view.cpp:1262).
+ * There is no CPU fallback: without a usable GPU, j3dg_ctx_create fails.
+ */
+#ifndef J3DG_H
+#define J3DG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define J3DG_ABI_VERSION 1
+
+typedef enum j3dg_status {
+  J3DG_OK = 0,
+  J3DG_ERR_INVALID_ARGUMENT = 1,
+  J3DG_ERR_CUDA = 2,
+  J3DG_ERR_OUT_OF_MEMORY = 3,
+  J3DG_ERR_NO_DEVICE = 4,
+  J3DG_ERR_DEVICE_STATUS = 5, /* a kernel raised its status word (see j3dg_ctx_device_status) */
+  J3DG_ERR_UNSUPPORTED = 6
+} j3dg_status;
+
+/* Device status word bits raised by kernels instead of trapping. */
+#define J3DG_DEV_STACK_OVERFLOW 0x1u
+#define J3DG_DEV_VISIT_CAP 0x2u
+#define J3DG_DEV_BAD_INDEX 0x4u
+
+typedef struct j3dg_ctx j3dg_ctx;
+typedef struct j3dg_mesh j3dg_mesh;
+typedef struct j3dg_canvas j3dg_canvas;
+typedef struct j3dg_matcap j3dg_matcap;
+
+/* pixel.h:11-27 -- byte-identical 32-byte G-buffer record.
+   mark bit 0: in shadow; bit 1: r,g,b hold texture / vertex colour. */
+typedef struct j3dg_pixel {
+  uint8_t mark, r, g, b;
+  float u;
+  float v;
+  float depth;
+  uint32_t object_id;
+  float barycentric_u;
+  float barycentric_v;
+  uint32_t db_id;
+} j3dg_pixel;
+
+/* jtk::ray {float4 orig, dir; float t_near, t_far} (canvas.cpp:778-782) */
+typedef struct j3dg_ray {
+  float orig[4];
+  float dir[4];
+  float t_near;
+  float t_far;
+} j3dg_ray;
+
+/* jtk::hit {found, distance, u, v} plus the two out-parameters of
+   find_closest_triangle (object_id = triangle, two_level_index = object). */
+typedef struct j3dg_hit {
+  uint32_t found;
+  float distance;
+  float u;
+  float v;
+  uint32_t object_id;
+  uint32_t two_level_index;
+} j3dg_hit;
+
+/* One scene_object as canvas.cpp:729-742 gathers it: the mesh (with its BVH),
+   the object's coordinate system and its db id. */
+typedef struct j3dg_instance {
+  const j3dg_mesh* mesh;
+  float cs[16];
+  uint32_t db_id;
+  uint32_t reserved;
+} j3dg_instance;
+
+/* scene.h:40-51, the fields update_canvas reads (canvas.cpp:700-742). */
+typedef struct j3dg_scene {
+  const j3dg_instance* objects;
+  uint32_t n_objects;
+  uint32_t reserved;
+  float coordinate_system[16];
+  float coordinate_system_inv[16];
+  float pivot[3];
+  float diagonal;
+} j3dg_scene;
+
+/* camera.h:5-16 (fit_film: 0 = Fill, 1 = Overscan) */
+typedef struct j3dg_camera {
+  float focal_length;
+  float film_aperture_width_inch;
+  float film_aperture_height_inch;
+  float near_clipping_plane;
+  float far_clipping_plane;
+  float zoom;
+  int32_t fit_film;
+} j3dg_camera;
+
+/* canvas.h:16-25 */
+typedef struct j3dg_canvas_settings {
+  uint8_t one_bit;
+  uint8_t shadow;
+  uint8_t edges;
+  uint8_t wireframe;
+  uint8_t shading;
+  uint8_t textured;
+  uint8_t vertexcolors;
+  uint8_t reserved;
+} j3dg_canvas_settings;
+
+/* BVH build options (NULL = defaults). */
+typedef struct j3dg_build_opts {
+  uint32_t leaf_size;  /* max triangles per leaf, 1..8 (default 4) */
+  uint32_t flags;      /* reserved, 0 */
+} j3dg_build_opts;
+
+typedef struct j3dg_mesh_info {
+  uint32_t n_vertices;
+  uint32_t n_triangles;
+  float min_bb[3];
+  float max_bb[3];
+  uint32_t n_nodes;
+  uint32_t max_depth;
+  uint64_t device_bytes;
+  float build_ms; /* device time of the last build, CUDA events */
+} j3dg_mesh_info;
+
+/* ---------------------------------------------------------------- context */
+
+/* No reference counterpart (j3d owns no device). One stream per context. */
+int j3dg_ctx_create(int device, j3dg_ctx** out);
+int j3dg_ctx_destroy(j3dg_ctx* ctx);
+/* Waits for the stream; returns J3DG_ERR_DEVICE_STATUS if a kernel raised
+   the status word since the last check (the word is then cleared). */
+int j3dg_ctx_synchronize(j3dg_ctx* ctx);
+int j3dg_ctx_device_status(j3dg_ctx* ctx, uint32_t* status);
+/* The context's cudaStream_t, for callers that order their own work. */
+void* j3dg_ctx_stream(j3dg_ctx* ctx);
+const char* j3dg_last_error(const j3dg_ctx* ctx);
+/* Instrumentation (no reference counterpart): when enabled, frame kernels
+   add their BVH node visits and triangle tests to two device counters. */
+int j3dg_ctx_set_counting(j3dg_ctx* ctx, int enable);
+int j3dg_ctx_read_counters(j3dg_ctx* ctx, uint64_t out[2], int reset);
+const char* j3dg_status_string(int status);
+int j3dg_abi_version(void);
+
+/* ----------------------------------------------------------------- meshes */
+
+/* Replaces scene.cpp:20-23 in add_object: compute_triangle_normals,
+   compute_bb (mesh.cpp:39-58) and `new jtk::qbvh(triangles, vertices)`.
+   vertices: n_vertices x 3 float; triangles: n_triangles x 3 uint32 (host or
+   device). The arrays are copied; the caller keeps them. */
+int j3dg_mesh_build(j3dg_ctx* ctx, const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
+                    uint32_t n_triangles, const j3dg_build_opts* opts, j3dg_mesh** out);
+int j3dg_mesh_destroy(j3dg_mesh* mesh);
+int j3dg_mesh_get_info(const j3dg_mesh* mesh, j3dg_mesh_info* info);
+/* scene_object::triangle_normals (scene.h:14): n_triangles x 3 floats out. */
+int j3dg_mesh_get_triangle_normals(const j3dg_mesh* mesh, float* normals);
+/* Optional per-mesh data for the textured / vertex-colour branches of
+   canvas.cpp:803-834 (mesh.h:28-30). colors: n_vertices x 3 float in [0,1];
+   uv: n_triangles x 3 x 2 float; texture: w x h RGBA8. */
+int j3dg_mesh_set_vertex_colors(j3dg_mesh* mesh, const float* colors);
+int j3dg_mesh_set_uv(j3dg_mesh* mesh, const float* uv);
+int j3dg_mesh_set_texture(j3dg_mesh* mesh, const uint32_t* texture, uint32_t w, uint32_t h);
+
+/* ------------------------------------------------------------ ray queries */
+
+/* qbvh_two_level_with_transformations(bvhs, object_cs, n) +
+   find_closest_triangle (canvas.cpp:762,786) over a batch of rays. */
+int j3dg_find_closest(j3dg_ctx* ctx, const j3dg_instance* objects, uint32_t n_objects, const j3dg_ray* rays,
+                      uint32_t n_rays, j3dg_hit* hits);
+/* Occlusion form of the same query (canvas.cpp:854-856 only reads found). */
+int j3dg_find_any(j3dg_ctx* ctx, const j3dg_instance* objects, uint32_t n_objects, const j3dg_ray* rays,
+                  uint32_t n_rays, j3dg_hit* hits);
+
+/* ---------------------------------------------------------------- matcaps */
+
+/* matcap.h:18-24: a w x h RGBA8 texture plus its cavity colour, uploaded once. */
+int j3dg_matcap_create(j3dg_ctx* ctx, const uint32_t* pixels, uint32_t w, uint32_t h, uint32_t cavity_clr,
+                       j3dg_matcap** out);
+int j3dg_matcap_destroy(j3dg_matcap* m);
+
+/* ----------------------------------------------------------------- canvas */
+
+/* canvas::canvas(w, h) + resize (canvas.cpp:102-134): device G-buffer, image
+   and background; default camera (camera.cpp:5-16) and its projection. */
+int j3dg_canvas_create(j3dg_ctx* ctx, uint32_t w, uint32_t h, j3dg_canvas** out);
+int j3dg_canvas_destroy(j3dg_canvas* c);
+int j3dg_canvas_resize(j3dg_canvas* c, uint32_t w, uint32_t h);
+/* j3d keeps canvas::_camera at make_default_camera(); this lets a caller set
+   another film-gate camera (e.g. a 60 degree vertical field of view). */
+int j3dg_canvas_set_camera(j3dg_canvas* c, const j3dg_camera* cam);
+int j3dg_canvas_get_projection(const j3dg_canvas* c, float projection[16], float projection_inv[16]);
+/* canvas::set_background_color (canvas.cpp:136-139 -> fill_background 55-78) */
+int j3dg_canvas_set_background_color(j3dg_canvas* c, uint32_t clr_top, uint32_t clr_bottom);
+/* canvas::update_settings (canvas.h:56-59) */
+int j3dg_canvas_update_settings(j3dg_canvas* c, const j3dg_canvas_settings* s);
+/* canvas::update_canvas(x0, y0, x1, y1, scene) (canvas.cpp:672-874):
+   G-buffer only, for the clamped rectangle. */
+int j3dg_canvas_update_canvas(j3dg_canvas* c, int x0, int y0, int x1, int y1, const j3dg_scene* s);
+/* canvas::render_scene(const scene*) (canvas.cpp:893-898): image <- background,
+   then update_canvas over the whole canvas (s == NULL clears the G-buffer ids). */
+int j3dg_canvas_render_scene(j3dg_canvas* c, const j3dg_scene* s);
+/* canvas::canvas_to_image(matcap) (canvas.cpp:396-399, 582-670): shades the
+   canvas's G-buffer into its image; background pixels are left as they are. */
+int j3dg_canvas_to_image(j3dg_canvas* c, const j3dg_matcap* m);
+/* canvas_to_image(const image<pixel>&, matcap) (canvas.cpp:582): shades a
+   caller G-buffer (w x h records, host or device) into the canvas image. */
+int j3dg_canvas_to_image_from(j3dg_canvas* c, const j3dg_pixel* pixels, const j3dg_matcap* m);
+/* view::render_scene (view.cpp:421-430) fused: background, update_canvas,
+   canvas_to_image in one pass (one kernel for plain shading, two for the
+   neighbour-reading modes). Asynchronous on the context stream. */
+int j3dg_canvas_render_frame(j3dg_canvas* c, const j3dg_scene* s, const j3dg_matcap* m);
+/* canvas::get_pixels / get_image (canvas.h:81-87): copy out (host or device
+   destination, w x h elements). Synchronous; reports device status. */
+int j3dg_canvas_get_pixels(j3dg_canvas* c, j3dg_pixel* dst);
+int j3dg_canvas_get_image(j3dg_canvas* c, uint32_t* dst);
+/* Upload a caller G-buffer into the canvas (w x h records). */
+int j3dg_canvas_set_pixels(j3dg_canvas* c, const j3dg_pixel* src);
+/* Device pointers of the canvas buffers (valid until resize/destroy). */
+int j3dg_canvas_device_buffers(j3dg_canvas* c, j3dg_pixel** pixels, uint32_t** image, uint32_t** background);
+
+/* ---------------------------------------------------- host-side j3d math --
+   Plain C++ (no GPU), the same fp32 operation order as the device code. */
+
+/* camera.cpp:5-16 */
+void j3dg_make_default_camera(j3dg_camera* c);
+/* camera.cpp:32-73 */
+void j3dg_make_projection_matrix(const j3dg_camera* c, int w, int h, float out[16]);
+/* camera.cpp:26-30 */
+void j3dg_invert_projection_matrix(const float in[16], float out[16]);
+/* jtk invert_orthonormal (canvas.cpp:734, scene.cpp:109) */
+void j3dg_invert_orthonormal(const float in[16], float out[16]);
+/* scene.cpp:50-89 prepare_scene over the mesh objects */
+int j3dg_prepare_scene(const j3dg_instance* objects, uint32_t n, float min_bb[3], float max_bb[3],
+                       float* diagonal);
+/* scene.cpp:91-110 unzoom */
+void j3dg_unzoom(const float min_bb[3], const float max_bb[3], float diagonal, float cs[16], float cs_inv[16],
+                 float pivot[3]);
+/* matcap.cpp:9-268: type 0 red wax, 1 gray, 2 brown, 3 sketch; pixels must
+   hold 512 x 512. */
+int j3dg_make_matcap(int type, uint32_t* pixels, uint32_t* w, uint32_t* h, uint32_t* cavity_clr);
+/* canvas.cpp:55-78 */
+void j3dg_fill_background(uint32_t* bg, uint32_t w, uint32_t h, uint32_t clr_top, uint32_t clr_bottom);
+
+/* ------------------------------------------------- synthetic workloads ----
+   No reference counterpart: seeded stand-ins for the meshes j3d loads from
+   files (the mesh readers are not on this path). Deterministic on every
+   host: own PRNG and own sine, no libm transcendental calls. */
+
+/* Icosphere subdivided `level` times; radius 1 + amp * sum_k a_k sin(f_k (d.u_k) + phi_k)
+   with 8 seeded terms. V = 10*4^level + 2, T = 20*4^level. */
+int j3dg_synth_icosphere(uint32_t level, uint64_t seed, float amp, float* vertices, uint32_t* triangles);
+/* Torus R, r on an nu x nv periodic grid (V = nu*nv, T = 2*nu*nv); radial
+   displacement amp * sum of 16 seeded periodic sinusoids. */
+int j3dg_synth_torus(uint32_t nu, uint32_t nv, float R, float r, uint64_t seed, float amp, float* vertices,
+                     uint32_t* triangles);
+/* Camera-to-world look-at poses: n directions uniform on the sphere, radius
+   uniform in [r0, r1], looking at target. cs: n x 16 floats. */
+int j3dg_synth_cameras(uint32_t n, uint64_t seed, float r0, float r1, const float target[3], float* cs);
+/* Camera focal length (mm) giving a vertical field of view (degrees) for the
+   default film gate (camera.cpp:9-10). */
+float j3dg_focal_for_vfov(float vfov_deg, float film_aperture_height_inch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* J3DG_H */

@@ -1,0 +1,11 @@
+"""j3d_gb300: GB300 (sm_103a) implementation of j3d's ray-cast rendering hot path.
+
+BVH build over a triangle mesh (jtk qbvh), per-pixel closest hit, shadow ray
+and matcap shading into j3d's 32-byte pixel G-buffer and RGBA8 canvas, behind
+the C-ABI of include/j3dg.h (libj3dgpu.so). This package is the host-side
+mirror of the reference's scene/canvas interface over that C-ABI.
+"""
+from ._ffi import HIT_DTYPE, PIXEL_DTYPE, RAY_DTYPE, J3dgError, LIB_PATH, lib  # noqa: F401
+from .scene import (Canvas, Context, Matcap, Mesh, Scene, SceneObject, camera_for_vfov, fill_background,  # noqa: F401
+                    find_closest, invert_orthonormal, invert_projection_matrix, make_default_camera, make_matcap,
+                    make_projection_matrix, settings)

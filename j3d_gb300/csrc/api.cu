@@ -1,0 +1,777 @@
+// api.cu -- the extern "C" boundary of libj3dgpu.so (declared in include/j3dg.h).
+//
+// Objects own device memory; every call runs on the context's one stream.
+// Bulk arrays may be host or device pointers (cudaPointerGetAttributes).
+// No C++ exception crosses the boundary and there is no CPU fallback.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/j3dg.h"
+#include "device_common.cuh"
+#include "internal.h"
+#include "render.cuh"
+
+namespace j3dg {
+int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
+              std::string& err);
+}
+
+using j3dg::DevInst;
+using j3dg::FrameParams;
+
+namespace {
+
+// ring of instance-table slots: host staging (pinned) -> device
+const uint32_t kInstSlots = 8;
+
+struct CtxExtra {
+  std::vector<DevInst> last;  // the table in the most recent slot
+  int last_slot = -1;
+  uint32_t next_slot = 0;
+  cudaEvent_t slot_ev[kInstSlots];
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  unsigned long long* d_counters = nullptr;
+  bool counting = false;
+};
+
+int fail(j3dg_ctx* c, int code, const std::string& msg) {
+  if (c) c->last_error = msg;
+  return code;
+}
+
+int cuda_fail(j3dg_ctx* c, cudaError_t e, const char* where) {
+  if (e == cudaErrorMemoryAllocation) return fail(c, J3DG_ERR_OUT_OF_MEMORY, std::string(where) + ": out of device memory");
+  return fail(c, J3DG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(c, x, where)                          \
+  do {                                           \
+    cudaError_t e_ = (x);                        \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, where); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+cudaStream_t S(j3dg_ctx* c) { return (cudaStream_t)c->stream; }
+
+// Context layout: the opaque j3dg_ctx plus CtxExtra allocated together.
+struct CtxAll {
+  j3dg_ctx ctx;
+  CtxExtra ex;
+  DevInst* h_slots = nullptr;  // pinned, kInstSlots * inst_cap
+};
+
+CtxAll* all(j3dg_ctx* c) { return reinterpret_cast<CtxAll*>(c); }
+
+DevInst to_dev(const j3dg_instance& in) {
+  DevInst d;
+  memset(&d, 0, sizeof(d));
+  const j3dg_mesh* m = in.mesh;
+  d.nodes = (const float4*)m->d_nodes;
+  d.tris = (const float4*)m->d_tris;
+  d.normals = (const float4*)m->d_normals;
+  d.index = (const uint32_t*)m->d_index;
+  d.colors = (const float*)m->d_colors;
+  d.uv = (const float*)m->d_uv;
+  d.tex = (const uint32_t*)m->d_tex;
+  d.tex_w = m->tex_w;
+  d.tex_h = m->tex_h;
+  d.root_ref = m->root_ref;
+  d.n_nodes = m->n_nodes;
+  d.nt = m->nt;
+  d.db_id = in.db_id;
+  d.scale = m->scale;
+  memcpy(d.cs, in.cs, sizeof(d.cs));
+  j3dg_invert_orthonormal(in.cs, d.inv);  // canvas.cpp:734
+  return d;
+}
+
+// Uploads the instance table (skipped when unchanged); returns its device address.
+int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const DevInst** out) {
+  CtxAll* A = all(c);
+  CtxExtra& X = A->ex;
+  std::vector<DevInst> t(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!objs[i].mesh) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "instance without a mesh");
+    if (objs[i].mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh belongs to another context");
+    t[i] = to_dev(objs[i]);
+  }
+  if (n == 0) {
+    *out = nullptr;
+    return J3DG_OK;
+  }
+  if (n > c->inst_cap) {
+    // grow both rings (waits for in-flight copies)
+    CK(c, cudaStreamSynchronize(S(c)), "instance table");
+    uint32_t cap = std::max(n, 2 * c->inst_cap);
+    void* d = nullptr;
+    DevInst* h = nullptr;
+    CK(c, cudaMalloc(&d, sizeof(DevInst) * cap * kInstSlots), "instance table");
+    if (cudaMallocHost((void**)&h, sizeof(DevInst) * cap * kInstSlots) != cudaSuccess) {
+      cudaFree(d);
+      return fail(c, J3DG_ERR_OUT_OF_MEMORY, "instance table: pinned host allocation failed");
+    }
+    cudaFree(c->d_inst);
+    cudaFreeHost(A->h_slots);
+    c->d_inst = d;
+    A->h_slots = h;
+    c->inst_cap = cap;
+    X.last.clear();
+    X.last_slot = -1;
+  }
+  if (X.last_slot >= 0 && X.last.size() == n && memcmp(X.last.data(), t.data(), sizeof(DevInst) * n) == 0) {
+    *out = (const DevInst*)c->d_inst + (size_t)X.last_slot * c->inst_cap;
+    return J3DG_OK;
+  }
+  uint32_t slot = X.next_slot;
+  X.next_slot = (X.next_slot + 1) % kInstSlots;
+  CK(c, cudaEventSynchronize(X.slot_ev[slot]), "instance table");
+  DevInst* h = A->h_slots + (size_t)slot * c->inst_cap;
+  memcpy(h, t.data(), sizeof(DevInst) * n);
+  DevInst* d = (DevInst*)c->d_inst + (size_t)slot * c->inst_cap;
+  CK(c, cudaMemcpyAsync(d, h, sizeof(DevInst) * n, cudaMemcpyHostToDevice, S(c)), "instance table");
+  CK(c, cudaEventRecord(X.slot_ev[slot], S(c)), "instance table");
+  X.last = t;
+  X.last_slot = (int)slot;
+  *out = d;
+  return J3DG_OK;
+}
+
+int check_status(j3dg_ctx* c) {
+  uint32_t st = 0;
+  CK(c, cudaMemcpyAsync(&st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost, S(c)), "status");
+  CK(c, cudaStreamSynchronize(S(c)), "status");
+  if (st) {
+    CK(c, cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), S(c)), "status");
+    CK(c, cudaStreamSynchronize(S(c)), "status");
+    return fail(c, J3DG_ERR_DEVICE_STATUS, "device status word 0x" + std::to_string(st) +
+                                               " (1 stack overflow, 2 visit cap, 4 bad index)");
+  }
+  return J3DG_OK;
+}
+
+// Copies n bytes to dst (host or device) from device src, then synchronizes.
+int copy_out(j3dg_ctx* c, void* dst, const void* src, size_t n) {
+  cudaMemcpyKind k = is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  CK(c, cudaMemcpyAsync(dst, src, n, k, S(c)), "copy out");
+  return check_status(c);
+}
+
+void free_mesh_buffers(j3dg_mesh* m) {
+  cudaFree(m->d_nodes);
+  cudaFree(m->d_tris);
+  cudaFree(m->d_normals);
+  cudaFree(m->d_index);
+  cudaFree(m->d_colors);
+  cudaFree(m->d_uv);
+  cudaFree(m->d_tex);
+  m->d_nodes = m->d_tris = m->d_normals = m->d_index = m->d_colors = m->d_uv = m->d_tex = nullptr;
+}
+
+int shade_mode_of(const j3dg_canvas_settings& s) {
+  // canvas.cpp:584-669: one-bit, then wireframe, then edges, else plain
+  if (s.one_bit) return 3;
+  if (s.wireframe) return 2;
+  if (s.edges) return 1;
+  return 0;
+}
+
+void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevInst* inst, const j3dg_matcap* m) {
+  memset(&P, 0, sizeof(P));
+  P.inst = inst;
+  P.n_inst = s ? s->n_objects : 0;
+  P.w = cv->w;
+  P.h = cv->h;
+  P.x0 = 0;
+  P.y0 = 0;
+  P.x1 = (int)cv->w - 1;
+  P.y1 = (int)cv->h - 1;
+  if (s) {
+    memcpy(P.cs, s->coordinate_system, sizeof(P.cs));
+    memcpy(P.cs_inv, s->coordinate_system_inv, sizeof(P.cs_inv));
+    memcpy(P.pivot, s->pivot, sizeof(P.pivot));
+    P.diagonal = s->diagonal;
+  }
+  memcpy(P.pinv, cv->projection_inv, sizeof(P.pinv));
+  P.near_plane = cv->camera.near_clipping_plane;
+  P.gbuf = (j3dg_pixel*)cv->d_pixels;
+  P.im = cv->d_image;
+  P.background = cv->d_background;
+  if (m) {
+    P.matcap = m->d_pixels;
+    P.mw = m->w;
+    P.mh = m->h;
+    P.cavity = m->cavity;
+  }
+  P.shadow = cv->settings.shadow;
+  P.textured = cv->settings.textured;
+  P.vertexcolors = cv->settings.vertexcolors;
+  P.shading = cv->settings.shading;
+  P.status = cv->ctx->d_status;
+  CtxExtra& X = all(cv->ctx)->ex;
+  P.counters = X.counting ? X.d_counters : nullptr;
+}
+
+int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
+  j3dg_ctx* c = cv->ctx;
+  cudaFree(cv->d_pixels);
+  cudaFree(cv->d_image);
+  cudaFree(cv->d_background);
+  cv->d_pixels = nullptr;
+  cv->d_image = cv->d_background = nullptr;
+  cv->w = w;
+  cv->h = h;
+  size_t n = (size_t)w * h;
+  if (n) {
+    CK(c, cudaMalloc(&cv->d_pixels, sizeof(j3dg_pixel) * n), "canvas");
+    CK(c, cudaMalloc((void**)&cv->d_image, sizeof(uint32_t) * n), "canvas");
+    CK(c, cudaMalloc((void**)&cv->d_background, sizeof(uint32_t) * n), "canvas");
+    CK(c, cudaMemsetAsync(cv->d_image, 0, sizeof(uint32_t) * n, S(c)), "canvas");
+    CK(c, cudaMemsetAsync(cv->d_background, 0, sizeof(uint32_t) * n, S(c)), "canvas");
+    CK(c, j3dg::launch_init_pixels((j3dg_pixel*)cv->d_pixels, n, S(c)), "canvas");
+  }
+  // canvas.cpp:131-133: default camera and its projection
+  j3dg_make_projection_matrix(&cv->camera, (int)w, (int)h, cv->projection);
+  j3dg_invert_projection_matrix(cv->projection, cv->projection_inv);
+  CK(c, cudaStreamSynchronize(S(c)), "canvas");
+  return J3DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int j3dg_abi_version(void) { return J3DG_ABI_VERSION; }
+
+const char* j3dg_status_string(int s) {
+  switch (s) {
+    case J3DG_OK: return "ok";
+    case J3DG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case J3DG_ERR_CUDA: return "CUDA error";
+    case J3DG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case J3DG_ERR_NO_DEVICE: return "no CUDA device";
+    case J3DG_ERR_DEVICE_STATUS: return "device status raised";
+    case J3DG_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* j3dg_last_error(const j3dg_ctx* c) { return c ? c->last_error.c_str() : "no context"; }
+
+int j3dg_ctx_create(int device, j3dg_ctx** out) {
+  if (!out) return J3DG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return J3DG_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return J3DG_ERR_INVALID_ARGUMENT;
+  CtxAll* A = new (std::nothrow) CtxAll();
+  if (!A) return J3DG_ERR_OUT_OF_MEMORY;
+  j3dg_ctx* c = &A->ctx;
+  c->device = device;
+  c->h_inst = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete A;
+    return J3DG_ERR_CUDA;
+  }
+  cudaStream_t st;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete A;
+    return J3DG_ERR_CUDA;
+  }
+  c->stream = st;
+  bool ok = cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
+            cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
+            cudaMalloc((void**)&A->ex.d_counters, 2 * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMemset(A->ex.d_counters, 0, 2 * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaEventCreate(&A->ex.ev0) == cudaSuccess && cudaEventCreate(&A->ex.ev1) == cudaSuccess;
+  for (uint32_t i = 0; ok && i < kInstSlots; ++i) ok = cudaEventCreateWithFlags(&A->ex.slot_ev[i], cudaEventDisableTiming) == cudaSuccess;
+  if (ok) {
+    c->inst_cap = 16;
+    ok = cudaMalloc(&c->d_inst, sizeof(DevInst) * c->inst_cap * kInstSlots) == cudaSuccess &&
+         cudaMallocHost((void**)&A->h_slots, sizeof(DevInst) * c->inst_cap * kInstSlots) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    j3dg_ctx_destroy(c);
+    return J3DG_ERR_CUDA;
+  }
+  *out = c;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_destroy(j3dg_ctx* c) {
+  if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  CtxAll* A = all(c);
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(S(c));
+  cudaFree(c->d_status);
+  cudaFree(c->d_inst);
+  cudaFree(A->ex.d_counters);
+  if (A->h_slots) cudaFreeHost(A->h_slots);
+  for (uint32_t i = 0; i < kInstSlots; ++i)
+    if (A->ex.slot_ev[i]) cudaEventDestroy(A->ex.slot_ev[i]);
+  if (A->ex.ev0) cudaEventDestroy(A->ex.ev0);
+  if (A->ex.ev1) cudaEventDestroy(A->ex.ev1);
+  if (c->stream) cudaStreamDestroy(S(c));
+  delete A;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_synchronize(j3dg_ctx* c) {
+  if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  return check_status(c);
+}
+
+int j3dg_ctx_device_status(j3dg_ctx* c, uint32_t* status) {
+  if (!c || !status) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  CK(c, cudaMemcpyAsync(status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, S(c)), "status");
+  CK(c, cudaStreamSynchronize(S(c)), "status");
+  return J3DG_OK;
+}
+
+void* j3dg_ctx_stream(j3dg_ctx* c) { return c ? c->stream : nullptr; }
+
+// Instrumentation: per-frame node-visit and triangle-test counters.
+int j3dg_ctx_set_counting(j3dg_ctx* c, int enable) {
+  if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  all(c)->ex.counting = enable != 0;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_read_counters(j3dg_ctx* c, uint64_t out[2], int reset) {
+  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  unsigned long long h[2];
+  CK(c, cudaMemcpyAsync(h, all(c)->ex.d_counters, sizeof(h), cudaMemcpyDeviceToHost, S(c)), "counters");
+  if (reset) CK(c, cudaMemsetAsync(all(c)->ex.d_counters, 0, sizeof(h), S(c)), "counters");
+  CK(c, cudaStreamSynchronize(S(c)), "counters");
+  out[0] = h[0];
+  out[1] = h[1];
+  return J3DG_OK;
+}
+
+// ------------------------------------------------------------------ mesh
+
+int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, uint32_t nt,
+                    const j3dg_build_opts* opts, j3dg_mesh** out) {
+  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!V || !T || nv == 0 || nt == 0) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: empty mesh");
+  if (nt >= J3DG_MAX_TRIANGLES) return fail(c, J3DG_ERR_UNSUPPORTED, "mesh_build: more than 2^28 triangles");
+  uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 4u;
+  if (leaf < 1 || leaf > J3DG_MAX_LEAF) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: leaf_size must be 1..8");
+  cudaSetDevice(c->device);
+  j3dg_mesh* m = new (std::nothrow) j3dg_mesh();
+  if (!m) return J3DG_ERR_OUT_OF_MEMORY;
+  m->ctx = c;
+  m->nv = nv;
+  m->nt = nt;
+  m->leaf_size = leaf;
+  CtxExtra& X = all(c)->ex;
+  float* dV = nullptr;
+  bool ownV = false;
+  int rc = J3DG_OK;
+  std::string err;
+  cudaError_t e = cudaMalloc(&m->d_index, sizeof(uint32_t) * 3 * (size_t)nt);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(m->d_index, T, sizeof(uint32_t) * 3 * (size_t)nt,
+                        is_device_ptr(T) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c));
+  if (e == cudaSuccess) {
+    if (is_device_ptr(V)) {
+      dV = const_cast<float*>(V);
+    } else {
+      ownV = true;
+      e = cudaMalloc((void**)&dV, sizeof(float) * 3 * (size_t)nv);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dV, V, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice, S(c));
+    }
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(X.ev0, S(c));
+  if (e != cudaSuccess) {
+    rc = cuda_fail(c, e, "mesh_build upload");
+  } else {
+    rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, S(c), c->d_status, err);
+    if (rc == J3DG_OK) {
+      cudaEventRecord(X.ev1, S(c));
+      cudaEventSynchronize(X.ev1);
+      cudaEventElapsedTime(&m->build_ms, X.ev0, X.ev1);
+      rc = check_status(c);
+    } else {
+      fail(c, rc, "mesh_build: " + err);
+    }
+  }
+  if (ownV) cudaFree(dV);
+  if (rc != J3DG_OK) {
+    free_mesh_buffers(m);
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_destroy(j3dg_mesh* m) {
+  if (!m) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(S(m->ctx));
+  all(m->ctx)->ex.last_slot = -1;  // the cached instance table may name this mesh
+  free_mesh_buffers(m);
+  delete m;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_get_info(const j3dg_mesh* m, j3dg_mesh_info* info) {
+  if (!m || !info) return J3DG_ERR_INVALID_ARGUMENT;
+  info->n_vertices = m->nv;
+  info->n_triangles = m->nt;
+  memcpy(info->min_bb, m->min_bb, sizeof(info->min_bb));
+  memcpy(info->max_bb, m->max_bb, sizeof(info->max_bb));
+  info->n_nodes = m->n_nodes;
+  info->max_depth = m->max_depth;
+  info->device_bytes = m->device_bytes;
+  info->build_ms = m->build_ms;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_get_triangle_normals(const j3dg_mesh* m, float* normals) {
+  if (!m || !normals) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = m->ctx;
+  cudaSetDevice(c->device);
+  std::vector<float> tmp(4 * (size_t)m->nt);
+  CK(c, cudaMemcpyAsync(tmp.data(), m->d_normals, sizeof(float) * 4 * (size_t)m->nt, cudaMemcpyDeviceToHost, S(c)),
+     "normals");
+  CK(c, cudaStreamSynchronize(S(c)), "normals");
+  for (size_t i = 0; i < m->nt; ++i)
+    for (int k = 0; k < 3; ++k) normals[3 * i + k] = tmp[4 * i + k];
+  return J3DG_OK;
+}
+
+static int upload_owned(j3dg_ctx* c, void** dst, const void* src, size_t bytes, const char* what) {
+  cudaFree(*dst);
+  *dst = nullptr;
+  if (!src) return J3DG_OK;
+  CK(c, cudaMalloc(dst, bytes), what);
+  CK(c, cudaMemcpyAsync(*dst, src, bytes, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c)),
+     what);
+  CK(c, cudaStreamSynchronize(S(c)), what);
+  all(c)->ex.last_slot = -1;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_set_vertex_colors(j3dg_mesh* m, const float* colors) {
+  if (!m) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(S(m->ctx));
+  return upload_owned(m->ctx, &m->d_colors, colors, sizeof(float) * 3 * (size_t)m->nv, "vertex colors");
+}
+
+int j3dg_mesh_set_uv(j3dg_mesh* m, const float* uv) {
+  if (!m) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(S(m->ctx));
+  return upload_owned(m->ctx, &m->d_uv, uv, sizeof(float) * 6 * (size_t)m->nt, "uv");
+}
+
+int j3dg_mesh_set_texture(j3dg_mesh* m, const uint32_t* tex, uint32_t w, uint32_t h) {
+  if (!m || (tex && (w == 0 || h == 0))) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(S(m->ctx));
+  m->tex_w = tex ? w : 0;
+  m->tex_h = tex ? h : 0;
+  return upload_owned(m->ctx, &m->d_tex, tex, sizeof(uint32_t) * (size_t)w * h, "texture");
+}
+
+// ------------------------------------------------------------ ray batches
+
+static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, const j3dg_ray* rays, uint32_t n,
+                     j3dg_hit* hits, bool any) {
+  if (!c || (n && (!rays || !hits)) || (n_obj && !objs)) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  const DevInst* dinst = nullptr;
+  int rc = upload_instances(c, objs, n_obj, &dinst);
+  if (rc) return rc;
+  if (n == 0) return J3DG_OK;
+  const bool rays_dev = is_device_ptr(rays), hits_dev = is_device_ptr(hits);
+  j3dg_ray* dr = const_cast<j3dg_ray*>(rays);
+  j3dg_hit* dh = hits;
+  if (!rays_dev) {
+    CK(c, cudaMallocAsync((void**)&dr, sizeof(j3dg_ray) * (size_t)n, S(c)), "rays");
+    CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "rays");
+  }
+  if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n, S(c)), "hits");
+  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, c->d_status, S(c)), "find");
+  if (!hits_dev) {
+    CK(c, cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * (size_t)n, cudaMemcpyDeviceToHost, S(c)), "hits");
+    cudaFreeAsync(dh, S(c));
+  }
+  if (!rays_dev) cudaFreeAsync(dr, S(c));
+  return check_status(c);
+}
+
+int j3dg_find_closest(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, const j3dg_ray* rays, uint32_t n,
+                      j3dg_hit* hits) {
+  return ray_query(c, objs, n_obj, rays, n, hits, false);
+}
+
+int j3dg_find_any(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, const j3dg_ray* rays, uint32_t n,
+                  j3dg_hit* hits) {
+  return ray_query(c, objs, n_obj, rays, n, hits, true);
+}
+
+// --------------------------------------------------------------- matcap
+
+int j3dg_matcap_create(j3dg_ctx* c, const uint32_t* px, uint32_t w, uint32_t h, uint32_t cavity, j3dg_matcap** out) {
+  if (!c || !px || !out || w == 0 || h == 0) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  j3dg_matcap* m = new (std::nothrow) j3dg_matcap();
+  if (!m) return J3DG_ERR_OUT_OF_MEMORY;
+  m->ctx = c;
+  m->w = w;
+  m->h = h;
+  m->cavity = cavity;
+  void* d = nullptr;
+  int rc = upload_owned(c, &d, px, sizeof(uint32_t) * (size_t)w * h, "matcap");
+  if (rc) {
+    delete m;
+    return rc;
+  }
+  m->d_pixels = (uint32_t*)d;
+  *out = m;
+  return J3DG_OK;
+}
+
+int j3dg_matcap_destroy(j3dg_matcap* m) {
+  if (!m) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(S(m->ctx));
+  cudaFree(m->d_pixels);
+  delete m;
+  return J3DG_OK;
+}
+
+// --------------------------------------------------------------- canvas
+
+int j3dg_canvas_create(j3dg_ctx* c, uint32_t w, uint32_t h, j3dg_canvas** out) {
+  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  j3dg_canvas* cv = new (std::nothrow) j3dg_canvas();
+  if (!cv) return J3DG_ERR_OUT_OF_MEMORY;
+  cv->ctx = c;
+  j3dg_make_default_camera(&cv->camera);
+  memset(&cv->settings, 0, sizeof(cv->settings));
+  int rc = canvas_alloc(cv, w, h);
+  if (rc) {
+    j3dg_canvas_destroy(cv);
+    return rc;
+  }
+  *out = cv;
+  return J3DG_OK;
+}
+
+int j3dg_canvas_destroy(j3dg_canvas* cv) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(cv->ctx->device);
+  cudaStreamSynchronize(S(cv->ctx));
+  cudaFree(cv->d_pixels);
+  cudaFree(cv->d_image);
+  cudaFree(cv->d_background);
+  delete cv;
+  return J3DG_OK;
+}
+
+int j3dg_canvas_resize(j3dg_canvas* cv, uint32_t w, uint32_t h) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(cv->ctx->device);
+  cudaStreamSynchronize(S(cv->ctx));
+  j3dg_make_default_camera(&cv->camera);  // canvas.cpp:131
+  return canvas_alloc(cv, w, h);
+}
+
+int j3dg_canvas_set_camera(j3dg_canvas* cv, const j3dg_camera* cam) {
+  if (!cv || !cam) return J3DG_ERR_INVALID_ARGUMENT;
+  cv->camera = *cam;
+  j3dg_make_projection_matrix(&cv->camera, (int)cv->w, (int)cv->h, cv->projection);
+  j3dg_invert_projection_matrix(cv->projection, cv->projection_inv);
+  return J3DG_OK;
+}
+
+int j3dg_canvas_get_projection(const j3dg_canvas* cv, float* P, float* Pinv) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  if (P) memcpy(P, cv->projection, sizeof(cv->projection));
+  if (Pinv) memcpy(Pinv, cv->projection_inv, sizeof(cv->projection_inv));
+  return J3DG_OK;
+}
+
+int j3dg_canvas_set_background_color(j3dg_canvas* cv, uint32_t top, uint32_t bottom) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  cudaSetDevice(c->device);
+  std::vector<uint32_t> bg((size_t)cv->w * cv->h);
+  j3dg_fill_background(bg.data(), cv->w, cv->h, top, bottom);
+  if (bg.empty()) return J3DG_OK;
+  CK(c, cudaMemcpyAsync(cv->d_background, bg.data(), sizeof(uint32_t) * bg.size(), cudaMemcpyHostToDevice, S(c)),
+     "background");
+  CK(c, cudaStreamSynchronize(S(c)), "background");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_update_settings(j3dg_canvas* cv, const j3dg_canvas_settings* s) {
+  if (!cv || !s) return J3DG_ERR_INVALID_ARGUMENT;
+  cv->settings = *s;
+  return J3DG_OK;
+}
+
+static int scene_ok(j3dg_ctx* c, const j3dg_scene* s) {
+  if (s && s->n_objects && !s->objects) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "scene with objects == NULL");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, const j3dg_scene* s) {
+  if (!cv || !s) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  if (int rc = scene_ok(c, s)) return rc;
+  if (cv->w == 0 || cv->h == 0) return J3DG_OK;
+  cudaSetDevice(c->device);
+  const DevInst* dinst = nullptr;
+  if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
+  // canvas.cpp:681-698: clamp the rectangle
+  const int w = (int)cv->w, h = (int)cv->h;
+  auto clampv = [](int v, int hi) { return v < 0 ? 0 : (v >= hi ? hi - 1 : v); };
+  x0 = clampv(x0, w);
+  y0 = clampv(y0, h);
+  x1 = clampv(x1, w);
+  y1 = clampv(y1, h);
+  FrameParams P;
+  fill_frame(P, cv, s, dinst, nullptr);
+  P.x0 = x0;
+  P.y0 = y0;
+  P.x1 = x1;
+  P.y1 = y1;
+  P.shade_mode = 0;
+  CK(c, j3dg::launch_render(P, S(c)), "update_canvas");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_render_scene(j3dg_canvas* cv, const j3dg_scene* s) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  if (int rc = scene_ok(c, s)) return rc;
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)cv->w * cv->h;
+  CK(c, j3dg::launch_copy_u32(cv->d_image, cv->d_background, n, S(c)), "render_scene");
+  if (!s) {
+    CK(c, j3dg::launch_clear_ids((j3dg_pixel*)cv->d_pixels, n, S(c)), "render_scene");
+    return J3DG_OK;
+  }
+  return j3dg_canvas_update_canvas(cv, 0, 0, (int)cv->w - 1, (int)cv->h - 1, s);
+}
+
+static int shade(j3dg_canvas* cv, const j3dg_pixel* G, const j3dg_matcap* m, int fill_background) {
+  j3dg_ctx* c = cv->ctx;
+  if (!m) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "canvas_to_image: no matcap");
+  if (cv->w == 0 || cv->h == 0) return J3DG_OK;
+  FrameParams P;
+  fill_frame(P, cv, nullptr, nullptr, m);
+  CK(c, j3dg::launch_shade(P, G, shade_mode_of(cv->settings), fill_background, S(c)), "canvas_to_image");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_to_image(j3dg_canvas* cv, const j3dg_matcap* m) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(cv->ctx->device);
+  return shade(cv, (const j3dg_pixel*)cv->d_pixels, m, 0);
+}
+
+int j3dg_canvas_to_image_from(j3dg_canvas* cv, const j3dg_pixel* px, const j3dg_matcap* m) {
+  if (!cv || !px) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  cudaSetDevice(c->device);
+  if (is_device_ptr(px)) return shade(cv, px, m, 0);
+  const size_t n = (size_t)cv->w * cv->h;
+  j3dg_pixel* d = nullptr;
+  CK(c, cudaMallocAsync((void**)&d, sizeof(j3dg_pixel) * n, S(c)), "canvas_to_image");
+  CK(c, cudaMemcpyAsync(d, px, sizeof(j3dg_pixel) * n, cudaMemcpyHostToDevice, S(c)), "canvas_to_image");
+  int rc = shade(cv, d, m, 0);
+  cudaFreeAsync(d, S(c));
+  return rc;
+}
+
+int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_matcap* m) {
+  if (!cv || !m) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  if (int rc = scene_ok(c, s)) return rc;
+  if (cv->w == 0 || cv->h == 0) return J3DG_OK;
+  cudaSetDevice(c->device);
+  const DevInst* dinst = nullptr;
+  if (s)
+    if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
+  const int mode = shade_mode_of(cv->settings);
+  if (!s) {
+    const size_t n = (size_t)cv->w * cv->h;
+    CK(c, j3dg::launch_copy_u32(cv->d_image, cv->d_background, n, S(c)), "render_frame");
+    CK(c, j3dg::launch_clear_ids((j3dg_pixel*)cv->d_pixels, n, S(c)), "render_frame");
+    return J3DG_OK;
+  }
+  FrameParams P;
+  fill_frame(P, cv, s, dinst, m);
+  if (mode == 0) {
+    P.shade_mode = 1;  // one kernel: G-buffer, shadow, plain shading, background
+    CK(c, j3dg::launch_render(P, S(c)), "render_frame");
+  } else {
+    P.shade_mode = 0;
+    CK(c, j3dg::launch_render(P, S(c)), "render_frame");
+    CK(c, j3dg::launch_shade(P, (const j3dg_pixel*)cv->d_pixels, mode, 1, S(c)), "render_frame");
+  }
+  return J3DG_OK;
+}
+
+int j3dg_canvas_get_pixels(j3dg_canvas* cv, j3dg_pixel* dst) {
+  if (!cv || !dst) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(cv->ctx->device);
+  return copy_out(cv->ctx, dst, cv->d_pixels, sizeof(j3dg_pixel) * (size_t)cv->w * cv->h);
+}
+
+int j3dg_canvas_get_image(j3dg_canvas* cv, uint32_t* dst) {
+  if (!cv || !dst) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(cv->ctx->device);
+  return copy_out(cv->ctx, dst, cv->d_image, sizeof(uint32_t) * (size_t)cv->w * cv->h);
+}
+
+int j3dg_canvas_set_pixels(j3dg_canvas* cv, const j3dg_pixel* src) {
+  if (!cv || !src) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  cudaSetDevice(c->device);
+  CK(c, cudaMemcpyAsync(cv->d_pixels, src, sizeof(j3dg_pixel) * (size_t)cv->w * cv->h,
+                        is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c)),
+     "set_pixels");
+  CK(c, cudaStreamSynchronize(S(c)), "set_pixels");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_device_buffers(j3dg_canvas* cv, j3dg_pixel** px, uint32_t** im, uint32_t** bg) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  if (px) *px = (j3dg_pixel*)cv->d_pixels;
+  if (im) *im = cv->d_image;
+  if (bg) *bg = cv->d_background;
+  return J3DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,591 @@
+// build.cu -- GPU construction of the 4-wide BVH over an indexed triangle mesh.
+//
+// Replaces, in scene.cpp:20-23 (add_object), compute_triangle_normals,
+// compute_bb (mesh.cpp:39-58) and `new jtk::qbvh(triangles, vertices)`.
+//
+// Pipeline (all on the context stream):
+//   1. vertex bbox: two-pass min/max reduction (exact)
+//   2. per triangle: normal (fixed fp32 order), AABB centroid -> 48-bit Morton
+//      code over the vertex bbox
+//   3. LSD radix sort of (Morton, triangle id), 8-bit digits, stable
+//   4. leaf-ordered triangle array: 3 float4 per triangle (v0.w = id bits)
+//   5. binary LBVH, bottom-up in one pass (Apetrei 2014, "Fast and Simple
+//      Agglomerative LBVH Construction"), with a strict total order on the
+//      split keys (xor of neighbouring codes, then i ^ (i+1), then i)
+//   6. collapse to 4-wide nodes level by level: open the largest-area child
+//      until four children; subtrees of <= leaf_size triangles become leaves.
+// Child boxes are exact unions of triangle boxes, which the traversal's
+// topology-independence argument requires.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace j3dg {
+
+static const int kMortonBitsPerAxis = 16;
+static const int kRadixPasses = (3 * kMortonBitsPerAxis + 7) / 8;
+
+// ------------------------------------------------------------- 1. bbox ----
+
+__global__ void k_bbox_partial(const float* __restrict__ V, uint32_t nv, float* __restrict__ part) {
+  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float x = V[3 * (size_t)i + k];
+      mn[k] = fminf(mn[k], x);
+      mx[k] = fmaxf(mx[k], x);
+    }
+  }
+  __shared__ float s[6][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  if (lane == 0)
+    for (int k = 0; k < 3; ++k) {
+      s[k][warp] = mn[k];
+      s[3 + k][warp] = mx[k];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float v = s[threadIdx.x][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      v = threadIdx.x < 3 ? fminf(v, s[threadIdx.x][w]) : fmaxf(v, s[threadIdx.x][w]);
+    part[6 * blockIdx.x + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_bbox_final(const float* __restrict__ part, int n, float* __restrict__ out) {
+  if (threadIdx.x < 6) {
+    float v = part[threadIdx.x];
+    for (int b = 1; b < n; ++b) v = threadIdx.x < 3 ? fminf(v, part[6 * b + threadIdx.x]) : fmaxf(v, part[6 * b + threadIdx.x]);
+    out[threadIdx.x] = v;
+  }
+}
+
+// ------------------------------------------------ 2. normals and Morton ----
+
+// spreads the low 21 bits of x to every third bit (Morton interleave)
+__device__ __forceinline__ uint64_t spread3(uint32_t x) {
+  uint64_t v = x & 0x1fffffu;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+__global__ void k_tri_prep(const float* __restrict__ V, uint32_t nv, const uint32_t* __restrict__ T, uint32_t nt,
+                           const float* __restrict__ bb, float4* __restrict__ normals, uint64_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals, uint32_t* status) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  uint32_t a = T[3 * (size_t)i], b = T[3 * (size_t)i + 1], c = T[3 * (size_t)i + 2];
+  if (a >= nv || b >= nv || c >= nv) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    a = b = c = 0;
+  }
+  const float* A = V + 3 * (size_t)a;
+  const float* B = V + 3 * (size_t)b;
+  const float* C = V + 3 * (size_t)c;
+  // jtk compute_triangle_normals: normalize(cross(V1 - V0, V2 - V0))
+  float e1x = fs(B[0], A[0]), e1y = fs(B[1], A[1]), e1z = fs(B[2], A[2]);
+  float e2x = fs(C[0], A[0]), e2y = fs(C[1], A[1]), e2z = fs(C[2], A[2]);
+  float nx = fs(fm(e1y, e2z), fm(e1z, e2y));
+  float ny = fs(fm(e1z, e2x), fm(e1x, e2z));
+  float nz = fs(fm(e1x, e2y), fm(e1y, e2x));
+  float len = __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz));
+  if (len > 0.f) {
+    nx = __fdiv_rn(nx, len);
+    ny = __fdiv_rn(ny, len);
+    nz = __fdiv_rn(nz, len);
+  }
+  normals[i] = make_float4(nx, ny, nz, 0.f);
+  // Morton code of the AABB centroid over the vertex bbox
+  const float scale = (float)(1u << kMortonBitsPerAxis);
+  uint32_t q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float lo = fminf(fminf(A[k], B[k]), C[k]), hi = fmaxf(fmaxf(A[k], B[k]), C[k]);
+    float cen = (lo + hi) * 0.5f;
+    float ext = bb[3 + k] - bb[k];
+    float f = ext > 0.f ? (cen - bb[k]) / ext * scale : 0.f;
+    f = fminf(fmaxf(f, 0.f), scale - 1.f);
+    q[k] = (uint32_t)f;
+  }
+  keys[i] = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+  vals[i] = i;
+}
+
+// ------------------------------------------------------ 3. radix sort ----
+
+static const int kSortThreads = 256;
+static const int kSortItems = 16;
+static const int kSortTile = kSortThreads * kSortItems;
+
+__global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift, uint32_t num_tiles,
+                             uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  size_t base = (size_t)blockIdx.x * kSortTile;
+#pragma unroll 4
+  for (int j = 0; j < kSortItems; ++j) {
+    size_t idx = base + (size_t)j * kSortThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan helpers (three phases over chunks of 1024 elements)
+__global__ void k_scan_chunks(const uint32_t* in, uint32_t* out, uint32_t n,
+                              uint32_t* __restrict__ sums) {
+  __shared__ uint32_t s[1024];
+  uint32_t i = blockIdx.x * 1024 + threadIdx.x;
+  uint32_t v = i < n ? in[i] : 0;
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint32_t t = threadIdx.x >= (uint32_t)o ? s[threadIdx.x - o] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) out[i] = s[threadIdx.x] - v;
+  if (threadIdx.x == 1023) sums[blockIdx.x] = s[1023];
+}
+
+__global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t n) {
+  // single block, sequential over per-thread strips
+  __shared__ uint32_t part[1024];
+  uint32_t per = (n + 1023) / 1024;
+  uint32_t b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t acc = 0;
+  for (uint32_t i = b; i < e; ++i) acc += sums[i];
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int t = 0; t < 1024; ++t) {
+      uint32_t x = part[t];
+      part[t] = run;
+      run += x;
+    }
+  }
+  __syncthreads();
+  acc = part[threadIdx.x];
+  for (uint32_t i = b; i < e; ++i) {
+    uint32_t x = sums[i];
+    sums[i] = acc;
+    acc += x;
+  }
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, uint32_t n, const uint32_t* __restrict__ sums) {
+  uint32_t i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+}
+
+__global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n, int shift,
+                                uint32_t num_tiles, const uint32_t* __restrict__ offsets, uint32_t* status) {
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t wc[kSortThreads / 32][257];
+  __shared__ uint32_t total[256];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  base[tid] = offsets[(size_t)tid * num_tiles + blockIdx.x];
+  size_t tile = (size_t)blockIdx.x * kSortTile;
+  for (int j = 0; j < kSortItems; ++j) {
+    for (int w = 0; w < kSortThreads / 32; ++w) wc[w][tid] = 0;
+    if (tid == 0)
+      for (int w = 0; w < kSortThreads / 32; ++w) wc[w][256] = 0;
+    __syncthreads();
+    size_t idx = tile + (size_t)j * kSortThreads + tid;
+    bool valid = idx < n;
+    uint64_t k = valid ? kin[idx] : 0;
+    uint32_t d = valid ? (uint32_t)((k >> shift) & 255u) : 256u;
+    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    if (rank == 0) wc[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t run = 0;
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        uint32_t c = wc[w][tid];
+        wc[w][tid] = run;
+        run += c;
+      }
+      total[tid] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      uint32_t pos = base[d] + wc[warp][d] + rank;
+      if (pos < n) {
+        kout[pos] = k;
+        vout[pos] = vin[idx];
+      } else {
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+      }
+    }
+    __syncthreads();
+    base[tid] += total[tid];
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------- 4. leaf-ordered triangles ----
+
+__global__ void k_soup(const float* __restrict__ V, const uint32_t* __restrict__ T, const uint32_t* __restrict__ order,
+                       uint32_t nt, uint32_t nv, float4* __restrict__ tris, uint32_t* status) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  uint32_t id = order[i];
+  if (id >= nt) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    id = 0;
+  }
+  uint32_t a = T[3 * (size_t)id], b = T[3 * (size_t)id + 1], c = T[3 * (size_t)id + 2];
+  if (a >= nv || b >= nv || c >= nv) a = b = c = 0;
+  tris[3 * (size_t)i] = make_float4(V[3 * (size_t)a], V[3 * (size_t)a + 1], V[3 * (size_t)a + 2], __uint_as_float(id));
+  tris[3 * (size_t)i + 1] = make_float4(V[3 * (size_t)b], V[3 * (size_t)b + 1], V[3 * (size_t)b + 2], 0.f);
+  tris[3 * (size_t)i + 2] = make_float4(V[3 * (size_t)c], V[3 * (size_t)c + 1], V[3 * (size_t)c + 2], 0.f);
+}
+
+// ------------------------------------------------------------- 5. LBVH ----
+
+struct BinNode {   // binary node n (split between sorted leaves n and n+1)
+  float4 lo, hi;   // box (w unused)
+};
+
+__device__ __forceinline__ void leaf_box(const float4* __restrict__ tris, uint32_t i, float4& lo, float4& hi) {
+  float4 a = tris[3 * (size_t)i], b = tris[3 * (size_t)i + 1], c = tris[3 * (size_t)i + 2];
+  lo = make_float4(fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z), 0.f);
+  hi = make_float4(fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z), 0.f);
+}
+
+// split order: smaller (xor, i ^ (i+1), i) merges first
+__device__ __forceinline__ bool split_less(const uint64_t* __restrict__ k, uint32_t a, uint32_t b) {
+  uint64_t xa = k[a] ^ k[a + 1], xb = k[b] ^ k[b + 1];
+  if (xa != xb) return xa < xb;
+  uint32_t sa = a ^ (a + 1), sb = b ^ (b + 1);
+  if (sa != sb) return sa < sb;
+  return a < b;
+}
+
+// child refs: bit 31 set = sorted leaf index, else binary node index
+__global__ void k_lbvh(const uint64_t* __restrict__ keys, const float4* __restrict__ tris, uint32_t n,
+                       uint2* __restrict__ child, BinNode* __restrict__ box, uint2* __restrict__ range,
+                       uint32_t* __restrict__ other, uint32_t* __restrict__ root) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t l = i, r = i;
+  uint32_t cur = 0x80000000u | i;
+  float4 lo, hi;
+  leaf_box(tris, i, lo, hi);
+  for (;;) {
+    uint32_t p, prev;
+    bool as_left;
+    if (l == 0 || (r != n - 1 && split_less(keys, r, l - 1))) {
+      p = r;
+      as_left = true;
+      __stcg(&child[p].x, cur);
+      __threadfence();
+      prev = atomicExch(&other[p], l);
+    } else {
+      p = l - 1;
+      as_left = false;
+      __stcg(&child[p].y, cur);
+      __threadfence();
+      prev = atomicExch(&other[p], r);
+    }
+    if (prev == 0xffffffffu) return;  // first to arrive: the sibling finishes p
+    __threadfence();
+    if (as_left)
+      r = prev;
+    else
+      l = prev;
+    uint32_t sib = as_left ? __ldcg(&child[p].y) : __ldcg(&child[p].x);
+    float4 slo, shi;
+    if (sib & 0x80000000u) {
+      leaf_box(tris, sib & 0x7fffffffu, slo, shi);
+    } else {
+      slo = __ldcg(&box[sib].lo);
+      shi = __ldcg(&box[sib].hi);
+    }
+    lo = make_float4(fminf(lo.x, slo.x), fminf(lo.y, slo.y), fminf(lo.z, slo.z), 0.f);
+    hi = make_float4(fmaxf(hi.x, shi.x), fmaxf(hi.y, shi.y), fmaxf(hi.z, shi.z), 0.f);
+    __stcg(&box[p].lo, lo);
+    __stcg(&box[p].hi, hi);
+    __stcg(&range[p], make_uint2(l, r));
+    cur = p;
+    if (l == 0 && r == n - 1) {
+      *root = p;
+      return;
+    }
+  }
+}
+
+// --------------------------------------------------------- 6. collapse ----
+
+struct CollapseItem {
+  uint32_t bin;    // binary node index
+  uint32_t wide;   // wide node index to fill
+  uint32_t depth;
+};
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+  float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                           const uint2* __restrict__ range, const float4* __restrict__ tris,
+                           const CollapseItem* __restrict__ qin, uint32_t n_in, CollapseItem* __restrict__ qout,
+                           uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
+                           uint32_t leaf_size, uint32_t* __restrict__ max_depth) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_in) return;
+  CollapseItem it = qin[t];
+  uint32_t ref[4];
+  float4 lo[4], hi[4];
+  uint32_t cnt[4];
+  int m = 0;
+  auto load = [&](uint32_t r, int s) {
+    ref[s] = r;
+    if (r & 0x80000000u) {
+      leaf_box(tris, r & 0x7fffffffu, lo[s], hi[s]);
+      cnt[s] = 1;
+    } else {
+      lo[s] = box[r].lo;
+      hi[s] = box[r].hi;
+      uint2 rg = range[r];
+      cnt[s] = rg.y - rg.x + 1;
+    }
+  };
+  uint2 c = child[it.bin];
+  load(c.x, 0);
+  load(c.y, 1);
+  m = 2;
+  while (m < 4) {
+    int best = -1;
+    float ba = -1.f;
+    for (int s = 0; s < m; ++s)
+      if (cnt[s] > leaf_size) {
+        float a = half_area(lo[s], hi[s]);
+        if (a > ba) {
+          ba = a;
+          best = s;
+        }
+      }
+    if (best < 0) break;
+    uint2 cc = child[ref[best]];
+    load(cc.y, m);
+    load(cc.x, best);
+    ++m;
+  }
+  float4* W = wide + 8 * (size_t)it.wide;
+  float v[6][4];
+  uint32_t out_ref[4];
+  for (int s = 0; s < 4; ++s) {
+    if (s < m) {
+      v[0][s] = lo[s].x;
+      v[1][s] = hi[s].x;
+      v[2][s] = lo[s].y;
+      v[3][s] = hi[s].y;
+      v[4][s] = lo[s].z;
+      v[5][s] = hi[s].z;
+      if (cnt[s] <= leaf_size) {
+        uint32_t first = (ref[s] & 0x80000000u) ? (ref[s] & 0x7fffffffu) : range[ref[s]].x;
+        out_ref[s] = J3DG_LEAF_BIT | (first << 3) | (cnt[s] - 1u);
+      } else {
+        uint32_t w = atomicAdd(n_wide, 1u);
+        uint32_t q = atomicAdd(n_out, 1u);
+        qout[q] = CollapseItem{ref[s], w, it.depth + 1};
+        out_ref[s] = w;
+      }
+    } else {
+      v[0][s] = v[2][s] = v[4][s] = 3.4e38f;
+      v[1][s] = v[3][s] = v[5][s] = -3.4e38f;
+      out_ref[s] = J3DG_EMPTY_REF;
+    }
+  }
+  for (int k = 0; k < 6; ++k) W[k] = make_float4(v[k][0], v[k][1], v[k][2], v[k][3]);
+  W[6] = make_float4(__uint_as_float(out_ref[0]), __uint_as_float(out_ref[1]), __uint_as_float(out_ref[2]),
+                     __uint_as_float(out_ref[3]));
+  W[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+  atomicMax(max_depth, it.depth);
+}
+
+// ------------------------------------------------------------- driver ----
+
+#define J3DG_CK(x)                                             \
+  do {                                                         \
+    cudaError_t e_ = (x);                                      \
+    if (e_ != cudaSuccess) {                                   \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);   \
+      rc = J3DG_ERR_CUDA;                                      \
+      goto cleanup;                                            \
+    }                                                          \
+  } while (0)
+
+// Builds the device BVH. dV and dT are device arrays. On success fills the
+// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals).
+int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
+              std::string& err) {
+  int rc = J3DG_OK;
+  const uint32_t nv = m->nv, nt = m->nt;
+  float* d_part = nullptr;
+  float* d_bb = nullptr;
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  uint32_t *v0 = nullptr, *v1 = nullptr, *hist = nullptr, *sums = nullptr;
+  uint2 *child = nullptr, *range = nullptr;
+  BinNode* box = nullptr;
+  uint32_t *other = nullptr, *counters = nullptr;
+  CollapseItem *qa = nullptr, *qb = nullptr;
+  float4* wide = nullptr;
+  const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
+  const uint32_t hist_n = 256 * n_tiles;
+  const uint32_t scan_blocks = (hist_n + 1023) / 1024;
+  const int bbox_blocks = 1024;
+  float hbb[6];
+  uint32_t hc[4] = {0, 0, 0, 0};
+  uint32_t n_in = 0;
+  CollapseItem root_item;
+
+  J3DG_CK(cudaMallocAsync((void**)&d_part, sizeof(float) * 6 * bbox_blocks, st));
+  J3DG_CK(cudaMallocAsync((void**)&d_bb, sizeof(float) * 6, st));
+  k_bbox_partial<<<bbox_blocks, 256, 0, st>>>(dV, nv, d_part);
+  k_bbox_final<<<1, 32, 0, st>>>(d_part, bbox_blocks, d_bb);
+  J3DG_CK(cudaGetLastError());
+  J3DG_CK(cudaMemcpyAsync(hbb, d_bb, sizeof(hbb), cudaMemcpyDeviceToHost, st));
+  J3DG_CK(cudaStreamSynchronize(st));
+  m->scale = 0.f;
+  for (int k = 0; k < 3; ++k) {
+    m->min_bb[k] = hbb[k];
+    m->max_bb[k] = hbb[3 + k];
+  }
+  for (int k = 0; k < 6; ++k) m->scale = std::max(m->scale, std::fabs(hbb[k]));
+
+  J3DG_CK(cudaMalloc(&m->d_normals, sizeof(float4) * (size_t)nt));
+  J3DG_CK(cudaMalloc(&m->d_tris, sizeof(float4) * 3 * (size_t)nt));
+  J3DG_CK(cudaMallocAsync((void**)&k0, sizeof(uint64_t) * nt, st));
+  J3DG_CK(cudaMallocAsync((void**)&k1, sizeof(uint64_t) * nt, st));
+  J3DG_CK(cudaMallocAsync((void**)&v0, sizeof(uint32_t) * nt, st));
+  J3DG_CK(cudaMallocAsync((void**)&v1, sizeof(uint32_t) * nt, st));
+  k_tri_prep<<<(nt + 255) / 256, 256, 0, st>>>(dV, nv, dT, nt, d_bb, (float4*)m->d_normals, k0, v0, d_status);
+  J3DG_CK(cudaGetLastError());
+
+  J3DG_CK(cudaMallocAsync((void**)&hist, sizeof(uint32_t) * hist_n, st));
+  J3DG_CK(cudaMallocAsync((void**)&sums, sizeof(uint32_t) * (scan_blocks + 1), st));
+  for (int pass = 0; pass < kRadixPasses; ++pass) {
+    const int shift = 8 * pass;
+    k_radix_hist<<<n_tiles, kSortThreads, 0, st>>>(k0, nt, shift, n_tiles, hist);
+    k_scan_chunks<<<scan_blocks, 1024, 0, st>>>(hist, hist, hist_n, sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, scan_blocks);
+    k_scan_add<<<scan_blocks, 1024, 0, st>>>(hist, hist_n, sums);
+    k_radix_scatter<<<n_tiles, kSortThreads, 0, st>>>(k0, v0, k1, v1, nt, shift, n_tiles, hist, d_status);
+    J3DG_CK(cudaGetLastError());
+    std::swap(k0, k1);
+    std::swap(v0, v1);
+  }
+  k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, v0, nt, nv, (float4*)m->d_tris, d_status);
+  J3DG_CK(cudaGetLastError());
+
+  if (nt <= m->leaf_size) {  // tiny mesh: the root is one leaf
+    m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
+    m->n_nodes = 0;
+    m->max_depth = 0;
+    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8));
+    J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * 8, st));
+    goto cleanup;
+  }
+
+  J3DG_CK(cudaMallocAsync((void**)&child, sizeof(uint2) * (nt - 1), st));
+  J3DG_CK(cudaMallocAsync((void**)&range, sizeof(uint2) * (nt - 1), st));
+  J3DG_CK(cudaMallocAsync((void**)&box, sizeof(BinNode) * (nt - 1), st));
+  J3DG_CK(cudaMallocAsync((void**)&other, sizeof(uint32_t) * (nt - 1), st));
+  J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
+  J3DG_CK(cudaMemsetAsync(other, 0xff, sizeof(uint32_t) * (nt - 1), st));
+  J3DG_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * 4, st));
+  k_lbvh<<<(nt + 255) / 256, 256, 0, st>>>(k0, (const float4*)m->d_tris, nt, child, box, range, other, counters);
+  J3DG_CK(cudaGetLastError());
+
+  // every wide node has >= 2 children, so there are at most nt - 1 of them
+  J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * 8 * (size_t)nt, st));
+  J3DG_CK(cudaMallocAsync((void**)&qa, sizeof(CollapseItem) * (size_t)nt, st));
+  J3DG_CK(cudaMallocAsync((void**)&qb, sizeof(CollapseItem) * (size_t)nt, st));
+  J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  J3DG_CK(cudaStreamSynchronize(st));
+  root_item = CollapseItem{hc[0], 0u, 1u};
+  J3DG_CK(cudaMemcpyAsync(qa, &root_item, sizeof(root_item), cudaMemcpyHostToDevice, st));
+  hc[0] = 0u;  // unused
+  hc[1] = 1u;  // wide nodes allocated (the root)
+  hc[2] = 0u;  // queue out
+  hc[3] = 0u;  // max depth
+  J3DG_CK(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+  n_in = 1;
+  while (n_in > 0) {
+    J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
+    k_collapse<<<(n_in + 127) / 128, 128, 0, st>>>(child, box, range, (const float4*)m->d_tris, qa, n_in, qb,
+                                                   counters + 2, counters + 1, wide, m->leaf_size, counters + 3);
+    J3DG_CK(cudaGetLastError());
+    J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    J3DG_CK(cudaStreamSynchronize(st));
+    n_in = hc[2];
+    std::swap(qa, qb);
+  }
+  m->n_nodes = hc[1];
+  m->max_depth = hc[3];
+  m->root_ref = 0;
+  J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
+  J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
+
+cleanup:
+  if (d_part) cudaFreeAsync(d_part, st);
+  if (d_bb) cudaFreeAsync(d_bb, st);
+  if (k0) cudaFreeAsync(k0, st);
+  if (k1) cudaFreeAsync(k1, st);
+  if (v0) cudaFreeAsync(v0, st);
+  if (v1) cudaFreeAsync(v1, st);
+  if (hist) cudaFreeAsync(hist, st);
+  if (sums) cudaFreeAsync(sums, st);
+  if (child) cudaFreeAsync(child, st);
+  if (range) cudaFreeAsync(range, st);
+  if (box) cudaFreeAsync(box, st);
+  if (other) cudaFreeAsync(other, st);
+  if (counters) cudaFreeAsync(counters, st);
+  if (wide) cudaFreeAsync(wide, st);
+  if (qa) cudaFreeAsync(qa, st);
+  if (qb) cudaFreeAsync(qb, st);
+  {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == J3DG_OK && e != cudaSuccess) {
+      err = std::string("build: ") + cudaGetErrorString(e);
+      rc = J3DG_ERR_CUDA;
+    }
+  }
+  if (rc != J3DG_OK) return rc;
+  if (m->max_depth > J3DG_MAX_DEPTH) {
+    err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack";
+    return J3DG_ERR_UNSUPPORTED;
+  }
+  m->device_bytes = sizeof(float4) * 8 * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
+                    sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 3 * (uint64_t)nt;
+  return J3DG_OK;
+}
+
+}  // namespace j3dg

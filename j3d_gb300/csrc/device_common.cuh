@@ -1,0 +1,285 @@
+// device_common.cuh -- exact fp32 math, ray preparation, slab test,
+// Moller-Trumbore with the bounds gate, and wide-BVH traversal.
+//
+// Every operation that decides a hit or produces a G-buffer value is written
+// with round-to-nearest intrinsics (__fmul_rn, __fadd_rn, __fdiv_rn,
+// __fsqrt_rn, __fmaf_rn), so it matches the host restatement bit for bit
+// regardless of FMA contraction. The fixed operation order:
+//   mat x vec   r_i = ((m[i] x + m[4+i] y) + m[8+i] z) + m[12+i] w   (column-major)
+//   dot3        (a.x b.x + a.y b.y) + a.z b.z
+//   cross       (a.y b.z - a.z b.y, a.z b.x - a.x b.z, a.x b.y - a.y b.x)
+//   triangle    Moller-Trumbore (1997), double sided; accept iff det != 0,
+//               u >= 0, v >= 0, u + v <= 1, t > t_near, the hit t inside the
+//               slab interval of the triangle's own AABB, and (t, object,
+//               triangle) smaller than the best so far (strictly t < t_far).
+//   slab        d' = d with |d_i| < 1e-12 replaced by copysign(1e-12, d_i),
+//               inv = 1/d', pad = (max|o| + mesh scale) 2^-19, near/far
+//               origins o -/+ pad by sign(inv), t = fma(plane, inv, -(o') inv),
+//               enter = max over axes, exit = min over axes.
+// Node boxes hold their triangles' boxes exactly (min/max are exact) and the
+// slab formula is monotone in the planes, so no node on the path to an
+// accepted triangle is ever culled: results do not depend on the BVH shape.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace j3dg {
+
+struct DevInst {
+  const float4* nodes;     // 8 float4 per wide node
+  const float4* tris;      // 3 float4 per triangle, leaf order; v0.w = id bits
+  const float4* normals;   // per triangle id
+  const uint32_t* index;   // caller's triangle indices (3 per triangle)
+  const float* colors;     // per vertex rgb or null
+  const float* uv;         // 6 per triangle or null
+  const uint32_t* tex;     // RGBA8 or null
+  uint32_t tex_w, tex_h;
+  uint32_t root_ref;       // inner node 0, or a leaf ref for tiny meshes
+  uint32_t n_nodes;
+  uint32_t nt;
+  uint32_t db_id;
+  float scale;
+  float pad_;
+  float cs[16];
+  float inv[16];
+};
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+
+__device__ __forceinline__ float4 mat_vec(const float* m, float x, float y, float z, float w) {
+  float r[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r[i] = fa(fa(fa(fm(m[i], x), fm(m[4 + i], y)), fm(m[8 + i], z)), fm(m[12 + i], w));
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+  return fa(fa(fm(ax, bx), fm(ay, by)), fm(az, bz));
+}
+
+struct Ray {
+  float ox, oy, oz, dx, dy, dz;
+  float ix, iy, iz;     // 1 / clamped direction
+  float nnx, nny, nnz;  // -(near origin) * inv
+  float nfx, nfy, nfz;  // -(far origin) * inv
+  uint32_t neg;         // bit a: inv_a < 0
+  float t_near;
+};
+
+__device__ __forceinline__ void prep_axis(float o, float d, float pad, float& inv, float& nn, float& nf, bool& neg) {
+  float dd = (fabsf(d) < 1e-12f) ? copysignf(1e-12f, d) : d;
+  inv = __fdiv_rn(1.f, dd);
+  neg = inv < 0.f;
+  float on = neg ? fs(o, pad) : fa(o, pad);
+  float of = neg ? fa(o, pad) : fs(o, pad);
+  nn = fm(-on, inv);
+  nf = fm(-of, inv);
+}
+
+__device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, float dy, float dz, float t_near,
+                                        float scale) {
+  Ray r;
+  r.ox = ox;
+  r.oy = oy;
+  r.oz = oz;
+  r.dx = dx;
+  r.dy = dy;
+  r.dz = dz;
+  r.t_near = t_near;
+  float mo = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+  float pad = fm(fa(mo, scale), 0x1p-19f);
+  bool nx, ny, nz;
+  prep_axis(ox, dx, pad, r.ix, r.nnx, r.nfx, nx);
+  prep_axis(oy, dy, pad, r.iy, r.nny, r.nfy, ny);
+  prep_axis(oz, dz, pad, r.iz, r.nnz, r.nfz, nz);
+  r.neg = (nx ? 1u : 0u) | (ny ? 2u : 0u) | (nz ? 4u : 0u);
+  return r;
+}
+
+// Slab interval of [lo, hi]; returns (enter, exit) before clipping.
+__device__ __forceinline__ void slab(const Ray& r, float lox, float loy, float loz, float hix, float hiy, float hiz,
+                                     float& tn, float& tf) {
+  float pnx = (r.neg & 1u) ? hix : lox, pfx = (r.neg & 1u) ? lox : hix;
+  float pny = (r.neg & 2u) ? hiy : loy, pfy = (r.neg & 2u) ? loy : hiy;
+  float pnz = (r.neg & 4u) ? hiz : loz, pfz = (r.neg & 4u) ? loz : hiz;
+  tn = fmaxf(fmaxf(__fmaf_rn(pnx, r.ix, r.nnx), __fmaf_rn(pny, r.iy, r.nny)), __fmaf_rn(pnz, r.iz, r.nnz));
+  tf = fminf(fminf(__fmaf_rn(pfx, r.ix, r.nfx), __fmaf_rn(pfy, r.iy, r.nfy)), __fmaf_rn(pfz, r.iz, r.nfz));
+}
+
+struct Best {
+  float t;
+  uint32_t inst, tri;  // key = (inst, tri); found == (t < t_far set by an accept)
+  float u, v;
+  uint32_t slot;       // leaf-order position of the best triangle
+  bool found;
+};
+
+__device__ __forceinline__ bool key_less(uint32_t ia, uint32_t ta, uint32_t ib, uint32_t tb) {
+  return ia < ib || (ia == ib && ta < tb);
+}
+
+// Moller-Trumbore + gate for triangle `slot`. ANY: the caller stops at the
+// first accept, so the (t, key) comparison only needs t < t_best.
+template <bool ANY>
+__device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict__ tris, uint32_t slot, uint32_t inst,
+                                         Best& b) {
+  const float4 a = __ldg(tris + 3 * (size_t)slot);
+  const float4 c1 = __ldg(tris + 3 * (size_t)slot + 1);
+  const float4 c2 = __ldg(tris + 3 * (size_t)slot + 2);
+  float e1x = fs(c1.x, a.x), e1y = fs(c1.y, a.y), e1z = fs(c1.z, a.z);
+  float e2x = fs(c2.x, a.x), e2y = fs(c2.y, a.y), e2z = fs(c2.z, a.z);
+  float px = fs(fm(r.dy, e2z), fm(r.dz, e2y));
+  float py = fs(fm(r.dz, e2x), fm(r.dx, e2z));
+  float pz = fs(fm(r.dx, e2y), fm(r.dy, e2x));
+  float det = dot3(e1x, e1y, e1z, px, py, pz);
+  if (det == 0.f) return false;
+  float inv = __fdiv_rn(1.f, det);
+  float sx = fs(r.ox, a.x), sy = fs(r.oy, a.y), sz = fs(r.oz, a.z);
+  float u = fm(dot3(sx, sy, sz, px, py, pz), inv);
+  float qx = fs(fm(sy, e1z), fm(sz, e1y));
+  float qy = fs(fm(sz, e1x), fm(sx, e1z));
+  float qz = fs(fm(sx, e1y), fm(sy, e1x));
+  float v = fm(dot3(r.dx, r.dy, r.dz, qx, qy, qz), inv);
+  float t = fm(dot3(e2x, e2y, e2z, qx, qy, qz), inv);
+  if (!(u >= 0.f && v >= 0.f && fa(u, v) <= 1.f)) return false;
+  if (!(t > r.t_near)) return false;
+  uint32_t id = __float_as_uint(a.w);
+  if (ANY) {
+    if (!(t < b.t)) return false;
+  } else {
+    if (!(t < b.t || (t == b.t && b.found && key_less(inst, id, b.inst, b.tri)))) return false;
+  }
+  // bounds gate: t inside the slab interval of the triangle's own box
+  float tn, tf;
+  slab(r, fminf(fminf(a.x, c1.x), c2.x), fminf(fminf(a.y, c1.y), c2.y), fminf(fminf(a.z, c1.z), c2.z),
+       fmaxf(fmaxf(a.x, c1.x), c2.x), fmaxf(fmaxf(a.y, c1.y), c2.y), fmaxf(fmaxf(a.z, c1.z), c2.z), tn, tf);
+  if (!(tn <= t && t <= tf)) return false;
+  b.t = t;
+  b.inst = inst;
+  b.tri = id;
+  b.u = u;
+  b.v = v;
+  b.slot = slot;
+  b.found = true;
+  return true;
+}
+
+// Traverses one object's BVH4 with an object-space ray. Returns true if ANY
+// and a triangle was accepted. Raises status bits on stack overflow or when
+// more nodes are visited than the BVH holds (a corrupt tree), and stops.
+template <bool ANY>
+__device__ __forceinline__ bool traverse(const DevInst& I, const Ray& r, uint32_t inst, Best& b,
+                                         uint32_t* status, uint32_t& visits, uint32_t& tests) {
+  const float4* __restrict__ nodes = I.nodes;
+  uint32_t stack_ref[J3DG_STACK];
+  float stack_t[J3DG_STACK];
+  int sp = 0;
+  uint32_t cur = I.root_ref;
+  uint32_t budget = I.n_nodes + 1;
+  for (;;) {
+    if (cur != J3DG_EMPTY_REF) {
+      if (cur & J3DG_LEAF_BIT) {
+        uint32_t first = (cur & 0x7fffffffu) >> 3, cnt = (cur & 7u) + 1u;
+        if (first + cnt > I.nt) {
+          atomicOr(status, J3DG_DEV_BAD_INDEX);
+          return false;
+        }
+        for (uint32_t k = 0; k < cnt; ++k) {
+          ++tests;
+          if (tri_test<ANY>(r, I.tris, first + k, inst, b) && ANY) return true;
+        }
+        cur = J3DG_EMPTY_REF;
+      } else {
+        if (budget-- == 0) {
+          atomicOr(status, J3DG_DEV_VISIT_CAP);
+          return false;
+        }
+        if (cur >= I.n_nodes) {
+          atomicOr(status, J3DG_DEV_BAD_INDEX);
+          return false;
+        }
+        ++visits;
+        const float4* N = nodes + 8 * (size_t)cur;
+        const float4 lox = __ldg(N + 0), hix = __ldg(N + 1), loy = __ldg(N + 2), hiy = __ldg(N + 3);
+        const float4 loz = __ldg(N + 4), hiz = __ldg(N + 5);
+        const uint4 ch = *reinterpret_cast<const uint4*>(&N[6]);
+        float tc[4];
+        uint32_t rc[4] = {ch.x, ch.y, ch.z, ch.w};
+        const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+        const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+        const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float tn, tf;
+          slab(r, lx[c], ly[c], lz[c], hx[c], hy[c], hz[c], tn, tf);
+          float a = fmaxf(tn, r.t_near), e = fminf(tf, b.t);
+          bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
+          tc[c] = hit ? a : __int_as_float(0x7f800000);
+          if (!hit) rc[c] = J3DG_EMPTY_REF;
+        }
+        // sort the four (t, ref) pairs ascending (5 compare-exchanges)
+#define J3DG_CX(i, j)                    \
+  if (tc[j] < tc[i]) {                   \
+    float tt = tc[i];                    \
+    tc[i] = tc[j];                       \
+    tc[j] = tt;                          \
+    uint32_t rr = rc[i];                 \
+    rc[i] = rc[j];                       \
+    rc[j] = rr;                          \
+  }
+        J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(1, 2)
+#undef J3DG_CX
+        if (sp + 3 > J3DG_STACK) {
+          atomicOr(status, J3DG_DEV_STACK_OVERFLOW);
+          return false;
+        }
+#pragma unroll
+        for (int c = 3; c >= 1; --c)
+          if (rc[c] != J3DG_EMPTY_REF) {
+            stack_ref[sp] = rc[c];
+            stack_t[sp] = tc[c];
+            ++sp;
+          }
+        cur = rc[0];
+        continue;
+      }
+    }
+    // pop the nearest entry that can still hold a better hit
+    bool got = false;
+    while (sp > 0) {
+      --sp;
+      if (stack_t[sp] <= b.t) {
+        cur = stack_ref[sp];
+        got = true;
+        break;
+      }
+    }
+    if (!got) return false;
+  }
+}
+
+// qbvh_two_level_with_transformations::find_closest_triangle over all
+// objects: the world ray goes to each object's space as a point and a vector.
+template <bool ANY>
+__device__ __forceinline__ void find_closest(const DevInst* __restrict__ inst, uint32_t n_inst, float ox, float oy,
+                                             float oz, float dx, float dy, float dz, float t_near, float t_far,
+                                             Best& b, uint32_t* status, uint32_t& visits, uint32_t& tests) {
+  b.t = t_far;
+  b.found = false;
+  b.inst = b.tri = 0;
+  b.u = b.v = 0.f;
+  b.slot = 0;
+  for (uint32_t i = 0; i < n_inst; ++i) {
+    const DevInst& I = inst[i];
+    float4 o = mat_vec(I.inv, ox, oy, oz, 1.f);
+    float4 d = mat_vec(I.inv, dx, dy, dz, 0.f);
+    Ray r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, t_near, I.scale);
+    if (traverse<ANY>(I, r, i, b, status, visits, tests) && ANY) return;
+  }
+}
+
+}  // namespace j3dg

@@ -1,0 +1,65 @@
+// internal.h -- host-side definitions of the opaque C-ABI objects.
+#pragma once
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/j3dg.h"
+
+// Wide-node child reference: inner node index, or a leaf of up to 8
+// consecutive triangles of the leaf-ordered triangle array.
+#define J3DG_LEAF_BIT 0x80000000u
+#define J3DG_EMPTY_REF 0xffffffffu
+#define J3DG_MAX_LEAF 8u
+#define J3DG_MAX_TRIANGLES (1u << 28)
+// Traversal stack entries per thread; builds whose depth could overflow it
+// are refused at build time, so the device check never fires on valid BVHs.
+#define J3DG_STACK 96
+#define J3DG_MAX_DEPTH ((J3DG_STACK - 1) / 3)
+
+struct j3dg_ctx {
+  int device = 0;
+  void* stream = nullptr;        // cudaStream_t
+  uint32_t* d_status = nullptr;  // device status word
+  void* d_inst = nullptr;        // device instance table (DevInst[])
+  uint32_t inst_cap = 0;
+  void* h_inst = nullptr;        // pinned staging for the instance table
+  int sm_count = 0;
+  std::string last_error;
+};
+
+struct j3dg_mesh {
+  j3dg_ctx* ctx = nullptr;
+  uint32_t nv = 0, nt = 0;
+  float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
+  float scale = 0.f;  // max |coordinate| of the bbox corners
+  uint32_t leaf_size = 4;
+  uint32_t n_nodes = 0, max_depth = 0, root_ref = 0;
+  float build_ms = 0.f;
+  uint64_t device_bytes = 0;
+  void* d_nodes = nullptr;    // float4[8 * n_nodes]
+  void* d_tris = nullptr;     // float4[3 * nt], leaf order, v0.w = triangle id
+  void* d_normals = nullptr;  // float4[nt], by triangle id
+  void* d_index = nullptr;    // uint32[3 * nt], the caller's triangles
+  void* d_colors = nullptr;   // float[3 * nv] or null
+  void* d_uv = nullptr;       // float[6 * nt] or null
+  void* d_tex = nullptr;      // uint32[tex_w * tex_h] or null
+  uint32_t tex_w = 0, tex_h = 0;
+};
+
+struct j3dg_matcap {
+  j3dg_ctx* ctx = nullptr;
+  uint32_t w = 0, h = 0, cavity = 0;
+  uint32_t* d_pixels = nullptr;
+};
+
+struct j3dg_canvas {
+  j3dg_ctx* ctx = nullptr;
+  uint32_t w = 0, h = 0;
+  j3dg_camera camera;
+  float projection[16], projection_inv[16];
+  j3dg_canvas_settings settings;
+  void* d_pixels = nullptr;      // j3dg_pixel[w*h]
+  uint32_t* d_image = nullptr;   // w*h
+  uint32_t* d_background = nullptr;
+};

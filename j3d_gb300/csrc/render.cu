@@ -1,0 +1,407 @@
+// render.cu -- per-frame kernels: the fused ray-cast frame (primary ray,
+// closest hit, G-buffer record, shadow ray, plain matcap shading), the
+// neighbour-reading shading modes, and batched ray queries.
+//
+// k_render replaces the per-pixel body of canvas::update_canvas
+// (canvas.cpp:765-873) and, in plain mode, canvas_to_image (canvas.cpp:650-669)
+// plus the background copy of canvas::render_scene (canvas.cpp:893-898).
+// k_shade replaces canvas_to_image's edges, wireframe and one-bit modes
+// (canvas.cpp:449-649), which read the right and upper neighbours.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "render.cuh"
+
+namespace j3dg {
+
+// ------------------------------------------------------------ shading ----
+
+__device__ __forceinline__ uint32_t tex_index(float f, uint32_t size) {
+  if (!(f >= 0.f)) f = 0.f;
+  float mx = (float)(size - 1);
+  if (f > mx) f = mx;
+  return (uint32_t)f;
+}
+
+// canvas.cpp:320-328
+__device__ __forceinline__ uint32_t get_U(float u, uint32_t W) {
+  return tex_index(floorf(fa(0.5f, fm(fm(fa(u, 1.f), (float)(W - 1)), 0.5f))), W);
+}
+__device__ __forceinline__ uint32_t get_V(float v, uint32_t H) {
+  return tex_index(floorf(fa(0.5f, fm(fm(fa(-v, 1.f), (float)(H - 1)), 0.5f))), H);
+}
+
+// canvas.cpp:330-344
+__device__ __forceinline__ uint32_t get_color(const uint32_t* __restrict__ mc, uint32_t mw, uint32_t U, uint32_t V,
+                                              uint32_t shadow) {
+  uint32_t clr = __ldg(mc + (size_t)V * mw + U);
+  if (shadow) {
+    uint32_t r = clr & 0xffu, g = (clr >> 8) & 0xffu, b = (clr >> 16) & 0xffu;
+    clr = 0xff000000u | ((b >> 2) << 16) | ((g >> 2) << 8) | (r >> 2);
+  }
+  return clr;
+}
+
+// canvas.cpp:346-389 (acosf: CUDA's, within 1 LSB of the host's after rounding)
+__device__ __forceinline__ uint32_t get_angle_color(float angle, const FrameParams& P, float u, float v,
+                                                    uint32_t mark) {
+  uint32_t clr = get_color(P.matcap, P.mw, get_U(u, P.mw), get_V(v, P.mh), mark);
+  if (fabsf(angle) <= 1.f) {
+    uint32_t r = clr & 0xffu, g = (clr >> 8) & 0xffu, b = (clr >> 16) & 0xffu;
+    const float hp = 1.57079632679489f;
+    float scale = __fdiv_rn(fs(hp, fabsf(fs(acosf(angle), hp))), hp);
+    scale = __fsqrt_rn(fs(1.f, scale));
+    uint32_t c = P.cavity;
+    uint32_t r2 = c & 0xffu, g2 = (c >> 8) & 0xffu, b2 = (c >> 16) & 0xffu;
+    float f = angle > 0.f ? 1.2f : 0.5f;
+    float om = fs(1.f, scale);
+    r = (uint32_t)fa(fm((float)r, om), fm(fm((float)r2, scale), f));
+    g = (uint32_t)fa(fm((float)g, om), fm(fm((float)g2, scale), f));
+    b = (uint32_t)fa(fm((float)b, om), fm(fm((float)b2, scale), f));
+    r = r > 255u ? 255u : r;
+    g = g > 255u ? 255u : g;
+    b = b > 255u ? 255u : b;
+    clr = 0xff000000u | (b << 16) | (g << 8) | r;
+  }
+  return clr;
+}
+
+// canvas.cpp:402-441 (_get_color)
+__device__ __forceinline__ uint32_t pixel_color(const FrameParams& P, uint32_t mark, uint32_t pr, uint32_t pg,
+                                                uint32_t pb, float u, float v) {
+  if (mark & 2u) {
+    if (P.shading) {
+      float nz = __fsqrt_rn(fs(fs(1.f, fm(u, u)), fm(v, v)));
+      float d = fa(fa(fa(fm(u, 0.f), fm(v, 0.f)), fm(nz, 1.f)), fm(0.f, 0.f));
+      d = d < 0.f ? 0.f : (d > 1.f ? 1.f : d);
+      float dif = fm(d, (mark & 1u) ? 0.3f : 1.f);
+      return 0xff000000u | ((uint32_t)fm((float)pb, dif) << 16) | ((uint32_t)fm((float)pg, dif) << 8) |
+             (uint32_t)fm((float)pr, dif);
+    }
+    if (mark & 1u) return 0xff000000u | ((pb >> 2) << 16) | ((pg >> 2) << 8) | (pr >> 2);
+    return 0xff000000u | (pb << 16) | (pg << 8) | pr;
+  }
+  return get_color(P.matcap, P.mw, get_U(u, P.mw), get_V(v, P.mh), mark);
+}
+
+// ------------------------------------------------------------- render ----
+
+__global__ void __launch_bounds__(128) k_render(const FrameParams P) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x = P.x0 + (int)blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const int y = P.y0 + (int)blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  if (x > P.x1 || y > P.y1) return;
+  const size_t pix = (size_t)y * P.w + x;
+  j3dg_pixel* rec = P.gbuf + pix;
+  uint32_t visits = 0, tests = 0;
+  if (P.n_inst == 0) {
+    // canvas.cpp:744-759: no objects, every pixel a miss
+    rec->db_id = 0u;
+    rec->object_id = 0xffffffffu;
+    rec->u = 0.f;
+    rec->v = 0.f;
+    rec->depth = FLT_MAX;
+    if (P.shade_mode == 1) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
+    return;
+  }
+  // canvas.cpp:700-705
+  const float4 origin = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
+  const float ld = fm(P.diagonal, 3.f);
+  const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
+  // canvas.cpp:773-782
+  const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
+  const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
+  float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
+  d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
+  const float t_near = __fdiv_rn(P.diagonal, 100.f);
+  Best b;
+  find_closest<false>(P.inst, P.n_inst, origin.x, origin.y, origin.z, d.x, d.y, d.z, t_near, FLT_MAX, b, P.status,
+                      visits, tests);
+  uint32_t color = 0;
+  if (b.found) {
+    // canvas.cpp:788-801
+    const DevInst& I = P.inst[b.inst];
+    const float4 N = __ldg(I.normals + b.tri);
+    float4 n = mat_vec(P.cs_inv, N.x, N.y, N.z, 0.f);
+    n = mat_vec(I.cs, n.x, n.y, n.z, n.w);
+    uint32_t mark = 0, pr = 0, pg = 0, pb = 0;
+    bool rgb = false;
+    const float wgt = fs(fs(1.f, b.u), b.v);
+    if (P.textured && I.uv != nullptr && I.tex != nullptr) {
+      // canvas.cpp:803-820
+      const float* uv = I.uv + 6 * (size_t)b.tri;
+      float c0 = fa(fa(fm(wgt, uv[0]), fm(b.u, uv[2])), fm(b.v, uv[4]));
+      float c1 = fa(fa(fm(wgt, uv[1]), fm(b.u, uv[3])), fm(b.v, uv[5]));
+      c0 = fmaxf(fminf(c0, 1.f), 0.f);
+      c1 = fmaxf(fminf(c1, 1.f), 0.f);
+      const int tw = (int)I.tex_w, th = (int)I.tex_h;
+      int tx = (int)fm(c0, (float)tw), ty = (int)fm(c1, (float)th);
+      tx = tx < 0 ? 0 : tx >= tw ? tw - 1 : tx;
+      ty = ty < 0 ? 0 : ty >= th ? th - 1 : ty;
+      const uint32_t c = __ldg(I.tex + (size_t)ty * I.tex_w + tx);
+      pr = c & 0xffu;
+      pg = (c >> 8) & 0xffu;
+      pb = (c >> 16) & 0xffu;
+      mark |= 2u;
+      rgb = true;
+    } else if (P.vertexcolors && I.colors != nullptr) {
+      // canvas.cpp:821-834
+      const uint32_t* T = I.index + 3 * (size_t)b.tri;
+      const float* C0 = I.colors + 3 * (size_t)T[0];
+      const float* C1 = I.colors + 3 * (size_t)T[1];
+      const float* C2 = I.colors + 3 * (size_t)T[2];
+      float c[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u, C1[k])), fm(b.v, C2[k]));
+      pr = (uint8_t)fm(c[0], 255.f);
+      pg = (uint8_t)fm(c[1], 255.f);
+      pb = (uint8_t)fm(c[2], 255.f);
+      mark |= 2u;
+      rgb = true;
+    }
+    if (P.shadow) {
+      // canvas.cpp:836-857: shadow ray from the hit point towards the light
+      const float4 A = __ldg(I.tris + 3 * (size_t)b.slot);
+      const float4 B = __ldg(I.tris + 3 * (size_t)b.slot + 1);
+      const float4 C = __ldg(I.tris + 3 * (size_t)b.slot + 2);
+      const float4 V0 = mat_vec(I.cs, A.x, A.y, A.z, 1.f);
+      const float4 V1 = mat_vec(I.cs, B.x, B.y, B.z, 1.f);
+      const float4 V2 = mat_vec(I.cs, C.x, C.y, C.z, 1.f);
+      const float px = fa(fa(fm(V0.x, wgt), fm(b.u, V1.x)), fm(b.v, V2.x));
+      const float py = fa(fa(fm(V0.y, wgt), fm(b.u, V1.y)), fm(b.v, V2.y));
+      const float pz = fa(fa(fm(V0.z, wgt), fm(b.u, V1.z)), fm(b.v, V2.z));
+      Best b2;
+      find_closest<true>(P.inst, P.n_inst, px, py, pz, fs(light.x, px), fs(light.y, py), fs(light.z, pz), 1e-3f,
+                         FLT_MAX, b2, P.status, visits, tests);
+      if (b2.found) mark |= 1u;
+    }
+    if (rgb) {
+      reinterpret_cast<uint32_t*>(rec)[0] = mark | (pr << 8) | (pg << 16) | (pb << 24);
+    } else {
+      reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
+    }
+    rec->u = n.x;
+    rec->v = n.y;
+    rec->depth = b.t;
+    *reinterpret_cast<uint4*>(&rec->object_id) =
+        make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
+    if (P.shade_mode == 1) color = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
+  } else {
+    // canvas.cpp:859-866
+    rec->db_id = 0u;
+    rec->object_id = 0xffffffffu;
+    rec->u = 0.f;
+    rec->v = 0.f;
+    rec->depth = FLT_MAX;
+    if (P.shade_mode == 1) color = P.background ? __ldg(P.background + pix) : P.im[pix];
+  }
+  if (P.shade_mode == 1) P.im[pix] = color;
+  if (P.counters) {
+    atomicAdd(P.counters + 0, (unsigned long long)visits);
+    atomicAdd(P.counters + 1, (unsigned long long)tests);
+  }
+}
+
+// ----------------------------------------------------------- k_shade ----
+
+__device__ __forceinline__ bool differs(const j3dg_pixel& a, const j3dg_pixel& b) {
+  const float th = 0.001f;
+  return b.object_id != 0xffffffffu && (fabsf(fs(a.u, b.u)) > th || fabsf(fs(a.v, b.v)) > th);
+}
+
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+  return fa(fa(fa(fm(a.x, b.x), fm(a.y, b.y)), fm(a.z, b.z)), fm(a.w, b.w));
+}
+
+// canvas.cpp:287-315
+__device__ float convex_cos_angle(const FrameParams& P, float x1, float y1, float u1, float v1, float depth1, float x2,
+                                  float y2, float u2, float v2, float depth2) {
+  float4 d1 = mat_vec(P.pinv, fs(fm(2.f, __fdiv_rn(fa(x1, 0.5f), (float)P.w)), 1.f),
+                      fs(fm(2.f, __fdiv_rn(fa(y1, 0.5f), (float)P.h)), 1.f), P.near_plane, 1.f);
+  d1.w = 0.f;
+  float4 p1 = make_float4(fm(depth1, d1.x), fm(depth1, d1.y), fm(depth1, d1.z), fm(depth1, d1.w));
+  float4 d2 = mat_vec(P.pinv, fs(fm(2.f, __fdiv_rn(fa(x2, 0.5f), (float)P.w)), 1.f),
+                      fs(fm(2.f, __fdiv_rn(fa(y2, 0.5f), (float)P.h)), 1.f), P.near_plane, 1.f);
+  d2.w = 0.f;
+  float4 p2 = make_float4(fm(depth2, d2.x), fm(depth2, d2.y), fm(depth2, d2.z), fm(depth2, d2.w));
+  float4 n1 = make_float4(u1, v1, __fsqrt_rn(fs(fs(1.f, fm(u1, u1)), fm(v1, v1))), 0.f);
+  float4 n2 = make_float4(u2, v2, __fsqrt_rn(fs(fs(1.f, fm(u2, u2)), fm(v2, v2))), 0.f);
+  if ((double)fabsf(fs(dot4(n1, n2), 1.f)) > 0.0001) {
+    float4 pt = make_float4(fs(p2.x, p1.x), fs(p2.y, p1.y), fs(p2.z, p1.z), fs(p2.w, p1.w));
+    float len = __fsqrt_rn(dot4(pt, pt));
+    pt = make_float4(__fdiv_rn(pt.x, len), __fdiv_rn(pt.y, len), __fdiv_rn(pt.z, len), __fdiv_rn(pt.w, len));
+    return dot4(pt, n1);
+  }
+  return 0.f;
+}
+
+__device__ __forceinline__ uint32_t one_bit_res(uint32_t clr) {
+  return ((((clr & 0xff0000u) >> 16) + ((clr & 0xff00u) >> 8) + (clr & 0xffu)) >> 7) + 1u;
+}
+
+// canvas_to_image for one pixel. mode: 0 plain, 1 edges, 2 wireframe, 3 one-bit.
+__global__ void __launch_bounds__(256) k_shade(const FrameParams P, const j3dg_pixel* __restrict__ G, int mode,
+                                               int fill_background) {
+  const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31);
+  const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= P.w || y >= P.h) return;
+  const size_t pix = (size_t)y * P.w + x;
+  const j3dg_pixel p = G[pix];
+  if (p.object_id == 0xffffffffu) {
+    if (fill_background) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
+    return;
+  }
+  const uint32_t mark = p.mark;
+  uint32_t out;
+  const bool last_col = (x + 1 == P.w);
+  const j3dg_pixel* up = G + (size_t)(y == 0 ? 0 : y - 1) * P.w + x;
+  if (mode == 3) {
+    uint32_t clr = get_color(P.matcap, P.mw, get_U(p.u, P.mw), get_V(p.v, P.mh), mark);
+    uint32_t res = one_bit_res(clr);
+    if (last_col) {
+      out = (((P.w - 1) % res == 0) && (y % res == 0)) ? 0xff000000u : 0xffffffffu;
+    } else {
+      float angle = 1.f;
+      const j3dg_pixel r = G[pix + 1];
+      const j3dg_pixel* q = nullptr;
+      j3dg_pixel u = *up;
+      if (differs(p, r))
+        q = &r;
+      else if (differs(p, u))
+        q = &u;
+      if (q) {
+        float w1 = __fsqrt_rn(fs(fs(1.f, fm(p.u, p.u)), fm(p.v, p.v)));
+        float w2 = __fsqrt_rn(fs(fs(1.f, fm(q->u, q->u)), fm(q->v, q->v)));
+        angle = fa(fa(fm(p.u, q->u), fm(p.v, q->v)), fm(w1, w2));
+      }
+      bool black = ((x % res == 0) && (y % res == 0));
+      if (fabsf(angle) < 0.95f) black = (res == 1) ? !black : true;
+      out = black ? 0xff000000u : 0xffffffffu;
+    }
+  } else if (mode == 2 && !last_col) {
+    const j3dg_pixel r = G[pix + 1];
+    const j3dg_pixel u = *up;
+    if ((r.object_id != 0xffffffffu && r.object_id != p.object_id) ||
+        (u.object_id != 0xffffffffu && u.object_id != p.object_id)) {
+      const float scale = fm(fa(fm(p.u, p.u), fm(p.v, p.v)), 0.5f);
+      uint32_t c = (unsigned char)fm(255.f, scale);
+      out = 0xff000000u | (c << 16) | (c << 8) | c;
+    } else {
+      out = pixel_color(P, mark, p.r, p.g, p.b, p.u, p.v);
+    }
+  } else if (mode == 1 && !last_col) {
+    const j3dg_pixel r = G[pix + 1];
+    const j3dg_pixel u = *up;
+    if (differs(p, r)) {
+      float a = convex_cos_angle(P, (float)x, (float)y, p.u, p.v, p.depth, fa((float)x, 1.f), (float)y, r.u, r.v,
+                                 r.depth);
+      out = get_angle_color(a, P, p.u, p.v, mark);
+    } else if (differs(p, u)) {
+      float a = convex_cos_angle(P, (float)x, (float)y, p.u, p.v, p.depth, (float)x, fs((float)y, 1.f), u.u, u.v,
+                                 u.depth);
+      out = get_angle_color(a, P, p.u, p.v, mark);
+    } else {
+      out = pixel_color(P, mark, p.r, p.g, p.b, p.u, p.v);
+    }
+  } else {
+    out = pixel_color(P, mark, p.r, p.g, p.b, p.u, p.v);
+  }
+  P.im[pix] = out;
+}
+
+__global__ void k_copy_u32(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
+__global__ void k_clear_ids(j3dg_pixel* __restrict__ G, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    G[i].db_id = 0u;
+    G[i].object_id = 0xffffffffu;
+  }
+}
+
+__global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    // pixel() constructor (pixel.h:13) followed by canvas::resize (canvas.cpp:126-130)
+    uint4* q = reinterpret_cast<uint4*>(G + i);
+    q[0] = make_uint4(0u, 0u, 0u, 0u);
+    q[1] = make_uint4(0xffffffffu, 0u, 0u, 0u);
+  }
+}
+
+// ------------------------------------------------------- ray batches ----
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_rays(const DevInst* __restrict__ inst, uint32_t n_inst,
+                                              const j3dg_ray* __restrict__ rays, uint32_t n, j3dg_hit* __restrict__ hits,
+                                              uint32_t* status) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4* R = reinterpret_cast<const float4*>(rays + i);
+  // j3dg_ray is 40 bytes: only 8-byte aligned in general
+  const float* f = reinterpret_cast<const float*>(rays + i);
+  (void)R;
+  float ox = f[0], oy = f[1], oz = f[2], dx = f[4], dy = f[5], dz = f[6], tn = f[8], tf = f[9];
+  uint32_t visits = 0, tests = 0;
+  Best b;
+  find_closest<ANY>(inst, n_inst, ox, oy, oz, dx, dy, dz, tn, tf, b, status, visits, tests);
+  j3dg_hit h;
+  h.found = b.found ? 1u : 0u;
+  h.distance = b.found ? b.t : tf;
+  h.u = b.u;
+  h.v = b.v;
+  h.object_id = b.found ? b.tri : 0xffffffffu;
+  h.two_level_index = b.found ? b.inst : 0xffffffffu;
+  hits[i] = h;
+}
+
+// ------------------------------------------------------------ launchers ----
+
+cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
+  const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
+  if (rw <= 0 || rh <= 0) return cudaSuccess;
+  dim3 grid((rw + 15) / 16, (rh + 7) / 8);
+  k_render<<<grid, 128, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st) {
+  dim3 grid((P.w + 31) / 32, (P.h + 7) / 8);
+  k_shade<<<grid, 256, 0, st>>>(P, G, mode, fill_background);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_copy_u32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst, src, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_clear_ids<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_init_pixels<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(G, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
+                        bool any, uint32_t* status, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (any)
+    k_rays<true><<<(n + 127) / 128, 128, 0, st>>>(inst, n_inst, rays, n, hits, status);
+  else
+    k_rays<false><<<(n + 127) / 128, 128, 0, st>>>(inst, n_inst, rays, n, hits, status);
+  return cudaGetLastError();
+}
+
+}  // namespace j3dg

@@ -1,0 +1,41 @@
+// render.cuh -- launch parameters and launchers of the per-frame kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/j3dg.h"
+
+namespace j3dg {
+
+struct DevInst;
+
+struct FrameParams {
+  const DevInst* inst;
+  uint32_t n_inst;
+  uint32_t w, h;
+  int x0, y0, x1, y1;
+  float cs[16], cs_inv[16], pinv[16];
+  float pivot[3];
+  float diagonal;
+  float near_plane;
+  j3dg_pixel* gbuf;
+  uint32_t* im;
+  const uint32_t* background;
+  const uint32_t* matcap;
+  uint32_t mw, mh, cavity;
+  uint32_t shadow, textured, vertexcolors, shading;
+  int shade_mode;  // 0: G-buffer only; 1: also plain shading into im (misses <- background)
+  uint32_t* status;
+  unsigned long long* counters;  // optional [node visits, triangle tests]
+};
+
+cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
+// mode: 0 plain, 1 edges, 2 wireframe, 3 one-bit
+cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st);
+cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaStream_t st);
+cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st);
+cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st);
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
+                        bool any, uint32_t* status, cudaStream_t st);
+
+}  // namespace j3dg

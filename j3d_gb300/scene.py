@@ -1,0 +1,401 @@
+"""Host-side mirror of j3d's scene / canvas / camera / matcap API over the C-ABI.
+
+Same names, argument meaning and error behaviour as the reference's classes:
+  add_object (scene.cpp:8-38)        -> Scene.add_object (BVH built on the GPU)
+  prepare_scene / unzoom (scene.cpp:50-110)
+  canvas(w, h), resize, update_settings, set_background_color,
+  update_canvas, render_scene, canvas_to_image, get_pixels, get_image
+                                     (canvas.h:27-101)
+  view::render_scene (view.cpp:421-430) -> Canvas.render_frame
+Calls that the C-ABI rejects raise J3dgError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import (HIT_DTYPE, PIXEL_DTYPE, RAY_DTYPE, BuildOpts, Camera, CanvasSettings, Instance, J3dgError,
+                   MeshInfo, fptr, lib, vptr)
+
+IDENTITY = np.eye(4, dtype=np.float32).reshape(-1)  # column-major == row-major for identity
+
+
+def _check(ctx_handle, status: int) -> None:
+    if status != _ffi.J3DG_OK:
+        msg = lib().j3dg_last_error(ctx_handle) if ctx_handle else b""
+        raise J3dgError(status, (msg or b"").decode())
+
+
+class Context:
+    """One device, one CUDA stream (no reference counterpart)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib().j3dg_ctx_create(device, C.byref(h))
+        if st != _ffi.J3DG_OK:
+            raise J3dgError(st, f"j3dg_ctx_create(device={device})")
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self) -> None:
+        _check(self.h, lib().j3dg_ctx_synchronize(self.h))
+
+    def device_status(self) -> int:
+        s = C.c_uint32()
+        _check(self.h, lib().j3dg_ctx_device_status(self.h, C.byref(s)))
+        return s.value
+
+    def stream(self) -> int:
+        return lib().j3dg_ctx_stream(self.h) or 0
+
+    def set_counting(self, on: bool) -> None:
+        _check(self.h, lib().j3dg_ctx_set_counting(self.h, 1 if on else 0))
+
+    def read_counters(self, reset: bool = True) -> tuple[int, int]:
+        out = (C.c_uint64 * 2)()
+        _check(self.h, lib().j3dg_ctx_read_counters(self.h, out, 1 if reset else 0))
+        return int(out[0]), int(out[1])
+
+
+class Mesh:
+    """scene_object's mesh + qbvh (scene.h:10-25), resident on the device."""
+
+    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 4):
+        self.ctx = ctx
+        nv = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
+        nt = int(triangles.shape[0]) if triangles.ndim > 1 else int(triangles.size // 3)
+        h = C.c_void_p()
+        opts = BuildOpts(leaf_size, 0)
+        _check(ctx.h, lib().j3dg_mesh_build(ctx.h, vptr(vertices), nv, vptr(triangles), nt, C.byref(opts),
+                                            C.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> MeshInfo:
+        i = MeshInfo()
+        _check(self.ctx.h, lib().j3dg_mesh_get_info(self.h, C.byref(i)))
+        return i
+
+    def triangle_normals(self) -> np.ndarray:
+        i = self.info()
+        out = np.empty((i.n_triangles, 3), np.float32)
+        _check(self.ctx.h, lib().j3dg_mesh_get_triangle_normals(self.h, vptr(out)))
+        return out
+
+    def set_vertex_colors(self, colors) -> None:
+        _check(self.ctx.h, lib().j3dg_mesh_set_vertex_colors(self.h, vptr(colors)))
+
+    def set_uv(self, uv) -> None:
+        _check(self.ctx.h, lib().j3dg_mesh_set_uv(self.h, vptr(uv)))
+
+    def set_texture(self, tex: np.ndarray) -> None:
+        h, w = tex.shape
+        _check(self.ctx.h, lib().j3dg_mesh_set_texture(self.h, vptr(tex), w, h))
+
+
+class SceneObject:
+    def __init__(self, mesh: Mesh, cs=None, db_id: int = 1):
+        self.mesh = mesh
+        self.cs = np.ascontiguousarray(IDENTITY if cs is None else np.asarray(cs, np.float32).reshape(16))
+        self.db_id = db_id
+
+
+class Scene:
+    """scene (scene.h:40-51): objects, coordinate_system(+inv), pivot, bbox, diagonal."""
+
+    def __init__(self):
+        self.objects: list[SceneObject] = []
+        self.coordinate_system = IDENTITY.copy()
+        self.coordinate_system_inv = IDENTITY.copy()
+        self.pivot = np.zeros(3, np.float32)
+        self.min_bb = np.zeros(3, np.float32)
+        self.max_bb = np.zeros(3, np.float32)
+        self.diagonal = np.float32(0)
+
+    def add_object(self, mesh: Mesh, cs=None, db_id: int = 1) -> SceneObject:
+        # scene.cpp:8-38 (the BVH was built when the Mesh was made)
+        o = SceneObject(mesh, cs, db_id)
+        self.objects.append(o)
+        return o
+
+    def remove_object(self, db_id: int) -> None:
+        # scene.cpp:40-48
+        for i, o in enumerate(self.objects):
+            if o.db_id == db_id:
+                del self.objects[i]
+                return
+
+    def _instances(self):
+        arr = (Instance * max(1, len(self.objects)))()
+        for i, o in enumerate(self.objects):
+            arr[i].mesh = o.mesh.h
+            C.memmove(arr[i].cs, o.cs.ctypes.data, 64)
+            arr[i].db_id = o.db_id
+        return arr
+
+    def prepare_scene(self) -> None:
+        # scene.cpp:50-89
+        inst = self._instances()
+        mn = np.zeros(3, np.float32)
+        mx = np.zeros(3, np.float32)
+        d = np.zeros(1, np.float32)
+        ctx = self.objects[0].mesh.ctx.h if self.objects else None
+        _check(ctx, lib().j3dg_prepare_scene(inst, len(self.objects), fptr(mn), fptr(mx), fptr(d)))
+        self.min_bb, self.max_bb, self.diagonal = mn, mx, np.float32(d[0])
+
+    def unzoom(self) -> None:
+        # scene.cpp:91-110
+        cs = np.zeros(16, np.float32)
+        inv = np.zeros(16, np.float32)
+        piv = np.zeros(3, np.float32)
+        lib().j3dg_unzoom(fptr(self.min_bb), fptr(self.max_bb), float(self.diagonal), fptr(cs), fptr(inv),
+                          fptr(piv))
+        self.coordinate_system, self.coordinate_system_inv, self.pivot = cs, inv, piv
+
+    def set_pose(self, cs) -> None:
+        """Sets coordinate_system (camera to world) and its orthonormal inverse."""
+        self.coordinate_system = np.ascontiguousarray(np.asarray(cs, np.float32).reshape(16))
+        self.coordinate_system_inv = invert_orthonormal(self.coordinate_system)
+
+    def as_c(self):
+        """(j3dg_scene, keep-alive) for the C-ABI."""
+        inst = self._instances()
+        s = _ffi.Scene()
+        s.objects = C.cast(inst, C.POINTER(Instance))
+        s.n_objects = len(self.objects)
+        C.memmove(s.coordinate_system, self.coordinate_system.ctypes.data, 64)
+        C.memmove(s.coordinate_system_inv, self.coordinate_system_inv.ctypes.data, 64)
+        C.memmove(s.pivot, np.ascontiguousarray(self.pivot, np.float32).ctypes.data, 12)
+        s.diagonal = float(self.diagonal)
+        return s, inst
+
+
+class Matcap:
+    """matcap (matcap.h:18-24) uploaded to the device."""
+
+    def __init__(self, ctx: Context, pixels: np.ndarray, cavity_clr: int):
+        self.ctx = ctx
+        self.pixels = np.ascontiguousarray(pixels, np.uint32)
+        self.cavity_clr = int(cavity_clr)
+        h = C.c_void_p()
+        H, W = self.pixels.shape
+        _check(ctx.h, lib().j3dg_matcap_create(ctx.h, vptr(self.pixels), W, H, self.cavity_clr, C.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def make(ctx: Context, kind: int = 0) -> "Matcap":
+        px, cav = make_matcap(kind)
+        return Matcap(ctx, px, cav)
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_matcap_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def settings(one_bit=False, shadow=False, edges=True, wireframe=False, shading=True, textured=True,
+             vertexcolors=True) -> CanvasSettings:
+    """canvas_settings; defaults are j3d's (settings.cpp:5-25)."""
+    return CanvasSettings(int(one_bit), int(shadow), int(edges), int(wireframe), int(shading), int(textured),
+                          int(vertexcolors), 0)
+
+
+class Canvas:
+    """canvas (canvas.h:27-101) with device-resident G-buffer and image."""
+
+    def __init__(self, ctx: Context, w: int, h: int):
+        self.ctx = ctx
+        hh = C.c_void_p()
+        _check(ctx.h, lib().j3dg_canvas_create(ctx.h, w, h, C.byref(hh)))
+        self.h = hh
+        self.w, self.h_px = w, h
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_canvas_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def width(self) -> int:
+        return self.w
+
+    @property
+    def height(self) -> int:
+        return self.h_px
+
+    def resize(self, w: int, h: int) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_resize(self.h, w, h))
+        self.w, self.h_px = w, h
+
+    def set_camera(self, cam: Camera) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_set_camera(self.h, C.byref(cam)))
+
+    def get_projection(self) -> tuple[np.ndarray, np.ndarray]:
+        p = np.zeros(16, np.float32)
+        pi = np.zeros(16, np.float32)
+        _check(self.ctx.h, lib().j3dg_canvas_get_projection(self.h, fptr(p), fptr(pi)))
+        return p, pi
+
+    def set_background_color(self, clr_top: int = 0xff000000, clr_bottom: int = 0xff404040) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_set_background_color(self.h, clr_top, clr_bottom))
+
+    def update_settings(self, s: CanvasSettings) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_update_settings(self.h, C.byref(s)))
+
+    def update_canvas(self, x0: int, y0: int, x1: int, y1: int, scene: Scene) -> None:
+        s, keep = scene.as_c()
+        _check(self.ctx.h, lib().j3dg_canvas_update_canvas(self.h, x0, y0, x1, y1, C.byref(s)))
+        del keep
+
+    def render_scene(self, scene: Scene | None) -> None:
+        if scene is None:
+            _check(self.ctx.h, lib().j3dg_canvas_render_scene(self.h, None))
+            return
+        s, keep = scene.as_c()
+        _check(self.ctx.h, lib().j3dg_canvas_render_scene(self.h, C.byref(s)))
+        del keep
+
+    def canvas_to_image(self, matcap: Matcap, pixels=None) -> None:
+        if pixels is None:
+            _check(self.ctx.h, lib().j3dg_canvas_to_image(self.h, matcap.h))
+        else:
+            _check(self.ctx.h, lib().j3dg_canvas_to_image_from(self.h, vptr(pixels), matcap.h))
+
+    def render_frame(self, scene: Scene | None, matcap: Matcap) -> None:
+        """view::render_scene (view.cpp:421-430), asynchronous on the context stream."""
+        if scene is None:
+            _check(self.ctx.h, lib().j3dg_canvas_render_frame(self.h, None, matcap.h))
+            return
+        s, keep = scene.as_c()
+        _check(self.ctx.h, lib().j3dg_canvas_render_frame(self.h, C.byref(s), matcap.h))
+        del keep
+
+    def get_pixels(self, out=None):
+        if out is None:
+            out = np.empty((self.h_px, self.w), PIXEL_DTYPE)
+        _check(self.ctx.h, lib().j3dg_canvas_get_pixels(self.h, vptr(out)))
+        return out
+
+    def get_image(self, out=None):
+        if out is None:
+            out = np.empty((self.h_px, self.w), np.uint32)
+        _check(self.ctx.h, lib().j3dg_canvas_get_image(self.h, vptr(out)))
+        return out
+
+    def set_pixels(self, px) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_set_pixels(self.h, vptr(px)))
+
+    def device_buffers(self) -> tuple[int, int, int]:
+        a, b, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(self.ctx.h, lib().j3dg_canvas_device_buffers(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+
+# ------------------------------------------------------------- ray queries
+
+def _instances(objs: list[SceneObject]):
+    arr = (Instance * max(1, len(objs)))()
+    for i, o in enumerate(objs):
+        arr[i].mesh = o.mesh.h
+        C.memmove(arr[i].cs, o.cs.ctypes.data, 64)
+        arr[i].db_id = o.db_id
+    return arr
+
+
+def find_closest(ctx: Context, objs: list[SceneObject], rays, hits=None, any_hit: bool = False):
+    """qbvh_two_level_with_transformations::find_closest_triangle over a ray batch."""
+    n = len(rays)
+    if hits is None:
+        hits = np.empty(n, HIT_DTYPE)
+    inst = _instances(objs)
+    f = lib().j3dg_find_any if any_hit else lib().j3dg_find_closest
+    _check(ctx.h, f(ctx.h, inst, len(objs), vptr(rays), n, vptr(hits)))
+    return hits
+
+
+# --------------------------------------------------------- host j3d math
+
+def make_default_camera() -> Camera:
+    c = Camera()
+    lib().j3dg_make_default_camera(C.byref(c))
+    return c
+
+
+def make_projection_matrix(cam: Camera, w: int, h: int) -> np.ndarray:
+    out = np.zeros(16, np.float32)
+    lib().j3dg_make_projection_matrix(C.byref(cam), w, h, fptr(out))
+    return out
+
+
+def invert_projection_matrix(p: np.ndarray) -> np.ndarray:
+    out = np.zeros(16, np.float32)
+    lib().j3dg_invert_projection_matrix(fptr(np.ascontiguousarray(p, np.float32)), fptr(out))
+    return out
+
+
+def invert_orthonormal(m: np.ndarray) -> np.ndarray:
+    out = np.zeros(16, np.float32)
+    lib().j3dg_invert_orthonormal(fptr(np.ascontiguousarray(m, np.float32).reshape(16)), fptr(out))
+    return out
+
+
+def make_matcap(kind: int = 0) -> tuple[np.ndarray, int]:
+    px = np.zeros((512, 512), np.uint32)
+    w, h, cav = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    st = lib().j3dg_make_matcap(kind, vptr(px), C.byref(w), C.byref(h), C.byref(cav))
+    if st:
+        raise J3dgError(st, f"make_matcap({kind})")
+    return px, int(cav.value)
+
+
+def fill_background(w: int, h: int, top: int = 0xff000000, bottom: int = 0xff404040) -> np.ndarray:
+    bg = np.zeros((h, w), np.uint32)
+    lib().j3dg_fill_background(vptr(bg), w, h, top, bottom)
+    return bg
+
+
+def camera_for_vfov(vfov_deg: float) -> Camera:
+    """Default film-gate camera (camera.cpp:5-16) with the focal length giving vfov_deg."""
+    c = make_default_camera()
+    c.focal_length = lib().j3dg_focal_for_vfov(vfov_deg, c.film_aperture_height_inch)
+    return c
+
+
+__all__ = ["Context", "Mesh", "Scene", "SceneObject", "Matcap", "Canvas", "settings", "find_closest",
+           "make_default_camera", "make_projection_matrix", "invert_projection_matrix", "invert_orthonormal",
+           "make_matcap", "fill_background", "camera_for_vfov", "PIXEL_DTYPE", "RAY_DTYPE", "HIT_DTYPE",
+           "J3dgError"]

@@ -37,6 +37,7 @@ struct CtxExtra {
   cudaEvent_t slot_ev[kInstSlots];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   unsigned long long* d_counters = nullptr;
+  uint32_t* d_ray_counter = nullptr;  // work counter of ray-batch queries
   bool counting = false;
 };
 
@@ -221,6 +222,8 @@ void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevI
   P.vertexcolors = cv->settings.vertexcolors;
   P.shading = cv->settings.shading;
   P.status = cv->ctx->d_status;
+  P.work = cv->d_work;
+  P.queue = (float4*)cv->d_queue;
   CtxExtra& X = all(cv->ctx)->ex;
   P.counters = X.counting ? X.d_counters : nullptr;
 }
@@ -230,8 +233,10 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
   cudaFree(cv->d_pixels);
   cudaFree(cv->d_image);
   cudaFree(cv->d_background);
-  cv->d_pixels = nullptr;
-  cv->d_image = cv->d_background = nullptr;
+  cudaFree(cv->d_queue);
+  cudaFree(cv->d_work);
+  cv->d_pixels = cv->d_queue = nullptr;
+  cv->d_image = cv->d_background = cv->d_work = nullptr;
   cv->w = w;
   cv->h = h;
   size_t n = (size_t)w * h;
@@ -239,6 +244,8 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
     CK(c, cudaMalloc(&cv->d_pixels, sizeof(j3dg_pixel) * n), "canvas");
     CK(c, cudaMalloc((void**)&cv->d_image, sizeof(uint32_t) * n), "canvas");
     CK(c, cudaMalloc((void**)&cv->d_background, sizeof(uint32_t) * n), "canvas");
+    CK(c, cudaMalloc(&cv->d_queue, 2 * sizeof(float4) * n), "canvas");
+    CK(c, cudaMalloc((void**)&cv->d_work, 4 * sizeof(uint32_t)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_image, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_background, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, j3dg::launch_init_pixels((j3dg_pixel*)cv->d_pixels, n, S(c)), "canvas");
@@ -299,6 +306,7 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
   bool ok = cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_counters, 2 * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc((void**)&A->ex.d_ray_counter, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(A->ex.d_counters, 0, 2 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaEventCreate(&A->ex.ev0) == cudaSuccess && cudaEventCreate(&A->ex.ev1) == cudaSuccess;
   for (uint32_t i = 0; ok && i < kInstSlots; ++i) ok = cudaEventCreateWithFlags(&A->ex.slot_ev[i], cudaEventDisableTiming) == cudaSuccess;
@@ -324,6 +332,7 @@ int j3dg_ctx_destroy(j3dg_ctx* c) {
   cudaFree(c->d_status);
   cudaFree(c->d_inst);
   cudaFree(A->ex.d_counters);
+  cudaFree(A->ex.d_ray_counter);
   if (A->h_slots) cudaFreeHost(A->h_slots);
   for (uint32_t i = 0; i < kInstSlots; ++i)
     if (A->ex.slot_ev[i]) cudaEventDestroy(A->ex.slot_ev[i]);
@@ -517,7 +526,7 @@ static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, con
     CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "rays");
   }
   if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n, S(c)), "hits");
-  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, c->d_status, S(c)), "find");
+  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, S(c)), "find");
   if (!hits_dev) {
     CK(c, cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * (size_t)n, cudaMemcpyDeviceToHost, S(c)), "hits");
     cudaFreeAsync(dh, S(c));
@@ -593,6 +602,8 @@ int j3dg_canvas_destroy(j3dg_canvas* cv) {
   cudaFree(cv->d_pixels);
   cudaFree(cv->d_image);
   cudaFree(cv->d_background);
+  cudaFree(cv->d_queue);
+  cudaFree(cv->d_work);
   delete cv;
   return J3DG_OK;
 }

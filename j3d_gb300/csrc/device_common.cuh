@@ -168,117 +168,196 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
   return true;
 }
 
-// Traverses one object's BVH4 with an object-space ray. Returns true if ANY
-// and a triangle was accepted. Raises status bits on stack overflow or when
-// more nodes are visited than the BVH holds (a corrupt tree), and stops.
+// Resumable traversal of one world ray over all objects of the scene
+// (qbvh_two_level_with_transformations::find_closest_triangle): the ray is
+// taken to each object's space (origin as a point, direction as a vector) and
+// that object's BVH4 is walked with a per-thread stack. run() advances by at
+// most `iters` node or leaf steps, so persistent warps can refill lanes whose
+// rays have finished. Corrupt trees raise status bits instead of trapping.
 template <bool ANY>
-__device__ __forceinline__ bool traverse(const DevInst& I, const Ray& r, uint32_t inst, Best& b,
-                                         uint32_t* status, uint32_t& visits, uint32_t& tests) {
-  const float4* __restrict__ nodes = I.nodes;
+struct Tracer {
+  float wox, woy, woz, wdx, wdy, wdz;  // world ray
+  Ray r;                                // object-space ray of object `inst`
+  Best b;
+  const float4* nodes;
+  const float4* tris;
+  uint32_t n_nodes, nt;
+  uint32_t cur;
+  int sp;
+  uint32_t inst;
+  uint32_t budget;
   uint32_t stack_ref[J3DG_STACK];
   float stack_t[J3DG_STACK];
-  int sp = 0;
-  uint32_t cur = I.root_ref;
-  uint32_t budget = I.n_nodes + 1;
-  for (;;) {
-    if (cur != J3DG_EMPTY_REF) {
-      if (cur & J3DG_LEAF_BIT) {
-        uint32_t first = (cur & 0x7fffffffu) >> 3, cnt = (cur & 7u) + 1u;
-        if (first + cnt > I.nt) {
-          atomicOr(status, J3DG_DEV_BAD_INDEX);
-          return false;
+
+  __device__ __forceinline__ void start_object(const DevInst* __restrict__ insts) {
+    const DevInst& I = insts[inst];
+    float4 o = mat_vec(I.inv, wox, woy, woz, 1.f);
+    float4 d = mat_vec(I.inv, wdx, wdy, wdz, 0.f);
+    r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, r.t_near, I.scale);
+    nodes = I.nodes;
+    tris = I.tris;
+    n_nodes = I.n_nodes;
+    nt = I.nt;
+    cur = I.root_ref;
+    sp = 0;
+    budget = n_nodes + 1;
+  }
+
+  // Returns true if the ray is already finished (no objects).
+  __device__ __forceinline__ bool begin(const DevInst* __restrict__ insts, uint32_t n_inst, float ox, float oy,
+                                        float oz, float dx, float dy, float dz, float t_near, float t_far) {
+    wox = ox;
+    woy = oy;
+    woz = oz;
+    wdx = dx;
+    wdy = dy;
+    wdz = dz;
+    r.t_near = t_near;
+    b.t = t_far;
+    b.found = false;
+    b.inst = b.tri = 0;
+    b.u = b.v = 0.f;
+    b.slot = 0;
+    inst = 0;
+    if (n_inst == 0) return true;
+    start_object(insts);
+    return false;
+  }
+
+  __device__ __forceinline__ bool run(const DevInst* __restrict__ insts, uint32_t n_inst, int iters,
+                                      uint32_t* status, uint32_t& visits, uint32_t& tests) {
+#pragma unroll 1
+    for (int it = 0; it < iters; ++it) {
+      if (cur == J3DG_EMPTY_REF) {
+        bool got = false;
+        while (sp > 0) {
+          --sp;
+          if (stack_t[sp] <= b.t) {
+            cur = stack_ref[sp];
+            got = true;
+            break;
+          }
         }
+        if (!got) {
+          if (++inst >= n_inst) return true;
+          start_object(insts);
+          continue;
+        }
+      }
+      if (cur & J3DG_LEAF_BIT) {
+        const uint32_t first = (cur & 0x7fffffffu) >> 3, cnt = (cur & 7u) + 1u;
+        if (first + cnt > nt) {
+          atomicOr(status, J3DG_DEV_BAD_INDEX);
+          return true;
+        }
+#pragma unroll 1
         for (uint32_t k = 0; k < cnt; ++k) {
           ++tests;
-          if (tri_test<ANY>(r, I.tris, first + k, inst, b) && ANY) return true;
+          if (tri_test<ANY>(r, tris, first + k, inst, b) && ANY) return true;
         }
         cur = J3DG_EMPTY_REF;
-      } else {
-        if (budget-- == 0) {
-          atomicOr(status, J3DG_DEV_VISIT_CAP);
-          return false;
-        }
-        if (cur >= I.n_nodes) {
-          atomicOr(status, J3DG_DEV_BAD_INDEX);
-          return false;
-        }
-        ++visits;
-        const float4* N = nodes + 8 * (size_t)cur;
-        const float4 lox = __ldg(N + 0), hix = __ldg(N + 1), loy = __ldg(N + 2), hiy = __ldg(N + 3);
-        const float4 loz = __ldg(N + 4), hiz = __ldg(N + 5);
-        const uint4 ch = *reinterpret_cast<const uint4*>(&N[6]);
-        float tc[4];
-        uint32_t rc[4] = {ch.x, ch.y, ch.z, ch.w};
-        const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-        const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-        const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          float tn, tf;
-          slab(r, lx[c], ly[c], lz[c], hx[c], hy[c], hz[c], tn, tf);
-          float a = fmaxf(tn, r.t_near), e = fminf(tf, b.t);
-          bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
-          tc[c] = hit ? a : __int_as_float(0x7f800000);
-          if (!hit) rc[c] = J3DG_EMPTY_REF;
-        }
-        // sort the four (t, ref) pairs ascending (5 compare-exchanges)
-#define J3DG_CX(i, j)                    \
-  if (tc[j] < tc[i]) {                   \
-    float tt = tc[i];                    \
-    tc[i] = tc[j];                       \
-    tc[j] = tt;                          \
-    uint32_t rr = rc[i];                 \
-    rc[i] = rc[j];                       \
-    rc[j] = rr;                          \
-  }
-        J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(1, 2)
-#undef J3DG_CX
-        if (sp + 3 > J3DG_STACK) {
-          atomicOr(status, J3DG_DEV_STACK_OVERFLOW);
-          return false;
-        }
-#pragma unroll
-        for (int c = 3; c >= 1; --c)
-          if (rc[c] != J3DG_EMPTY_REF) {
-            stack_ref[sp] = rc[c];
-            stack_t[sp] = tc[c];
-            ++sp;
-          }
-        cur = rc[0];
         continue;
       }
+      if (budget-- == 0) {
+        atomicOr(status, J3DG_DEV_VISIT_CAP);
+        return true;
+      }
+      if (cur >= n_nodes) {
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+        return true;
+      }
+      ++visits;
+      const float4* N = nodes + 8 * (size_t)cur;
+      const float4 lox = __ldg(N + 0), hix = __ldg(N + 1), loy = __ldg(N + 2), hiy = __ldg(N + 3);
+      const float4 loz = __ldg(N + 4), hiz = __ldg(N + 5);
+      const float4 chf = __ldg(N + 6);
+      float tc[4];
+      uint32_t rc[4] = {__float_as_uint(chf.x), __float_as_uint(chf.y), __float_as_uint(chf.z),
+                        __float_as_uint(chf.w)};
+      const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+      const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+      const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float tn, tf;
+        slab(r, lx[c], ly[c], lz[c], hx[c], hy[c], hz[c], tn, tf);
+        float a = fmaxf(tn, r.t_near), e = fminf(tf, b.t);
+        bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
+        tc[c] = hit ? a : __int_as_float(0x7f800000);
+        if (!hit) rc[c] = J3DG_EMPTY_REF;
+      }
+      // ascending (t, ref): 5 compare-exchanges
+#define J3DG_CX(i, j)  \
+  if (tc[j] < tc[i]) { \
+    float tt = tc[i];  \
+    tc[i] = tc[j];     \
+    tc[j] = tt;        \
+    uint32_t rr = rc[i]; \
+    rc[i] = rc[j];     \
+    rc[j] = rr;        \
+  }
+      J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(1, 2)
+#undef J3DG_CX
+      if (sp + 3 > J3DG_STACK) {
+        atomicOr(status, J3DG_DEV_STACK_OVERFLOW);
+        return true;
+      }
+#pragma unroll
+      for (int c = 3; c >= 1; --c)
+        if (rc[c] != J3DG_EMPTY_REF) {
+          stack_ref[sp] = rc[c];
+          stack_t[sp] = tc[c];
+          ++sp;
+        }
+      cur = rc[0];
     }
-    // pop the nearest entry that can still hold a better hit
-    bool got = false;
-    while (sp > 0) {
-      --sp;
-      if (stack_t[sp] <= b.t) {
-        cur = stack_ref[sp];
-        got = true;
-        break;
+    return false;
+  }
+};
+
+// Persistent warps with per-lane refill (Aila and Laine 2009, "dynamic
+// fetch"): every lane whose ray finished takes the next work item; the warp
+// fetches for all such lanes with one atomic. Src supplies count(), begin()
+// (returns false when the item needs no tracing and was handled) and
+// finish(); ITERS node/leaf steps run between refills.
+template <bool ANY, int ITERS, class Src>
+__device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __restrict__ insts, uint32_t n_inst,
+                                                 uint32_t* counter, uint32_t* status,
+                                                 unsigned long long* counters) {
+  Tracer<ANY> T;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t n = src.count();
+  int64_t idx = -1;
+  bool exhausted = false;
+  uint32_t visits = 0, tests = 0;
+#pragma unroll 1
+  for (;;) {
+    const bool need = idx < 0 && !exhausted;
+    const uint32_t m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t my = base + __popc(m & ((1u << lane) - 1u));
+        if (my < n) {
+          idx = my;
+          if (!src.begin(T, insts, n_inst, my)) idx = -1;  // handled without tracing
+        } else {
+          exhausted = true;
+        }
       }
     }
-    if (!got) return false;
+    if (__all_sync(0xffffffffu, idx < 0 && exhausted)) break;
+    if (idx >= 0 && T.run(insts, n_inst, ITERS, status, visits, tests)) {
+      src.finish(T, (uint32_t)idx);
+      idx = -1;
+    }
   }
-}
-
-// qbvh_two_level_with_transformations::find_closest_triangle over all
-// objects: the world ray goes to each object's space as a point and a vector.
-template <bool ANY>
-__device__ __forceinline__ void find_closest(const DevInst* __restrict__ inst, uint32_t n_inst, float ox, float oy,
-                                             float oz, float dx, float dy, float dz, float t_near, float t_far,
-                                             Best& b, uint32_t* status, uint32_t& visits, uint32_t& tests) {
-  b.t = t_far;
-  b.found = false;
-  b.inst = b.tri = 0;
-  b.u = b.v = 0.f;
-  b.slot = 0;
-  for (uint32_t i = 0; i < n_inst; ++i) {
-    const DevInst& I = inst[i];
-    float4 o = mat_vec(I.inv, ox, oy, oz, 1.f);
-    float4 d = mat_vec(I.inv, dx, dy, dz, 0.f);
-    Ray r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, t_near, I.scale);
-    if (traverse<ANY>(I, r, i, b, status, visits, tests) && ANY) return;
+  if (counters) {
+    atomicAdd(counters + 0, (unsigned long long)visits);
+    atomicAdd(counters + 1, (unsigned long long)tests);
   }
 }
 

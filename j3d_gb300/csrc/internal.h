@@ -62,4 +62,6 @@ struct j3dg_canvas {
   void* d_pixels = nullptr;      // j3dg_pixel[w*h]
   uint32_t* d_image = nullptr;   // w*h
   uint32_t* d_background = nullptr;
+  void* d_queue = nullptr;       // shadow-ray jobs, 2 float4 per pixel
+  uint32_t* d_work = nullptr;    // per-frame work counters
 };

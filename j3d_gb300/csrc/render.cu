@@ -1,10 +1,13 @@
-// render.cu -- per-frame kernels: the fused ray-cast frame (primary ray,
-// closest hit, G-buffer record, shadow ray, plain matcap shading), the
+// render.cu -- per-frame kernels: the ray-cast frame (primary rays, closest
+// hit, G-buffer record, shadow rays, plain matcap shading), the
 // neighbour-reading shading modes, and batched ray queries.
 //
-// k_render replaces the per-pixel body of canvas::update_canvas
-// (canvas.cpp:765-873) and, in plain mode, canvas_to_image (canvas.cpp:650-669)
-// plus the background copy of canvas::render_scene (canvas.cpp:893-898).
+// A frame is two persistent kernels. k_primary replaces the per-pixel body of
+// canvas::update_canvas (canvas.cpp:765-834) and, in plain mode, the
+// background copy of canvas::render_scene (canvas.cpp:893-898) and the
+// colour of shadow-free pixels; hit pixels that need a shadow ray append a
+// job to a compacted queue. k_shadow traces the queue (canvas.cpp:836-857)
+// and writes those pixels' colour (canvas_to_image plain, canvas.cpp:650-669).
 // k_shade replaces canvas_to_image's edges, wireframe and one-bit modes
 // (canvas.cpp:449-649), which read the right and upper neighbours.
 #include <cuda_runtime.h>
@@ -88,41 +91,64 @@ __device__ __forceinline__ uint32_t pixel_color(const FrameParams& P, uint32_t m
 
 // ------------------------------------------------------------- render ----
 
-__global__ void __launch_bounds__(128) k_render(const FrameParams P) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int x = P.x0 + (int)blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-  const int y = P.y0 + (int)blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
-  if (x > P.x1 || y > P.y1) return;
-  const size_t pix = (size_t)y * P.w + x;
+// Pixel of work item `idx`: 8x4 tiles in row-major tile order over the
+// rectangle, so the 32 rays of a warp's refill come from one tile.
+__device__ __forceinline__ bool item_pixel(const FrameParams& P, uint32_t idx, int& x, int& y) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1);
+  const uint32_t tiles_x = (rw + 7u) >> 3;
+  const uint32_t tile = idx >> 5, within = idx & 31u;
+  x = P.x0 + (int)((tile % tiles_x) * 8u + (within & 7u));
+  y = P.y0 + (int)((tile / tiles_x) * 4u + (within >> 3));
+  return x <= P.x1 && y <= P.y1;
+}
+
+__device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
+  // canvas.cpp:859-866 (other fields keep their previous values)
   j3dg_pixel* rec = P.gbuf + pix;
-  uint32_t visits = 0, tests = 0;
-  if (P.n_inst == 0) {
-    // canvas.cpp:744-759: no objects, every pixel a miss
-    rec->db_id = 0u;
-    rec->object_id = 0xffffffffu;
-    rec->u = 0.f;
-    rec->v = 0.f;
-    rec->depth = FLT_MAX;
-    if (P.shade_mode == 1) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
-    return;
+  rec->db_id = 0u;
+  rec->object_id = 0xffffffffu;
+  rec->u = 0.f;
+  rec->v = 0.f;
+  rec->depth = FLT_MAX;
+  if (P.shade_mode == 1) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
+}
+
+// Primary rays (canvas.cpp:765-834): G-buffer record, texture / vertex colour,
+// then either the colour (no shadow) or a compacted shadow-ray job.
+struct PrimarySrc {
+  const FrameParams& P;
+  __device__ __forceinline__ uint32_t count() const {
+    const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+    return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
   }
-  // canvas.cpp:700-705
-  const float4 origin = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
-  const float ld = fm(P.diagonal, 3.f);
-  const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
-  // canvas.cpp:773-782
-  const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
-  const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
-  float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
-  d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
-  const float t_near = __fdiv_rn(P.diagonal, 100.f);
-  Best b;
-  find_closest<false>(P.inst, P.n_inst, origin.x, origin.y, origin.z, d.x, d.y, d.z, t_near, FLT_MAX, b, P.status,
-                      visits, tests);
-  uint32_t color = 0;
-  if (b.found) {
-    // canvas.cpp:788-801
+  __device__ __forceinline__ bool begin(Tracer<false>& T, const DevInst* insts, uint32_t n_inst, uint32_t idx) {
+    int x, y;
+    if (!item_pixel(P, idx, x, y)) return false;
+    if (n_inst == 0) {
+      write_miss(P, (size_t)y * P.w + x);
+      return false;
+    }
+    // canvas.cpp:700-701, 773-782
+    const float4 o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
+    const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
+    const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
+    float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
+    d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
+    T.begin(insts, n_inst, o.x, o.y, o.z, d.x, d.y, d.z, __fdiv_rn(P.diagonal, 100.f), FLT_MAX);
+    return true;
+  }
+  __device__ __forceinline__ void finish(Tracer<false>& T, uint32_t idx) {
+    int x, y;
+    item_pixel(P, idx, x, y);
+    const size_t pix = (size_t)y * P.w + x;
+    const Best& b = T.b;
+    if (!b.found) {
+      write_miss(P, pix);
+      return;
+    }
+    j3dg_pixel* rec = P.gbuf + pix;
     const DevInst& I = P.inst[b.inst];
+    // canvas.cpp:788-801
     const float4 N = __ldg(I.normals + b.tri);
     float4 n = mat_vec(P.cs_inv, N.x, N.y, N.z, 0.f);
     n = mat_vec(I.cs, n.x, n.y, n.z, n.w);
@@ -148,10 +174,10 @@ __global__ void __launch_bounds__(128) k_render(const FrameParams P) {
       rgb = true;
     } else if (P.vertexcolors && I.colors != nullptr) {
       // canvas.cpp:821-834
-      const uint32_t* T = I.index + 3 * (size_t)b.tri;
-      const float* C0 = I.colors + 3 * (size_t)T[0];
-      const float* C1 = I.colors + 3 * (size_t)T[1];
-      const float* C2 = I.colors + 3 * (size_t)T[2];
+      const uint32_t* Ti = I.index + 3 * (size_t)b.tri;
+      const float* C0 = I.colors + 3 * (size_t)Ti[0];
+      const float* C1 = I.colors + 3 * (size_t)Ti[1];
+      const float* C2 = I.colors + 3 * (size_t)Ti[2];
       float c[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u, C1[k])), fm(b.v, C2[k]));
@@ -161,8 +187,18 @@ __global__ void __launch_bounds__(128) k_render(const FrameParams P) {
       mark |= 2u;
       rgb = true;
     }
+    if (rgb)
+      reinterpret_cast<uint32_t*>(rec)[0] = mark | (pr << 8) | (pg << 16) | (pb << 24);
+    else
+      reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
+    rec->u = n.x;
+    rec->v = n.y;
+    rec->depth = b.t;
+    *reinterpret_cast<uint4*>(&rec->object_id) = make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
     if (P.shadow) {
-      // canvas.cpp:836-857: shadow ray from the hit point towards the light
+      // canvas.cpp:836-853: the shadow ray starts at the hit point, towards the light
+      const float ld = fm(P.diagonal, 3.f);
+      const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
       const float4 A = __ldg(I.tris + 3 * (size_t)b.slot);
       const float4 B = __ldg(I.tris + 3 * (size_t)b.slot + 1);
       const float4 C = __ldg(I.tris + 3 * (size_t)b.slot + 2);
@@ -172,36 +208,103 @@ __global__ void __launch_bounds__(128) k_render(const FrameParams P) {
       const float px = fa(fa(fm(V0.x, wgt), fm(b.u, V1.x)), fm(b.v, V2.x));
       const float py = fa(fa(fm(V0.y, wgt), fm(b.u, V1.y)), fm(b.v, V2.y));
       const float pz = fa(fa(fm(V0.z, wgt), fm(b.u, V1.z)), fm(b.v, V2.z));
-      Best b2;
-      find_closest<true>(P.inst, P.n_inst, px, py, pz, fs(light.x, px), fs(light.y, py), fs(light.z, pz), 1e-3f,
-                         FLT_MAX, b2, P.status, visits, tests);
-      if (b2.found) mark |= 1u;
+      // warp-aggregated append to the shadow queue
+      const uint32_t m = __activemask();
+      const int leader = __ffs(m) - 1;
+      const uint32_t lane = threadIdx.x & 31u;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(P.work + 1, (uint32_t)__popc(m));
+      base = __shfl_sync(m, base, leader);
+      const uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
+      P.queue[2 * (size_t)slot] = make_float4(px, py, pz, __uint_as_float((uint32_t)pix));
+      P.queue[2 * (size_t)slot + 1] = make_float4(fs(light.x, px), fs(light.y, py), fs(light.z, pz), 0.f);
+    } else if (P.shade_mode == 1) {
+      P.im[pix] = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
     }
-    if (rgb) {
-      reinterpret_cast<uint32_t*>(rec)[0] = mark | (pr << 8) | (pg << 16) | (pb << 24);
-    } else {
+  }
+};
+
+// Shadow rays from the compacted queue (canvas.cpp:848-857): any hit marks
+// the pixel; in plain mode the pixel's colour is written here.
+struct ShadowSrc {
+  const FrameParams& P;
+  __device__ __forceinline__ uint32_t count() const { return *(volatile const uint32_t*)(P.work + 1); }
+  __device__ __forceinline__ bool begin(Tracer<true>& T, const DevInst* insts, uint32_t n_inst, uint32_t idx) {
+    const float4 a = P.queue[2 * (size_t)idx], d = P.queue[2 * (size_t)idx + 1];
+    T.begin(insts, n_inst, a.x, a.y, a.z, d.x, d.y, d.z, 1e-3f, FLT_MAX);
+    return true;
+  }
+  __device__ __forceinline__ void finish(Tracer<true>& T, uint32_t idx) {
+    const size_t pix = __float_as_uint(P.queue[2 * (size_t)idx].w);
+    j3dg_pixel* rec = P.gbuf + pix;
+    const uint32_t w0 = reinterpret_cast<const uint32_t*>(rec)[0];
+    uint32_t mark = w0 & 0xffu;
+    if (T.b.found) {
+      mark |= 1u;
       reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
     }
-    rec->u = n.x;
-    rec->v = n.y;
-    rec->depth = b.t;
-    *reinterpret_cast<uint4*>(&rec->object_id) =
-        make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
-    if (P.shade_mode == 1) color = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
-  } else {
-    // canvas.cpp:859-866
-    rec->db_id = 0u;
-    rec->object_id = 0xffffffffu;
-    rec->u = 0.f;
-    rec->v = 0.f;
-    rec->depth = FLT_MAX;
-    if (P.shade_mode == 1) color = P.background ? __ldg(P.background + pix) : P.im[pix];
+    if (P.shade_mode == 1)
+      P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, rec->u, rec->v);
   }
-  if (P.shade_mode == 1) P.im[pix] = color;
-  if (P.counters) {
-    atomicAdd(P.counters + 0, (unsigned long long)visits);
-    atomicAdd(P.counters + 1, (unsigned long long)tests);
+};
+
+static const int kTraceThreads = 128;
+static const int kIters = 16;
+
+__global__ void __launch_bounds__(kTraceThreads) k_primary(const FrameParams P) {
+  PrimarySrc src{P};
+  persistent_trace<false, kIters>(src, P.inst, P.n_inst, P.work + 0, P.status, P.counters);
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_shadow(const FrameParams P) {
+  ShadowSrc src{P};
+  persistent_trace<true, kIters>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
+}
+
+// j3dg_ray batches (find_closest / find_any through the C-ABI)
+template <bool ANY>
+struct BatchSrc {
+  const j3dg_ray* rays;
+  j3dg_hit* hits;
+  uint32_t n;
+  __device__ __forceinline__ uint32_t count() const { return n; }
+  __device__ __forceinline__ bool begin(Tracer<ANY>& T, const DevInst* insts, uint32_t n_inst, uint32_t i) {
+    const float* f = reinterpret_cast<const float*>(rays + i);  // 40-byte records: 4-byte loads
+    if (T.begin(insts, n_inst, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9])) {
+      finish(T, i);
+      return false;
+    }
+    return true;
   }
+  __device__ __forceinline__ void finish(Tracer<ANY>& T, uint32_t i) {
+    const float t_far = reinterpret_cast<const float*>(rays + i)[9];
+    j3dg_hit h;
+    h.found = T.b.found ? 1u : 0u;
+    h.distance = T.b.found ? T.b.t : t_far;
+    h.u = T.b.u;
+    h.v = T.b.v;
+    h.object_id = T.b.found ? T.b.tri : 0xffffffffu;
+    h.two_level_index = T.b.found ? T.b.inst : 0xffffffffu;
+    hits[i] = h;
+  }
+};
+
+template <bool ANY>
+__global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restrict__ inst, uint32_t n_inst,
+                                                        const j3dg_ray* __restrict__ rays, uint32_t n,
+                                                        j3dg_hit* __restrict__ hits, uint32_t* counter,
+                                                        uint32_t* status) {
+  BatchSrc<ANY> src{rays, hits, n};
+  persistent_trace<ANY, kIters>(src, inst, n_inst, counter, status, nullptr);
+}
+
+template <class K>
+static int persistent_blocks(K* kernel) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kTraceThreads, 0);
+  return sms * (per > 0 ? per : 1);
 }
 
 // ----------------------------------------------------------- k_shade ----
@@ -334,39 +437,20 @@ __global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
   }
 }
 
-// ------------------------------------------------------- ray batches ----
-
-template <bool ANY>
-__global__ void __launch_bounds__(128) k_rays(const DevInst* __restrict__ inst, uint32_t n_inst,
-                                              const j3dg_ray* __restrict__ rays, uint32_t n, j3dg_hit* __restrict__ hits,
-                                              uint32_t* status) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4* R = reinterpret_cast<const float4*>(rays + i);
-  // j3dg_ray is 40 bytes: only 8-byte aligned in general
-  const float* f = reinterpret_cast<const float*>(rays + i);
-  (void)R;
-  float ox = f[0], oy = f[1], oz = f[2], dx = f[4], dy = f[5], dz = f[6], tn = f[8], tf = f[9];
-  uint32_t visits = 0, tests = 0;
-  Best b;
-  find_closest<ANY>(inst, n_inst, ox, oy, oz, dx, dy, dz, tn, tf, b, status, visits, tests);
-  j3dg_hit h;
-  h.found = b.found ? 1u : 0u;
-  h.distance = b.found ? b.t : tf;
-  h.u = b.u;
-  h.v = b.v;
-  h.object_id = b.found ? b.tri : 0xffffffffu;
-  h.two_level_index = b.found ? b.inst : 0xffffffffu;
-  hits[i] = h;
-}
-
 // ------------------------------------------------------------ launchers ----
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
   if (rw <= 0 || rh <= 0) return cudaSuccess;
-  dim3 grid((rw + 15) / 16, (rh + 7) / 8);
-  k_render<<<grid, 128, 0, st>>>(P);
+  static int blocks_p = 0, blocks_s = 0;
+  if (!blocks_p) {
+    blocks_p = persistent_blocks(k_primary);
+    blocks_s = persistent_blocks(k_shadow);
+  }
+  cudaError_t e = cudaMemsetAsync(P.work, 0, 4 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  k_primary<<<blocks_p, kTraceThreads, 0, st>>>(P);
+  if (P.shadow && P.n_inst > 0) k_shadow<<<blocks_s, kTraceThreads, 0, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -395,12 +479,19 @@ cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st) {
 }
 
 cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* status, cudaStream_t st) {
+                        bool any, uint32_t* counter, uint32_t* status, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  static int blocks_c = 0, blocks_a = 0;
+  if (!blocks_c) {
+    blocks_c = persistent_blocks(k_rays<false>);
+    blocks_a = persistent_blocks(k_rays<true>);
+  }
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
   if (any)
-    k_rays<true><<<(n + 127) / 128, 128, 0, st>>>(inst, n_inst, rays, n, hits, status);
+    k_rays<true><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status);
   else
-    k_rays<false><<<(n + 127) / 128, 128, 0, st>>>(inst, n_inst, rays, n, hits, status);
+    k_rays<false><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status);
   return cudaGetLastError();
 }
 

@@ -25,6 +25,8 @@ struct FrameParams {
   uint32_t mw, mh, cavity;
   uint32_t shadow, textured, vertexcolors, shading;
   int shade_mode;  // 0: G-buffer only; 1: also plain shading into im (misses <- background)
+  uint32_t* work;   // [0] primary items taken, [1] shadow jobs queued, [2] shadow items taken
+  float4* queue;    // shadow jobs: (origin, pixel index bits), (direction, 0); w*h entries
   uint32_t* status;
   unsigned long long* counters;  // optional [node visits, triangle tests]
 };
@@ -36,6 +38,6 @@ cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaSt
 cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* status, cudaStream_t st);
+                        bool any, uint32_t* counter, uint32_t* status, cudaStream_t st);
 
 }  // namespace j3dg

@@ -253,13 +253,12 @@ def run_own(args):
     e1.synchronize()
     ctx.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    from j3d_gb300.multi import reduce_timing
     if ws > 1:
         torch.distributed.barrier()
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    clk = clocks.stop()
-    value = rays_per_step * ws / (ms / 1e3) / 1e6
+    ms, total_rays = reduce_timing(ms, rays_per_step)
+    value = total_rays / (ms / 1e3) / 1e6
 
     # per-frame kernel time (one k_render launch per frame in plain mode)
     fe0 = [torch.cuda.Event(enable_timing=True) for _ in wl.poses]
@@ -336,13 +335,13 @@ def run_own(args):
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "k_render", "peak_kind": peak_kind,
+                     "kernel": "frame = k_primary + k_shadow (timed together per frame)", "peak_kind": peak_kind,
                      "bytes_per_ray": round(alg_bytes / rays_per_step, 1),
                      "node_visits_per_ray": round(node_per_ray, 3), "tri_tests_per_ray": round(tri_per_ray, 3),
                      "per_ray_model": "36 B per primary ray + node_visits*128 B + tri_tests*48 B (oracle BVH4 SAH)"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": N_CAMERAS * args.steps,
+        "gpu_launches": 2 * N_CAMERAS * args.steps,  # k_primary + k_shadow per frame
         "clocks": clk,
     }
     if cpu:

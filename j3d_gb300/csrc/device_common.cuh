@@ -122,11 +122,10 @@ __device__ __forceinline__ bool key_less(uint32_t ia, uint32_t ta, uint32_t ib, 
   return ia < ib || (ia == ib && ta < tb);
 }
 
-// Moller-Trumbore + gate for triangle `slot`. ANY: the caller stops at the
+// Moller-Trumbore + gate for triangle `slot`. any: the caller stops at the
 // first accept, so the (t, key) comparison only needs t < t_best.
-template <bool ANY>
 __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict__ tris, uint32_t slot, uint32_t inst,
-                                         Best& b) {
+                                         Best& b, bool any) {
   const float4 a = __ldg(tris + 3 * (size_t)slot);
   const float4 c1 = __ldg(tris + 3 * (size_t)slot + 1);
   const float4 c2 = __ldg(tris + 3 * (size_t)slot + 2);
@@ -148,11 +147,7 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
   if (!(u >= 0.f && v >= 0.f && fa(u, v) <= 1.f)) return false;
   if (!(t > r.t_near)) return false;
   uint32_t id = __float_as_uint(a.w);
-  if (ANY) {
-    if (!(t < b.t)) return false;
-  } else {
-    if (!(t < b.t || (t == b.t && b.found && key_less(inst, id, b.inst, b.tri)))) return false;
-  }
+  if (!(t < b.t || (!any && t == b.t && b.found && key_less(inst, id, b.inst, b.tri)))) return false;
   // bounds gate: t inside the slab interval of the triangle's own box
   float tn, tf;
   slab(r, fminf(fminf(a.x, c1.x), c2.x), fminf(fminf(a.y, c1.y), c2.y), fminf(fminf(a.z, c1.z), c2.z),
@@ -174,9 +169,9 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
 // that object's BVH4 is walked with a per-thread stack. run() advances by at
 // most `iters` node or leaf steps, so persistent warps can refill lanes whose
 // rays have finished. Corrupt trees raise status bits instead of trapping.
-template <bool ANY>
 struct Tracer {
   float wox, woy, woz, wdx, wdy, wdz;  // world ray
+  bool any;                             // stop at the first accepted triangle
   Ray r;                                // object-space ray of object `inst`
   Best b;
   const float4* nodes;
@@ -186,8 +181,6 @@ struct Tracer {
   int sp;
   uint32_t inst;
   uint32_t budget;
-  uint32_t stack_ref[J3DG_STACK];
-  float stack_t[J3DG_STACK];
 
   __device__ __forceinline__ void start_object(const DevInst* __restrict__ insts) {
     const DevInst& I = insts[inst];
@@ -205,7 +198,9 @@ struct Tracer {
 
   // Returns true if the ray is already finished (no objects).
   __device__ __forceinline__ bool begin(const DevInst* __restrict__ insts, uint32_t n_inst, float ox, float oy,
-                                        float oz, float dx, float dy, float dz, float t_near, float t_far) {
+                                        float oz, float dx, float dy, float dz, float t_near, float t_far,
+                                        bool any_hit) {
+    any = any_hit;
     wox = ox;
     woy = oy;
     woz = oz;
@@ -224,8 +219,11 @@ struct Tracer {
     return false;
   }
 
+  // stack_ref / stack_t: the caller's per-thread traversal stack (kept out
+  // of the struct so that its scalar state can stay in registers)
   __device__ __forceinline__ bool run(const DevInst* __restrict__ insts, uint32_t n_inst, int iters,
-                                      uint32_t* status, uint32_t& visits, uint32_t& tests) {
+                                      uint32_t* status, uint32_t& visits, uint32_t& tests,
+                                      uint32_t* __restrict__ stack_ref, float* __restrict__ stack_t) {
 #pragma unroll 1
     for (int it = 0; it < iters; ++it) {
       if (cur == J3DG_EMPTY_REF) {
@@ -253,7 +251,7 @@ struct Tracer {
 #pragma unroll 1
         for (uint32_t k = 0; k < cnt; ++k) {
           ++tests;
-          if (tri_test<ANY>(r, tris, first + k, inst, b) && ANY) return true;
+          if (tri_test(r, tris, first + k, inst, b, any) && any) return true;
         }
         cur = J3DG_EMPTY_REF;
         continue;
@@ -320,11 +318,13 @@ struct Tracer {
 // fetches for all such lanes with one atomic. Src supplies count(), begin()
 // (returns false when the item needs no tracing and was handled) and
 // finish(); ITERS node/leaf steps run between refills.
-template <bool ANY, int ITERS, class Src>
+template <int ITERS, class Src>
 __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __restrict__ insts, uint32_t n_inst,
                                                  uint32_t* counter, uint32_t* status,
                                                  unsigned long long* counters) {
-  Tracer<ANY> T;
+  Tracer T;
+  uint32_t stack_ref[J3DG_STACK];
+  float stack_t[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = src.count();
   int64_t idx = -1;
@@ -350,7 +350,7 @@ __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __rest
       }
     }
     if (__all_sync(0xffffffffu, idx < 0 && exhausted)) break;
-    if (idx >= 0 && T.run(insts, n_inst, ITERS, status, visits, tests)) {
+    if (idx >= 0 && T.run(insts, n_inst, ITERS, status, visits, tests, stack_ref, stack_t)) {
       src.finish(T, (uint32_t)idx);
       idx = -1;
     }

@@ -2,12 +2,10 @@
 // hit, G-buffer record, shadow rays, plain matcap shading), the
 // neighbour-reading shading modes, and batched ray queries.
 //
-// A frame is two persistent kernels. k_primary replaces the per-pixel body of
-// canvas::update_canvas (canvas.cpp:765-834) and, in plain mode, the
-// background copy of canvas::render_scene (canvas.cpp:893-898) and the
-// colour of shadow-free pixels; hit pixels that need a shadow ray append a
-// job to a compacted queue. k_shadow traces the queue (canvas.cpp:836-857)
-// and writes those pixels' colour (canvas_to_image plain, canvas.cpp:650-669).
+// A frame is one persistent kernel, k_frame: it replaces the per-pixel body
+// of canvas::update_canvas (canvas.cpp:765-857) and, in plain mode, the
+// background copy of canvas::render_scene (canvas.cpp:893-898) and
+// canvas_to_image's plain shading (canvas.cpp:650-669).
 // k_shade replaces canvas_to_image's edges, wireframe and one-bit modes
 // (canvas.cpp:449-649), which read the right and upper neighbours.
 #include <cuda_runtime.h>
@@ -113,170 +111,194 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
   if (P.shade_mode == 1) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
 }
 
-// Primary rays (canvas.cpp:765-834): G-buffer record, texture / vertex colour,
-// then either the colour (no shadow) or a compacted shadow-ray job.
-struct PrimarySrc {
-  const FrameParams& P;
-  __device__ __forceinline__ uint32_t count() const {
-    const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
-    return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
-  }
-  __device__ __forceinline__ bool begin(Tracer<false>& T, const DevInst* insts, uint32_t n_inst, uint32_t idx) {
-    int x, y;
-    if (!item_pixel(P, idx, x, y)) return false;
-    if (n_inst == 0) {
-      write_miss(P, (size_t)y * P.w + x);
-      return false;
-    }
-    // canvas.cpp:700-701, 773-782
-    const float4 o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
-    const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
-    const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
-    float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
-    d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
-    T.begin(insts, n_inst, o.x, o.y, o.z, d.x, d.y, d.z, __fdiv_rn(P.diagonal, 100.f), FLT_MAX);
-    return true;
-  }
-  __device__ __forceinline__ void finish(Tracer<false>& T, uint32_t idx) {
-    int x, y;
-    item_pixel(P, idx, x, y);
-    const size_t pix = (size_t)y * P.w + x;
-    const Best& b = T.b;
-    if (!b.found) {
-      write_miss(P, pix);
-      return;
-    }
-    j3dg_pixel* rec = P.gbuf + pix;
-    const DevInst& I = P.inst[b.inst];
-    // canvas.cpp:788-801
-    const float4 N = __ldg(I.normals + b.tri);
-    float4 n = mat_vec(P.cs_inv, N.x, N.y, N.z, 0.f);
-    n = mat_vec(I.cs, n.x, n.y, n.z, n.w);
-    uint32_t mark = 0, pr = 0, pg = 0, pb = 0;
-    bool rgb = false;
-    const float wgt = fs(fs(1.f, b.u), b.v);
-    if (P.textured && I.uv != nullptr && I.tex != nullptr) {
-      // canvas.cpp:803-820
-      const float* uv = I.uv + 6 * (size_t)b.tri;
-      float c0 = fa(fa(fm(wgt, uv[0]), fm(b.u, uv[2])), fm(b.v, uv[4]));
-      float c1 = fa(fa(fm(wgt, uv[1]), fm(b.u, uv[3])), fm(b.v, uv[5]));
-      c0 = fmaxf(fminf(c0, 1.f), 0.f);
-      c1 = fmaxf(fminf(c1, 1.f), 0.f);
-      const int tw = (int)I.tex_w, th = (int)I.tex_h;
-      int tx = (int)fm(c0, (float)tw), ty = (int)fm(c1, (float)th);
-      tx = tx < 0 ? 0 : tx >= tw ? tw - 1 : tx;
-      ty = ty < 0 ? 0 : ty >= th ? th - 1 : ty;
-      const uint32_t c = __ldg(I.tex + (size_t)ty * I.tex_w + tx);
-      pr = c & 0xffu;
-      pg = (c >> 8) & 0xffu;
-      pb = (c >> 16) & 0xffu;
-      mark |= 2u;
-      rgb = true;
-    } else if (P.vertexcolors && I.colors != nullptr) {
-      // canvas.cpp:821-834
-      const uint32_t* Ti = I.index + 3 * (size_t)b.tri;
-      const float* C0 = I.colors + 3 * (size_t)Ti[0];
-      const float* C1 = I.colors + 3 * (size_t)Ti[1];
-      const float* C2 = I.colors + 3 * (size_t)Ti[2];
-      float c[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u, C1[k])), fm(b.v, C2[k]));
-      pr = (uint8_t)fm(c[0], 255.f);
-      pg = (uint8_t)fm(c[1], 255.f);
-      pb = (uint8_t)fm(c[2], 255.f);
-      mark |= 2u;
-      rgb = true;
-    }
-    if (rgb)
-      reinterpret_cast<uint32_t*>(rec)[0] = mark | (pr << 8) | (pg << 16) | (pb << 24);
-    else
-      reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
-    rec->u = n.x;
-    rec->v = n.y;
-    rec->depth = b.t;
-    *reinterpret_cast<uint4*>(&rec->object_id) = make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
-    if (P.shadow) {
-      // canvas.cpp:836-853: the shadow ray starts at the hit point, towards the light
-      const float ld = fm(P.diagonal, 3.f);
-      const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
-      const float4 A = __ldg(I.tris + 3 * (size_t)b.slot);
-      const float4 B = __ldg(I.tris + 3 * (size_t)b.slot + 1);
-      const float4 C = __ldg(I.tris + 3 * (size_t)b.slot + 2);
-      const float4 V0 = mat_vec(I.cs, A.x, A.y, A.z, 1.f);
-      const float4 V1 = mat_vec(I.cs, B.x, B.y, B.z, 1.f);
-      const float4 V2 = mat_vec(I.cs, C.x, C.y, C.z, 1.f);
-      const float px = fa(fa(fm(V0.x, wgt), fm(b.u, V1.x)), fm(b.v, V2.x));
-      const float py = fa(fa(fm(V0.y, wgt), fm(b.u, V1.y)), fm(b.v, V2.y));
-      const float pz = fa(fa(fm(V0.z, wgt), fm(b.u, V1.z)), fm(b.v, V2.z));
-      // warp-aggregated append to the shadow queue
-      const uint32_t m = __activemask();
-      const int leader = __ffs(m) - 1;
-      const uint32_t lane = threadIdx.x & 31u;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(P.work + 1, (uint32_t)__popc(m));
-      base = __shfl_sync(m, base, leader);
-      const uint32_t slot = base + __popc(m & ((1u << lane) - 1u));
-      P.queue[2 * (size_t)slot] = make_float4(px, py, pz, __uint_as_float((uint32_t)pix));
-      P.queue[2 * (size_t)slot + 1] = make_float4(fs(light.x, px), fs(light.y, py), fs(light.z, pz), 0.f);
-    } else if (P.shade_mode == 1) {
-      P.im[pix] = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
-    }
-  }
-};
-
-// Shadow rays from the compacted queue (canvas.cpp:848-857): any hit marks
-// the pixel; in plain mode the pixel's colour is written here.
-struct ShadowSrc {
-  const FrameParams& P;
-  __device__ __forceinline__ uint32_t count() const { return *(volatile const uint32_t*)(P.work + 1); }
-  __device__ __forceinline__ bool begin(Tracer<true>& T, const DevInst* insts, uint32_t n_inst, uint32_t idx) {
-    const float4 a = P.queue[2 * (size_t)idx], d = P.queue[2 * (size_t)idx + 1];
-    T.begin(insts, n_inst, a.x, a.y, a.z, d.x, d.y, d.z, 1e-3f, FLT_MAX);
-    return true;
-  }
-  __device__ __forceinline__ void finish(Tracer<true>& T, uint32_t idx) {
-    const size_t pix = __float_as_uint(P.queue[2 * (size_t)idx].w);
-    j3dg_pixel* rec = P.gbuf + pix;
-    const uint32_t w0 = reinterpret_cast<const uint32_t*>(rec)[0];
-    uint32_t mark = w0 & 0xffu;
-    if (T.b.found) {
-      mark |= 1u;
-      reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
-    }
-    if (P.shade_mode == 1)
-      P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, rec->u, rec->v);
-  }
-};
-
+// A frame in one persistent kernel: each lane runs primary ray -> (shadow ray)
+// -> next pixel, refilled from the tile-ordered pixel list by warp-aggregated
+// atomics (Aila and Laine 2009 dynamic fetch), so shadow rays overlap other
+// lanes' primary rays and the frame has a single tail.
+//   primary (canvas.cpp:765-834): G-buffer record, texture / vertex colour;
+//   shadow  (canvas.cpp:836-857): any hit towards the light marks the pixel;
+//   plain shading (canvas.cpp:650-669) when shade_mode == 1, misses get the
+//   background (canvas.cpp:893-898).
 static const int kTraceThreads = 128;
 static const int kIters = 16;
 
-__global__ void __launch_bounds__(kTraceThreads) k_primary(const FrameParams P) {
-  PrimarySrc src{P};
-  persistent_trace<false, kIters>(src, P.inst, P.n_inst, P.work + 0, P.status, P.counters);
+__device__ __forceinline__ uint32_t primary_count(const FrameParams& P) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_shadow(const FrameParams P) {
-  ShadowSrc src{P};
-  persistent_trace<true, kIters>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
+__device__ __forceinline__ void primary_begin(const FrameParams& P, Tracer& T, int x, int y) {
+  // canvas.cpp:700-701, 773-782
+  const float4 o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
+  const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
+  const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
+  float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
+  d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
+  T.begin(P.inst, P.n_inst, o.x, o.y, o.z, d.x, d.y, d.z, __fdiv_rn(P.diagonal, 100.f), FLT_MAX, false);
+}
+
+// Writes the hit record; returns true and sets up the shadow ray in T when
+// one is needed. w0 / su / sv keep what the final colour needs.
+__device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, size_t pix, uint32_t& w0, float& su,
+                                               float& sv) {
+  const Best b = T.b;
+  if (!b.found) {
+    write_miss(P, pix);
+    return false;
+  }
+  j3dg_pixel* rec = P.gbuf + pix;
+  const DevInst& I = P.inst[b.inst];
+  // canvas.cpp:788-801
+  const float4 N = __ldg(I.normals + b.tri);
+  float4 n = mat_vec(P.cs_inv, N.x, N.y, N.z, 0.f);
+  n = mat_vec(I.cs, n.x, n.y, n.z, n.w);
+  uint32_t mark = 0, pr = 0, pg = 0, pb = 0;
+  bool rgb = false;
+  const float wgt = fs(fs(1.f, b.u), b.v);
+  if (P.textured && I.uv != nullptr && I.tex != nullptr) {
+    // canvas.cpp:803-820
+    const float* uv = I.uv + 6 * (size_t)b.tri;
+    float c0 = fa(fa(fm(wgt, uv[0]), fm(b.u, uv[2])), fm(b.v, uv[4]));
+    float c1 = fa(fa(fm(wgt, uv[1]), fm(b.u, uv[3])), fm(b.v, uv[5]));
+    c0 = fmaxf(fminf(c0, 1.f), 0.f);
+    c1 = fmaxf(fminf(c1, 1.f), 0.f);
+    const int tw = (int)I.tex_w, th = (int)I.tex_h;
+    int tx = (int)fm(c0, (float)tw), ty = (int)fm(c1, (float)th);
+    tx = tx < 0 ? 0 : tx >= tw ? tw - 1 : tx;
+    ty = ty < 0 ? 0 : ty >= th ? th - 1 : ty;
+    const uint32_t c = __ldg(I.tex + (size_t)ty * I.tex_w + tx);
+    pr = c & 0xffu;
+    pg = (c >> 8) & 0xffu;
+    pb = (c >> 16) & 0xffu;
+    mark |= 2u;
+    rgb = true;
+  } else if (P.vertexcolors && I.colors != nullptr) {
+    // canvas.cpp:821-834
+    const uint32_t* Ti = I.index + 3 * (size_t)b.tri;
+    const float* C0 = I.colors + 3 * (size_t)Ti[0];
+    const float* C1 = I.colors + 3 * (size_t)Ti[1];
+    const float* C2 = I.colors + 3 * (size_t)Ti[2];
+    float c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u, C1[k])), fm(b.v, C2[k]));
+    pr = (uint8_t)fm(c[0], 255.f);
+    pg = (uint8_t)fm(c[1], 255.f);
+    pb = (uint8_t)fm(c[2], 255.f);
+    mark |= 2u;
+    rgb = true;
+  }
+  w0 = mark | (pr << 8) | (pg << 16) | (pb << 24);
+  if (rgb)
+    reinterpret_cast<uint32_t*>(rec)[0] = w0;
+  else
+    reinterpret_cast<uint8_t*>(rec)[0] = (uint8_t)mark;
+  rec->u = n.x;
+  rec->v = n.y;
+  rec->depth = b.t;
+  *reinterpret_cast<uint4*>(&rec->object_id) = make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
+  su = n.x;
+  sv = n.y;
+  if (!P.shadow) {
+    if (P.shade_mode == 1) P.im[pix] = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
+    return false;
+  }
+  // canvas.cpp:836-853: from the hit point towards the light
+  const float ld = fm(P.diagonal, 3.f);
+  const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
+  const float4 A = __ldg(I.tris + 3 * (size_t)b.slot);
+  const float4 B = __ldg(I.tris + 3 * (size_t)b.slot + 1);
+  const float4 C = __ldg(I.tris + 3 * (size_t)b.slot + 2);
+  const float4 V0 = mat_vec(I.cs, A.x, A.y, A.z, 1.f);
+  const float4 V1 = mat_vec(I.cs, B.x, B.y, B.z, 1.f);
+  const float4 V2 = mat_vec(I.cs, C.x, C.y, C.z, 1.f);
+  const float px = fa(fa(fm(V0.x, wgt), fm(b.u, V1.x)), fm(b.v, V2.x));
+  const float py = fa(fa(fm(V0.y, wgt), fm(b.u, V1.y)), fm(b.v, V2.y));
+  const float pz = fa(fa(fm(V0.z, wgt), fm(b.u, V1.z)), fm(b.v, V2.z));
+  T.begin(P.inst, P.n_inst, px, py, pz, fs(light.x, px), fs(light.y, py), fs(light.z, pz), 1e-3f, FLT_MAX, true);
+  return true;
+}
+
+__device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer& T, size_t pix, uint32_t w0, float su,
+                                              float sv) {
+  uint32_t mark = w0 & 0xffu;
+  if (T.b.found) {
+    mark |= 1u;
+    reinterpret_cast<uint8_t*>(P.gbuf + pix)[0] = (uint8_t)mark;
+  }
+  if (P.shade_mode == 1)
+    P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
+}
+
+__global__ void __launch_bounds__(kTraceThreads) k_frame(const FrameParams P) {
+  Tracer T;
+  uint32_t stack_ref[J3DG_STACK];
+  float stack_t[J3DG_STACK];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t n = primary_count(P);
+  int phase = 0;  // 0 idle, 1 primary, 2 shadow
+  bool exhausted = false;
+  size_t pix = 0;
+  uint32_t w0 = 0;
+  float su = 0.f, sv = 0.f;
+  uint32_t visits = 0, tests = 0;
+#pragma unroll 1
+  for (;;) {
+    const bool need = phase == 0 && !exhausted;
+    const uint32_t m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(P.work, (uint32_t)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t my = base + __popc(m & ((1u << lane) - 1u));
+        int x, y;
+        if (my >= n) {
+          exhausted = true;
+        } else if (item_pixel(P, my, x, y)) {
+          pix = (size_t)y * P.w + x;
+          if (P.n_inst == 0) {
+            write_miss(P, pix);
+          } else {
+            primary_begin(P, T, x, y);
+            phase = 1;
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
+    if (phase != 0 && T.run(P.inst, P.n_inst, kIters, P.status, visits, tests, stack_ref, stack_t)) {
+      if (phase == 1) {
+        phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
+      } else {
+        shadow_finish(P, T, pix, w0, su, sv);
+        phase = 0;
+      }
+    }
+  }
+  if (P.counters) {
+    atomicAdd(P.counters + 0, (unsigned long long)visits);
+    atomicAdd(P.counters + 1, (unsigned long long)tests);
+  }
 }
 
 // j3dg_ray batches (find_closest / find_any through the C-ABI)
 template <bool ANY>
 struct BatchSrc {
+  static const bool kAny = ANY;
   const j3dg_ray* rays;
   j3dg_hit* hits;
   uint32_t n;
   __device__ __forceinline__ uint32_t count() const { return n; }
-  __device__ __forceinline__ bool begin(Tracer<ANY>& T, const DevInst* insts, uint32_t n_inst, uint32_t i) {
+  __device__ __forceinline__ bool begin(Tracer& T, const DevInst* insts, uint32_t n_inst, uint32_t i) {
     const float* f = reinterpret_cast<const float*>(rays + i);  // 40-byte records: 4-byte loads
-    if (T.begin(insts, n_inst, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9])) {
+    if (T.begin(insts, n_inst, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], ANY)) {
       finish(T, i);
       return false;
     }
     return true;
   }
-  __device__ __forceinline__ void finish(Tracer<ANY>& T, uint32_t i) {
+  __device__ __forceinline__ void finish(Tracer& T, uint32_t i) {
     const float t_far = reinterpret_cast<const float*>(rays + i)[9];
     j3dg_hit h;
     h.found = T.b.found ? 1u : 0u;
@@ -295,7 +317,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restric
                                                         j3dg_hit* __restrict__ hits, uint32_t* counter,
                                                         uint32_t* status) {
   BatchSrc<ANY> src{rays, hits, n};
-  persistent_trace<ANY, kIters>(src, inst, n_inst, counter, status, nullptr);
+  persistent_trace<kIters>(src, inst, n_inst, counter, status, nullptr);
 }
 
 template <class K>
@@ -442,15 +464,11 @@ __global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
   if (rw <= 0 || rh <= 0) return cudaSuccess;
-  static int blocks_p = 0, blocks_s = 0;
-  if (!blocks_p) {
-    blocks_p = persistent_blocks(k_primary);
-    blocks_s = persistent_blocks(k_shadow);
-  }
-  cudaError_t e = cudaMemsetAsync(P.work, 0, 4 * sizeof(uint32_t), st);
+  static int blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_frame);
+  cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  k_primary<<<blocks_p, kTraceThreads, 0, st>>>(P);
-  if (P.shadow && P.n_inst > 0) k_shadow<<<blocks_s, kTraceThreads, 0, st>>>(P);
+  k_frame<<<blocks, kTraceThreads, 0, st>>>(P);
   return cudaGetLastError();
 }
 

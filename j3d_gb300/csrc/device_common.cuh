@@ -225,7 +225,17 @@ struct Tracer {
                                       uint32_t* status, uint32_t& visits, uint32_t& tests,
                                       uint32_t* __restrict__ stack_ref, float* __restrict__ stack_t) {
 #pragma unroll 1
-    for (int it = 0; it < iters; ++it) {
+    for (int it = 0; it < iters; ++it)
+      if (step(insts, n_inst, status, visits, tests, stack_ref, stack_t)) return true;
+    return false;
+  }
+
+  // One traversal step: a pop, a leaf (its triangles) or a node. Returns
+  // true when the ray is finished.
+  __device__ __forceinline__ bool step(const DevInst* __restrict__ insts, uint32_t n_inst, uint32_t* status,
+                                       uint32_t& visits, uint32_t& tests, uint32_t* __restrict__ stack_ref,
+                                       float* __restrict__ stack_t) {
+    {
       if (cur == J3DG_EMPTY_REF) {
         bool got = false;
         while (sp > 0) {
@@ -239,7 +249,7 @@ struct Tracer {
         if (!got) {
           if (++inst >= n_inst) return true;
           start_object(insts);
-          continue;
+          return false;
         }
       }
       if (cur & J3DG_LEAF_BIT) {
@@ -254,7 +264,7 @@ struct Tracer {
           if (tri_test(r, tris, first + k, inst, b, any) && any) return true;
         }
         cur = J3DG_EMPTY_REF;
-        continue;
+        return false;
       }
       if (budget-- == 0) {
         atomicOr(status, J3DG_DEV_VISIT_CAP);

@@ -119,8 +119,21 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 //   shadow  (canvas.cpp:836-857): any hit towards the light marks the pixel;
 //   plain shading (canvas.cpp:650-669) when shade_mode == 1, misses get the
 //   background (canvas.cpp:893-898).
-static const int kTraceThreads = 128;
-static const int kIters = 16;
+#ifndef J3DG_TRACE_THREADS
+#define J3DG_TRACE_THREADS 128
+#endif
+#ifndef J3DG_TRACE_MINBLOCKS
+#define J3DG_TRACE_MINBLOCKS 5
+#endif
+#ifndef J3DG_TRACE_ITERS
+#define J3DG_TRACE_ITERS 16
+#endif
+// idle lanes that make a warp stop tracing and fetch new pixels
+#ifndef J3DG_REFILL_AT
+#define J3DG_REFILL_AT 12
+#endif
+static const int kTraceThreads = J3DG_TRACE_THREADS;
+static const int kIters = J3DG_TRACE_ITERS;
 
 __device__ __forceinline__ uint32_t primary_count(const FrameParams& P) {
   const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
@@ -229,7 +242,7 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
     P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_frame(const FrameParams P) {
+__global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(const FrameParams P) {
   Tracer T;
   uint32_t stack_ref[J3DG_STACK];
   float stack_t[J3DG_STACK];
@@ -243,6 +256,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_frame(const FrameParams P) {
   uint32_t visits = 0, tests = 0;
 #pragma unroll 1
   for (;;) {
+    // refill: every idle lane takes the next pixel; one atomic per warp
     const bool need = phase == 0 && !exhausted;
     const uint32_t m = __ballot_sync(0xffffffffu, need);
     if (m) {
@@ -267,13 +281,19 @@ __global__ void __launch_bounds__(kTraceThreads) k_frame(const FrameParams P) {
       }
     }
     if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
-    if (phase != 0 && T.run(P.inst, P.n_inst, kIters, P.status, visits, tests, stack_ref, stack_t)) {
-      if (phase == 1) {
-        phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
-      } else {
-        shadow_finish(P, T, pix, w0, su, sv);
-        phase = 0;
+    // all lanes step together; leave to refill once enough lanes are idle
+#pragma unroll 1
+    for (;;) {
+      if (phase != 0 && T.step(P.inst, P.n_inst, P.status, visits, tests, stack_ref, stack_t)) {
+        if (phase == 1) {
+          phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
+        } else {
+          shadow_finish(P, T, pix, w0, su, sv);
+          phase = 0;
+        }
       }
+      if (__all_sync(0xffffffffu, phase == 0)) break;
+      if (__popc(__ballot_sync(0xffffffffu, phase == 0 && !exhausted)) >= J3DG_REFILL_AT) break;
     }
   }
   if (P.counters) {

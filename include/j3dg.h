@@ -42,6 +42,7 @@ typedef enum j3dg_status {
 #define J3DG_DEV_STACK_OVERFLOW 0x1u
 #define J3DG_DEV_VISIT_CAP 0x2u
 #define J3DG_DEV_BAD_INDEX 0x4u
+#define J3DG_DEV_HIT_OVERFLOW 0x8u /* more than 64 hits on one voxelization ray */
 
 typedef struct j3dg_ctx j3dg_ctx;
 typedef struct j3dg_mesh j3dg_mesh;
@@ -188,6 +189,22 @@ int j3dg_find_closest(j3dg_ctx* ctx, const j3dg_instance* objects, uint32_t n_ob
 int j3dg_find_any(j3dg_ctx* ctx, const j3dg_instance* objects, uint32_t n_objects, const j3dg_ray* rays,
                   uint32_t n_rays, j3dg_hit* hits);
 
+/* jtk find_all_triangles (vox.cpp:333) on one mesh: for each ray, every
+   accepted triangle with t < t_far, sorted by (t, triangle id); the first
+   `cap` go to hits[ray * cap ...], the full count to counts[ray]. */
+int j3dg_find_all(j3dg_ctx* ctx, const j3dg_mesh* mesh, const j3dg_ray* rays, uint32_t n_rays, uint32_t cap,
+                  j3dg_hit* hits, uint32_t* counts);
+
+/* The voxel grid of write_vox (vox.cpp:284-380): dims from max_dim and the
+   mesh bbox (vox.cpp:292-299), three axis-aligned sweeps of all-hits rays,
+   each hit's voxel (index x + (y + z dim1) dim0) set to its colour index
+   (vox.cpp:154-173; texture if uv and texture are set, else vertex colours,
+   else white). Sweep, ray and hit order are fixed and the last write wins.
+   With voxels == NULL only dims are returned; otherwise capacity must hold
+   dims[0] * dims[1] * dims[2] bytes. max_dim <= 1024. */
+int j3dg_voxelize(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3], uint8_t* voxels,
+                  uint64_t capacity);
+
 /* ---------------------------------------------------------------- matcaps */
 
 /* matcap.h:18-24: a w x h RGBA8 texture plus its cavity colour, uploaded once. */
@@ -252,6 +269,13 @@ int j3dg_prepare_scene(const j3dg_instance* objects, uint32_t n, float min_bb[3]
 /* scene.cpp:91-110 unzoom */
 void j3dg_unzoom(const float min_bb[3], const float max_bb[3], float diagonal, float cs[16], float cs_inv[16],
                  float pivot[3]);
+/* pixel.cpp:6-25 get_closest_vertex: the vertex of the pixel's triangle
+   nearest to its hit point (vertices: V x 3 float, triangles: T x 3). */
+uint32_t j3dg_get_closest_vertex(const j3dg_pixel* p, const float* vertices, const uint32_t* triangles);
+/* view.cpp:439-459 get_world_position (mesh branch): the hit point of the
+   pixel in world space through the object's cs. */
+void j3dg_get_world_position(const j3dg_pixel* p, const float* vertices, const uint32_t* triangles,
+                             const float cs[16], float out[3]);
 /* matcap.cpp:9-268: type 0 red wax, 1 gray, 2 brown, 3 sketch; pixels must
    hold 512 x 512. */
 int j3dg_make_matcap(int type, uint32_t* pixels, uint32_t* w, uint32_t* h, uint32_t* cavity_clr);

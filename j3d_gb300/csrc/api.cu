@@ -15,6 +15,7 @@
 #include "../../include/j3dg.h"
 #include "device_common.cuh"
 #include "internal.h"
+#include "query.cuh"
 #include "render.cuh"
 
 namespace j3dg {
@@ -543,6 +544,91 @@ int j3dg_find_closest(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, co
 int j3dg_find_any(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, const j3dg_ray* rays, uint32_t n,
                   j3dg_hit* hits) {
   return ray_query(c, objs, n_obj, rays, n, hits, true);
+}
+
+int j3dg_find_all(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* rays, uint32_t n, uint32_t cap, j3dg_hit* hits,
+                  uint32_t* counts) {
+  if (!c || !mesh || (n && (!rays || !counts || (cap && !hits)))) return J3DG_ERR_INVALID_ARGUMENT;
+  if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "find_all: mesh of another context");
+  cudaSetDevice(c->device);
+  j3dg_instance one;
+  one.mesh = mesh;
+  for (int i = 0; i < 16; ++i) one.cs[i] = (i % 5 == 0) ? 1.f : 0.f;
+  one.db_id = 0;
+  one.reserved = 0;
+  const DevInst* dinst = nullptr;
+  if (int rc = upload_instances(c, &one, 1, &dinst)) return rc;
+  if (n == 0) return J3DG_OK;
+  const bool rays_dev = is_device_ptr(rays), hits_dev = !cap || is_device_ptr(hits), counts_dev = is_device_ptr(counts);
+  j3dg_ray* dr = const_cast<j3dg_ray*>(rays);
+  j3dg_hit* dh = hits;
+  uint32_t* dc = counts;
+  if (!rays_dev) {
+    CK(c, cudaMallocAsync((void**)&dr, sizeof(j3dg_ray) * (size_t)n, S(c)), "find_all");
+    CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "find_all");
+  }
+  if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n * cap, S(c)), "find_all");
+  if (!counts_dev) CK(c, cudaMallocAsync((void**)&dc, sizeof(uint32_t) * (size_t)n, S(c)), "find_all");
+  CK(c, j3dg::launch_find_all(dinst, dr, n, cap, dh, dc, c->d_status, S(c)), "find_all");
+  if (!hits_dev) {
+    CK(c, cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * (size_t)n * cap, cudaMemcpyDeviceToHost, S(c)), "find_all");
+    cudaFreeAsync(dh, S(c));
+  }
+  if (!counts_dev) {
+    CK(c, cudaMemcpyAsync(counts, dc, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost, S(c)), "find_all");
+    cudaFreeAsync(dc, S(c));
+  }
+  if (!rays_dev) cudaFreeAsync(dr, S(c));
+  return check_status(c);
+}
+
+int j3dg_voxelize(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3], uint8_t* voxels,
+                  uint64_t capacity) {
+  if (!c || !mesh || !dims) return J3DG_ERR_INVALID_ARGUMENT;
+  if (max_dim == 0 || max_dim > 1024) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize: max_dim must be 1..1024");
+  if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize: mesh of another context");
+  cudaSetDevice(c->device);
+  // vox.cpp:286-299
+  const float* mn = mesh->min_bb;
+  const float* mx = mesh->max_bb;
+  int L = 0;
+  if ((mx[1] - mn[1]) > (mx[L] - mn[L])) L = 1;
+  if ((mx[2] - mn[2]) > (mx[L] - mn[L])) L = 2;
+  j3dg::VoxParams V;
+  memset(&V, 0, sizeof(V));
+  for (int j = 0; j < 3; ++j) {
+    V.dim[j] = (uint32_t)((float)max_dim * (mx[j] - mn[j]) / (mx[L] - mn[L]));
+    if (V.dim[j] == 0) V.dim[j] = 1;
+    dims[j] = V.dim[j];
+    V.mn[j] = mn[j];
+    V.mx[j] = mx[j];
+  }
+  const uint64_t total = (uint64_t)V.dim[0] * V.dim[1] * V.dim[2];
+  if (!voxels) return J3DG_OK;
+  if (capacity < total) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize: capacity below dims product");
+  for (int d = 0; d < 3; ++d) V.rays[d] = V.dim[(d + 1) % 3] * V.dim[(d + 2) % 3];
+  V.rays_total = V.rays[0] + V.rays[1] + V.rays[2];
+  V.use_texture = mesh->d_uv && mesh->d_tex && mesh->tex_w && mesh->tex_h;
+  V.use_colors = !V.use_texture && mesh->d_colors;
+  j3dg_instance one;
+  one.mesh = mesh;
+  for (int i = 0; i < 16; ++i) one.cs[i] = (i % 5 == 0) ? 1.f : 0.f;
+  one.db_id = 0;
+  one.reserved = 0;
+  const DevInst* dinst = nullptr;
+  if (int rc = upload_instances(c, &one, 1, &dinst)) return rc;
+  uint32_t* keys = nullptr;
+  uint8_t* dout = voxels;
+  const bool out_dev = is_device_ptr(voxels);
+  CK(c, cudaMallocAsync((void**)&keys, sizeof(uint32_t) * total, S(c)), "voxelize");
+  if (!out_dev) CK(c, cudaMallocAsync((void**)&dout, total, S(c)), "voxelize");
+  CK(c, j3dg::launch_voxelize(dinst, V, keys, dout, c->d_status, S(c)), "voxelize");
+  if (!out_dev) {
+    CK(c, cudaMemcpyAsync(voxels, dout, total, cudaMemcpyDeviceToHost, S(c)), "voxelize");
+    cudaFreeAsync(dout, S(c));
+  }
+  cudaFreeAsync(keys, S(c));
+  return check_status(c);
 }
 
 // --------------------------------------------------------------- matcap

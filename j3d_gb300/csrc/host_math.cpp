@@ -232,6 +232,45 @@ extern "C" void j3dg_unzoom(const float* mn, const float* mx, float diagonal, fl
   j3dg_invert_orthonormal(cs, cs_inv);
 }
 
+// -------------------------------------------------------------- picking ----
+
+extern "C" uint32_t j3dg_get_closest_vertex(const j3dg_pixel* p, const float* V, const uint32_t* T) {
+  // pixel.cpp:6-25
+  const uint32_t* t = T + 3 * (size_t)p->object_id;
+  const float* A = V + 3 * (size_t)t[0];
+  const float* B = V + 3 * (size_t)t[1];
+  const float* C = V + 3 * (size_t)t[2];
+  const float wgt = 1.f - p->barycentric_u - p->barycentric_v;
+  float pos[3], d[3] = {0.f, 0.f, 0.f};
+  for (int k = 0; k < 3; ++k) pos[k] = A[k] * wgt + p->barycentric_u * B[k] + p->barycentric_v * C[k];
+  const float* P[3] = {A, B, C};
+  for (int j = 0; j < 3; ++j) {
+    float e0 = pos[0] - P[j][0], e1 = pos[1] - P[j][1], e2 = pos[2] - P[j][2];
+    float s = e0 * e0;
+    s = s + e1 * e1;
+    d[j] = s + e2 * e2;
+  }
+  return (d[0] < d[1]) ? ((d[0] < d[2]) ? t[0] : t[2]) : ((d[1] < d[2]) ? t[1] : t[2]);
+}
+
+extern "C" void j3dg_get_world_position(const j3dg_pixel* p, const float* V, const uint32_t* T, const float* cs,
+                                        float* out) {
+  // view.cpp:439-459, mesh branch: barycentric point, then cs x point
+  const uint32_t* t = T + 3 * (size_t)p->object_id;
+  const float* A = V + 3 * (size_t)t[0];
+  const float* B = V + 3 * (size_t)t[1];
+  const float* C = V + 3 * (size_t)t[2];
+  const float wgt = 1.f - p->barycentric_u - p->barycentric_v;
+  float pos[4];
+  for (int k = 0; k < 3; ++k) pos[k] = A[k] * wgt + p->barycentric_u * B[k] + p->barycentric_v * C[k];
+  pos[3] = 1.f * wgt + p->barycentric_u * 1.f + p->barycentric_v * 1.f;
+  float w[4];
+  mat_vec(cs, pos, w);
+  out[0] = w[0];
+  out[1] = w[1];
+  out[2] = w[2];
+}
+
 // --------------------------------------------------------------- canvas ----
 
 extern "C" void j3dg_fill_background(uint32_t* bg, uint32_t w, uint32_t h, uint32_t top, uint32_t bottom) {

@@ -347,6 +347,38 @@ def find_closest(ctx: Context, objs: list[SceneObject], rays, hits=None, any_hit
     return hits
 
 
+def find_all(ctx: Context, mesh: Mesh, rays, cap: int = 64):
+    """find_all_triangles (vox.cpp:333): (hits[n, cap] sorted by (t, id), counts[n])."""
+    n = len(rays)
+    hits = np.zeros((n, cap), HIT_DTYPE)
+    counts = np.zeros(n, np.uint32)
+    _check(ctx.h, lib().j3dg_find_all(ctx.h, mesh.h, vptr(rays), n, cap, vptr(hits) if cap else None, vptr(counts)))
+    return hits, counts
+
+
+def voxelize(ctx: Context, mesh: Mesh, max_dim: int = 100) -> np.ndarray:
+    """The voxel grid of write_vox (vox.cpp:284-380) as uint8[z, y, x]."""
+    dims = (C.c_uint32 * 3)()
+    _check(ctx.h, lib().j3dg_voxelize(ctx.h, mesh.h, max_dim, dims, None, 0))
+    out = np.zeros(int(dims[0]) * int(dims[1]) * int(dims[2]), np.uint8)
+    _check(ctx.h, lib().j3dg_voxelize(ctx.h, mesh.h, max_dim, dims, vptr(out), out.size))
+    return out.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+
+
+def get_closest_vertex(p, V: np.ndarray, T: np.ndarray) -> int:
+    """pixel.cpp:6-25"""
+    rec = np.ascontiguousarray(np.asarray(p).reshape(1), PIXEL_DTYPE)
+    return int(lib().j3dg_get_closest_vertex(vptr(rec), vptr(V), vptr(T)))
+
+
+def get_world_position(p, V: np.ndarray, T: np.ndarray, cs) -> np.ndarray:
+    """view.cpp:439-459 (mesh branch)"""
+    rec = np.ascontiguousarray(np.asarray(p).reshape(1), PIXEL_DTYPE)
+    out = np.zeros(3, np.float32)
+    lib().j3dg_get_world_position(vptr(rec), vptr(V), vptr(T), fptr(np.ascontiguousarray(cs, np.float32)), fptr(out))
+    return out
+
+
 # --------------------------------------------------------- host j3d math
 
 def make_default_camera() -> Camera:
@@ -395,7 +427,8 @@ def camera_for_vfov(vfov_deg: float) -> Camera:
     return c
 
 
-__all__ = ["Context", "Mesh", "Scene", "SceneObject", "Matcap", "Canvas", "settings", "find_closest",
+__all__ = ["Context", "Mesh", "Scene", "SceneObject", "Matcap", "Canvas", "settings", "find_closest", "find_all",
+           "voxelize", "get_closest_vertex", "get_world_position",
            "make_default_camera", "make_projection_matrix", "invert_projection_matrix", "invert_orthonormal",
            "make_matcap", "fill_background", "camera_for_vfov", "PIXEL_DTYPE", "RAY_DTYPE", "HIT_DTYPE",
            "J3dgError"]

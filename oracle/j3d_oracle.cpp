@@ -955,24 +955,60 @@ void orc_find_closest(const orc_instance* inst, uint32_t n_inst, const orc_ray* 
   }
 }
 
-uint32_t orc_find_all(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap) {
-  float o4[4] = {ray->orig[0], ray->orig[1], ray->orig[2], 1.f};
-  RayPre r = prep_ray({o4[0], o4[1], o4[2]}, {ray->dir[0], ray->dir[1], ray->dir[2]}, ray->t_near, m->scale);
-  std::vector<orc_hit> all;
-  for (uint32_t id = 0; id < m->nt; ++id) {
-    const uint32_t* T = m->tris + 3 * (size_t)id;
+// All accepted triangles along the ray (t < t_far), through the BVH (any
+// node whose slab interval meets [t_near, t_far]) or by brute force.
+static void all_hits(const orc_mesh& m, const RayPre& r, float t_far, bool brute, std::vector<orc_hit>& out) {
+  auto test = [&](uint32_t id) {
+    const uint32_t* T = m.tris + 3 * (size_t)id;
     float t, u, v;
-    if (!tri_test(r, load3(m->vertices + 3 * (size_t)T[0]), load3(m->vertices + 3 * (size_t)T[1]),
-                  load3(m->vertices + 3 * (size_t)T[2]), t, u, v))
-      continue;
-    if (!(t < ray->t_far)) continue;
-    all.push_back({1u, t, u, v, id, 0u});
+    if (!tri_test(r, load3(m.vertices + 3 * (size_t)T[0]), load3(m.vertices + 3 * (size_t)T[1]),
+                  load3(m.vertices + 3 * (size_t)T[2]), t, u, v))
+      return;
+    if (!(t < t_far)) return;
+    out.push_back({1u, t, u, v, id, 0u});
+  };
+  if (brute || m.has_root_leaf) {
+    for (uint32_t id = 0; id < m.nt; ++id) test(id);
+  } else {
+    std::vector<uint32_t> stack{0u};
+    while (!stack.empty()) {
+      const Node4& N = m.nodes[stack.back()];
+      stack.pop_back();
+      for (int k = 0; k < 4; ++k) {
+        if (N.child[k] < 0) continue;
+        float lo[3] = {N.lo[0][k], N.lo[1][k], N.lo[2][k]};
+        float hi[3] = {N.hi[0][k], N.hi[1][k], N.hi[2][k]};
+        float tn, tf;
+        slab(r, lo, hi, tn, tf);
+        if (!(std::fmax(tn, r.t_near) <= std::fmin(tf, t_far))) continue;
+        if (N.count[k] > 0) {
+          for (uint32_t j = 0; j < N.count[k]; ++j) test(m.prims[(uint32_t)N.child[k] + j]);
+        } else {
+          stack.push_back((uint32_t)N.child[k]);
+        }
+      }
+    }
   }
-  std::sort(all.begin(), all.end(), [](const orc_hit& a, const orc_hit& b) {
+  std::sort(out.begin(), out.end(), [](const orc_hit& a, const orc_hit& b) {
     return a.distance < b.distance || (a.distance == b.distance && a.object_id < b.object_id);
   });
+}
+
+static uint32_t find_all_impl(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap, bool brute) {
+  RayPre r = prep_ray({ray->orig[0], ray->orig[1], ray->orig[2]}, {ray->dir[0], ray->dir[1], ray->dir[2]},
+                      ray->t_near, m->scale);
+  std::vector<orc_hit> all;
+  all_hits(*m, r, ray->t_far, brute, all);
   for (uint32_t i = 0; i < (uint32_t)all.size() && i < cap; ++i) hits[i] = all[i];
   return (uint32_t)all.size();
+}
+
+uint32_t orc_find_all(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap) {
+  return find_all_impl(m, ray, hits, cap, false);
+}
+
+uint32_t orc_find_all_brute(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap) {
+  return find_all_impl(m, ray, hits, cap, true);
 }
 
 // canvas.cpp:55-78
@@ -1321,6 +1357,120 @@ uint32_t orc_get_closest_vertex(const orc_pixel* p, const float* V, const uint32
   f3 A = sub3(pos, V0), B = sub3(pos, V1), C = sub3(pos, V2);
   float dA = dot3(A, A), dB = dot3(B, B), dC = dot3(C, C);
   return (dA < dB) ? ((dA < dC) ? t[0] : t[2]) : ((dB < dC) ? t[1] : t[2]);
+}
+
+// view.cpp:439-459, mesh branch
+void orc_get_world_position(const orc_pixel* p, const float* V, const uint32_t* T, const float* cs, float* out) {
+  const uint32_t* t = T + 3 * (size_t)p->object_id;
+  const float* A = V + 3 * (size_t)t[0];
+  const float* B = V + 3 * (size_t)t[1];
+  const float* C = V + 3 * (size_t)t[2];
+  float wgt = 1.f - p->barycentric_u - p->barycentric_v;
+  float pos[4];
+  for (int k = 0; k < 3; ++k) pos[k] = A[k] * wgt + p->barycentric_u * B[k] + p->barycentric_v * C[k];
+  pos[3] = 1.f * wgt + p->barycentric_u * 1.f + p->barycentric_v * 1.f;
+  float w[4];
+  mat_vec(cs, pos, w);
+  out[0] = w[0];
+  out[1] = w[1];
+  out[2] = w[2];
+}
+
+// vox.cpp:154-173
+static uint8_t color_to_index(uint8_t r, uint8_t g, uint8_t b) {
+  r = r < 16 ? 0 : (uint8_t)(r - 16);
+  g = g < 16 ? 0 : (uint8_t)(g - 16);
+  b = b < 32 ? 0 : (uint8_t)(b - 32);
+  uint8_t ret = (uint8_t)(((r >> 5) << 5) | ((g >> 5) << 2) | (b >> 6));
+  return ret == 0 ? 1 : ret;
+}
+
+static uint32_t vox_cell(float p, float lo, float hi, uint32_t dim) {
+  float x = (p - lo) / (hi - lo);
+  float f = x * (float)dim;
+  uint32_t X = f > 0.f ? (uint32_t)f : 0u;
+  if (X >= dim) X = dim - 1;
+  return X;
+}
+
+// vox.cpp:284-380
+uint64_t orc_voxelize(const orc_mesh* m, uint32_t max_dim, uint32_t* dims, uint8_t* out, uint64_t cap) {
+  const float* mn = m->min_bb;
+  const float* mx = m->max_bb;
+  int L = 0;
+  if ((mx[1] - mn[1]) > (mx[L] - mn[L])) L = 1;
+  if ((mx[2] - mn[2]) > (mx[L] - mn[L])) L = 2;
+  uint32_t dim[3];
+  for (int j = 0; j < 3; ++j) {
+    dim[j] = (uint32_t)((float)max_dim * (mx[j] - mn[j]) / (mx[L] - mn[L]));
+    if (dim[j] == 0) dim[j] = 1;
+    dims[j] = dim[j];
+  }
+  uint64_t total = (uint64_t)dim[0] * dim[1] * dim[2];
+  if (!out || cap < total) return total;
+  std::memset(out, 0, total);
+  const bool use_texture = m->uv != nullptr && m->tex != nullptr && m->tex_w > 0 && m->tex_h > 0;
+  const bool use_colors = !use_texture && m->colors != nullptr;
+  std::vector<orc_hit> hits(1u << 16);
+  for (int dd = 0; dd < 3; ++dd) {
+    float dir[3] = {0.f, 0.f, 0.f};
+    dir[dd] = dd == 2 ? 2.f : 1.f;  // vox.cpp:311-315
+    const int d1i = (dd + 1) % 3, d2i = (dd + 2) % 3;
+    for (uint32_t d1 = 0; d1 < dim[d1i]; ++d1)
+      for (uint32_t d2 = 0; d2 < dim[d2i]; ++d2) {
+        float st[3];
+        st[dd] = mn[dd];
+        st[d1i] = (((float)d1 + 0.5f) / (float)dim[d1i]) * (mx[d1i] - mn[d1i]) + mn[d1i];
+        st[d2i] = (((float)d2 + 0.5f) / (float)dim[d2i]) * (mx[d2i] - mn[d2i]) + mn[d2i];
+        orc_ray r;
+        r.orig[0] = st[0];
+        r.orig[1] = st[1];
+        r.orig[2] = st[2];
+        r.orig[3] = 1.f;
+        r.dir[0] = dir[0];
+        r.dir[1] = dir[1];
+        r.dir[2] = dir[2];
+        r.dir[3] = 0.f;
+        r.t_near = 0.f;
+        r.t_far = std::numeric_limits<float>::max();
+        uint32_t n = orc_find_all(m, &r, hits.data(), (uint32_t)hits.size());
+        for (uint32_t i = 0; i < n && i < hits.size(); ++i) {
+          const orc_hit& h = hits[i];
+          const uint32_t* t = m->tris + 3 * (size_t)h.object_id;
+          const float* A = m->vertices + 3 * (size_t)t[0];
+          const float* B = m->vertices + 3 * (size_t)t[1];
+          const float* C = m->vertices + 3 * (size_t)t[2];
+          float wgt = 1.f - h.u - h.v;
+          float pos[3];
+          for (int k = 0; k < 3; ++k) pos[k] = A[k] * wgt + h.u * B[k] + h.v * C[k];
+          float clr[3] = {1.f, 1.f, 1.f};
+          if (use_texture) {
+            const float* uv = m->uv + 6 * (size_t)h.object_id;
+            float c0 = wgt * uv[0] + h.u * uv[2] + h.v * uv[4];
+            float c1 = wgt * uv[1] + h.u * uv[3] + h.v * uv[5];
+            c0 = std::max(std::min(c0, 1.f), 0.f);
+            c1 = std::max(std::min(c1, 1.f), 0.f);
+            int x = (int)(c0 * (float)(m->tex_w - 1));
+            int y = (int)(c1 * (float)(m->tex_h - 1));
+            uint32_t color = m->tex[(size_t)y * m->tex_w + x];
+            clr[0] = (float)(color & 255) / 255.f;
+            clr[1] = (float)((color >> 8) & 255) / 255.f;
+            clr[2] = (float)((color >> 16) & 255) / 255.f;
+          } else if (use_colors) {
+            const float* c0 = m->colors + 3 * (size_t)t[0];
+            const float* c1 = m->colors + 3 * (size_t)t[1];
+            const float* c2 = m->colors + 3 * (size_t)t[2];
+            for (int k = 0; k < 3; ++k) clr[k] = c0[k] * wgt + h.u * c1[k] + h.v * c2[k];
+          }
+          uint32_t X = vox_cell(pos[0], mn[0], mx[0], dim[0]);
+          uint32_t Y = vox_cell(pos[1], mn[1], mx[1], dim[1]);
+          uint32_t Z = vox_cell(pos[2], mn[2], mx[2], dim[2]);
+          uint8_t ci = color_to_index((uint8_t)(clr[0] * 255.f), (uint8_t)(clr[1] * 255.f), (uint8_t)(clr[2] * 255.f));
+          out[X + ((size_t)Y + (size_t)Z * dim[1]) * dim[0]] = ci;  // vox.cpp:123-127
+        }
+      }
+  }
+  return total;
 }
 
 }  // extern "C"

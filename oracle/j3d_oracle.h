@@ -123,9 +123,11 @@ void orc_mesh_set_texture(orc_mesh* m, const uint32_t* tex, uint32_t w, uint32_t
 void orc_find_closest(const orc_instance* inst, uint32_t n_inst, const orc_ray* rays, uint32_t n,
                       orc_hit* hits, int mode, int any_hit, int n_threads, orc_stats* stats);
 
-/* find_all_triangles (vox.cpp:333): every accepted triangle along the ray,
-   sorted by (t, id). Returns the count; writes up to cap hits. */
+/* find_all_triangles (vox.cpp:333): every accepted triangle along the ray
+   (t < t_far), sorted by (t, id); through the BVH or by brute force.
+   Returns the count; writes up to cap hits. */
 uint32_t orc_find_all(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap);
+uint32_t orc_find_all_brute(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap);
 
 /* ---- canvas.cpp ---- */
 void orc_fill_background(uint32_t* bg, uint32_t w, uint32_t h, uint32_t clr_top, uint32_t clr_bottom);
@@ -147,6 +149,17 @@ void orc_make_matcap(int type, uint32_t* pixels, uint32_t* cavity_clr);
 
 /* view.cpp:439-480 picking helpers */
 uint32_t orc_get_closest_vertex(const orc_pixel* p, const float* vertices, const uint32_t* tris);
+/* view.cpp:439-459 (mesh branch): world position of the pixel's hit point */
+void orc_get_world_position(const orc_pixel* p, const float* vertices, const uint32_t* tris, const float cs[16],
+                            float out[3]);
+
+/* vox.cpp:284-380 (the voxel grid of write_vox): grid dims from max_dim and
+   the mesh bbox, three axis-aligned ray sweeps with find_all_triangles, each
+   hit's voxel set to its colour index; writes in sweep order, hits in (t, id)
+   order, the last write of a voxel wins. Colours: uv + texture if set, else
+   vertex colours if set, else white. Returns the voxel count (dims product);
+   fills dims and, if out != NULL and cap is large enough, the voxels. */
+uint64_t orc_voxelize(const orc_mesh* m, uint32_t max_dim, uint32_t dims[3], uint8_t* out, uint64_t cap);
 
 #ifdef __cplusplus
 }

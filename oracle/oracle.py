@@ -72,6 +72,9 @@ _SIG = {
     "orc_mesh_set_texture": (None, [_P, _P, _U, _U]),
     "orc_find_closest": (None, [C.POINTER(Instance), _U, _P, _U, _P, _I, _I, _I, C.POINTER(Stats)]),
     "orc_find_all": (_U, [_P, _P, _P, _U]),
+    "orc_find_all_brute": (_U, [_P, _P, _P, _U]),
+    "orc_get_world_position": (None, [_P, _P, _P, _P, _P]),
+    "orc_voxelize": (C.c_uint64, [_P, _U, _P, _P, C.c_uint64]),
     "orc_fill_background": (None, [_P, _U, _U, _U, _U]),
     "orc_update_canvas": (None, [_P, _U, _U, _I, _I, _I, _I, C.POINTER(Instance), _U, C.POINTER(View),
                                  C.POINTER(Settings), _I, C.POINTER(Stats)]),
@@ -286,11 +289,29 @@ def find_closest(objs, rays: np.ndarray, brute: bool = False, any_hit: bool = Fa
     return hits, st
 
 
-def find_all(mesh: Mesh, ray: np.ndarray, cap: int = 4096) -> np.ndarray:
+def find_all(mesh: Mesh, ray: np.ndarray, cap: int = 4096, brute: bool = False) -> np.ndarray:
+    """find_all_triangles (vox.cpp:333): hits sorted by (t, id)."""
     hits = np.zeros(cap, HIT_DTYPE)
-    r = np.ascontiguousarray(ray.reshape(1), RAY_DTYPE)
-    n = lib().orc_find_all(mesh.h, _p(r), _p(hits), cap)
+    r = np.ascontiguousarray(np.asarray(ray).reshape(1), RAY_DTYPE)
+    f = lib().orc_find_all_brute if brute else lib().orc_find_all
+    n = f(mesh.h, _p(r), _p(hits), cap)
     return hits[:min(n, cap)]
+
+
+def get_world_position(p: np.ndarray, V: np.ndarray, T: np.ndarray, cs: np.ndarray) -> np.ndarray:
+    rec = np.ascontiguousarray(np.asarray(p).reshape(1), PIXEL_DTYPE)
+    out = np.zeros(3, np.float32)
+    lib().orc_get_world_position(_p(rec), _p(V), _p(T), _p(np.ascontiguousarray(cs, np.float32)), _p(out))
+    return out
+
+
+def voxelize(mesh: Mesh, max_dim: int) -> np.ndarray:
+    """The voxel grid of write_vox (vox.cpp:284-380) as uint8[z, y, x]."""
+    dims = np.zeros(3, np.uint32)
+    total = lib().orc_voxelize(mesh.h, max_dim, _p(dims), None, 0)
+    out = np.zeros(total, np.uint8)
+    lib().orc_voxelize(mesh.h, max_dim, _p(dims), _p(out), total)
+    return out.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
 
 
 def update_canvas(pix: np.ndarray, objs, v: View, s: Settings, rect=None, n_threads: int | None = None) -> Stats:

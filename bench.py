@@ -356,6 +356,95 @@ def run_own(args):
     return 0
 
 
+def run_batch(args):
+    """Batched frames (64 meshes of uneven size x 16 cameras, mixed resolutions):
+    per-frame launches vs one persistent launch vs a replayed CUDA graph, with
+    leaf size and block shape from the autotuner."""
+    import torch
+
+    from j3d_gb300 import (Batch, Canvas, Context, Matcap, Mesh, Scene, build as B, camera_for_vfov,
+                           render_batch, settings, workloads as Wk)
+    from j3d_gb300.autotune import Autotuner, bucket_of
+    B.build()
+    wl = Wk.config2(args.batch_meshes, args.batch_cameras)
+    ctx = Context(0)
+    tuner = Autotuner(ctx)
+    t0 = time.perf_counter()
+    buckets = {}
+    for V, T in wl.meshes:
+        buckets.setdefault(bucket_of(len(T)), (V, T))
+    for b, (V, T) in sorted(buckets.items()):
+        tuner.tune(V, T, wl.poses[0][:4], resolution=(384, 384), repeats=2)
+    tune_s = time.perf_counter() - t0
+    weights = {b: 0.0 for b in buckets}
+    for V, T in wl.meshes:
+        weights[bucket_of(len(T))] += len(T)
+    heavy = max(weights, key=weights.get)
+    ctx.set_batch_block(tuner.table[heavy].block_threads)
+    t0 = time.perf_counter()
+    meshes = [Mesh(ctx, V, T, tuner.table[bucket_of(len(T))].leaf_size) for V, T in wl.meshes]
+    ctx.synchronize()
+    build_s = time.perf_counter() - t0
+    build_ms = sum(m.info().build_ms for m in meshes)
+    mc = Matcap.make(ctx, 0)
+    cam = camera_for_vfov(60.0)
+    frames = []
+    k = 0
+    for i, m in enumerate(meshes):
+        for c in range(args.batch_cameras):
+            sc = Scene()
+            sc.add_object(m, db_id=i + 1)
+            sc.prepare_scene()
+            sc.unzoom()
+            sc.set_pose(wl.poses[i][c])
+            cv = Canvas(ctx, *wl.resolutions[k])
+            cv.set_camera(cam)
+            cv.set_background_color()
+            cv.update_settings(settings(shadow=True, edges=False))
+            frames.append((cv, sc, mc))
+            k += 1
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    render_batch(ctx, frames)
+    ctx.synchronize()
+    prim = sum(cv.width * cv.height for cv, _, _ in frames)
+    shadow = sum(cv.count_hits()[0] for cv, _, _ in frames)
+    rays = prim + shadow
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_single = timed(lambda: [cv.render_frame(sc, m) for cv, sc, m in frames], args.steps)
+    ms_batch = timed(lambda: render_batch(ctx, frames), args.steps)
+    g = Batch(ctx, frames)
+    ms_graph = timed(g.launch, args.steps)
+    line = {"metric": "Mrays/s, batched frames (config 2)", "value": round(rays / (ms_graph / 1e3) / 1e6, 3),
+            "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_graph, 3), "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded icospheres and tori)",
+            "config": {"workload": wl.name, "frames": len(frames), "triangles_total": int(sum(len(T) for _, T in wl.meshes)),
+                       "rays_per_step": rays, "pixels_per_step": prim,
+                       "per_frame_launches_ms": round(ms_single, 3), "one_launch_ms": round(ms_batch, 3),
+                       "graph_ms": round(ms_graph, 3), "per_frame_launches_mrays_s": round(rays / ms_single / 1e3, 3),
+                       "one_launch_mrays_s": round(rays / ms_batch / 1e3, 3),
+                       "builds_ms_device": round(build_ms, 2), "builds_wall_s": round(build_s, 3),
+                       "autotune_s": round(tune_s, 2),
+                       "autotune": {str(b): [c.leaf_size, c.block_threads, round(c.ms_per_frame, 4)]
+                                    for b, c in sorted(tuner.table.items())},
+                       "block_threads": tuner.table[heavy].block_threads}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,7 +455,13 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="torus", choices=["torus", "batch"],
+                    help="torus: the headline 28M-triangle frames; batch: config-2 batched frames")
+    ap.add_argument("--batch-meshes", type=int, default=64)
+    ap.add_argument("--batch-cameras", type=int, default=16)
     args = ap.parse_args()
+    if args.workload == "batch":
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

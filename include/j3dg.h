@@ -249,8 +249,41 @@ int j3dg_canvas_get_pixels(j3dg_canvas* c, j3dg_pixel* dst);
 int j3dg_canvas_get_image(j3dg_canvas* c, uint32_t* dst);
 /* Upload a caller G-buffer into the canvas (w x h records). */
 int j3dg_canvas_set_pixels(j3dg_canvas* c, const j3dg_pixel* src);
+/* Counts the canvas's G-buffer records with a hit and with the shadow bit
+   (no reference counterpart; for ray accounting without a copy-out). */
+int j3dg_canvas_count_hits(j3dg_canvas* c, uint64_t* hits, uint64_t* shadowed);
 /* Device pointers of the canvas buffers (valid until resize/destroy). */
 int j3dg_canvas_device_buffers(j3dg_canvas* c, j3dg_pixel** pixels, uint32_t** image, uint32_t** background);
+
+/* ---------------------------------------------------------------- batches
+   No reference counterpart (j3d renders one canvas per call): many frames,
+   each its own canvas (any resolution), scene and matcap, rendered by one
+   persistent launch over all their pixels, so uneven frames share the GPU
+   with a single tail. Shading modes other than plain add one shading pass
+   per such frame. Canvases of one batch must be distinct. */
+typedef struct j3dg_frame {
+  j3dg_canvas* canvas;
+  const j3dg_scene* scene;
+  const j3dg_matcap* matcap;
+} j3dg_frame;
+
+typedef struct j3dg_batch j3dg_batch;
+
+/* One-shot: packs the frames' parameters, one upload, one launch. Async. */
+int j3dg_render_batch(j3dg_ctx* ctx, const j3dg_frame* frames, uint32_t n);
+/* Block shape of batched launches (64, 128 or 256 threads; default 128),
+   for an autotuner. Applies to batches created or rendered afterwards. */
+int j3dg_ctx_set_batch_block(j3dg_ctx* ctx, int threads);
+/* A fixed set of frames captured once as a CUDA graph (parameter upload,
+   counter reset, the persistent launch, shading passes); replayed by
+   j3dg_batch_launch. */
+int j3dg_batch_create(j3dg_ctx* ctx, const j3dg_frame* frames, uint32_t n, j3dg_batch** out);
+/* Replaces frame i's scene (camera pose, objects) for the next launches; the
+   number of objects must not exceed the one given at creation. Waits for
+   the previous launch of this batch. */
+int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* scene);
+int j3dg_batch_launch(j3dg_batch* b);
+int j3dg_batch_destroy(j3dg_batch* b);
 
 /* ---------------------------------------------------- host-side j3d math --
    Plain C++ (no GPU), the same fp32 operation order as the device code. */

@@ -58,6 +58,10 @@ class CanvasSettings(C.Structure):
                 ("reserved", C.c_uint8)]
 
 
+class Frame(C.Structure):
+    _fields_ = [("canvas", C.c_void_p), ("scene", C.POINTER(Scene)), ("matcap", C.c_void_p)]
+
+
 class BuildOpts(C.Structure):
     _fields_ = [("leaf_size", C.c_uint32), ("flags", C.c_uint32)]
 
@@ -116,7 +120,14 @@ SIGNATURES = {
     "j3dg_canvas_get_pixels": (_I, [_P, _P]),
     "j3dg_canvas_get_image": (_I, [_P, _P]),
     "j3dg_canvas_set_pixels": (_I, [_P, _P]),
+    "j3dg_canvas_count_hits": (_I, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "j3dg_canvas_device_buffers": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "j3dg_render_batch": (_I, [_P, C.POINTER(Frame), _U]),
+    "j3dg_ctx_set_batch_block": (_I, [_P, _I]),
+    "j3dg_batch_create": (_I, [_P, C.POINTER(Frame), _U, C.POINTER(_P)]),
+    "j3dg_batch_set_scene": (_I, [_P, _U, C.POINTER(Scene)]),
+    "j3dg_batch_launch": (_I, [_P]),
+    "j3dg_batch_destroy": (_I, [_P]),
     "j3dg_make_default_camera": (None, [C.POINTER(Camera)]),
     "j3dg_make_projection_matrix": (None, [C.POINTER(Camera), _I, _I, _FP]),
     "j3dg_invert_projection_matrix": (None, [_FP, _FP]),

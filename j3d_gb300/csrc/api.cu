@@ -40,6 +40,7 @@ struct CtxExtra {
   unsigned long long* d_counters = nullptr;
   uint32_t* d_ray_counter = nullptr;  // work counter of ray-batch queries
   bool counting = false;
+  int batch_threads = 128;            // block shape of batched launches
 };
 
 int fail(j3dg_ctx* c, int code, const std::string& msg) {
@@ -306,7 +307,7 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
   c->stream = st;
   bool ok = cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
-            cudaMalloc((void**)&A->ex.d_counters, 2 * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc((void**)&A->ex.d_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_ray_counter, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(A->ex.d_counters, 0, 2 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaEventCreate(&A->ex.ev0) == cudaSuccess && cudaEventCreate(&A->ex.ev1) == cudaSuccess;
@@ -364,6 +365,12 @@ void* j3dg_ctx_stream(j3dg_ctx* c) { return c ? c->stream : nullptr; }
 int j3dg_ctx_set_counting(j3dg_ctx* c, int enable) {
   if (!c) return J3DG_ERR_INVALID_ARGUMENT;
   all(c)->ex.counting = enable != 0;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_set_batch_block(j3dg_ctx* c, int threads) {
+  if (!c || (threads != 64 && threads != 128 && threads != 256)) return J3DG_ERR_INVALID_ARGUMENT;
+  all(c)->ex.batch_threads = threads;
   return J3DG_OK;
 }
 
@@ -840,6 +847,214 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   return J3DG_OK;
 }
 
+// ----------------------------------------------------------------- batches
+
+namespace {
+
+// Packed batch parameters: [FrameParams x n][offsets x (n+1), padded][DevInst x m]
+struct BatchLayout {
+  size_t off_params = 0, off_offsets = 0, off_inst = 0, bytes = 0;
+  uint32_t n = 0, n_inst = 0;
+  void set(uint32_t frames, uint32_t inst) {
+    n = frames;
+    n_inst = inst;
+    off_params = 0;
+    off_offsets = (sizeof(FrameParams) * n + 255) & ~size_t(255);
+    off_inst = (off_offsets + sizeof(uint32_t) * (n + 1) + 255) & ~size_t(255);
+    bytes = off_inst + sizeof(DevInst) * (inst ? inst : 1);
+  }
+};
+
+int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_inst) {
+  total_inst = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!f[i].canvas || !f[i].matcap) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: frame without canvas or matcap");
+    if (f[i].canvas->ctx != c || f[i].matcap->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: object of another context");
+    for (uint32_t j = 0; j < i; ++j)
+      if (f[j].canvas == f[i].canvas) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: a canvas appears twice");
+    if (f[i].scene) {
+      if (int rc = scene_ok(c, f[i].scene)) return rc;
+      for (uint32_t k = 0; k < f[i].scene->n_objects; ++k)
+        if (!f[i].scene->objects[k].mesh || f[i].scene->objects[k].mesh->ctx != c)
+          return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: bad scene object");
+      total_inst += f[i].scene->n_objects;
+    }
+  }
+  return J3DG_OK;
+}
+
+// Fills host staging `h` for device base `d` (pointers inside point to `d`).
+// Frame i's objects take cap[i] instance slots (its object count if cap is null).
+void pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h, char* d,
+                 const uint32_t* cap = nullptr) {
+  FrameParams* P = reinterpret_cast<FrameParams*>(h + L.off_params);
+  uint32_t* off = reinterpret_cast<uint32_t*>(h + L.off_offsets);
+  DevInst* I = reinterpret_cast<DevInst*>(h + L.off_inst);
+  DevInst* dI = reinterpret_cast<DevInst*>(d + L.off_inst);
+  uint32_t k = 0, items = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const j3dg_scene* s = f[i].scene;
+    const uint32_t ni = s ? s->n_objects : 0;
+    for (uint32_t j = 0; j < ni; ++j) I[k + j] = to_dev(s->objects[j]);
+    fill_frame(P[i], f[i].canvas, s, ni ? dI + k : nullptr, f[i].matcap);
+    P[i].shade_mode = shade_mode_of(f[i].canvas->settings) == 0 ? 1 : 0;
+    k += cap ? cap[i] : ni;
+    off[i] = items;
+    items += f[i].canvas->w && f[i].canvas->h ? j3dg::primary_items(P[i]) : 0u;
+  }
+  off[n] = items;
+}
+
+int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* d, uint32_t* work) {
+  const FrameParams* dP = reinterpret_cast<const FrameParams*>(d + L.off_params);
+  const uint32_t* dOff = reinterpret_cast<const uint32_t*>(d + L.off_offsets);
+  CK(c, j3dg::launch_render_batch(dP, dOff, n, work, all(c)->ex.batch_threads, S(c)), "batch");
+  for (uint32_t i = 0; i < n; ++i) {
+    const int mode = shade_mode_of(f[i].canvas->settings);
+    if (mode != 0 && f[i].canvas->w && f[i].canvas->h) {
+      FrameParams P;
+      fill_frame(P, f[i].canvas, f[i].scene, nullptr, f[i].matcap);
+      CK(c, j3dg::launch_shade(P, (const j3dg_pixel*)f[i].canvas->d_pixels, mode, 1, S(c)), "batch");
+    }
+  }
+  return J3DG_OK;
+}
+
+}  // namespace
+
+struct j3dg_batch {
+  j3dg_ctx* ctx = nullptr;
+  std::vector<j3dg_frame> frames;
+  std::vector<std::vector<j3dg_instance>> objects;  // copies of each frame's objects
+  std::vector<j3dg_scene> scenes;
+  std::vector<uint32_t> caps;  // instance slots of each frame (its object count at creation)
+  BatchLayout L;
+  char* h = nullptr;  // pinned staging
+  char* d = nullptr;  // device copy
+  uint32_t* work = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
+  if (!c || (n && !f)) return J3DG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return J3DG_OK;
+  cudaSetDevice(c->device);
+  uint32_t total_inst = 0;
+  if (int rc = check_frames(c, f, n, total_inst)) return rc;
+  BatchLayout L;
+  L.set(n, total_inst);
+  char* d = nullptr;
+  uint32_t* work = nullptr;
+  std::vector<char> h(L.bytes);
+  CK(c, cudaMallocAsync((void**)&d, L.bytes + 256, S(c)), "render_batch");
+  work = reinterpret_cast<uint32_t*>(d + L.bytes);
+  pack_frames(f, n, L, h.data(), d);
+  // pageable source: the copy is staged before the call returns
+  CK(c, cudaMemcpyAsync(d, h.data(), L.bytes, cudaMemcpyHostToDevice, S(c)), "render_batch");
+  int rc = enqueue_batch(c, f, n, L, d, work);
+  cudaFreeAsync(d, S(c));
+  return rc;
+}
+
+int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch** out) {
+  if (!c || !out || n == 0 || !f) return J3DG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaSetDevice(c->device);
+  uint32_t total_inst = 0;
+  if (int rc = check_frames(c, f, n, total_inst)) return rc;
+  j3dg_batch* b = new (std::nothrow) j3dg_batch();
+  if (!b) return J3DG_ERR_OUT_OF_MEMORY;
+  b->ctx = c;
+  b->frames.assign(f, f + n);
+  b->objects.resize(n);
+  b->scenes.resize(n);
+  b->caps.assign(n, 0u);
+  for (uint32_t i = 0; i < n; ++i) {
+    b->caps[i] = f[i].scene ? f[i].scene->n_objects : 0u;
+    if (f[i].scene) {
+      b->scenes[i] = *f[i].scene;
+      b->objects[i].assign(f[i].scene->objects, f[i].scene->objects + f[i].scene->n_objects);
+      b->scenes[i].objects = b->objects[i].data();
+      b->frames[i].scene = &b->scenes[i];
+    }
+  }
+  b->L.set(n, total_inst);
+  cudaError_t e = cudaMallocHost((void**)&b->h, b->L.bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d, b->L.bytes + 256);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    j3dg_batch_destroy(b);
+    return cuda_fail(c, e, "batch_create");
+  }
+  b->work = reinterpret_cast<uint32_t*>(b->d + b->L.bytes);
+  pack_frames(b->frames.data(), n, b->L, b->h, b->d);
+  // capture: upload of the staged parameters, the launch and the shading passes
+  cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  e = cudaStreamBeginCapture(S(c), mode);
+  int rc = J3DG_OK;
+  if (e == cudaSuccess) {
+    e = cudaMemcpyAsync(b->d, b->h, b->L.bytes, cudaMemcpyHostToDevice, S(c));
+    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, b->work);
+    cudaError_t e2 = cudaStreamEndCapture(S(c), &b->graph);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess && rc == J3DG_OK) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess || rc != J3DG_OK) {
+    j3dg_batch_destroy(b);
+    return rc != J3DG_OK ? rc : cuda_fail(c, e, "batch_create");
+  }
+  *out = b;
+  return J3DG_OK;
+}
+
+int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* s) {
+  if (!b || i >= b->frames.size() || !s) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = b->ctx;
+  if (int rc = scene_ok(c, s)) return rc;
+  const uint32_t cap = b->caps[i];
+  if (s->n_objects > cap) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_set_scene: more objects than at creation");
+  for (uint32_t k = 0; k < s->n_objects; ++k)
+    if (!s->objects[k].mesh || s->objects[k].mesh->ctx != c)
+      return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_set_scene: bad scene object");
+  cudaSetDevice(c->device);
+  CK(c, cudaEventSynchronize(b->done), "batch_set_scene");  // the staging is read by the running launch
+  b->objects[i].assign(s->objects, s->objects + s->n_objects);
+  b->scenes[i] = *s;
+  b->scenes[i].objects = b->objects[i].data();
+  // frame k keeps the instance slots it had at creation
+  std::vector<uint32_t> caps(b->frames.size());
+  for (size_t k = 0; k < caps.size(); ++k) caps[k] = b->caps[k];
+  std::vector<j3dg_frame> fr = b->frames;
+  for (size_t k = 0; k < fr.size(); ++k)
+    if (fr[k].scene) fr[k].scene = &b->scenes[k];
+  pack_frames(fr.data(), (uint32_t)fr.size(), b->L, b->h, b->d, caps.data());
+  return J3DG_OK;
+}
+
+int j3dg_batch_launch(j3dg_batch* b) {
+  if (!b) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = b->ctx;
+  cudaSetDevice(c->device);
+  CK(c, cudaGraphLaunch(b->exec, S(c)), "batch_launch");
+  CK(c, cudaEventRecord(b->done, S(c)), "batch_launch");
+  return J3DG_OK;
+}
+
+int j3dg_batch_destroy(j3dg_batch* b) {
+  if (!b) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(S(b->ctx));
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->done) cudaEventDestroy(b->done);
+  cudaFree(b->d);
+  if (b->h) cudaFreeHost(b->h);
+  delete b;
+  return J3DG_OK;
+}
+
 int j3dg_canvas_get_pixels(j3dg_canvas* cv, j3dg_pixel* dst) {
   if (!cv || !dst) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(cv->ctx->device);
@@ -860,6 +1075,20 @@ int j3dg_canvas_set_pixels(j3dg_canvas* cv, const j3dg_pixel* src) {
                         is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c)),
      "set_pixels");
   CK(c, cudaStreamSynchronize(S(c)), "set_pixels");
+  return J3DG_OK;
+}
+
+int j3dg_canvas_count_hits(j3dg_canvas* cv, uint64_t* hits, uint64_t* shadowed) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  cudaSetDevice(c->device);
+  unsigned long long* d = all(c)->ex.d_counters + 2;
+  unsigned long long h[2] = {0, 0};
+  CK(c, j3dg::launch_count_hits((const j3dg_pixel*)cv->d_pixels, (size_t)cv->w * cv->h, d, S(c)), "count_hits");
+  CK(c, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, S(c)), "count_hits");
+  CK(c, cudaStreamSynchronize(S(c)), "count_hits");
+  if (hits) *hits = h[0];
+  if (shadowed) *shadowed = h[1];
   return J3DG_OK;
 }
 

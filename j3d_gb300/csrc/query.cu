@@ -242,3 +242,32 @@ cudaError_t launch_voxelize(const DevInst* inst, const VoxParams& V, uint32_t* k
 }
 
 }  // namespace j3dg
+
+namespace j3dg {
+
+// Counts G-buffer records with a hit (object_id != ~0) and with the shadow bit.
+__global__ void k_count_hits(const j3dg_pixel* __restrict__ G, size_t n, unsigned long long* out) {
+  unsigned long long hits = 0, shadowed = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t id = G[i].object_id;
+    hits += id != 0xffffffffu;
+    shadowed += id != 0xffffffffu && (G[i].mark & 1u);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    hits += __shfl_xor_sync(0xffffffffu, hits, o);
+    shadowed += __shfl_xor_sync(0xffffffffu, shadowed, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, hits);
+    atomicAdd(out + 1, shadowed);
+  }
+}
+
+cudaError_t launch_count_hits(const j3dg_pixel* G, size_t n, unsigned long long* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess || n == 0) return e;
+  k_count_hits<<<256, 256, 0, st>>>(G, n, out);
+  return cudaGetLastError();
+}
+
+}  // namespace j3dg

@@ -22,4 +22,6 @@ cudaError_t launch_find_all(const DevInst* inst, const j3dg_ray* rays, uint32_t 
 cudaError_t launch_voxelize(const DevInst* inst, const VoxParams& V, uint32_t* keys, uint8_t* out, uint32_t* status,
                             cudaStream_t st);
 
+cudaError_t launch_count_hits(const j3dg_pixel* G, size_t n, unsigned long long* out, cudaStream_t st);
+
 }  // namespace j3dg

@@ -340,12 +340,101 @@ __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restric
   persistent_trace<kIters>(src, inst, n_inst, counter, status, nullptr);
 }
 
+// Many frames (canvases, scenes, cameras, resolutions of uneven size) in one
+// persistent launch: the pixel lists of all frames are concatenated
+// (offsets[f] = first work item of frame f, offsets[n] = total) and lanes
+// refill from the one list, so small and large frames share the GPU with a
+// single tail. Per-frame parameters live in device memory.
+// blocks per SM that keep registers at or under ~96 for a block of TPB threads
+template <int TPB>
+struct MinBlocks {
+  static const int value = TPB >= 256 ? 2 : (TPB >= 128 ? 5 : 10);
+};
+
+template <int TPB>
+__global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
+    k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
+                  uint32_t* work) {
+  Tracer T;
+  uint32_t stack_ref[J3DG_STACK];
+  float stack_t[J3DG_STACK];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t total = offsets[n_frames];
+  int phase = 0;
+  bool exhausted = false;
+  uint32_t frame = 0;
+  size_t pix = 0;
+  uint32_t w0 = 0;
+  float su = 0.f, sv = 0.f;
+  uint32_t visits = 0, tests = 0;
+#pragma unroll 1
+  for (;;) {
+    const bool need = phase == 0 && !exhausted;
+    const uint32_t m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(work, (uint32_t)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t my = base + __popc(m & ((1u << lane) - 1u));
+        if (my >= total) {
+          exhausted = true;
+        } else {
+          uint32_t lo = 0, hi = n_frames;  // offsets[lo] <= my < offsets[hi]
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(offsets + mid) <= my)
+              lo = mid;
+            else
+              hi = mid;
+          }
+          frame = lo;
+          const FrameParams& P = params[frame];
+          int x, y;
+          if (item_pixel(P, my - __ldg(offsets + frame), x, y)) {
+            pix = (size_t)y * P.w + x;
+            if (P.n_inst == 0) {
+              write_miss(P, pix);
+            } else {
+              primary_begin(P, T, x, y);
+              phase = 1;
+            }
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
+#pragma unroll 1
+    for (;;) {
+      if (phase != 0) {
+        const FrameParams& P = params[frame];
+        if (T.step(P.inst, P.n_inst, P.status, visits, tests, stack_ref, stack_t)) {
+          if (phase == 1) {
+            phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
+          } else {
+            shadow_finish(P, T, pix, w0, su, sv);
+            phase = 0;
+          }
+        }
+      }
+      if (__all_sync(0xffffffffu, phase == 0)) break;
+      if (__popc(__ballot_sync(0xffffffffu, phase == 0 && !exhausted)) >= J3DG_REFILL_AT) break;
+    }
+  }
+  unsigned long long* counters = params[0].counters;
+  if (counters) {
+    atomicAdd(counters + 0, (unsigned long long)visits);
+    atomicAdd(counters + 1, (unsigned long long)tests);
+  }
+}
+
 template <class K>
-static int persistent_blocks(K* kernel) {
+static int persistent_blocks(K* kernel, int threads = kTraceThreads) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kTraceThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
   return sms * (per > 0 ? per : 1);
 }
 
@@ -490,6 +579,31 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   k_frame<<<blocks, kTraceThreads, 0, st>>>(P);
   return cudaGetLastError();
+}
+
+cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
+                                uint32_t* work, int block_threads, cudaStream_t st) {
+  if (n_frames == 0) return cudaSuccess;
+  static int b64 = 0, b128 = 0, b256 = 0;
+  if (!b64) {
+    b64 = persistent_blocks(k_frame_batch<64>, 64);
+    b128 = persistent_blocks(k_frame_batch<128>, 128);
+    b256 = persistent_blocks(k_frame_batch<256>, 256);
+  }
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (block_threads == 64)
+    k_frame_batch<64><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
+  else if (block_threads == 256)
+    k_frame_batch<256><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
+  else
+    k_frame_batch<128><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
+  return cudaGetLastError();
+}
+
+uint32_t primary_items(const FrameParams& P) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
 }
 
 cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st) {

@@ -63,6 +63,9 @@ class Context:
     def set_counting(self, on: bool) -> None:
         _check(self.h, lib().j3dg_ctx_set_counting(self.h, 1 if on else 0))
 
+    def set_batch_block(self, threads: int) -> None:
+        _check(self.h, lib().j3dg_ctx_set_batch_block(self.h, threads))
+
     def read_counters(self, reset: bool = True) -> tuple[int, int]:
         out = (C.c_uint64 * 2)()
         _check(self.h, lib().j3dg_ctx_read_counters(self.h, out, 1 if reset else 0))
@@ -319,10 +322,70 @@ class Canvas:
     def set_pixels(self, px) -> None:
         _check(self.ctx.h, lib().j3dg_canvas_set_pixels(self.h, vptr(px)))
 
+    def count_hits(self) -> tuple[int, int]:
+        """(pixels with a hit, of which in shadow), counted on the device."""
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(self.ctx.h, lib().j3dg_canvas_count_hits(self.h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
     def device_buffers(self) -> tuple[int, int, int]:
         a, b, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
         _check(self.ctx.h, lib().j3dg_canvas_device_buffers(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+
+# ----------------------------------------------------------------- batches
+
+def _frames(frames):
+    arr = (_ffi.Frame * max(1, len(frames)))()
+    keep = []
+    for i, (cv, sc, mc) in enumerate(frames):
+        arr[i].canvas = cv.h
+        arr[i].matcap = mc.h
+        if sc is not None:
+            s, k = sc.as_c()
+            keep.append((s, k))
+            arr[i].scene = C.pointer(s)
+    return arr, keep
+
+
+def render_batch(ctx: Context, frames) -> None:
+    """Renders [(canvas, scene, matcap), ...] in one persistent launch (asynchronous)."""
+    arr, keep = _frames(frames)
+    _check(ctx.h, lib().j3dg_render_batch(ctx.h, arr, len(frames)))
+    del keep
+
+
+class Batch:
+    """A fixed set of frames captured as a CUDA graph; set_scene() moves cameras."""
+
+    def __init__(self, ctx: Context, frames):
+        self.ctx = ctx
+        self.frames = list(frames)
+        arr, keep = _frames(self.frames)
+        h = C.c_void_p()
+        _check(ctx.h, lib().j3dg_batch_create(ctx.h, arr, len(self.frames), C.byref(h)))
+        self.h = h
+        del keep
+
+    def set_scene(self, i: int, scene: "Scene") -> None:
+        s, keep = scene.as_c()
+        _check(self.ctx.h, lib().j3dg_batch_set_scene(self.h, i, C.byref(s)))
+        del keep
+
+    def launch(self) -> None:
+        _check(self.ctx.h, lib().j3dg_batch_launch(self.h))
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------- ray queries
@@ -428,6 +491,7 @@ def camera_for_vfov(vfov_deg: float) -> Camera:
 
 
 __all__ = ["Context", "Mesh", "Scene", "SceneObject", "Matcap", "Canvas", "settings", "find_closest", "find_all",
+           "render_batch", "Batch",
            "voxelize", "get_closest_vertex", "get_world_position",
            "make_default_camera", "make_projection_matrix", "invert_projection_matrix", "invert_orthonormal",
            "make_matcap", "fill_background", "camera_for_vfov", "PIXEL_DTYPE", "RAY_DTYPE", "HIT_DTYPE",

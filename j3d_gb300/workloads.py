@@ -94,3 +94,34 @@ def config1(n_cameras: int = 32, width: int = 1920, height: int = 1080, nu: int 
     poses = cameras(n_cameras, SEED_BASE + 1 + (1 << 32), 2.5, 4.0)
     return Workload("torus-%dx%d-%dtris-%dx%d-x%d" % (nu, nv, 2 * nu * nv, width, height, n_cameras), V, T, poses,
                     width, height)
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    meshes: list            # (V, T) per mesh
+    poses: np.ndarray       # (n_meshes, n_cameras, 16)
+    resolutions: list       # per (mesh, camera): (w, h)
+
+
+def config2(n_meshes: int = 64, n_cameras: int = 16, t_min: float = 1e4, t_max: float = 2e6,
+            seed: int = SEED_BASE + 2) -> BatchWorkload:
+    """Batched frames: n_meshes meshes with triangle counts log-uniform in
+    [t_min, t_max] (an icosphere level when one lands within 15 %, else a
+    torus grid), n_cameras seeded cameras each, resolutions drawn from
+    {256^2, 512^2, 768x512, 1024^2}. Draws: per mesh its count then kind; per
+    frame its resolution index (numpy PCG64 seeded with `seed`)."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for i in range(n_meshes):
+        t = float(np.exp(rng.uniform(np.log(t_min), np.log(t_max))))
+        lvl = int(round(np.log(t / 20.0) / np.log(4.0)))
+        if 0 <= lvl <= 9 and abs(20 * 4 ** lvl - t) <= 0.15 * t:
+            meshes.append(icosphere(lvl, seed + 100 + i))
+        else:
+            nu, nv = torus_grid_for(int(t))
+            meshes.append(torus(nu, nv, seed=seed + 100 + i))
+    poses = np.stack([cameras(n_cameras, seed + 1000 + i, 2.5, 4.0) for i in range(n_meshes)])
+    choices = [(256, 256), (512, 512), (768, 512), (1024, 1024)]
+    res = [choices[int(rng.integers(0, 4))] for _ in range(n_meshes * n_cameras)]
+    return BatchWorkload("batch-%dmeshes-x%dcams" % (n_meshes, n_cameras), meshes, poses, res)

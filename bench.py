@@ -445,6 +445,48 @@ def run_batch(args):
     return 0
 
 
+def run_serve(args):
+    """Serving (config 4): 8 resident tori (200k .. 28M triangles), Poisson
+    render requests at 400/s, resolutions {512^2, 1280x720, 1920x1080},
+    admission by HBM footprint (150 GB, then a cap that binds)."""
+    from j3d_gb300 import Context, build as B, workloads as Wk
+    from j3d_gb300.serve import CanvasPool, RenderServer, poisson_requests
+    B.build()
+    ctx = Context(0)
+    sizes = [200_000, 500_000, 1_000_000, 2_000_000, 5_000_000, 10_000_000, 20_000_000, 28_090_000]
+    out = {}
+    for cap_name in ("150GB", "binding"):
+        srv = RenderServer(ctx, 150 << 30, max_slots=64, max_in_flight=2)
+        for i, t in enumerate(sizes):
+            nu, nv = (5300, 2650) if t == 28_090_000 else Wk.torus_grid_for(t)
+            assert srv.add_mesh(f"torus{t}", *Wk.torus(nu, nv, seed=Wk.SEED_BASE + 4 + i))
+        if cap_name == "binding":
+            srv.cap = srv.mesh_bytes + 3 * CanvasPool.canvas_bytes(1920, 1080)
+        names = list(srv.meshes)
+        warm = poisson_requests(64, args.serve_rate * 4, names, seed=Wk.SEED_BASE + 40)
+        srv.run(warm, realtime=True)
+        reqs = poisson_requests(args.serve_requests, args.serve_rate, names, seed=Wk.SEED_BASE + 41)
+        st = srv.run(reqs, realtime=True)
+        out[cap_name] = {"p50_ms": round(st.p50_ms, 3), "p99_ms": round(st.p99_ms, 3), "mean_ms": round(st.mean_ms, 3),
+                         "frames_per_s": round(st.frames_per_s, 1), "batches": st.batches,
+                         "mean_batch": round(st.mean_batch, 2), "peak_hbm_gb": round(st.peak_bytes / 2**30, 2),
+                         "cap_gb": round(srv.cap / 2**30, 2), "canvases": srv.pool.count,
+                         "resident_mesh_gb": round(srv.mesh_bytes / 2**30, 2)}
+        for c in list(srv.pool.free.values()):
+            for cv in c:
+                cv.close()
+        for m in srv.meshes.values():
+            m.close()
+    line = {"metric": "serving p50/p99 frame latency (ms) and frames/s (config 4)",
+            "value": out["150GB"]["p99_ms"], "unit": "ms (p99)", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f32", "data": "synthetic (seeded tori, Poisson arrivals)",
+            "config": {"workload": "8 tori 200k..28.09M tris, Poisson %.0f req/s, %d requests, "
+                                   "512^2 / 1280x720 / 1920x1080, primary + shadow" % (args.serve_rate, args.serve_requests),
+                       "runs": out}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -455,13 +497,18 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="torus", choices=["torus", "batch"],
-                    help="torus: the headline 28M-triangle frames; batch: config-2 batched frames")
+    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve"],
+                    help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
+                         "serve: config-4 request serving")
+    ap.add_argument("--serve-rate", type=float, default=400.0)
+    ap.add_argument("--serve-requests", type=int, default=1200)
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--batch-cameras", type=int, default=16)
     args = ap.parse_args()
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

@@ -493,7 +493,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--leaf", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")

@@ -126,7 +126,7 @@ typedef struct j3dg_canvas_settings {
 
 /* BVH build options (NULL = defaults). */
 typedef struct j3dg_build_opts {
-  uint32_t leaf_size;  /* max triangles per leaf, 1..8 (default 4) */
+  uint32_t leaf_size;  /* max triangles per leaf, 1..8 (default 2: fastest on the torus frames) */
   uint32_t flags;      /* reserved, 0 */
 } j3dg_build_opts;
 

@@ -90,7 +90,7 @@ struct scene {
 // add_object (scene.cpp:8-38): normals, bbox and the BVH, built on the GPU.
 inline void add_object(context& ctx, uint32_t id, scene& s, const float* vertices, uint32_t n_vertices,
                        const uint32_t* triangles, uint32_t n_triangles, const float* cs = nullptr,
-                       uint32_t leaf_size = 4) {
+                       uint32_t leaf_size = 2) {
   scene_object o;
   o.db_id = id;
   if (cs)

@@ -394,7 +394,7 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   *out = nullptr;
   if (!V || !T || nv == 0 || nt == 0) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: empty mesh");
   if (nt >= J3DG_MAX_TRIANGLES) return fail(c, J3DG_ERR_UNSUPPORTED, "mesh_build: more than 2^28 triangles");
-  uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 4u;
+  uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 2u;
   if (leaf < 1 || leaf > J3DG_MAX_LEAF) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: leaf_size must be 1..8");
   cudaSetDevice(c->device);
   j3dg_mesh* m = new (std::nothrow) j3dg_mesh();

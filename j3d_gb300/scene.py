@@ -75,7 +75,7 @@ class Context:
 class Mesh:
     """scene_object's mesh + qbvh (scene.h:10-25), resident on the device."""
 
-    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 4):
+    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2):
         self.ctx = ctx
         nv = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
         nt = int(triangles.shape[0]) if triangles.ndim > 1 else int(triangles.size // 3)

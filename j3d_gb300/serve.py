@@ -80,6 +80,25 @@ class CanvasPool:
     def give(self, res, cv) -> None:
         self.free.setdefault(res, []).append(cv)
 
+    def evict(self, keep_res, nbytes: int, reserved: dict) -> int:
+        """Frees idle canvases of other resolutions (not reserved for the
+        group being formed) until nbytes are released; returns bytes freed."""
+        freed = 0
+        for res in list(self.free):
+            if res == keep_res:
+                continue
+            lst = self.free[res]
+            while lst and len(lst) > reserved.get(res, 0) and freed < nbytes:
+                cv = lst.pop()
+                cv.close()
+                self.count -= 1
+                b = self.canvas_bytes(*res)
+                self.bytes -= b
+                freed += b
+            if freed >= nbytes:
+                break
+        return freed
+
 
 class RenderServer:
     def __init__(self, ctx, hbm_cap_bytes: int, max_slots: int = 64, max_in_flight: int = 2, shadow: bool = True,
@@ -140,6 +159,9 @@ class RenderServer:
         if len(self.pool.free.get(res, [])) > reserved.get(res, 0):
             return 0
         need = CanvasPool.canvas_bytes(*res)
+        over = self.footprint() + new_bytes + need - self.cap
+        if over > 0:
+            self.pool.evict(res, over, reserved)
         return need if self.footprint() + new_bytes + need <= self.cap else -1
 
     def _launch(self, reqs: list) -> None:

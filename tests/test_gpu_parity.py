@@ -69,7 +69,7 @@ def test_icosphere_config0_parity_and_golden(gpu_ctx, oracle_mod):
             compare_rgba(gi, oi, 1, "config0 edges")
 
 
-@pytest.mark.parametrize("leaf", [1, 4, 8])
+@pytest.mark.parametrize("leaf", [1, 2, 4, 8])
 def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf):
     from j3d_gb300 import workloads as W
     O = oracle_mod

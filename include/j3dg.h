@@ -205,6 +205,27 @@ int j3dg_find_all(j3dg_ctx* ctx, const j3dg_mesh* mesh, const j3dg_ray* rays, ui
 int j3dg_voxelize(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3], uint8_t* voxels,
                   uint64_t capacity);
 
+/* No counterpart in the reference. The same voxel grid as j3dg_voxelize,
+   for callers that must not allocate device memory while they run: a
+   viewer or service that reserved its memory budget up front (for instance
+   a render server sized to its HBM cap, or a host whose device memory is
+   owned by another allocator), or a caller that cannot afford the device
+   synchronisation an allocation may cause in the middle of its work. The
+   call allocates nothing: its scratch (a 4-byte key and 1 staging byte per
+   voxel) is a fixed array inside the library, J3DG_NOALLOC_MAX_VOXELS voxels
+   (2,097,152, e.g. 128 x 128 x 128) on every GPU that loads the library,
+   kept until the process exits. Grids larger than that are rejected with
+   J3DG_ERR_INVALID_ARGUMENT and a message naming both sizes. The caller
+   passes the mesh and the output (device or host memory, capacity >= the
+   dims product). The first call on each device looks the scratch up for
+   that device; make that first call before capturing any CUDA graph. All
+   calls share the one scratch array, which keeps the last call's contents
+   (the call clears what must start at zero): calls that overlap on the GPU,
+   from two contexts or two threads, race on it. */
+#define J3DG_NOALLOC_MAX_VOXELS (1u << 21)
+int j3dg_voxelize_noalloc(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3],
+                          uint8_t* voxels, uint64_t capacity);
+
 /* ---------------------------------------------------------------- matcaps */
 
 /* matcap.h:18-24: a w x h RGBA8 texture plus its cavity colour, uploaded once. */

@@ -101,6 +101,7 @@ SIGNATURES = {
     "j3dg_find_any": (_I, [_P, C.POINTER(Instance), _U, _P, _U, _P]),
     "j3dg_find_all": (_I, [_P, _P, _P, _U, _U, _P, _P]),
     "j3dg_voxelize": (_I, [_P, _P, _U, C.POINTER(_U), _P, C.c_uint64]),
+    "j3dg_voxelize_noalloc": (_I, [_P, _P, _U, C.POINTER(_U), _P, C.c_uint64]),
     "j3dg_get_closest_vertex": (_U, [_P, _P, _P]),
     "j3dg_get_world_position": (None, [_P, _P, _P, _FP, _FP]),
     "j3dg_matcap_create": (_I, [_P, _P, _U, _U, _U, C.POINTER(_P)]),

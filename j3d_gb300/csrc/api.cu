@@ -638,6 +638,57 @@ int j3dg_voxelize(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t
   return check_status(c);
 }
 
+// Voxel grid without device allocation: the scratch is the library's
+// file-scope array (query.cu); the instance table uses the context's ring,
+// which holds one object without growing.
+int j3dg_voxelize_noalloc(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3], uint8_t* voxels,
+                          uint64_t capacity) {
+  if (!c || !mesh || !dims) return J3DG_ERR_INVALID_ARGUMENT;
+  if (max_dim == 0 || max_dim > 1024) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: max_dim must be 1..1024");
+  if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: mesh of another context");
+  cudaSetDevice(c->device);
+  const float* mn = mesh->min_bb;
+  const float* mx = mesh->max_bb;
+  int L = 0;
+  if ((mx[1] - mn[1]) > (mx[L] - mn[L])) L = 1;
+  if ((mx[2] - mn[2]) > (mx[L] - mn[L])) L = 2;
+  j3dg::VoxParams V;
+  memset(&V, 0, sizeof(V));
+  for (int j = 0; j < 3; ++j) {
+    V.dim[j] = (uint32_t)((float)max_dim * (mx[j] - mn[j]) / (mx[L] - mn[L]));
+    if (V.dim[j] == 0) V.dim[j] = 1;
+    dims[j] = V.dim[j];
+    V.mn[j] = mn[j];
+    V.mx[j] = mx[j];
+  }
+  const uint64_t total = (uint64_t)V.dim[0] * V.dim[1] * V.dim[2];
+  if (total > J3DG_NOALLOC_MAX_VOXELS)
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT,
+                "voxelize_noalloc: the grid needs " + std::to_string(total) + " voxels, the scratch holds " +
+                    std::to_string(J3DG_NOALLOC_MAX_VOXELS) + " (use j3dg_voxelize or a smaller max_dim)");
+  if (!voxels) return J3DG_OK;
+  if (capacity < total) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: capacity below dims product");
+  uint32_t* keys = nullptr;
+  uint8_t* staging = nullptr;
+  std::string err;
+  if (int rc = j3dg::voxel_scratch(c->device, &keys, &staging, err)) return fail(c, rc, err);
+  for (int d = 0; d < 3; ++d) V.rays[d] = V.dim[(d + 1) % 3] * V.dim[(d + 2) % 3];
+  V.rays_total = V.rays[0] + V.rays[1] + V.rays[2];
+  V.use_texture = mesh->d_uv && mesh->d_tex && mesh->tex_w && mesh->tex_h;
+  V.use_colors = !V.use_texture && mesh->d_colors;
+  j3dg_instance one;
+  one.mesh = mesh;
+  for (int i = 0; i < 16; ++i) one.cs[i] = (i % 5 == 0) ? 1.f : 0.f;
+  one.db_id = 0;
+  one.reserved = 0;
+  const DevInst* dinst = nullptr;
+  if (int rc = upload_instances(c, &one, 1, &dinst)) return rc;
+  const bool out_dev = is_device_ptr(voxels);
+  CK(c, j3dg::launch_voxelize(dinst, V, keys, out_dev ? voxels : staging, c->d_status, S(c)), "voxelize_noalloc");
+  if (!out_dev) CK(c, cudaMemcpyAsync(voxels, staging, total, cudaMemcpyDeviceToHost, S(c)), "voxelize_noalloc");
+  return check_status(c);
+}
+
 // --------------------------------------------------------------- matcap
 
 int j3dg_matcap_create(j3dg_ctx* c, const uint32_t* px, uint32_t w, uint32_t h, uint32_t cavity, j3dg_matcap** out) {

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/j3dg.h"
 
 namespace j3dg {
@@ -21,6 +23,12 @@ cudaError_t launch_find_all(const DevInst* inst, const j3dg_ray* rays, uint32_t 
                             uint32_t* counts, uint32_t* status, cudaStream_t st);
 cudaError_t launch_voxelize(const DevInst* inst, const VoxParams& V, uint32_t* keys, uint8_t* out, uint32_t* status,
                             cudaStream_t st);
+
+// Device addresses of the file-scope scratch of the no-allocation voxel grid
+// (keys: J3DG_NOALLOC_MAX_VOXELS words; staging: as many bytes), resolved
+// with cudaGetSymbolAddress on the first call for `device` (which must be
+// current).
+int voxel_scratch(int device, uint32_t** keys, uint8_t** staging, std::string& err);
 
 cudaError_t launch_count_hits(const j3dg_pixel* G, size_t n, unsigned long long* out, cudaStream_t st);
 

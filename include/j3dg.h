@@ -306,6 +306,47 @@ int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* scene);
 int j3dg_batch_launch(j3dg_batch* b);
 int j3dg_batch_destroy(j3dg_batch* b);
 
+/* ----------------------------------------------------------- learned tmax
+   No reference counterpart. A network predicts, from a ray, which of the
+   mesh's clusters (the BVH subtrees at cluster_depth: at most 4096, Morton-
+   ordered ranges of triangles) holds its closest hit: 16-band Fourier
+   features of origin and direction, four 128-wide GELU layers, 4096 logits;
+   bf16 weights, fp32 accumulation on the tensor cores; trained on the GPU
+   (softmax cross-entropy, Adam) on rays traced by the plain method. A
+   learned query traverses its two predicted clusters first and seeds the
+   exact traversal with their best hit: results equal j3dg_find_closest's. */
+typedef struct j3dg_learned j3dg_learned;
+typedef struct j3dg_learned_opts {
+  uint32_t cluster_depth; /* BVH depth of the clusters, 1..6 (default 6) */
+  uint32_t batch;         /* training batch, a multiple of 128 (default 16384) */
+  float lr;               /* Adam learning rate (default 2e-3) */
+  uint32_t reserved;
+  uint64_t seed;          /* weights and training rays */
+} j3dg_learned_opts;
+
+int j3dg_learned_create(j3dg_ctx* ctx, const j3dg_mesh* mesh, const j3dg_learned_opts* opts, j3dg_learned** out);
+int j3dg_learned_destroy(j3dg_learned* l);
+int j3dg_learned_info(const j3dg_learned* l, uint32_t* n_clusters, uint64_t* n_params);
+/* Trains on n_rays rays from cameras at radius r0..r1 around the mesh
+   (generated and traced on the GPU); reports the last batch's loss and
+   top-1 accuracy over its hit rays, and the wall time. */
+int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, float* final_loss, float* accuracy,
+                       float* seconds);
+/* The two most likely clusters of each ray (n x 2, host or device). */
+int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2);
+/* Closest hits through the learned tmax (host or device arrays). */
+int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits);
+/* Parameters (fp32 master copy, layout W1 b1 ... W5 b5, W row-major [in][out]). */
+int j3dg_learned_get_params(j3dg_learned* l, float* out);
+int j3dg_learned_set_params(j3dg_learned* l, const float* in);
+/* Mean loss and gradients of a batch of features (B x 256 fp32, B a
+   multiple of 128) and labels (-1 = no hit), for gradient checks. */
+int j3dg_learned_loss_grad(j3dg_learned* l, const float* features, const int32_t* labels, uint32_t B, float* loss,
+                           float* grads);
+/* Checkpoint (header + fp32 parameters). */
+int j3dg_learned_save(j3dg_learned* l, const char* path);
+int j3dg_learned_load(j3dg_learned* l, const char* path);
+
 /* ---------------------------------------------------- host-side j3d math --
    Plain C++ (no GPU), the same fp32 operation order as the device code. */
 

@@ -129,6 +129,17 @@ SIGNATURES = {
     "j3dg_batch_set_scene": (_I, [_P, _U, C.POINTER(Scene)]),
     "j3dg_batch_launch": (_I, [_P]),
     "j3dg_batch_destroy": (_I, [_P]),
+    "j3dg_learned_create": (_I, [_P, _P, _P, C.POINTER(_P)]),
+    "j3dg_learned_destroy": (_I, [_P]),
+    "j3dg_learned_info": (_I, [_P, C.POINTER(_U), C.POINTER(C.c_uint64)]),
+    "j3dg_learned_train": (_I, [_P, C.c_uint64, _F, _F, C.POINTER(_F), C.POINTER(_F), C.POINTER(_F)]),
+    "j3dg_learned_predict": (_I, [_P, _P, _U, _P]),
+    "j3dg_learned_find_closest": (_I, [_P, _P, _U, _P]),
+    "j3dg_learned_get_params": (_I, [_P, _P]),
+    "j3dg_learned_set_params": (_I, [_P, _P]),
+    "j3dg_learned_loss_grad": (_I, [_P, _P, _P, _U, C.POINTER(_F), _P]),
+    "j3dg_learned_save": (_I, [_P, C.c_char_p]),
+    "j3dg_learned_load": (_I, [_P, C.c_char_p]),
     "j3dg_make_default_camera": (None, [C.POINTER(Camera)]),
     "j3dg_make_projection_matrix": (None, [C.POINTER(Camera), _I, _I, _FP]),
     "j3dg_invert_projection_matrix": (None, [_FP, _FP]),

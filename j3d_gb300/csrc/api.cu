@@ -261,6 +261,31 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
 
 }  // namespace
 
+namespace j3dg {
+
+int ctx_fail(j3dg_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
+
+// The device instance table of one mesh with the identity transform.
+int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out) {
+  if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh of another context");
+  j3dg_instance one;
+  one.mesh = mesh;
+  for (int i = 0; i < 16; ++i) one.cs[i] = (i % 5 == 0) ? 1.f : 0.f;
+  one.db_id = 0;
+  one.reserved = 0;
+  return upload_instances(c, &one, 1, out);
+}
+
+// Plain closest hit of device rays against one mesh into device hits (async).
+int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits) {
+  const DevInst* dinst = nullptr;
+  if (int rc = mesh_devinst(c, mesh, &dinst)) return rc;
+  CK(c, launch_rays(dinst, 1, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, S(c)), "ray query");
+  return J3DG_OK;
+}
+
+}  // namespace j3dg
+
 extern "C" {
 
 int j3dg_abi_version(void) { return J3DG_ABI_VERSION; }

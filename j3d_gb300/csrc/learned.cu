@@ -1,0 +1,836 @@
+// learned.cu -- learned tmax for closest-hit traversal.
+//
+// A small network maps a ray (origin, direction) to a cluster of the mesh:
+// 16-band Fourier features of the 6 ray coordinates (192 values, padded to
+// 256), four 128-wide GELU layers, 4096 cluster logits; bf16 weights, fp32
+// accumulation (mma.sync tensor-core GEMMs of mlp_gemm.cu), trained with
+// softmax cross-entropy and Adam on rays traced by the plain method.
+// Clusters are the BVH4 subtrees at a fixed depth (depth 6: at most 4096),
+// which are Morton-ordered ranges of the mesh because the tree is an LBVH.
+//
+// A learned query traverses the two most likely clusters first; their
+// closest accepted hit seeds the exact traversal of the whole tree as its
+// best (t, triangle) so far, which only prunes: the final hit is the same
+// (bit for bit) as the plain traversal's.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/j3dg.h"
+#include "device_common.cuh"
+#include "internal.h"
+#include "mlp.cuh"
+
+namespace j3dg {
+int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits);
+int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out);
+int ctx_fail(j3dg_ctx* c, int code, const std::string& msg);
+}
+
+namespace j3dg {
+
+static const int kIn = 256;        // 192 Fourier features + zero padding
+static const int kHid = 128;
+static const int kOut = 4096;
+static const int kBands = 16;
+
+// parameter offsets in the flat vectors (W row-major [in][out])
+struct Layout {
+  size_t w[5], b[5], total;
+  int in[5], out[5];
+  Layout() {
+    const int ins[5] = {kIn, kHid, kHid, kHid, kHid}, outs[5] = {kHid, kHid, kHid, kHid, kOut};
+    size_t o = 0;
+    for (int l = 0; l < 5; ++l) {
+      in[l] = ins[l];
+      out[l] = outs[l];
+      w[l] = o;
+      o += (size_t)ins[l] * outs[l];
+      b[l] = o;
+      o += outs[l];
+    }
+    total = o;
+  }
+};
+
+// ------------------------------------------------------------------ kernels
+
+// Fourier features of (origin, direction): x_i = ((o - c) / s, d / |d|),
+// sin / cos of pi 2^(k/2) x_i for k = 0..15; features [i][k][sin, cos].
+__global__ void k_features(const j3dg_ray* __restrict__ rays, uint32_t n, uint32_t n_pad, float cx, float cy,
+                           float cz, float inv_s, __nv_bfloat16* __restrict__ X) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_pad) return;
+  __nv_bfloat16* x = X + (size_t)r * kIn;
+  if (r >= n) {
+    for (int j = 0; j < kIn; ++j) x[j] = __float2bfloat16(0.f);
+    return;
+  }
+  const float* f = reinterpret_cast<const float*>(rays + r);
+  const float dl = rsqrtf(f[4] * f[4] + f[5] * f[5] + f[6] * f[6] + 1e-30f);
+  const float in6[6] = {(f[0] - cx) * inv_s, (f[1] - cy) * inv_s, (f[2] - cz) * inv_s, f[4] * dl, f[5] * dl, f[6] * dl};
+  for (int i = 0; i < 6; ++i)
+    for (int k = 0; k < kBands; ++k) {
+      const float fr = 3.14159265f * exp2f(0.5f * (float)k);
+      float s, c;
+      sincosf(fr * in6[i], &s, &c);
+      x[(i * kBands + k) * 2] = __float2bfloat16(s);
+      x[(i * kBands + k) * 2 + 1] = __float2bfloat16(c);
+    }
+  for (int j = 6 * kBands * 2; j < kIn; ++j) x[j] = __float2bfloat16(0.f);
+}
+
+// Softmax cross-entropy over the first K logits of each row; rows with
+// label < 0 contribute nothing. dlogits = (softmax - onehot) / n_valid.
+__global__ void k_softmax_ce(const float* __restrict__ logits, const int32_t* __restrict__ labels, uint32_t rows,
+                             uint32_t K, float inv_valid, __nv_bfloat16* __restrict__ dlogits,
+                             float* __restrict__ loss, uint32_t* __restrict__ correct) {
+  const uint32_t row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const float* z = logits + (size_t)row * kOut;
+  __nv_bfloat16* dz = dlogits + (size_t)row * kOut;
+  const int32_t lab = labels[row];
+  if (lab < 0) {
+    for (uint32_t j = lane; j < kOut; j += 32) dz[j] = __float2bfloat16(0.f);
+    return;
+  }
+  float mx = -FLT_MAX;
+  uint32_t arg = 0;
+  for (uint32_t j = lane; j < K; j += 32)
+    if (z[j] > mx) {
+      mx = z[j];
+      arg = j;
+    }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float om = __shfl_xor_sync(0xffffffffu, mx, o);
+    const uint32_t oa = __shfl_xor_sync(0xffffffffu, arg, o);
+    if (om > mx || (om == mx && oa < arg)) {
+      mx = om;
+      arg = oa;
+    }
+  }
+  float sum = 0.f;
+  for (uint32_t j = lane; j < K; j += 32) sum += __expf(z[j] - mx);
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  const float inv = 1.f / sum;
+  for (uint32_t j = lane; j < kOut; j += 32) {
+    float g = 0.f;
+    if (j < K) g = __expf(z[j] - mx) * inv - (j == (uint32_t)lab ? 1.f : 0.f);
+    dz[j] = __float2bfloat16(g * inv_valid);
+  }
+  if (lane == 0) {
+    atomicAdd(loss, logf(sum) - (z[lab] - mx));
+    if (arg == (uint32_t)lab) atomicAdd(correct, 1u);
+  }
+}
+
+// column sums of a bf16 [rows x cols] matrix into fp32
+__global__ void k_colsum(const __nv_bfloat16* __restrict__ M, uint32_t rows, uint32_t cols, float* __restrict__ out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (uint32_t r = 0; r < rows; ++r) s += __bfloat162float(M[(size_t)r * cols + c]);
+  out[c] = s;
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       __nv_bfloat16* __restrict__ pb, size_t n, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16(pi);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ pb, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pb[i] = __float2bfloat16(p[i]);
+}
+
+// top-2 of the first K logits per row (ties to the smaller index)
+__global__ void k_top2(const float* __restrict__ logits, uint32_t rows, uint32_t K, uint32_t* __restrict__ out) {
+  const uint32_t row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  const float* z = logits + (size_t)row * kOut;
+  float v1 = -FLT_MAX, v2 = -FLT_MAX;
+  uint32_t i1 = 0xffffffffu, i2 = 0xffffffffu;
+  for (uint32_t j = lane; j < K; j += 32) {
+    const float x = z[j];
+    if (x > v1) {
+      v2 = v1;
+      i2 = i1;
+      v1 = x;
+      i1 = j;
+    } else if (x > v2) {
+      v2 = x;
+      i2 = j;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float a1 = __shfl_xor_sync(0xffffffffu, v1, o), a2 = __shfl_xor_sync(0xffffffffu, v2, o);
+    const uint32_t j1 = __shfl_xor_sync(0xffffffffu, i1, o), j2 = __shfl_xor_sync(0xffffffffu, i2, o);
+    // merge (v1,i1),(v2,i2) with (a1,j1),(a2,j2)
+    float c[4] = {v1, v2, a1, a2};
+    uint32_t ci[4] = {i1, i2, j1, j2};
+    float b1 = -FLT_MAX, b2 = -FLT_MAX;
+    uint32_t k1 = 0xffffffffu, k2 = 0xffffffffu;
+    for (int q = 0; q < 4; ++q) {
+      if (ci[q] == 0xffffffffu || ci[q] == k1) continue;
+      if (c[q] > b1 || (c[q] == b1 && ci[q] < k1)) {
+        b2 = b1;
+        k2 = k1;
+        b1 = c[q];
+        k1 = ci[q];
+      } else if (ci[q] != k2 && (c[q] > b2 || (c[q] == b2 && ci[q] < k2))) {
+        b2 = c[q];
+        k2 = ci[q];
+      }
+    }
+    v1 = b1;
+    v2 = b2;
+    i1 = k1;
+    i2 = k2;
+  }
+  if (lane == 0) {
+    out[2 * row] = i1;
+    out[2 * row + 1] = i2;
+  }
+}
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ float u01(uint32_t seed, uint32_t i, uint32_t k) {
+  return (float)(hash32(seed ^ hash32(i * 8u + k)) >> 8) * (1.f / 16777216.f);
+}
+
+// Training rays: a camera on a sphere of radius U(r0, r1) around the mesh
+// centre looking at it, a uniform image point of a 60-degree (vertical),
+// 16:9 frustum; rays are j3d primary rays (t_near = diagonal / 100).
+__global__ void k_train_rays(uint32_t seed, uint32_t first, uint32_t n, float cx, float cy, float cz, float r0,
+                             float r1, float t_near, j3dg_ray* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t id = first + i;
+  const float z = 2.f * u01(seed, id, 0) - 1.f, ph = 6.2831853f * u01(seed, id, 1);
+  const float sr = sqrtf(fmaxf(0.f, 1.f - z * z));
+  const float bx = sr * cosf(ph), by = sr * sinf(ph), bz = z;  // back axis
+  const float rad = r0 + (r1 - r0) * u01(seed, id, 2);
+  const float ex = cx + rad * bx, ey = cy + rad * by, ez = cz + rad * bz;
+  float ux = 0.f, uy = 1.f, uz = 0.f;
+  if (fabsf(by) > 0.99f) {
+    uy = 0.f;
+    uz = 1.f;
+  }
+  float rx = uy * bz - uz * by, ry = uz * bx - ux * bz, rz = ux * by - uy * bx;
+  const float rl = rsqrtf(rx * rx + ry * ry + rz * rz);
+  rx *= rl;
+  ry *= rl;
+  rz *= rl;
+  const float vx = by * rz - bz * ry, vy = bz * rx - bx * rz, vz = bx * ry - by * rx;
+  const float th = 0.57735027f;  // tan 30 deg
+  const float sx = (2.f * u01(seed, id, 3) - 1.f) * th * (16.f / 9.f), sy = (2.f * u01(seed, id, 4) - 1.f) * th;
+  j3dg_ray r;
+  r.orig[0] = ex;
+  r.orig[1] = ey;
+  r.orig[2] = ez;
+  r.orig[3] = 1.f;
+  r.dir[0] = sx * rx + sy * vx - bx;
+  r.dir[1] = sx * ry + sy * vy - by;
+  r.dir[2] = sx * rz + sy * vz - bz;
+  r.dir[3] = 0.f;
+  r.t_near = t_near;
+  r.t_far = FLT_MAX;
+  out[i] = r;
+}
+
+__global__ void k_labels(const j3dg_hit* __restrict__ hits, uint32_t n, uint32_t n_pad,
+                         const uint16_t* __restrict__ cluster_of_tri, int32_t* __restrict__ labels) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  labels[i] = (i < n && hits[i].found) ? (int32_t)cluster_of_tri[hits[i].object_id] : -1;
+}
+
+// cluster_of_tri for every triangle under cluster root `roots[c]`
+__global__ void k_cluster_map(const DevInst* __restrict__ inst, const uint32_t* __restrict__ roots, uint32_t n_roots,
+                              uint16_t* __restrict__ cluster_of_tri, uint32_t* status) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_roots) return;
+  const DevInst& I = inst[0];
+  uint32_t stack[J3DG_STACK];
+  int sp = 0;
+  stack[sp++] = roots[c];
+  uint32_t budget = I.n_nodes + 1;
+  while (sp > 0) {
+    const uint32_t ref = stack[--sp];
+    if (ref == J3DG_EMPTY_REF) continue;
+    if (ref & J3DG_LEAF_BIT) {
+      const uint32_t first = (ref & 0x7fffffffu) >> 3, cnt = (ref & 7u) + 1u;
+      if (first + cnt > I.nt) {
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+        return;
+      }
+      for (uint32_t k = 0; k < cnt; ++k) cluster_of_tri[__float_as_uint(I.tris[3 * (size_t)(first + k)].w)] = (uint16_t)c;
+      continue;
+    }
+    if (budget-- == 0 || ref >= I.n_nodes || sp + 4 > J3DG_STACK) {
+      atomicOr(status, J3DG_DEV_BAD_INDEX);
+      return;
+    }
+    const float4 ch = I.nodes[8 * (size_t)ref + 6];
+    stack[sp++] = __float_as_uint(ch.x);
+    stack[sp++] = __float_as_uint(ch.y);
+    stack[sp++] = __float_as_uint(ch.z);
+    stack[sp++] = __float_as_uint(ch.w);
+  }
+}
+
+// Learned closest hit: the two predicted clusters first, then the whole
+// tree with their best hit as the starting best (exact).
+__global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict__ inst, const j3dg_ray* __restrict__ rays,
+                                                      uint32_t n, const uint32_t* __restrict__ top2,
+                                                      const uint32_t* __restrict__ roots, uint32_t n_roots,
+                                                      j3dg_hit* __restrict__ hits, uint32_t* status,
+                                                      unsigned long long* counters) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* f = reinterpret_cast<const float*>(rays + i);
+  Tracer T;
+  uint32_t stack_ref[J3DG_STACK];
+  float stack_t[J3DG_STACK];
+  uint32_t visits = 0, tests = 0;
+  T.begin(inst, 1, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], false);
+  const uint32_t c0 = top2[2 * i], c1 = top2[2 * i + 1];
+  for (int phase = 0; phase < 3; ++phase) {
+    uint32_t ref;
+    if (phase < 2) {
+      const uint32_t c = phase == 0 ? c0 : c1;
+      if (c >= n_roots) continue;
+      ref = roots[c];
+    } else {
+      ref = inst[0].root_ref;
+    }
+    T.cur = ref;
+    T.sp = 0;
+    T.inst = 0;
+    T.budget = T.n_nodes + 1;
+    while (!T.step(inst, 1, status, visits, tests, stack_ref, stack_t)) {
+    }
+  }
+  j3dg_hit h;
+  h.found = T.b.found ? 1u : 0u;
+  h.distance = T.b.found ? T.b.t : f[9];
+  h.u = T.b.u;
+  h.v = T.b.v;
+  h.object_id = T.b.found ? T.b.tri : 0xffffffffu;
+  h.two_level_index = T.b.found ? 0u : 0xffffffffu;
+  hits[i] = h;
+  if (counters) {
+    atomicAdd(counters + 0, (unsigned long long)visits);
+    atomicAdd(counters + 1, (unsigned long long)tests);
+  }
+}
+
+}  // namespace j3dg
+
+// ------------------------------------------------------------------ host
+
+using j3dg::DevInst;
+using j3dg::GemmArgs;
+
+struct j3dg_learned {
+  j3dg_ctx* ctx = nullptr;
+  const j3dg_mesh* mesh = nullptr;
+  j3dg_learned_opts opts;
+  j3dg::Layout L;
+  uint32_t n_clusters = 0;
+  std::vector<uint32_t> h_roots;
+  uint32_t* d_roots = nullptr;
+  uint16_t* d_cluster_of_tri = nullptr;
+  float *d_p = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+  __nv_bfloat16* d_pb = nullptr;
+  uint32_t adam_t = 0;
+  // per-batch workspace (batch rows)
+  uint32_t B = 0;
+  __nv_bfloat16 *X = nullptr, *H[4] = {nullptr, nullptr, nullptr, nullptr}, *Z[4] = {nullptr, nullptr, nullptr, nullptr};
+  __nv_bfloat16 *dZ5 = nullptr, *dA = nullptr, *dB = nullptr;
+  float* logits = nullptr;
+  int32_t* labels = nullptr;
+  float* d_loss = nullptr;
+  uint32_t* d_correct = nullptr;
+  j3dg_ray* rays = nullptr;
+  j3dg_hit* hits = nullptr;
+  uint32_t* top2 = nullptr;
+  float center[3] = {0, 0, 0}, inv_scale = 1.f, t_near = 0.f;
+};
+
+namespace {
+
+cudaStream_t LS(j3dg_learned* l) { return (cudaStream_t)l->ctx->stream; }
+
+#define LCK(x, where)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (x);                                                                          \
+    if (e_ != cudaSuccess) return j3dg::ctx_fail(l->ctx, J3DG_ERR_CUDA, std::string(where) + ": " + \
+                                                     cudaGetErrorString(e_));                      \
+  } while (0)
+
+int alloc_workspace(j3dg_learned* l, uint32_t B) {
+  if (l->B >= B) return J3DG_OK;
+  cudaFree(l->X);
+  for (int k = 0; k < 4; ++k) {
+    cudaFree(l->H[k]);
+    cudaFree(l->Z[k]);
+  }
+  cudaFree(l->dZ5);
+  cudaFree(l->dA);
+  cudaFree(l->dB);
+  cudaFree(l->logits);
+  cudaFree(l->labels);
+  cudaFree(l->rays);
+  cudaFree(l->hits);
+  cudaFree(l->top2);
+  l->B = B;
+  LCK(cudaMalloc(&l->X, sizeof(__nv_bfloat16) * B * j3dg::kIn), "learned workspace");
+  for (int k = 0; k < 4; ++k) {
+    LCK(cudaMalloc(&l->H[k], sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+    LCK(cudaMalloc(&l->Z[k], sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  }
+  LCK(cudaMalloc(&l->dZ5, sizeof(__nv_bfloat16) * B * j3dg::kOut), "learned workspace");
+  LCK(cudaMalloc(&l->dA, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  LCK(cudaMalloc(&l->dB, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  LCK(cudaMalloc(&l->logits, sizeof(float) * B * j3dg::kOut), "learned workspace");
+  LCK(cudaMalloc(&l->labels, sizeof(int32_t) * B), "learned workspace");
+  LCK(cudaMalloc(&l->rays, sizeof(j3dg_ray) * B), "learned workspace");
+  LCK(cudaMalloc(&l->hits, sizeof(j3dg_hit) * B), "learned workspace");
+  LCK(cudaMalloc(&l->top2, sizeof(uint32_t) * 2 * B), "learned workspace");
+  return J3DG_OK;
+}
+
+__nv_bfloat16* W(j3dg_learned* l, int k) { return l->d_pb + l->L.w[k]; }
+const float* Bias(j3dg_learned* l, int k) { return l->d_p + l->L.b[k]; }
+
+// forward over X (B rows): H1..H4, logits
+int forward(j3dg_learned* l, uint32_t B) {
+  const __nv_bfloat16* in = l->X;
+  int in_dim = j3dg::kIn;
+  for (int k = 0; k < 4; ++k) {
+    GemmArgs g{in, W(l, k), l->H[k], l->Z[k], Bias(l, k), (int)B, j3dg::kHid, in_dim, in_dim, j3dg::kHid, j3dg::kHid};
+    LCK(j3dg::gemm_bf16(g, false, false, j3dg::EPI_BIAS_GELU, LS(l)), "learned forward");
+    in = l->H[k];
+    in_dim = j3dg::kHid;
+  }
+  GemmArgs g{l->H[3], W(l, 4), l->logits, nullptr, Bias(l, 4), (int)B, j3dg::kOut, j3dg::kHid, j3dg::kHid, j3dg::kOut,
+             j3dg::kOut};
+  LCK(j3dg::gemm_bf16(g, false, false, j3dg::EPI_BIAS_F32, LS(l)), "learned forward");
+  return J3DG_OK;
+}
+
+// softmax CE + backward into l->d_g (all gradients overwritten)
+int backward(j3dg_learned* l, uint32_t B, float inv_valid) {
+  j3dg::k_softmax_ce<<<(B + 7) / 8, 256, 0, LS(l)>>>(l->logits, l->labels, B, l->n_clusters, inv_valid, l->dZ5,
+                                                       l->d_loss, l->d_correct);
+  LCK(cudaGetLastError(), "learned softmax");
+  float* g = l->d_g;
+  // layer 5: dW5 = H4^T dZ5, db5 = colsum(dZ5), dZ4 = (dZ5 W5^T) * gelu'(Z4)
+  {
+    GemmArgs a{l->H[3], l->dZ5, g + l->L.w[4], nullptr, nullptr, j3dg::kHid, j3dg::kOut, (int)B, j3dg::kHid, j3dg::kOut,
+               j3dg::kOut};
+    LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
+    j3dg::k_colsum<<<(j3dg::kOut + 255) / 256, 256, 0, LS(l)>>>(l->dZ5, B, j3dg::kOut, g + l->L.b[4]);
+    GemmArgs d{l->dZ5, W(l, 4), l->dA, l->Z[3], nullptr, (int)B, j3dg::kHid, j3dg::kOut, j3dg::kOut, j3dg::kOut,
+               j3dg::kHid};
+    LCK(j3dg::gemm_bf16(d, false, true, j3dg::EPI_GELU_BWD, LS(l)), "learned backward");
+  }
+  __nv_bfloat16* dcur = l->dA;
+  __nv_bfloat16* dnext = l->dB;
+  for (int k = 3; k >= 0; --k) {
+    const __nv_bfloat16* in = k ? l->H[k - 1] : l->X;
+    const int in_dim = k ? j3dg::kHid : j3dg::kIn;
+    GemmArgs a{in, dcur, g + l->L.w[k], nullptr, nullptr, in_dim, j3dg::kHid, (int)B, in_dim, j3dg::kHid, j3dg::kHid};
+    LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
+    j3dg::k_colsum<<<1, 128, 0, LS(l)>>>(dcur, B, j3dg::kHid, g + l->L.b[k]);
+    if (k > 0) {
+      GemmArgs d{dcur, W(l, k), dnext, l->Z[k - 1], nullptr, (int)B, j3dg::kHid, j3dg::kHid, j3dg::kHid, j3dg::kHid,
+                 j3dg::kHid};
+      LCK(j3dg::gemm_bf16(d, false, true, j3dg::EPI_GELU_BWD, LS(l)), "learned backward");
+      std::swap(dcur, dnext);
+    }
+  }
+  LCK(cudaGetLastError(), "learned backward");
+  return J3DG_OK;
+}
+
+int features(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t n_pad) {
+  j3dg::k_features<<<(n_pad + 127) / 128, 128, 0, LS(l)>>>(d_rays, n, n_pad, l->center[0], l->center[1], l->center[2],
+                                                            l->inv_scale, l->X);
+  LCK(cudaGetLastError(), "learned features");
+  return J3DG_OK;
+}
+
+uint32_t pad128(uint32_t n) { return (n + 127u) & ~127u; }
+
+}  // namespace
+
+extern "C" {
+
+int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_opts* opts, j3dg_learned** out) {
+  if (!c || !mesh || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaSetDevice(c->device);
+  j3dg_learned* l = new (std::nothrow) j3dg_learned();
+  if (!l) return J3DG_ERR_OUT_OF_MEMORY;
+  l->ctx = c;
+  l->mesh = mesh;
+  l->opts.cluster_depth = 6;
+  l->opts.batch = 16384;
+  l->opts.lr = 2e-3f;
+  l->opts.seed = 0x6A3D0003ull;
+  if (opts) {
+    if (opts->cluster_depth) l->opts.cluster_depth = opts->cluster_depth;
+    if (opts->batch) l->opts.batch = opts->batch;
+    if (opts->lr > 0.f) l->opts.lr = opts->lr;
+    l->opts.seed = opts->seed;
+  }
+  if (l->opts.cluster_depth > 6 || l->opts.batch % 128) {
+    delete l;
+    return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned: cluster_depth <= 6, batch a multiple of 128");
+  }
+  // clusters: the refs at cluster_depth below the root (and shallower leaves)
+  const uint32_t top = std::min<uint32_t>(mesh->n_nodes, 1u << 14);
+  std::vector<float> nodes((size_t)top * 32);
+  cudaError_t e = cudaSuccess;
+  if (top) e = cudaMemcpy(nodes.data(), mesh->d_nodes, sizeof(float) * 32 * top, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    delete l;
+    return j3dg::ctx_fail(c, J3DG_ERR_CUDA, "learned: reading nodes failed");
+  }
+  std::vector<uint32_t> level{mesh->root_ref};
+  for (uint32_t d = 0; d < l->opts.cluster_depth; ++d) {
+    std::vector<uint32_t> next;
+    for (uint32_t ref : level) {
+      if (ref & J3DG_LEAF_BIT) {
+        next.push_back(ref);
+        continue;
+      }
+      if (ref >= top) {
+        delete l;
+        return j3dg::ctx_fail(c, J3DG_ERR_UNSUPPORTED, "learned: cluster level beyond the first nodes");
+      }
+      for (int k = 0; k < 4; ++k) {
+        uint32_t ch;
+        memcpy(&ch, &nodes[(size_t)ref * 32 + 24 + k], 4);
+        if (ch != J3DG_EMPTY_REF) next.push_back(ch);
+      }
+    }
+    level.swap(next);
+  }
+  if (level.size() > (size_t)j3dg::kOut) {
+    delete l;
+    return j3dg::ctx_fail(c, J3DG_ERR_UNSUPPORTED, "learned: more than 4096 clusters");
+  }
+  l->h_roots = level;
+  l->n_clusters = (uint32_t)level.size();
+  const DevInst* dinst = nullptr;
+  int rc = j3dg::mesh_devinst(c, mesh, &dinst);
+  if (rc) {
+    delete l;
+    return rc;
+  }
+  e = cudaMalloc(&l->d_roots, sizeof(uint32_t) * l->n_clusters);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_cluster_of_tri, sizeof(uint16_t) * mesh->nt);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(l->d_roots, l->h_roots.data(), sizeof(uint32_t) * l->n_clusters, cudaMemcpyHostToDevice,
+                        LS(l));
+  if (e == cudaSuccess) {
+    j3dg::k_cluster_map<<<(l->n_clusters + 63) / 64, 64, 0, LS(l)>>>(dinst, l->d_roots, l->n_clusters,
+                                                                    l->d_cluster_of_tri, c->d_status);
+    e = cudaGetLastError();
+  }
+  // parameters: N(0, sqrt(2 / fan_in)) weights (seeded, host), zero biases
+  const size_t P = l->L.total;
+  std::vector<float> hp(P, 0.f);
+  uint64_t s = l->opts.seed * 0x9E3779B97F4A7C15ull + 1;
+  auto next = [&]() {
+    s ^= s << 13;
+    s ^= s >> 7;
+    s ^= s << 17;
+    return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int k = 0; k < 5; ++k) {
+    const double sd = std::sqrt(2.0 / (k == 0 ? 192.0 : 128.0));
+    for (size_t i = 0; i < (size_t)l->L.in[k] * l->L.out[k]; ++i) {
+      const double u1 = std::max(next(), 1e-12), u2 = next();
+      hp[l->L.w[k] + i] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+    }
+    if (k == 0)  // rows of the zero padding features stay zero
+      for (int r = 192; r < j3dg::kIn; ++r)
+        for (int o = 0; o < j3dg::kHid; ++o) hp[l->L.w[0] + (size_t)r * j3dg::kHid + o] = 0.f;
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_p, sizeof(float) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_g, sizeof(float) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_m, sizeof(float) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_v, sizeof(float) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_pb, sizeof(__nv_bfloat16) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_loss, sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_correct, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(l->d_p, hp.data(), sizeof(float) * P, cudaMemcpyHostToDevice, LS(l));
+  if (e == cudaSuccess) e = cudaMemsetAsync(l->d_m, 0, sizeof(float) * P, LS(l));
+  if (e == cudaSuccess) e = cudaMemsetAsync(l->d_v, 0, sizeof(float) * P, LS(l));
+  if (e == cudaSuccess) {
+    j3dg::k_to_bf16<<<(unsigned)((P + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_pb, P);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(LS(l));
+  if (e != cudaSuccess) {
+    j3dg_learned_destroy(l);
+    return j3dg::ctx_fail(c, J3DG_ERR_CUDA, std::string("learned_create: ") + cudaGetErrorString(e));
+  }
+  // normalisation of ray origins: mesh bbox centre and half of its largest extent
+  float ext = 0.f;
+  for (int k = 0; k < 3; ++k) {
+    l->center[k] = 0.5f * (mesh->min_bb[k] + mesh->max_bb[k]);
+    ext = std::max(ext, mesh->max_bb[k] - mesh->min_bb[k]);
+  }
+  l->inv_scale = ext > 0.f ? 2.f / ext : 1.f;
+  l->t_near = ext / 100.f;
+  *out = l;
+  return J3DG_OK;
+}
+
+int j3dg_learned_destroy(j3dg_learned* l) {
+  if (!l) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(l->ctx->device);
+  cudaStreamSynchronize(LS(l));
+  void* ptrs[] = {l->d_roots, l->d_cluster_of_tri, l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb, l->X, l->dZ5, l->dA, l->dB,
+                  l->logits, l->labels, l->d_loss, l->d_correct, l->rays, l->hits, l->top2};
+  for (void* p : ptrs) cudaFree(p);
+  for (int k = 0; k < 4; ++k) {
+    cudaFree(l->H[k]);
+    cudaFree(l->Z[k]);
+  }
+  delete l;
+  return J3DG_OK;
+}
+
+int j3dg_learned_info(const j3dg_learned* l, uint32_t* n_clusters, uint64_t* n_params) {
+  if (!l) return J3DG_ERR_INVALID_ARGUMENT;
+  if (n_clusters) *n_clusters = l->n_clusters;
+  if (n_params) *n_params = l->L.total;
+  return J3DG_OK;
+}
+
+int j3dg_learned_get_params(j3dg_learned* l, float* out) {
+  if (!l || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(l->ctx->device);
+  LCK(cudaMemcpyAsync(out, l->d_p, sizeof(float) * l->L.total, cudaMemcpyDeviceToHost, LS(l)), "get_params");
+  LCK(cudaStreamSynchronize(LS(l)), "get_params");
+  return J3DG_OK;
+}
+
+int j3dg_learned_set_params(j3dg_learned* l, const float* in) {
+  if (!l || !in) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(l->ctx->device);
+  const size_t P = l->L.total;
+  LCK(cudaMemcpyAsync(l->d_p, in, sizeof(float) * P, cudaMemcpyHostToDevice, LS(l)), "set_params");
+  j3dg::k_to_bf16<<<(unsigned)((P + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_pb, P);
+  LCK(cudaStreamSynchronize(LS(l)), "set_params");
+  return J3DG_OK;
+}
+
+// Loss and gradients for a batch of given features (B x 256, fp32; rounded
+// to bf16 as the network reads them) and labels; for gradient checks.
+int j3dg_learned_loss_grad(j3dg_learned* l, const float* feats, const int32_t* labels, uint32_t B, float* loss,
+                           float* grads) {
+  if (!l || !feats || !labels || B == 0 || B % 128) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(l->ctx->device);
+  if (int rc = alloc_workspace(l, std::max(B, l->opts.batch))) return rc;
+  std::vector<__nv_bfloat16> xb((size_t)B * j3dg::kIn);
+  for (size_t i = 0; i < xb.size(); ++i) xb[i] = __float2bfloat16(feats[i]);
+  uint32_t valid = 0;
+  for (uint32_t i = 0; i < B; ++i) valid += labels[i] >= 0;
+  LCK(cudaMemcpyAsync(l->X, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice, LS(l)), "loss_grad");
+  LCK(cudaMemcpyAsync(l->labels, labels, sizeof(int32_t) * B, cudaMemcpyHostToDevice, LS(l)), "loss_grad");
+  LCK(cudaMemsetAsync(l->d_loss, 0, sizeof(float), LS(l)), "loss_grad");
+  LCK(cudaMemsetAsync(l->d_correct, 0, sizeof(uint32_t), LS(l)), "loss_grad");
+  if (int rc = forward(l, B)) return rc;
+  if (int rc = backward(l, B, valid ? 1.f / (float)valid : 0.f)) return rc;
+  float ls = 0.f;
+  LCK(cudaMemcpyAsync(&ls, l->d_loss, sizeof(float), cudaMemcpyDeviceToHost, LS(l)), "loss_grad");
+  if (grads) LCK(cudaMemcpyAsync(grads, l->d_g, sizeof(float) * l->L.total, cudaMemcpyDeviceToHost, LS(l)), "loss_grad");
+  LCK(cudaStreamSynchronize(LS(l)), "loss_grad");
+  if (loss) *loss = valid ? ls / (float)valid : 0.f;
+  return J3DG_OK;
+}
+
+int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, float* final_loss, float* accuracy,
+                       float* seconds) {
+  if (!l || n_rays == 0 || !(r1 >= r0) || r0 <= 0.f) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = l->ctx;
+  cudaSetDevice(c->device);
+  const uint32_t B = l->opts.batch;
+  if (int rc = alloc_workspace(l, B)) return rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint64_t steps = (n_rays + B - 1) / B;
+  const float b1 = 0.9f, b2 = 0.999f;
+  float last_loss = 0.f, last_acc = 0.f;
+  std::vector<int32_t> lab(B);
+  for (uint64_t s = 0; s < steps; ++s) {
+    j3dg::k_train_rays<<<(B + 127) / 128, 128, 0, LS(l)>>>((uint32_t)l->opts.seed, (uint32_t)(s * B), B, l->center[0],
+                                                           l->center[1], l->center[2], r0, r1, l->t_near, l->rays);
+    LCK(cudaGetLastError(), "train rays");
+    if (int rc = j3dg::ray_query_device(c, l->mesh, l->rays, B, l->hits)) return rc;
+    j3dg::k_labels<<<(B + 127) / 128, 128, 0, LS(l)>>>(l->hits, B, B, l->d_cluster_of_tri, l->labels);
+    if (int rc = features(l, l->rays, B, B)) return rc;
+    LCK(cudaMemsetAsync(l->d_loss, 0, sizeof(float), LS(l)), "train");
+    LCK(cudaMemsetAsync(l->d_correct, 0, sizeof(uint32_t), LS(l)), "train");
+    if (int rc = forward(l, B)) return rc;
+    // hit fraction of the training rays is ~ constant; scale by the batch
+    if (int rc = backward(l, B, 1.f / (float)B)) return rc;
+    ++l->adam_t;
+    const float c1 = 1.f / (1.f - std::pow(b1, (float)l->adam_t)), c2 = 1.f / (1.f - std::pow(b2, (float)l->adam_t));
+    j3dg::k_adam<<<(unsigned)((l->L.total + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb,
+                                                                         l->L.total, l->opts.lr, b1, b2, 1e-8f, c1, c2);
+    LCK(cudaGetLastError(), "adam");
+    if (s + 1 == steps || (s % 64) == 63) {
+      float ls = 0.f;
+      uint32_t corr = 0;
+      LCK(cudaMemcpyAsync(&ls, l->d_loss, sizeof(float), cudaMemcpyDeviceToHost, LS(l)), "train");
+      LCK(cudaMemcpyAsync(&corr, l->d_correct, sizeof(uint32_t), cudaMemcpyDeviceToHost, LS(l)), "train");
+      LCK(cudaMemcpyAsync(lab.data(), l->labels, sizeof(int32_t) * B, cudaMemcpyDeviceToHost, LS(l)), "train");
+      LCK(cudaStreamSynchronize(LS(l)), "train");
+      uint32_t valid = 0;
+      for (int32_t x : lab) valid += x >= 0;
+      last_loss = valid ? ls / (float)valid : 0.f;
+      last_acc = valid ? (float)corr / (float)valid : 0.f;
+    }
+  }
+  LCK(cudaStreamSynchronize(LS(l)), "train");
+  if (final_loss) *final_loss = last_loss;
+  if (accuracy) *accuracy = last_acc;
+  if (seconds) *seconds = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+  return J3DG_OK;
+}
+
+// top-2 clusters per ray (device or host arrays)
+static int predict_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2) {
+  const uint32_t B = l->opts.batch;
+  if (int rc = alloc_workspace(l, B)) return rc;
+  for (uint32_t off = 0; off < n; off += B) {
+    const uint32_t m = std::min(B, n - off);
+    const uint32_t mp = pad128(m);
+    if (int rc = features(l, d_rays + off, m, mp)) return rc;
+    if (int rc = forward(l, mp)) return rc;
+    j3dg::k_top2<<<(m + 7) / 8, 256, 0, LS(l)>>>(l->logits, m, l->n_clusters, d_top2 + 2 * (size_t)off);
+    LCK(cudaGetLastError(), "top2");
+  }
+  return J3DG_OK;
+}
+
+int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2) {
+  if (!l || (n && (!rays || !top2))) return J3DG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return J3DG_OK;
+  cudaSetDevice(l->ctx->device);
+  j3dg_ray* dr = nullptr;
+  uint32_t* dt = nullptr;
+  LCK(cudaMallocAsync((void**)&dr, sizeof(j3dg_ray) * n, LS(l)), "predict");
+  LCK(cudaMallocAsync((void**)&dt, sizeof(uint32_t) * 2 * n, LS(l)), "predict");
+  LCK(cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * n, cudaMemcpyDefault, LS(l)), "predict");
+  int rc = predict_device(l, dr, n, dt);
+  if (rc == J3DG_OK) LCK(cudaMemcpyAsync(top2, dt, sizeof(uint32_t) * 2 * n, cudaMemcpyDefault, LS(l)), "predict");
+  cudaFreeAsync(dr, LS(l));
+  cudaFreeAsync(dt, LS(l));
+  LCK(cudaStreamSynchronize(LS(l)), "predict");
+  return rc;
+}
+
+int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits) {
+  if (!l || (n && (!rays || !hits))) return J3DG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return J3DG_OK;
+  j3dg_ctx* c = l->ctx;
+  cudaSetDevice(c->device);
+  cudaPointerAttributes ar, ah;
+  const bool rays_dev = cudaPointerGetAttributes(&ar, rays) == cudaSuccess && ar.type == cudaMemoryTypeDevice;
+  const bool hits_dev = cudaPointerGetAttributes(&ah, hits) == cudaSuccess && ah.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  j3dg_ray* dr = const_cast<j3dg_ray*>(rays);
+  j3dg_hit* dh = hits;
+  uint32_t* dt = nullptr;
+  if (!rays_dev) {
+    LCK(cudaMallocAsync((void**)&dr, sizeof(j3dg_ray) * n, LS(l)), "learned find");
+    LCK(cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * n, cudaMemcpyHostToDevice, LS(l)), "learned find");
+  }
+  if (!hits_dev) LCK(cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * n, LS(l)), "learned find");
+  LCK(cudaMallocAsync((void**)&dt, sizeof(uint32_t) * 2 * n, LS(l)), "learned find");
+  int rc = predict_device(l, dr, n, dt);
+  const DevInst* dinst = nullptr;
+  if (rc == J3DG_OK) rc = j3dg::mesh_devinst(c, l->mesh, &dinst);
+  if (rc == J3DG_OK) {
+    unsigned long long* counters = nullptr;
+    j3dg::k_rays_learned<<<(n + 127) / 128, 128, 0, LS(l)>>>(dinst, dr, n, dt, l->d_roots, l->n_clusters, dh,
+                                                            c->d_status, counters);
+    LCK(cudaGetLastError(), "learned find");
+  }
+  if (!hits_dev) {
+    LCK(cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * n, cudaMemcpyDeviceToHost, LS(l)), "learned find");
+    cudaFreeAsync(dh, LS(l));
+  }
+  if (!rays_dev) cudaFreeAsync(dr, LS(l));
+  cudaFreeAsync(dt, LS(l));
+  LCK(cudaStreamSynchronize(LS(l)), "learned find");
+  uint32_t st = 0;
+  LCK(cudaMemcpy(&st, c->d_status, sizeof(st), cudaMemcpyDeviceToHost), "learned find");
+  if (st) return j3dg::ctx_fail(c, J3DG_ERR_DEVICE_STATUS, "learned find: device status raised");
+  return rc;
+}
+
+// Checkpoint: a small header and the fp32 parameters.
+int j3dg_learned_save(j3dg_learned* l, const char* path) {
+  if (!l || !path) return J3DG_ERR_INVALID_ARGUMENT;
+  std::vector<float> p(l->L.total);
+  if (int rc = j3dg_learned_get_params(l, p.data())) return rc;
+  FILE* f = fopen(path, "wb");
+  if (!f) return j3dg::ctx_fail(l->ctx, J3DG_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+  const uint32_t hdr[4] = {0x4A334C4Du, 1u, l->n_clusters, (uint32_t)l->L.total};
+  bool ok = fwrite(hdr, sizeof(hdr), 1, f) == 1 && fwrite(p.data(), sizeof(float), p.size(), f) == p.size();
+  ok = (fclose(f) == 0) && ok;
+  return ok ? J3DG_OK : j3dg::ctx_fail(l->ctx, J3DG_ERR_INVALID_ARGUMENT, "checkpoint write failed");
+}
+
+int j3dg_learned_load(j3dg_learned* l, const char* path) {
+  if (!l || !path) return J3DG_ERR_INVALID_ARGUMENT;
+  FILE* f = fopen(path, "rb");
+  if (!f) return j3dg::ctx_fail(l->ctx, J3DG_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+  uint32_t hdr[4];
+  std::vector<float> p(l->L.total);
+  bool ok = fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == 0x4A334C4Du && hdr[1] == 1u && hdr[2] == l->n_clusters &&
+            hdr[3] == (uint32_t)l->L.total && fread(p.data(), sizeof(float), p.size(), f) == p.size();
+  fclose(f);
+  if (!ok) return j3dg::ctx_fail(l->ctx, J3DG_ERR_INVALID_ARGUMENT, "checkpoint does not match this network");
+  return j3dg_learned_set_params(l, p.data());
+}
+
+}  // extern "C"

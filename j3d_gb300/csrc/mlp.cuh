@@ -1,0 +1,50 @@
+// mlp.cuh -- bf16 tensor-core GEMM with fused epilogues for the ray ->
+// cluster network of the learned-tmax traversal.
+//
+//   C[m][n] = sum_k A(m, k) B(k, n), fp32 accumulation
+//   A(m, k) = AT ? A[k * lda + m] : A[m * lda + k]
+//   B(k, n) = BT ? B[n * ldb + k] : B[k * ldb + n]
+//
+// Tiles of 128 x 128 x 32 per block (8 warps, each 64 x 32), operands staged
+// k-contiguous in shared memory (double-buffered), fragments by ldmatrix,
+// products by mma.sync m16n8k16 bf16 -> f32. M, N, K must be multiples of
+// 128, 128, 32 (the callers pad).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace j3dg {
+
+enum Epilogue : int {
+  EPI_F32 = 0,            // C (float) = acc
+  EPI_F32_ACCUM = 1,      // C (float) += acc
+  EPI_BIAS_GELU = 2,      // Z (bf16) = acc + bias; C (bf16) = gelu(Z)
+  EPI_BIAS_F32 = 3,       // C (float) = acc + bias
+  EPI_GELU_BWD = 4,       // C (bf16) = acc * gelu'(Z), Z given (bf16)
+};
+
+struct GemmArgs {
+  const __nv_bfloat16* A;
+  const __nv_bfloat16* B;
+  void* C;
+  __nv_bfloat16* Z;      // pre-activation out (EPI_BIAS_GELU) or in (EPI_GELU_BWD)
+  const float* bias;
+  int M, N, K, lda, ldb, ldc;
+};
+
+cudaError_t gemm_bf16(const GemmArgs& g, bool at, bool bt, int epi, cudaStream_t st);
+
+// tanh-form GELU and its derivative (the network's activation)
+__device__ __forceinline__ float gelu_f(float x) {
+  const float k = 0.7978845608028654f;  // sqrt(2 / pi)
+  return 0.5f * x * (1.f + tanhf(k * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_grad_f(float x) {
+  const float k = 0.7978845608028654f;
+  const float u = k * (x + 0.044715f * x * x * x);
+  const float th = tanhf(u);
+  return 0.5f * (1.f + th) + 0.5f * x * (1.f - th * th) * k * (1.f + 3.f * 0.044715f * x * x);
+}
+
+}  // namespace j3dg

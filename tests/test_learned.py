@@ -1,0 +1,115 @@
+"""Learned tmax: the CPU oracle's gradients against finite differences, the
+GPU's forward/backward against the oracle, training, and exactness of the
+learned traversal (hit ids identical to the plain traversal)."""
+import numpy as np
+import pytest
+
+FLT_MAX = np.float32(np.finfo(np.float32).max)
+
+
+def _layout():
+    from j3d_gb300.learned import param_layout
+    return param_layout()
+
+
+def _small_layout(n_in=8, n_hid=6, n_out=5):
+    """The same network shape family, tiny, for finite differences."""
+    ins = [n_in, n_hid, n_hid, n_hid, n_hid]
+    outs = [n_hid, n_hid, n_hid, n_hid, n_out]
+    out, o = [], 0
+    for k in range(5):
+        out.append((f"W{k + 1}", o, (ins[k], outs[k])))
+        o += ins[k] * outs[k]
+        out.append((f"b{k + 1}", o, (outs[k],)))
+        o += outs[k]
+    return out, o
+
+
+def test_oracle_gradients_match_finite_differences():
+    from oracle.mlp_oracle import loss_grad
+    layout, n = _small_layout()
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.5, n)
+    X = rng.normal(0, 1, (7, 8))
+    lab = np.array([0, 4, 2, -1, 1, 3, 0])
+    f0, g = loss_grad(p, layout, X, lab, 5, bf16_round=False, dtype=np.float64)
+    eps = 1e-6
+    for i in rng.choice(n, 60, replace=False):
+        q = p.copy()
+        q[i] += eps
+        f1, _ = loss_grad(q, layout, X, lab, 5, bf16_round=False, dtype=np.float64)
+        q[i] -= 2 * eps
+        f2, _ = loss_grad(q, layout, X, lab, 5, bf16_round=False, dtype=np.float64)
+        assert abs((f1 - f2) / (2 * eps) - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+def test_oracle_bf16_rounding():
+    from oracle.mlp_oracle import bf16
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.14159265], np.float32)
+    y = bf16(x)
+    assert y[0] == 1.0 and y[1] == 1.0 and y[2] == 1.0078125 and y[3] == -2.5 and y[4] == 3.140625
+
+
+@pytest.mark.gpu
+def test_gpu_gradients_match_cpu_oracle(gpu_ctx):
+    from j3d_gb300 import Mesh, workloads as W
+    from j3d_gb300.learned import Learned
+    from oracle.mlp_oracle import loss_grad
+    V, T = W.icosphere(5, W.SEED_BASE + 70)
+    net = Learned(gpu_ctx, Mesh(gpu_ctx, V, T))
+    layout, n = _layout()
+    assert n == net.n_params
+    rng = np.random.default_rng(1)
+    p = net.get_params()
+    p[layout[1][1]:layout[1][1] + 128] = rng.normal(0, 0.1, 128)  # non-zero biases too
+    net.set_params(p)
+    B = 256
+    X = np.zeros((B, 256), np.float32)
+    X[:, :192] = rng.uniform(-1, 1, (B, 192))
+    lab = rng.integers(0, net.n_clusters, B).astype(np.int32)
+    lab[::7] = -1
+    loss_g, g_gpu = net.loss_grad(X, lab)
+    loss_c, g_cpu = loss_grad(p, layout, X, lab, net.n_clusters)
+    assert abs(loss_g - loss_c) <= 2e-3 * abs(loss_c)
+    for name, o, shape in layout:
+        a, b = g_gpu[o:o + int(np.prod(shape))], g_cpu[o:o + int(np.prod(shape))]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert rel < 3e-2, f"{name}: relative gradient error {rel:.3g}"
+
+
+@pytest.mark.gpu
+def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
+    from j3d_gb300 import Mesh, SceneObject, find_closest, workloads as W
+    from j3d_gb300.learned import Learned
+    V, T = W.torus(400, 200, seed=W.SEED_BASE + 71)
+    mesh = Mesh(gpu_ctx, V, T)
+    net = Learned(gpu_ctx, mesh, batch=8192, lr=2e-3, seed=5)
+    assert 16 < net.n_clusters <= 4096
+    loss0, acc0, _ = net.train(8192 * 4)
+    loss1, acc1, secs = net.train(8192 * 200)
+    assert loss1 < loss0 and acc1 > 0.3, (loss0, loss1, acc1)
+    # fresh rays: primary rays of seeded cameras plus random ones
+    rng = np.random.default_rng(7)
+    n = 20000
+    poses = W.cameras(n, W.SEED_BASE + 72, 2.0, 5.0)
+    rays = np.zeros(n, [("orig", "<f4", 4), ("dir", "<f4", 4), ("t_near", "<f4"), ("t_far", "<f4")])
+    P = poses.reshape(n, 4, 4)
+    rays["orig"][:, :3] = P[:, 3, :3]
+    rays["orig"][:, 3] = 1
+    jit = rng.uniform(-0.5, 0.5, (n, 2)).astype(np.float32)
+    rays["dir"][:, :3] = -P[:, 2, :3] + jit[:, :1] * P[:, 0, :3] + jit[:, 1:] * P[:, 1, :3]
+    rays["t_near"] = 0.02
+    rays["t_far"] = np.where(rng.uniform(size=n) < 0.1, 3.0, FLT_MAX).astype(np.float32)
+    plain = find_closest(gpu_ctx, [SceneObject(mesh, None, 1)], rays)
+    learned = net.find_closest(rays)
+    for f in ("found", "distance", "u", "v", "object_id"):
+        assert np.array_equal(learned[f], plain[f]), f
+    assert plain["found"].mean() > 0.2
+    top2 = net.predict(rays)
+    assert (top2[:, 0] < net.n_clusters).all()
+    # checkpoint round trip
+    path = tmp_path / "net.bin"
+    net.save(path)
+    net2 = Learned(gpu_ctx, mesh, batch=8192, seed=99)
+    net2.load(path)
+    assert np.array_equal(net2.predict(rays), top2)

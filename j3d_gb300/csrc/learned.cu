@@ -66,7 +66,7 @@ struct Layout {
 // ------------------------------------------------------------------ kernels
 
 // Fourier features of (origin, direction): x_i = ((o - c) / s, d / |d|),
-// sin / cos of pi 2^(k/2) x_i for k = 0..15; features [i][k][sin, cos].
+// sin / cos of pi 2^(k/4) x_i for k = 0..15; features [i][k][sin, cos].
 __global__ void k_features(const j3dg_ray* __restrict__ rays, uint32_t n, uint32_t n_pad, float cx, float cy,
                            float cz, float inv_s, __nv_bfloat16* __restrict__ X) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,7 +81,7 @@ __global__ void k_features(const j3dg_ray* __restrict__ rays, uint32_t n, uint32
   const float in6[6] = {(f[0] - cx) * inv_s, (f[1] - cy) * inv_s, (f[2] - cz) * inv_s, f[4] * dl, f[5] * dl, f[6] * dl};
   for (int i = 0; i < 6; ++i)
     for (int k = 0; k < kBands; ++k) {
-      const float fr = 3.14159265f * exp2f(0.5f * (float)k);
+      const float fr = 3.14159265f * exp2f(0.25f * (float)k);
       float s, c;
       sincosf(fr * in6[i], &s, &c);
       x[(i * kBands + k) * 2] = __float2bfloat16(s);

@@ -37,14 +37,16 @@ def loss_grad(params: np.ndarray, layout, X: np.ndarray, labels: np.ndarray, n_c
               dtype=np.float32):
     """Mean softmax-CE loss over rows with label >= 0 and the gradient of the
     sum of per-row losses divided by the number of such rows."""
-    r = bf16 if bf16_round else (lambda a: a)
+    def r(a):  # the GPU's bf16 stores, or nothing
+        return bf16(np.asarray(a, np.float32)).astype(dtype) if bf16_round else np.asarray(a, dtype)
+
     P = unpack(params.astype(dtype), layout)
-    Wb = {k: (r(v).astype(dtype) if k.startswith("W") else v) for k, v in P.items()}
-    h = r(X.astype(np.float32)).astype(dtype)
+    Wb = {k: (r(v) if k.startswith("W") else v) for k, v in P.items()}
+    h = r(X)
     acts, zs = [h], []
     for k in range(1, 5):
-        z = r((h @ Wb[f"W{k}"] + P[f"b{k}"]).astype(np.float32)).astype(dtype)
-        h = r(gelu(z).astype(np.float32)).astype(dtype)
+        z = r(h @ Wb[f"W{k}"] + P[f"b{k}"])
+        h = r(gelu(z))
         zs.append(z)
         acts.append(h)
     logits = (h @ Wb["W5"] + P["b5"]).astype(dtype)
@@ -61,13 +63,13 @@ def loss_grad(params: np.ndarray, layout, X: np.ndarray, labels: np.ndarray, n_c
     d[:, :n_classes] = e / s
     d[np.arange(len(d)), lab] -= 1.0
     d[~valid] = 0.0
-    d = r((d / nv).astype(np.float32)).astype(dtype)
+    d = r(d / nv)
     G = {}
     G["W5"] = acts[4].T @ d
     G["b5"] = d.sum(axis=0)
     dh = d @ Wb["W5"].T
     for k in range(4, 0, -1):
-        dz = r((dh * gelu_grad(zs[k - 1])).astype(np.float32)).astype(dtype)
+        dz = r(dh * gelu_grad(zs[k - 1]))
         G[f"W{k}"] = acts[k - 1].T @ dz
         G[f"b{k}"] = dz.sum(axis=0)
         dh = dz @ Wb[f"W{k}"].T

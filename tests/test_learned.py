@@ -83,11 +83,13 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
     from j3d_gb300.learned import Learned
     V, T = W.torus(400, 200, seed=W.SEED_BASE + 71)
     mesh = Mesh(gpu_ctx, V, T)
-    net = Learned(gpu_ctx, mesh, batch=8192, lr=2e-3, seed=5)
-    assert 16 < net.n_clusters <= 4096
+    # 64 clusters (BVH depth 3) keep this check short; depth 6 (4096) is the
+    # configuration the benchmark trains on 50M rays
+    net = Learned(gpu_ctx, mesh, cluster_depth=3, batch=8192, lr=2e-3, seed=5)
+    assert 16 < net.n_clusters <= 64
     loss0, acc0, _ = net.train(8192 * 4)
-    loss1, acc1, secs = net.train(8192 * 200)
-    assert loss1 < loss0 and acc1 > 0.3, (loss0, loss1, acc1)
+    loss1, acc1, secs = net.train(8192 * 300)
+    assert loss1 < 0.8 * loss0 and acc1 > 0.3, (loss0, loss1, acc1)
     # fresh rays: primary rays of seeded cameras plus random ones
     rng = np.random.default_rng(7)
     n = 20000
@@ -106,10 +108,15 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
         assert np.array_equal(learned[f], plain[f]), f
     assert plain["found"].mean() > 0.2
     top2 = net.predict(rays)
+    # a 4096-cluster network trains too (loss falls from log K)
+    deep = Learned(gpu_ctx, mesh, cluster_depth=6, batch=8192, seed=6)
+    la, _, _ = deep.train(8192 * 4)
+    lb, _, _ = deep.train(8192 * 100)
+    assert deep.n_clusters > 1000 and lb < la
     assert (top2[:, 0] < net.n_clusters).all()
     # checkpoint round trip
     path = tmp_path / "net.bin"
     net.save(path)
-    net2 = Learned(gpu_ctx, mesh, batch=8192, seed=99)
+    net2 = Learned(gpu_ctx, mesh, cluster_depth=3, batch=8192, seed=99)
     net2.load(path)
     assert np.array_equal(net2.predict(rays), top2)

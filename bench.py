@@ -487,6 +487,113 @@ def run_serve(args):
     return 0
 
 
+def primary_rays(pose, pinv, w, h, near, t_near):
+    """j3d primary rays (canvas.cpp:773-782) of one camera, float32 numpy."""
+    cs = np.asarray(pose, np.float32).reshape(4, 4)  # column-major storage: rows are columns
+    P = np.asarray(pinv, np.float32).reshape(4, 4)
+    xs = (np.float32(2) * ((np.arange(w, dtype=np.float32) + np.float32(0.5)) / np.float32(w)) - np.float32(1))
+    ys = (np.float32(2) * ((np.arange(h, dtype=np.float32) + np.float32(0.5)) / np.float32(h)) - np.float32(1))
+    sx, sy = np.meshgrid(xs, ys)
+    s = np.stack([sx, sy, np.full_like(sx, near), np.ones_like(sx)], -1).reshape(-1, 4)
+    d = s @ P
+    d[:, 3] = 0
+    d = d @ cs
+    rays = np.zeros(len(d), [("orig", "<f4", 4), ("dir", "<f4", 4), ("t_near", "<f4"), ("t_far", "<f4")])
+    rays["orig"][:] = cs[3]
+    rays["dir"][:] = d
+    rays["t_near"] = t_near
+    rays["t_far"] = np.finfo(np.float32).max
+    return rays
+
+
+def run_learned(args):
+    """Learned tmax (config 3): the 4096-cluster network trained on 50M rays
+    of the 28.09M-triangle torus, then learned vs plain closest hit on the
+    primary rays of 4 cameras at 1920x1080 (hit ids must be identical)."""
+    import torch
+
+    from j3d_gb300 import (Context, Mesh, SceneObject, build as B, camera_for_vfov, find_closest,
+                           invert_projection_matrix, make_projection_matrix, workloads as Wk)
+    from j3d_gb300.learned import Learned
+    B.build()
+    wl = Wk.config1(N_CAMERAS, W_, H_)
+    ctx = Context(0)
+    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    net = Learned(ctx, mesh, cluster_depth=6, batch=16384, lr=2e-3, seed=Wk.SEED_BASE + 3)
+    loss, acc, train_s = net.train(args.learned_rays, 2.0, 5.0)
+    info = mesh.info()
+    diag = max(info.max_bb[k] - info.min_bb[k] for k in range(3))
+    cam = camera_for_vfov(60.0)
+    pinv = invert_projection_matrix(make_projection_matrix(cam, W_, H_))
+    host = np.concatenate([primary_rays(p, pinv, W_, H_, cam.near_clipping_plane, np.float32(diag) / np.float32(100))
+                           for p in wl.poses[:4]])
+    n = len(host)
+    d_rays = torch.from_numpy(host.view(np.uint8)).cuda()
+    d_plain = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    d_learn = torch.zeros(n * 24, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    objs = [SceneObject(mesh, None, 1)]
+
+    def timed(fn, reps=3):
+        fn()
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    from j3d_gb300 import _ffi
+    from j3d_gb300.scene import _instances
+    L = _ffi.lib()
+    inst = _instances(objs)
+
+    def plain():
+        assert L.j3dg_find_closest(ctx.h, inst, 1, d_rays.data_ptr(), n, d_plain.data_ptr()) == 0
+
+    def learned():
+        assert L.j3dg_learned_find_closest(net.h, d_rays.data_ptr(), n, d_learn.data_ptr()) == 0
+
+    ms_plain = timed(plain)
+    ms_learned = timed(learned)
+    ctx.set_counting(True)
+    ctx.read_counters(reset=True)
+    plain()
+    ctx.synchronize()
+    pv, pt = ctx.read_counters(reset=True)
+    learned()
+    ctx.synchronize()
+    lv, lt = ctx.read_counters(reset=True)
+    ctx.set_counting(False)
+    hp = d_plain.cpu().numpy().view(_ffi.HIT_DTYPE)
+    hl = d_learn.cpu().numpy().view(_ffi.HIT_DTYPE)
+    same = bool(all(np.array_equal(hp[f], hl[f]) for f in ("found", "distance", "u", "v", "object_id")))
+    # the network alone: top-2 prediction time on the same rays
+    d_top2 = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+    ms_predict = timed(lambda: L.j3dg_learned_predict(net.h, d_rays.data_ptr(), n, d_top2.data_ptr()))
+    flops = 2.0 * (256 * 128 + 3 * 128 * 128 + 128 * 4096) * n
+    line = {"metric": "learned vs plain closest-hit Mrays/s (config 3)", "value": round(n / ms_learned / 1e3, 3),
+            "unit": "Mrays/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 network / f32 traversal",
+            "data": "synthetic (seeded displaced torus; training rays from cameras at radius 2-5)",
+            "config": {"workload": "torus 28.09M tris, primary rays of 4 cameras at 1920x1080 (%d rays)" % n,
+                       "clusters": net.n_clusters, "params": net.n_params, "train_rays": args.learned_rays,
+                       "train_seconds": round(train_s, 2), "train_final_loss": round(loss, 4),
+                       "train_top1_accuracy": round(acc, 4),
+                       "plain_ms": round(ms_plain, 3), "learned_ms": round(ms_learned, 3),
+                       "network_predict_ms": round(ms_predict, 3),
+                       "network_tflops": round(flops / (ms_predict / 1e3) / 1e12, 2),
+                       "plain_mrays_s": round(n / ms_plain / 1e3, 3),
+                       "learned_over_plain": round(ms_plain / ms_learned, 4),
+                       "hits_identical": same, "hit_fraction": round(float(hp["found"].mean()), 4),
+                       "plain_node_visits_per_ray": round(pv / n, 3), "learned_node_visits_per_ray": round(lv / n, 3),
+                       "plain_tri_tests_per_ray": round(pt / n, 3), "learned_tri_tests_per_ray": round(lt / n, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -497,11 +604,12 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve"],
+    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve", "learned"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
                          "serve: config-4 request serving")
     ap.add_argument("--serve-rate", type=float, default=400.0)
     ap.add_argument("--serve-requests", type=int, default=1200)
+    ap.add_argument("--learned-rays", type=int, default=50_000_000)
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--batch-cameras", type=int, default=16)
     args = ap.parse_args()
@@ -509,6 +617,8 @@ def main():
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "learned":
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

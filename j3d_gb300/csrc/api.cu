@@ -265,6 +265,9 @@ namespace j3dg {
 
 int ctx_fail(j3dg_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
 
+// node-visit / triangle-test counters while counting is on, else null
+unsigned long long* ctx_counters(j3dg_ctx* c) { return all(c)->ex.counting ? all(c)->ex.d_counters : nullptr; }
+
 // The device instance table of one mesh with the identity transform.
 int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out) {
   if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh of another context");
@@ -280,7 +283,8 @@ int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out) {
 int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits) {
   const DevInst* dinst = nullptr;
   if (int rc = mesh_devinst(c, mesh, &dinst)) return rc;
-  CK(c, launch_rays(dinst, 1, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, S(c)), "ray query");
+  CK(c, launch_rays(dinst, 1, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, nullptr, S(c)),
+     "ray query");
   return J3DG_OK;
 }
 
@@ -559,7 +563,9 @@ static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, con
     CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "rays");
   }
   if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n, S(c)), "hits");
-  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, S(c)), "find");
+  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, j3dg::ctx_counters(c),
+                          S(c)),
+     "find");
   if (!hits_dev) {
     CK(c, cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * (size_t)n, cudaMemcpyDeviceToHost, S(c)), "hits");
     cudaFreeAsync(dh, S(c));

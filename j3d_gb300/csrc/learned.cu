@@ -35,6 +35,7 @@ namespace j3dg {
 int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits);
 int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out);
 int ctx_fail(j3dg_ctx* c, int code, const std::string& msg);
+unsigned long long* ctx_counters(j3dg_ctx* c);
 }
 
 namespace j3dg {
@@ -135,13 +136,15 @@ __global__ void k_softmax_ce(const float* __restrict__ logits, const int32_t* __
   }
 }
 
-// column sums of a bf16 [rows x cols] matrix into fp32
+// column sums of a bf16 [rows x cols] matrix into fp32 `out` (zeroed by the
+// caller): blockIdx.y takes a chunk of 128 rows, atomics combine the chunks
 __global__ void k_colsum(const __nv_bfloat16* __restrict__ M, uint32_t rows, uint32_t cols, float* __restrict__ out) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cols) return;
+  const uint32_t r0 = blockIdx.y * 128u, r1 = min(rows, r0 + 128u);
   float s = 0.f;
-  for (uint32_t r = 0; r < rows; ++r) s += __bfloat162float(M[(size_t)r * cols + c]);
-  out[c] = s;
+  for (uint32_t r = r0; r < r1; ++r) s += __bfloat162float(M[(size_t)r * cols + c]);
+  atomicAdd(out + c, s);
 }
 
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -460,7 +463,9 @@ int backward(j3dg_learned* l, uint32_t B, float inv_valid) {
     GemmArgs a{l->H[3], l->dZ5, g + l->L.w[4], nullptr, nullptr, j3dg::kHid, j3dg::kOut, (int)B, j3dg::kHid, j3dg::kOut,
                j3dg::kOut};
     LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
-    j3dg::k_colsum<<<(j3dg::kOut + 255) / 256, 256, 0, LS(l)>>>(l->dZ5, B, j3dg::kOut, g + l->L.b[4]);
+    LCK(cudaMemsetAsync(g + l->L.b[4], 0, sizeof(float) * j3dg::kOut, LS(l)), "learned backward");
+    j3dg::k_colsum<<<dim3((j3dg::kOut + 255) / 256, (B + 127) / 128), 256, 0, LS(l)>>>(l->dZ5, B, j3dg::kOut,
+                                                                                        g + l->L.b[4]);
     GemmArgs d{l->dZ5, W(l, 4), l->dA, l->Z[3], nullptr, (int)B, j3dg::kHid, j3dg::kOut, j3dg::kOut, j3dg::kOut,
                j3dg::kHid};
     LCK(j3dg::gemm_bf16(d, false, true, j3dg::EPI_GELU_BWD, LS(l)), "learned backward");
@@ -472,7 +477,8 @@ int backward(j3dg_learned* l, uint32_t B, float inv_valid) {
     const int in_dim = k ? j3dg::kHid : j3dg::kIn;
     GemmArgs a{in, dcur, g + l->L.w[k], nullptr, nullptr, in_dim, j3dg::kHid, (int)B, in_dim, j3dg::kHid, j3dg::kHid};
     LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
-    j3dg::k_colsum<<<1, 128, 0, LS(l)>>>(dcur, B, j3dg::kHid, g + l->L.b[k]);
+    LCK(cudaMemsetAsync(g + l->L.b[k], 0, sizeof(float) * j3dg::kHid, LS(l)), "learned backward");
+    j3dg::k_colsum<<<dim3(1, (B + 127) / 128), 128, 0, LS(l)>>>(dcur, B, j3dg::kHid, g + l->L.b[k]);
     if (k > 0) {
       GemmArgs d{dcur, W(l, k), dnext, l->Z[k - 1], nullptr, (int)B, j3dg::kHid, j3dg::kHid, j3dg::kHid, j3dg::kHid,
                  j3dg::kHid};
@@ -789,7 +795,7 @@ int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n,
   const DevInst* dinst = nullptr;
   if (rc == J3DG_OK) rc = j3dg::mesh_devinst(c, l->mesh, &dinst);
   if (rc == J3DG_OK) {
-    unsigned long long* counters = nullptr;
+    unsigned long long* counters = j3dg::ctx_counters(c);
     j3dg::k_rays_learned<<<(n + 127) / 128, 128, 0, LS(l)>>>(dinst, dr, n, dt, l->d_roots, l->n_clusters, dh,
                                                             c->d_status, counters);
     LCK(cudaGetLastError(), "learned find");

@@ -335,9 +335,9 @@ template <bool ANY>
 __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restrict__ inst, uint32_t n_inst,
                                                         const j3dg_ray* __restrict__ rays, uint32_t n,
                                                         j3dg_hit* __restrict__ hits, uint32_t* counter,
-                                                        uint32_t* status) {
+                                                        uint32_t* status, unsigned long long* counters) {
   BatchSrc<ANY> src{rays, hits, n};
-  persistent_trace<kIters>(src, inst, n_inst, counter, status, nullptr);
+  persistent_trace<kIters>(src, inst, n_inst, counter, status, counters);
 }
 
 // Many frames (canvases, scenes, cameras, resolutions of uneven size) in one
@@ -631,7 +631,7 @@ cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st) {
 }
 
 cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* counter, uint32_t* status, cudaStream_t st) {
+                        bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   static int blocks_c = 0, blocks_a = 0;
   if (!blocks_c) {
@@ -641,9 +641,9 @@ cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* ra
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (any)
-    k_rays<true><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status);
+    k_rays<true><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
   else
-    k_rays<false><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status);
+    k_rays<false><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
   return cudaGetLastError();
 }
 

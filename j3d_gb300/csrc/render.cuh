@@ -42,6 +42,6 @@ cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaSt
 cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* counter, uint32_t* status, cudaStream_t st);
+                        bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters, cudaStream_t st);
 
 }  // namespace j3dg

@@ -335,13 +335,14 @@ def run_own(args):
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "frame = k_primary + k_shadow (timed together per frame)", "peak_kind": peak_kind,
+                     "kernel": "k_frame (primary + shadow + shading, one launch per frame)", "peak_kind": peak_kind,
                      "bytes_per_ray": round(alg_bytes / rays_per_step, 1),
                      "node_visits_per_ray": round(node_per_ray, 3), "tri_tests_per_ray": round(tri_per_ray, 3),
-                     "per_ray_model": "36 B per primary ray + node_visits*128 B + tri_tests*48 B (oracle BVH4 SAH)"},
+                     "per_ray_model": "36 B per primary ray + node_visits*128 B + tri_tests*48 B ("
+                                      + ("oracle BVH4 SAH counts" if cpu else "GPU BVH counts") + ")"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": 2 * N_CAMERAS * args.steps,  # k_primary + k_shadow per frame
+        "gpu_launches": N_CAMERAS * args.steps,  # one k_frame per frame
         "clocks": clk,
     }
     if cpu:

@@ -33,6 +33,13 @@ N_CAMERAS = 32
 NODE_BYTES = 128      # one BVH4 node: 4 child AABBs (96 B) + 4 refs, padded
 TRI_BYTES = 48        # 12 B index triple + 36 B of vertices per tested triangle
 RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
+# DRAM and L2 bytes of one k_frame launch on this workload (leaf size 2),
+# mean over the 32 launches of one step, from an ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
+# (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
+# --warmup 3 --no-cpu`): reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB.
+FRAME_DRAM_BYTES = 463_159_392 + 70_692_880
+FRAME_L2_BYTES = 1_837_113_990
 
 
 def peaks():
@@ -334,7 +341,11 @@ def run_own(args):
                        gpu_node_visits_per_ray=round(gvis / rays_per_step, 3),
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4),
+                     "traffic": FRAME_DRAM_BYTES if args.leaf == 2 else None,
+                     "traffic_l2": FRAME_L2_BYTES if args.leaf == 2 else None,
+                     "traffic_note": "bytes per k_frame launch (ncu, mean of the 32 cameras); the algorithmic "
+                                     "bytes per launch are bytes_per_ray x rays_per_step / 32",
                      "kernel": "k_frame (primary + shadow + shading, one launch per frame)", "peak_kind": peak_kind,
                      "bytes_per_ray": round(alg_bytes / rays_per_step, 1),
                      "node_visits_per_ray": round(node_per_ray, 3), "tri_tests_per_ray": round(tri_per_ray, 3),
@@ -595,6 +606,91 @@ def run_learned(args):
     return 0
 
 
+def run_ingest(args):
+    """Mesh ingest: the 28.09M-triangle torus written as a binary PLY (the
+    Stanford scan layout: float xyz, uchar count + int indices) and as a
+    binary STL, read from the file straight into a device mesh with its BVH
+    (j3dg_geometry_read_file + j3dg_mesh_build_geometry), wall clock per
+    load. The file is in the page cache (written just before). An OBJ of
+    2.1M triangles times the host-threaded text path. The CPU baseline
+    parses the same PLY with numpy and builds the oracle's BVH on the host
+    cores."""
+    import shutil
+    import tempfile
+
+    from j3d_gb300 import Context, Geometry, mesh_from_geometry, workloads as W
+    from oracle import formats as F
+
+    ctx = Context(0)
+    V, T = W.torus()
+    tmp = Path(tempfile.mkdtemp(prefix="j3dg_ingest_"))
+    out = {}
+    try:
+        files = {"ply": tmp / "torus.ply", "stl": tmp / "torus.stl"}
+        files["ply"].write_bytes(F.write_ply_triangles_fast(V, T))
+        files["stl"].write_bytes(F.write_stl_binary(V, T))
+        Vo, To = W.torus(1030, 1030, seed=W.SEED_BASE + 75)
+        files["obj"] = tmp / "torus2M.obj"
+        with open(files["obj"], "w") as f:
+            f.write("".join(f"v {a!r} {b!r} {c!r}\n" for a, b, c in Vo.astype(np.float64).tolist()))
+            f.write("".join(f"f {a + 1} {b + 1} {c + 1}\n" for a, b, c in To.tolist()))
+        for fmt, path in files.items():
+            times, infos, builds = [], [], []
+            for rep in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                g = Geometry.read_file(ctx, path)
+                m = mesh_from_geometry(ctx, g, args.leaf)
+                dt = time.perf_counter() - t0
+                if rep >= args.warmup:
+                    times.append(dt)
+                    infos.append(g.info)
+                    builds.append(m.info().build_ms)
+                m.close()
+                g.close()
+            i = infos[-1]
+            size = path.stat().st_size
+            out[fmt] = {"file_mb": round(size / 1e6, 1), "triangles": int(i.n_triangles),
+                        "vertices": int(i.n_vertices), "load_and_build_ms": round(1e3 * float(np.median(times)), 1),
+                        "read_ms": round(float(np.median([x.read_ms for x in infos])), 1),
+                        "decode_ms": round(float(np.median([x.decode_ms for x in infos])), 1),
+                        "bvh_build_ms_device": round(float(np.median(builds)), 2),
+                        "device_decoded": bool(i.device_decoded),
+                        "file_gb_per_s": round(size / float(np.median(times)) / 1e9, 2)}
+        cpu = None
+        if not args.no_cpu:
+            import oracle.oracle as O
+            O.build()
+            t0 = time.perf_counter()
+            data = files["ply"].read_bytes()
+            enc, elements, at = F.parse_ply_header(data)
+            nv, nf = elements[0]["count"], elements[1]["count"]
+            Vc = np.frombuffer(data, "<f4", 3 * nv, at).reshape(-1, 3)
+            fr = np.frombuffer(data, np.dtype([("n", "u1"), ("i", "<i4", 3)]), nf, at + 12 * nv)
+            assert (fr["n"] == 3).all()
+            Tc = fr["i"].astype(np.uint32)
+            t_parse = time.perf_counter() - t0
+            m = O.Mesh(np.ascontiguousarray(Vc), Tc, 4, os.cpu_count() or 1)
+            cpu = {"value": round(1e3 * (t_parse + m.build_seconds), 1), "unit": "ms",
+                   "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"numpy parse of the same PLY ({1e3 * t_parse:.0f} ms) + the oracle's binned-SAH "
+                             f"BVH4 build on all host threads ({1e3 * m.build_seconds:.0f} ms), one load"}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    line = {"metric": "mesh ingest: file -> device mesh + BVH (load + build ms, 28.09M-tri binary PLY)",
+            "value": out["ply"]["load_and_build_ms"], "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "dtype": "f32",
+            "data": "synthetic (seeded displaced torus written to a local file, page cache warm)",
+            "config": {"workload": "torus 28,090,000 tris as binary PLY (532 MB) and binary STL (1.4 GB); "
+                                   "torus 2.12M tris as OBJ", "formats": out,
+                       "reference_published": "README.md:37-45 (Lucy, 28.06M tris, other hardware): PLY load "
+                                              "2.52 s, STL 4.53 s, OBJ 34 s; BVH build 3.6 s"},
+            "gpu_launches": None}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -605,7 +701,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve", "learned"],
+    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve", "learned", "ingest"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
                          "serve: config-4 request serving")
     ap.add_argument("--serve-rate", type=float, default=400.0)
@@ -620,6 +716,8 @@ def main():
         return run_serve(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "ingest":
+        return run_ingest(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

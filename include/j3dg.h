@@ -226,6 +226,65 @@ int j3dg_voxelize(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32
 int j3dg_voxelize_noalloc(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3],
                           uint8_t* voxels, uint64_t capacity);
 
+/* ----------------------------------------------------------- mesh ingest --
+   mesh.cpp:76-176 read_from_file and pc.cpp:32-110 pick a reader from the
+   file extension (io.h:8-43; PLY/STL/OFF through jtk, OBJ/XYZ/PTS in
+   io.cpp:292-713) and hand host vectors to add_object. Here the file goes
+   to the device in pinned chunks and binary bodies (PLY, STL) are decoded
+   there; text formats are parsed on host threads and uploaded. The decoded
+   arrays stay on the device and feed j3dg_mesh_build_geometry (which
+   computes the bbox and normals on the device, scene.cpp:20) without a host
+   round trip. TRC (trico) is not supported: its format has no
+   specification in the reference. */
+
+typedef struct j3dg_geometry j3dg_geometry;
+
+typedef enum j3dg_file_format {
+  J3DG_FORMAT_AUTO = 0, /* from the extension (read_file) or the content (read_memory) */
+  J3DG_FORMAT_PLY = 1,
+  J3DG_FORMAT_STL = 2,
+  J3DG_FORMAT_OBJ = 3,
+  J3DG_FORMAT_OFF = 4,
+  J3DG_FORMAT_XYZ = 5,
+  J3DG_FORMAT_PTS = 6
+} j3dg_file_format;
+
+typedef struct j3dg_geometry_info {
+  uint64_t n_vertices;
+  uint64_t n_triangles;
+  uint32_t format;      /* j3dg_file_format that was read */
+  uint32_t encoding;    /* 0 text, 1 binary little endian, 2 binary big endian */
+  uint32_t has_colors;  /* per-vertex 0xff000000 | b << 16 | g << 8 | r */
+  uint32_t has_normals; /* per-vertex normals (3 floats) */
+  uint32_t has_uv;      /* per-triangle texture coordinates (6 floats) */
+  uint32_t device_decoded; /* 1 when the body was decoded by device kernels */
+  uint64_t file_bytes;
+  float read_ms;        /* file -> host (pinned chunks) */
+  float decode_ms;      /* host parse + upload + device decode after the read */
+  float total_ms;       /* wall time of the whole call */
+  float reserved;
+} j3dg_geometry_info;
+
+/* read_from_file's reader dispatch (mesh.cpp:76-176, pc.cpp:32-110) into
+   device arrays. format = J3DG_FORMAT_AUTO picks the reader from the
+   extension as mesh.cpp:88-92 does. */
+int j3dg_geometry_read_file(j3dg_ctx* ctx, const char* path, int format, j3dg_geometry** out);
+/* The same readers over bytes already in memory (format AUTO: PLY/OFF by
+   their magic, "solid" or the binary size rule for STL, else an error). */
+int j3dg_geometry_read_memory(j3dg_ctx* ctx, const void* bytes, uint64_t n_bytes, int format,
+                              j3dg_geometry** out);
+int j3dg_geometry_get_info(const j3dg_geometry* g, j3dg_geometry_info* info);
+/* Copies the arrays out (host or device pointers; NULL skips an array):
+   vertices V x 3, triangles T x 3, colors V, normals V x 3, uv T x 6. */
+int j3dg_geometry_get_arrays(const j3dg_geometry* g, float* vertices, uint32_t* triangles, uint32_t* colors,
+                             float* normals, float* uv);
+int j3dg_geometry_destroy(j3dg_geometry* g);
+/* add_object's mesh (scene.cpp:17-26) from decoded geometry: the BVH build
+   of j3dg_mesh_build on the device arrays, vertex colours converted as
+   mesh.cpp:216-228 does, uv kept, and mesh.cpp:172-173's 512 x 512 dummy
+   checker texture when there are uv but no texture. */
+int j3dg_mesh_build_geometry(j3dg_ctx* ctx, const j3dg_geometry* g, const j3dg_build_opts* opts, j3dg_mesh** out);
+
 /* ---------------------------------------------------------------- matcaps */
 
 /* matcap.h:18-24: a w x h RGBA8 texture plus its cavity colour, uploaded once. */

@@ -72,6 +72,15 @@ class MeshInfo(C.Structure):
                 ("device_bytes", C.c_uint64), ("build_ms", C.c_float)]
 
 
+class GeometryInfo(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint64), ("n_triangles", C.c_uint64), ("format", C.c_uint32),
+                ("encoding", C.c_uint32), ("has_colors", C.c_uint32), ("has_normals", C.c_uint32),
+                ("has_uv", C.c_uint32), ("device_decoded", C.c_uint32), ("file_bytes", C.c_uint64),
+                ("read_ms", C.c_float), ("decode_ms", C.c_float), ("total_ms", C.c_float), ("reserved", C.c_float)]
+
+
+FORMATS = {"auto": 0, "ply": 1, "stl": 2, "obj": 3, "off": 4, "xyz": 5, "pts": 6}
+
 _P = C.c_void_p
 _I = C.c_int
 _U = C.c_uint32
@@ -104,6 +113,12 @@ SIGNATURES = {
     "j3dg_voxelize_noalloc": (_I, [_P, _P, _U, C.POINTER(_U), _P, C.c_uint64]),
     "j3dg_get_closest_vertex": (_U, [_P, _P, _P]),
     "j3dg_get_world_position": (None, [_P, _P, _P, _FP, _FP]),
+    "j3dg_geometry_read_file": (_I, [_P, C.c_char_p, _I, C.POINTER(_P)]),
+    "j3dg_geometry_read_memory": (_I, [_P, _P, C.c_uint64, _I, C.POINTER(_P)]),
+    "j3dg_geometry_get_info": (_I, [_P, C.POINTER(GeometryInfo)]),
+    "j3dg_geometry_get_arrays": (_I, [_P, _P, _P, _P, _P, _P]),
+    "j3dg_geometry_destroy": (_I, [_P]),
+    "j3dg_mesh_build_geometry": (_I, [_P, _P, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_matcap_create": (_I, [_P, _P, _U, _U, _U, C.POINTER(_P)]),
     "j3dg_matcap_destroy": (_I, [_P]),
     "j3dg_canvas_create": (_I, [_P, _U, _U, C.POINTER(_P)]),

@@ -24,8 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-c
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
-CU_SOURCES = ["build.cu", "render.cu", "query.cu", "mlp_gemm.cu", "learned.cu", "api.cu"]
-CXX_SOURCES = ["host_math.cpp"]
+CU_SOURCES = ["build.cu", "render.cu", "query.cu", "mlp_gemm.cu", "learned.cu", "ingest.cu", "api.cu"]
+CXX_SOURCES = ["host_math.cpp", "ingest_parse.cpp"]
 
 
 def nvcc() -> str:

@@ -118,6 +118,71 @@ class Mesh:
         _check(self.ctx.h, lib().j3dg_mesh_set_texture(self.h, vptr(tex), w, h))
 
 
+class Geometry:
+    """Decoded mesh / point-cloud file resident on the device: the reader
+    dispatch of read_from_file (mesh.cpp:76-176, pc.cpp:32-110)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.h = handle
+        i = _ffi.GeometryInfo()
+        _check(ctx.h, lib().j3dg_geometry_get_info(self.h, C.byref(i)))
+        self.info = i
+
+    @classmethod
+    def read_file(cls, ctx: Context, path, fmt: str = "auto") -> "Geometry":
+        h = C.c_void_p()
+        _check(ctx.h, lib().j3dg_geometry_read_file(ctx.h, str(path).encode(), _ffi.FORMATS[fmt], C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def read_memory(cls, ctx: Context, data: bytes, fmt: str = "auto") -> "Geometry":
+        buf = np.frombuffer(data, np.uint8) if len(data) else np.zeros(1, np.uint8)
+        h = C.c_void_p()
+        _check(ctx.h, lib().j3dg_geometry_read_memory(ctx.h, buf.ctypes.data, len(data), _ffi.FORMATS[fmt],
+                                                      C.byref(h)))
+        return cls(ctx, h)
+
+    def arrays(self) -> dict:
+        """Host copies: vertices (V,3), triangles (T,3), and colors (V,),
+        normals (V,3), uv (T,6) when present."""
+        i = self.info
+        out = {"vertices": np.empty((i.n_vertices, 3), np.float32),
+               "triangles": np.empty((i.n_triangles, 3), np.uint32)}
+        if i.has_colors:
+            out["colors"] = np.empty(i.n_vertices, np.uint32)
+        if i.has_normals:
+            out["normals"] = np.empty((i.n_vertices, 3), np.float32)
+        if i.has_uv:
+            out["uv"] = np.empty((i.n_triangles, 6), np.float32)
+        _check(self.ctx.h, lib().j3dg_geometry_get_arrays(
+            self.h, vptr(out["vertices"]), vptr(out["triangles"]), vptr(out.get("colors")),
+            vptr(out.get("normals")), vptr(out.get("uv"))))
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_geometry_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2) -> Mesh:
+    """add_object's mesh built straight from device-resident geometry."""
+    m = Mesh.__new__(Mesh)
+    m.ctx = ctx
+    h = C.c_void_p()
+    opts = BuildOpts(leaf_size, 0)
+    _check(ctx.h, lib().j3dg_mesh_build_geometry(ctx.h, geom.h, C.byref(opts), C.byref(h)))
+    m.h = h
+    return m
+
+
 class SceneObject:
     def __init__(self, mesh: Mesh, cs=None, db_id: int = 1):
         self.mesh = mesh

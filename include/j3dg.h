@@ -285,6 +285,45 @@ int j3dg_geometry_destroy(j3dg_geometry* g);
    checker texture when there are uv but no texture. */
 int j3dg_mesh_build_geometry(j3dg_ctx* ctx, const j3dg_geometry* g, const j3dg_build_opts* opts, j3dg_mesh** out);
 
+/* ------------------------------------------------------------ point clouds --
+   pc.h:23-31 / scene_pointcloud (scene.h:27-38): vertices (+ packed RGBA8
+   colours) resident on the device, drawn after the mesh frame by
+   canvas::render_pointclouds_on_image (canvas.cpp:952-1030). */
+
+typedef struct j3dg_pointcloud j3dg_pointcloud;
+
+typedef struct j3dg_pointcloud_instance {
+  const j3dg_pointcloud* pointcloud;
+  float cs[16];     /* pc::cs, column-major */
+  uint32_t db_id;
+  uint32_t reserved;
+} j3dg_pointcloud_instance;
+
+/* Uploads n points (vertices n x 3, colors n or NULL; host or device
+   pointers) and computes their bbox (compute_bb, mesh.cpp:39-58). */
+int j3dg_pointcloud_create(j3dg_ctx* ctx, const float* vertices, uint64_t n, const uint32_t* colors,
+                           j3dg_pointcloud** out);
+/* The vertices (and colours) of decoded geometry as a point cloud, on the
+   device (pc.cpp:32-110 reads point clouds with the mesh readers). */
+int j3dg_pointcloud_from_geometry(j3dg_ctx* ctx, const j3dg_geometry* g, j3dg_pointcloud** out);
+int j3dg_pointcloud_destroy(j3dg_pointcloud* pc);
+int j3dg_pointcloud_get_bounds(const j3dg_pointcloud* pc, float min_bb[3], float max_bb[3]);
+/* scene.cpp:50-89 prepare_scene over mesh objects and point clouds. */
+int j3dg_prepare_scene_pointclouds(const j3dg_instance* objects, uint32_t n, const j3dg_pointcloud_instance* pcs,
+                                   uint32_t n_pcs, float min_bb[3], float max_bb[3], float* diagonal);
+/* canvas::render_pointclouds_on_image (canvas.cpp:952-1030) after a frame:
+   a depth buffer of 1/depth from the G-buffer (0 where db_id is 0), then
+   each cloud in order: every point projected through its cs, the scene's
+   coordinate_system_inv and the canvas projection onto the pixel whose
+   primary ray passes nearest to it, kept where its 1/depth is strictly
+   greater (equal depths: the smaller vertex id); the pixel's object_id,
+   depth (1 / (1/depth)) and db_id are set and its image colour becomes the
+   point's colour (white without colours or in one_bit mode). Points at or
+   before the near clipping plane are not drawn. The shading of points by
+   their normals is not done (jtk/render.h, which does it, is absent). */
+int j3dg_canvas_render_pointclouds(j3dg_canvas* c, const j3dg_scene* s, const j3dg_pointcloud_instance* pcs,
+                                   uint32_t n_pcs);
+
 /* ---------------------------------------------------------------- matcaps */
 
 /* matcap.h:18-24: a w x h RGBA8 texture plus its cavity colour, uploaded once. */

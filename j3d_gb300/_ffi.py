@@ -79,6 +79,10 @@ class GeometryInfo(C.Structure):
                 ("read_ms", C.c_float), ("decode_ms", C.c_float), ("total_ms", C.c_float), ("reserved", C.c_float)]
 
 
+class PointCloudInstance(C.Structure):
+    _fields_ = [("pointcloud", C.c_void_p), ("cs", C.c_float * 16), ("db_id", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 FORMATS = {"auto": 0, "ply": 1, "stl": 2, "obj": 3, "off": 4, "xyz": 5, "pts": 6}
 
 _P = C.c_void_p
@@ -119,6 +123,13 @@ SIGNATURES = {
     "j3dg_geometry_get_arrays": (_I, [_P, _P, _P, _P, _P, _P]),
     "j3dg_geometry_destroy": (_I, [_P]),
     "j3dg_mesh_build_geometry": (_I, [_P, _P, C.POINTER(BuildOpts), C.POINTER(_P)]),
+    "j3dg_pointcloud_create": (_I, [_P, _P, C.c_uint64, _P, C.POINTER(_P)]),
+    "j3dg_pointcloud_from_geometry": (_I, [_P, _P, C.POINTER(_P)]),
+    "j3dg_pointcloud_destroy": (_I, [_P]),
+    "j3dg_pointcloud_get_bounds": (_I, [_P, _FP, _FP]),
+    "j3dg_prepare_scene_pointclouds": (_I, [C.POINTER(Instance), _U, C.POINTER(PointCloudInstance), _U, _FP, _FP,
+                                            _FP]),
+    "j3dg_canvas_render_pointclouds": (_I, [_P, C.POINTER(Scene), C.POINTER(PointCloudInstance), _U]),
     "j3dg_matcap_create": (_I, [_P, _P, _U, _U, _U, C.POINTER(_P)]),
     "j3dg_matcap_destroy": (_I, [_P]),
     "j3dg_canvas_create": (_I, [_P, _U, _U, C.POINTER(_P)]),

@@ -222,6 +222,35 @@ extern "C" int j3dg_prepare_scene(const j3dg_instance* objects, uint32_t n, floa
   return J3DG_OK;
 }
 
+extern "C" int j3dg_prepare_scene_pointclouds(const j3dg_instance* objects, uint32_t n, const j3dg_pointcloud_instance* pcs,
+                                              uint32_t n_pcs, float* mn, float* mx, float* diagonal) {
+  // scene.cpp:50-89: the first mesh object's box (else the first cloud's)
+  // widened by every object's and every cloud's box, each through its cs
+  if (!mn || !mx || !diagonal || (n && !objects) || (n_pcs && !pcs)) return J3DG_ERR_INVALID_ARGUMENT;
+  if (int rc = j3dg_prepare_scene(objects, n, mn, mx, diagonal)) return rc;
+  for (uint32_t i = 0; i < n_pcs; ++i) {
+    if (!pcs[i].pointcloud) return J3DG_ERR_INVALID_ARGUMENT;
+    float a[3], b[3], v[4], r[4];
+    for (int k = 0; k < 3; ++k) v[k] = pcs[i].pointcloud->min_bb[k];
+    v[3] = 1.f;
+    mat_vec(pcs[i].cs, v, r);
+    for (int k = 0; k < 3; ++k) a[k] = r[k];
+    for (int k = 0; k < 3; ++k) v[k] = pcs[i].pointcloud->max_bb[k];
+    mat_vec(pcs[i].cs, v, r);
+    for (int k = 0; k < 3; ++k) b[k] = r[k];
+    for (int k = 0; k < 3; ++k) {
+      const float lo = std::min(a[k], b[k]), hi = std::max(a[k], b[k]);
+      mn[k] = (n == 0 && i == 0) ? lo : std::min(mn[k], lo);
+      mx[k] = (n == 0 && i == 0) ? hi : std::max(mx[k], hi);
+    }
+  }
+  float d = mx[0] - mn[0];
+  d = std::max<float>(d, mx[1] - mn[1]);
+  d = std::max<float>(d, mx[2] - mn[2]);
+  *diagonal = d;
+  return J3DG_OK;
+}
+
 extern "C" void j3dg_unzoom(const float* mn, const float* mx, float diagonal, float* cs, float* cs_inv, float* pivot) {
   // scene.cpp:91-110, y axis up
   for (int i = 0; i < 16; ++i) cs[i] = (i % 5 == 0) ? 1.f : 0.f;

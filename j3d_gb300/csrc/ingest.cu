@@ -29,17 +29,6 @@
 
 using namespace j3dg::ingest;
 
-struct j3dg_geometry {
-  j3dg_ctx* ctx = nullptr;
-  uint64_t nv = 0, nt = 0;
-  float* d_v = nullptr;
-  uint32_t* d_t = nullptr;
-  uint32_t* d_c = nullptr;
-  float* d_n = nullptr;
-  float* d_uv = nullptr;
-  j3dg_geometry_info info;
-};
-
 namespace j3dg {
 int ctx_fail(j3dg_ctx* c, int code, const std::string& msg);
 }

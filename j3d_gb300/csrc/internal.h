@@ -65,3 +65,24 @@ struct j3dg_canvas {
   void* d_queue = nullptr;       // shadow-ray jobs, 2 float4 per pixel
   uint32_t* d_work = nullptr;    // per-frame work counters
 };
+
+// Decoded mesh / point-cloud file on the device (ingest.cu).
+struct j3dg_geometry {
+  j3dg_ctx* ctx = nullptr;
+  uint64_t nv = 0, nt = 0;
+  float* d_v = nullptr;      // 3 nv
+  uint32_t* d_t = nullptr;   // 3 nt
+  uint32_t* d_c = nullptr;   // nv packed RGBA8, or null
+  float* d_n = nullptr;      // 3 nv, or null
+  float* d_uv = nullptr;     // 6 nt, or null
+  j3dg_geometry_info info;
+};
+
+// Point cloud on the device (pointcloud.cu).
+struct j3dg_pointcloud {
+  j3dg_ctx* ctx = nullptr;
+  uint64_t n = 0;
+  float* d_v = nullptr;      // 3 n
+  uint32_t* d_c = nullptr;   // n packed RGBA8, or null
+  float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
+};

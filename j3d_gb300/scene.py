@@ -172,6 +172,46 @@ class Geometry:
             pass
 
 
+class PointCloud:
+    """pc (pc.h:23-31): points and optional packed RGBA8 colours on the device."""
+
+    def __init__(self, ctx: Context, vertices=None, colors=None, geometry: "Geometry | None" = None):
+        self.ctx = ctx
+        h = C.c_void_p()
+        if geometry is not None:
+            _check(ctx.h, lib().j3dg_pointcloud_from_geometry(ctx.h, geometry.h, C.byref(h)))
+        else:
+            n = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
+            _check(ctx.h, lib().j3dg_pointcloud_create(ctx.h, vptr(vertices), n, vptr(colors), C.byref(h)))
+        self.h = h
+
+    def bounds(self) -> tuple[np.ndarray, np.ndarray]:
+        mn = np.zeros(3, np.float32)
+        mx = np.zeros(3, np.float32)
+        _check(self.ctx.h, lib().j3dg_pointcloud_get_bounds(self.h, fptr(mn), fptr(mx)))
+        return mn, mx
+
+    def close(self) -> None:
+        if self.h:
+            lib().j3dg_pointcloud_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ScenePointCloud:
+    """scene_pointcloud (scene.h:27-38)."""
+
+    def __init__(self, pc: PointCloud, cs=None, db_id: int = 2):
+        self.pointcloud = pc
+        self.cs = np.ascontiguousarray(IDENTITY if cs is None else np.asarray(cs, np.float32).reshape(16))
+        self.db_id = db_id
+
+
 def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2) -> Mesh:
     """add_object's mesh built straight from device-resident geometry."""
     m = Mesh.__new__(Mesh)
@@ -195,12 +235,27 @@ class Scene:
 
     def __init__(self):
         self.objects: list[SceneObject] = []
+        self.pointclouds: list[ScenePointCloud] = []
         self.coordinate_system = IDENTITY.copy()
         self.coordinate_system_inv = IDENTITY.copy()
         self.pivot = np.zeros(3, np.float32)
         self.min_bb = np.zeros(3, np.float32)
         self.max_bb = np.zeros(3, np.float32)
         self.diagonal = np.float32(0)
+
+    def add_pointcloud(self, pc: PointCloud, cs=None, db_id: int = 2) -> ScenePointCloud:
+        # scene.cpp:27-36
+        o = ScenePointCloud(pc, cs, db_id)
+        self.pointclouds.append(o)
+        return o
+
+    def _pc_instances(self):
+        arr = (_ffi.PointCloudInstance * max(1, len(self.pointclouds)))()
+        for i, o in enumerate(self.pointclouds):
+            arr[i].pointcloud = o.pointcloud.h
+            C.memmove(arr[i].cs, o.cs.ctypes.data, 64)
+            arr[i].db_id = o.db_id
+        return arr
 
     def add_object(self, mesh: Mesh, cs=None, db_id: int = 1) -> SceneObject:
         # scene.cpp:8-38 (the BVH was built when the Mesh was made)
@@ -213,7 +268,11 @@ class Scene:
         for i, o in enumerate(self.objects):
             if o.db_id == db_id:
                 del self.objects[i]
-                return
+                break
+        for i, o in enumerate(self.pointclouds):
+            if o.db_id == db_id:
+                del self.pointclouds[i]
+                break
 
     def _instances(self):
         arr = (Instance * max(1, len(self.objects)))()
@@ -230,7 +289,11 @@ class Scene:
         mx = np.zeros(3, np.float32)
         d = np.zeros(1, np.float32)
         ctx = self.objects[0].mesh.ctx.h if self.objects else None
-        _check(ctx, lib().j3dg_prepare_scene(inst, len(self.objects), fptr(mn), fptr(mx), fptr(d)))
+        if self.pointclouds:
+            _check(ctx, lib().j3dg_prepare_scene_pointclouds(inst, len(self.objects), self._pc_instances(),
+                                                             len(self.pointclouds), fptr(mn), fptr(mx), fptr(d)))
+        else:
+            _check(ctx, lib().j3dg_prepare_scene(inst, len(self.objects), fptr(mn), fptr(mx), fptr(d)))
         self.min_bb, self.max_bb, self.diagonal = mn, mx, np.float32(d[0])
 
     def unzoom(self) -> None:
@@ -371,6 +434,13 @@ class Canvas:
         s, keep = scene.as_c()
         _check(self.ctx.h, lib().j3dg_canvas_render_frame(self.h, C.byref(s), matcap.h))
         del keep
+
+    def render_pointclouds(self, scene: Scene) -> None:
+        """canvas::render_pointclouds_on_image (canvas.cpp:952-1030) over the
+        scene's point clouds, after a frame."""
+        s, keep = scene.as_c()
+        pcs = scene._pc_instances()
+        _check(self.ctx.h, lib().j3dg_canvas_render_pointclouds(self.h, C.byref(s), pcs, len(scene.pointclouds)))
 
     def get_pixels(self, out=None):
         if out is None:

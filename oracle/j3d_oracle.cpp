@@ -1474,3 +1474,45 @@ uint64_t orc_voxelize(const orc_mesh* m, uint32_t max_dim, uint32_t* dims, uint8
 }
 
 }  // extern "C"
+
+// canvas.cpp:952-1030 render_pointclouds_on_image (sequential restatement)
+void orc_render_pointclouds(orc_pixel* pix, uint32_t* im, uint32_t w, uint32_t h, const float* P,
+                            const float* cs_inv, float near_plane, uint32_t n_clouds, const float* const* vertices,
+                            const uint64_t* counts, const uint32_t* const* colors, const float* cs,
+                            const uint32_t* db_ids, int one_bit) {
+  const size_t npix = (size_t)w * h;
+  std::vector<float> z(npix);
+  for (size_t i = 0; i < npix; ++i) z[i] = pix[i].db_id != 0 ? 1.f / pix[i].depth : 0.f;  // canvas.cpp:966
+  const float half_w = 0.5f * (float)w, half_h = 0.5f * (float)h;
+  for (uint32_t k = 0; k < n_clouds; ++k) {
+    const float* V = vertices[k];
+    const float* M = cs + 16 * (size_t)k;
+    for (uint64_t i = 0; i < counts[k]; ++i) {
+      float v[4] = {V[3 * i], V[3 * i + 1], V[3 * i + 2], 1.f}, wv[4], cv[4];
+      mat_vec(M, v, wv);
+      mat_vec(cs_inv, wv, cv);
+      const float d = -cv[2];
+      if (!(d > near_plane)) continue;
+      const float inv_d = 1.f / d;
+      float sx = P[0] * cv[0];
+      sx = sx * inv_d;
+      sx = sx + P[8];
+      float sy = P[5] * cv[1];
+      sy = sy * inv_d;
+      sy = sy + P[9];
+      const float fx = (sx + 1.f) * half_w;
+      const float fy = (sy + 1.f) * half_h;
+      if (!(fx >= 0.f && fx < (float)w && fy >= 0.f && fy < (float)h)) continue;
+      const uint32_t col = std::min((uint32_t)fx, w - 1), row = std::min((uint32_t)fy, h - 1);
+      const size_t idx = (size_t)row * w + col;
+      if (inv_d > z[idx]) {
+        z[idx] = inv_d;
+        pix[idx].object_id = (uint32_t)i;
+        pix[idx].depth = 1.f / z[idx];
+        pix[idx].db_id = db_ids[k];
+        im[idx] = (colors[k] && !one_bit) ? colors[k][i] : 0xffffffffu;
+      }
+    }
+  }
+}
+

@@ -130,6 +130,19 @@ uint32_t orc_find_all(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint
 uint32_t orc_find_all_brute(const orc_mesh* m, const orc_ray* ray, orc_hit* hits, uint32_t cap);
 
 /* ---- canvas.cpp ---- */
+/* canvas::render_pointclouds_on_image (canvas.cpp:952-1030), restated
+   sequentially: z-buffer of 1/depth from the G-buffer (0 where db_id is
+   0); for each cloud in order and each point in id order, the point in
+   camera space (cloud cs, then cs_inv), d = -z; drawn only for d > near;
+   pixel (floor((P0 x/d + P8 + 1) w/2), floor((P5 y/d + P9 + 1) h/2)); kept
+   when 1/d > z-buffer; sets object_id = point id, depth = 1/(1/d), db_id and
+   the image colour (the point colour, white without colours or one_bit).
+   colors[k] may be NULL. */
+void orc_render_pointclouds(orc_pixel* pix, uint32_t* im, uint32_t w, uint32_t h, const float projection[16],
+                            const float cs_inv[16], float near_plane, uint32_t n_clouds, const float* const* vertices,
+                            const uint64_t* counts, const uint32_t* const* colors, const float* cs,
+                            const uint32_t* db_ids, int one_bit);
+
 void orc_fill_background(uint32_t* bg, uint32_t w, uint32_t h, uint32_t clr_top, uint32_t clr_bottom);
 void orc_update_canvas(orc_pixel* out, uint32_t w, uint32_t h, int x0, int y0, int x1, int y1,
                        const orc_instance* inst, uint32_t n_inst, const orc_view* view,

@@ -54,6 +54,7 @@ class Stats(C.Structure):
 _P, _I, _U, _F = C.c_void_p, C.c_int, C.c_uint32, C.c_float
 _SIG = {
     "orc_make_default_camera": (None, [C.POINTER(Camera)]),
+    "orc_render_pointclouds": (None, [_P, _P, _U, _U, _P, _P, _F, _U, _P, _P, _P, _P, _P, _I]),
     "orc_make_projection_matrix": (None, [C.POINTER(Camera), _I, _I, _P]),
     "orc_invert_projection_matrix": (None, [_P, _P]),
     "orc_invert_orthonormal": (None, [_P, _P]),
@@ -372,3 +373,34 @@ def primary_rays(w: int, h: int, cs: np.ndarray, pinv: np.ndarray, near: float, 
             rays[k]["t_far"] = FLT_MAX
             k += 1
     return rays
+
+
+def render_pointclouds(pix: np.ndarray, im: np.ndarray, projection: np.ndarray, cs_inv: np.ndarray,
+                       near_plane: float, clouds, one_bit: bool = False) -> None:
+    """canvas::render_pointclouds_on_image (canvas.cpp:952-1030) in place on
+    the G-buffer `pix` and image `im`. clouds: [(vertices (n,3) f32, colors
+    (n,) u32 or None, cs (16,) f32, db_id)]."""
+    h, w = pix.shape
+    k = len(clouds)
+    keep = []
+    vps = (C.c_void_p * max(1, k))()
+    cps = (C.c_void_p * max(1, k))()
+    counts = np.zeros(max(1, k), np.uint64)
+    css = np.zeros((max(1, k), 16), np.float32)
+    dbs = np.zeros(max(1, k), np.uint32)
+    for i, (V, col, cs, db) in enumerate(clouds):
+        V = np.ascontiguousarray(V, np.float32)
+        keep.append(V)
+        vps[i] = V.ctypes.data
+        if col is not None:
+            col = np.ascontiguousarray(col, np.uint32)
+            keep.append(col)
+            cps[i] = col.ctypes.data
+        counts[i] = len(V)
+        css[i] = np.asarray(cs, np.float32).reshape(16)
+        dbs[i] = db
+    lib().orc_render_pointclouds(_p(pix), _p(im), w, h, _p(np.ascontiguousarray(projection, np.float32)),
+                                 _p(np.ascontiguousarray(cs_inv, np.float32)), float(near_plane), k,
+                                 C.cast(vps, C.c_void_p), _p(counts), C.cast(cps, C.c_void_p), _p(css), _p(dbs),
+                                 int(one_bit))
+

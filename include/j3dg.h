@@ -445,6 +445,13 @@ int j3dg_learned_loss_grad(j3dg_learned* l, const float* features, const int32_t
 int j3dg_learned_save(j3dg_learned* l, const char* path);
 int j3dg_learned_load(j3dg_learned* l, const char* path);
 
+/* Diagnostics (no reference counterpart): the network's two bf16
+   tensor-core GEMMs, C[M x N] fp32 = A[M x K] . Bt[N x K]^T on device
+   arrays (A, Bt bf16 row-major). impl 0: mma.sync (M, N % 128, K % 32);
+   impl 1: tcgen05 with a TMEM accumulator (M, N % 128, K % 64). Synchronous. */
+int j3dg_gemm_bf16(j3dg_ctx* ctx, const void* A, const void* Bt, float* C, uint32_t M, uint32_t N, uint32_t K,
+                   int impl);
+
 /* ---------------------------------------------------- host-side j3d math --
    Plain C++ (no GPU), the same fp32 operation order as the device code. */
 

@@ -155,6 +155,7 @@ SIGNATURES = {
     "j3dg_batch_set_scene": (_I, [_P, _U, C.POINTER(Scene)]),
     "j3dg_batch_launch": (_I, [_P]),
     "j3dg_batch_destroy": (_I, [_P]),
+    "j3dg_gemm_bf16": (_I, [_P, _P, _P, _P, _U, _U, _U, _I]),
     "j3dg_learned_create": (_I, [_P, _P, _P, C.POINTER(_P)]),
     "j3dg_learned_destroy": (_I, [_P]),
     "j3dg_learned_info": (_I, [_P, C.POINTER(_U), C.POINTER(C.c_uint64)]),

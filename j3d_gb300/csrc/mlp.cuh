@@ -35,6 +35,17 @@ struct GemmArgs {
 
 cudaError_t gemm_bf16(const GemmArgs& g, bool at, bool bt, int epi, cudaStream_t st);
 
+// C[M x N] fp32 = A[M x K] . Bt[N x K]^T on the tcgen05 tensor cores
+// (umma_gemm.cu). M % 128, N % 128, K % 64 == 0; lda, ldb multiples of 8;
+// 16-byte aligned pointers. A timed-out wait raises J3DG_DEV_VISIT_CAP.
+struct UmmaArgs {
+  const __nv_bfloat16* A;
+  const __nv_bfloat16* Bt;
+  float* C;
+  int M, N, K, lda, ldb, ldc;
+};
+cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st);
+
 // tanh-form GELU and its derivative (the network's activation)
 __device__ __forceinline__ float gelu_f(float x) {
   const float k = 0.7978845608028654f;  // sqrt(2 / pi)

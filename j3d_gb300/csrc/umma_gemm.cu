@@ -1,0 +1,178 @@
+// umma_gemm.cu -- bf16 GEMM on the tcgen05 tensor cores with the
+// accumulator in tensor memory:
+//   C[M x N] (fp32) = A[M x K] . Bt[N x K]^T     (A and Bt row-major, K-major)
+// One CTA of 4 warps per 128 x BN tile. K advances in chunks of 64 through a
+// two-stage shared-memory ring: all threads copy the next chunk into the
+// canonical no-swizzle layout while the tensor core works on the previous
+// one; thread 0 issues the four K = 16 MMAs of a chunk and commits them to
+// the stage's mbarrier, which frees the stage for the chunk after next.
+// The epilogue moves each warp's 32 accumulator rows out of TMEM with
+// tcgen05.ld. Every wait is bounded (clock budget); on timeout the kernel
+// raises J3DG_DEV_VISIT_CAP in the status word, skips the epilogue and still
+// frees its TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/j3dg.h"
+#include "internal.h"
+#include "mlp.cuh"
+#include "umma.cuh"
+
+namespace j3dg {
+
+namespace {
+
+const int kChunkK = 64;                     // K per stage
+const long long kWaitBudget = 4000000000ll; // ~2 s at 2 GHz
+const uint32_t kTmemCols = 512;             // whole TMEM: one CTA per SM
+
+template <int BN>
+struct GemmSmem {
+  static constexpr uint32_t a_bytes = 128 * kChunkK * 2;  // 16 KB
+  static constexpr uint32_t b_bytes = BN * kChunkK * 2;
+  static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
+  // + alignment slack; at least 120 KB so that one CTA runs per SM (each
+  // takes all 512 TMEM columns)
+  static constexpr uint32_t total = 2 * stage_bytes + 1024 > 122880u ? 2 * stage_bytes + 1024 : 122880u;
+};
+
+// Copies rows [r0, r0 + rows) x K-chunk [k0, k0 + 64) of a row-major bf16
+// matrix into the canonical layout (8 core matrices along K).
+__device__ __forceinline__ void copy_chunk(const __nv_bfloat16* __restrict__ src, int ld, int r0, int rows, int k0,
+                                           uint8_t* dst) {
+  const int pieces = rows * (kChunkK / 8);
+  for (int p = threadIdx.x; p < pieces; p += blockDim.x) {
+    const int row = p >> 3, kg = p & 7;
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)(r0 + row) * ld + k0 + kg * 8));
+    *reinterpret_cast<uint4*>(dst + umma::tile_offset(row, kg * 8, kChunkK / 8)) = v;
+  }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __restrict__ A,
+                                                      const __nv_bfloat16* __restrict__ Bt, float* __restrict__ C,
+                                                      int K, int lda, int ldb, int ldc, uint32_t* status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t taddr_s;
+  uint8_t* sm = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
+  using L = GemmSmem<BN>;
+
+  if (warp == 0) {
+    umma::tmem_alloc(umma::smem_u32(&taddr_s), kTmemCols);
+    umma::tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    umma::mbar_init(umma::smem_u32(&mbar[0]), 1);
+    umma::mbar_init(umma::smem_u32(&mbar[1]), 1);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t taddr = taddr_s;
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(128, BN);
+
+  const int nk = K / kChunkK;
+  bool ok = true;
+  for (int kc = 0; kc < nk; ++kc) {
+    const int s = kc & 1;
+    uint8_t* sA = sm + s * L::stage_bytes;
+    uint8_t* sB = sA + L::a_bytes;
+    if (kc >= 2) ok = umma::mbar_wait(umma::smem_u32(&mbar[s]), ((kc - 2) >> 1) & 1, kWaitBudget);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    copy_chunk(A, lda, m0, 128, kc * kChunkK, sA);
+    copy_chunk(Bt, ldb, n0, BN, kc * kChunkK, sB);
+    umma::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      umma::fence_after_sync();
+      const uint32_t a0 = umma::smem_u32(sA), b0 = umma::smem_u32(sB);
+#pragma unroll
+      for (int k = 0; k < kChunkK / 16; ++k)
+        umma::mma_bf16(taddr, umma::desc(a0 + k * 256, 128, (kChunkK / 8) * 128),
+                       umma::desc(b0 + k * 256, 128, (kChunkK / 8) * 128), idesc, (kc | k) != 0);
+      umma::commit(umma::smem_u32(&mbar[s]));
+    }
+  }
+  if (ok && nk > 0) ok = umma::mbar_wait(umma::smem_u32(&mbar[(nk - 1) & 1]), ((nk - 1) >> 1) & 1, kWaitBudget);
+  ok = __syncthreads_and(ok);
+  umma::fence_after_sync();
+  if (ok) {
+    const int row = m0 + warp * 32 + lane;
+    float* c = C + (size_t)row * ldc + n0;
+#pragma unroll 1
+    for (int j = 0; j < BN / 16; ++j) {
+      float v[16];
+      umma::ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * 16), v);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        reinterpret_cast<float4*>(c + j * 16)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+  } else if (threadIdx.x == 0) {
+    atomicOr(status, J3DG_DEV_VISIT_CAP);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(taddr, kTmemCols);
+  }
+}
+
+template <int BN>
+cudaError_t launch(const UmmaArgs& g, uint32_t* status, cudaStream_t st) {
+  const uint32_t smem = GemmSmem<BN>::total;
+  cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(g.N / BN, g.M / 128);
+  k_umma_gemm<BN><<<grid, 128, smem, st>>>(g.A, g.Bt, g.C, g.K, g.lda, g.ldb, g.ldc, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.M % 128 || g.K % kChunkK || g.lda % 8 || g.ldb % 8 || g.ldc % 4 ||
+      ((uintptr_t)g.A & 15) || ((uintptr_t)g.Bt & 15) || ((uintptr_t)g.C & 15))
+    return cudaErrorInvalidValue;
+  if (g.N % 256 == 0) return launch<256>(g, status, st);
+  if (g.N % 128 == 0) return launch<128>(g, status, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace j3dg
+
+namespace j3dg {
+int ctx_fail(j3dg_ctx* c, int code, const std::string& msg);
+}
+
+extern "C" int j3dg_gemm_bf16(j3dg_ctx* c, const void* A, const void* Bt, float* C, uint32_t M, uint32_t N, uint32_t K,
+                              int impl) {
+  if (!c || !A || !Bt || !C) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  cudaStream_t st = (cudaStream_t)c->stream;
+  cudaError_t e;
+  if (impl == 0) {
+    j3dg::GemmArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, nullptr, nullptr, (int)M, (int)N, (int)K,
+                     (int)K, (int)K, (int)N};
+    e = j3dg::gemm_bf16(g, false, true, j3dg::EPI_F32, st);
+  } else if (impl == 1) {
+    j3dg::UmmaArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, (int)M, (int)N, (int)K, (int)K, (int)K, (int)N};
+    e = j3dg::umma_gemm_bf16(g, c->d_status, st);
+  } else {
+    return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: impl must be 0 or 1");
+  }
+  if (e == cudaErrorInvalidValue) return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: unsupported shape");
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return j3dg::ctx_fail(c, J3DG_ERR_CUDA, std::string("gemm_bf16: ") + cudaGetErrorString(e));
+  return j3dg_ctx_synchronize(c);
+}
+

@@ -1,0 +1,55 @@
+"""The network's bf16 tensor-core GEMMs against an fp32 reference:
+impl 0 = mma.sync, impl 1 = tcgen05 with the accumulator in tensor memory.
+C = A . Bt^T with A [M x K], Bt [N x K] bf16; the reference multiplies the
+same bf16 values in float64, and the tolerance is 1e-5 of the sum of |a b|
+(fp32 accumulation in another order)."""
+import numpy as np
+import pytest
+
+
+def _case(M, N, K, seed):
+    import torch
+    g = torch.Generator().manual_seed(seed)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    Bt = torch.randn(N, K, generator=g).to(torch.bfloat16)
+    ref = A.double() @ Bt.double().T
+    mag = A.double().abs() @ Bt.double().abs().T
+    return A, Bt, ref.numpy(), mag.numpy()
+
+
+def _run(ctx, A, Bt, impl):
+    import torch
+    from j3d_gb300 import _ffi
+    from j3d_gb300.scene import _check
+    M, K = A.shape
+    N = Bt.shape[0]
+    dA, dB = A.cuda().contiguous(), Bt.cuda().contiguous()
+    C = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+    _check(ctx.h, _ffi.lib().j3dg_gemm_bf16(ctx.h, dA.data_ptr(), dB.data_ptr(), C.data_ptr(), M, N, K, impl))
+    return C.cpu().double().numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(128, 128, 64), (128, 256, 64), (256, 384, 320), (512, 1024, 256),
+                                   (2048, 4096, 128)])
+@pytest.mark.parametrize("impl", [1, 0])
+def test_gemm_matches_fp32_reference(gpu_ctx, shape, impl):
+    M, N, K = shape
+    A, Bt, ref, mag = _case(M, N, K, seed=M + N + K)
+    C = _run(gpu_ctx, A, Bt, impl)
+    err = np.abs(C - ref)
+    assert np.isfinite(C).all()
+    assert (err <= 1e-5 * mag + 1e-30).all(), float((err / (mag + 1e-30)).max())
+
+
+@pytest.mark.gpu
+def test_gemm_rejects_unsupported_shapes(gpu_ctx):
+    import torch
+    from j3d_gb300 import J3dgError, _ffi
+    from j3d_gb300.scene import _check
+    A = torch.zeros(128, 96, dtype=torch.bfloat16, device="cuda")
+    B = torch.zeros(128, 96, dtype=torch.bfloat16, device="cuda")
+    C = torch.zeros(128, 128, dtype=torch.float32, device="cuda")
+    with pytest.raises(J3dgError):  # K % 64 != 0 on the tcgen05 path
+        _check(gpu_ctx.h, _ffi.lib().j3dg_gemm_bf16(gpu_ctx.h, A.data_ptr(), B.data_ptr(), C.data_ptr(),
+                                                    128, 128, 96, 1))

@@ -585,8 +585,14 @@ def run_learned(args):
     same = bool(all(np.array_equal(hp[f], hl[f]) for f in ("found", "distance", "u", "v", "object_id")))
     # the network alone: top-2 prediction time on the same rays
     d_top2 = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
-    ms_predict = timed(lambda: L.j3dg_learned_predict(net.h, d_rays.data_ptr(), n, d_top2.data_ptr()))
+    d_top2_layered = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+    ms_predict = timed(lambda: L.j3dg_learned_predict_impl(net.h, d_rays.data_ptr(), n, d_top2.data_ptr(), 1))
+    ms_layered = timed(lambda: L.j3dg_learned_predict_impl(net.h, d_rays.data_ptr(), n, d_top2_layered.data_ptr(), 0))
+    agree = float((d_top2.view(-1, 2)[:, 0] == d_top2_layered.view(-1, 2)[:, 0]).float().mean())
     flops = 2.0 * (256 * 128 + 3 * 128 * 128 + 128 * 4096) * n
+    pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak_tf, peak_kind = (float(pk["bf16_tflops"]), "measured") if "bf16_tflops" in pk else (1900.0, "fallback")
+    tf_fused = flops / (ms_predict / 1e3) / 1e12
     line = {"metric": "learned vs plain closest-hit Mrays/s (config 3)", "value": round(n / ms_learned / 1e3, 3),
             "unit": "Mrays/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 network / f32 traversal",
             "data": "synthetic (seeded displaced torus; training rays from cameras at radius 2-5)",
@@ -596,12 +602,18 @@ def run_learned(args):
                        "train_top1_accuracy": round(acc, 4),
                        "plain_ms": round(ms_plain, 3), "learned_ms": round(ms_learned, 3),
                        "network_predict_ms": round(ms_predict, 3),
-                       "network_tflops": round(flops / (ms_predict / 1e3) / 1e12, 2),
+                       "network_tflops": round(tf_fused, 2),
+                       "network_layered_mma_sync_ms": round(ms_layered, 3),
+                       "network_layered_tflops": round(flops / (ms_layered / 1e3) / 1e12, 2),
+                       "fused_vs_layered_top1_agreement": round(agree, 5),
                        "plain_mrays_s": round(n / ms_plain / 1e3, 3),
                        "learned_over_plain": round(ms_plain / ms_learned, 4),
                        "hits_identical": same, "hit_fraction": round(float(hp["found"].mean()), 4),
                        "plain_node_visits_per_ray": round(pv / n, 3), "learned_node_visits_per_ray": round(lv / n, 3),
-                       "plain_tri_tests_per_ray": round(pt / n, 3), "learned_tri_tests_per_ray": round(lt / n, 3)}}
+                       "plain_tri_tests_per_ray": round(pt / n, 3), "learned_tri_tests_per_ray": round(lt / n, 3)},
+            "roofline": {"bound": "tensor", "achieved": round(tf_fused, 1), "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": round(tf_fused / peak_tf, 4), "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_learned_fused (features, 5 tcgen05 layers, running top-2; 1.196 MFLOP per ray)"}}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -430,8 +430,14 @@ int j3dg_learned_info(const j3dg_learned* l, uint32_t* n_clusters, uint64_t* n_p
    top-1 accuracy over its hit rays, and the wall time. */
 int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, float* final_loss, float* accuracy,
                        float* seconds);
-/* The two most likely clusters of each ray (n x 2, host or device). */
+/* The two most likely clusters of each ray (n x 2, host or device), by the
+   fused inference kernel (tcgen05, activations and logits kept on chip). */
 int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2);
+/* The same with a choice of implementation: 1 the fused tcgen05 kernel, 0 the
+   layer-by-layer mma.sync GEMMs of training plus a top-2 pass over the
+   logits. Both round activations to bf16 at the same points; the fp32
+   accumulation order differs, so near-ties may rank differently. */
+int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2, int impl);
 /* Closest hits through the learned tmax (host or device arrays). */
 int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits);
 /* Parameters (fp32 master copy, layout W1 b1 ... W5 b5, W row-major [in][out]). */

@@ -161,6 +161,7 @@ SIGNATURES = {
     "j3dg_learned_info": (_I, [_P, C.POINTER(_U), C.POINTER(C.c_uint64)]),
     "j3dg_learned_train": (_I, [_P, C.c_uint64, _F, _F, C.POINTER(_F), C.POINTER(_F), C.POINTER(_F)]),
     "j3dg_learned_predict": (_I, [_P, _P, _U, _P]),
+    "j3dg_learned_predict_impl": (_I, [_P, _P, _U, _P, _I]),
     "j3dg_learned_find_closest": (_I, [_P, _P, _U, _P]),
     "j3dg_learned_get_params": (_I, [_P, _P]),
     "j3dg_learned_set_params": (_I, [_P, _P]),

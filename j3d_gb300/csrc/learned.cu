@@ -30,6 +30,7 @@
 #include "device_common.cuh"
 #include "internal.h"
 #include "mlp.cuh"
+#include "umma.cuh"
 
 namespace j3dg {
 int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits);
@@ -68,27 +69,41 @@ struct Layout {
 
 // Fourier features of (origin, direction): x_i = ((o - c) / s, d / |d|),
 // sin / cos of pi 2^(k/4) x_i for k = 0..15; features [i][k][sin, cos].
+__device__ __forceinline__ void ray_inputs(const j3dg_ray* ray, float cx, float cy, float cz, float inv_s,
+                                           float (&in6)[6]) {
+  const float* f = reinterpret_cast<const float*>(ray);
+  const float dl = rsqrtf(f[4] * f[4] + f[5] * f[5] + f[6] * f[6] + 1e-30f);
+  in6[0] = (f[0] - cx) * inv_s;
+  in6[1] = (f[1] - cy) * inv_s;
+  in6[2] = (f[2] - cz) * inv_s;
+  in6[3] = f[4] * dl;
+  in6[4] = f[5] * dl;
+  in6[5] = f[6] * dl;
+}
+
+// feature pair m = i * 16 + k (columns 2m: sin, 2m + 1: cos)
+__device__ __forceinline__ __nv_bfloat162 feature_pair(const float (&in6)[6], int m) {
+  const int i = m / kBands, k = m % kBands;
+  const float fr = 3.14159265f * exp2f(0.25f * (float)k);
+  float s, c;
+  sincosf(fr * in6[i], &s, &c);
+  return __halves2bfloat162(__float2bfloat16(s), __float2bfloat16(c));
+}
+
 __global__ void k_features(const j3dg_ray* __restrict__ rays, uint32_t n, uint32_t n_pad, float cx, float cy,
                            float cz, float inv_s, __nv_bfloat16* __restrict__ X) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_pad) return;
-  __nv_bfloat16* x = X + (size_t)r * kIn;
+  __nv_bfloat162* x = reinterpret_cast<__nv_bfloat162*>(X + (size_t)r * kIn);
+  const __nv_bfloat162 zero = __halves2bfloat162(__float2bfloat16(0.f), __float2bfloat16(0.f));
   if (r >= n) {
-    for (int j = 0; j < kIn; ++j) x[j] = __float2bfloat16(0.f);
+    for (int j = 0; j < kIn / 2; ++j) x[j] = zero;
     return;
   }
-  const float* f = reinterpret_cast<const float*>(rays + r);
-  const float dl = rsqrtf(f[4] * f[4] + f[5] * f[5] + f[6] * f[6] + 1e-30f);
-  const float in6[6] = {(f[0] - cx) * inv_s, (f[1] - cy) * inv_s, (f[2] - cz) * inv_s, f[4] * dl, f[5] * dl, f[6] * dl};
-  for (int i = 0; i < 6; ++i)
-    for (int k = 0; k < kBands; ++k) {
-      const float fr = 3.14159265f * exp2f(0.25f * (float)k);
-      float s, c;
-      sincosf(fr * in6[i], &s, &c);
-      x[(i * kBands + k) * 2] = __float2bfloat16(s);
-      x[(i * kBands + k) * 2 + 1] = __float2bfloat16(c);
-    }
-  for (int j = 6 * kBands * 2; j < kIn; ++j) x[j] = __float2bfloat16(0.f);
+  float in6[6];
+  ray_inputs(rays + r, cx, cy, cz, inv_s, in6);
+  for (int m = 0; m < 6 * kBands; ++m) x[m] = feature_pair(in6, m);
+  for (int j = 6 * kBands; j < kIn / 2; ++j) x[j] = zero;
 }
 
 // Softmax cross-entropy over the first K logits of each row; rows with
@@ -216,6 +231,276 @@ __global__ void k_top2(const float* __restrict__ logits, uint32_t rows, uint32_t
     out[2 * row] = i1;
     out[2 * row + 1] = i2;
   }
+}
+
+// ------------------------------------------- fused inference on tcgen05 ----
+//
+// One CTA of 8 warps per 128 rays runs the whole network on chip: the
+// features go to shared memory, every layer is a tcgen05 MMA chain (thread
+// 0 issues K / 16 MMAs of M = 128) into a TMEM accumulator, the hidden
+// epilogues (bias, bf16, GELU, bf16 -- as the layer-by-layer path rounds)
+// read TMEM with tcgen05.ld and write the next layer's operand back to
+// shared memory, and the 4096 logits are consumed in 16 chunks of 256
+// columns, alternating between two TMEM column ranges and two weight
+// buffers, by a per-row running top-2 (thread = row = TMEM lane). No
+// activation or logit leaves the SM. Weights are packed once per call into
+// the canonical K-major layout; thread 0 streams each layer / chunk into a
+// shared-memory buffer with cp.async.bulk as soon as the MMA that read the
+// buffer's previous contents has completed, so the copies run under the
+// epilogues.
+
+static const uint32_t kFusedXBytes = 128 * kIn * 2;   // 64 KB: features, then hidden activations
+static const uint32_t kFusedWBytes = 256 * kHid * 2;  // 64 KB: W1 (128 x 256) or a 256-row W5 chunk
+static const uint32_t kFusedBiasBytes = (4 * kHid + kOut) * 4;
+static const uint32_t kFusedSmem = kFusedXBytes + 2 * kFusedWBytes + kFusedBiasBytes + 1024;
+static const long long kFusedWait = 500000000ll;      // ~0.25 s at 2 GHz per wait
+
+// W (fp32 row-major [K][N]) -> bf16 K-major operand Bt[N][K], canonical layout
+__global__ void k_pack_weights(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)K * N) return;
+  const int n = (int)(i / K), k = (int)(i % K);
+  out[umma::tile_offset(n, k, K / 8) / 2] = __float2bfloat16(W[(size_t)k * N + n]);
+}
+
+struct FusedArgs {
+  const j3dg_ray* rays;
+  uint32_t n;
+  float cx, cy, cz, inv_s;
+  const __nv_bfloat16* w[5];  // packed layers
+  const float* b[5];
+  uint32_t n_clusters;
+  uint32_t* top2;
+  uint32_t* status;
+};
+
+__device__ __forceinline__ uint32_t bits2(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+
+// thread 0: D[tmem] = X[128 x K] . W^T, W given as N rows of K
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* X, const uint8_t* W, int K, int N) {
+  const uint32_t idesc = N == 256 ? umma::idesc_bf16_f32(128, 256) : umma::idesc_bf16_f32(128, 128);
+  const uint32_t sbo = (uint32_t)(K / 8) * 128u, x0 = umma::smem_u32(X), w0 = umma::smem_u32(W);
+  for (int s = 0; s < K / 16; ++s)
+    umma::mma_bf16(d_tmem, umma::desc(x0 + s * 256, 128, sbo), umma::desc(w0 + s * 256, 128, sbo), idesc, s > 0);
+}
+
+// bias, bf16, GELU, bf16 (EPI_BIAS_GELU) -> next operand rows in X (K = 128);
+// this thread's row and 64-column half h
+__device__ __forceinline__ void hidden_epilogue(uint32_t t_lane, const float* bias, uint8_t* X, int row, int h) {
+  {
+    float v[64];
+    umma::ld64(t_lane + (uint32_t)(h * 64), v);
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      uint32_t pk[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = g * 8 + 2 * q, c0 = h * 64 + i;
+        const __nv_bfloat16 z0 = __float2bfloat16(v[i] + bias[c0]);
+        const __nv_bfloat16 z1 = __float2bfloat16(v[i + 1] + bias[c0 + 1]);
+        pk[q] = bits2(__halves2bfloat162(__float2bfloat16(gelu_f(__bfloat162float(z0))),
+                                         __float2bfloat16(gelu_f(__bfloat162float(z1)))));
+      }
+      *reinterpret_cast<uint4*>(X + umma::tile_offset(row, h * 64 + g * 8, kHid / 8)) =
+          make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+
+// 8 warps: warp w reads TMEM lane quarter w % 4 (rows 32 (w % 4) + lane)
+// and works on column half w / 4 of every epilogue.
+__global__ void __launch_bounds__(256, 1) k_learned_fused(const FusedArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t mma_bar[2];
+  __shared__ __align__(8) uint64_t load_bar[2];
+  __shared__ uint32_t taddr_s;
+  uint8_t* X = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* Wb[2] = {X + kFusedXBytes, X + kFusedXBytes + kFusedWBytes};
+  float* bias = reinterpret_cast<float*>(X + kFusedXBytes + 2 * kFusedWBytes);  // b1..b4, then b5 (-inf past n_clusters)
+  const int tid = threadIdx.x, warp = tid >> 5, row = tid & 127, half = tid >> 7;
+  const uint32_t r = blockIdx.x * 128u + (uint32_t)row;
+  bool ok = true;
+  float v1 = -FLT_MAX, v2 = -FLT_MAX;
+  uint32_t i1 = 0xffffffffu, i2 = 0xffffffffu, taddr = 0, t_lane = 0, mb[2] = {0, 0}, lb[2] = {0, 0};
+
+  // a CTA that timed out raised the status word: the rest of the grid stops
+  if (*reinterpret_cast<volatile uint32_t*>(a.status) & J3DG_DEV_VISIT_CAP) return;
+  if (warp == 0) {
+    umma::tmem_alloc(umma::smem_u32(&taddr_s), 512);
+    umma::tmem_relinquish();
+  }
+  mb[0] = umma::smem_u32(&mma_bar[0]);
+  mb[1] = umma::smem_u32(&mma_bar[1]);
+  lb[0] = umma::smem_u32(&load_bar[0]);
+  lb[1] = umma::smem_u32(&load_bar[1]);
+  if (tid == 0) {
+    for (int k = 0; k < 2; ++k) {
+      umma::mbar_init(mb[k], 1);
+      umma::mbar_init(lb[k], 1);
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  taddr = taddr_s;
+  t_lane = taddr + ((uint32_t)((warp & 3) * 32) << 16);
+  if (tid == 0) {  // W1 -> buffer 0, W2 -> buffer 1
+    umma::mbar_arrive_expect_tx(lb[0], kIn * kHid * 2);
+    umma::bulk_copy(umma::smem_u32(Wb[0]), a.w[0], kIn * kHid * 2, lb[0]);
+    umma::mbar_arrive_expect_tx(lb[1], kHid * kHid * 2);
+    umma::bulk_copy(umma::smem_u32(Wb[1]), a.w[1], kHid * kHid * 2, lb[1]);
+  }
+
+// all threads: wait for MMA barrier `bar` phase `parity` (bounded)
+#define J3DG_FUSED_WAIT(bar, parity)                                                   \
+  do {                                                                                 \
+    ok = __syncthreads_and(umma::mbar_wait(mb[bar], (parity), kFusedWait)) != 0;        \
+    if (!ok) goto done;                                                                \
+    umma::fence_after_sync();                                                          \
+  } while (0)
+// thread 0: refill weight buffer `buf` with `bytes` from `src` (its previous
+// MMA has completed: the caller waited for it)
+#define J3DG_FUSED_LOAD(buf, src, bytes)                                               \
+  do {                                                                                 \
+    if (tid == 0) {                                                                    \
+      umma::mbar_arrive_expect_tx(lb[buf], (bytes));                                   \
+      umma::bulk_copy(umma::smem_u32(Wb[buf]), (src), (bytes), lb[buf]);               \
+    }                                                                                  \
+  } while (0)
+// all threads publish their shared-memory writes and TMEM reads; thread 0
+// waits for the weights of buffer `buf` (load phase `lpar`) and issues
+#define J3DG_FUSED_ISSUE(dcol, buf, lpar, K, N)                                        \
+  do {                                                                                 \
+    umma::fence_async_smem();                                                          \
+    umma::fence_before_sync();                                                         \
+    __syncthreads();                                                                   \
+    if (tid == 0) {                                                                    \
+      const bool got = umma::mbar_wait(lb[buf], (lpar), kFusedWait);                   \
+      umma::fence_after_sync();                                                        \
+      if (got) issue_layer(taddr + (dcol), X, Wb[buf], (K), (N));                      \
+      else atomicOr(a.status, J3DG_DEV_VISIT_CAP);                                     \
+      umma::commit(mb[buf]);                                                           \
+    }                                                                                  \
+  } while (0)
+
+  for (int i = tid; i < 4 * kHid; i += 256) bias[i] = a.b[i / kHid][i % kHid];
+  for (int i = tid; i < kOut; i += 256) bias[4 * kHid + i] = (uint32_t)i < a.n_clusters ? a.b[4][i] : -INFINITY;
+  {  // features of ray r (zeros past n), K = 256 operand rows; this half's 16 core matrices
+    float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool live = r < a.n;
+    if (live) ray_inputs(a.rays + r, a.cx, a.cy, a.cz, a.inv_s, in6);
+    const __nv_bfloat162 zero = __halves2bfloat162(__float2bfloat16(0.f), __float2bfloat16(0.f));
+#pragma unroll 1
+    for (int kg = half * (kIn / 16); kg < (half + 1) * (kIn / 16); ++kg) {
+      uint32_t p[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int m = kg * 4 + q;
+        p[q] = bits2((live && m < 6 * kBands) ? feature_pair(in6, m) : zero);
+      }
+      *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kg * 8, kIn / 8)) = make_uint4(p[0], p[1], p[2], p[3]);
+    }
+  }
+  J3DG_FUSED_ISSUE(0, 0, 0, kIn, kHid);  // layer 1: W buffer 0, load phase 0, mma phase 0
+  J3DG_FUSED_WAIT(0, 0);
+  J3DG_FUSED_LOAD(0, a.w[2], kHid * kHid * 2);  // W3
+  hidden_epilogue(t_lane, bias, X, row, half);
+  J3DG_FUSED_ISSUE(0, 1, 0, kHid, kHid);  // layer 2
+  J3DG_FUSED_WAIT(1, 0);
+  J3DG_FUSED_LOAD(1, a.w[3], kHid * kHid * 2);  // W4
+  hidden_epilogue(t_lane, bias + kHid, X, row, half);
+  J3DG_FUSED_ISSUE(0, 0, 1, kHid, kHid);  // layer 3
+  J3DG_FUSED_WAIT(0, 1);
+  J3DG_FUSED_LOAD(0, a.w[4], kFusedWBytes);  // W5 chunk 0
+  hidden_epilogue(t_lane, bias + 2 * kHid, X, row, half);
+  J3DG_FUSED_ISSUE(0, 1, 1, kHid, kHid);  // layer 4
+  J3DG_FUSED_WAIT(1, 1);
+  J3DG_FUSED_LOAD(1, a.w[4] + 256 * kHid, kFusedWBytes);  // W5 chunk 1
+  hidden_epilogue(t_lane, bias + 3 * kHid, X, row, half);
+  J3DG_FUSED_ISSUE(0, 0, 0, kHid, 256);    // logits chunk 0 (load phase 2, mma phase 2)
+  J3DG_FUSED_ISSUE(256, 1, 0, kHid, 256);  // chunk 1
+#pragma unroll 1
+  for (int c = 0; c < kOut / 256; ++c) {
+    const int s = c & 1;
+    J3DG_FUSED_WAIT(s, (c >> 1) & 1);  // chunk c is commit 2 + c / 2 of its barriers
+    if (c + 2 < kOut / 256) J3DG_FUSED_LOAD(s, a.w[4] + (size_t)(c + 2) * 256 * kHid, kFusedWBytes);
+    const float* b5 = bias + 4 * kHid + c * 256;
+#pragma unroll 1
+    for (int h = 2 * half; h < 2 * half + 2; ++h) {
+      float v[64];
+      umma::ld64(t_lane + (uint32_t)(s * 256 + h * 64), v);
+      float m = -FLT_MAX;
+#pragma unroll
+      for (int q = 0; q < 64; ++q) {
+        v[q] += b5[h * 64 + q];
+        m = fmaxf(m, v[q]);
+      }
+      if (m > v2) {  // rare once the running top-2 is established
+#pragma unroll
+        for (int q = 0; q < 64; ++q) {
+          const float x = v[q];
+          if (x > v2) {
+            const uint32_t col = (uint32_t)(c * 256 + h * 64 + q);
+            if (x > v1) {
+              v2 = v1;
+              i2 = i1;
+              v1 = x;
+              i1 = col;
+            } else {
+              v2 = x;
+              i2 = col;
+            }
+          }
+        }
+      }
+    }
+    // chunk c + 2 is load 2 + (c + 2) / 2 of buffer s
+    if (c + 2 < kOut / 256) J3DG_FUSED_ISSUE(s * 256, s, ((c >> 1) + 1) & 1, kHid, 256);
+  }
+  {  // merge the two halves' top-2 by (value desc, index asc) -- the order a
+     // sequential scan with strict comparisons keeps
+    float* pv = reinterpret_cast<float*>(Wb[0]);  // the weight buffers are idle now
+    uint32_t* pi = reinterpret_cast<uint32_t*>(Wb[0] + 1024);
+    if (half == 1) {
+      pv[2 * row] = v1;
+      pv[2 * row + 1] = v2;
+      pi[2 * row] = i1;
+      pi[2 * row + 1] = i2;
+    }
+    __syncthreads();
+    if (half == 0 && r < a.n) {
+      const float c[4] = {v1, v2, pv[2 * row], pv[2 * row + 1]};
+      const uint32_t ci[4] = {i1, i2, pi[2 * row], pi[2 * row + 1]};
+      float b1 = -FLT_MAX, b2 = -FLT_MAX;
+      uint32_t k1 = 0xffffffffu, k2 = 0xffffffffu;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (ci[q] == 0xffffffffu) continue;
+        if (c[q] > b1 || (c[q] == b1 && ci[q] < k1)) {
+          b2 = b1;
+          k2 = k1;
+          b1 = c[q];
+          k1 = ci[q];
+        } else if (c[q] > b2 || (c[q] == b2 && ci[q] < k2)) {
+          b2 = c[q];
+          k2 = ci[q];
+        }
+      }
+      a.top2[2 * (size_t)r] = k1;
+      a.top2[2 * (size_t)r + 1] = k2;
+    }
+  }
+done:
+  if (!ok && tid == 0) atomicOr(a.status, J3DG_DEV_VISIT_CAP);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(taddr, 512);
+  }
+#undef J3DG_FUSED_WAIT
+#undef J3DG_FUSED_LOAD
+#undef J3DG_FUSED_ISSUE
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -387,6 +672,7 @@ struct j3dg_learned {
   j3dg_ray* rays = nullptr;
   j3dg_hit* hits = nullptr;
   uint32_t* top2 = nullptr;
+  __nv_bfloat16* d_wpack = nullptr;  // weights in the tcgen05 operand layout (fused inference)
   float center[3] = {0, 0, 0}, inv_scale = 1.f, t_near = 0.f;
 };
 
@@ -632,7 +918,7 @@ int j3dg_learned_destroy(j3dg_learned* l) {
   cudaSetDevice(l->ctx->device);
   cudaStreamSynchronize(LS(l));
   void* ptrs[] = {l->d_roots, l->d_cluster_of_tri, l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb, l->X, l->dZ5, l->dA, l->dB,
-                  l->logits, l->labels, l->d_loss, l->d_correct, l->rays, l->hits, l->top2};
+                  l->logits, l->labels, l->d_loss, l->d_correct, l->rays, l->hits, l->top2, l->d_wpack};
   for (void* p : ptrs) cudaFree(p);
   for (int k = 0; k < 4; ++k) {
     cudaFree(l->H[k]);
@@ -741,8 +1027,43 @@ int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, flo
   return J3DG_OK;
 }
 
-// top-2 clusters per ray (device or host arrays)
-static int predict_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2) {
+// top-2 clusters per ray on device arrays: the fused tcgen05 kernel
+static int predict_fused(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2) {
+  const j3dg::Layout& L = l->L;
+  size_t total = 0;
+  for (int k = 0; k < 5; ++k) total += (size_t)L.in[k] * L.out[k];
+  if (!l->d_wpack) LCK(cudaMalloc(&l->d_wpack, sizeof(__nv_bfloat16) * total), "learned pack");
+  j3dg::FusedArgs a;
+  size_t off = 0;
+  for (int k = 0; k < 5; ++k) {
+    const size_t cnt = (size_t)L.in[k] * L.out[k];
+    j3dg::k_pack_weights<<<(unsigned)((cnt + 255) / 256), 256, 0, LS(l)>>>(l->d_p + L.w[k], L.in[k], L.out[k],
+                                                                            l->d_wpack + off);
+    LCK(cudaGetLastError(), "learned pack");
+    a.w[k] = l->d_wpack + off;
+    a.b[k] = l->d_p + L.b[k];
+    off += cnt;
+  }
+  a.rays = d_rays;
+  a.n = n;
+  a.cx = l->center[0];
+  a.cy = l->center[1];
+  a.cz = l->center[2];
+  a.inv_s = l->inv_scale;
+  a.n_clusters = l->n_clusters;
+  a.top2 = d_top2;
+  a.status = l->ctx->d_status;
+  LCK(cudaFuncSetAttribute(j3dg::k_learned_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)j3dg::kFusedSmem),
+      "learned fused");
+  j3dg::k_learned_fused<<<(n + 127) / 128, 256, j3dg::kFusedSmem, LS(l)>>>(a);
+  LCK(cudaGetLastError(), "learned fused");
+  return J3DG_OK;
+}
+
+// top-2 clusters per ray on device arrays: impl 1 fused tcgen05 kernel,
+// impl 0 layer-by-layer mma.sync GEMMs + a top-2 pass over the logits
+static int predict_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2, int impl = 1) {
+  if (impl == 1) return predict_fused(l, d_rays, n, d_top2);
   const uint32_t B = l->opts.batch;
   if (int rc = alloc_workspace(l, B)) return rc;
   for (uint32_t off = 0; off < n; off += B) {
@@ -757,7 +1078,11 @@ static int predict_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, u
 }
 
 int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2) {
-  if (!l || (n && (!rays || !top2))) return J3DG_ERR_INVALID_ARGUMENT;
+  return j3dg_learned_predict_impl(l, rays, n, top2, 1);
+}
+
+int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2, int impl) {
+  if (!l || (n && (!rays || !top2)) || (impl != 0 && impl != 1)) return J3DG_ERR_INVALID_ARGUMENT;
   if (n == 0) return J3DG_OK;
   cudaSetDevice(l->ctx->device);
   j3dg_ray* dr = nullptr;
@@ -765,11 +1090,12 @@ int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint
   LCK(cudaMallocAsync((void**)&dr, sizeof(j3dg_ray) * n, LS(l)), "predict");
   LCK(cudaMallocAsync((void**)&dt, sizeof(uint32_t) * 2 * n, LS(l)), "predict");
   LCK(cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * n, cudaMemcpyDefault, LS(l)), "predict");
-  int rc = predict_device(l, dr, n, dt);
+  int rc = predict_device(l, dr, n, dt, impl);
   if (rc == J3DG_OK) LCK(cudaMemcpyAsync(top2, dt, sizeof(uint32_t) * 2 * n, cudaMemcpyDefault, LS(l)), "predict");
   cudaFreeAsync(dr, LS(l));
   cudaFreeAsync(dt, LS(l));
   LCK(cudaStreamSynchronize(LS(l)), "predict");
+  if (rc == J3DG_OK) rc = j3dg_ctx_synchronize(l->ctx);
   return rc;
 }
 

@@ -26,7 +26,7 @@ namespace j3dg {
 namespace {
 
 const int kChunkK = 64;                     // K per stage
-const long long kWaitBudget = 4000000000ll; // ~2 s at 2 GHz
+const long long kWaitBudget = 500000000ll;  // ~0.25 s at 2 GHz
 const uint32_t kTmemCols = 512;             // whole TMEM: one CTA per SM
 
 template <int BN>
@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
   const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
   using L = GemmSmem<BN>;
 
+  // a CTA that timed out raised the status word: the rest of the grid stops
+  if (*reinterpret_cast<volatile uint32_t*>(status) & J3DG_DEV_VISIT_CAP) return;
   if (warp == 0) {
     umma::tmem_alloc(umma::smem_u32(&taddr_s), kTmemCols);
     umma::tmem_relinquish();

@@ -60,9 +60,11 @@ class Learned:
         _check(self.ctx.h, lib().j3dg_learned_train(self.h, n_rays, r0, r1, C.byref(loss), C.byref(acc), C.byref(secs)))
         return float(loss.value), float(acc.value), float(secs.value)
 
-    def predict(self, rays) -> np.ndarray:
+    def predict(self, rays, impl: int = 1) -> np.ndarray:
+        """Top-2 clusters per ray: impl 1 the fused tcgen05 kernel, 0 the
+        layer-by-layer mma.sync GEMMs."""
         out = np.zeros((len(rays), 2), np.uint32)
-        _check(self.ctx.h, lib().j3dg_learned_predict(self.h, vptr(rays), len(rays), vptr(out)))
+        _check(self.ctx.h, lib().j3dg_learned_predict_impl(self.h, vptr(rays), len(rays), vptr(out), impl))
         return out
 
     def find_closest(self, rays, hits=None):

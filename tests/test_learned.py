@@ -108,11 +108,18 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
         assert np.array_equal(learned[f], plain[f]), f
     assert plain["found"].mean() > 0.2
     top2 = net.predict(rays)
+    # the fused tcgen05 inference agrees with the layer-by-layer GEMMs (they
+    # differ only in fp32 accumulation order, so near-ties may swap)
+    top2_layered = net.predict(rays, impl=0)
+    assert (top2[:, 0] == top2_layered[:, 0]).mean() > 0.99
+    assert (np.sort(top2, 1) == np.sort(top2_layered, 1)).all(1).mean() > 0.97
     # a 4096-cluster network trains too (loss falls from log K)
     deep = Learned(gpu_ctx, mesh, cluster_depth=6, batch=8192, seed=6)
     la, _, _ = deep.train(8192 * 4)
     lb, _, _ = deep.train(8192 * 100)
     assert deep.n_clusters > 1000 and lb < la
+    d1, d0 = deep.predict(rays), deep.predict(rays, impl=0)
+    assert (d1 < deep.n_clusters).all() and (d1[:, 0] == d0[:, 0]).mean() > 0.98
     assert (top2[:, 0] < net.n_clusters).all()
     # checkpoint round trip
     path = tmp_path / "net.bin"
@@ -120,3 +127,25 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
     net2 = Learned(gpu_ctx, mesh, cluster_depth=3, batch=8192, seed=99)
     net2.load(path)
     assert np.array_equal(net2.predict(rays), top2)
+
+
+@pytest.mark.gpu
+def test_fused_inference_matches_layered(gpu_ctx):
+    """The fused tcgen05 kernel (features, five layers, running top-2, all on
+    chip) against the layer-by-layer mma.sync GEMMs + top-2 pass, on random
+    weights and rays (a ray count that leaves a partial 128-ray tile)."""
+    from j3d_gb300 import Mesh, workloads as W
+    from j3d_gb300.learned import Learned
+    V, T = W.icosphere(5, W.SEED_BASE + 76)
+    net = Learned(gpu_ctx, Mesh(gpu_ctx, V, T), cluster_depth=6, seed=8)
+    rng = np.random.default_rng(13)
+    net.set_params(rng.normal(0, 0.15, net.n_params).astype(np.float32))
+    n = 5000
+    rays = np.zeros(n, [("orig", "<f4", 4), ("dir", "<f4", 4), ("t_near", "<f4"), ("t_far", "<f4")])
+    rays["orig"][:, :3] = rng.normal(0, 3, (n, 3))
+    rays["orig"][:, 3] = 1
+    rays["dir"][:, :3] = rng.normal(0, 1, (n, 3))
+    rays["t_far"] = FLT_MAX
+    t1, t0 = net.predict(rays, impl=1), net.predict(rays, impl=0)
+    assert (t1 < net.n_clusters).all() and (t1[:, 0] != t1[:, 1]).all()
+    assert (t1[:, 0] == t0[:, 0]).mean() > 0.99, (t1[:, 0] == t0[:, 0]).mean()

@@ -276,19 +276,25 @@ struct Tracer {
       }
       ++visits;
       const float4* N = nodes + 8 * (size_t)cur;
-      const float4 lox = __ldg(N + 0), hix = __ldg(N + 1), loy = __ldg(N + 2), hiy = __ldg(N + 3);
-      const float4 loz = __ldg(N + 4), hiz = __ldg(N + 5);
+      // near / far planes by the ray's octant: the same values slab() selects,
+      // picked by the load offsets instead of per-child selects
+      const uint32_t ox = r.neg & 1u, oy = (r.neg >> 1) & 1u, oz = (r.neg >> 2) & 1u;
+      const float4 nx4 = __ldg(N + ox), fx4 = __ldg(N + (ox ^ 1u));
+      const float4 ny4 = __ldg(N + 2 + oy), fy4 = __ldg(N + 2 + (oy ^ 1u));
+      const float4 nz4 = __ldg(N + 4 + oz), fz4 = __ldg(N + 4 + (oz ^ 1u));
       const float4 chf = __ldg(N + 6);
       float tc[4];
       uint32_t rc[4] = {__float_as_uint(chf.x), __float_as_uint(chf.y), __float_as_uint(chf.z),
                         __float_as_uint(chf.w)};
-      const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-      const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-      const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+      const float pnx[4] = {nx4.x, nx4.y, nx4.z, nx4.w}, pfx[4] = {fx4.x, fx4.y, fx4.z, fx4.w};
+      const float pny[4] = {ny4.x, ny4.y, ny4.z, ny4.w}, pfy[4] = {fy4.x, fy4.y, fy4.z, fy4.w};
+      const float pnz[4] = {nz4.x, nz4.y, nz4.z, nz4.w}, pfz[4] = {fz4.x, fz4.y, fz4.z, fz4.w};
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        float tn, tf;
-        slab(r, lx[c], ly[c], lz[c], hx[c], hy[c], hz[c], tn, tf);
+        const float tn = fmaxf(fmaxf(__fmaf_rn(pnx[c], r.ix, r.nnx), __fmaf_rn(pny[c], r.iy, r.nny)),
+                               __fmaf_rn(pnz[c], r.iz, r.nnz));
+        const float tf = fminf(fminf(__fmaf_rn(pfx[c], r.ix, r.nfx), __fmaf_rn(pfy[c], r.iy, r.nfy)),
+                               __fmaf_rn(pfz[c], r.iz, r.nfz));
         float a = fmaxf(tn, r.t_near), e = fminf(tf, b.t);
         bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
         tc[c] = hit ? a : __int_as_float(0x7f800000);

@@ -580,6 +580,7 @@ def run_learned(args):
     ctx.synchronize()
     lv, lt = ctx.read_counters(reset=True)
     ctx.set_counting(False)
+    _, phase = net.find_closest_stats(host[:n])
     hp = d_plain.cpu().numpy().view(_ffi.HIT_DTYPE)
     hl = d_learn.cpu().numpy().view(_ffi.HIT_DTYPE)
     same = bool(all(np.array_equal(hp[f], hl[f]) for f in ("found", "distance", "u", "v", "object_id")))
@@ -610,7 +611,10 @@ def run_learned(args):
                        "learned_over_plain": round(ms_plain / ms_learned, 4),
                        "hits_identical": same, "hit_fraction": round(float(hp["found"].mean()), 4),
                        "plain_node_visits_per_ray": round(pv / n, 3), "learned_node_visits_per_ray": round(lv / n, 3),
-                       "plain_tri_tests_per_ray": round(pt / n, 3), "learned_tri_tests_per_ray": round(lt / n, 3)},
+                       "plain_tri_tests_per_ray": round(pt / n, 3), "learned_tri_tests_per_ray": round(lt / n, 3),
+                       "learned_cluster_phase_visits_per_ray": round(phase["cluster_visits"] / n, 3),
+                       "learned_exact_phase_visits_per_ray": round(phase["exact_visits"] / n, 3),
+                       "exact_phase_visit_saving_vs_plain": round(1 - phase["exact_visits"] / max(1, pv), 4)},
             "roofline": {"bound": "tensor", "achieved": round(tf_fused, 1), "peak": peak_tf, "unit": "TFLOP/s",
                          "frac": round(tf_fused / peak_tf, 4), "traffic": None, "peak_kind": peak_kind,
                          "kernel": "k_learned_fused (features, 5 tcgen05 layers, running top-2; 1.196 MFLOP per ray)"}}

@@ -440,6 +440,14 @@ int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint
 int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2, int impl);
 /* Closest hits through the learned tmax (host or device arrays). */
 int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits);
+/* The same, reporting what each phase cost: stats = {node visits and
+   triangle tests of the two predicted clusters, node visits and triangle
+   tests of the exact traversal seeded with their best hit}. The exact
+   phase never visits more nodes than the plain traversal of the same rays
+   (its best-so-far is never larger at any step); the difference is what
+   the network's prediction saves it. */
+int j3dg_learned_find_closest_stats(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
+                                    uint64_t stats[4]);
 /* Parameters (fp32 master copy, layout W1 b1 ... W5 b5, W row-major [in][out]). */
 int j3dg_learned_get_params(j3dg_learned* l, float* out);
 int j3dg_learned_set_params(j3dg_learned* l, const float* in);

@@ -163,6 +163,7 @@ SIGNATURES = {
     "j3dg_learned_predict": (_I, [_P, _P, _U, _P]),
     "j3dg_learned_predict_impl": (_I, [_P, _P, _U, _P, _I]),
     "j3dg_learned_find_closest": (_I, [_P, _P, _U, _P]),
+    "j3dg_learned_find_closest_stats": (_I, [_P, _P, _U, _P, C.POINTER(C.c_uint64)]),
     "j3dg_learned_get_params": (_I, [_P, _P]),
     "j3dg_learned_set_params": (_I, [_P, _P]),
     "j3dg_learned_loss_grad": (_I, [_P, _P, _P, _U, C.POINTER(_F), _P]),

@@ -602,14 +602,15 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
                                                       uint32_t n, const uint32_t* __restrict__ top2,
                                                       const uint32_t* __restrict__ roots, uint32_t n_roots,
                                                       j3dg_hit* __restrict__ hits, uint32_t* status,
-                                                      unsigned long long* counters) {
+                                                      unsigned long long* counters,
+                                                      unsigned long long* phase_counters) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  uint32_t visits = 0, tests = 0, exact_visits = 0, exact_tests = 0;
+  if (i < n) {
   const float* f = reinterpret_cast<const float*>(rays + i);
   Tracer T;
   uint32_t stack_ref[J3DG_STACK];
   float stack_t[J3DG_STACK];
-  uint32_t visits = 0, tests = 0;
   T.begin(inst, 1, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], false);
   const uint32_t c0 = top2[2 * i], c1 = top2[2 * i + 1];
   for (int phase = 0; phase < 3; ++phase) {
@@ -625,7 +626,9 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
     T.sp = 0;
     T.inst = 0;
     T.budget = T.n_nodes + 1;
-    while (!T.step(inst, 1, status, visits, tests, stack_ref, stack_t)) {
+    uint32_t& pv = phase < 2 ? visits : exact_visits;
+    uint32_t& pt = phase < 2 ? tests : exact_tests;
+    while (!T.step(inst, 1, status, pv, pt, stack_ref, stack_t)) {
     }
   }
   j3dg_hit h;
@@ -636,9 +639,16 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
   h.object_id = T.b.found ? T.b.tri : 0xffffffffu;
   h.two_level_index = T.b.found ? 0u : 0xffffffffu;
   hits[i] = h;
-  if (counters) {
-    atomicAdd(counters + 0, (unsigned long long)visits);
-    atomicAdd(counters + 1, (unsigned long long)tests);
+  }
+  if (counters && i < n) {
+    atomicAdd(counters + 0, (unsigned long long)(visits + exact_visits));
+    atomicAdd(counters + 1, (unsigned long long)(tests + exact_tests));
+  }
+  if (phase_counters) {  // [cluster visits, cluster tests, exact visits, exact tests]
+    const uint32_t v[4] = {__reduce_add_sync(0xffffffffu, visits), __reduce_add_sync(0xffffffffu, tests),
+                           __reduce_add_sync(0xffffffffu, exact_visits), __reduce_add_sync(0xffffffffu, exact_tests)};
+    if ((threadIdx.x & 31u) == 0)
+      for (int k = 0; k < 4; ++k) atomicAdd(phase_counters + k, (unsigned long long)v[k]);
   }
 }
 
@@ -1100,7 +1110,14 @@ int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n,
 }
 
 int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits) {
+  return j3dg_learned_find_closest_stats(l, rays, n, hits, nullptr);
+}
+
+int j3dg_learned_find_closest_stats(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
+                                    uint64_t stats[4]) {
   if (!l || (n && (!rays || !hits))) return J3DG_ERR_INVALID_ARGUMENT;
+  if (stats)
+    for (int k = 0; k < 4; ++k) stats[k] = 0;
   if (n == 0) return J3DG_OK;
   j3dg_ctx* c = l->ctx;
   cudaSetDevice(c->device);
@@ -1117,14 +1134,26 @@ int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n,
   }
   if (!hits_dev) LCK(cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * n, LS(l)), "learned find");
   LCK(cudaMallocAsync((void**)&dt, sizeof(uint32_t) * 2 * n, LS(l)), "learned find");
+  unsigned long long* d_phase = nullptr;
+  if (stats) {
+    LCK(cudaMallocAsync((void**)&d_phase, sizeof(unsigned long long) * 4, LS(l)), "learned find");
+    LCK(cudaMemsetAsync(d_phase, 0, sizeof(unsigned long long) * 4, LS(l)), "learned find");
+  }
   int rc = predict_device(l, dr, n, dt);
   const DevInst* dinst = nullptr;
   if (rc == J3DG_OK) rc = j3dg::mesh_devinst(c, l->mesh, &dinst);
   if (rc == J3DG_OK) {
     unsigned long long* counters = j3dg::ctx_counters(c);
     j3dg::k_rays_learned<<<(n + 127) / 128, 128, 0, LS(l)>>>(dinst, dr, n, dt, l->d_roots, l->n_clusters, dh,
-                                                            c->d_status, counters);
+                                                            c->d_status, counters, d_phase);
     LCK(cudaGetLastError(), "learned find");
+  }
+  if (stats) {
+    unsigned long long h[4] = {0, 0, 0, 0};
+    LCK(cudaMemcpyAsync(h, d_phase, sizeof(h), cudaMemcpyDeviceToHost, LS(l)), "learned find");
+    LCK(cudaStreamSynchronize(LS(l)), "learned find");
+    for (int k = 0; k < 4; ++k) stats[k] = h[k];
+    cudaFreeAsync(d_phase, LS(l));
   }
   if (!hits_dev) {
     LCK(cudaMemcpyAsync(hits, dh, sizeof(j3dg_hit) * n, cudaMemcpyDeviceToHost, LS(l)), "learned find");

@@ -73,6 +73,14 @@ class Learned:
         _check(self.ctx.h, lib().j3dg_learned_find_closest(self.h, vptr(rays), len(rays), vptr(hits)))
         return hits
 
+    def find_closest_stats(self, rays, hits=None):
+        """(hits, {cluster_visits, cluster_tests, exact_visits, exact_tests})."""
+        if hits is None:
+            hits = np.zeros(len(rays), HIT_DTYPE)
+        st = (C.c_uint64 * 4)()
+        _check(self.ctx.h, lib().j3dg_learned_find_closest_stats(self.h, vptr(rays), len(rays), vptr(hits), st))
+        return hits, dict(zip(("cluster_visits", "cluster_tests", "exact_visits", "exact_tests"), list(st)))
+
     def get_params(self) -> np.ndarray:
         out = np.zeros(self.n_params, np.float32)
         _check(self.ctx.h, lib().j3dg_learned_get_params(self.h, vptr(out)))

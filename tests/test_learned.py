@@ -102,11 +102,23 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
     rays["dir"][:, :3] = -P[:, 2, :3] + jit[:, :1] * P[:, 0, :3] + jit[:, 1:] * P[:, 1, :3]
     rays["t_near"] = 0.02
     rays["t_far"] = np.where(rng.uniform(size=n) < 0.1, 3.0, FLT_MAX).astype(np.float32)
+    gpu_ctx.set_counting(True)
+    gpu_ctx.read_counters(reset=True)
     plain = find_closest(gpu_ctx, [SceneObject(mesh, None, 1)], rays)
-    learned = net.find_closest(rays)
+    plain_visits, plain_tests = gpu_ctx.read_counters(reset=True)
+    gpu_ctx.set_counting(False)
+    learned, st = net.find_closest_stats(rays)
     for f in ("found", "distance", "u", "v", "object_id"):
         assert np.array_equal(learned[f], plain[f]), f
     assert plain["found"].mean() > 0.2
+    # what the network gains: the exact traversal seeded with the predicted
+    # clusters' best hit never visits more nodes than the plain traversal
+    # (and here visits fewer); the cluster phase is the price paid for it
+    assert st["exact_visits"] <= plain_visits and st["exact_tests"] <= plain_tests
+    assert st["exact_visits"] < plain_visits
+    print(f"\nlearned tmax on {n} rays: exact phase {st['exact_visits'] / n:.3f} node visits/ray vs plain "
+          f"{plain_visits / n:.3f} ({1 - st['exact_visits'] / plain_visits:.1%} fewer); cluster phase "
+          f"{st['cluster_visits'] / n:.3f}/ray")
     top2 = net.predict(rays)
     # the fused tcgen05 inference agrees with the layer-by-layer GEMMs (they
     # differ only in fp32 accumulation order, so near-ties may swap)

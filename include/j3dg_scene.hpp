@@ -69,6 +69,14 @@ struct scene_object {
   float min_bb[3], max_bb[3];
 };
 
+// scene_pointcloud (scene.h:27-38): the points live on the device.
+struct scene_pointcloud {
+  uint32_t db_id = 0;
+  j3dg_pointcloud* points = nullptr;
+  float cs[16];
+  float min_bb[3], max_bb[3];
+};
+
 // scene (scene.h:40-51)
 struct scene {
   float coordinate_system[16], coordinate_system_inv[16];
@@ -76,12 +84,14 @@ struct scene {
   float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
   float diagonal = 0.f;
   std::list<scene_object> objects;
+  std::list<scene_pointcloud> pointclouds;
   scene() {
     identity(coordinate_system);
     identity(coordinate_system_inv);
   }
   ~scene() {
     for (auto& o : objects) j3dg_mesh_destroy(o.bvh);
+    for (auto& o : pointclouds) j3dg_pointcloud_destroy(o.points);
   }
   scene(const scene&) = delete;
   scene& operator=(const scene&) = delete;
@@ -107,14 +117,94 @@ inline void add_object(context& ctx, uint32_t id, scene& s, const float* vertice
   s.objects.push_back(o);
 }
 
+// add_object's point-cloud branch (scene.cpp:27-36): n points (n x 3
+// floats), optional packed RGBA8 colours.
+inline void add_pointcloud(context& ctx, uint32_t id, scene& s, const float* vertices, uint64_t n,
+                           const uint32_t* colors = nullptr, const float* cs = nullptr) {
+  scene_pointcloud o;
+  o.db_id = id;
+  if (cs)
+    std::memcpy(o.cs, cs, sizeof(o.cs));
+  else
+    identity(o.cs);
+  check(j3dg_pointcloud_create(ctx.get(), vertices, n, colors, &o.points), ctx.get(), "add_pointcloud");
+  check(j3dg_pointcloud_get_bounds(o.points, o.min_bb, o.max_bb), ctx.get(), "add_pointcloud");
+  s.pointclouds.push_back(o);
+}
+
+// read_from_file (mesh.cpp:76-176 / pc.cpp:32-110) + add_object: the file is
+// decoded on the device; a file with triangles becomes a mesh object with its
+// BVH, one without becomes a point cloud. Returns true for a mesh.
+inline bool add_object_from_file(context& ctx, uint32_t id, scene& s, const char* path, const float* cs = nullptr,
+                                 uint32_t leaf_size = 2) {
+  j3dg_geometry* g = nullptr;
+  check(j3dg_geometry_read_file(ctx.get(), path, J3DG_FORMAT_AUTO, &g), ctx.get(), "read_from_file");
+  j3dg_geometry_info info;
+  j3dg_geometry_get_info(g, &info);
+  const bool is_mesh = info.n_triangles > 0;
+  int rc = J3DG_OK;
+  if (is_mesh) {
+    scene_object o;
+    o.db_id = id;
+    if (cs)
+      std::memcpy(o.cs, cs, sizeof(o.cs));
+    else
+      identity(o.cs);
+    j3dg_build_opts opts{leaf_size, 0};
+    rc = j3dg_mesh_build_geometry(ctx.get(), g, &opts, &o.bvh);
+    if (rc == J3DG_OK) {
+      j3dg_mesh_info mi;
+      j3dg_mesh_get_info(o.bvh, &mi);
+      std::memcpy(o.min_bb, mi.min_bb, sizeof(o.min_bb));
+      std::memcpy(o.max_bb, mi.max_bb, sizeof(o.max_bb));
+      s.objects.push_back(o);
+    }
+  } else {
+    scene_pointcloud o;
+    o.db_id = id;
+    if (cs)
+      std::memcpy(o.cs, cs, sizeof(o.cs));
+    else
+      identity(o.cs);
+    rc = j3dg_pointcloud_from_geometry(ctx.get(), g, &o.points);
+    if (rc == J3DG_OK) {
+      j3dg_pointcloud_get_bounds(o.points, o.min_bb, o.max_bb);
+      s.pointclouds.push_back(o);
+    }
+  }
+  j3dg_geometry_destroy(g);
+  check(rc, ctx.get(), "read_from_file");
+  return is_mesh;
+}
+
 // remove_object (scene.cpp:40-48)
 inline void remove_object(uint32_t id, scene& s) {
   for (auto it = s.objects.begin(); it != s.objects.end(); ++it)
     if (it->db_id == id) {
       j3dg_mesh_destroy(it->bvh);
       s.objects.erase(it);
-      return;
+      break;
     }
+  for (auto it = s.pointclouds.begin(); it != s.pointclouds.end(); ++it)
+    if (it->db_id == id) {
+      j3dg_pointcloud_destroy(it->points);
+      s.pointclouds.erase(it);
+      break;
+    }
+}
+
+inline std::vector<j3dg_pointcloud_instance> pointcloud_instances(const scene& s) {
+  std::vector<j3dg_pointcloud_instance> v;
+  v.reserve(s.pointclouds.size());
+  for (const auto& o : s.pointclouds) {
+    j3dg_pointcloud_instance i;
+    i.pointcloud = o.points;
+    std::memcpy(i.cs, o.cs, sizeof(i.cs));
+    i.db_id = o.db_id;
+    i.reserved = 0;
+    v.push_back(i);
+  }
+  return v;
 }
 
 inline std::vector<j3dg_instance> instances(const scene& s) {
@@ -134,8 +224,10 @@ inline std::vector<j3dg_instance> instances(const scene& s) {
 // prepare_scene (scene.cpp:50-89)
 inline void prepare_scene(scene& s) {
   auto inst = instances(s);
-  check(j3dg_prepare_scene(inst.data(), (uint32_t)inst.size(), s.min_bb, s.max_bb, &s.diagonal), nullptr,
-        "prepare_scene");
+  auto pcs = pointcloud_instances(s);
+  check(j3dg_prepare_scene_pointclouds(inst.data(), (uint32_t)inst.size(), pcs.data(), (uint32_t)pcs.size(),
+                                       s.min_bb, s.max_bb, &s.diagonal),
+        nullptr, "prepare_scene");
 }
 
 // unzoom (scene.cpp:91-110)
@@ -241,6 +333,15 @@ class canvas {
     j3dg_scene c;
     if (s) c = to_c(*s, keep);
     check(j3dg_canvas_render_frame(cv_, s ? &c : nullptr, m.get()), ctx_.get(), "render_frame");
+  }
+  // canvas::render_pointclouds_on_image (canvas.cpp:952-1030), after a frame
+  void render_pointclouds_on_image(const scene* s) {
+    if (!s || s->pointclouds.empty()) return;
+    std::vector<j3dg_instance> keep;
+    j3dg_scene c = to_c(*s, keep);
+    auto pcs = pointcloud_instances(*s);
+    check(j3dg_canvas_render_pointclouds(cv_, &c, pcs.data(), (uint32_t)pcs.size()), ctx_.get(),
+          "render_pointclouds_on_image");
   }
   std::vector<pixel> get_pixels() const {
     std::vector<pixel> out((size_t)w_ * h_);

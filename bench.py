@@ -37,9 +37,11 @@ RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # mean over the 32 launches of one step, from an ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
 # (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
-# --warmup 3 --no-cpu`): reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB.
-FRAME_DRAM_BYTES = 463_159_392 + 70_692_880
-FRAME_L2_BYTES = 1_837_113_990
+# --warmup 3 --no-cpu [--build lbvh]`), per BVH builder:
+#   ploc: reads 444.7 MB, writes 69.9 MB, L2 1763.2 MB
+#   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB
+FRAME_TRAFFIC = {"ploc": (444_731_920 + 69_880_184, 1_763_229_795),
+                 "lbvh": (463_159_392 + 70_692_880, 1_837_113_990)}
 
 
 def peaks():
@@ -207,11 +209,11 @@ def run_own(args):
     wl = Wk.config1(N_CAMERAS, W_, H_)
     ctx = Context(local)
     t0 = time.perf_counter()
-    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build)
     build_wall = time.perf_counter() - t0
     info = mesh.info()
     # a second build with warm allocator gives the steady build time
-    mesh2 = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    mesh2 = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build)
     build_ms = mesh2.info().build_ms
     mesh2.close()
     sc = Scene()
@@ -336,14 +338,15 @@ def run_own(args):
                        rays_per_step=rays_per_step, shadow_ray_fraction=round(sum(shadow_rays) / (prim * N_CAMERAS), 4),
                        bvh_build_ms=round(build_ms, 3), bvh_first_build_wall_s=round(build_wall, 3),
                        bvh_nodes=info.n_nodes, bvh_depth=info.max_depth, leaf_size=args.leaf,
+                       bvh_builder=args.build,
                        mesh_device_bytes=int(info.device_bytes),
                        bvh_build_mtris_per_s=round(28_090_000 / (build_ms / 1e3) / 1e6, 1),
                        gpu_node_visits_per_ray=round(gvis / rays_per_step, 3),
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
-                     "traffic": FRAME_DRAM_BYTES if args.leaf == 2 else None,
-                     "traffic_l2": FRAME_L2_BYTES if args.leaf == 2 else None,
+                     "traffic": FRAME_TRAFFIC[args.build][0] if args.leaf == 2 else None,
+                     "traffic_l2": FRAME_TRAFFIC[args.build][1] if args.leaf == 2 else None,
                      "traffic_note": "bytes per k_frame launch (ncu, mean of the 32 cameras); the algorithmic "
                                      "bytes per launch are bytes_per_ray x rays_per_step / 32",
                      "kernel": "k_frame (primary + shadow + shading, one launch per frame)", "peak_kind": peak_kind,
@@ -787,6 +790,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--leaf", type=int, default=2)
+    ap.add_argument("--build", default="ploc", choices=["ploc", "lbvh"], help="BVH builder of the headline mesh")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
     ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")

@@ -432,6 +432,11 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   m->nv = nv;
   m->nt = nt;
   m->leaf_size = leaf;
+  m->build_flags = opts ? opts->flags : 0u;
+  if (m->build_flags & ~(uint32_t)J3DG_BUILD_LBVH) {
+    delete m;
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: unknown build flags");
+  }
   CtxExtra& X = all(c)->ex;
   float* dV = nullptr;
   bool ownV = false;

@@ -9,14 +9,17 @@
 //      code over the vertex bbox
 //   3. LSD radix sort of (Morton, triangle id), 8-bit digits, stable
 //   4. leaf-ordered triangle array: 3 float4 per triangle (v0.w = id bits)
-//   5. binary LBVH, bottom-up in one pass (Apetrei 2014, "Fast and Simple
-//      Agglomerative LBVH Construction"), with a strict total order on the
-//      split keys (xor of neighbouring codes, then i ^ (i+1), then i)
+//   5. binary tree: by default PLOC clustering over the sorted triangles
+//      (section 5b); with J3DG_BUILD_LBVH the LBVH, bottom-up in one pass
+//      (Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction"),
+//      with a strict total order on the split keys (xor of neighbouring
+//      codes, then i ^ (i+1), then i)
 //   6. collapse to 4-wide nodes level by level: open the largest-area child
 //      until four children; subtrees of <= leaf_size triangles become leaves.
 // Child boxes are exact unions of triangle boxes, which the traversal's
 // topology-independence argument requires.
 #include <cuda_runtime.h>
+#include <float.h>
 #include <stdint.h>
 
 #include <algorithm>
@@ -430,6 +433,231 @@ __global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __res
   atomicMax(max_depth, it.depth);
 }
 
+// -------------------------------------------------------- 5b. PLOC ----
+//
+// Parallel locally-ordered clustering (Meister and Bittner 2018, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction"):
+// the Morton-sorted leaves start as clusters; every cluster picks the
+// cluster within kPlocRadius list positions whose union box has the smallest
+// surface area (equal areas: the smaller position; with the pair order this
+// is a total order, so the globally best pair is always mutual and every
+// round merges); mutual pairs become a new binary node at the lower
+// position; the list is compacted (two exclusive scans) and the rounds
+// repeat until one cluster is left. Subtrees are no longer Morton ranges, so
+// the collapse below carries each subtree's first position in the new leaf
+// order and writes the triangles there.
+
+#ifndef J3DG_PLOC_RADIUS
+#define J3DG_PLOC_RADIUS 8  // 2..64 measured on the torus frames: 8 visits the fewest nodes
+#endif
+static const int kPlocRadius = J3DG_PLOC_RADIUS;
+static const int kPlocBlock = 256;
+
+__global__ void k_ploc_init(const float4* __restrict__ tris, uint32_t n, uint32_t* __restrict__ C,
+                            float4* __restrict__ lo, float4* __restrict__ hi) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  C[i] = 0x80000000u | i;
+  leaf_box(tris, i, lo[i], hi[i]);
+}
+
+__device__ __forceinline__ float merged_area(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+  const float dx = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
+  const float dy = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
+  const float dz = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+  const float a = dx * dy + dy * dz + dz * dx;
+  return a == a ? a : FLT_MAX;  // boxes with NaN planes still get an order
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict__ lo, const float4* __restrict__ hi,
+                                                       uint32_t m, uint32_t* __restrict__ nn) {
+  __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+  const int base = (int)(blockIdx.x * kPlocBlock) - kPlocRadius;
+  for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += blockDim.x) {
+    const int j = base + k;
+    if (j >= 0 && j < (int)m) {
+      slo[k] = lo[j];
+      shi[k] = hi[j];
+    }
+  }
+  __syncthreads();
+  const int i = (int)(blockIdx.x * kPlocBlock + threadIdx.x);
+  if (i >= (int)m) return;
+  const int si = threadIdx.x + kPlocRadius;
+  const float4 alo = slo[si], ahi = shi[si];
+  float best = INFINITY;
+  int bj = i == 0 ? 1 : i - 1;
+  for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
+    const int j = i + o;
+    if (o == 0 || j < 0 || j >= (int)m) continue;
+    const float a = merged_area(alo, ahi, slo[si + o], shi[si + o]);
+    if (a < best) {  // increasing j: the first of equal areas is the smaller position
+      best = a;
+      bj = j;
+    }
+  }
+  nn[i] = (uint32_t)bj;
+}
+
+__global__ void k_ploc_flags(const uint32_t* __restrict__ nn, uint32_t m, uint32_t* __restrict__ create,
+                             uint32_t* __restrict__ survive) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t j = nn[i];
+  const bool mutual = j < m && nn[j] == i;
+  create[i] = (mutual && i < j) ? 1u : 0u;
+  survive[i] = (!mutual || i < j) ? 1u : 0u;
+}
+
+// totals of the two exclusive scans: [creates, survivors]
+__global__ void k_ploc_totals(const uint32_t* create, const uint32_t* cscan, const uint32_t* survive,
+                              const uint32_t* sscan, uint32_t m, uint32_t* out) {
+  out[0] = cscan[m - 1] + create[m - 1];
+  out[1] = sscan[m - 1] + survive[m - 1];
+}
+
+__global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
+                             const float4* __restrict__ hi, const uint32_t* __restrict__ nn,
+                             const uint32_t* __restrict__ cscan, const uint32_t* __restrict__ sscan, uint32_t m,
+                             uint32_t node_base, uint32_t* __restrict__ C2, float4* __restrict__ lo2,
+                             float4* __restrict__ hi2, uint2* __restrict__ child, BinNode* __restrict__ box,
+                             uint32_t* __restrict__ count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t j = nn[i];
+  const bool mutual = j < m && nn[j] == i;
+  if (mutual && i > j) return;  // merged into the node made at j
+  const uint32_t pos = sscan[i];
+  if (!mutual) {
+    C2[pos] = C[i];
+    lo2[pos] = lo[i];
+    hi2[pos] = hi[i];
+    return;
+  }
+  const uint32_t p = node_base + cscan[i];
+  const uint32_t a = C[i], b = C[j];
+  const float4 l = make_float4(fminf(lo[i].x, lo[j].x), fminf(lo[i].y, lo[j].y), fminf(lo[i].z, lo[j].z), 0.f);
+  const float4 h = make_float4(fmaxf(hi[i].x, hi[j].x), fmaxf(hi[i].y, hi[j].y), fmaxf(hi[i].z, hi[j].z), 0.f);
+  child[p] = make_uint2(a, b);
+  box[p].lo = l;
+  box[p].hi = h;
+  count[p] = ((a & 0x80000000u) ? 1u : count[a]) + ((b & 0x80000000u) ? 1u : count[b]);
+  C2[pos] = p;
+  lo2[pos] = l;
+  hi2[pos] = h;
+}
+
+struct PlaceItem {
+  uint32_t bin;    // binary node index
+  uint32_t wide;   // wide node index to fill
+  uint32_t depth;
+  uint32_t start;  // first leaf-order position of the subtree
+};
+
+// The collapse of k_collapse over a tree whose subtrees are not ranges of the
+// sorted leaves: each slot carries its subtree's first position; leaves are
+// written to tris_out at those positions in depth-first order.
+__global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                 const uint32_t* __restrict__ count, const float4* __restrict__ tris,
+                                 const PlaceItem* __restrict__ qin, uint32_t n_in, PlaceItem* __restrict__ qout,
+                                 uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
+                                 uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
+                                 uint32_t nt, uint32_t* status) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_in) return;
+  const PlaceItem it = qin[t];
+  uint32_t ref[4], cnt[4], start[4];
+  float4 lo[4], hi[4];
+  auto load = [&](uint32_t r, int s, uint32_t first) {
+    ref[s] = r;
+    start[s] = first;
+    if (r & 0x80000000u) {
+      leaf_box(tris, r & 0x7fffffffu, lo[s], hi[s]);
+      cnt[s] = 1;
+    } else {
+      lo[s] = box[r].lo;
+      hi[s] = box[r].hi;
+      cnt[s] = count[r];
+    }
+  };
+  const uint2 c = child[it.bin];
+  load(c.x, 0, it.start);
+  load(c.y, 1, it.start + cnt[0]);
+  int m = 2;
+  while (m < 4) {
+    int best = -1;
+    float ba = -1.f;
+    for (int s = 0; s < m; ++s)
+      if (cnt[s] > leaf_size) {
+        const float a = half_area(lo[s], hi[s]);
+        if (a > ba) {
+          ba = a;
+          best = s;
+        }
+      }
+    if (best < 0) break;
+    const uint2 cc = child[ref[best]];
+    const uint32_t s0 = start[best];
+    load(cc.x, best, s0);
+    load(cc.y, m, s0 + cnt[best]);
+    ++m;
+  }
+  float4* W = wide + 8 * (size_t)it.wide;
+  float v[6][4];
+  uint32_t out_ref[4];
+  for (int s = 0; s < 4; ++s) {
+    if (s < m) {
+      v[0][s] = lo[s].x;
+      v[1][s] = hi[s].x;
+      v[2][s] = lo[s].y;
+      v[3][s] = hi[s].y;
+      v[4][s] = lo[s].z;
+      v[5][s] = hi[s].z;
+      if (cnt[s] <= leaf_size) {
+        out_ref[s] = J3DG_LEAF_BIT | (start[s] << 3) | (cnt[s] - 1u);
+        uint32_t stk[J3DG_MAX_LEAF];
+        int sp = 0;
+        uint32_t k = 0;
+        stk[sp++] = ref[s];
+        while (sp > 0) {
+          const uint32_t r = stk[--sp];
+          if (r & 0x80000000u) {
+            const uint32_t src = r & 0x7fffffffu, dst = start[s] + k++;
+            if (src < nt && dst < nt) {
+              tris_out[3 * (size_t)dst] = tris[3 * (size_t)src];
+              tris_out[3 * (size_t)dst + 1] = tris[3 * (size_t)src + 1];
+              tris_out[3 * (size_t)dst + 2] = tris[3 * (size_t)src + 2];
+            } else {
+              atomicOr(status, J3DG_DEV_BAD_INDEX);
+            }
+          } else if (sp + 2 <= (int)J3DG_MAX_LEAF) {
+            const uint2 cc = child[r];
+            stk[sp++] = cc.y;
+            stk[sp++] = cc.x;
+          } else {
+            atomicOr(status, J3DG_DEV_STACK_OVERFLOW);
+            break;
+          }
+        }
+      } else {
+        const uint32_t w = atomicAdd(n_wide, 1u);
+        const uint32_t q = atomicAdd(n_out, 1u);
+        qout[q] = PlaceItem{ref[s], w, it.depth + 1, start[s]};
+        out_ref[s] = w;
+      }
+    } else {
+      v[0][s] = v[2][s] = v[4][s] = 3.4e38f;
+      v[1][s] = v[3][s] = v[5][s] = -3.4e38f;
+      out_ref[s] = J3DG_EMPTY_REF;
+    }
+  }
+  for (int k = 0; k < 6; ++k) W[k] = make_float4(v[k][0], v[k][1], v[k][2], v[k][3]);
+  W[6] = make_float4(__uint_as_float(out_ref[0]), __uint_as_float(out_ref[1]), __uint_as_float(out_ref[2]),
+                     __uint_as_float(out_ref[3]));
+  W[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+  atomicMax(max_depth, it.depth);
+}
+
 // ------------------------------------------------------------- driver ----
 
 #define J3DG_CK(x)                                             \
@@ -457,6 +685,11 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   uint32_t *other = nullptr, *counters = nullptr;
   CollapseItem *qa = nullptr, *qb = nullptr;
   float4* wide = nullptr;
+  // PLOC
+  uint32_t *C0 = nullptr, *C1 = nullptr, *nn = nullptr, *create = nullptr, *survive = nullptr, *cscan = nullptr,
+           *sscan = nullptr, *pl_sums = nullptr, *count = nullptr, *tot = nullptr;
+  float4 *lo0 = nullptr, *hi0 = nullptr, *lo1 = nullptr, *hi1 = nullptr, *tris_out = nullptr;
+  PlaceItem *pa = nullptr, *pb = nullptr;
   const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
   const uint32_t hist_n = 256 * n_tiles;
   const uint32_t scan_blocks = (hist_n + 1023) / 1024;
@@ -511,6 +744,100 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->max_depth = 0;
     J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8));
     J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * 8, st));
+    goto cleanup;
+  }
+
+  if (!(m->build_flags & J3DG_BUILD_LBVH)) {
+    uint32_t mcount = nt, node_base = 0, iters = 0, htot[2] = {0, 0}, root = 0;
+    const uint32_t sblocks_max = (nt + 1023) / 1024;
+    J3DG_CK(cudaMallocAsync((void**)&child, sizeof(uint2) * (nt - 1), st));
+    J3DG_CK(cudaMallocAsync((void**)&box, sizeof(BinNode) * (nt - 1), st));
+    J3DG_CK(cudaMallocAsync((void**)&count, sizeof(uint32_t) * (nt - 1), st));
+    J3DG_CK(cudaMallocAsync((void**)&C0, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&C1, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&nn, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&create, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&survive, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&cscan, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&sscan, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&pl_sums, sizeof(uint32_t) * (sblocks_max + 1), st));
+    J3DG_CK(cudaMallocAsync((void**)&tot, sizeof(uint32_t) * 2, st));
+    J3DG_CK(cudaMallocAsync((void**)&lo0, sizeof(float4) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&hi0, sizeof(float4) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&lo1, sizeof(float4) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&hi1, sizeof(float4) * nt, st));
+    k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, C0, lo0, hi0);
+    J3DG_CK(cudaGetLastError());
+    while (mcount > 1) {
+      const uint32_t blocks = (mcount + kPlocBlock - 1) / kPlocBlock, sb = (mcount + 1023) / 1024;
+      k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, mcount, nn);
+      k_ploc_flags<<<blocks, kPlocBlock, 0, st>>>(nn, mcount, create, survive);
+      k_scan_chunks<<<sb, 1024, 0, st>>>(create, cscan, mcount, pl_sums);
+      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
+      k_scan_add<<<sb, 1024, 0, st>>>(cscan, mcount, pl_sums);
+      k_scan_chunks<<<sb, 1024, 0, st>>>(survive, sscan, mcount, pl_sums);
+      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
+      k_scan_add<<<sb, 1024, 0, st>>>(sscan, mcount, pl_sums);
+      k_ploc_totals<<<1, 1, 0, st>>>(create, cscan, survive, sscan, mcount, tot);
+      J3DG_CK(cudaGetLastError());
+      J3DG_CK(cudaMemcpyAsync(htot, tot, sizeof(htot), cudaMemcpyDeviceToHost, st));
+      J3DG_CK(cudaStreamSynchronize(st));
+      if (htot[0] == 0 || htot[1] >= mcount || node_base + htot[0] > nt - 1 || ++iters > 100000) {
+        err = "PLOC clustering made no progress";
+        rc = J3DG_ERR_CUDA;
+        goto cleanup;
+      }
+      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, nn, cscan, sscan, mcount, node_base, C1, lo1, hi1,
+                                                 child, box, count);
+      J3DG_CK(cudaGetLastError());
+      node_base += htot[0];
+      mcount = htot[1];
+      std::swap(C0, C1);
+      std::swap(lo0, lo1);
+      std::swap(hi0, hi1);
+    }
+    J3DG_CK(cudaMemcpyAsync(&root, C0, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    J3DG_CK(cudaStreamSynchronize(st));
+    if (node_base != nt - 1 || (root & 0x80000000u)) {
+      err = "PLOC clustering ended with a malformed tree";
+      rc = J3DG_ERR_CUDA;
+      goto cleanup;
+    }
+    J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
+    J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * 8 * (size_t)nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&pa, sizeof(PlaceItem) * (size_t)nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&pb, sizeof(PlaceItem) * (size_t)nt, st));
+    J3DG_CK(cudaMalloc((void**)&tris_out, sizeof(float4) * 3 * (size_t)nt));
+    {
+      const PlaceItem root_place{root, 0u, 1u, 0u};
+      J3DG_CK(cudaMemcpyAsync(pa, &root_place, sizeof(root_place), cudaMemcpyHostToDevice, st));
+    }
+    hc[0] = 0u;
+    hc[1] = 1u;  // wide nodes allocated (the root)
+    hc[2] = 0u;  // queue out
+    hc[3] = 0u;  // max depth
+    J3DG_CK(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    n_in = 1;
+    while (n_in > 0) {
+      J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
+      k_collapse_place<<<(n_in + 127) / 128, 128, 0, st>>>(child, box, count, (const float4*)m->d_tris, pa, n_in, pb,
+                                                          counters + 2, counters + 1, wide, m->leaf_size, counters + 3,
+                                                          tris_out, nt, d_status);
+      J3DG_CK(cudaGetLastError());
+      J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+      J3DG_CK(cudaStreamSynchronize(st));
+      n_in = hc[2];
+      std::swap(pa, pb);
+    }
+    m->n_nodes = hc[1];
+    m->max_depth = hc[3];
+    m->root_ref = 0;
+    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
+    J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
+    J3DG_CK(cudaStreamSynchronize(st));
+    cudaFree(m->d_tris);  // the leaf-ordered triangles are the placed ones now
+    m->d_tris = tris_out;
+    tris_out = nullptr;
     goto cleanup;
   }
 
@@ -571,6 +898,13 @@ cleanup:
   if (wide) cudaFreeAsync(wide, st);
   if (qa) cudaFreeAsync(qa, st);
   if (qb) cudaFreeAsync(qb, st);
+  for (uint32_t* p : {C0, C1, nn, create, survive, cscan, sscan, pl_sums, count, tot})
+    if (p) cudaFreeAsync(p, st);
+  for (float4* p : {lo0, hi0, lo1, hi1})
+    if (p) cudaFreeAsync(p, st);
+  if (pa) cudaFreeAsync(pa, st);
+  if (pb) cudaFreeAsync(pb, st);
+  if (tris_out) cudaFree(tris_out);
   {
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == J3DG_OK && e != cudaSuccess) {

@@ -34,6 +34,7 @@ struct j3dg_mesh {
   float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
   float scale = 0.f;  // max |coordinate| of the bbox corners
   uint32_t leaf_size = 4;
+  uint32_t build_flags = 0;  // j3dg_build_opts::flags
   uint32_t n_nodes = 0, max_depth = 0, root_ref = 0;
   float build_ms = 0.f;
   uint64_t device_bytes = 0;

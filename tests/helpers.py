@@ -22,9 +22,9 @@ def oracle_scene(O, V, T, poses, w, h, vfov=60.0, leaf=4, n_threads=None, cs_obj
     return m, views, (mn, mx, diag, piv, P, Pi)
 
 
-def gpu_scene(ctx, V, T, pose, leaf=2, db_id=1, cs_obj=None):
+def gpu_scene(ctx, V, T, pose, leaf=2, db_id=1, cs_obj=None, build="ploc"):
     from j3d_gb300 import Mesh, Scene
-    mesh = Mesh(ctx, V, T, leaf)
+    mesh = Mesh(ctx, V, T, leaf, build)
     sc = Scene()
     sc.add_object(mesh, cs_obj, db_id)
     sc.prepare_scene()

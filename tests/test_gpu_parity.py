@@ -69,8 +69,24 @@ def test_icosphere_config0_parity_and_golden(gpu_ctx, oracle_mod):
             compare_rgba(gi, oi, 1, "config0 edges")
 
 
-@pytest.mark.parametrize("leaf", [1, 2, 4, 8])
-def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf):
+def test_icosphere_config0_golden_with_lbvh_tree(gpu_ctx):
+    """The LBVH tree differs from the default (PLOC) tree but the frame is bit
+    for bit the committed golden frame (results do not depend on the tree)."""
+    from j3d_gb300 import workloads as W
+    wl = W.config0()
+    mesh, sc = gpu_scene(gpu_ctx, wl.vertices, wl.triangles, wl.poses[0], build="lbvh")
+    gold = json.loads((GOLDEN / "golden.json").read_text())["icosphere_L6_1024x768"]
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    gp, gi, cv, mc = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
+    assert sha(gp) == gold["frames"][0]["plain"]["gbuffer_sha"]
+    assert sha(gi) == gold["frames"][0]["plain"]["rgba_sha"]
+    ploc = gpu_scene(gpu_ctx, wl.vertices, wl.triangles, wl.poses[0])[0]
+    assert mesh.info().n_nodes != ploc.info().n_nodes or mesh.info().max_depth != ploc.info().max_depth
+
+
+@pytest.mark.parametrize("leaf,build", [(1, "lbvh"), (2, "lbvh"), (4, "lbvh"), (8, "lbvh"), (1, "ploc"),
+                                        (2, "ploc"), (8, "ploc")])
+def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build):
     from j3d_gb300 import workloads as W
     O = oracle_mod
     V, T = W.torus(300, 150, seed=W.SEED_BASE + 1)
@@ -78,7 +94,7 @@ def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf):
     m, views, _ = oracle_scene(O, V, T, poses, 480, 270)
     mesh = None
     for i, p in enumerate(poses):
-        mesh, sc = gpu_scene(gpu_ctx, V, T, p, leaf=leaf) if mesh is None else (mesh, sc)
+        mesh, sc = gpu_scene(gpu_ctx, V, T, p, leaf=leaf, build=build) if mesh is None else (mesh, sc)
         sc.set_pose(p)
         gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 480, 270, gst(shadow=True, edges=False))
         op, oi = oracle_frame(O, m, views[i], 480, 270, O.settings(shadow=True, edges=False))

@@ -469,7 +469,10 @@ int j3dg_learned_load(j3dg_learned* l, const char* path);
 /* Diagnostics (no reference counterpart): the network's two bf16
    tensor-core GEMMs, C[M x N] fp32 = A[M x K] . Bt[N x K]^T on device
    arrays (A, Bt bf16 row-major). impl 0: mma.sync (M, N % 128, K % 32);
-   impl 1: tcgen05 with a TMEM accumulator (M, N % 128, K % 64). Synchronous. */
+   impl 1: tcgen05 with a TMEM accumulator (M, N % 128, K % 64); impl 2: the
+   tcgen05 kernel with its MMAs withheld, so that its bounded mbarrier wait
+   runs out (~0.25 s): the call must return J3DG_ERR_DEVICE_STATUS with
+   J3DG_DEV_VISIT_CAP raised, and the context stays usable. Synchronous. */
 int j3dg_gemm_bf16(j3dg_ctx* ctx, const void* A, const void* Bt, float* C, uint32_t M, uint32_t N, uint32_t K,
                    int impl);
 

@@ -44,7 +44,9 @@ struct UmmaArgs {
   float* C;
   int M, N, K, lda, ldb, ldc;
 };
-cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st);
+// withhold != 0 issues no MMA and no commit, so the kernel's bounded wait runs
+// out (the failure path, exercised by a test)
+cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold = 0);
 
 // tanh(u) = 1 - 2 / (e^(2u) + 1) with the hardware exp2 approximation: its
 // error is a few ulp of 1, which is what the activation adds tanh to; the

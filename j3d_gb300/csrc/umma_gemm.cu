@@ -54,7 +54,8 @@ __device__ __forceinline__ void copy_chunk(const __nv_bfloat16* __restrict__ src
 template <int BN>
 __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __restrict__ A,
                                                       const __nv_bfloat16* __restrict__ Bt, float* __restrict__ C,
-                                                      int K, int lda, int ldb, int ldc, uint32_t* status) {
+                                                      int K, int lda, int ldb, int ldc, uint32_t* status,
+                                                      int withhold) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t taddr_s;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
     copy_chunk(Bt, ldb, n0, BN, kc * kChunkK, sB);
     umma::fence_async_smem();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !withhold) {  // withhold: nothing completes the barrier (failure-path test)
       umma::fence_after_sync();
       const uint32_t a0 = umma::smem_u32(sA), b0 = umma::smem_u32(sB);
 #pragma unroll
@@ -130,23 +131,23 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
 }
 
 template <int BN>
-cudaError_t launch(const UmmaArgs& g, uint32_t* status, cudaStream_t st) {
+cudaError_t launch(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold) {
   const uint32_t smem = GemmSmem<BN>::total;
   cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   dim3 grid(g.N / BN, g.M / 128);
-  k_umma_gemm<BN><<<grid, 128, smem, st>>>(g.A, g.Bt, g.C, g.K, g.lda, g.ldb, g.ldc, status);
+  k_umma_gemm<BN><<<grid, 128, smem, st>>>(g.A, g.Bt, g.C, g.K, g.lda, g.ldb, g.ldc, status, withhold);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st) {
+cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold) {
   if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.M % 128 || g.K % kChunkK || g.lda % 8 || g.ldb % 8 || g.ldc % 4 ||
       ((uintptr_t)g.A & 15) || ((uintptr_t)g.Bt & 15) || ((uintptr_t)g.C & 15))
     return cudaErrorInvalidValue;
-  if (g.N % 256 == 0) return launch<256>(g, status, st);
-  if (g.N % 128 == 0) return launch<128>(g, status, st);
+  if (g.N % 256 == 0) return launch<256>(g, status, st, withhold);
+  if (g.N % 128 == 0) return launch<128>(g, status, st, withhold);
   return cudaErrorInvalidValue;
 }
 
@@ -166,11 +167,11 @@ extern "C" int j3dg_gemm_bf16(j3dg_ctx* c, const void* A, const void* Bt, float*
     j3dg::GemmArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, nullptr, nullptr, (int)M, (int)N, (int)K,
                      (int)K, (int)K, (int)N};
     e = j3dg::gemm_bf16(g, false, true, j3dg::EPI_F32, st);
-  } else if (impl == 1) {
+  } else if (impl == 1 || impl == 2) {
     j3dg::UmmaArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, (int)M, (int)N, (int)K, (int)K, (int)K, (int)N};
-    e = j3dg::umma_gemm_bf16(g, c->d_status, st);
+    e = j3dg::umma_gemm_bf16(g, c->d_status, st, impl == 2);
   } else {
-    return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: impl must be 0 or 1");
+    return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: impl must be 0, 1 or 2");
   }
   if (e == cudaErrorInvalidValue) return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: unsupported shape");
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

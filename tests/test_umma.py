@@ -53,3 +53,24 @@ def test_gemm_rejects_unsupported_shapes(gpu_ctx):
     with pytest.raises(J3dgError):  # K % 64 != 0 on the tcgen05 path
         _check(gpu_ctx.h, _ffi.lib().j3dg_gemm_bf16(gpu_ctx.h, A.data_ptr(), B.data_ptr(), C.data_ptr(),
                                                     128, 128, 96, 1))
+
+
+@pytest.mark.gpu
+def test_bounded_wait_times_out_and_reports(gpu_ctx):
+    """The tcgen05 kernel with its MMAs withheld: nothing ever completes its
+    mbarrier, the bounded wait runs out, the kernel raises the status word,
+    frees its tensor memory and returns; the context keeps working."""
+    import torch
+    from j3d_gb300 import J3dgError, _ffi
+    from j3d_gb300.scene import _check
+    A, Bt, ref, mag = _case(128, 128, 64, seed=5)
+    dA, dB = A.cuda(), Bt.cuda()
+    C = torch.zeros(128, 128, dtype=torch.float32, device="cuda")
+    with pytest.raises(J3dgError) as e:
+        _check(gpu_ctx.h, _ffi.lib().j3dg_gemm_bf16(gpu_ctx.h, dA.data_ptr(), dB.data_ptr(), C.data_ptr(),
+                                                    128, 128, 64, 2))
+    assert e.value.status == 5  # J3DG_ERR_DEVICE_STATUS
+    assert float(C.abs().max()) == 0.0  # no epilogue ran
+    # the status word was cleared by the failing call; the next one works
+    Cn = _run(gpu_ctx, A, Bt, 1)
+    assert (np.abs(Cn - ref) <= 1e-5 * mag + 1e-30).all()

@@ -341,6 +341,8 @@ def run_own(args):
                        bvh_builder=args.build,
                        mesh_device_bytes=int(info.device_bytes),
                        bvh_build_mtris_per_s=round(28_090_000 / (build_ms / 1e3) / 1e6, 1),
+                       # T (12 + 36) B read + T 24 B boxes + nodes x 128 B written, per build ms
+                       bvh_build_alg_gbs=round((28_090_000 * (48 + 24) + info.n_nodes * 128) / (build_ms / 1e3) / 1e9, 1),
                        gpu_node_visits_per_ray=round(gvis / rays_per_step, 3),
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -533,7 +535,9 @@ def run_learned(args):
     B.build()
     wl = Wk.config1(N_CAMERAS, W_, H_)
     ctx = Context(0)
-    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf)
+    # the LBVH: its depth-6 subtrees are Morton-ordered ranges of the mesh,
+    # the "4096 spatial clusters (Morton order)" of this configuration
+    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, "lbvh")
     net = Learned(ctx, mesh, cluster_depth=6, batch=16384, lr=2e-3, seed=Wk.SEED_BASE + 3)
     loss, acc, train_s = net.train(args.learned_rays, 2.0, 5.0)
     info = mesh.info()

@@ -373,6 +373,16 @@ int j3dg_canvas_render_frame(j3dg_canvas* c, const j3dg_scene* s, const j3dg_mat
    destination, w x h elements). Synchronous; reports device status. */
 int j3dg_canvas_get_pixels(j3dg_canvas* c, j3dg_pixel* dst);
 int j3dg_canvas_get_image(j3dg_canvas* c, uint32_t* dst);
+/* No reference counterpart. Starts copying the G-buffer and/or the image
+   (either may be NULL; host memory should be pinned for the copy to run
+   asynchronously) on the context's copy stream, after the work already
+   queued on the canvas, and returns at once; the context stream keeps
+   rendering (another canvas, typically) while the copy runs. Calls that
+   write this canvas later wait on the device for the copy. */
+int j3dg_canvas_download_async(j3dg_canvas* c, j3dg_pixel* pixels, uint32_t* image);
+/* Blocks the host until the canvas's last download_async has completed
+   (device status is reported by j3dg_ctx_synchronize). */
+int j3dg_canvas_download_wait(j3dg_canvas* c);
 /* Upload a caller G-buffer into the canvas (w x h records). */
 int j3dg_canvas_set_pixels(j3dg_canvas* c, const j3dg_pixel* src);
 /* Counts the canvas's G-buffer records with a hit and with the shadow bit

@@ -147,6 +147,8 @@ SIGNATURES = {
     "j3dg_canvas_get_pixels": (_I, [_P, _P]),
     "j3dg_canvas_get_image": (_I, [_P, _P]),
     "j3dg_canvas_set_pixels": (_I, [_P, _P]),
+    "j3dg_canvas_download_async": (_I, [_P, _P, _P]),
+    "j3dg_canvas_download_wait": (_I, [_P]),
     "j3dg_canvas_count_hits": (_I, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "j3dg_canvas_device_buffers": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "j3dg_render_batch": (_I, [_P, C.POINTER(Frame), _U]),

@@ -265,6 +265,20 @@ namespace j3dg {
 
 int ctx_fail(j3dg_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
 
+// Before work that writes the canvas: the context stream waits (on the
+// device) for a download of the canvas still running on the copy stream.
+void canvas_writable(j3dg_canvas* cv) {
+  if (!cv->copy_pending) return;
+  cudaStreamWaitEvent(S(cv->ctx), (cudaEvent_t)cv->ev_copied, 0);
+  cv->copy_pending = false;
+}
+
+// Before the host frees or reallocates the canvas buffers.
+void canvas_settle(j3dg_canvas* cv) {
+  if (cv->ev_copied) cudaEventSynchronize((cudaEvent_t)cv->ev_copied);
+  cv->copy_pending = false;
+}
+
 // node-visit / triangle-test counters while counting is on, else null
 unsigned long long* ctx_counters(j3dg_ctx* c) { return all(c)->ex.counting ? all(c)->ex.d_counters : nullptr; }
 
@@ -334,6 +348,13 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
     return J3DG_ERR_CUDA;
   }
   c->stream = st;
+  cudaStream_t cst;
+  if (cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(st);
+    delete A;
+    return J3DG_ERR_CUDA;
+  }
+  c->copy_stream = cst;
   bool ok = cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
@@ -360,6 +381,7 @@ int j3dg_ctx_destroy(j3dg_ctx* c) {
   CtxAll* A = all(c);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(S(c));
+  if (c->copy_stream) cudaStreamSynchronize((cudaStream_t)c->copy_stream);
   cudaFree(c->d_status);
   cudaFree(c->d_inst);
   cudaFree(A->ex.d_counters);
@@ -370,6 +392,7 @@ int j3dg_ctx_destroy(j3dg_ctx* c) {
   if (A->ex.ev0) cudaEventDestroy(A->ex.ev0);
   if (A->ex.ev1) cudaEventDestroy(A->ex.ev1);
   if (c->stream) cudaStreamDestroy(S(c));
+  if (c->copy_stream) cudaStreamDestroy((cudaStream_t)c->copy_stream);
   delete A;
   return J3DG_OK;
 }
@@ -779,11 +802,14 @@ int j3dg_canvas_destroy(j3dg_canvas* cv) {
   if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(cv->ctx->device);
   cudaStreamSynchronize(S(cv->ctx));
+  j3dg::canvas_settle(cv);
   cudaFree(cv->d_pixels);
   cudaFree(cv->d_image);
   cudaFree(cv->d_background);
   cudaFree(cv->d_queue);
   cudaFree(cv->d_work);
+  if (cv->ev_ready) cudaEventDestroy((cudaEvent_t)cv->ev_ready);
+  if (cv->ev_copied) cudaEventDestroy((cudaEvent_t)cv->ev_copied);
   delete cv;
   return J3DG_OK;
 }
@@ -792,6 +818,7 @@ int j3dg_canvas_resize(j3dg_canvas* cv, uint32_t w, uint32_t h) {
   if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(cv->ctx->device);
   cudaStreamSynchronize(S(cv->ctx));
+  j3dg::canvas_settle(cv);
   j3dg_make_default_camera(&cv->camera);  // canvas.cpp:131
   return canvas_alloc(cv, w, h);
 }
@@ -841,6 +868,7 @@ int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, c
   if (int rc = scene_ok(c, s)) return rc;
   if (cv->w == 0 || cv->h == 0) return J3DG_OK;
   cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
   const DevInst* dinst = nullptr;
   if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
   // canvas.cpp:681-698: clamp the rectangle
@@ -866,6 +894,7 @@ int j3dg_canvas_render_scene(j3dg_canvas* cv, const j3dg_scene* s) {
   j3dg_ctx* c = cv->ctx;
   if (int rc = scene_ok(c, s)) return rc;
   cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
   const size_t n = (size_t)cv->w * cv->h;
   CK(c, j3dg::launch_copy_u32(cv->d_image, cv->d_background, n, S(c)), "render_scene");
   if (!s) {
@@ -879,6 +908,7 @@ static int shade(j3dg_canvas* cv, const j3dg_pixel* G, const j3dg_matcap* m, int
   j3dg_ctx* c = cv->ctx;
   if (!m) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "canvas_to_image: no matcap");
   if (cv->w == 0 || cv->h == 0) return J3DG_OK;
+  j3dg::canvas_writable(cv);
   FrameParams P;
   fill_frame(P, cv, nullptr, nullptr, m);
   CK(c, j3dg::launch_shade(P, G, shade_mode_of(cv->settings), fill_background, S(c)), "canvas_to_image");
@@ -911,6 +941,7 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   if (int rc = scene_ok(c, s)) return rc;
   if (cv->w == 0 || cv->h == 0) return J3DG_OK;
   cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
   const DevInst* dinst = nullptr;
   if (s)
     if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
@@ -1030,6 +1061,7 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
   cudaSetDevice(c->device);
   uint32_t total_inst = 0;
   if (int rc = check_frames(c, f, n, total_inst)) return rc;
+  for (uint32_t i = 0; i < n; ++i) j3dg::canvas_writable(f[i].canvas);
   BatchLayout L;
   L.set(n, total_inst);
   char* d = nullptr;
@@ -1124,6 +1156,7 @@ int j3dg_batch_launch(j3dg_batch* b) {
   if (!b) return J3DG_ERR_INVALID_ARGUMENT;
   j3dg_ctx* c = b->ctx;
   cudaSetDevice(c->device);
+  for (const auto& f : b->frames) j3dg::canvas_writable(f.canvas);
   CK(c, cudaGraphLaunch(b->exec, S(c)), "batch_launch");
   CK(c, cudaEventRecord(b->done, S(c)), "batch_launch");
   return J3DG_OK;
@@ -1154,10 +1187,44 @@ int j3dg_canvas_get_image(j3dg_canvas* cv, uint32_t* dst) {
   return copy_out(cv->ctx, dst, cv->d_image, sizeof(uint32_t) * (size_t)cv->w * cv->h);
 }
 
+int j3dg_canvas_download_async(j3dg_canvas* cv, j3dg_pixel* pixels, uint32_t* image) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  cudaSetDevice(c->device);
+  cudaStream_t cs = (cudaStream_t)c->copy_stream;
+  if (!cv->ev_ready) {
+    CK(c, cudaEventCreateWithFlags((cudaEvent_t*)&cv->ev_ready, cudaEventDisableTiming), "download_async");
+    CK(c, cudaEventCreateWithFlags((cudaEvent_t*)&cv->ev_copied, cudaEventDisableTiming), "download_async");
+  }
+  const size_t n = (size_t)cv->w * cv->h;
+  CK(c, cudaEventRecord((cudaEvent_t)cv->ev_ready, S(c)), "download_async");
+  CK(c, cudaStreamWaitEvent(cs, (cudaEvent_t)cv->ev_ready, 0), "download_async");
+  if (pixels && n)
+    CK(c, cudaMemcpyAsync(pixels, cv->d_pixels, sizeof(j3dg_pixel) * n,
+                          is_device_ptr(pixels) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, cs),
+       "download_async");
+  if (image && n)
+    CK(c, cudaMemcpyAsync(image, cv->d_image, sizeof(uint32_t) * n,
+                          is_device_ptr(image) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, cs),
+       "download_async");
+  CK(c, cudaEventRecord((cudaEvent_t)cv->ev_copied, cs), "download_async");
+  cv->copy_pending = true;
+  return J3DG_OK;
+}
+
+int j3dg_canvas_download_wait(j3dg_canvas* cv) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  if (!cv->ev_copied) return J3DG_OK;
+  cudaSetDevice(cv->ctx->device);
+  CK(cv->ctx, cudaEventSynchronize((cudaEvent_t)cv->ev_copied), "download_wait");
+  return J3DG_OK;
+}
+
 int j3dg_canvas_set_pixels(j3dg_canvas* cv, const j3dg_pixel* src) {
   if (!cv || !src) return J3DG_ERR_INVALID_ARGUMENT;
   j3dg_ctx* c = cv->ctx;
   cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
   CK(c, cudaMemcpyAsync(cv->d_pixels, src, sizeof(j3dg_pixel) * (size_t)cv->w * cv->h,
                         is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c)),
      "set_pixels");

@@ -20,6 +20,7 @@
 struct j3dg_ctx {
   int device = 0;
   void* stream = nullptr;        // cudaStream_t
+  void* copy_stream = nullptr;   // cudaStream_t of asynchronous canvas downloads
   uint32_t* d_status = nullptr;  // device status word
   void* d_inst = nullptr;        // device instance table (DevInst[])
   uint32_t inst_cap = 0;
@@ -65,6 +66,10 @@ struct j3dg_canvas {
   uint32_t* d_background = nullptr;
   void* d_queue = nullptr;       // shadow-ray jobs, 2 float4 per pixel
   uint32_t* d_work = nullptr;    // per-frame work counters
+  // asynchronous download: ev_ready marks the work queued before it, ev_copied its end
+  void* ev_ready = nullptr;
+  void* ev_copied = nullptr;
+  bool copy_pending = false;
 };
 
 // Decoded mesh / point-cloud file on the device (ingest.cu).

@@ -26,6 +26,7 @@
 
 namespace j3dg {
 int ctx_fail(j3dg_ctx* c, int code, const std::string& msg);
+void canvas_writable(j3dg_canvas* cv);
 }
 
 namespace {
@@ -254,6 +255,7 @@ int j3dg_canvas_render_pointclouds(j3dg_canvas* cv, const j3dg_scene* s, const j
   const uint64_t npix = (uint64_t)cv->w * cv->h;
   if (n_pcs == 0 || npix == 0) return J3DG_OK;
   cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
   // the shadow-ray queue (32 bytes per pixel) is idle between frames
   unsigned long long* keys = (unsigned long long*)cv->d_queue;
   const unsigned pix_blocks = (unsigned)((npix + 255) / 256);

@@ -446,6 +446,14 @@ class Canvas:
         pcs = scene._pc_instances()
         _check(self.ctx.h, lib().j3dg_canvas_render_pointclouds(self.h, C.byref(s), pcs, len(scene.pointclouds)))
 
+    def download_async(self, pixels=None, image=None) -> None:
+        """Starts copying the G-buffer / image into `pixels` / `image` (pinned
+        host or device buffers) on the copy stream; returns at once."""
+        _check(self.ctx.h, lib().j3dg_canvas_download_async(self.h, vptr(pixels), vptr(image)))
+
+    def download_wait(self) -> None:
+        _check(self.ctx.h, lib().j3dg_canvas_download_wait(self.h))
+
     def get_pixels(self, out=None):
         if out is None:
             out = np.empty((self.h_px, self.w), PIXEL_DTYPE)

@@ -259,3 +259,26 @@ def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod):
         assert (gp["depth"][hit] > 0).all() and (gp["depth"][~hit] == FLT_MAX).all()
         ids = gp["object_id"][hit]
         assert ids.max() < 28_090_000
+
+
+def test_async_download_overlaps_and_keeps_frame(gpu_ctx):
+    """download_async copies the frame queued before it even when the next
+    frame is rendered into the same canvas right after (the render waits for
+    the copy on the device); the copy equals get_pixels / get_image."""
+    import torch
+    from j3d_gb300 import workloads as W
+    V, T = W.icosphere(4, W.SEED_BASE + 95)
+    poses = [W.translation(0, 0, 3.0), W.translation(0.4, 0, 2.5)]
+    mesh, sc = gpu_scene(gpu_ctx, V, T, poses[0])
+    gp_a, gi_a, cv, mc = gpu_frame(gpu_ctx, sc, 320, 240, gst(shadow=True, edges=False))
+    hp = torch.zeros(320 * 240 * 32, dtype=torch.uint8, pin_memory=True)
+    hi = torch.zeros(320 * 240 * 4, dtype=torch.uint8, pin_memory=True)
+    cv.render_frame(sc, mc)
+    cv.download_async(hp, hi)
+    sc.set_pose(poses[1])
+    cv.render_frame(sc, mc)  # frame B into the same buffers
+    cv.download_wait()
+    assert np.array_equal(hp.numpy().view(gp_a.dtype).reshape(gp_a.shape), gp_a)
+    assert np.array_equal(hi.numpy().view(np.uint32).reshape(gi_a.shape), gi_a)
+    gp_b = cv.get_pixels()
+    assert not np.array_equal(gp_b, gp_a)

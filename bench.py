@@ -169,22 +169,27 @@ def run_reference(args):
     cpu = CpuRenderer(wl, n_threads)
     per_step = max(2.0, min(15.0, args.cpu_total / max(1, args.warmup + args.steps)))
     vals = []
-    total_rays = 0
+    total_rays = total_visits = total_tests = 0
     for i in range(args.warmup + args.steps):
         r = cpu.sample(tuple((i + k) % N_CAMERAS for k in range(N_CAMERAS)), per_step)
         if i >= args.warmup:
             vals.append(r[0] / r[1] / 1e6)
             total_rays += r[0]
+            total_visits += r[2]
+            total_tests += r[3]
     v = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
             "data": "synthetic (seeded displaced torus, no dataset)", "config": CONFIG,
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": n_threads, "kind": "port",
-                             "sample": f"per step ~{per_step:.1f} s of bands of 8 rows every 72 rows of one "
-                                       f"camera's 1920x1080 frame (primary + shadow + shading), {total_rays} rays "
-                                       "timed; the reference itself cannot be built (jtk absent, SSE-only canvas)"},
+                             "sample": f"per step up to {per_step:.1f} s of bands of 8 rows every 72 rows, "
+                                       "cycling over the 32 cameras' 1920x1080 frames (primary + shadow + "
+                                       f"shading), {total_rays} rays timed; the reference itself cannot be built "
+                                       "(jtk absent, SSE-only canvas)"},
             "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "bvh_build_s": round(cpu.m.build_seconds, 3)}
+            "bvh_build_s": round(cpu.m.build_seconds, 3),
+            "oracle_node_visits_per_ray": round(total_visits / max(1, total_rays), 4),
+            "oracle_tri_tests_per_ray": round(total_tests / max(1, total_rays), 4)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -319,20 +324,23 @@ def run_own(args):
             torch.distributed.destroy_process_group()
         return 0
 
-    # CPU baseline (oracle port) on a bounded sample; also gives the
-    # algorithmic bytes per ray of the 4-wide SAH BVH
+    # CPU baseline (oracle port) on a bounded sample, in a fresh process (no
+    # CUDA context or torch threads beside it: measured in-process it reads
+    # about half as fast); it also gives the algorithmic bytes per ray of the
+    # 4-wide SAH BVH
     cpu = None
     if not args.no_cpu:
-        import oracle.oracle as O
-        O.build()
-        n_threads = os.cpu_count() or 1
-        cr = CpuRenderer(wl, n_threads)
-        r = cr.sample(tuple(range(N_CAMERAS)), args.cpu_budget)
-        cpu = (r[0], r[1], r[2], r[3], cr.m.build_seconds, r[4], n_threads)
+        env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+        rr = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
+                             "--warmup", "0", "--cpu-total", str(args.cpu_budget)], capture_output=True, text=True,
+                            env=env)
+        ref = json.loads(rr.stdout.strip().splitlines()[-1]) if rr.returncode == 0 else None
+        if ref and "value" in ref:
+            cpu = ref
     peak, peak_kind = peaks()
     if cpu:
-        node_per_ray = cpu[2] / cpu[0]
-        tri_per_ray = cpu[3] / cpu[0]
+        node_per_ray = cpu["oracle_node_visits_per_ray"]
+        tri_per_ray = cpu["oracle_tri_tests_per_ray"]
     else:
         node_per_ray = gvis / rays_per_step
         tri_per_ray = gtests / rays_per_step
@@ -372,11 +380,9 @@ def run_own(args):
         "clocks": clk,
     }
     if cpu:
-        line["cpu_baseline"] = {"value": round(cpu[0] / cpu[1] / 1e6, 4), "unit": "Mrays/s", "cores": cpu[6],
-                                "kind": "port",
-                                "sample": f"{cpu[5]} rows (bands of 8 rows every 72 rows, cycling over the 32 cameras) of the "
-                                          f"1920x1080 primary+shadow+shading frames, {cpu[0]} rays in {cpu[1]:.1f} s; "
-                                          f"oracle BVH build {cpu[4]:.2f} s"}
+        line["cpu_baseline"] = dict(cpu["cpu_baseline"])
+        line["cpu_baseline"]["sample"] = ("separate process: " + cpu["cpu_baseline"]["sample"] +
+                                          f"; oracle BVH build {cpu['bvh_build_s']:.2f} s")
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

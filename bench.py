@@ -82,6 +82,10 @@ class ClockSampler:
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t0 = time.time()
+        while not self.rows and time.time() - t0 < 5.0:  # nvidia-smi is up and sampling
+            time.sleep(0.005)
+        self.first = len(self.rows)  # samples from here on fall in the timed region
 
     def _read(self):
         for line in self.proc.stdout:
@@ -96,12 +100,13 @@ class ClockSampler:
                 self.proc.kill()
             if self.thread:
                 self.thread.join(timeout=2)
-        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        rows = self.rows[getattr(self, "first", 0):] or self.rows
+        sm = [float(r[1]) for r in rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 class CpuRenderer:

@@ -57,6 +57,19 @@ __device__ __forceinline__ float4 mat_vec(const float* m, float x, float y, floa
   return make_float4(r[0], r[1], r[2], r[3]);
 }
 
+// three-input min / max (one instruction each on sm_100 and later); min and
+// max are exact, so the grouping does not change any value
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
   return fa(fa(fm(ax, bx), fm(ay, by)), fm(az, bz));
 }
@@ -106,8 +119,8 @@ __device__ __forceinline__ void slab(const Ray& r, float lox, float loy, float l
   float pnx = (r.neg & 1u) ? hix : lox, pfx = (r.neg & 1u) ? lox : hix;
   float pny = (r.neg & 2u) ? hiy : loy, pfy = (r.neg & 2u) ? loy : hiy;
   float pnz = (r.neg & 4u) ? hiz : loz, pfz = (r.neg & 4u) ? loz : hiz;
-  tn = fmaxf(fmaxf(__fmaf_rn(pnx, r.ix, r.nnx), __fmaf_rn(pny, r.iy, r.nny)), __fmaf_rn(pnz, r.iz, r.nnz));
-  tf = fminf(fminf(__fmaf_rn(pfx, r.ix, r.nfx), __fmaf_rn(pfy, r.iy, r.nfy)), __fmaf_rn(pfz, r.iz, r.nfz));
+  tn = max3f(__fmaf_rn(pnx, r.ix, r.nnx), __fmaf_rn(pny, r.iy, r.nny), __fmaf_rn(pnz, r.iz, r.nnz));
+  tf = min3f(__fmaf_rn(pfx, r.ix, r.nfx), __fmaf_rn(pfy, r.iy, r.nfy), __fmaf_rn(pfz, r.iz, r.nfz));
 }
 
 struct Best {
@@ -150,8 +163,8 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
   if (!(t < b.t || (!any && t == b.t && b.found && key_less(inst, id, b.inst, b.tri)))) return false;
   // bounds gate: t inside the slab interval of the triangle's own box
   float tn, tf;
-  slab(r, fminf(fminf(a.x, c1.x), c2.x), fminf(fminf(a.y, c1.y), c2.y), fminf(fminf(a.z, c1.z), c2.z),
-       fmaxf(fmaxf(a.x, c1.x), c2.x), fmaxf(fmaxf(a.y, c1.y), c2.y), fmaxf(fmaxf(a.z, c1.z), c2.z), tn, tf);
+  slab(r, min3f(a.x, c1.x, c2.x), min3f(a.y, c1.y, c2.y), min3f(a.z, c1.z, c2.z), max3f(a.x, c1.x, c2.x),
+       max3f(a.y, c1.y, c2.y), max3f(a.z, c1.z, c2.z), tn, tf);
   if (!(tn <= t && t <= tf)) return false;
   b.t = t;
   b.inst = inst;
@@ -219,29 +232,30 @@ struct Tracer {
     return false;
   }
 
-  // stack_ref / stack_t: the caller's per-thread traversal stack (kept out
-  // of the struct so that its scalar state can stay in registers)
+  // stack: the caller's per-thread traversal stack of (ref, entry t bits)
+  // pairs, one 8-byte access per push or pop (kept out of the struct so
+  // that its scalar state can stay in registers)
   __device__ __forceinline__ bool run(const DevInst* __restrict__ insts, uint32_t n_inst, int iters,
                                       uint32_t* status, uint32_t& visits, uint32_t& tests,
-                                      uint32_t* __restrict__ stack_ref, float* __restrict__ stack_t) {
+                                      uint2* __restrict__ stack) {
 #pragma unroll 1
     for (int it = 0; it < iters; ++it)
-      if (step(insts, n_inst, status, visits, tests, stack_ref, stack_t)) return true;
+      if (step(insts, n_inst, status, visits, tests, stack)) return true;
     return false;
   }
 
   // One traversal step: a pop, a leaf (its triangles) or a node. Returns
   // true when the ray is finished.
   __device__ __forceinline__ bool step(const DevInst* __restrict__ insts, uint32_t n_inst, uint32_t* status,
-                                       uint32_t& visits, uint32_t& tests, uint32_t* __restrict__ stack_ref,
-                                       float* __restrict__ stack_t) {
+                                       uint32_t& visits, uint32_t& tests, uint2* __restrict__ stack) {
     {
       if (cur == J3DG_EMPTY_REF) {
         bool got = false;
         while (sp > 0) {
           --sp;
-          if (stack_t[sp] <= b.t) {
-            cur = stack_ref[sp];
+          const uint2 e = stack[sp];
+          if (__uint_as_float(e.y) <= b.t) {
+            cur = e.x;
             got = true;
             break;
           }
@@ -291,11 +305,11 @@ struct Tracer {
       const float pnz[4] = {nz4.x, nz4.y, nz4.z, nz4.w}, pfz[4] = {fz4.x, fz4.y, fz4.z, fz4.w};
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const float tn = fmaxf(fmaxf(__fmaf_rn(pnx[c], r.ix, r.nnx), __fmaf_rn(pny[c], r.iy, r.nny)),
-                               __fmaf_rn(pnz[c], r.iz, r.nnz));
-        const float tf = fminf(fminf(__fmaf_rn(pfx[c], r.ix, r.nfx), __fmaf_rn(pfy[c], r.iy, r.nfy)),
-                               __fmaf_rn(pfz[c], r.iz, r.nfz));
-        float a = fmaxf(tn, r.t_near), e = fminf(tf, b.t);
+        // enter = max(tx, ty, tz, t_near), exit = min(tx, ty, tz, t_best)
+        const float a = max3f(__fmaf_rn(pnx[c], r.ix, r.nnx), __fmaf_rn(pny[c], r.iy, r.nny),
+                              fmaxf(__fmaf_rn(pnz[c], r.iz, r.nnz), r.t_near));
+        const float e = min3f(__fmaf_rn(pfx[c], r.ix, r.nfx), __fmaf_rn(pfy[c], r.iy, r.nfy),
+                              fminf(__fmaf_rn(pfz[c], r.iz, r.nfz), b.t));
         bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
         tc[c] = hit ? a : __int_as_float(0x7f800000);
         if (!hit) rc[c] = J3DG_EMPTY_REF;
@@ -319,8 +333,7 @@ struct Tracer {
 #pragma unroll
       for (int c = 3; c >= 1; --c)
         if (rc[c] != J3DG_EMPTY_REF) {
-          stack_ref[sp] = rc[c];
-          stack_t[sp] = tc[c];
+          stack[sp] = make_uint2(rc[c], __float_as_uint(tc[c]));
           ++sp;
         }
       cur = rc[0];
@@ -339,8 +352,7 @@ __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __rest
                                                  uint32_t* counter, uint32_t* status,
                                                  unsigned long long* counters) {
   Tracer T;
-  uint32_t stack_ref[J3DG_STACK];
-  float stack_t[J3DG_STACK];
+  uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = src.count();
   int64_t idx = -1;
@@ -366,7 +378,7 @@ __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __rest
       }
     }
     if (__all_sync(0xffffffffu, idx < 0 && exhausted)) break;
-    if (idx >= 0 && T.run(insts, n_inst, ITERS, status, visits, tests, stack_ref, stack_t)) {
+    if (idx >= 0 && T.run(insts, n_inst, ITERS, status, visits, tests, stack)) {
       src.finish(T, (uint32_t)idx);
       idx = -1;
     }

@@ -609,8 +609,7 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
   if (i < n) {
   const float* f = reinterpret_cast<const float*>(rays + i);
   Tracer T;
-  uint32_t stack_ref[J3DG_STACK];
-  float stack_t[J3DG_STACK];
+  uint2 stack[J3DG_STACK];
   T.begin(inst, 1, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], false);
   const uint32_t c0 = top2[2 * i], c1 = top2[2 * i + 1];
   for (int phase = 0; phase < 3; ++phase) {
@@ -628,7 +627,7 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
     T.budget = T.n_nodes + 1;
     uint32_t& pv = phase < 2 ? visits : exact_visits;
     uint32_t& pt = phase < 2 ? tests : exact_tests;
-    while (!T.step(inst, 1, status, pv, pt, stack_ref, stack_t)) {
+    while (!T.step(inst, 1, status, pv, pt, stack)) {
     }
   }
   j3dg_hit h;

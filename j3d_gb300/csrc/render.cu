@@ -244,8 +244,7 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
 
 __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(const FrameParams P) {
   Tracer T;
-  uint32_t stack_ref[J3DG_STACK];
-  float stack_t[J3DG_STACK];
+  uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
   int phase = 0;  // 0 idle, 1 primary, 2 shadow
@@ -284,7 +283,7 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(c
     // all lanes step together; leave to refill once enough lanes are idle
 #pragma unroll 1
     for (;;) {
-      if (phase != 0 && T.step(P.inst, P.n_inst, P.status, visits, tests, stack_ref, stack_t)) {
+      if (phase != 0 && T.step(P.inst, P.n_inst, P.status, visits, tests, stack)) {
         if (phase == 1) {
           phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
         } else {
@@ -356,8 +355,7 @@ __global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
     k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
                   uint32_t* work) {
   Tracer T;
-  uint32_t stack_ref[J3DG_STACK];
-  float stack_t[J3DG_STACK];
+  uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t total = offsets[n_frames];
   int phase = 0;
@@ -409,7 +407,7 @@ __global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
     for (;;) {
       if (phase != 0) {
         const FrameParams& P = params[frame];
-        if (T.step(P.inst, P.n_inst, P.status, visits, tests, stack_ref, stack_t)) {
+        if (T.step(P.inst, P.n_inst, P.status, visits, tests, stack)) {
           if (phase == 1) {
             phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
           } else {

@@ -132,6 +132,13 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 #ifndef J3DG_REFILL_AT
 #define J3DG_REFILL_AT 12
 #endif
+// 1: a lane whose ray finished parks until the warp leaves the tracing loop,
+// and the parked lanes run the finish code (hit record, shadow ray setup,
+// shading) together there, instead of the whole warp running that long
+// branch for one lane in most tracing steps
+#ifndef J3DG_DEFER_FINISH
+#define J3DG_DEFER_FINISH 1
+#endif
 static const int kTraceThreads = J3DG_TRACE_THREADS;
 static const int kIters = J3DG_TRACE_ITERS;
 
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(c
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
-  int phase = 0;  // 0 idle, 1 primary, 2 shadow
+  int phase = 0;  // 0 idle, 1 primary, 2 shadow, 3 / 4 primary / shadow finished (parked)
   bool exhausted = false;
   size_t pix = 0;
   uint32_t w0 = 0;
@@ -255,6 +262,12 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(c
   uint32_t visits = 0, tests = 0;
 #pragma unroll 1
   for (;;) {
+    if (phase == 3) {
+      phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
+    } else if (phase == 4) {
+      shadow_finish(P, T, pix, w0, su, sv);
+      phase = 0;
+    }
     // refill: every idle lane takes the next pixel; one atomic per warp
     const bool need = phase == 0 && !exhausted;
     const uint32_t m = __ballot_sync(0xffffffffu, need);
@@ -283,16 +296,20 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(c
     // all lanes step together; leave to refill once enough lanes are idle
 #pragma unroll 1
     for (;;) {
-      if (phase != 0 && T.step(P.inst, P.n_inst, P.status, visits, tests, stack)) {
+      if ((phase == 1 || phase == 2) && T.step(P.inst, P.n_inst, P.status, visits, tests, stack)) {
+#if J3DG_DEFER_FINISH
+        phase += 2;
+#else
         if (phase == 1) {
           phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
         } else {
           shadow_finish(P, T, pix, w0, su, sv);
           phase = 0;
         }
+#endif
       }
-      if (__all_sync(0xffffffffu, phase == 0)) break;
-      if (__popc(__ballot_sync(0xffffffffu, phase == 0 && !exhausted)) >= J3DG_REFILL_AT) break;
+      if (__all_sync(0xffffffffu, phase != 1 && phase != 2)) break;
+      if (__popc(__ballot_sync(0xffffffffu, (phase == 0 && !exhausted) || phase >= 3)) >= J3DG_REFILL_AT) break;
     }
   }
   if (P.counters) {
@@ -367,6 +384,15 @@ __global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
   uint32_t visits = 0, tests = 0;
 #pragma unroll 1
   for (;;) {
+    if (phase >= 3) {
+      const FrameParams& P = params[frame];
+      if (phase == 3) {
+        phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
+      } else {
+        shadow_finish(P, T, pix, w0, su, sv);
+        phase = 0;
+      }
+    }
     const bool need = phase == 0 && !exhausted;
     const uint32_t m = __ballot_sync(0xffffffffu, need);
     if (m) {
@@ -405,19 +431,23 @@ __global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
     if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
 #pragma unroll 1
     for (;;) {
-      if (phase != 0) {
+      if (phase == 1 || phase == 2) {
         const FrameParams& P = params[frame];
         if (T.step(P.inst, P.n_inst, P.status, visits, tests, stack)) {
+#if J3DG_DEFER_FINISH
+          phase += 2;
+#else
           if (phase == 1) {
             phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
           } else {
             shadow_finish(P, T, pix, w0, su, sv);
             phase = 0;
           }
+#endif
         }
       }
-      if (__all_sync(0xffffffffu, phase == 0)) break;
-      if (__popc(__ballot_sync(0xffffffffu, phase == 0 && !exhausted)) >= J3DG_REFILL_AT) break;
+      if (__all_sync(0xffffffffu, phase != 1 && phase != 2)) break;
+      if (__popc(__ballot_sync(0xffffffffu, (phase == 0 && !exhausted) || phase >= 3)) >= J3DG_REFILL_AT) break;
     }
   }
   unsigned long long* counters = params[0].counters;

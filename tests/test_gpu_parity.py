@@ -103,6 +103,38 @@ def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build):
         assert (gp["object_id"] != NO_ID).any()
 
 
+@pytest.mark.parametrize("case", ["inside_box", "looking_away", "off_centre"])
+def test_camera_placements_match_oracle(gpu_ctx, oracle_mod, case):
+    """Frames with the camera inside the mesh's box (in the torus hole),
+    looking away from the mesh (every ray misses), or with the mesh across
+    the image edge equal the oracle's."""
+    from j3d_gb300 import workloads as W
+    O = oracle_mod
+    V, T = W.torus(200, 100, seed=W.SEED_BASE + 3)
+    if case == "inside_box":
+        poses = W.cameras(3, W.SEED_BASE + 21, 0.05, 0.6)
+    elif case == "looking_away":
+        poses = W.cameras(3, W.SEED_BASE + 22, 2.5, 4.0)
+        poses[:, 0:3] *= -1.0  # rotate 180 degrees about the camera's y axis
+        poses[:, 8:11] *= -1.0
+    else:
+        poses = W.cameras(3, W.SEED_BASE + 23, 2.5, 4.0, target=(1.6, 0.4, -0.9))
+    m, views, _ = oracle_scene(O, V, T, poses, 320, 200)
+    mesh, sc = gpu_scene(gpu_ctx, V, T, poses[0])
+    hits = 0
+    for i, p in enumerate(poses):
+        sc.set_pose(p)
+        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 320, 200, gst(shadow=True, edges=False))
+        op, oi = oracle_frame(O, m, views[i], 320, 200, O.settings(shadow=True, edges=False))
+        assert compare_gbuffers(gp, op, f"{case} cam {i}") == 0
+        assert np.array_equal(gi, oi)
+        hits += int((gp["object_id"] != NO_ID).sum())
+    if case == "looking_away":
+        assert hits == 0
+    else:
+        assert hits > 0
+
+
 @pytest.mark.parametrize("mode", ["wireframe", "one_bit", "noshadow_edges", "shading_off"])
 def test_shading_modes(gpu_ctx, oracle_mod, mode):
     from j3d_gb300 import workloads as W

@@ -658,6 +658,101 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
   atomicMax(max_depth, it.depth);
 }
 
+// ------------------------------------------------ 7. depth-first order ----
+//
+// The collapse numbers wide nodes level by level, so the nodes on one ray's
+// path from the root to a leaf lie far apart in memory (one per level, each
+// level hundreds of MB wide at the bottom). Renumbering in depth-first order
+// puts every subtree in one contiguous range: the deep part of a path, and
+// the paths of neighbouring rays, then fall in the same few pages. Each
+// level is a contiguous index range (a collapse launch allocates exactly the
+// next level), so subtree sizes go bottom-up and new positions top-down, one
+// launch per level.
+
+#ifndef J3DG_DFS_ORDER
+#define J3DG_DFS_ORDER 1
+#endif
+
+__device__ __forceinline__ void child_refs(const float4* __restrict__ wide, uint32_t i, uint32_t r[4]) {
+  const float4 ch = wide[8 * (size_t)i + 6];
+  r[0] = __float_as_uint(ch.x);
+  r[1] = __float_as_uint(ch.y);
+  r[2] = __float_as_uint(ch.z);
+  r[3] = __float_as_uint(ch.w);
+}
+
+// size[i] = wide nodes in the subtree of i (children of level lo..hi are done)
+__global__ void k_dfs_size(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, uint32_t* __restrict__ size) {
+  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  uint32_t r[4], s = 1;
+  child_refs(wide, i, r);
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (!(r[c] & J3DG_LEAF_BIT)) s += size[r[c]];  // the empty ref has the leaf bit
+  size[i] = s;
+}
+
+// children of the level's nodes take consecutive ranges after their parent
+__global__ void k_dfs_place(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ size,
+                            uint32_t* __restrict__ pos) {
+  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  uint32_t r[4], next = pos[i] + 1;
+  child_refs(wide, i, r);
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (!(r[c] & J3DG_LEAF_BIT)) {
+      pos[r[c]] = next;
+      next += size[r[c]];
+    }
+}
+
+__global__ void k_dfs_permute(const float4* __restrict__ wide, uint32_t n, const uint32_t* __restrict__ pos,
+                              float4* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4* src = wide + 8 * (size_t)i;
+  float4* dst = out + 8 * (size_t)pos[i];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) dst[k] = src[k];
+  uint32_t r[4];
+  child_refs(wide, i, r);
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (!(r[c] & J3DG_LEAF_BIT)) r[c] = pos[r[c]];
+  dst[6] = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]), __uint_as_float(r[3]));
+  dst[7] = src[7];
+}
+
+// out = the n wide nodes of `wide` (root 0, level L = [level_end[L-1],
+// level_end[L]) with level_end[-1] = 0) in depth-first order; root stays 0.
+static cudaError_t dfs_order(const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end, float4* out,
+                             cudaStream_t st) {
+  uint32_t *size = nullptr, *pos = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&size, sizeof(uint32_t) * (size_t)n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&pos, sizeof(uint32_t) * (size_t)n, st);
+  const size_t L = level_end.size();
+  for (size_t l = L; e == cudaSuccess && l-- > 0;) {
+    const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
+    if (hi > lo) k_dfs_size<<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(pos, 0, sizeof(uint32_t), st);
+  for (size_t l = 0; e == cudaSuccess && l < L; ++l) {
+    const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
+    if (hi > lo) k_dfs_place<<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size, pos);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    k_dfs_permute<<<(n + 255) / 256, 256, 0, st>>>(wide, n, pos, out);
+    e = cudaGetLastError();
+  }
+  if (size) cudaFreeAsync(size, st);
+  if (pos) cudaFreeAsync(pos, st);
+  return e;
+}
+
 // ------------------------------------------------------------- driver ----
 
 #define J3DG_CK(x)                                             \
@@ -698,6 +793,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   uint32_t hc[4] = {0, 0, 0, 0};
   uint32_t n_in = 0;
   CollapseItem root_item;
+  std::vector<uint32_t> level_end(1, 1u);  // wide nodes of level L end at level_end[L]
 
   J3DG_CK(cudaMallocAsync((void**)&d_part, sizeof(float) * 6 * bbox_blocks, st));
   J3DG_CK(cudaMallocAsync((void**)&d_bb, sizeof(float) * 6, st));
@@ -827,13 +923,17 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
       J3DG_CK(cudaStreamSynchronize(st));
       n_in = hc[2];
+      if (hc[1] > level_end.back()) level_end.push_back(hc[1]);
       std::swap(pa, pb);
     }
     m->n_nodes = hc[1];
     m->max_depth = hc[3];
     m->root_ref = 0;
     J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
-    J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
+    if (J3DG_DFS_ORDER)
+      J3DG_CK(dfs_order(wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
+    else
+      J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
     J3DG_CK(cudaStreamSynchronize(st));
     cudaFree(m->d_tris);  // the leaf-ordered triangles are the placed ones now
     m->d_tris = tris_out;
@@ -873,13 +973,17 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
     J3DG_CK(cudaStreamSynchronize(st));
     n_in = hc[2];
+    if (hc[1] > level_end.back()) level_end.push_back(hc[1]);
     std::swap(qa, qb);
   }
   m->n_nodes = hc[1];
   m->max_depth = hc[3];
   m->root_ref = 0;
   J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
-  J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
+  if (J3DG_DFS_ORDER)
+    J3DG_CK(dfs_order(wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
+  else
+    J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
 
 cleanup:
   if (d_part) cudaFreeAsync(d_part, st);

@@ -38,9 +38,11 @@ RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
 # (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
 # --warmup 3 --no-cpu [--build lbvh]`), per BVH builder:
-#   ploc: reads 444.7 MB, writes 69.9 MB, L2 1763.2 MB
-#   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB
-FRAME_TRAFFIC = {"ploc": (444_731_920 + 69_880_184, 1_763_229_795),
+#   ploc: reads 446.6 MB, writes 68.9 MB, L2 1830.3 MB (depth-first node
+#         order, parked finishes)
+#   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB (level-order nodes,
+#         finishes in the tracing loop)
+FRAME_TRAFFIC = {"ploc": (446_644_712 + 68_909_984, 1_830_267_674),
                  "lbvh": (463_159_392 + 70_692_880, 1_837_113_990)}
 
 

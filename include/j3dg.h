@@ -152,6 +152,9 @@ typedef struct j3dg_mesh_info {
 
 /* No reference counterpart (j3d owns no device). One stream per context. */
 int j3dg_ctx_create(int device, j3dg_ctx** out);
+/* Returns J3DG_ERR_INVALID_ARGUMENT, and keeps the context, while meshes,
+   geometries, point clouds, matcaps, canvases, batches or learned predictors
+   made from it are not destroyed. */
 int j3dg_ctx_destroy(j3dg_ctx* ctx);
 /* Waits for the stream; returns J3DG_ERR_DEVICE_STATUS if a kernel raised
    the status word since the last check (the word is then cleared). */
@@ -341,7 +344,10 @@ int j3dg_matcap_destroy(j3dg_matcap* m);
 /* ----------------------------------------------------------------- canvas */
 
 /* canvas::canvas(w, h) + resize (canvas.cpp:102-134): device G-buffer, image
-   and background; default camera (camera.cpp:5-16) and its projection. */
+   and background; default camera (camera.cpp:5-16) and its projection.
+   The buffers come from a stream-ordered pool of the context: create,
+   resize and destroy are ordered on the context stream (after a pending
+   download) and do not wait for the device. */
 int j3dg_canvas_create(j3dg_ctx* ctx, uint32_t w, uint32_t h, j3dg_canvas** out);
 int j3dg_canvas_destroy(j3dg_canvas* c);
 int j3dg_canvas_resize(j3dg_canvas* c, uint32_t w, uint32_t h);

@@ -26,6 +26,7 @@ HIT_DTYPE = np.dtype([("found", "<u4"), ("distance", "<f4"), ("u", "<f4"), ("v",
 assert PIXEL_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 40 and HIT_DTYPE.itemsize == 24
 
 J3DG_OK = 0
+J3DG_ERR_INVALID_ARGUMENT = 1
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "no CUDA device",
                 5: "device status raised", 6: "unsupported"}
 

@@ -41,6 +41,11 @@ struct CtxExtra {
   uint32_t* d_ray_counter = nullptr;  // work counter of ray-batch queries
   bool counting = false;
   int batch_threads = 128;            // block shape of batched launches
+  // canvas buffers: stream-ordered allocations from a pool that keeps freed
+  // memory reserved, so a server that evicts and re-creates canvases under
+  // an HBM cap neither synchronizes the device (as cudaFree does) nor waits
+  // for the driver to map memory again
+  cudaMemPool_t canvas_pool = nullptr;
 };
 
 int fail(j3dg_ctx* c, int code, const std::string& msg) {
@@ -230,24 +235,37 @@ void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevI
   P.counters = X.counting ? X.d_counters : nullptr;
 }
 
-int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
+}  // namespace
+namespace j3dg {
+void canvas_writable(j3dg_canvas* cv);
+}  // namespace j3dg
+namespace {
+
+// Frees the canvas buffers in stream order on the context stream (after a
+// download still running on the copy stream, which the stream waits for).
+void canvas_release(j3dg_canvas* cv) {
   j3dg_ctx* c = cv->ctx;
-  cudaFree(cv->d_pixels);
-  cudaFree(cv->d_image);
-  cudaFree(cv->d_background);
-  cudaFree(cv->d_queue);
-  cudaFree(cv->d_work);
+  j3dg::canvas_writable(cv);
+  void* bufs[5] = {cv->d_pixels, cv->d_image, cv->d_background, cv->d_queue, cv->d_work};
+  for (void* b : bufs)
+    if (b) cudaFreeAsync(b, S(c));
   cv->d_pixels = cv->d_queue = nullptr;
   cv->d_image = cv->d_background = cv->d_work = nullptr;
+}
+
+int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
+  j3dg_ctx* c = cv->ctx;
+  canvas_release(cv);
   cv->w = w;
   cv->h = h;
   size_t n = (size_t)w * h;
   if (n) {
-    CK(c, cudaMalloc(&cv->d_pixels, sizeof(j3dg_pixel) * n), "canvas");
-    CK(c, cudaMalloc((void**)&cv->d_image, sizeof(uint32_t) * n), "canvas");
-    CK(c, cudaMalloc((void**)&cv->d_background, sizeof(uint32_t) * n), "canvas");
-    CK(c, cudaMalloc(&cv->d_queue, 2 * sizeof(float4) * n), "canvas");
-    CK(c, cudaMalloc((void**)&cv->d_work, 4 * sizeof(uint32_t)), "canvas");
+    cudaMemPool_t pool = all(c)->ex.canvas_pool;
+    CK(c, cudaMallocFromPoolAsync(&cv->d_pixels, sizeof(j3dg_pixel) * n, pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_image, sizeof(uint32_t) * n, pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_background, sizeof(uint32_t) * n, pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync(&cv->d_queue, 2 * sizeof(float4) * n, pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_work, 4 * sizeof(uint32_t), pool, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_image, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_background, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, j3dg::launch_init_pixels((j3dg_pixel*)cv->d_pixels, n, S(c)), "canvas");
@@ -255,7 +273,6 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
   // canvas.cpp:131-133: default camera and its projection
   j3dg_make_projection_matrix(&cv->camera, (int)w, (int)h, cv->projection);
   j3dg_invert_projection_matrix(cv->projection, cv->projection_inv);
-  CK(c, cudaStreamSynchronize(S(c)), "canvas");
   return J3DG_OK;
 }
 
@@ -270,12 +287,6 @@ int ctx_fail(j3dg_ctx* c, int code, const std::string& msg) { return fail(c, cod
 void canvas_writable(j3dg_canvas* cv) {
   if (!cv->copy_pending) return;
   cudaStreamWaitEvent(S(cv->ctx), (cudaEvent_t)cv->ev_copied, 0);
-  cv->copy_pending = false;
-}
-
-// Before the host frees or reallocates the canvas buffers.
-void canvas_settle(j3dg_canvas* cv) {
-  if (cv->ev_copied) cudaEventSynchronize((cudaEvent_t)cv->ev_copied);
   cv->copy_pending = false;
 }
 
@@ -355,7 +366,15 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
     return J3DG_ERR_CUDA;
   }
   c->copy_stream = cst;
-  bool ok = cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
+  cudaMemPoolProps props;
+  memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  uint64_t keep = UINT64_MAX;
+  bool ok = cudaMemPoolCreate(&A->ex.canvas_pool, &props) == cudaSuccess &&
+            cudaMemPoolSetAttribute(A->ex.canvas_pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess &&
+            cudaMalloc((void**)&c->d_status, sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_ray_counter, sizeof(uint32_t)) == cudaSuccess &&
@@ -378,6 +397,9 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
 
 int j3dg_ctx_destroy(j3dg_ctx* c) {
   if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  if (const uint32_t n = c->live.load())
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT,
+                "context still used by " + std::to_string(n) + " object(s): destroy them first");
   CtxAll* A = all(c);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(S(c));
@@ -391,6 +413,8 @@ int j3dg_ctx_destroy(j3dg_ctx* c) {
     if (A->ex.slot_ev[i]) cudaEventDestroy(A->ex.slot_ev[i]);
   if (A->ex.ev0) cudaEventDestroy(A->ex.ev0);
   if (A->ex.ev1) cudaEventDestroy(A->ex.ev1);
+  // canvases still alive keep their memory until they are destroyed
+  if (A->ex.canvas_pool) cudaMemPoolDestroy(A->ex.canvas_pool);
   if (c->stream) cudaStreamDestroy(S(c));
   if (c->copy_stream) cudaStreamDestroy((cudaStream_t)c->copy_stream);
   delete A;
@@ -452,6 +476,7 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   j3dg_mesh* m = new (std::nothrow) j3dg_mesh();
   if (!m) return J3DG_ERR_OUT_OF_MEMORY;
   m->ctx = c;
+  m->hold.attach(c);
   m->nv = nv;
   m->nt = nt;
   m->leaf_size = leaf;
@@ -756,6 +781,7 @@ int j3dg_matcap_create(j3dg_ctx* c, const uint32_t* px, uint32_t w, uint32_t h, 
   j3dg_matcap* m = new (std::nothrow) j3dg_matcap();
   if (!m) return J3DG_ERR_OUT_OF_MEMORY;
   m->ctx = c;
+  m->hold.attach(c);
   m->w = w;
   m->h = h;
   m->cavity = cavity;
@@ -787,6 +813,7 @@ int j3dg_canvas_create(j3dg_ctx* c, uint32_t w, uint32_t h, j3dg_canvas** out) {
   j3dg_canvas* cv = new (std::nothrow) j3dg_canvas();
   if (!cv) return J3DG_ERR_OUT_OF_MEMORY;
   cv->ctx = c;
+  cv->hold.attach(c);
   j3dg_make_default_camera(&cv->camera);
   memset(&cv->settings, 0, sizeof(cv->settings));
   int rc = canvas_alloc(cv, w, h);
@@ -801,13 +828,7 @@ int j3dg_canvas_create(j3dg_ctx* c, uint32_t w, uint32_t h, j3dg_canvas** out) {
 int j3dg_canvas_destroy(j3dg_canvas* cv) {
   if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(cv->ctx->device);
-  cudaStreamSynchronize(S(cv->ctx));
-  j3dg::canvas_settle(cv);
-  cudaFree(cv->d_pixels);
-  cudaFree(cv->d_image);
-  cudaFree(cv->d_background);
-  cudaFree(cv->d_queue);
-  cudaFree(cv->d_work);
+  canvas_release(cv);  // stream-ordered: no wait on the host
   if (cv->ev_ready) cudaEventDestroy((cudaEvent_t)cv->ev_ready);
   if (cv->ev_copied) cudaEventDestroy((cudaEvent_t)cv->ev_copied);
   delete cv;
@@ -817,8 +838,6 @@ int j3dg_canvas_destroy(j3dg_canvas* cv) {
 int j3dg_canvas_resize(j3dg_canvas* cv, uint32_t w, uint32_t h) {
   if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(cv->ctx->device);
-  cudaStreamSynchronize(S(cv->ctx));
-  j3dg::canvas_settle(cv);
   j3dg_make_default_camera(&cv->camera);  // canvas.cpp:131
   return canvas_alloc(cv, w, h);
 }
@@ -1042,6 +1061,7 @@ int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayou
 
 struct j3dg_batch {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   std::vector<j3dg_frame> frames;
   std::vector<std::vector<j3dg_instance>> objects;  // copies of each frame's objects
   std::vector<j3dg_scene> scenes;
@@ -1086,6 +1106,7 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
   j3dg_batch* b = new (std::nothrow) j3dg_batch();
   if (!b) return J3DG_ERR_OUT_OF_MEMORY;
   b->ctx = c;
+  b->hold.attach(c);
   b->frames.assign(f, f + n);
   b->objects.resize(n);
   b->scenes.resize(n);

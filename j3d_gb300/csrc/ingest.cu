@@ -671,6 +671,7 @@ int read_any(j3dg_ctx* c, Source& src, int format, j3dg_geometry** out) {
   if (!g) return J3DG_ERR_OUT_OF_MEMORY;
   memset(&g->info, 0, sizeof(g->info));
   g->ctx = c;
+  g->hold.attach(c);
   g->info.file_bytes = src.size;
   // header bytes for format detection and the PLY / STL headers
   std::vector<char> head((size_t)std::min<uint64_t>(src.size, 1 << 16));

@@ -2,6 +2,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <atomic>
+
 #include <string>
 
 #include "../../include/j3dg.h"
@@ -27,10 +29,29 @@ struct j3dg_ctx {
   void* h_inst = nullptr;        // pinned staging for the instance table
   int sm_count = 0;
   std::string last_error;
+  std::atomic<uint32_t> live{0};  // meshes, canvases, ... made from this context and not destroyed
+};
+
+// Member of every object made from a context: counts the object in the
+// context's `live` from attach() until the object is deleted, so that
+// j3dg_ctx_destroy can refuse to free a context that objects still use.
+struct CtxHold {
+  j3dg_ctx* ctx = nullptr;
+  CtxHold() = default;
+  CtxHold(const CtxHold&) = delete;
+  CtxHold& operator=(const CtxHold&) = delete;
+  void attach(j3dg_ctx* c) {
+    ctx = c;
+    if (c) c->live.fetch_add(1);
+  }
+  ~CtxHold() {
+    if (ctx) ctx->live.fetch_sub(1);
+  }
 };
 
 struct j3dg_mesh {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   uint32_t nv = 0, nt = 0;
   float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
   float scale = 0.f;  // max |coordinate| of the bbox corners
@@ -51,12 +72,14 @@ struct j3dg_mesh {
 
 struct j3dg_matcap {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   uint32_t w = 0, h = 0, cavity = 0;
   uint32_t* d_pixels = nullptr;
 };
 
 struct j3dg_canvas {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   uint32_t w = 0, h = 0;
   j3dg_camera camera;
   float projection[16], projection_inv[16];
@@ -75,6 +98,7 @@ struct j3dg_canvas {
 // Decoded mesh / point-cloud file on the device (ingest.cu).
 struct j3dg_geometry {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   uint64_t nv = 0, nt = 0;
   float* d_v = nullptr;      // 3 nv
   uint32_t* d_t = nullptr;   // 3 nt
@@ -87,6 +111,7 @@ struct j3dg_geometry {
 // Point cloud on the device (pointcloud.cu).
 struct j3dg_pointcloud {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   uint64_t n = 0;
   float* d_v = nullptr;      // 3 n
   uint32_t* d_c = nullptr;   // n packed RGBA8, or null

@@ -660,6 +660,7 @@ using j3dg::GemmArgs;
 
 struct j3dg_learned {
   j3dg_ctx* ctx = nullptr;
+  CtxHold hold;
   const j3dg_mesh* mesh = nullptr;
   j3dg_learned_opts opts;
   j3dg::Layout L;
@@ -805,6 +806,7 @@ int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_o
   j3dg_learned* l = new (std::nothrow) j3dg_learned();
   if (!l) return J3DG_ERR_OUT_OF_MEMORY;
   l->ctx = c;
+  l->hold.attach(c);
   l->mesh = mesh;
   l->opts.cluster_depth = 6;
   l->opts.batch = 16384;
@@ -820,34 +822,42 @@ int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_o
     delete l;
     return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned: cluster_depth <= 6, batch a multiple of 128");
   }
-  // clusters: the refs at cluster_depth below the root (and shallower leaves)
-  const uint32_t top = std::min<uint32_t>(mesh->n_nodes, 1u << 14);
-  std::vector<float> nodes((size_t)top * 32);
+  // clusters: the refs at cluster_depth below the root (and shallower
+  // leaves), found by walking the tree from the root (node numbering is free)
+  std::vector<uint32_t> level{mesh->root_ref};
   cudaError_t e = cudaSuccess;
-  if (top) e = cudaMemcpy(nodes.data(), mesh->d_nodes, sizeof(float) * 32 * top, cudaMemcpyDeviceToHost);
+  for (uint32_t d = 0; d < l->opts.cluster_depth && e == cudaSuccess; ++d) {
+    std::vector<uint32_t> inner;
+    for (uint32_t ref : level)
+      if (!(ref & J3DG_LEAF_BIT)) inner.push_back(ref);
+    std::vector<uint32_t> refs(4 * inner.size());
+    for (size_t i = 0; i < inner.size() && e == cudaSuccess; ++i) {
+      if (inner[i] >= mesh->n_nodes) {
+        delete l;
+        return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned: corrupt node reference");
+      }
+      // the child references: float4 6 of the node
+      e = cudaMemcpyAsync(&refs[4 * i], (const float4*)mesh->d_nodes + 8 * (size_t)inner[i] + 6, 16,
+                          cudaMemcpyDeviceToHost, LS(l));
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(LS(l));
+    // children in the order of their parents and slots, leaves kept in place
+    size_t li = 0;
+    std::vector<uint32_t> ordered;
+    for (uint32_t ref : level) {
+      if (ref & J3DG_LEAF_BIT) {
+        ordered.push_back(ref);
+        continue;
+      }
+      for (int k = 0; k < 4; ++k)
+        if (refs[4 * li + k] != J3DG_EMPTY_REF) ordered.push_back(refs[4 * li + k]);
+      ++li;
+    }
+    level.swap(ordered);
+  }
   if (e != cudaSuccess) {
     delete l;
     return j3dg::ctx_fail(c, J3DG_ERR_CUDA, "learned: reading nodes failed");
-  }
-  std::vector<uint32_t> level{mesh->root_ref};
-  for (uint32_t d = 0; d < l->opts.cluster_depth; ++d) {
-    std::vector<uint32_t> next;
-    for (uint32_t ref : level) {
-      if (ref & J3DG_LEAF_BIT) {
-        next.push_back(ref);
-        continue;
-      }
-      if (ref >= top) {
-        delete l;
-        return j3dg::ctx_fail(c, J3DG_ERR_UNSUPPORTED, "learned: cluster level beyond the first nodes");
-      }
-      for (int k = 0; k < 4; ++k) {
-        uint32_t ch;
-        memcpy(&ch, &nodes[(size_t)ref * 32 + 24 + k], 4);
-        if (ch != J3DG_EMPTY_REF) next.push_back(ch);
-      }
-    }
-    level.swap(next);
   }
   if (level.size() > (size_t)j3dg::kOut) {
     delete l;

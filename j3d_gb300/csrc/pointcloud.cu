@@ -161,6 +161,7 @@ int make_pc(j3dg_ctx* c, uint64_t n, j3dg_pointcloud** out, j3dg_pointcloud** pc
   *pc = new (std::nothrow) j3dg_pointcloud();
   if (!*pc) return J3DG_ERR_OUT_OF_MEMORY;
   (*pc)->ctx = c;
+  (*pc)->hold.attach(c);
   (*pc)->n = n;
   *out = nullptr;
   return J3DG_OK;

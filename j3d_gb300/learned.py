@@ -40,6 +40,7 @@ class Learned:
         o = LearnedOpts(cluster_depth, batch, lr, 0, seed)
         _check(ctx.h, lib().j3dg_learned_create(ctx.h, mesh.h, C.byref(o), C.byref(h)))
         self.h = h
+        ctx._own(self)
         k, p = C.c_uint32(), C.c_uint64()
         _check(ctx.h, lib().j3dg_learned_info(self.h, C.byref(k), C.byref(p)))
         self.n_clusters, self.n_params = int(k.value), int(p.value)

@@ -12,6 +12,7 @@ Calls that the C-ABI rejects raise J3dgError.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -37,10 +38,26 @@ class Context:
         if st != _ffi.J3DG_OK:
             raise J3dgError(st, f"j3dg_ctx_create(device={device})")
         self.h = h
+        self._objs: dict = {}  # id -> weak reference, in creation order
+
+    def _own(self, obj) -> None:
+        """Registers an object made from this context; close() closes it first.
+        The entry goes away with the object (a server makes many canvases)."""
+        objs, key = self._objs, id(obj)
+        objs[key] = weakref.ref(obj, lambda _r: objs.pop(key, None))
 
     def close(self) -> None:
+        """Closes the meshes, canvases, ... made from this context (newest
+        first), then the context itself."""
         if self.h:
-            lib().j3dg_ctx_destroy(self.h)
+            for r in reversed(list(self._objs.values())):
+                o = r()
+                if o is not None:
+                    o.close()
+            self._objs.clear()
+            st = lib().j3dg_ctx_destroy(self.h)
+            if st != _ffi.J3DG_OK:
+                raise J3dgError(st, lib().j3dg_last_error(self.h).decode())
             self.h = None
 
     def __del__(self):
@@ -88,6 +105,7 @@ class Mesh:
         _check(ctx.h, lib().j3dg_mesh_build(ctx.h, vptr(vertices), nv, vptr(triangles), nt, C.byref(opts),
                                             C.byref(h)))
         self.h = h
+        ctx._own(self)
 
     def close(self) -> None:
         if self.h:
@@ -129,6 +147,7 @@ class Geometry:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
         self.h = handle
+        ctx._own(self)
         i = _ffi.GeometryInfo()
         _check(ctx.h, lib().j3dg_geometry_get_info(self.h, C.byref(i)))
         self.info = i
@@ -188,6 +207,7 @@ class PointCloud:
             n = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
             _check(ctx.h, lib().j3dg_pointcloud_create(ctx.h, vptr(vertices), n, vptr(colors), C.byref(h)))
         self.h = h
+        ctx._own(self)
 
     def bounds(self) -> tuple[np.ndarray, np.ndarray]:
         mn = np.zeros(3, np.float32)
@@ -224,6 +244,7 @@ def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2, build: 
     opts = BuildOpts(leaf_size, Mesh.BUILDERS[build])
     _check(ctx.h, lib().j3dg_mesh_build_geometry(ctx.h, geom.h, C.byref(opts), C.byref(h)))
     m.h = h
+    ctx._own(m)
     return m
 
 
@@ -338,6 +359,7 @@ class Matcap:
         H, W = self.pixels.shape
         _check(ctx.h, lib().j3dg_matcap_create(ctx.h, vptr(self.pixels), W, H, self.cavity_clr, C.byref(h)))
         self.h = h
+        ctx._own(self)
 
     @staticmethod
     def make(ctx: Context, kind: int = 0) -> "Matcap":
@@ -371,6 +393,7 @@ class Canvas:
         hh = C.c_void_p()
         _check(ctx.h, lib().j3dg_canvas_create(ctx.h, w, h, C.byref(hh)))
         self.h = hh
+        ctx._own(self)
         self.w, self.h_px = w, h
 
     def close(self) -> None:
@@ -513,6 +536,7 @@ class Batch:
         h = C.c_void_p()
         _check(ctx.h, lib().j3dg_batch_create(ctx.h, arr, len(self.frames), C.byref(h)))
         self.h = h
+        ctx._own(self)
         del keep
 
     def set_scene(self, i: int, scene: "Scene") -> None:

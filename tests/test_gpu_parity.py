@@ -314,3 +314,68 @@ def test_async_download_overlaps_and_keeps_frame(gpu_ctx):
     assert np.array_equal(hi.numpy().view(np.uint32).reshape(gi_a.shape), gi_a)
     gp_b = cv.get_pixels()
     assert not np.array_equal(gp_b, gp_a)
+
+
+def test_canvas_resize_and_churn_keep_frames(gpu_ctx, oracle_mod):
+    """Canvas buffers are freed in stream order: a resize right after
+    download_async still delivers the downloaded frame, the resized canvas
+    renders the oracle's frame, and canvases created and destroyed in a loop
+    (the pattern of a server evicting canvases under an HBM cap) all render
+    the oracle's frame."""
+    import torch
+    from j3d_gb300 import Canvas, camera_for_vfov
+    from j3d_gb300 import workloads as W
+    O = oracle_mod
+    V, T = W.icosphere(4, W.SEED_BASE + 96)
+    pose = W.translation(0.2, -0.1, 2.8)
+    mesh, sc = gpu_scene(gpu_ctx, V, T, pose)
+    st = gst(shadow=True, edges=False)
+    gp_a, gi_a, cv, mc = gpu_frame(gpu_ctx, sc, 320, 240, st)
+    hp = torch.zeros(320 * 240 * 32, dtype=torch.uint8, pin_memory=True)
+    hi = torch.zeros(320 * 240 * 4, dtype=torch.uint8, pin_memory=True)
+    cv.render_frame(sc, mc)
+    cv.download_async(hp, hi)
+    cv.resize(200, 150)
+    cv.download_wait()
+    assert np.array_equal(hp.numpy().view(gp_a.dtype).reshape(gp_a.shape), gp_a)
+    assert np.array_equal(hi.numpy().view(np.uint32).reshape(gi_a.shape), gi_a)
+    ref = {}
+    for w, h in ((200, 150), (320, 240)):
+        m, views, _ = oracle_scene(O, V, T, [pose], w, h)
+        ref[(w, h)] = oracle_frame(O, m, views[0], w, h, O.settings(shadow=True, edges=False))
+    cv.set_camera(camera_for_vfov(60.0))
+    cv.set_background_color()
+    cv.render_frame(sc, mc)
+    assert compare_gbuffers(cv.get_pixels(), ref[(200, 150)][0], "resized") == 0
+    assert np.array_equal(cv.get_image(), ref[(200, 150)][1])
+    for i in range(12):
+        w, h = (200, 150) if i % 2 else (320, 240)
+        c2 = Canvas(gpu_ctx, w, h)
+        c2.set_camera(camera_for_vfov(60.0))
+        c2.set_background_color()
+        c2.update_settings(st)
+        c2.render_frame(sc, mc)
+        assert compare_gbuffers(c2.get_pixels(), ref[(w, h)][0], f"churn {i}") == 0
+        assert np.array_equal(c2.get_image(), ref[(w, h)][1])
+        c2.close()
+
+
+def test_context_refuses_to_close_under_live_objects(gpu_ctx):
+    """j3dg_ctx_destroy refuses while meshes, canvases, ... made from the
+    context are alive (the context stays usable); Context.close() closes
+    them first (newest first) and then the context."""
+    from j3d_gb300 import Canvas, Context, J3dgError, Matcap, Mesh, _ffi
+    from j3d_gb300 import workloads as W
+    from j3d_gb300.scene import _check
+    V, T = W.icosphere(2, W.SEED_BASE + 97)
+    ctx = Context(0)
+    mesh = Mesh(ctx, V, T)
+    cv = Canvas(ctx, 64, 48)
+    mc = Matcap.make(ctx, 0)
+    with pytest.raises(J3dgError) as e:
+        _check(ctx.h, _ffi.lib().j3dg_ctx_destroy(ctx.h))
+    assert e.value.status == _ffi.J3DG_ERR_INVALID_ARGUMENT
+    assert b"3 object" in _ffi.lib().j3dg_last_error(ctx.h)
+    cv.render_frame(gpu_scene(ctx, V, T, W.translation(0, 0, 3.0))[1], mc)  # still works
+    ctx.close()
+    assert ctx.h is None and mesh.h is None and cv.h is None and mc.h is None

@@ -1022,8 +1022,9 @@ int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_i
 
 // Fills host staging `h` for device base `d` (pointers inside point to `d`).
 // Frame i's objects take cap[i] instance slots (its object count if cap is null).
-void pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h, char* d,
-                 const uint32_t* cap = nullptr) {
+// Returns the total primary items of the frames.
+uint32_t pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h, char* d,
+                     const uint32_t* cap = nullptr) {
   FrameParams* P = reinterpret_cast<FrameParams*>(h + L.off_params);
   uint32_t* off = reinterpret_cast<uint32_t*>(h + L.off_offsets);
   DevInst* I = reinterpret_cast<DevInst*>(h + L.off_inst);
@@ -1040,12 +1041,14 @@ void pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h,
     items += f[i].canvas->w && f[i].canvas->h ? j3dg::primary_items(P[i]) : 0u;
   }
   off[n] = items;
+  return items;
 }
 
-int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* d, uint32_t* work) {
+int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* d, uint32_t items,
+                  uint32_t* work) {
   const FrameParams* dP = reinterpret_cast<const FrameParams*>(d + L.off_params);
   const uint32_t* dOff = reinterpret_cast<const uint32_t*>(d + L.off_offsets);
-  CK(c, j3dg::launch_render_batch(dP, dOff, n, work, all(c)->ex.batch_threads, S(c)), "batch");
+  CK(c, j3dg::launch_render_batch(dP, dOff, n, items, work, all(c)->ex.batch_threads, S(c)), "batch");
   for (uint32_t i = 0; i < n; ++i) {
     const int mode = shade_mode_of(f[i].canvas->settings);
     if (mode != 0 && f[i].canvas->w && f[i].canvas->h) {
@@ -1089,10 +1092,10 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
   std::vector<char> h(L.bytes);
   CK(c, cudaMallocAsync((void**)&d, L.bytes + 256, S(c)), "render_batch");
   work = reinterpret_cast<uint32_t*>(d + L.bytes);
-  pack_frames(f, n, L, h.data(), d);
+  const uint32_t items = pack_frames(f, n, L, h.data(), d);
   // pageable source: the copy is staged before the call returns
   CK(c, cudaMemcpyAsync(d, h.data(), L.bytes, cudaMemcpyHostToDevice, S(c)), "render_batch");
-  int rc = enqueue_batch(c, f, n, L, d, work);
+  int rc = enqueue_batch(c, f, n, L, d, items, work);
   cudaFreeAsync(d, S(c));
   return rc;
 }
@@ -1129,14 +1132,14 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
     return cuda_fail(c, e, "batch_create");
   }
   b->work = reinterpret_cast<uint32_t*>(b->d + b->L.bytes);
-  pack_frames(b->frames.data(), n, b->L, b->h, b->d);
+  const uint32_t items = pack_frames(b->frames.data(), n, b->L, b->h, b->d);
   // capture: upload of the staged parameters, the launch and the shading passes
   cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   e = cudaStreamBeginCapture(S(c), mode);
   int rc = J3DG_OK;
   if (e == cudaSuccess) {
     e = cudaMemcpyAsync(b->d, b->h, b->L.bytes, cudaMemcpyHostToDevice, S(c));
-    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, b->work);
+    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work);
     cudaError_t e2 = cudaStreamEndCapture(S(c), &b->graph);
     if (e == cudaSuccess) e = e2;
   }

@@ -123,12 +123,49 @@ __device__ __forceinline__ void slab(const Ray& r, float lox, float loy, float l
   tf = min3f(__fmaf_rn(pfx, r.ix, r.nfx), __fmaf_rn(pfy, r.iy, r.nfy), __fmaf_rn(pfz, r.iz, r.nfz));
 }
 
+// 1: state a traversal step does not read (the world ray, the best hit's
+// attributes) lives in shared memory, one slot per thread, so that the
+// registers left cover the step's working set and more warps fit an SM.
+// Every kernel that traces runs blocks of at most J3DG_COLD_MAX threads.
+#ifndef J3DG_COLD_SMEM
+#define J3DG_COLD_SMEM 7
+#endif
+#ifndef J3DG_COLD_MAX
+#define J3DG_COLD_MAX 256
+#endif
+#if J3DG_COLD_SMEM & 1
+__shared__ float j3dg_cold_ray[6][J3DG_COLD_MAX];
+#endif
+#if J3DG_COLD_SMEM & 2
+__shared__ float j3dg_cold_uv[2][J3DG_COLD_MAX];
+__shared__ uint32_t j3dg_cold_key[3][J3DG_COLD_MAX];
+#endif
+
+// Best hit so far: t and found are read every step; the key (inst, tri) only
+// on a t tie, u / v / slot only when the ray finishes.
 struct Best {
   float t;
-  uint32_t inst, tri;  // key = (inst, tri); found == (t < t_far set by an accept)
-  float u, v;
-  uint32_t slot;       // leaf-order position of the best triangle
-  bool found;
+  bool found;  // found == (t < t_far set by an accept)
+#if J3DG_COLD_SMEM & 2
+  __device__ __forceinline__ float& u() const { return j3dg_cold_uv[0][threadIdx.x]; }
+  __device__ __forceinline__ float& v() const { return j3dg_cold_uv[1][threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& inst() const { return j3dg_cold_key[0][threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& tri() const { return j3dg_cold_key[1][threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& slot() const { return j3dg_cold_key[2][threadIdx.x]; }
+#else
+  float u_, v_;
+  uint32_t inst_, tri_, slot_;
+  __device__ __forceinline__ float& u() { return u_; }
+  __device__ __forceinline__ float& v() { return v_; }
+  __device__ __forceinline__ uint32_t& inst() { return inst_; }
+  __device__ __forceinline__ uint32_t& tri() { return tri_; }
+  __device__ __forceinline__ uint32_t& slot() { return slot_; }
+  __device__ __forceinline__ float u() const { return u_; }
+  __device__ __forceinline__ float v() const { return v_; }
+  __device__ __forceinline__ uint32_t inst() const { return inst_; }
+  __device__ __forceinline__ uint32_t tri() const { return tri_; }
+  __device__ __forceinline__ uint32_t slot() const { return slot_; }
+#endif
 };
 
 __device__ __forceinline__ bool key_less(uint32_t ia, uint32_t ta, uint32_t ib, uint32_t tb) {
@@ -160,18 +197,18 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
   if (!(u >= 0.f && v >= 0.f && fa(u, v) <= 1.f)) return false;
   if (!(t > r.t_near)) return false;
   uint32_t id = __float_as_uint(a.w);
-  if (!(t < b.t || (!any && t == b.t && b.found && key_less(inst, id, b.inst, b.tri)))) return false;
+  if (!(t < b.t || (!any && t == b.t && b.found && key_less(inst, id, b.inst(), b.tri())))) return false;
   // bounds gate: t inside the slab interval of the triangle's own box
   float tn, tf;
   slab(r, min3f(a.x, c1.x, c2.x), min3f(a.y, c1.y, c2.y), min3f(a.z, c1.z, c2.z), max3f(a.x, c1.x, c2.x),
        max3f(a.y, c1.y, c2.y), max3f(a.z, c1.z, c2.z), tn, tf);
   if (!(tn <= t && t <= tf)) return false;
   b.t = t;
-  b.inst = inst;
-  b.tri = id;
-  b.u = u;
-  b.v = v;
-  b.slot = slot;
+  b.inst() = inst;
+  b.tri() = id;
+  b.u() = u;
+  b.v() = v;
+  b.slot() = slot;
   b.found = true;
   return true;
 }
@@ -183,7 +220,13 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
 // most `iters` node or leaf steps, so persistent warps can refill lanes whose
 // rays have finished. Corrupt trees raise status bits instead of trapping.
 struct Tracer {
-  float wox, woy, woz, wdx, wdy, wdz;  // world ray
+#if J3DG_COLD_SMEM & 1
+  // world ray: read only when an object's walk starts, kept in shared memory
+  __device__ __forceinline__ float& wr(int k) { return j3dg_cold_ray[k][threadIdx.x]; }
+#else
+  float wr_[6];  // world ray
+  __device__ __forceinline__ float& wr(int k) { return wr_[k]; }
+#endif
   bool any;                             // stop at the first accepted triangle
   Ray r;                                // object-space ray of object `inst`
   Best b;
@@ -197,8 +240,8 @@ struct Tracer {
 
   __device__ __forceinline__ void start_object(const DevInst* __restrict__ insts) {
     const DevInst& I = insts[inst];
-    float4 o = mat_vec(I.inv, wox, woy, woz, 1.f);
-    float4 d = mat_vec(I.inv, wdx, wdy, wdz, 0.f);
+    float4 o = mat_vec(I.inv, wr(0), wr(1), wr(2), 1.f);
+    float4 d = mat_vec(I.inv, wr(3), wr(4), wr(5), 0.f);
     r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, r.t_near, I.scale);
     nodes = I.nodes;
     tris = I.tris;
@@ -214,18 +257,18 @@ struct Tracer {
                                         float oz, float dx, float dy, float dz, float t_near, float t_far,
                                         bool any_hit) {
     any = any_hit;
-    wox = ox;
-    woy = oy;
-    woz = oz;
-    wdx = dx;
-    wdy = dy;
-    wdz = dz;
+    wr(0) = ox;
+    wr(1) = oy;
+    wr(2) = oz;
+    wr(3) = dx;
+    wr(4) = dy;
+    wr(5) = dz;
     r.t_near = t_near;
     b.t = t_far;
     b.found = false;
-    b.inst = b.tri = 0;
-    b.u = b.v = 0.f;
-    b.slot = 0;
+    b.inst() = b.tri() = 0;
+    b.u() = b.v() = 0.f;
+    b.slot() = 0;
     inst = 0;
     if (n_inst == 0) return true;
     start_object(insts);

@@ -598,6 +598,7 @@ __global__ void k_cluster_map(const DevInst* __restrict__ inst, const uint32_t* 
 
 // Learned closest hit: the two predicted clusters first, then the whole
 // tree with their best hit as the starting best (exact).
+static_assert(128 <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
 __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict__ inst, const j3dg_ray* __restrict__ rays,
                                                       uint32_t n, const uint32_t* __restrict__ top2,
                                                       const uint32_t* __restrict__ roots, uint32_t n_roots,
@@ -633,9 +634,9 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
   j3dg_hit h;
   h.found = T.b.found ? 1u : 0u;
   h.distance = T.b.found ? T.b.t : f[9];
-  h.u = T.b.u;
-  h.v = T.b.v;
-  h.object_id = T.b.found ? T.b.tri : 0xffffffffu;
+  h.u = T.b.u();
+  h.v = T.b.v();
+  h.object_id = T.b.found ? T.b.tri() : 0xffffffffu;
   h.two_level_index = T.b.found ? 0u : 0xffffffffu;
   hits[i] = h;
   }

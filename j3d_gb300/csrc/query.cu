@@ -20,6 +20,10 @@
 
 namespace j3dg {
 
+// block size of the query kernels (they trace: at most J3DG_COLD_MAX threads)
+static const int kQueryThreads = 128;
+static_assert(kQueryThreads <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
+
 // Inserts (t, id, u, v) into the sorted buffer h[0..n) of capacity cap.
 // `extra` goes to two_level_index (the object, or a leaf slot internally).
 __device__ __forceinline__ void insert_sorted(j3dg_hit* h, uint32_t& n, uint32_t cap, float t, uint32_t id, float u,
@@ -68,7 +72,7 @@ __device__ bool all_hits(const DevInst& I, const Ray& r, float t_far, uint32_t* 
           Best b;
           b.t = t_far;
           b.found = false;
-          if (tri_test(r, I.tris, first + k, 0u, b, true)) on_hit(first + k, b.t, b.u, b.v);
+          if (tri_test(r, I.tris, first + k, 0u, b, true)) on_hit(first + k, b.t, b.u(), b.v());
         }
         cur = J3DG_EMPTY_REF;
       } else {
@@ -107,7 +111,7 @@ __device__ bool all_hits(const DevInst& I, const Ray& r, float t_far, uint32_t* 
   }
 }
 
-__global__ void k_find_all(const DevInst* __restrict__ inst, const j3dg_ray* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(kQueryThreads) k_find_all(const DevInst* __restrict__ inst, const j3dg_ray* __restrict__ rays, uint32_t n,
                            uint32_t cap, j3dg_hit* __restrict__ hits, uint32_t* __restrict__ counts,
                            uint32_t* status) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,7 +149,7 @@ __device__ __forceinline__ uint32_t vox_cell(float p, float lo, float hi, uint32
 
 static const uint32_t kVoxHits = 64;
 
-__global__ void k_voxelize(const DevInst* __restrict__ inst, VoxParams V, uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kQueryThreads) k_voxelize(const DevInst* __restrict__ inst, VoxParams V, uint32_t* __restrict__ keys,
                            uint32_t* status) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= V.rays_total) return;
@@ -230,7 +234,7 @@ __global__ void k_keys_to_voxels(const uint32_t* __restrict__ keys, uint8_t* __r
 cudaError_t launch_find_all(const DevInst* inst, const j3dg_ray* rays, uint32_t n, uint32_t cap, j3dg_hit* hits,
                             uint32_t* counts, uint32_t* status, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_find_all<<<(n + 127) / 128, 128, 0, st>>>(inst, rays, n, cap, hits, counts, status);
+  k_find_all<<<(n + kQueryThreads - 1) / kQueryThreads, kQueryThreads, 0, st>>>(inst, rays, n, cap, hits, counts, status);
   return cudaGetLastError();
 }
 
@@ -239,7 +243,7 @@ cudaError_t launch_voxelize(const DevInst* inst, const VoxParams& V, uint32_t* k
   const size_t total = (size_t)V.dim[0] * V.dim[1] * V.dim[2];
   cudaError_t e = cudaMemsetAsync(keys, 0, sizeof(uint32_t) * total, st);
   if (e != cudaSuccess) return e;
-  if (V.rays_total) k_voxelize<<<(V.rays_total + 127) / 128, 128, 0, st>>>(inst, V, keys, status);
+  if (V.rays_total) k_voxelize<<<(V.rays_total + kQueryThreads - 1) / kQueryThreads, kQueryThreads, 0, st>>>(inst, V, keys, status);
   k_keys_to_voxels<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(keys, out, total);
   return cudaGetLastError();
 }

@@ -122,8 +122,23 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 #ifndef J3DG_TRACE_THREADS
 #define J3DG_TRACE_THREADS 128
 #endif
+// blocks per SM the frame kernels are compiled for: 6 x 128 threads leave
+// 85 registers a thread, which the step's working set fits without spills
+// once the state read only at a pixel's start and finish is in shared
+// memory (J3DG_COLD_SMEM); latency-bound traversal gains from the extra warps
 #ifndef J3DG_TRACE_MINBLOCKS
-#define J3DG_TRACE_MINBLOCKS 5
+#define J3DG_TRACE_MINBLOCKS 6
+#endif
+// A frame (or batch) of fewer primary items than J3DG_THROUGHPUT_ITEMS runs
+// the latency build instead: 5 blocks per SM with the pixel state in
+// registers. Measured on single frames: below about one 1920x1080 frame the
+// extra warps of the throughput build lengthen the frame (a 512x512 frame
+// of the 28M-triangle torus 0.80 -> 0.89 ms); from there on they shorten it.
+#ifndef J3DG_LATENCY_MINBLOCKS
+#define J3DG_LATENCY_MINBLOCKS 5
+#endif
+#ifndef J3DG_THROUGHPUT_ITEMS
+#define J3DG_THROUGHPUT_ITEMS 2000000u
 #endif
 #ifndef J3DG_TRACE_ITERS
 #define J3DG_TRACE_ITERS 16
@@ -140,7 +155,27 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 #define J3DG_DEFER_FINISH 1
 #endif
 static const int kTraceThreads = J3DG_TRACE_THREADS;
+static_assert(kTraceThreads <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
 static const int kIters = J3DG_TRACE_ITERS;
+
+// Pixel and colour state of a lane: read only at a pixel's start and
+// finish. The throughput build keeps it in a per-block shared array
+// (J3DG_COLD_SMEM bit 4), the latency build in registers.
+struct PixState {
+  size_t pix;
+  uint32_t w0, frame;
+  float su, sv;
+};
+
+template <bool kShared, int N>
+__device__ __forceinline__ PixState& pix_state(PixState& local) {
+  if constexpr (kShared) {
+    __shared__ PixState s[N];
+    return s[threadIdx.x];
+  } else {
+    return local;
+  }
+}
 
 __device__ __forceinline__ uint32_t primary_count(const FrameParams& P) {
   const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
@@ -167,19 +202,19 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
     return false;
   }
   j3dg_pixel* rec = P.gbuf + pix;
-  const DevInst& I = P.inst[b.inst];
+  const DevInst& I = P.inst[b.inst()];
   // canvas.cpp:788-801
-  const float4 N = __ldg(I.normals + b.tri);
+  const float4 N = __ldg(I.normals + b.tri());
   float4 n = mat_vec(P.cs_inv, N.x, N.y, N.z, 0.f);
   n = mat_vec(I.cs, n.x, n.y, n.z, n.w);
   uint32_t mark = 0, pr = 0, pg = 0, pb = 0;
   bool rgb = false;
-  const float wgt = fs(fs(1.f, b.u), b.v);
+  const float wgt = fs(fs(1.f, b.u()), b.v());
   if (P.textured && I.uv != nullptr && I.tex != nullptr) {
     // canvas.cpp:803-820
-    const float* uv = I.uv + 6 * (size_t)b.tri;
-    float c0 = fa(fa(fm(wgt, uv[0]), fm(b.u, uv[2])), fm(b.v, uv[4]));
-    float c1 = fa(fa(fm(wgt, uv[1]), fm(b.u, uv[3])), fm(b.v, uv[5]));
+    const float* uv = I.uv + 6 * (size_t)b.tri();
+    float c0 = fa(fa(fm(wgt, uv[0]), fm(b.u(), uv[2])), fm(b.v(), uv[4]));
+    float c1 = fa(fa(fm(wgt, uv[1]), fm(b.u(), uv[3])), fm(b.v(), uv[5]));
     c0 = fmaxf(fminf(c0, 1.f), 0.f);
     c1 = fmaxf(fminf(c1, 1.f), 0.f);
     const int tw = (int)I.tex_w, th = (int)I.tex_h;
@@ -194,13 +229,13 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
     rgb = true;
   } else if (P.vertexcolors && I.colors != nullptr) {
     // canvas.cpp:821-834
-    const uint32_t* Ti = I.index + 3 * (size_t)b.tri;
+    const uint32_t* Ti = I.index + 3 * (size_t)b.tri();
     const float* C0 = I.colors + 3 * (size_t)Ti[0];
     const float* C1 = I.colors + 3 * (size_t)Ti[1];
     const float* C2 = I.colors + 3 * (size_t)Ti[2];
     float c[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u, C1[k])), fm(b.v, C2[k]));
+    for (int k = 0; k < 3; ++k) c[k] = fa(fa(fm(C0[k], wgt), fm(b.u(), C1[k])), fm(b.v(), C2[k]));
     pr = (uint8_t)fm(c[0], 255.f);
     pg = (uint8_t)fm(c[1], 255.f);
     pb = (uint8_t)fm(c[2], 255.f);
@@ -215,7 +250,7 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   rec->u = n.x;
   rec->v = n.y;
   rec->depth = b.t;
-  *reinterpret_cast<uint4*>(&rec->object_id) = make_uint4(b.tri, __float_as_uint(b.u), __float_as_uint(b.v), I.db_id);
+  *reinterpret_cast<uint4*>(&rec->object_id) = make_uint4(b.tri(), __float_as_uint(b.u()), __float_as_uint(b.v()), I.db_id);
   su = n.x;
   sv = n.y;
   if (!P.shadow) {
@@ -225,15 +260,15 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   // canvas.cpp:836-853: from the hit point towards the light
   const float ld = fm(P.diagonal, 3.f);
   const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
-  const float4 A = __ldg(I.tris + 3 * (size_t)b.slot);
-  const float4 B = __ldg(I.tris + 3 * (size_t)b.slot + 1);
-  const float4 C = __ldg(I.tris + 3 * (size_t)b.slot + 2);
+  const float4 A = __ldg(I.tris + 3 * (size_t)b.slot());
+  const float4 B = __ldg(I.tris + 3 * (size_t)b.slot() + 1);
+  const float4 C = __ldg(I.tris + 3 * (size_t)b.slot() + 2);
   const float4 V0 = mat_vec(I.cs, A.x, A.y, A.z, 1.f);
   const float4 V1 = mat_vec(I.cs, B.x, B.y, B.z, 1.f);
   const float4 V2 = mat_vec(I.cs, C.x, C.y, C.z, 1.f);
-  const float px = fa(fa(fm(V0.x, wgt), fm(b.u, V1.x)), fm(b.v, V2.x));
-  const float py = fa(fa(fm(V0.y, wgt), fm(b.u, V1.y)), fm(b.v, V2.y));
-  const float pz = fa(fa(fm(V0.z, wgt), fm(b.u, V1.z)), fm(b.v, V2.z));
+  const float px = fa(fa(fm(V0.x, wgt), fm(b.u(), V1.x)), fm(b.v(), V2.x));
+  const float py = fa(fa(fm(V0.y, wgt), fm(b.u(), V1.y)), fm(b.v(), V2.y));
+  const float pz = fa(fa(fm(V0.z, wgt), fm(b.u(), V1.z)), fm(b.v(), V2.z));
   T.begin(P.inst, P.n_inst, px, py, pz, fs(light.x, px), fs(light.y, py), fs(light.z, pz), 1e-3f, FLT_MAX, true);
   return true;
 }
@@ -249,16 +284,21 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
     P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
 }
 
-__global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_frame(const FrameParams P) {
+template <bool kThroughput>
+__global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
+    k_frame(const FrameParams P) {
   Tracer T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
   int phase = 0;  // 0 idle, 1 primary, 2 shadow, 3 / 4 primary / shadow finished (parked)
   bool exhausted = false;
-  size_t pix = 0;
-  uint32_t w0 = 0;
-  float su = 0.f, sv = 0.f;
+  PixState local;
+  PixState& ps = pix_state<kThroughput && (J3DG_COLD_SMEM & 4) != 0, kTraceThreads>(local);
+  ps = PixState{0, 0u, 0u, 0.f, 0.f};
+  size_t& pix = ps.pix;
+  uint32_t& w0 = ps.w0;
+  float &su = ps.su, &sv = ps.sv;
   uint32_t visits = 0, tests = 0;
 #pragma unroll 1
   for (;;) {
@@ -339,10 +379,10 @@ struct BatchSrc {
     j3dg_hit h;
     h.found = T.b.found ? 1u : 0u;
     h.distance = T.b.found ? T.b.t : t_far;
-    h.u = T.b.u;
-    h.v = T.b.v;
-    h.object_id = T.b.found ? T.b.tri : 0xffffffffu;
-    h.two_level_index = T.b.found ? T.b.inst : 0xffffffffu;
+    h.u = T.b.u();
+    h.v = T.b.v();
+    h.object_id = T.b.found ? T.b.tri() : 0xffffffffu;
+    h.two_level_index = T.b.found ? T.b.inst() : 0xffffffffu;
     hits[i] = h;
   }
 };
@@ -362,25 +402,30 @@ __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restric
 // refill from the one list, so small and large frames share the GPU with a
 // single tail. Per-frame parameters live in device memory.
 // blocks per SM that keep registers at or under ~96 for a block of TPB threads
-template <int TPB>
-struct MinBlocks {
-  static const int value = TPB >= 256 ? 2 : (TPB >= 128 ? 5 : 10);
+template <int TPB, bool kThroughput>
+struct MinBlocks {  // the same warps per SM as k_frame
+  static const int per128 = kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS;
+  static const int value = TPB >= 256 ? per128 / 2 : (TPB >= 128 ? per128 : 2 * per128);
 };
 
-template <int TPB>
-__global__ void __launch_bounds__(TPB, MinBlocks<TPB>::value)
+template <int TPB, bool kThroughput>
+__global__ void __launch_bounds__(TPB, (MinBlocks<TPB, kThroughput>::value))
     k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
                   uint32_t* work) {
+  static_assert(TPB <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
   Tracer T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t total = offsets[n_frames];
   int phase = 0;
   bool exhausted = false;
-  uint32_t frame = 0;
-  size_t pix = 0;
-  uint32_t w0 = 0;
-  float su = 0.f, sv = 0.f;
+  PixState local;
+  PixState& ps = pix_state<kThroughput && (J3DG_COLD_SMEM & 4) != 0, TPB>(local);
+  ps = PixState{0, 0u, 0u, 0.f, 0.f};
+  uint32_t& frame = ps.frame;
+  size_t& pix = ps.pix;
+  uint32_t& w0 = ps.w0;
+  float &su = ps.su, &sv = ps.sv;
   uint32_t visits = 0, tests = 0;
 #pragma unroll 1
   for (;;) {
@@ -601,32 +646,50 @@ __global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
   if (rw <= 0 || rh <= 0) return cudaSuccess;
-  static int blocks = 0;
-  if (!blocks) blocks = persistent_blocks(k_frame);
+  static int blocks_t = 0, blocks_l = 0;
+  if (!blocks_t) {
+    blocks_t = persistent_blocks(k_frame<true>);
+    blocks_l = persistent_blocks(k_frame<false>);
+  }
   cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  k_frame<<<blocks, kTraceThreads, 0, st>>>(P);
+  if (primary_items(P) >= J3DG_THROUGHPUT_ITEMS)
+    k_frame<true><<<blocks_t, kTraceThreads, 0, st>>>(P);
+  else
+    k_frame<false><<<blocks_l, kTraceThreads, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+template <bool kT>
+static cudaError_t launch_batch_variant(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
+                                        uint32_t* work, int block_threads, cudaStream_t st) {
+  static int b64 = 0, b128 = 0, b256 = 0;
+  if (!b64) {
+    b64 = persistent_blocks(k_frame_batch<64, kT>, 64);
+    b128 = persistent_blocks(k_frame_batch<128, kT>, 128);
+#if J3DG_COLD_MAX >= 256
+    b256 = persistent_blocks(k_frame_batch<256, kT>, 256);
+#endif
+  }
+  if (block_threads == 64)
+    k_frame_batch<64, kT><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
+#if J3DG_COLD_MAX >= 256
+  else if (block_threads == 256)
+    k_frame_batch<256, kT><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
+#endif
+  else
+    k_frame_batch<128, kT><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
   return cudaGetLastError();
 }
 
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t* work, int block_threads, cudaStream_t st) {
+                                uint32_t total_items, uint32_t* work, int block_threads, cudaStream_t st) {
   if (n_frames == 0) return cudaSuccess;
-  static int b64 = 0, b128 = 0, b256 = 0;
-  if (!b64) {
-    b64 = persistent_blocks(k_frame_batch<64>, 64);
-    b128 = persistent_blocks(k_frame_batch<128>, 128);
-    b256 = persistent_blocks(k_frame_batch<256>, 256);
-  }
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  if (block_threads == 64)
-    k_frame_batch<64><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
-  else if (block_threads == 256)
-    k_frame_batch<256><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
-  else
-    k_frame_batch<128><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
-  return cudaGetLastError();
+  return total_items >= J3DG_THROUGHPUT_ITEMS
+             ? launch_batch_variant<true>(d_params, d_offsets, n_frames, work, block_threads, st)
+             : launch_batch_variant<false>(d_params, d_offsets, n_frames, work, block_threads, st);
 }
 
 uint32_t primary_items(const FrameParams& P) {

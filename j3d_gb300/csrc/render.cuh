@@ -33,8 +33,9 @@ struct FrameParams {
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
 // all frames in one persistent launch; offsets = prefix sums of primary_items
+// total_items = offsets[n_frames] (the sum of primary_items of the frames)
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t* work, int block_threads, cudaStream_t st);
+                                uint32_t total_items, uint32_t* work, int block_threads, cudaStream_t st);
 uint32_t primary_items(const FrameParams& P);
 // mode: 0 plain, 1 edges, 2 wireframe, 3 one-bit
 cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st);

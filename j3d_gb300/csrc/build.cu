@@ -354,6 +354,7 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
   float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
   return dx * dy + dy * dz + dz * dx;
 }
+__device__ __forceinline__ float half_area4(float4 lo, float4 hi) { return half_area(lo, hi); }
 
 __global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __restrict__ box,
                            const uint2* __restrict__ range, const float4* __restrict__ tris,
@@ -547,6 +548,83 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
   hi2[pos] = h;
 }
 
+// ------------------------------------------- 6b. cost-optimal collapse ----
+//
+// SAH cost of covering the subtree of binary node n with at most i = 1..4
+// slots of a wide node (the dynamic programme of Ylitie, Karras and Laine
+// 2017, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs", section 3.1, for 4-wide nodes). A is half the surface area:
+//   C(tri, i) = A(tri) c_t
+//   C(n, 1)   = min(leaf: A(n) N(n) c_t if N(n) <= leaf_size,
+//                   node: A(n) c_n + min_k C(left, k) + C(right, 4 - k))
+//   C(n, i)   = min(C(n, i - 1), min_k C(left, k) + C(right, i - k))
+// Children are made in earlier PLOC rounds, so one launch per round, in
+// round order, sees its children's costs. The decisions steer the collapse:
+// dec.x = the k of the node case (bit 7 set: the leaf case is cheaper);
+// dec.y, .z, .w for i = 2, 3, 4: 0 = as i - 1, else the k of the best split.
+
+#ifndef J3DG_SAH_COLLAPSE
+#define J3DG_SAH_COLLAPSE 1
+#endif
+#ifndef J3DG_SAH_CTRI
+#define J3DG_SAH_CTRI 0.5f  // cost of a triangle test relative to a node visit
+#endif
+
+__device__ __forceinline__ float half_area4(float4 lo, float4 hi);
+
+__device__ __forceinline__ void sub_costs(const float4* __restrict__ cost, const float4* __restrict__ tris, uint32_t r,
+                                          float c[5]) {
+  if (r & 0x80000000u) {
+    float4 lo, hi;
+    leaf_box(tris, r & 0x7fffffffu, lo, hi);
+    c[1] = c[2] = c[3] = c[4] = half_area4(lo, hi) * J3DG_SAH_CTRI;
+  } else {
+    const float4 v = cost[r];
+    c[1] = v.x;
+    c[2] = v.y;
+    c[3] = v.z;
+    c[4] = v.w;
+  }
+}
+
+__global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                const uint32_t* __restrict__ count, const float4* __restrict__ tris, uint32_t lo,
+                                uint32_t hi, uint32_t leaf_size, float4* __restrict__ cost, uchar4* __restrict__ dec) {
+  const uint32_t n = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= hi) return;
+  const uint2 c = child[n];
+  float cl[5], cr[5], C[5];
+  sub_costs(cost, tris, c.x, cl);
+  sub_costs(cost, tris, c.y, cr);
+  const float A = half_area4(box[n].lo, box[n].hi);
+  float best = FLT_MAX;
+  uint32_t bk = 1;
+  for (uint32_t k = 1; k <= 3; ++k)
+    if (cl[k] + cr[4 - k] < best) {
+      best = cl[k] + cr[4 - k];
+      bk = k;
+    }
+  const float node = A + best;  // c_n = 1
+  const uint32_t N = count[n];
+  const float leaf = N <= leaf_size ? A * (float)N * J3DG_SAH_CTRI : FLT_MAX;
+  C[1] = fminf(leaf, node);
+  uint8_t d[4];
+  d[0] = (uint8_t)(bk | (leaf <= node ? 0x80u : 0u));
+  for (uint32_t i = 2; i <= 4; ++i) {
+    float v = C[i - 1];
+    uint32_t dk = 0;
+    for (uint32_t k = 1; k < i; ++k)
+      if (cl[k] + cr[i - k] < v) {
+        v = cl[k] + cr[i - k];
+        dk = k;
+      }
+    C[i] = v;
+    d[i - 1] = (uint8_t)dk;
+  }
+  cost[n] = make_float4(C[1], C[2], C[3], C[4]);
+  dec[n] = make_uchar4(d[0], d[1], d[2], d[3]);
+}
+
 struct PlaceItem {
   uint32_t bin;    // binary node index
   uint32_t wide;   // wide node index to fill
@@ -562,7 +640,7 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
                                  const PlaceItem* __restrict__ qin, uint32_t n_in, PlaceItem* __restrict__ qout,
                                  uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
                                  uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
-                                 uint32_t nt, uint32_t* status) {
+                                 uint32_t nt, uint32_t* status, const uchar4* __restrict__ dec) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_in) return;
   const PlaceItem it = qin[t];
@@ -581,10 +659,41 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     }
   };
   const uint2 c = child[it.bin];
-  load(c.x, 0, it.start);
-  load(c.y, 1, it.start + cnt[0]);
-  int m = 2;
-  while (m < 4) {
+  int m = 0;
+  if (dec) {
+    // the slots the cost decisions give: expand(left, k) then expand(right, 4 - k)
+    struct Slot {
+      uint32_t r, i, start;
+    };
+    Slot stk[8];
+    int sp = 0;
+    const uint32_t k = dec[it.bin].x & 0x7fu;
+    const uint32_t nl = (c.x & 0x80000000u) ? 1u : count[c.x];
+    stk[sp++] = Slot{c.y, 4u - k, it.start + nl};
+    stk[sp++] = Slot{c.x, k, it.start};
+    while (sp > 0 && m < 4) {
+      const Slot e = stk[--sp];
+      if ((e.r & 0x80000000u) || e.i <= 1u) {
+        load(e.r, m++, e.start);
+        continue;
+      }
+      const uchar4 dd = dec[e.r];
+      const uint32_t d = e.i == 2u ? dd.y : (e.i == 3u ? dd.z : dd.w);
+      if (d == 0u || sp + 2 > 8) {
+        stk[sp++] = Slot{e.r, e.i - 1u, e.start};
+        continue;
+      }
+      const uint2 cc = child[e.r];
+      const uint32_t ml = (cc.x & 0x80000000u) ? 1u : count[cc.x];
+      stk[sp++] = Slot{cc.y, e.i - d, e.start + ml};
+      stk[sp++] = Slot{cc.x, d, e.start};
+    }
+  } else {
+    load(c.x, 0, it.start);
+    load(c.y, 1, it.start + cnt[0]);
+    m = 2;
+  }
+  while (!dec && m < 4) {
     int best = -1;
     float ba = -1.f;
     for (int s = 0; s < m; ++s)
@@ -613,7 +722,8 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
       v[3][s] = hi[s].y;
       v[4][s] = lo[s].z;
       v[5][s] = hi[s].z;
-      if (cnt[s] <= leaf_size) {
+      const bool as_leaf = (ref[s] & 0x80000000u) || (dec ? (dec[ref[s]].x & 0x80u) != 0 : cnt[s] <= leaf_size);
+      if (as_leaf && cnt[s] <= J3DG_MAX_LEAF) {
         out_ref[s] = J3DG_LEAF_BIT | (start[s] << 3) | (cnt[s] - 1u);
         uint32_t stk[J3DG_MAX_LEAF];
         int sp = 0;
@@ -794,6 +904,9 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   uint32_t n_in = 0;
   CollapseItem root_item;
   std::vector<uint32_t> level_end(1, 1u);  // wide nodes of level L end at level_end[L]
+  std::vector<uint32_t> round_end;         // binary nodes of PLOC round r end at round_end[r]
+  float4* dp_cost = nullptr;
+  uchar4* dp_dec = nullptr;
 
   J3DG_CK(cudaMallocAsync((void**)&d_part, sizeof(float) * 6 * bbox_blocks, st));
   J3DG_CK(cudaMallocAsync((void**)&d_bb, sizeof(float) * 6, st));
@@ -887,6 +1000,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
                                                  child, box, count);
       J3DG_CK(cudaGetLastError());
       node_base += htot[0];
+      round_end.push_back(node_base);
       mcount = htot[1];
       std::swap(C0, C1);
       std::swap(lo0, lo1);
@@ -898,6 +1012,17 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       err = "PLOC clustering ended with a malformed tree";
       rc = J3DG_ERR_CUDA;
       goto cleanup;
+    }
+    if (J3DG_SAH_COLLAPSE) {
+      J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float4) * (nt - 1), st));
+      J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uchar4) * (nt - 1), st));
+      uint32_t lo_n = 0;
+      for (uint32_t hi_n : round_end) {
+        k_collapse_cost<<<(hi_n - lo_n + 255) / 256, 256, 0, st>>>(child, box, count, (const float4*)m->d_tris, lo_n,
+                                                                     hi_n, m->leaf_size, dp_cost, dp_dec);
+        lo_n = hi_n;
+      }
+      J3DG_CK(cudaGetLastError());
     }
     J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
     J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * 8 * (size_t)nt, st));
@@ -918,7 +1043,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
       k_collapse_place<<<(n_in + 127) / 128, 128, 0, st>>>(child, box, count, (const float4*)m->d_tris, pa, n_in, pb,
                                                           counters + 2, counters + 1, wide, m->leaf_size, counters + 3,
-                                                          tris_out, nt, d_status);
+                                                          tris_out, nt, d_status, dp_dec);
       J3DG_CK(cudaGetLastError());
       J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
       J3DG_CK(cudaStreamSynchronize(st));
@@ -1000,6 +1125,8 @@ cleanup:
   if (other) cudaFreeAsync(other, st);
   if (counters) cudaFreeAsync(counters, st);
   if (wide) cudaFreeAsync(wide, st);
+  if (dp_cost) cudaFreeAsync(dp_cost, st);
+  if (dp_dec) cudaFreeAsync(dp_dec, st);
   if (qa) cudaFreeAsync(qa, st);
   if (qb) cudaFreeAsync(qb, st);
   for (uint32_t* p : {C0, C1, nn, create, survive, cscan, sscan, pl_sums, count, tot})

@@ -267,16 +267,28 @@ def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod):
 
 
 def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod):
-    """28.09M-triangle torus at 1920x1080: GPU frame vs oracle on sampled rows;
-    every GPU hit record re-derived on the CPU (size-independent checks)."""
+    """28.09M-triangle torus at 1920x1080, the 32 cameras of the benchmark:
+    hit and shadowed pixels of every frame equal the oracle's full-frame
+    counts (tests/golden/traffic.json, made by make_traffic.py), and so does
+    the ray total; on two cameras the GPU frame equals the oracle's on
+    sampled rows, with size-independent checks of every hit record."""
     from j3d_gb300 import workloads as W
     O = oracle_mod
-    wl = W.config1(n_cameras=2)
+    wl = W.config1()
+    ref = json.loads((GOLDEN / "traffic.json").read_text())["config1"]
     mesh, sc = gpu_scene(gpu_ctx, wl.vertices, wl.triangles, wl.poses[0])
     info = mesh.info()
     assert info.n_triangles == 28_090_000 and info.n_vertices == 14_045_000
-    m, views, _ = oracle_scene(O, wl.vertices, wl.triangles, wl.poses, wl.width, wl.height)
-    for i, pose in enumerate(wl.poses):
+    hits, shadowed = [], []
+    for pose in wl.poses:
+        sc.set_pose(pose)
+        gp, _, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
+        hits.append(int((gp["object_id"] != NO_ID).sum()))
+        shadowed.append(int(((gp["mark"] & 1) != 0).sum()))
+    assert hits == ref["hit_pixels"] and shadowed == ref["shadowed_pixels"]
+    assert len(wl.poses) * wl.width * wl.height + sum(hits) == ref["rays"]
+    m, views, _ = oracle_scene(O, wl.vertices, wl.triangles, wl.poses[:2], wl.width, wl.height)
+    for i, pose in enumerate(wl.poses[:2]):
         sc.set_pose(pose)
         gp, gi, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
         rows = list(range(3, wl.height, 67))

@@ -9,13 +9,17 @@
 //      code over the vertex bbox
 //   3. LSD radix sort of (Morton, triangle id), 8-bit digits, stable
 //   4. leaf-ordered triangle array: 3 float4 per triangle (v0.w = id bits)
-//   5. binary tree: by default PLOC clustering over the sorted triangles
-//      (section 5b); with J3DG_BUILD_LBVH the LBVH, bottom-up in one pass
+//   5. binary tree: by default binned-SAH splits top-down down to ranges of
+//      at most J3DG_SAH_TOP triangles (section 5c), then PLOC clustering
+//      within each range (section 5b); with J3DG_BUILD_LBVH the LBVH,
+//      bottom-up in one pass
 //      (Apetrei 2014, "Fast and Simple Agglomerative LBVH Construction"),
 //      with a strict total order on the split keys (xor of neighbouring
 //      codes, then i ^ (i+1), then i)
-//   6. collapse to 4-wide nodes level by level: open the largest-area child
-//      until four children; subtrees of <= leaf_size triangles become leaves.
+//   6. collapse to 4-wide nodes level by level: slots and leaves chosen by
+//      the SAH cost programme of section 6b (LBVH: open the largest-area
+//      child until four children, subtrees of <= leaf_size triangles become
+//      leaves); then the wide nodes are numbered depth-first (section 7).
 // Child boxes are exact unions of triangle boxes, which the traversal's
 // topology-independence argument requires.
 #include <cuda_runtime.h>
@@ -470,15 +474,21 @@ __device__ __forceinline__ float merged_area(float4 alo, float4 ahi, float4 blo,
   return a == a ? a : FLT_MAX;  // boxes with NaN planes still get an order
 }
 
+// Clusters are searched within their own segment (seg: the segment of each
+// list position, all 0 for one segment); a cluster alone in its segment gets
+// no neighbour (0xffffffff) and so never merges.
 __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict__ lo, const float4* __restrict__ hi,
-                                                       uint32_t m, uint32_t* __restrict__ nn) {
+                                                       const uint32_t* __restrict__ seg, uint32_t m,
+                                                       uint32_t* __restrict__ nn) {
   __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+  __shared__ uint32_t sseg[kPlocBlock + 2 * kPlocRadius];
   const int base = (int)(blockIdx.x * kPlocBlock) - kPlocRadius;
   for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += blockDim.x) {
     const int j = base + k;
     if (j >= 0 && j < (int)m) {
       slo[k] = lo[j];
       shi[k] = hi[j];
+      sseg[k] = seg[j];
     }
   }
   __syncthreads();
@@ -486,18 +496,19 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict
   if (i >= (int)m) return;
   const int si = threadIdx.x + kPlocRadius;
   const float4 alo = slo[si], ahi = shi[si];
+  const uint32_t my = sseg[si];
   float best = INFINITY;
-  int bj = i == 0 ? 1 : i - 1;
+  uint32_t bj = 0xffffffffu;
   for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
     const int j = i + o;
-    if (o == 0 || j < 0 || j >= (int)m) continue;
+    if (o == 0 || j < 0 || j >= (int)m || sseg[si + o] != my) continue;
     const float a = merged_area(alo, ahi, slo[si + o], shi[si + o]);
     if (a < best) {  // increasing j: the first of equal areas is the smaller position
       best = a;
-      bj = j;
+      bj = (uint32_t)j;
     }
   }
-  nn[i] = (uint32_t)bj;
+  nn[i] = bj;
 }
 
 __global__ void k_ploc_flags(const uint32_t* __restrict__ nn, uint32_t m, uint32_t* __restrict__ create,
@@ -518,10 +529,11 @@ __global__ void k_ploc_totals(const uint32_t* create, const uint32_t* cscan, con
 }
 
 __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
-                             const float4* __restrict__ hi, const uint32_t* __restrict__ nn,
-                             const uint32_t* __restrict__ cscan, const uint32_t* __restrict__ sscan, uint32_t m,
-                             uint32_t node_base, uint32_t* __restrict__ C2, float4* __restrict__ lo2,
-                             float4* __restrict__ hi2, uint2* __restrict__ child, BinNode* __restrict__ box,
+                             const float4* __restrict__ hi, const uint32_t* __restrict__ seg,
+                             const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cscan,
+                             const uint32_t* __restrict__ sscan, uint32_t m, uint32_t node_base,
+                             uint32_t* __restrict__ C2, float4* __restrict__ lo2, float4* __restrict__ hi2,
+                             uint32_t* __restrict__ seg2, uint2* __restrict__ child, BinNode* __restrict__ box,
                              uint32_t* __restrict__ count) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
@@ -529,6 +541,7 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
   const bool mutual = j < m && nn[j] == i;
   if (mutual && i > j) return;  // merged into the node made at j
   const uint32_t pos = sscan[i];
+  seg2[pos] = seg[i];
   if (!mutual) {
     C2[pos] = C[i];
     lo2[pos] = lo[i];
@@ -863,6 +876,410 @@ static cudaError_t dfs_order(const float4* wide, uint32_t n, const std::vector<u
   return e;
 }
 
+// -------------------------------------------------- 5c. SAH top levels ----
+//
+// Above J3DG_SAH_TOP triangles a node is split top-down by binned SAH (Wald
+// 2007, "On fast Construction of SAH-based Bounding Volume Hierarchies"):
+// per level, every task (a range of the triangle order `ord`) bins its
+// triangles' centroids into kTopBins bins per axis (per-block bins in shared
+// memory, then merged into the task's bins), one thread per task sweeps the
+// bins for the split of least A_L N_L + A_R N_R, and a stable partition
+// (flags, one exclusive scan) reorders the range. A stable partition of the
+// Morton-sorted order keeps every range in Morton order, so each range of at
+// most J3DG_SAH_TOP triangles (a segment) is then clustered by PLOC on its
+// own (neighbours searched within the segment only), and the segment roots
+// are linked under the top nodes.
+
+// segment size below which PLOC takes over (0: PLOC over the whole mesh).
+// Measured on the 28M-triangle torus frames (node visits per ray, ms per
+// 1080p frame, build ms): PLOC only 6.955 / 0.881 / 39; 4096: 6.402 / 0.862
+// / 67; 256: 6.256 / 0.855 / 76; 64: 6.200 / 0.851 / 87; 16: 6.193 / 0.852
+// / 112.
+#ifndef J3DG_SAH_TOP
+#define J3DG_SAH_TOP 64u
+#endif
+static const int kTopBins = 16;
+static const int kTopVals = 13;  // count, centroid lo/hi xyz, box lo/hi xyz (ordered-float encoded)
+static const uint32_t kNoTask = 0xffffffffu;
+static const uint32_t kPendingRef = 0xfffffffeu;  // child slot filled by a segment root later
+
+struct TopTask {
+  uint32_t begin, end, node, pad;
+  float4 clo, chi;  // centroid bounds
+};
+
+struct TopSplit {
+  uint32_t axis;   // 3: split by position (no usable SAH split)
+  uint32_t bin;    // bins 0..bin go left
+  uint32_t nleft;
+  uint32_t pad;
+  uint32_t task[2];  // the children's tasks of the next level (kNoTask: a finished range)
+  uint32_t pad2[2];
+  float4 lclo, lchi, rclo, rchi;  // children's centroid bounds
+};
+
+// triangle boxes by triangle, computed once for the top levels
+__global__ void k_top_boxes(const float4* __restrict__ tris, uint32_t n, float4* __restrict__ blo,
+                            float4* __restrict__ bhi) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) leaf_box(tris, i, blo[i], bhi[i]);
+}
+
+struct TopRange {  // a finished range: a segment for PLOC
+  uint32_t begin, end, parent, side;
+};
+
+// float <-> uint32 with the same order (for atomic min / max)
+__device__ __forceinline__ uint32_t f2o(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t o) { return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o); }
+
+__device__ __forceinline__ int top_bin(float c, float lo, float hi) {
+  const float ext = hi - lo;
+  if (!(ext > 0.f)) return 0;
+  const int b = (int)((c - lo) / ext * (float)kTopBins);
+  return b < 0 ? 0 : (b >= kTopBins ? kTopBins - 1 : b);
+}
+
+__global__ void k_top_bins_init(uint32_t* __restrict__ bins, uint32_t n_words) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_words) return;
+  const uint32_t v = i % kTopVals;
+  bins[i] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);  // lo fields: max code, hi fields: 0
+}
+
+static const int kTopChunk = 2048;
+
+// bins of every active task: [task][axis][bin][kTopVals]
+__global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
+                                                 const float4* __restrict__ bhi, const uint32_t* __restrict__ task_of,
+                                                 const TopTask* __restrict__ tasks, uint32_t n_tasks, uint32_t n,
+                                                 uint32_t* __restrict__ bins) {
+  __shared__ uint32_t sb[3 * kTopBins * kTopVals];
+  __shared__ uint32_t s_task;
+  const uint32_t c0 = blockIdx.x * kTopChunk, c1 = min(n, c0 + kTopChunk);
+  if (c0 >= n) return;
+  if (threadIdx.x == 0) {
+    const uint32_t a = task_of[c0], b = task_of[c1 - 1];
+    s_task = (a == b && a < n_tasks) ? a : kNoTask;
+  }
+  for (uint32_t k = threadIdx.x; k < 3 * kTopBins * kTopVals; k += blockDim.x) {
+    const uint32_t v = k % kTopVals;
+    sb[k] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);
+  }
+  __syncthreads();
+  const uint32_t st = s_task;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = c0; base < c1; base += blockDim.x) {  // uniform trip count: whole warps
+    const uint32_t p = base + threadIdx.x;
+    const uint32_t t = p < c1 ? (st != kNoTask ? st : task_of[p]) : kNoTask;
+    const bool valid = t < n_tasks;
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo, c = lo;
+    int bx = 0, by = 0, bz = 0;
+    if (valid) {
+      const uint32_t tri = ord[p];
+      lo = blo[tri];
+      hi = bhi[tri];
+      c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
+      const TopTask T = tasks[t];
+      bx = top_bin(c.x, T.clo.x, T.chi.x);
+      by = top_bin(c.y, T.clo.y, T.chi.y);
+      bz = top_bin(c.z, T.clo.z, T.chi.z);
+    }
+    // neighbouring triangles (Morton order) mostly share a task and bins:
+    // lanes of one (task, bin) reduce in registers and one lane updates the
+    // bin -- in shared memory when the whole chunk is one task, else in the
+    // task's global bins
+    const uint32_t vm = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      const uint32_t v[12] = {f2o(c.x),  f2o(c.y),  f2o(c.z),  f2o(c.x),  f2o(c.y),  f2o(c.z),
+                              f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+      const int bins3[3] = {bx, by, bz};
+      uint32_t* dst = st != kNoTask ? sb : bins + (size_t)t * 3 * kTopBins * kTopVals;
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        const uint32_t g = __match_any_sync(vm, t * (uint32_t)kTopBins + (uint32_t)bins3[ax]);
+        const uint32_t n_g = (uint32_t)__popc(g);
+        uint32_t r[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) r[k] = ((k % 6) < 3) ? __reduce_min_sync(g, v[k]) : __reduce_max_sync(g, v[k]);
+        if (lane == (uint32_t)(__ffs(g) - 1)) {
+          uint32_t* b = dst + (ax * kTopBins + bins3[ax]) * kTopVals;
+          atomicAdd(b, n_g);
+#pragma unroll
+          for (int k = 0; k < 12; ++k) {
+            if ((k % 6) < 3)
+              atomicMin(b + 1 + k, r[k]);
+            else
+              atomicMax(b + 1 + k, r[k]);
+          }
+        }
+      }
+    }
+  }
+  if (st == kNoTask) return;
+  __syncthreads();
+  uint32_t* g = bins + (size_t)st * 3 * kTopBins * kTopVals;
+  for (uint32_t k = threadIdx.x; k < 3 * kTopBins * kTopVals; k += blockDim.x) {
+    const uint32_t v = k % kTopVals;
+    if (v == 0) {
+      if (sb[k]) atomicAdd(g + k, sb[k]);
+    } else if (((v - 1) % 6) < 3) {
+      atomicMin(g + k, sb[k]);
+    } else {
+      atomicMax(g + k, sb[k]);
+    }
+  }
+}
+
+__device__ __forceinline__ float box_half_area(float lx, float ly, float lz, float hx, float hy, float hz) {
+  const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// one thread per task: the split of least SAH cost; writes the node's box and count
+__global__ void k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks, const uint32_t* __restrict__ bins,
+                            TopSplit* __restrict__ splits, BinNode* __restrict__ box, uint32_t* __restrict__ count) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tasks) return;
+  const TopTask T = tasks[t];
+  const uint32_t* B = bins + (size_t)t * 3 * kTopBins * kTopVals;
+  const uint32_t n = T.end - T.begin;
+  float best = FLT_MAX;
+  uint32_t ba = 3, bb = 0, bl = n / 2;
+  float nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int ax = 0; ax < 3; ++ax) {
+    const uint32_t* A = B + ax * kTopBins * kTopVals;
+    float ra[kTopBins];  // area of bins b..15
+    uint32_t rn[kTopBins];
+    float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t cnt = 0;
+    for (int b = kTopBins - 1; b >= 0; --b) {
+      const uint32_t* V = A + b * kTopVals;
+      if (V[0]) {
+        for (int k = 0; k < 3; ++k) {
+          l[k] = fminf(l[k], o2f(V[7 + k]));
+          h[k] = fmaxf(h[k], o2f(V[10 + k]));
+        }
+        cnt += V[0];
+      }
+      ra[b] = cnt ? box_half_area(l[0], l[1], l[2], h[0], h[1], h[2]) : 0.f;
+      rn[b] = cnt;
+    }
+    if (ax == 0)
+      for (int k = 0; k < 3; ++k) {
+        nlo[k] = l[k];
+        nhi[k] = h[k];
+      }
+    float L[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, H[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    uint32_t lc = 0;
+    for (int b = 0; b + 1 < kTopBins; ++b) {
+      const uint32_t* V = A + b * kTopVals;
+      if (V[0]) {
+        for (int k = 0; k < 3; ++k) {
+          L[k] = fminf(L[k], o2f(V[7 + k]));
+          H[k] = fmaxf(H[k], o2f(V[10 + k]));
+        }
+        lc += V[0];
+      }
+      const uint32_t rc = rn[b + 1];
+      if (lc == 0 || rc == 0) continue;
+      const float cost = box_half_area(L[0], L[1], L[2], H[0], H[1], H[2]) * (float)lc + ra[b + 1] * (float)rc;
+      if (cost < best) {
+        best = cost;
+        ba = (uint32_t)ax;
+        bb = (uint32_t)b;
+        bl = lc;
+      }
+    }
+  }
+  TopSplit S;
+  S.axis = ba;
+  S.bin = bb;
+  S.nleft = bl;
+  S.pad = 0;
+  S.lclo = S.rclo = T.clo;
+  S.lchi = S.rchi = T.chi;
+  if (ba < 3) {  // exact centroid bounds of both sides from the split axis's bins
+    const uint32_t* A = B + ba * kTopBins * kTopVals;
+    float l0[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h0[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float l1[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h1[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int b = 0; b < kTopBins; ++b) {
+      const uint32_t* V = A + b * kTopVals;
+      if (!V[0]) continue;
+      float* lo = b <= (int)bb ? l0 : l1;
+      float* hi = b <= (int)bb ? h0 : h1;
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = fminf(lo[k], o2f(V[1 + k]));
+        hi[k] = fmaxf(hi[k], o2f(V[4 + k]));
+      }
+    }
+    S.lclo = make_float4(l0[0], l0[1], l0[2], 0.f);
+    S.lchi = make_float4(h0[0], h0[1], h0[2], 0.f);
+    S.rclo = make_float4(l1[0], l1[1], l1[2], 0.f);
+    S.rchi = make_float4(h1[0], h1[1], h1[2], 0.f);
+  }
+  splits[t] = S;
+  box[T.node].lo = make_float4(nlo[0], nlo[1], nlo[2], 0.f);
+  box[T.node].hi = make_float4(nhi[0], nhi[1], nhi[2], 0.f);
+  count[T.node] = n;
+}
+
+// flags[p] = 1 if position p of an active task goes left
+__global__ void k_top_flags(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
+                            const float4* __restrict__ bhi, const uint32_t* __restrict__ task_of,
+                            const TopTask* __restrict__ tasks, const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                            uint32_t n, uint32_t* __restrict__ flags) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t t = task_of[p];
+  uint32_t f = 0;
+  if (t < n_tasks) {
+    const TopSplit S = splits[t];
+    const TopTask T = tasks[t];
+    if (S.axis < 3) {
+      const uint32_t tri = ord[p];
+      const float4 lo = blo[tri], hi = bhi[tri];
+      const float c = S.axis == 0 ? 0.5f * (lo.x + hi.x) : (S.axis == 1 ? 0.5f * (lo.y + hi.y) : 0.5f * (lo.z + hi.z));
+      const float clo = S.axis == 0 ? T.clo.x : (S.axis == 1 ? T.clo.y : T.clo.z);
+      const float chi = S.axis == 0 ? T.chi.x : (S.axis == 1 ? T.chi.y : T.chi.z);
+      f = top_bin(c, clo, chi) <= (int)S.bin ? 1u : 0u;
+    } else {
+      f = (p - T.begin) < S.nleft ? 1u : 0u;
+    }
+  }
+  flags[p] = f;
+}
+
+// stable partition of every active task's range (scan = exclusive scan of flags)
+// stable partition of every active task's range (scan = exclusive scan of
+// flags); task_of2 gets each position's task of the next level
+__global__ void k_top_scatter(const uint32_t* __restrict__ ord, uint32_t* __restrict__ ord2,
+                              const uint32_t* __restrict__ task_of, uint32_t* __restrict__ task_of2,
+                              const TopTask* __restrict__ tasks, const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                              const uint32_t* __restrict__ flags, const uint32_t* __restrict__ scan, uint32_t n,
+                              uint32_t* status) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t t = task_of[p];
+  uint32_t d = p, next = kNoTask;
+  if (t < n_tasks) {
+    const TopTask T = tasks[t];
+    const TopSplit S = splits[t];
+    const uint32_t l = scan[p] - scan[T.begin];  // lefts before p within the task
+    d = flags[p] ? T.begin + l : T.begin + S.nleft + (p - T.begin - l);
+    next = S.task[flags[p] ? 0 : 1];
+    if (d < T.begin || d >= T.end) {
+      atomicOr(status, J3DG_DEV_BAD_INDEX);
+      return;
+    }
+  }
+  ord2[d] = ord[p];
+  task_of2[d] = next;
+}
+
+// children of every task: a new task above J3DG_SAH_TOP triangles, else a
+// finished range (segment) whose root PLOC supplies later
+__global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __restrict__ splits,
+                               uint32_t n_tasks, uint32_t seg_max, uint32_t* __restrict__ counters,
+                               TopTask* __restrict__ next, TopRange* __restrict__ ranges, uint2* __restrict__ child,
+                               uint32_t cap_tasks, uint32_t cap_ranges, uint32_t max_nodes, uint32_t* status) {
+  // counters: [0] nodes allocated, [1] next tasks, [2] ranges
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tasks) return;
+  const TopTask T = tasks[t];
+  TopSplit S = splits[t];
+  const uint32_t n = T.end - T.begin;
+  uint32_t nl = S.nleft;
+  if (nl == 0 || nl >= n) {  // cannot happen (both sides of a split are non-empty); kept safe
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    nl = n / 2;
+    S.axis = 3;
+    S.nleft = nl;
+  }
+  const uint32_t mid = T.begin + nl;
+  uint32_t ref[2];
+  S.task[0] = S.task[1] = kNoTask;
+  for (int side = 0; side < 2; ++side) {
+    const uint32_t b = side ? mid : T.begin, e = side ? T.end : mid;
+    if (e - b > seg_max) {
+      const uint32_t q = atomicAdd(counters + 1, 1u);
+      const uint32_t node = atomicAdd(counters + 0, 1u);
+      if (q >= cap_tasks || node >= max_nodes) {
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+        ref[side] = kPendingRef;
+        continue;
+      }
+      TopTask C;
+      C.begin = b;
+      C.end = e;
+      C.node = node;
+      C.pad = 0;
+      C.clo = side ? S.rclo : S.lclo;
+      C.chi = side ? S.rchi : S.lchi;
+      next[q] = C;
+      ref[side] = node;
+      S.task[side] = q;
+    } else {
+      const uint32_t q = atomicAdd(counters + 2, 1u);
+      if (q < cap_ranges)
+        ranges[q] = TopRange{b, e, T.node, (uint32_t)side};
+      else
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+      ref[side] = kPendingRef;
+    }
+  }
+  child[T.node] = make_uint2(ref[0], ref[1]);
+  splits[t] = S;
+}
+
+__global__ void k_iota(uint32_t* __restrict__ a, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = i;
+}
+
+// segment starts: flags[begin] = 1 for every finished range
+__global__ void k_top_seg_starts(const TopRange* __restrict__ ranges, uint32_t n_ranges, uint32_t n,
+                                 uint32_t* __restrict__ flags) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n_ranges && ranges[r].begin < n) flags[ranges[r].begin] = 1u;
+}
+
+// PLOC's initial clusters in the order `ord`, with the segment of each position
+// (seg = inclusive scan of the starts - 1)
+__global__ void k_ploc_init_seg(const float4* __restrict__ tris, const uint32_t* __restrict__ ord, uint32_t n,
+                                const uint32_t* __restrict__ starts, const uint32_t* __restrict__ scan,
+                                uint32_t* __restrict__ C, float4* __restrict__ lo, float4* __restrict__ hi,
+                                uint32_t* __restrict__ seg) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t t = ord[i];
+  C[i] = 0x80000000u | t;
+  leaf_box(tris, t, lo[i], hi[i]);
+  seg[i] = scan[i] + starts[i] - 1u;
+}
+
+// the root of segment s (its one cluster left, at list position s) fills the
+// child slot of the top node that made the segment
+__global__ void k_top_link(const TopRange* __restrict__ ranges, uint32_t n_ranges, const uint32_t* __restrict__ starts,
+                           const uint32_t* __restrict__ scan, const uint32_t* __restrict__ C, uint32_t n_seg,
+                           uint2* __restrict__ child, uint32_t* status) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_ranges) return;
+  const TopRange R = ranges[r];
+  const uint32_t s = scan[R.begin] + starts[R.begin] - 1u;
+  if (s >= n_seg) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    return;
+  }
+  if (R.side)
+    child[R.parent].y = C[s];
+  else
+    child[R.parent].x = C[s];
+}
+
 // ------------------------------------------------------------- driver ----
 
 #define J3DG_CK(x)                                             \
@@ -895,6 +1312,16 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
            *sscan = nullptr, *pl_sums = nullptr, *count = nullptr, *tot = nullptr;
   float4 *lo0 = nullptr, *hi0 = nullptr, *lo1 = nullptr, *hi1 = nullptr, *tris_out = nullptr;
   PlaceItem *pa = nullptr, *pb = nullptr;
+  // SAH top levels
+  uint32_t *ord_a = nullptr, *ord_b = nullptr, *task_of = nullptr, *task_of2 = nullptr, *seg0 = nullptr,
+           *seg1 = nullptr, *seg_starts = nullptr, *seg_scan = nullptr, *top_bins = nullptr, *top_ctr = nullptr;
+  float4 *tbox_lo = nullptr, *tbox_hi = nullptr;
+  TopTask *tasks_a = nullptr, *tasks_b = nullptr;
+  TopSplit* splits = nullptr;
+  TopRange* ranges = nullptr;
+  std::vector<uint32_t> top_end;  // top nodes of level L end at top_end[L]
+  uint32_t n_top = 0, n_ranges = 0, n_seg = 1, hctr[3] = {0, 0, 0};
+  bool top = false;
   const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
   const uint32_t hist_n = 256 * n_tiles;
   const uint32_t scan_blocks = (hist_n + 1023) / 1024;
@@ -975,11 +1402,100 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_CK(cudaMallocAsync((void**)&hi0, sizeof(float4) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&lo1, sizeof(float4) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&hi1, sizeof(float4) * nt, st));
-    k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, C0, lo0, hi0);
+    J3DG_CK(cudaMallocAsync((void**)&seg0, sizeof(uint32_t) * nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&seg1, sizeof(uint32_t) * nt, st));
+    // exclusive scan of n words (n <= nt)
+    const auto scan_u32 = [&](const uint32_t* in, uint32_t* out, uint32_t n) {
+      const uint32_t sb = (n + 1023) / 1024;
+      k_scan_chunks<<<sb, 1024, 0, st>>>(in, out, n, pl_sums);
+      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
+      k_scan_add<<<sb, 1024, 0, st>>>(out, n, pl_sums);
+    };
+    top = J3DG_SAH_TOP > 0 && nt > J3DG_SAH_TOP;
+    if (top) {
+      const uint32_t cap_tasks = nt / J3DG_SAH_TOP + 1;  // tasks of one level are disjoint, each > J3DG_SAH_TOP
+      const size_t bin_words = (size_t)cap_tasks * 3 * kTopBins * kTopVals;
+      J3DG_CK(cudaMallocAsync((void**)&ord_a, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&ord_b, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&task_of, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&task_of2, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&tbox_lo, sizeof(float4) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&tbox_hi, sizeof(float4) * nt, st));
+      k_top_boxes<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, tbox_lo, tbox_hi);
+      J3DG_CK(cudaMallocAsync((void**)&seg_starts, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&seg_scan, sizeof(uint32_t) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&top_bins, sizeof(uint32_t) * bin_words, st));
+      J3DG_CK(cudaMallocAsync((void**)&top_ctr, sizeof(uint32_t) * 3, st));
+      J3DG_CK(cudaMallocAsync((void**)&tasks_a, sizeof(TopTask) * cap_tasks, st));
+      J3DG_CK(cudaMallocAsync((void**)&tasks_b, sizeof(TopTask) * cap_tasks, st));
+      J3DG_CK(cudaMallocAsync((void**)&splits, sizeof(TopSplit) * cap_tasks, st));
+      J3DG_CK(cudaMallocAsync((void**)&ranges, sizeof(TopRange) * nt, st));  // at most one range per triangle
+      {
+        TopTask r0;
+        r0.begin = 0;
+        r0.end = nt;
+        r0.node = 0;
+        r0.pad = 0;
+        r0.clo = make_float4(hbb[0], hbb[1], hbb[2], 0.f);  // the vertex bbox holds every centroid
+        r0.chi = make_float4(hbb[3], hbb[4], hbb[5], 0.f);
+        J3DG_CK(cudaMemcpyAsync(tasks_a, &r0, sizeof(r0), cudaMemcpyHostToDevice, st));
+      }
+      hctr[0] = 1u;  // nodes allocated (the root)
+      hctr[1] = hctr[2] = 0u;
+      J3DG_CK(cudaMemcpyAsync(top_ctr, hctr, sizeof(hctr), cudaMemcpyHostToDevice, st));
+      k_iota<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, nt);
+      J3DG_CK(cudaMemsetAsync(task_of, 0, sizeof(uint32_t) * nt, st));
+      top_end.push_back(1u);
+      uint32_t n_tasks = 1;
+      while (n_tasks > 0) {
+        const uint32_t words = n_tasks * 3 * kTopBins * kTopVals;
+        k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words);
+        k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
+                                                                     n_tasks, nt, top_bins);
+        k_top_split<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
+        J3DG_CK(cudaMemsetAsync(top_ctr + 1, 0, sizeof(uint32_t), st));
+        k_top_children<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, splits, n_tasks, J3DG_SAH_TOP, top_ctr,
+                                                               tasks_b, ranges, child, cap_tasks, nt, nt - 1,
+                                                               d_status);
+        k_top_flags<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a, splits, n_tasks, nt,
+                                                      create);
+        scan_u32(create, cscan, nt);
+        k_top_scatter<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, tasks_a, splits, n_tasks,
+                                                        create, cscan, nt, d_status);
+        std::swap(ord_a, ord_b);
+        std::swap(task_of, task_of2);
+        J3DG_CK(cudaGetLastError());
+        J3DG_CK(cudaMemcpyAsync(hctr, top_ctr, sizeof(hctr), cudaMemcpyDeviceToHost, st));
+        J3DG_CK(cudaStreamSynchronize(st));
+        if (hctr[1] > cap_tasks || hctr[2] > nt || hctr[0] > nt - 1 || ++iters > 100000) {
+          err = "SAH top levels overran their bounds";
+          rc = J3DG_ERR_CUDA;
+          goto cleanup;
+        }
+        n_tasks = hctr[1];
+        if (hctr[0] > top_end.back()) top_end.push_back(hctr[0]);
+        std::swap(tasks_a, tasks_b);
+      }
+      iters = 0;
+      n_top = hctr[0];
+      n_ranges = hctr[2];
+      node_base = n_top;
+      // segments numbered in position order: a flag at each range's start, one scan
+      J3DG_CK(cudaMemsetAsync(seg_starts, 0, sizeof(uint32_t) * nt, st));
+      k_top_seg_starts<<<(n_ranges + 255) / 256, 256, 0, st>>>(ranges, n_ranges, nt, seg_starts);
+      scan_u32(seg_starts, seg_scan, nt);
+      k_ploc_init_seg<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, ord_a, nt, seg_starts, seg_scan, C0,
+                                                        lo0, hi0, seg0);
+      n_seg = n_ranges;
+    } else {
+      k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, C0, lo0, hi0);
+      J3DG_CK(cudaMemsetAsync(seg0, 0, sizeof(uint32_t) * nt, st));
+      n_seg = 1;
+    }
     J3DG_CK(cudaGetLastError());
-    while (mcount > 1) {
+    while (mcount > n_seg) {
       const uint32_t blocks = (mcount + kPlocBlock - 1) / kPlocBlock, sb = (mcount + 1023) / 1024;
-      k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, mcount, nn);
+      k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, seg0, mcount, nn);
       k_ploc_flags<<<blocks, kPlocBlock, 0, st>>>(nn, mcount, create, survive);
       k_scan_chunks<<<sb, 1024, 0, st>>>(create, cscan, mcount, pl_sums);
       k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
@@ -996,8 +1512,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
         rc = J3DG_ERR_CUDA;
         goto cleanup;
       }
-      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, nn, cscan, sscan, mcount, node_base, C1, lo1, hi1,
-                                                 child, box, count);
+      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, seg0, nn, cscan, sscan, mcount, node_base, C1, lo1,
+                                                 hi1, seg1, child, box, count);
       J3DG_CK(cudaGetLastError());
       node_base += htot[0];
       round_end.push_back(node_base);
@@ -1005,8 +1521,16 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       std::swap(C0, C1);
       std::swap(lo0, lo1);
       std::swap(hi0, hi1);
+      std::swap(seg0, seg1);
     }
-    J3DG_CK(cudaMemcpyAsync(&root, C0, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (top) {
+      k_top_link<<<(n_ranges + 255) / 256, 256, 0, st>>>(ranges, n_ranges, seg_starts, seg_scan, C0, n_seg, child,
+                                                         d_status);
+      J3DG_CK(cudaGetLastError());
+      root = 0;
+    } else {
+      J3DG_CK(cudaMemcpyAsync(&root, C0, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    }
     J3DG_CK(cudaStreamSynchronize(st));
     if (node_base != nt - 1 || (root & 0x80000000u)) {
       err = "PLOC clustering ended with a malformed tree";
@@ -1016,11 +1540,17 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     if (J3DG_SAH_COLLAPSE) {
       J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float4) * (nt - 1), st));
       J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uchar4) * (nt - 1), st));
-      uint32_t lo_n = 0;
+      // children before parents: the PLOC rounds in order, then the top levels deepest first
+      uint32_t lo_n = n_top;
       for (uint32_t hi_n : round_end) {
         k_collapse_cost<<<(hi_n - lo_n + 255) / 256, 256, 0, st>>>(child, box, count, (const float4*)m->d_tris, lo_n,
                                                                      hi_n, m->leaf_size, dp_cost, dp_dec);
         lo_n = hi_n;
+      }
+      for (size_t k = top_end.size(); k-- > 0;) {
+        const uint32_t lo_t = k ? top_end[k - 1] : 0u, hi_t = top_end[k];
+        k_collapse_cost<<<(hi_t - lo_t + 255) / 256, 256, 0, st>>>(child, box, count, (const float4*)m->d_tris, lo_t,
+                                                                     hi_t, m->leaf_size, dp_cost, dp_dec);
       }
       J3DG_CK(cudaGetLastError());
     }
@@ -1126,6 +1656,14 @@ cleanup:
   if (counters) cudaFreeAsync(counters, st);
   if (wide) cudaFreeAsync(wide, st);
   if (dp_cost) cudaFreeAsync(dp_cost, st);
+  for (uint32_t* q : {ord_a, ord_b, task_of, task_of2, seg0, seg1, seg_starts, seg_scan, top_bins, top_ctr})
+    if (q) cudaFreeAsync(q, st);
+  if (tbox_lo) cudaFreeAsync(tbox_lo, st);
+  if (tbox_hi) cudaFreeAsync(tbox_hi, st);
+  if (tasks_a) cudaFreeAsync(tasks_a, st);
+  if (tasks_b) cudaFreeAsync(tasks_b, st);
+  if (splits) cudaFreeAsync(splits, st);
+  if (ranges) cudaFreeAsync(ranges, st);
   if (dp_dec) cudaFreeAsync(dp_dec, st);
   if (qa) cudaFreeAsync(qa, st);
   if (qb) cudaFreeAsync(qb, st);

@@ -38,11 +38,12 @@ RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
 # (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
 # --warmup 3 --no-cpu [--build lbvh]`), per BVH builder:
-#   ploc: reads 438.1 MB, writes 71.6 MB, L2 2090.9 MB (cost-optimal
-#         collapse, depth-first node order, parked finishes, 6 blocks per SM)
+#   ploc: reads 427.9 MB, writes 70.2 MB, L2 1916.3 MB (SAH top levels +
+#         PLOC below 64 triangles, cost-optimal collapse, depth-first node
+#         order, parked finishes, 6 blocks per SM)
 #   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB (level-order nodes,
 #         finishes in the tracing loop, 5 blocks per SM)
-FRAME_TRAFFIC = {"ploc": (438_078_680 + 71_556_024, 2_090_921_728),
+FRAME_TRAFFIC = {"ploc": (427_900_360 + 70_153_648, 1_916_251_470),
                  "lbvh": (463_159_392 + 70_692_880, 1_837_113_990)}
 
 

@@ -57,6 +57,10 @@ __device__ __forceinline__ float4 mat_vec(const float* m, float x, float y, floa
   return make_float4(r[0], r[1], r[2], r[3]);
 }
 
+#ifndef J3DG_PREFETCH
+#define J3DG_PREFETCH 1
+#endif
+
 // three-input min / max (one instruction each on sm_100 and later); min and
 // max are exact, so the grouping does not change any value
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -380,6 +384,18 @@ struct Tracer {
           ++sp;
         }
       cur = rc[0];
+#if J3DG_PREFETCH
+      // the next step starts with this child: its line is requested now, so
+      // the fetch runs while the warp finishes the other lanes' branches
+      if (cur != J3DG_EMPTY_REF) {
+        const bool leaf = (cur & J3DG_LEAF_BIT) != 0;
+        const uint32_t first = (cur & 0x7fffffffu) >> 3;
+        if (leaf ? first < nt : cur < n_nodes) {  // the checks the next step makes
+          const float4* line = leaf ? tris + 3 * (size_t)first : nodes + 8 * (size_t)cur;
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
+        }
+      }
+#endif
     }
     return false;
   }

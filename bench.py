@@ -38,12 +38,12 @@ RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
 # (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
 # --warmup 3 --no-cpu [--build lbvh]`), per BVH builder:
-#   ploc: reads 427.9 MB, writes 70.2 MB, L2 1916.3 MB (SAH top levels +
+#   ploc: reads 427.8 MB, writes 70.0 MB, L2 2583.1 MB (SAH top levels +
 #         PLOC below 64 triangles, cost-optimal collapse, depth-first node
-#         order, parked finishes, 6 blocks per SM)
+#         order, parked finishes, 6 blocks per SM, next-node prefetch)
 #   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB (level-order nodes,
 #         finishes in the tracing loop, 5 blocks per SM)
-FRAME_TRAFFIC = {"ploc": (427_900_360 + 70_153_648, 1_916_251_470),
+FRAME_TRAFFIC = {"ploc": (427_842_504 + 69_961_168, 2_583_094_821),
                  "lbvh": (463_159_392 + 70_692_880, 1_837_113_990)}
 
 

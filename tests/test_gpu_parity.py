@@ -182,6 +182,51 @@ def test_ray_batches_match_oracle(gpu_ctx, oracle_mod):
         assert hg["found"].mean() > 0.05
 
 
+def _random_rays(n, seed, spread=3.0):
+    import oracle.oracle as O
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-spread, spread, size=(n, 3)).astype(np.float32)
+    d = (rng.uniform(-1, 1, size=(n, 3)) - o * 0.3).astype(np.float32)
+    rays = np.zeros(n, O.RAY_DTYPE)
+    rays["orig"][:, :3] = o
+    rays["orig"][:, 3] = 1
+    rays["dir"][:, :3] = d
+    rays["t_near"] = np.float32(1e-4)
+    rays["t_far"] = FLT_MAX
+    return rays
+
+
+@pytest.mark.parametrize("case", ["stacked", "n64", "n65", "n129", "n1000", "flat", "lbvh_stacked"])
+def test_builder_edge_cases_match_brute_force(gpu_ctx, oracle_mod, case):
+    """Meshes that steer the builder into its edge cases give the oracle's
+    brute-force closest hits: every triangle's centroid in one bin (the SAH
+    split falls back to a split by position), sizes around the 64-triangle
+    range where PLOC takes over, a flat mesh (zero extent on one axis)."""
+    from j3d_gb300 import Mesh, SceneObject, find_closest
+    O = oracle_mod
+    rng = np.random.default_rng(sum(case.encode()))
+    if case in ("stacked", "lbvh_stacked"):
+        base = rng.uniform(-1, 1, size=(3, 3)).astype(np.float32)
+        V = np.concatenate([np.tile(base, (600, 1)), rng.uniform(-1, 1, size=(300, 3)).astype(np.float32)])
+        T = np.arange(len(V), dtype=np.uint32).reshape(-1, 3)
+    elif case == "flat":
+        V = rng.uniform(-1, 1, size=(3000, 3)).astype(np.float32)
+        V[:, 2] = 0.25
+        T = rng.integers(0, len(V), size=(2000, 3)).astype(np.uint32)
+    else:
+        nt = int(case[1:])
+        c = rng.uniform(-1, 1, size=(nt, 1, 3)).astype(np.float32)
+        V = (c + rng.uniform(-0.15, 0.15, size=(nt, 3, 3)).astype(np.float32)).reshape(-1, 3)
+        T = np.arange(3 * nt, dtype=np.uint32).reshape(-1, 3)
+    mesh = Mesh(gpu_ctx, V, T, 2, "lbvh" if case.startswith("lbvh") else "ploc")
+    m = O.Mesh(V, T)
+    rays = _random_rays(20000, 7)
+    hg = find_closest(gpu_ctx, [SceneObject(mesh, I16, 1)], rays)
+    ho, _ = O.find_closest([(m, I16, 1)], rays, brute=True)
+    assert np.array_equal(hg.view(np.uint8), ho.view(np.uint8))
+    assert hg["found"].any()
+
+
 def test_update_canvas_rect_empty_and_null_scene(gpu_ctx, oracle_mod):
     from j3d_gb300 import Canvas, Matcap, Scene, camera_for_vfov, workloads as W
     O = oracle_mod

@@ -951,6 +951,10 @@ __global__ void k_top_bins_init(uint32_t* __restrict__ bins, uint32_t n_words) {
 }
 
 static const int kTopChunk = 2048;
+// Tasks up to this size are binned by one warp each (k_top_bin_warp): at
+// that depth 32 neighbouring triangles span many bins, so grouping lanes by
+// bin (match + reductions per group) serialises; plain shared atomics do not.
+static const uint32_t kTopWarpTask = 2048;
 
 // bins of every active task: [task][axis][bin][kTopVals]
 __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
@@ -963,7 +967,7 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
   if (c0 >= n) return;
   if (threadIdx.x == 0) {
     const uint32_t a = task_of[c0], b = task_of[c1 - 1];
-    s_task = (a == b && a < n_tasks) ? a : kNoTask;
+    s_task = (a == b && a < n_tasks && tasks[a].end - tasks[a].begin > kTopWarpTask) ? a : kNoTask;
   }
   for (uint32_t k = threadIdx.x; k < 3 * kTopBins * kTopVals; k += blockDim.x) {
     const uint32_t v = k % kTopVals;
@@ -974,7 +978,8 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
   const uint32_t lane = threadIdx.x & 31u;
   for (uint32_t base = c0; base < c1; base += blockDim.x) {  // uniform trip count: whole warps
     const uint32_t p = base + threadIdx.x;
-    const uint32_t t = p < c1 ? (st != kNoTask ? st : task_of[p]) : kNoTask;
+    uint32_t t = p < c1 ? (st != kNoTask ? st : task_of[p]) : kNoTask;
+    if (st == kNoTask && t < n_tasks && tasks[t].end - tasks[t].begin <= kTopWarpTask) t = kNoTask;  // k_top_bin_warp's
     const bool valid = t < n_tasks;
     float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo, c = lo;
     int bx = 0, by = 0, bz = 0;
@@ -1032,6 +1037,49 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
       atomicMax(g + k, sb[k]);
     }
   }
+}
+
+// tasks of at most kTopWarpTask triangles: one warp bins a whole task into
+// its own shared-memory bins with per-lane shared atomics, then stores them
+__global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
+                                                      const float4* __restrict__ bhi, const TopTask* __restrict__ tasks,
+                                                      uint32_t n_tasks, uint32_t* __restrict__ bins) {
+  __shared__ uint32_t sb[8][3 * kTopBins * kTopVals];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t t = blockIdx.x * 8u + warp;
+  if (t >= n_tasks) return;  // whole warps leave together
+  const TopTask T = tasks[t];
+  if (T.end - T.begin > kTopWarpTask) return;
+  uint32_t* my = sb[warp];
+  for (uint32_t k = lane; k < 3 * kTopBins * kTopVals; k += 32) {
+    const uint32_t v = k % kTopVals;
+    my[k] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);
+  }
+  __syncwarp();
+  for (uint32_t p = T.begin + lane; p < T.end; p += 32) {
+    const uint32_t tri = ord[p];
+    const float4 lo = blo[tri], hi = bhi[tri];
+    const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
+    const int bins3[3] = {top_bin(c.x, T.clo.x, T.chi.x), top_bin(c.y, T.clo.y, T.chi.y),
+                          top_bin(c.z, T.clo.z, T.chi.z)};
+    const uint32_t v[12] = {f2o(c.x),  f2o(c.y),  f2o(c.z),  f2o(c.x),  f2o(c.y),  f2o(c.z),
+                            f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      uint32_t* b = my + (ax * kTopBins + bins3[ax]) * kTopVals;
+      atomicAdd(b, 1u);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        if ((k % 6) < 3)
+          atomicMin(b + 1 + k, v[k]);
+        else
+          atomicMax(b + 1 + k, v[k]);
+      }
+    }
+  }
+  __syncwarp();
+  uint32_t* g = bins + (size_t)t * 3 * kTopBins * kTopVals;
+  for (uint32_t k = lane; k < 3 * kTopBins * kTopVals; k += 32) g[k] = my[k];
 }
 
 __device__ __forceinline__ float box_half_area(float lx, float ly, float lz, float hx, float hy, float hz) {
@@ -1452,6 +1500,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
         k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words);
         k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
                                                                      n_tasks, nt, top_bins);
+        k_top_bin_warp<<<(n_tasks + 7) / 8, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, tasks_a, n_tasks, top_bins);
         k_top_split<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
         J3DG_CK(cudaMemsetAsync(top_ctr + 1, 0, sizeof(uint32_t), st));
         k_top_children<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, splits, n_tasks, J3DG_SAH_TOP, top_ctr,

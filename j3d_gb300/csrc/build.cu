@@ -1340,6 +1340,14 @@ __global__ void k_top_link(const TopRange* __restrict__ ranges, uint32_t n_range
     }                                                          \
   } while (0)
 
+// stream-ordered free of a scratch buffer as soon as it is dead (keeps the
+// build's peak device memory down); the pointer is cleared for the cleanup
+#define J3DG_DROP(p)             \
+  do {                           \
+    if (p) cudaFreeAsync(p, st); \
+    p = nullptr;                 \
+  } while (0)
+
 // Builds the device BVH. dV and dT are device arrays. On success fills the
 // mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals).
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
@@ -1421,6 +1429,11 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   }
   k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, v0, nt, nv, (float4*)m->d_tris, d_status);
   J3DG_CK(cudaGetLastError());
+  J3DG_DROP(k1);  // the sorted codes (k0) stay for the LBVH
+  J3DG_DROP(v0);
+  J3DG_DROP(v1);
+  J3DG_DROP(hist);
+  J3DG_DROP(sums);
 
   if (nt <= m->leaf_size) {  // tiny mesh: the root is one leaf
     m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
@@ -1434,6 +1447,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   if (!(m->build_flags & J3DG_BUILD_LBVH)) {
     uint32_t mcount = nt, node_base = 0, iters = 0, htot[2] = {0, 0}, root = 0;
     const uint32_t sblocks_max = (nt + 1023) / 1024;
+    J3DG_DROP(k0);
     J3DG_CK(cudaMallocAsync((void**)&child, sizeof(uint2) * (nt - 1), st));
     J3DG_CK(cudaMallocAsync((void**)&box, sizeof(BinNode) * (nt - 1), st));
     J3DG_CK(cudaMallocAsync((void**)&count, sizeof(uint32_t) * (nt - 1), st));
@@ -1536,6 +1550,16 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       k_ploc_init_seg<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, ord_a, nt, seg_starts, seg_scan, C0,
                                                         lo0, hi0, seg0);
       n_seg = n_ranges;
+      J3DG_DROP(ord_a);
+      J3DG_DROP(ord_b);
+      J3DG_DROP(task_of);
+      J3DG_DROP(task_of2);
+      J3DG_DROP(tbox_lo);
+      J3DG_DROP(tbox_hi);
+      J3DG_DROP(top_bins);
+      J3DG_DROP(tasks_a);
+      J3DG_DROP(tasks_b);
+      J3DG_DROP(splits);
     } else {
       k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, C0, lo0, hi0);
       J3DG_CK(cudaMemsetAsync(seg0, 0, sizeof(uint32_t) * nt, st));
@@ -1586,6 +1610,23 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       rc = J3DG_ERR_CUDA;
       goto cleanup;
     }
+    // the binary tree (child, box, count) is all the collapse needs
+    J3DG_DROP(C0);
+    J3DG_DROP(C1);
+    J3DG_DROP(nn);
+    J3DG_DROP(create);
+    J3DG_DROP(survive);
+    J3DG_DROP(cscan);
+    J3DG_DROP(sscan);
+    J3DG_DROP(lo0);
+    J3DG_DROP(hi0);
+    J3DG_DROP(lo1);
+    J3DG_DROP(hi1);
+    J3DG_DROP(seg0);
+    J3DG_DROP(seg1);
+    J3DG_DROP(seg_starts);
+    J3DG_DROP(seg_scan);
+    J3DG_DROP(ranges);
     if (J3DG_SAH_COLLAPSE) {
       J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float4) * (nt - 1), st));
       J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uchar4) * (nt - 1), st));

@@ -130,32 +130,42 @@ __device__ __forceinline__ void slab(const Ray& r, float lox, float loy, float l
 // 1: state a traversal step does not read (the world ray, the best hit's
 // attributes) lives in shared memory, one slot per thread, so that the
 // registers left cover the step's working set and more warps fit an SM.
-// Every kernel that traces runs blocks of at most J3DG_COLD_MAX threads.
+// The slots are sized by the tracing kernel's block (N threads): every
+// tracing kernel's launch bounds equal the N it instantiates.
 #ifndef J3DG_COLD_SMEM
 #define J3DG_COLD_SMEM 7
 #endif
-#ifndef J3DG_COLD_MAX
-#define J3DG_COLD_MAX 256
-#endif
-#if J3DG_COLD_SMEM & 1
-__shared__ float j3dg_cold_ray[6][J3DG_COLD_MAX];
-#endif
-#if J3DG_COLD_SMEM & 2
-__shared__ float j3dg_cold_uv[2][J3DG_COLD_MAX];
-__shared__ uint32_t j3dg_cold_key[3][J3DG_COLD_MAX];
-#endif
+template <int N>
+struct ColdSlots {
+  static constexpr int S = N;
+  // world ray [6][S], best-hit u / v [2][S], best-hit inst / tri / slot [3][S]
+  __device__ static __forceinline__ float* ray() {
+    __shared__ float a[6 * S];
+    return a;
+  }
+  __device__ static __forceinline__ float* uv() {
+    __shared__ float a[2 * S];
+    return a;
+  }
+  __device__ static __forceinline__ uint32_t* key() {
+    __shared__ uint32_t a[3 * S];
+    return a;
+  }
+};
 
 // Best hit so far: t and found are read every step; the key (inst, tri) only
 // on a t tie, u / v / slot only when the ray finishes.
-struct Best {
+template <int N>
+struct BestT {
   float t;
   bool found;  // found == (t < t_far set by an accept)
 #if J3DG_COLD_SMEM & 2
-  __device__ __forceinline__ float& u() const { return j3dg_cold_uv[0][threadIdx.x]; }
-  __device__ __forceinline__ float& v() const { return j3dg_cold_uv[1][threadIdx.x]; }
-  __device__ __forceinline__ uint32_t& inst() const { return j3dg_cold_key[0][threadIdx.x]; }
-  __device__ __forceinline__ uint32_t& tri() const { return j3dg_cold_key[1][threadIdx.x]; }
-  __device__ __forceinline__ uint32_t& slot() const { return j3dg_cold_key[2][threadIdx.x]; }
+  using C = ColdSlots<N>;
+  __device__ __forceinline__ float& u() const { return C::uv()[threadIdx.x]; }
+  __device__ __forceinline__ float& v() const { return C::uv()[C::S + threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& inst() const { return C::key()[threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& tri() const { return C::key()[C::S + threadIdx.x]; }
+  __device__ __forceinline__ uint32_t& slot() const { return C::key()[2 * C::S + threadIdx.x]; }
 #else
   float u_, v_;
   uint32_t inst_, tri_, slot_;
@@ -178,8 +188,9 @@ __device__ __forceinline__ bool key_less(uint32_t ia, uint32_t ta, uint32_t ib, 
 
 // Moller-Trumbore + gate for triangle `slot`. any: the caller stops at the
 // first accept, so the (t, key) comparison only needs t < t_best.
+template <class BestHit>
 __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict__ tris, uint32_t slot, uint32_t inst,
-                                         Best& b, bool any) {
+                                         BestHit& b, bool any) {
   const float4 a = __ldg(tris + 3 * (size_t)slot);
   const float4 c1 = __ldg(tris + 3 * (size_t)slot + 1);
   const float4 c2 = __ldg(tris + 3 * (size_t)slot + 2);
@@ -223,17 +234,18 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
 // that object's BVH4 is walked with a per-thread stack. run() advances by at
 // most `iters` node or leaf steps, so persistent warps can refill lanes whose
 // rays have finished. Corrupt trees raise status bits instead of trapping.
-struct Tracer {
+template <int N>
+struct TracerT {
 #if J3DG_COLD_SMEM & 1
   // world ray: read only when an object's walk starts, kept in shared memory
-  __device__ __forceinline__ float& wr(int k) { return j3dg_cold_ray[k][threadIdx.x]; }
+  __device__ __forceinline__ float& wr(int k) { return ColdSlots<N>::ray()[k * ColdSlots<N>::S + threadIdx.x]; }
 #else
   float wr_[6];  // world ray
   __device__ __forceinline__ float& wr(int k) { return wr_[k]; }
 #endif
   bool any;                             // stop at the first accepted triangle
   Ray r;                                // object-space ray of object `inst`
-  Best b;
+  BestT<N> b;
   const float4* nodes;
   const float4* tris;
   uint32_t n_nodes, nt;
@@ -406,11 +418,12 @@ struct Tracer {
 // fetches for all such lanes with one atomic. Src supplies count(), begin()
 // (returns false when the item needs no tracing and was handled) and
 // finish(); ITERS node/leaf steps run between refills.
-template <int ITERS, class Src>
+// N: the kernel's block size.
+template <int ITERS, int N, class Src>
 __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __restrict__ insts, uint32_t n_inst,
                                                  uint32_t* counter, uint32_t* status,
                                                  unsigned long long* counters) {
-  Tracer T;
+  TracerT<N> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = src.count();

@@ -598,7 +598,6 @@ __global__ void k_cluster_map(const DevInst* __restrict__ inst, const uint32_t* 
 
 // Learned closest hit: the two predicted clusters first, then the whole
 // tree with their best hit as the starting best (exact).
-static_assert(128 <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
 __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict__ inst, const j3dg_ray* __restrict__ rays,
                                                       uint32_t n, const uint32_t* __restrict__ top2,
                                                       const uint32_t* __restrict__ roots, uint32_t n_roots,
@@ -609,7 +608,7 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
   uint32_t visits = 0, tests = 0, exact_visits = 0, exact_tests = 0;
   if (i < n) {
   const float* f = reinterpret_cast<const float*>(rays + i);
-  Tracer T;
+  TracerT<128> T;
   uint2 stack[J3DG_STACK];
   T.begin(inst, 1, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], false);
   const uint32_t c0 = top2[2 * i], c1 = top2[2 * i + 1];

@@ -20,9 +20,9 @@
 
 namespace j3dg {
 
-// block size of the query kernels (they trace: at most J3DG_COLD_MAX threads)
+// block size of the query kernels (their launch bounds; the per-thread
+// shared slots of the hit record are sized by it)
 static const int kQueryThreads = 128;
-static_assert(kQueryThreads <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
 
 // Inserts (t, id, u, v) into the sorted buffer h[0..n) of capacity cap.
 // `extra` goes to two_level_index (the object, or a leaf slot internally).
@@ -69,7 +69,7 @@ __device__ bool all_hits(const DevInst& I, const Ray& r, float t_far, uint32_t* 
           return false;
         }
         for (uint32_t k = 0; k < cnt; ++k) {
-          Best b;
+          BestT<kQueryThreads> b;
           b.t = t_far;
           b.found = false;
           if (tri_test(r, I.tris, first + k, 0u, b, true)) on_hit(first + k, b.t, b.u(), b.v());

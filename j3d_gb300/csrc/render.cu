@@ -155,7 +155,6 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 #define J3DG_DEFER_FINISH 1
 #endif
 static const int kTraceThreads = J3DG_TRACE_THREADS;
-static_assert(kTraceThreads <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
 static const int kIters = J3DG_TRACE_ITERS;
 
 // Pixel and colour state of a lane: read only at a pixel's start and
@@ -182,6 +181,7 @@ __device__ __forceinline__ uint32_t primary_count(const FrameParams& P) {
   return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
 }
 
+template <class Tracer>
 __device__ __forceinline__ void primary_begin(const FrameParams& P, Tracer& T, int x, int y) {
   // canvas.cpp:700-701, 773-782
   const float4 o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
@@ -194,9 +194,10 @@ __device__ __forceinline__ void primary_begin(const FrameParams& P, Tracer& T, i
 
 // Writes the hit record; returns true and sets up the shadow ray in T when
 // one is needed. w0 / su / sv keep what the final colour needs.
+template <class Tracer>
 __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, size_t pix, uint32_t& w0, float& su,
                                                float& sv) {
-  const Best b = T.b;
+  const auto b = T.b;
   if (!b.found) {
     write_miss(P, pix);
     return false;
@@ -273,6 +274,7 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   return true;
 }
 
+template <class Tracer>
 __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer& T, size_t pix, uint32_t w0, float su,
                                               float sv) {
   uint32_t mark = w0 & 0xffu;
@@ -287,7 +289,7 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
 template <bool kThroughput>
 __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
     k_frame(const FrameParams P) {
-  Tracer T;
+  TracerT<kTraceThreads> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
@@ -366,6 +368,7 @@ struct BatchSrc {
   j3dg_hit* hits;
   uint32_t n;
   __device__ __forceinline__ uint32_t count() const { return n; }
+  template <class Tracer>
   __device__ __forceinline__ bool begin(Tracer& T, const DevInst* insts, uint32_t n_inst, uint32_t i) {
     const float* f = reinterpret_cast<const float*>(rays + i);  // 40-byte records: 4-byte loads
     if (T.begin(insts, n_inst, f[0], f[1], f[2], f[4], f[5], f[6], f[8], f[9], ANY)) {
@@ -374,6 +377,7 @@ struct BatchSrc {
     }
     return true;
   }
+  template <class Tracer>
   __device__ __forceinline__ void finish(Tracer& T, uint32_t i) {
     const float t_far = reinterpret_cast<const float*>(rays + i)[9];
     j3dg_hit h;
@@ -393,7 +397,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restric
                                                         j3dg_hit* __restrict__ hits, uint32_t* counter,
                                                         uint32_t* status, unsigned long long* counters) {
   BatchSrc<ANY> src{rays, hits, n};
-  persistent_trace<kIters>(src, inst, n_inst, counter, status, counters);
+  persistent_trace<kIters, kTraceThreads>(src, inst, n_inst, counter, status, counters);
 }
 
 // Many frames (canvases, scenes, cameras, resolutions of uneven size) in one
@@ -412,8 +416,7 @@ template <int TPB, bool kThroughput>
 __global__ void __launch_bounds__(TPB, (MinBlocks<TPB, kThroughput>::value))
     k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
                   uint32_t* work) {
-  static_assert(TPB <= J3DG_COLD_MAX, "tracing blocks must fit the per-thread shared slots");
-  Tracer T;
+  TracerT<TPB> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t total = offsets[n_frames];
@@ -667,16 +670,12 @@ static cudaError_t launch_batch_variant(const FrameParams* d_params, const uint3
   if (!b64) {
     b64 = persistent_blocks(k_frame_batch<64, kT>, 64);
     b128 = persistent_blocks(k_frame_batch<128, kT>, 128);
-#if J3DG_COLD_MAX >= 256
     b256 = persistent_blocks(k_frame_batch<256, kT>, 256);
-#endif
   }
   if (block_threads == 64)
     k_frame_batch<64, kT><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
-#if J3DG_COLD_MAX >= 256
   else if (block_threads == 256)
     k_frame_batch<256, kT><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
-#endif
   else
     k_frame_batch<128, kT><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
   return cudaGetLastError();

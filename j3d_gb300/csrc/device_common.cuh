@@ -402,7 +402,7 @@ struct TracerT {
       if (cur != J3DG_EMPTY_REF) {
         const bool leaf = (cur & J3DG_LEAF_BIT) != 0;
         const uint32_t first = (cur & 0x7fffffffu) >> 3;
-        if (leaf ? first < nt : cur < n_nodes) {  // the checks the next step makes
+        if (leaf ? first + (cur & 7u) + 1u <= nt : cur < n_nodes) {  // the checks the next step makes
           const float4* line = leaf ? tris + 3 * (size_t)first : nodes + 8 * (size_t)cur;
           asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
         }

@@ -167,6 +167,19 @@ const char* j3dg_last_error(const j3dg_ctx* ctx);
    add their BVH node visits and triangle tests to two device counters. */
 int j3dg_ctx_set_counting(j3dg_ctx* ctx, int enable);
 int j3dg_ctx_read_counters(j3dg_ctx* ctx, uint64_t out[2], int reset);
+/* How canvas frames (render_frame, update_canvas, render_scene) find the
+   primary hits (no reference counterpart; the result is the same either
+   way). TRACE walks the BVH per pixel. RASTER projects every triangle's box
+   to the screen and runs the traversal's own ray / triangle test on the
+   pixels inside, keeping each pixel's minimum of (t, object, triangle id),
+   which is the traversal's closest hit; it needs every object's box in
+   front of the camera and reads every triangle once per frame (frames
+   that do not allow it are traced). AUTO (the default) traces. Shadow rays
+   are always traced. */
+#define J3DG_PRIMARY_AUTO 0
+#define J3DG_PRIMARY_TRACE 1
+#define J3DG_PRIMARY_RASTER 2
+int j3dg_ctx_set_primary_mode(j3dg_ctx* ctx, int mode);
 const char* j3dg_status_string(int status);
 int j3dg_abi_version(void);
 
@@ -394,6 +407,10 @@ int j3dg_canvas_set_pixels(j3dg_canvas* c, const j3dg_pixel* src);
 /* Counts the canvas's G-buffer records with a hit and with the shadow bit
    (no reference counterpart; for ray accounting without a copy-out). */
 int j3dg_canvas_count_hits(j3dg_canvas* c, uint64_t* hits, uint64_t* shadowed);
+/* The primary-hit method of the canvas's last frame: J3DG_PRIMARY_TRACE or
+   J3DG_PRIMARY_RASTER (a rasterised frame whose list of large triangles
+   overflowed is traced on the device and still reports RASTER). */
+int j3dg_canvas_last_primary(const j3dg_canvas* c);
 /* Device pointers of the canvas buffers (valid until resize/destroy). */
 int j3dg_canvas_device_buffers(j3dg_canvas* c, j3dg_pixel** pixels, uint32_t** image, uint32_t** background);
 

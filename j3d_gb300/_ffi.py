@@ -27,6 +27,8 @@ assert PIXEL_DTYPE.itemsize == 32 and RAY_DTYPE.itemsize == 40 and HIT_DTYPE.ite
 
 J3DG_OK = 0
 J3DG_ERR_INVALID_ARGUMENT = 1
+# how canvas frames find primary hits (j3dg_ctx_set_primary_mode)
+PRIMARY_AUTO, PRIMARY_TRACE, PRIMARY_RASTER = 0, 1, 2
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "no CUDA device",
                 5: "device status raised", 6: "unsupported"}
 
@@ -154,6 +156,8 @@ SIGNATURES = {
     "j3dg_canvas_device_buffers": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "j3dg_render_batch": (_I, [_P, C.POINTER(Frame), _U]),
     "j3dg_ctx_set_batch_block": (_I, [_P, _I]),
+    "j3dg_ctx_set_primary_mode": (_I, [_P, _I]),
+    "j3dg_canvas_last_primary": (_I, [_P]),
     "j3dg_batch_create": (_I, [_P, C.POINTER(Frame), _U, C.POINTER(_P)]),
     "j3dg_batch_set_scene": (_I, [_P, _U, C.POINTER(Scene)]),
     "j3dg_batch_launch": (_I, [_P]),

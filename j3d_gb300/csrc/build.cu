@@ -1340,6 +1340,19 @@ __global__ void k_top_link(const TopRange* __restrict__ ranges, uint32_t n_range
     }                                                          \
   } while (0)
 
+// slot_of[id] = leaf position of triangle id (ids are a permutation of 0..nt)
+__global__ void k_slot_of(const float4* __restrict__ tris, uint32_t nt, uint32_t* __restrict__ slot_of,
+                          uint32_t* status) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const uint32_t id = __float_as_uint(tris[3 * (size_t)i].w);
+  if (id >= nt) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    return;
+  }
+  slot_of[id] = i;
+}
+
 // stream-ordered free of a scratch buffer as soon as it is dead (keeps the
 // build's peak device memory down); the pointer is cleared for the cleanup
 #define J3DG_DROP(p)             \
@@ -1731,6 +1744,17 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
 
 cleanup:
+  if (rc == J3DG_OK && m->d_tris) {  // the inverse of the leaf order, for lookups by triangle id
+    cudaError_t e = cudaMalloc(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt);
+    if (e == cudaSuccess) {
+      k_slot_of<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, (uint32_t*)m->d_slot_of, d_status);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      err = std::string("build: ") + cudaGetErrorString(e);
+      rc = J3DG_ERR_CUDA;
+    }
+  }
   if (d_part) cudaFreeAsync(d_part, st);
   if (d_bb) cudaFreeAsync(d_bb, st);
   if (k0) cudaFreeAsync(k0, st);
@@ -1777,7 +1801,7 @@ cleanup:
     return J3DG_ERR_UNSUPPORTED;
   }
   m->device_bytes = sizeof(float4) * 8 * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
-                    sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 3 * (uint64_t)nt;
+                    sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 4 * (uint64_t)nt;
   return J3DG_OK;
 }
 

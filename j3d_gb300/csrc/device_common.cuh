@@ -31,6 +31,7 @@ struct DevInst {
   const float4* nodes;     // 8 float4 per wide node
   const float4* tris;      // 3 float4 per triangle, leaf order; v0.w = id bits
   const float4* normals;   // per triangle id
+  const uint32_t* slot_of; // leaf-order position (tris) of each triangle id
   const uint32_t* index;   // caller's triangle indices (3 per triangle)
   const float* colors;     // per vertex rgb or null
   const float* uv;         // 6 per triangle or null

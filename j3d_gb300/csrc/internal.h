@@ -63,6 +63,7 @@ struct j3dg_mesh {
   void* d_nodes = nullptr;    // float4[8 * n_nodes]
   void* d_tris = nullptr;     // float4[3 * nt], leaf order, v0.w = triangle id
   void* d_normals = nullptr;  // float4[nt], by triangle id
+  void* d_slot_of = nullptr;  // uint32[nt]: leaf-order position of each triangle id
   void* d_index = nullptr;    // uint32[3 * nt], the caller's triangles
   void* d_colors = nullptr;   // float[3 * nv] or null
   void* d_uv = nullptr;       // float[6 * nt] or null
@@ -87,8 +88,9 @@ struct j3dg_canvas {
   void* d_pixels = nullptr;      // j3dg_pixel[w*h]
   uint32_t* d_image = nullptr;   // w*h
   uint32_t* d_background = nullptr;
-  void* d_queue = nullptr;       // shadow-ray jobs, 2 float4 per pixel
+  void* d_queue = nullptr;       // 48 B per pixel: raster keys, jobs and tables during a frame, splat keys after
   uint32_t* d_work = nullptr;    // per-frame work counters
+  int last_primary = 1;          // J3DG_PRIMARY_TRACE or J3DG_PRIMARY_RASTER
   // asynchronous download: ev_ready marks the work queued before it, ev_copied its end
   void* ev_ready = nullptr;
   void* ev_copied = nullptr;

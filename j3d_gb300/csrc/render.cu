@@ -181,15 +181,29 @@ __device__ __forceinline__ uint32_t primary_count(const FrameParams& P) {
   return ((rw + 7u) >> 3) * ((rh + 3u) >> 2) * 32u;
 }
 
-template <class Tracer>
-__device__ __forceinline__ void primary_begin(const FrameParams& P, Tracer& T, int x, int y) {
-  // canvas.cpp:700-701, 773-782
-  const float4 o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
+// world ray of pixel (x, y): canvas.cpp:700-701, 773-782
+__device__ __forceinline__ void primary_ray(const FrameParams& P, int x, int y, float4& o, float4& d) {
+  o = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
   const float sx = fs(fm(2.f, __fdiv_rn(fa((float)x, 0.5f), (float)P.w)), 1.f);
   const float sy = fs(fm(2.f, __fdiv_rn(fa((float)y, 0.5f), (float)P.h)), 1.f);
-  float4 d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
+  d = mat_vec(P.pinv, sx, sy, P.near_plane, 1.f);
   d = mat_vec(P.cs, d.x, d.y, d.z, 0.f);
-  T.begin(P.inst, P.n_inst, o.x, o.y, o.z, d.x, d.y, d.z, __fdiv_rn(P.diagonal, 100.f), FLT_MAX, false);
+}
+
+__device__ __forceinline__ float primary_t_near(const FrameParams& P) { return __fdiv_rn(P.diagonal, 100.f); }
+
+template <class Tracer>
+__device__ __forceinline__ void primary_begin(const FrameParams& P, Tracer& T, int x, int y) {
+  float4 o, d;
+  primary_ray(P, x, y, o, d);
+  T.begin(P.inst, P.n_inst, o.x, o.y, o.z, d.x, d.y, d.z, primary_t_near(P), FLT_MAX, false);
+}
+
+
+// canvas.cpp:836-838: the point light, three diagonals beyond the pivot
+__device__ __forceinline__ float4 light_position(const FrameParams& P) {
+  const float ld = fm(P.diagonal, 3.f);
+  return mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
 }
 
 // Writes the hit record; returns true and sets up the shadow ray in T when
@@ -259,8 +273,7 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
     return false;
   }
   // canvas.cpp:836-853: from the hit point towards the light
-  const float ld = fm(P.diagonal, 3.f);
-  const float4 light = mat_vec(P.cs, fa(P.pivot[0], ld), fa(P.pivot[1], ld), fa(P.pivot[2], ld), 1.f);
+  const float4 light = light_position(P);
   const float4 A = __ldg(I.tris + 3 * (size_t)b.slot());
   const float4 B = __ldg(I.tris + 3 * (size_t)b.slot() + 1);
   const float4 C = __ldg(I.tris + 3 * (size_t)b.slot() + 2);
@@ -286,9 +299,414 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
     P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
 }
 
+// ------------------------------------------------------- rasterisation ----
+//
+// Primary hits without traversal. A ray can only pass the bounds gate of a
+// triangle if it passes through the triangle's box widened by the ray's
+// slab padding, so every pixel whose ray can accept a triangle has its
+// centre inside the screen rectangle of that widened box's eight projected
+// corners. Each triangle takes those pixels (the rectangle grown by
+// kRasterMargin pixels, far above the rounding of either the projection or
+// the pixel rays) as candidates and runs on each the traversal's own
+// Moller-Trumbore + gate with the pixel's own ray; accepted candidates go
+// into a per-pixel 64-bit atomicMin of (t, instance, triangle id). The
+// traversal's closest hit is the minimum of that same key over the same
+// accepted triangles, so the minima are equal; k_frame rebuilds the hit
+// record from the key. Triangles with more than kRasterSmall candidates
+// (and any whose box reaches the camera plane) go to a list that
+// k_raster_large covers pixel-parallel; if the list overflows, k_frame
+// traces the frame instead.
+
+static const uint32_t kRasterSmall = 64;
+static const float kRasterMargin = 0.05f;
+static const int kRasterThreads = 256;
+
+// the best-hit record of one candidate test, in registers
+struct LocalBest {
+  float t;
+  bool found;
+  float u_, v_;
+  uint32_t inst_, tri_, slot_;
+  __device__ __forceinline__ float& u() { return u_; }
+  __device__ __forceinline__ float& v() { return v_; }
+  __device__ __forceinline__ uint32_t& inst() { return inst_; }
+  __device__ __forceinline__ uint32_t& tri() { return tri_; }
+  __device__ __forceinline__ uint32_t& slot() { return slot_; }
+};
+
+__device__ __forceinline__ uint32_t raster_key_low(const FrameParams& P, uint32_t inst, uint32_t id) {
+  return P.id_bits >= 32u ? id : ((inst << P.id_bits) | id);
+}
+
+// candidate queue: (pixel index, inst << id_bits | slot), in the shadow
+// jobs' space (free until k_resolve), 4 entries per canvas pixel
+__device__ __forceinline__ uint2* raster_queue(const FrameParams& P) {
+  return reinterpret_cast<uint2*>(P.keys + (size_t)P.w * P.h);
+}
+__device__ __forceinline__ uint32_t raster_queue_cap(const FrameParams& P) {
+  const size_t cap = 4 * (size_t)P.w * P.h;
+  return cap < 0xffffffffu ? (uint32_t)cap : 0xffffffffu;
+}
+
+// pixel (x, y) against triangle `slot` of instance `inst`
+__device__ __forceinline__ void raster_candidate(const FrameParams& P, uint32_t inst, uint32_t slot, int x, int y) {
+  float4 o, d;
+  primary_ray(P, x, y, o, d);
+  const DevInst& I = P.inst[inst];
+  // Tracer::start_object
+  const float4 oo = mat_vec(I.inv, o.x, o.y, o.z, 1.f);
+  const float4 dd = mat_vec(I.inv, d.x, d.y, d.z, 0.f);
+  const Ray r = make_ray(oo.x, oo.y, oo.z, dd.x, dd.y, dd.z, primary_t_near(P), I.scale);
+  LocalBest b;
+  b.t = FLT_MAX;
+  b.found = false;
+  if (tri_test(r, I.tris, slot, inst, b, false)) {
+    const unsigned long long key =
+        ((unsigned long long)__float_as_uint(b.t) << 32) | (unsigned long long)raster_key_low(P, inst, b.tri_);
+    atomicMin(P.keys + (size_t)y * P.w + x, key);
+  }
+}
+
+// Per-instance object -> clip matrices and paddings; resets the list.
+__global__ void k_raster_setup(const FrameParams P) {
+  __shared__ float w2c[16];  // proj * cs_inv
+  if (threadIdx.x < 16) {
+    const int r = threadIdx.x & 3, c = threadIdx.x >> 2;
+    float acc = 0.f;
+    for (int k = 0; k < 4; ++k) acc += P.proj[4 * k + r] * P.cs_inv[4 * c + k];
+    w2c[4 * c + r] = acc;
+  }
+  __syncthreads();
+  const float4 eye = mat_vec(P.cs, 0.f, 0.f, 0.f, 1.f);
+  for (uint32_t i = threadIdx.x; i < P.n_inst; i += blockDim.x) {
+    const DevInst& I = P.inst[i];
+    RasterInst& R = P.rinst[i];
+    for (int e = 0; e < 16; ++e) {
+      const int r = e & 3, c = e >> 2;
+      float acc = 0.f;
+      for (int k = 0; k < 4; ++k) acc += w2c[4 * k + r] * I.cs[4 * c + k];
+      R.M[e] = acc;
+    }
+    // make_ray's padding for the camera's rays in this object's space
+    const float4 oo = mat_vec(I.inv, eye.x, eye.y, eye.z, 1.f);
+    const float mo = fmaxf(fmaxf(fabsf(oo.x), fabsf(oo.y)), fabsf(oo.z));
+    R.pad = fm(fa(mo, I.scale), 0x1p-19f);
+    R.nt = I.nt;
+    R.unused = 0u;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t first = 0;
+    for (uint32_t i = 0; i < P.n_inst; ++i) {
+      P.rinst[i].first = first;
+      first += P.inst[i].nt;
+    }
+    P.rlist[0] = 0u;  // large triangles listed
+    P.rlist[1] = 0u;  // list overflow
+    P.rlist[2] = 0u;  // candidates queued
+  }
+}
+
+__device__ __forceinline__ uint32_t raster_instance(const FrameParams& P, uint32_t g) {
+  uint32_t lo = 0, hi = P.n_inst;  // last instance with first <= g
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (P.rinst[mid].first <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Candidate rectangle of triangle `slot` of instance `inst` (inclusive
+// pixel bounds, clamped to the frame's rectangle); false when empty. Clip x,
+// y and w are linear over the widened box, so their ranges are the low
+// corner's value plus the negative or positive parts of the three edge
+// terms; x / w over [x range] x [w range] (w > 0) is bounded by the four
+// corner quotients.
+__device__ __forceinline__ bool raster_rect(const FrameParams& P, const RasterInst& R, const float4* tris,
+                                            uint32_t slot, int& x0, int& y0, int& x1, int& y1) {
+  const float4 a = __ldg(tris + 3 * (size_t)slot);
+  const float4 b = __ldg(tris + 3 * (size_t)slot + 1);
+  const float4 c = __ldg(tris + 3 * (size_t)slot + 2);
+  const float e = 2.f * R.pad;
+  const float lx = min3f(a.x, b.x, c.x) - e, ly = min3f(a.y, b.y, c.y) - e, lz = min3f(a.z, b.z, c.z) - e;
+  const float dx = max3f(a.x, b.x, c.x) + e - lx, dy = max3f(a.y, b.y, c.y) + e - ly,
+              dz = max3f(a.z, b.z, c.z) + e - lz;
+  const float* M = R.M;
+  float xl = M[0] * lx + M[4] * ly + M[8] * lz + M[12], xh = xl;
+  float yl = M[1] * lx + M[5] * ly + M[9] * lz + M[13], yh = yl;
+  float wl = M[3] * lx + M[7] * ly + M[11] * lz + M[15], wh = wl;
+  const float tx[3] = {M[0] * dx, M[4] * dy, M[8] * dz};
+  const float ty[3] = {M[1] * dx, M[5] * dy, M[9] * dz};
+  const float tw[3] = {M[3] * dx, M[7] * dy, M[11] * dz};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    xl += fminf(tx[k], 0.f);
+    xh += fmaxf(tx[k], 0.f);
+    yl += fminf(ty[k], 0.f);
+    yh += fmaxf(ty[k], 0.f);
+    wl += fminf(tw[k], 0.f);
+    wh += fmaxf(tw[k], 0.f);
+  }
+  const float sx = 0.5f * (float)P.w, sy = 0.5f * (float)P.h;
+  float px0 = 0.f, px1 = -1.f, py0 = 0.f, py1 = -1.f;
+  if (wl > 0.f) {
+    // approximate reciprocals: the margin covers their error many times over
+    const float rl = __fdividef(1.f, wl), rh = __fdividef(1.f, wh);
+    // pixel x's ray passes through ndc 2 (x + 0.5) / w - 1
+    px0 = (fminf(xl * rl, xl * rh) + 1.f) * sx - 0.5f - kRasterMargin;
+    px1 = (fmaxf(xh * rl, xh * rh) + 1.f) * sx - 0.5f + kRasterMargin;
+    py0 = (fminf(yl * rl, yl * rh) + 1.f) * sy - 0.5f - kRasterMargin;
+    py1 = (fmaxf(yh * rl, yh * rh) + 1.f) * sy - 0.5f + kRasterMargin;
+  }
+  if (!(wl > 0.f) || !(px0 <= px1) || !(py0 <= py1)) {  // reaches the camera plane (or not finite): all pixels
+    x0 = P.x0;
+    y0 = P.y0;
+    x1 = P.x1;
+    y1 = P.y1;
+    return true;
+  }
+  // clamp in float first (the projected values may be huge)
+  x0 = (int)ceilf(fmaxf(px0, (float)P.x0));
+  x1 = (int)floorf(fminf(px1, (float)P.x1));
+  y0 = (int)ceilf(fmaxf(py0, (float)P.y0));
+  y1 = (int)floorf(fminf(py1, (float)P.y1));
+  return x0 <= x1 && y0 <= y1;
+}
+
+// One thread per triangle of every instance; small candidate sets are
+// spread over the warp's lanes, large ones listed for k_raster_large.
+__global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameParams P) {
+  const uint32_t lane = threadIdx.x & 31u;
+  {
+    const uint32_t g = blockIdx.x * kRasterThreads + threadIdx.x;
+    uint32_t cnt = 0, inst = 0, slot = 0;
+    int rx = 0, ry = 0, rw = 1;
+    if (g < P.raster_total) {
+      inst = raster_instance(P, g);
+      const RasterInst& R = P.rinst[inst];
+      slot = g - R.first;
+      int x0, y0, x1, y1;
+      if (slot < R.nt && raster_rect(P, R, P.inst[inst].tris, slot, x0, y0, x1, y1)) {
+        const uint64_t area = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
+        if (area <= kRasterSmall) {
+          cnt = (uint32_t)area;
+          rx = x0;
+          ry = y0;
+          rw = x1 - x0 + 1;
+        } else {
+          const uint32_t k = atomicAdd(P.rlist, 1u);
+          if (k < P.rlist_cap) {
+            uint32_t* E = P.rlist + kRasterListHeader + (size_t)k * kRasterEntryWords;
+            *reinterpret_cast<uint4*>(E) = make_uint4(inst, slot, (uint32_t)x0, (uint32_t)y0);
+            *reinterpret_cast<uint4*>(E + 4) = make_uint4((uint32_t)x1, (uint32_t)y1, 0u, 0u);
+          } else {
+            atomicOr(P.rlist + 1, 1u);
+          }
+        }
+      }
+    }
+    // the warp's candidates, 32 at a time: candidate c belongs to the first
+    // lane whose inclusive count exceeds c
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    // queued for k_raster_test (one thread per candidate: the tests run with
+    // every lane busy), one atomic per block; what does not fit the queue is
+    // tested here
+    __shared__ uint32_t warp_total[kRasterThreads / 32], block_base;
+    const uint32_t warp = threadIdx.x >> 5;
+    if (lane == 31) warp_total[warp] = total;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t sum = 0;
+      for (int k = 0; k < kRasterThreads / 32; ++k) sum += warp_total[k];
+      block_base = sum ? atomicAdd(P.rlist + 2, sum) : 0u;
+    }
+    __syncthreads();
+    if (total == 0) return;
+    uint32_t qbase = block_base;
+    for (uint32_t k = 0; k < warp; ++k) qbase += warp_total[k];
+    const uint32_t cap = raster_queue_cap(P);
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const uint32_t q = qbase + incl - cnt + j;
+      if (q < cap)
+        raster_queue(P)[q] = make_uint2((uint32_t)(ry + (int)(j / (uint32_t)rw)) * P.w + (uint32_t)(rx + (int)(j % (uint32_t)rw)),
+                                        raster_key_low(P, inst, slot));
+    }
+    if (qbase + total <= cap) return;
+    for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+      const uint32_t c = c0 + lane;
+      int own = 0;
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const uint32_t v = __shfl_sync(0xffffffffu, incl, own + step - 1);
+        if (v <= c) own += step;
+      }
+      const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, own), o_cnt = __shfl_sync(0xffffffffu, cnt, own);
+      const uint32_t o_inst = __shfl_sync(0xffffffffu, inst, own), o_slot = __shfl_sync(0xffffffffu, slot, own);
+      const int o_rx = __shfl_sync(0xffffffffu, rx, own), o_ry = __shfl_sync(0xffffffffu, ry, own);
+      const int o_rw = __shfl_sync(0xffffffffu, rw, own);
+      if (c < total && qbase + c >= cap) {
+        const uint32_t j = c - (o_incl - o_cnt);
+        raster_candidate(P, o_inst, o_slot, o_rx + (int)(j % (uint32_t)o_rw), o_ry + (int)(j / (uint32_t)o_rw));
+      }
+    }
+  }
+}
+
+// The queued (pixel, triangle) candidates.
+__global__ void __launch_bounds__(kRasterThreads) k_raster_test(const FrameParams P) {
+  if (P.rlist[1]) return;
+  const uint32_t n = min(P.rlist[2], raster_queue_cap(P));
+  const uint32_t mask = P.id_bits >= 32u ? 0xffffffffu : (1u << P.id_bits) - 1u;
+  for (uint32_t i = blockIdx.x * kRasterThreads + threadIdx.x; i < n; i += gridDim.x * kRasterThreads) {
+    const uint2 c = raster_queue(P)[i];
+    const uint32_t inst = P.id_bits >= 32u ? 0u : c.y >> P.id_bits;
+    raster_candidate(P, inst, c.y & mask, (int)(c.x % P.w), (int)(c.x / P.w));
+  }
+}
+
+// Listed triangles: each block column walks the pixels of a rectangle.
+__global__ void __launch_bounds__(kRasterThreads) k_raster_large(const FrameParams P) {
+  const uint32_t n = min(P.rlist[0], P.rlist_cap);
+  if (P.rlist[1]) return;  // overflowed: the frame is traced
+  for (uint32_t e = blockIdx.y; e < n; e += gridDim.y) {
+    const uint32_t* E = P.rlist + kRasterListHeader + (size_t)e * kRasterEntryWords;
+    const uint4 a = *reinterpret_cast<const uint4*>(E);
+    const uint4 b = *reinterpret_cast<const uint4*>(E + 4);
+    const int x0 = (int)a.z, y0 = (int)a.w, x1 = (int)b.x, y1 = (int)b.y;
+    const uint32_t rw = (uint32_t)(x1 - x0 + 1);
+    const uint64_t area = (uint64_t)rw * (uint64_t)(y1 - y0 + 1);
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < area; p += (uint64_t)gridDim.x * blockDim.x)
+      raster_candidate(P, a.x, a.y, x0 + (int)(p % rw), y0 + (int)(p / rw));
+  }
+}
+
+// Primary hit of pixel (x, y) from its raster key: the traversal's state as
+// if the ray had just finished. Returns false for a miss.
+template <class Tracer>
+__device__ __forceinline__ bool raster_resolve(const FrameParams& P, Tracer& T, int x, int y,
+                                               unsigned long long key) {
+  if (key == ~0ull) return false;
+  const uint32_t lo = (uint32_t)key;
+  const uint32_t inst = P.id_bits >= 32u ? 0u : lo >> P.id_bits;
+  const uint32_t id = P.id_bits >= 32u ? lo : lo & ((1u << P.id_bits) - 1u);
+  if (inst >= P.n_inst || id >= P.inst[inst].nt) {
+    atomicOr(P.status, J3DG_DEV_BAD_INDEX);
+    return false;
+  }
+  const DevInst& I = P.inst[inst];
+  const uint32_t slot = __ldg(I.slot_of + id);
+  if (slot >= I.nt) {
+    atomicOr(P.status, J3DG_DEV_BAD_INDEX);
+    return false;
+  }
+  primary_begin(P, T, x, y);
+  if (inst != 0u) {
+    T.inst = inst;
+    T.start_object(P.inst);
+  }
+  T.b.t = FLT_MAX;
+  T.b.found = false;
+  if (!tri_test(T.r, I.tris, slot, inst, T.b, false)) {  // the raster accepted it with the same test
+    atomicOr(P.status, J3DG_DEV_BAD_INDEX);
+    return false;
+  }
+  return true;
+}
+
+// A hit pixel's shadow ray and what its final colour needs; the direction
+// is recomputed from the light as primary_finish computes it.
+struct ShadowJob {
+  float px, py, pz;
+  uint32_t pix;
+  uint32_t w0;
+  float su, sv;
+  uint32_t unused;
+};
+static const int kResolveThreads = 256;
+
+__device__ __forceinline__ ShadowJob* shadow_jobs(const FrameParams& P) {
+  return reinterpret_cast<ShadowJob*>(P.keys + (size_t)P.w * P.h);
+}
+
+// One thread per pixel of the rectangle: the miss record, or the hit rebuilt
+// from its key and the primary finish (G-buffer record, shading); hits that
+// cast a shadow ray are queued for k_shadow.
+__global__ void __launch_bounds__(kResolveThreads) k_resolve(const FrameParams P) {
+  if (P.rlist[1]) return;  // the list overflowed: k_frame traces the frame
+  TracerT<kResolveThreads> T;
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  const uint32_t i = blockIdx.x * kResolveThreads + threadIdx.x;
+  bool queue = false;
+  ShadowJob J;
+  if (i < rw * rh) {
+    const int x = P.x0 + (int)(i % rw), y = P.y0 + (int)(i / rw);
+    const size_t pix = (size_t)y * P.w + x;
+    if (raster_resolve(P, T, x, y, P.keys[pix])) {
+      uint32_t w0 = 0;
+      float su = 0.f, sv = 0.f;
+      if (primary_finish(P, T, pix, w0, su, sv)) {
+        queue = true;
+        J = ShadowJob{T.wr(0), T.wr(1), T.wr(2), (uint32_t)pix, w0, su, sv, 0u};
+      }
+    } else {
+      write_miss(P, pix);
+    }
+  }
+  const uint32_t m = __ballot_sync(0xffffffffu, queue);
+  if (m) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(P.work + 1, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (queue) shadow_jobs(P)[base + __popc(m & ((1u << lane) - 1u))] = J;
+  }
+}
+
+// the queued shadow rays, traced by persistent warps
+struct ShadowSrc {
+  const FrameParams* P;
+  const ShadowJob* jobs;
+  uint32_t n;
+  float4 light;
+  __device__ __forceinline__ uint32_t count() const { return n; }
+  template <class Tracer>
+  __device__ __forceinline__ bool begin(Tracer& T, const DevInst* insts, uint32_t n_inst, uint32_t i) {
+    const ShadowJob J = jobs[i];
+    // primary_finish's shadow ray (canvas.cpp:836-853)
+    if (T.begin(insts, n_inst, J.px, J.py, J.pz, fs(light.x, J.px), fs(light.y, J.py), fs(light.z, J.pz), 1e-3f,
+                FLT_MAX, true)) {
+      finish(T, i);
+      return false;
+    }
+    return true;
+  }
+  template <class Tracer>
+  __device__ __forceinline__ void finish(Tracer& T, uint32_t i) {
+    const ShadowJob J = jobs[i];
+    shadow_finish(*P, T, J.pix, J.w0, J.su, J.sv);
+  }
+};
+
+__global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_shadow(const FrameParams P) {
+  if (P.rlist[1]) return;
+  ShadowSrc src{&P, shadow_jobs(P), P.work[1], light_position(P)};
+  persistent_trace<kIters, kTraceThreads>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
+}
+
 template <bool kThroughput>
 __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
     k_frame(const FrameParams P) {
+  if (P.raster && P.rlist[1] == 0u) return;  // the raster kernels made this frame
   TracerT<kTraceThreads> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
@@ -656,6 +1074,23 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   }
   cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
+  if (P.raster) {
+    static int blocks_s = 0, blocks_t = 0;
+    if (!blocks_s) {
+      blocks_s = persistent_blocks(k_shadow);
+      blocks_t = persistent_blocks(k_raster_test, kRasterThreads);
+    }
+    e = cudaMemsetAsync(P.work, 0, 4 * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P.keys, 0xff, sizeof(unsigned long long) * (size_t)P.w * P.h, st);
+    if (e != cudaSuccess) return e;
+    k_raster_setup<<<1, 128, 0, st>>>(P);
+    k_raster<<<(P.raster_total + kRasterThreads - 1) / kRasterThreads, kRasterThreads, 0, st>>>(P);
+    k_raster_large<<<dim3(16, 64), kRasterThreads, 0, st>>>(P);
+    k_raster_test<<<blocks_t, kRasterThreads, 0, st>>>(P);
+    k_resolve<<<(unsigned)(((size_t)rw * rh + kResolveThreads - 1) / kResolveThreads), kResolveThreads, 0, st>>>(P);
+    k_shadow<<<blocks_s, kTraceThreads, 0, st>>>(P);
+    // k_frame below returns at once unless the large-triangle list overflowed
+  }
   if (primary_items(P) >= J3DG_THROUGHPUT_ITEMS)
     k_frame<true><<<blocks_t, kTraceThreads, 0, st>>>(P);
   else

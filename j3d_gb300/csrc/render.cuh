@@ -9,6 +9,19 @@ namespace j3dg {
 
 struct DevInst;
 
+// Primary hits by conservative rasterisation (FrameParams::raster): per
+// instance, the object -> clip matrix of the frame's camera and the slab
+// padding of the camera's rays in object space.
+struct RasterInst {
+  float M[16];     // clip = proj * cs_inv * inst.cs (column-major)
+  float pad;       // make_ray's padding for rays from the camera
+  uint32_t first;  // first work item of the instance (prefix of nt)
+  uint32_t nt;
+  uint32_t unused;
+};
+static const uint32_t kRasterListHeader = 8;  // words before the large-triangle entries
+static const uint32_t kRasterEntryWords = 8;  // inst, slot, x0, y0, x1, y1, -, -
+
 struct FrameParams {
   const DevInst* inst;
   uint32_t n_inst;
@@ -29,6 +42,18 @@ struct FrameParams {
   float4* queue;    // shadow jobs: (origin, pixel index bits), (direction, 0); w*h entries
   uint32_t* status;
   unsigned long long* counters;  // optional [node visits, triangle tests]
+  // raster != 0: launch_render first fills keys[w*h] with the minimum of
+  // (t bits << 32 | inst << id_bits | triangle id) over each pixel's
+  // accepted triangles (id_bits 32: one instance), and k_frame takes the
+  // primary hit from there instead of tracing
+  uint32_t raster;
+  uint32_t id_bits;
+  uint32_t raster_total;  // triangles of all instances
+  uint32_t rlist_cap;     // large-triangle entries that fit rlist
+  float proj[16];         // the canvas projection
+  unsigned long long* keys;
+  RasterInst* rinst;      // n_inst entries
+  uint32_t* rlist;        // [0] entries pushed, [1] overflow, [2] candidates queued; entries from kRasterListHeader
 };
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);

@@ -83,6 +83,13 @@ class Context:
     def set_batch_block(self, threads: int) -> None:
         _check(self.h, lib().j3dg_ctx_set_batch_block(self.h, threads))
 
+    def set_primary_mode(self, mode: int) -> None:
+        """How canvas frames find primary hits: PRIMARY_AUTO (default),
+        PRIMARY_TRACE (BVH walk per pixel) or PRIMARY_RASTER (projected
+        triangle boxes, the traversal's own ray / triangle test per covered
+        pixel); the hits are the same."""
+        _check(self.h, lib().j3dg_ctx_set_primary_mode(self.h, mode))
+
     def read_counters(self, reset: bool = True) -> tuple[int, int]:
         out = (C.c_uint64 * 2)()
         _check(self.h, lib().j3dg_ctx_read_counters(self.h, out, 1 if reset else 0))
@@ -491,6 +498,10 @@ class Canvas:
 
     def set_pixels(self, px) -> None:
         _check(self.ctx.h, lib().j3dg_canvas_set_pixels(self.h, vptr(px)))
+
+    def last_primary(self) -> int:
+        """PRIMARY_TRACE or PRIMARY_RASTER: how the last frame found its primary hits."""
+        return int(lib().j3dg_canvas_last_primary(self.h))
 
     def count_hits(self) -> tuple[int, int]:
         """(pixels with a hit, of which in shadow), counted on the device."""

@@ -45,3 +45,13 @@ def gpu_ctx(product_lib):
     ctx = Context(0)
     yield ctx
     ctx.close()
+
+
+@pytest.fixture(params=["trace", "raster"])
+def primary(request, gpu_ctx):
+    """Runs a frame test once with traced and once with rasterised primary
+    hits (the context's mode is restored to automatic afterwards)."""
+    from j3d_gb300 import PRIMARY_AUTO, PRIMARY_RASTER, PRIMARY_TRACE
+    gpu_ctx.set_primary_mode(PRIMARY_TRACE if request.param == "trace" else PRIMARY_RASTER)
+    yield request.param
+    gpu_ctx.set_primary_mode(PRIMARY_AUTO)

@@ -18,8 +18,10 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 I16 = np.eye(4, dtype=np.float32).reshape(16)
 
 
-def gpu_frame(ctx, sc, w, h, st, vfov=60.0, kind=0, background=True):
-    from j3d_gb300 import Canvas, Matcap, camera_for_vfov
+def gpu_frame(ctx, sc, w, h, st, vfov=60.0, kind=0, background=True, expect=None):
+    """Renders one frame; expect: the primary-hit method the frame must have
+    used ("trace" / "raster"), or None."""
+    from j3d_gb300 import PRIMARY_RASTER, PRIMARY_TRACE, Canvas, Matcap, camera_for_vfov
     cv = Canvas(ctx, w, h)
     cv.set_camera(camera_for_vfov(vfov))
     if background:
@@ -27,6 +29,8 @@ def gpu_frame(ctx, sc, w, h, st, vfov=60.0, kind=0, background=True):
     cv.update_settings(st)
     mc = Matcap.make(ctx, kind)
     cv.render_frame(sc, mc)
+    if expect is not None:
+        assert cv.last_primary() == {"trace": PRIMARY_TRACE, "raster": PRIMARY_RASTER}[expect]
     return cv.get_pixels(), cv.get_image(), cv, mc
 
 
@@ -43,7 +47,7 @@ def gst(**kw):
     return settings(**kw)
 
 
-def test_icosphere_config0_parity_and_golden(gpu_ctx, oracle_mod):
+def test_icosphere_config0_parity_and_golden(gpu_ctx, oracle_mod, primary):
     from j3d_gb300 import workloads as W
     O = oracle_mod
     wl = W.config0()
@@ -57,7 +61,7 @@ def test_icosphere_config0_parity_and_golden(gpu_ctx, oracle_mod):
     gold = json.loads((GOLDEN / "golden.json").read_text())["icosphere_L6_1024x768"]
     sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
     for mode, kw in (("plain", dict(shadow=True, edges=False)), ("edges", dict(shadow=True, edges=True))):
-        gp, gi, cv, mc = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(**kw))
+        gp, gi, cv, mc = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(**kw), expect=primary)
         assert np.array_equal(cv.get_projection()[0], P)
         op, oi = oracle_frame(O, m, views[0], wl.width, wl.height, O.settings(**kw))
         compare_gbuffers(gp, op, f"config0 {mode}")
@@ -86,7 +90,7 @@ def test_icosphere_config0_golden_with_lbvh_tree(gpu_ctx):
 
 @pytest.mark.parametrize("leaf,build", [(1, "lbvh"), (2, "lbvh"), (4, "lbvh"), (8, "lbvh"), (1, "ploc"),
                                         (2, "ploc"), (8, "ploc")])
-def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build):
+def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build, primary):
     from j3d_gb300 import workloads as W
     O = oracle_mod
     V, T = W.torus(300, 150, seed=W.SEED_BASE + 1)
@@ -96,7 +100,7 @@ def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build):
     for i, p in enumerate(poses):
         mesh, sc = gpu_scene(gpu_ctx, V, T, p, leaf=leaf, build=build) if mesh is None else (mesh, sc)
         sc.set_pose(p)
-        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 480, 270, gst(shadow=True, edges=False))
+        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 480, 270, gst(shadow=True, edges=False), expect=primary)
         op, oi = oracle_frame(O, m, views[i], 480, 270, O.settings(shadow=True, edges=False))
         assert compare_gbuffers(gp, op, f"torus cam {i}") == 0
         assert np.array_equal(gi, oi)
@@ -104,7 +108,7 @@ def test_torus_cameras_parity(gpu_ctx, oracle_mod, leaf, build):
 
 
 @pytest.mark.parametrize("case", ["inside_box", "looking_away", "off_centre"])
-def test_camera_placements_match_oracle(gpu_ctx, oracle_mod, case):
+def test_camera_placements_match_oracle(gpu_ctx, oracle_mod, case, primary):
     """Frames with the camera inside the mesh's box (in the torus hole),
     looking away from the mesh (every ray misses), or with the mesh across
     the image edge equal the oracle's."""
@@ -124,7 +128,9 @@ def test_camera_placements_match_oracle(gpu_ctx, oracle_mod, case):
     hits = 0
     for i, p in enumerate(poses):
         sc.set_pose(p)
-        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 320, 200, gst(shadow=True, edges=False))
+        # a camera inside the mesh's box, or facing away, has triangles behind it: traced
+        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 320, 200, gst(shadow=True, edges=False),
+                                 expect="trace" if case in ("inside_box", "looking_away") else primary)
         op, oi = oracle_frame(O, m, views[i], 320, 200, O.settings(shadow=True, edges=False))
         assert compare_gbuffers(gp, op, f"{case} cam {i}") == 0
         assert np.array_equal(gi, oi)
@@ -136,7 +142,7 @@ def test_camera_placements_match_oracle(gpu_ctx, oracle_mod, case):
 
 
 @pytest.mark.parametrize("mode", ["wireframe", "one_bit", "noshadow_edges", "shading_off"])
-def test_shading_modes(gpu_ctx, oracle_mod, mode):
+def test_shading_modes(gpu_ctx, oracle_mod, mode, primary):
     from j3d_gb300 import workloads as W
     O = oracle_mod
     V, T = W.icosphere(4)
@@ -148,10 +154,53 @@ def test_shading_modes(gpu_ctx, oracle_mod, mode):
     mesh, sc = gpu_scene(gpu_ctx, V, T, pose)
     m, views, _ = oracle_scene(O, V, T, [pose], 320, 200)
     for kind in (0, 3):
-        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 320, 200, gst(**kw), kind=kind)
+        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, 320, 200, gst(**kw), kind=kind, expect=primary)
         op, oi = oracle_frame(O, m, views[0], 320, 200, O.settings(**kw), kind=kind)
         compare_gbuffers(gp, op, mode)
         compare_rgba(gi, oi, 1 if "edges" in mode else 0, mode)
+
+
+@pytest.mark.parametrize("case", ["large", "overflow", "duplicates"])
+def test_raster_large_triangles_overflow_and_ties(gpu_ctx, oracle_mod, case):
+    """Rasterised primary hits against the oracle where the raster takes its
+    other routes: triangles with many candidate pixels (the pixel-parallel
+    list), more such triangles than the list holds on a 16x16 canvas (the
+    frame is traced on the device instead), and every triangle twice (equal
+    t everywhere: the smaller triangle id must win, as in the traversal)."""
+    from j3d_gb300 import PRIMARY_AUTO, PRIMARY_RASTER, workloads as W
+    O = oracle_mod
+    if case == "large":
+        V, T = W.icosphere(1)
+        w, h = 320, 200
+    elif case == "overflow":
+        rng = np.random.default_rng(7)
+        k = np.arange(400, dtype=np.float32)
+        base = np.array([[-2.0, -2.0, 0.0], [2.0, -2.0, 0.0], [0.0, 2.0, 0.0]], np.float32)
+        V = (base[None] + rng.uniform(-0.2, 0.2, size=(400, 3, 3)).astype(np.float32))
+        V[:, :, 2] = -0.002 * k[:, None] + rng.uniform(-5e-4, 5e-4, size=(400, 3)).astype(np.float32)
+        V = V.reshape(-1, 3).astype(np.float32)
+        T = np.arange(1200, dtype=np.uint32).reshape(400, 3)
+        w, h = 16, 16
+    else:
+        V, T = W.icosphere(3, W.SEED_BASE + 9)
+        T = np.concatenate([T, T]).astype(np.uint32)
+        w, h = 320, 200
+    pose = W.translation(0.1, -0.05, 2.6)
+    mesh, sc = gpu_scene(gpu_ctx, V, T, pose)
+    m, views, _ = oracle_scene(O, V, T, [pose], w, h)
+    gpu_ctx.set_primary_mode(PRIMARY_RASTER)
+    try:
+        for kw in (dict(shadow=True, edges=False), dict(shadow=True, edges=True)):
+            gp, gi, _, _ = gpu_frame(gpu_ctx, sc, w, h, gst(**kw), expect="raster")
+            op, oi = oracle_frame(O, m, views[0], w, h, O.settings(**kw))
+            assert compare_gbuffers(gp, op, case) == 0
+            compare_rgba(gi, oi, 1 if kw["edges"] else 0, case)
+            hit = gp["object_id"] != NO_ID
+            assert hit.mean() > 0.2
+            if case == "duplicates":
+                assert (gp["object_id"][hit] < T.shape[0] // 2).all()
+    finally:
+        gpu_ctx.set_primary_mode(PRIMARY_AUTO)
 
 
 def test_ray_batches_match_oracle(gpu_ctx, oracle_mod):
@@ -227,8 +276,8 @@ def test_builder_edge_cases_match_brute_force(gpu_ctx, oracle_mod, case):
     assert hg["found"].any()
 
 
-def test_update_canvas_rect_empty_and_null_scene(gpu_ctx, oracle_mod):
-    from j3d_gb300 import Canvas, Matcap, Scene, camera_for_vfov, workloads as W
+def test_update_canvas_rect_empty_and_null_scene(gpu_ctx, oracle_mod, primary):
+    from j3d_gb300 import PRIMARY_RASTER, PRIMARY_TRACE, Canvas, Matcap, Scene, camera_for_vfov, workloads as W
     O = oracle_mod
     V, T = W.icosphere(3)
     pose = W.translation(0, 0, 3)
@@ -238,6 +287,7 @@ def test_update_canvas_rect_empty_and_null_scene(gpu_ctx, oracle_mod):
     cv.set_camera(camera_for_vfov(60.0))
     cv.update_settings(gst(shadow=True, edges=False))
     cv.update_canvas(-5, 7, 50, 1000, sc)  # clamped like canvas.cpp:681-698
+    assert cv.last_primary() == (PRIMARY_TRACE if primary == "trace" else PRIMARY_RASTER)
     op = O.fresh_pixels(96, 64)
     O.update_canvas(op, [(m, I16, 1)], views[0], O.settings(shadow=True, edges=False), rect=(0, 7, 50, 63))
     assert compare_gbuffers(cv.get_pixels(), op, "rect") == 0
@@ -262,8 +312,8 @@ def test_update_canvas_rect_empty_and_null_scene(gpu_ctx, oracle_mod):
     compare_rgba(cv.get_image(), oim, 1, "to_image_from")
 
 
-def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod):
-    from j3d_gb300 import Canvas, Matcap, Mesh, Scene, camera_for_vfov, workloads as W
+def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod, primary):
+    from j3d_gb300 import PRIMARY_RASTER, PRIMARY_TRACE, Canvas, Matcap, Mesh, Scene, camera_for_vfov, workloads as W
     O = oracle_mod
     V, T = W.icosphere(4, W.SEED_BASE + 5)
     rng = np.random.default_rng(2)
@@ -303,6 +353,7 @@ def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod):
         cv.update_settings(gst(**kw))
         mc = Matcap.make(gpu_ctx, 0)
         cv.render_frame(sc, mc)
+        assert cv.last_primary() == (PRIMARY_TRACE if primary == "trace" else PRIMARY_RASTER)
         op, oi = oracle_frame(O, None, v, 400, 300, O.settings(**kw), objs=objs)
         gp = cv.get_pixels()
         compare_gbuffers(gp, op, "textured")
@@ -311,7 +362,7 @@ def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod):
         compare_rgba(cv.get_image(), oi, 1 if kw.get("edges") else 0, "textured")
 
 
-def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod):
+def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod, primary):
     """28.09M-triangle torus at 1920x1080, the 32 cameras of the benchmark:
     hit and shadowed pixels of every frame equal the oracle's full-frame
     counts (tests/golden/traffic.json, made by make_traffic.py), and so does
@@ -327,7 +378,7 @@ def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod):
     hits, shadowed = [], []
     for pose in wl.poses:
         sc.set_pose(pose)
-        gp, _, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
+        gp, _, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False), expect=primary)
         hits.append(int((gp["object_id"] != NO_ID).sum()))
         shadowed.append(int(((gp["mark"] & 1) != 0).sum()))
     assert hits == ref["hit_pixels"] and shadowed == ref["shadowed_pixels"]

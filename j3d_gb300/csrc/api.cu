@@ -33,7 +33,7 @@ const uint32_t kInstSlots = 8;
 
 // canvas scratch per pixel: raster keys, shadow jobs and tables during a
 // frame; the point-cloud splat's depth keys after it
-const size_t kQueueBytesPerPixel = 48;
+const size_t kQueueBytesPerPixel = 48, kQueueBytesFixed = 16384;
 
 struct CtxExtra {
   std::vector<DevInst> last;  // the table in the most recent slot
@@ -298,7 +298,7 @@ void setup_raster(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s) {
   const uint64_t px = (uint64_t)(P.x1 - P.x0 + 1) * (uint64_t)(P.y1 - P.y0 + 1);
   if (mode == J3DG_PRIMARY_AUTO && (!kAutoRaster || (double)total > kRasterTrisPerPixel * (double)px)) return;
   // keys (8 B per pixel), shadow jobs (32 B per pixel), instance table, list
-  const size_t npx = (size_t)cv->w * cv->h, bytes = kQueueBytesPerPixel * npx;
+  const size_t npx = (size_t)cv->w * cv->h, bytes = kQueueBytesPerPixel * npx + kQueueBytesFixed;
   const size_t off_inst = (40 * npx + 255) & ~size_t(255);
   const size_t off_list = (off_inst + sizeof(j3dg::RasterInst) * n + 255) & ~size_t(255);
   const size_t min_entries = 16;
@@ -345,7 +345,7 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
     CK(c, cudaMallocFromPoolAsync(&cv->d_pixels, sizeof(j3dg_pixel) * n, pool, S(c)), "canvas");
     CK(c, cudaMallocFromPoolAsync((void**)&cv->d_image, sizeof(uint32_t) * n, pool, S(c)), "canvas");
     CK(c, cudaMallocFromPoolAsync((void**)&cv->d_background, sizeof(uint32_t) * n, pool, S(c)), "canvas");
-    CK(c, cudaMallocFromPoolAsync(&cv->d_queue, kQueueBytesPerPixel * n, pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync(&cv->d_queue, kQueueBytesPerPixel * n + kQueueBytesFixed, pool, S(c)), "canvas");
     CK(c, cudaMallocFromPoolAsync((void**)&cv->d_work, 4 * sizeof(uint32_t), pool, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_image, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_background, 0, sizeof(uint32_t) * n, S(c)), "canvas");

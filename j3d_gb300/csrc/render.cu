@@ -339,12 +339,14 @@ __device__ __forceinline__ uint32_t raster_key_low(const FrameParams& P, uint32_
 }
 
 // candidate queue: (pixel index, inst << id_bits | slot), in the shadow
-// jobs' space (free until k_resolve), 4 entries per canvas pixel
+// jobs' space (free until k_resolve), 4 entries per canvas pixel, cut into
+// kRasterStripes stripes with a counter each (warps append to the stripe of
+// their index, so no counter is contended by every warp)
 __device__ __forceinline__ uint2* raster_queue(const FrameParams& P) {
   return reinterpret_cast<uint2*>(P.keys + (size_t)P.w * P.h);
 }
-__device__ __forceinline__ uint32_t raster_queue_cap(const FrameParams& P) {
-  const size_t cap = 4 * (size_t)P.w * P.h;
+__device__ __forceinline__ uint32_t raster_stripe_cap(const FrameParams& P) {
+  const size_t cap = 4 * (size_t)P.w * P.h / kRasterStripes;
   return cap < 0xffffffffu ? (uint32_t)cap : 0xffffffffu;
 }
 
@@ -403,8 +405,8 @@ __global__ void k_raster_setup(const FrameParams P) {
     }
     P.rlist[0] = 0u;  // large triangles listed
     P.rlist[1] = 0u;  // list overflow
-    P.rlist[2] = 0u;  // candidates queued
   }
+  if (threadIdx.x < kRasterStripes) P.rlist[raster_stripe_counter(threadIdx.x)] = 0u;  // candidates per stripe
 }
 
 __device__ __forceinline__ uint32_t raster_instance(const FrameParams& P, uint32_t g) {
@@ -425,11 +427,8 @@ __device__ __forceinline__ uint32_t raster_instance(const FrameParams& P, uint32
 // corner's value plus the negative or positive parts of the three edge
 // terms; x / w over [x range] x [w range] (w > 0) is bounded by the four
 // corner quotients.
-__device__ __forceinline__ bool raster_rect(const FrameParams& P, const RasterInst& R, const float4* tris,
-                                            uint32_t slot, int& x0, int& y0, int& x1, int& y1) {
-  const float4 a = __ldg(tris + 3 * (size_t)slot);
-  const float4 b = __ldg(tris + 3 * (size_t)slot + 1);
-  const float4 c = __ldg(tris + 3 * (size_t)slot + 2);
+__device__ __forceinline__ bool raster_rect(const FrameParams& P, const RasterInst& R, const float4& a,
+                                            const float4& b, const float4& c, int& x0, int& y0, int& x1, int& y1) {
   const float e = 2.f * R.pad;
   const float lx = min3f(a.x, b.x, c.x) - e, ly = min3f(a.y, b.y, c.y) - e, lz = min3f(a.z, b.z, c.z) - e;
   const float dx = max3f(a.x, b.x, c.x) + e - lx, dy = max3f(a.y, b.y, c.y) + e - ly,
@@ -476,40 +475,71 @@ __device__ __forceinline__ bool raster_rect(const FrameParams& P, const RasterIn
   return x0 <= x1 && y0 <= y1;
 }
 
-// One thread per triangle of every instance; small candidate sets are
-// spread over the warp's lanes, large ones listed for k_raster_large.
-__global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameParams P) {
+// Persistent warps over chunks of 32 triangles (one per lane), the next
+// chunk's vertices loaded while the current one is projected. Small
+// candidate sets are queued for k_raster_test (or, when the warp's stripe is
+// full, tested by the warp itself with candidates spread over its lanes);
+// large ones are listed for k_raster_large.
+#ifndef J3DG_RASTER_MINBLOCKS
+#define J3DG_RASTER_MINBLOCKS 4
+#endif
+__global__ void __launch_bounds__(kRasterThreads, J3DG_RASTER_MINBLOCKS) k_raster(const FrameParams P) {
   const uint32_t lane = threadIdx.x & 31u;
-  {
-    const uint32_t g = blockIdx.x * kRasterThreads + threadIdx.x;
-    uint32_t cnt = 0, inst = 0, slot = 0;
+  const uint32_t warp_g = (blockIdx.x * kRasterThreads + threadIdx.x) >> 5;
+  const uint32_t n_warps = (gridDim.x * kRasterThreads) >> 5;
+  const uint32_t n_chunks = (P.raster_total + 31u) >> 5;
+  const uint32_t stripe = warp_g % kRasterStripes;
+  uint32_t* const stripe_count = P.rlist + raster_stripe_counter(stripe);
+  uint2* const queue = raster_queue(P) + (size_t)stripe * raster_stripe_cap(P);
+  const uint32_t cap = raster_stripe_cap(P);
+  float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na;
+  uint32_t n_inst = 0, n_slot = 0;
+  bool n_ok = false;
+  const auto fetch = [&](uint32_t chunk) {
+    const uint32_t g = (chunk << 5) + lane;
+    n_ok = false;
+    if (chunk < n_chunks && g < P.raster_total) {
+      n_inst = raster_instance(P, g);
+      const RasterInst& R = P.rinst[n_inst];
+      n_slot = g - R.first;
+      if (n_slot < R.nt) {
+        const float4* tr = P.inst[n_inst].tris + 3 * (size_t)n_slot;
+        na = __ldg(tr);
+        nb = __ldg(tr + 1);
+        nc = __ldg(tr + 2);
+        n_ok = true;
+      }
+    }
+  };
+  fetch(warp_g);
+  for (uint32_t chunk = warp_g; chunk < n_chunks; chunk += n_warps) {
+    const float4 a = na, b = nb, c = nc;
+    const uint32_t inst = n_inst, slot = n_slot;
+    const bool ok = n_ok;
+    fetch(chunk + n_warps);
+    uint32_t cnt = 0;
     int rx = 0, ry = 0, rw = 1;
-    if (g < P.raster_total) {
-      inst = raster_instance(P, g);
-      const RasterInst& R = P.rinst[inst];
-      slot = g - R.first;
-      int x0, y0, x1, y1;
-      if (slot < R.nt && raster_rect(P, R, P.inst[inst].tris, slot, x0, y0, x1, y1)) {
-        const uint64_t area = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
-        if (area <= kRasterSmall) {
-          cnt = (uint32_t)area;
-          rx = x0;
-          ry = y0;
-          rw = x1 - x0 + 1;
+    int x0, y0, x1, y1;
+    if (ok && raster_rect(P, P.rinst[inst], a, b, c, x0, y0, x1, y1)) {
+      const uint64_t area = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
+      if (area <= kRasterSmall) {
+        cnt = (uint32_t)area;
+        rx = x0;
+        ry = y0;
+        rw = x1 - x0 + 1;
+      } else {
+        const uint32_t k = atomicAdd(P.rlist, 1u);
+        if (k < P.rlist_cap) {
+          uint32_t* E = P.rlist + kRasterListHeader + (size_t)k * kRasterEntryWords;
+          *reinterpret_cast<uint4*>(E) = make_uint4(inst, slot, (uint32_t)x0, (uint32_t)y0);
+          *reinterpret_cast<uint4*>(E + 4) = make_uint4((uint32_t)x1, (uint32_t)y1, 0u, 0u);
         } else {
-          const uint32_t k = atomicAdd(P.rlist, 1u);
-          if (k < P.rlist_cap) {
-            uint32_t* E = P.rlist + kRasterListHeader + (size_t)k * kRasterEntryWords;
-            *reinterpret_cast<uint4*>(E) = make_uint4(inst, slot, (uint32_t)x0, (uint32_t)y0);
-            *reinterpret_cast<uint4*>(E + 4) = make_uint4((uint32_t)x1, (uint32_t)y1, 0u, 0u);
-          } else {
-            atomicOr(P.rlist + 1, 1u);
-          }
+          atomicOr(P.rlist + 1, 1u);
         }
       }
     }
-    // the warp's candidates, 32 at a time: candidate c belongs to the first
-    // lane whose inclusive count exceeds c
+    // candidate c of the warp belongs to the first lane whose inclusive
+    // count exceeds c
     uint32_t incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -517,59 +547,50 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const FrameParams P) 
       if ((int)lane >= o) incl += v;
     }
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    // queued for k_raster_test (one thread per candidate: the tests run with
-    // every lane busy), one atomic per block; what does not fit the queue is
-    // tested here
-    __shared__ uint32_t warp_total[kRasterThreads / 32], block_base;
-    const uint32_t warp = threadIdx.x >> 5;
-    if (lane == 31) warp_total[warp] = total;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t sum = 0;
-      for (int k = 0; k < kRasterThreads / 32; ++k) sum += warp_total[k];
-      block_base = sum ? atomicAdd(P.rlist + 2, sum) : 0u;
-    }
-    __syncthreads();
-    if (total == 0) return;
-    uint32_t qbase = block_base;
-    for (uint32_t k = 0; k < warp; ++k) qbase += warp_total[k];
-    const uint32_t cap = raster_queue_cap(P);
+    if (total == 0) continue;
+    uint32_t qbase = 0;
+    if (lane == 31) qbase = atomicAdd(stripe_count, total);
+    qbase = __shfl_sync(0xffffffffu, qbase, 31);
     for (uint32_t j = 0; j < cnt; ++j) {
       const uint32_t q = qbase + incl - cnt + j;
       if (q < cap)
-        raster_queue(P)[q] = make_uint2((uint32_t)(ry + (int)(j / (uint32_t)rw)) * P.w + (uint32_t)(rx + (int)(j % (uint32_t)rw)),
-                                        raster_key_low(P, inst, slot));
+        queue[q] = make_uint2((uint32_t)(ry + (int)(j / (uint32_t)rw)) * P.w + (uint32_t)(rx + (int)(j % (uint32_t)rw)),
+                              raster_key_low(P, inst, slot));
     }
-    if (qbase + total <= cap) return;
+    if (qbase + total <= cap) continue;
     for (uint32_t c0 = 0; c0 < total; c0 += 32) {
-      const uint32_t c = c0 + lane;
+      const uint32_t cc = c0 + lane;
       int own = 0;
 #pragma unroll
       for (int step = 16; step >= 1; step >>= 1) {
         const uint32_t v = __shfl_sync(0xffffffffu, incl, own + step - 1);
-        if (v <= c) own += step;
+        if (v <= cc) own += step;
       }
       const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, own), o_cnt = __shfl_sync(0xffffffffu, cnt, own);
       const uint32_t o_inst = __shfl_sync(0xffffffffu, inst, own), o_slot = __shfl_sync(0xffffffffu, slot, own);
       const int o_rx = __shfl_sync(0xffffffffu, rx, own), o_ry = __shfl_sync(0xffffffffu, ry, own);
       const int o_rw = __shfl_sync(0xffffffffu, rw, own);
-      if (c < total && qbase + c >= cap) {
-        const uint32_t j = c - (o_incl - o_cnt);
+      if (cc < total && qbase + cc >= cap) {
+        const uint32_t j = cc - (o_incl - o_cnt);
         raster_candidate(P, o_inst, o_slot, o_rx + (int)(j % (uint32_t)o_rw), o_ry + (int)(j / (uint32_t)o_rw));
       }
     }
   }
 }
 
-// The queued (pixel, triangle) candidates.
+// The queued (pixel, triangle) candidates, stripe by stripe.
 __global__ void __launch_bounds__(kRasterThreads) k_raster_test(const FrameParams P) {
   if (P.rlist[1]) return;
-  const uint32_t n = min(P.rlist[2], raster_queue_cap(P));
+  const uint32_t cap = raster_stripe_cap(P);
   const uint32_t mask = P.id_bits >= 32u ? 0xffffffffu : (1u << P.id_bits) - 1u;
-  for (uint32_t i = blockIdx.x * kRasterThreads + threadIdx.x; i < n; i += gridDim.x * kRasterThreads) {
-    const uint2 c = raster_queue(P)[i];
-    const uint32_t inst = P.id_bits >= 32u ? 0u : c.y >> P.id_bits;
-    raster_candidate(P, inst, c.y & mask, (int)(c.x % P.w), (int)(c.x / P.w));
+  const uint2* queue = raster_queue(P);
+  for (uint32_t s = 0; s < kRasterStripes; ++s) {
+    const uint32_t n = min(P.rlist[raster_stripe_counter(s)], cap);
+    for (uint32_t i = blockIdx.x * kRasterThreads + threadIdx.x; i < n; i += gridDim.x * kRasterThreads) {
+      const uint2 c = queue[(size_t)s * cap + i];
+      const uint32_t inst = P.id_bits >= 32u ? 0u : c.y >> P.id_bits;
+      raster_candidate(P, inst, c.y & mask, (int)(c.x % P.w), (int)(c.x / P.w));
+    }
   }
 }
 
@@ -1075,16 +1096,18 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (P.raster) {
-    static int blocks_s = 0, blocks_t = 0;
+    static int blocks_s = 0, blocks_t = 0, blocks_r = 0;
     if (!blocks_s) {
       blocks_s = persistent_blocks(k_shadow);
       blocks_t = persistent_blocks(k_raster_test, kRasterThreads);
+      blocks_r = persistent_blocks(k_raster, kRasterThreads);
     }
     e = cudaMemsetAsync(P.work, 0, 4 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(P.keys, 0xff, sizeof(unsigned long long) * (size_t)P.w * P.h, st);
     if (e != cudaSuccess) return e;
     k_raster_setup<<<1, 128, 0, st>>>(P);
-    k_raster<<<(P.raster_total + kRasterThreads - 1) / kRasterThreads, kRasterThreads, 0, st>>>(P);
+    const uint32_t need = (P.raster_total + kRasterThreads - 1) / kRasterThreads;
+    k_raster<<<need < (uint32_t)blocks_r ? need : (uint32_t)blocks_r, kRasterThreads, 0, st>>>(P);
     k_raster_large<<<dim3(16, 64), kRasterThreads, 0, st>>>(P);
     k_raster_test<<<blocks_t, kRasterThreads, 0, st>>>(P);
     k_resolve<<<(unsigned)(((size_t)rw * rh + kResolveThreads - 1) / kResolveThreads), kResolveThreads, 0, st>>>(P);

@@ -19,7 +19,14 @@ struct RasterInst {
   uint32_t nt;
   uint32_t unused;
 };
-static const uint32_t kRasterListHeader = 8;  // words before the large-triangle entries
+// rlist: [0] large triangles listed, [1] list overflow, then the count of
+// candidates queued in each stripe of the queue, one 128-byte line apart (so
+// that the stripes' atomics go to different L2 lines); entries from
+// kRasterListHeader
+static const uint32_t kRasterStripes = 64;
+static const uint32_t kRasterCounterStride = 32;
+static const uint32_t kRasterListHeader = 32 + kRasterStripes * kRasterCounterStride;
+__host__ __device__ inline uint32_t raster_stripe_counter(uint32_t s) { return 32 + s * kRasterCounterStride; }
 static const uint32_t kRasterEntryWords = 8;  // inst, slot, x0, y0, x1, y1, -, -
 
 struct FrameParams {
@@ -53,7 +60,7 @@ struct FrameParams {
   float proj[16];         // the canvas projection
   unsigned long long* keys;
   RasterInst* rinst;      // n_inst entries
-  uint32_t* rlist;        // [0] entries pushed, [1] overflow, [2] candidates queued; entries from kRasterListHeader
+  uint32_t* rlist;        // counters, then the large-triangle entries (kRasterListHeader)
 };
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);

@@ -293,6 +293,21 @@ def run_own(args):
     ctx.synchronize()
     frame_ms = [a.elapsed_time(b) for a, b in zip(fe0, fe1)]
 
+    # the same frames with the opt-in rasterised primary hits (identical
+    # images; the default traces because this measures slower): one warm-up
+    # step and one timed step, outside the timed region above
+    from j3d_gb300 import PRIMARY_AUTO, PRIMARY_RASTER
+    ctx.set_primary_mode(PRIMARY_RASTER)
+    step()
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    step()
+    r1.record(stream)
+    r1.synchronize()
+    raster_frame_ms = r0.elapsed_time(r1) / N_CAMERAS if cv.last_primary() == PRIMARY_RASTER else None
+    ctx.set_primary_mode(PRIMARY_AUTO)
+
     # end to end through the C-ABI: render + G-buffer and image into pinned
     # host memory; two canvases alternate so that frame k's download (copy
     # stream) overlaps frame k+1's render (context stream)
@@ -368,6 +383,7 @@ def run_own(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced torus, no dataset)",
         "config": dict(CONFIG, parallelism="replicas" if ws > 1 else "single GPU",
                        frame_ms_mean=round(ms / N_CAMERAS, 4), frame_ms_p50=round(float(np.median(frame_ms)), 4),
+                       raster_primary_frame_ms_mean=None if raster_frame_ms is None else round(raster_frame_ms, 4),
                        rays_per_step=rays_per_step, shadow_ray_fraction=round(sum(shadow_rays) / (prim * N_CAMERAS), 4),
                        bvh_build_ms=round(build_ms, 3), bvh_first_build_wall_s=round(build_wall, 3),
                        bvh_nodes=info.n_nodes, bvh_depth=info.max_depth, leaf_size=args.leaf,

@@ -483,6 +483,8 @@ __device__ __forceinline__ bool raster_rect(const FrameParams& P, const RasterIn
 #ifndef J3DG_RASTER_MINBLOCKS
 #define J3DG_RASTER_MINBLOCKS 4
 #endif
+// kOne: a single instance, whose matrix and padding are read once per block
+template <bool kOne>
 __global__ void __launch_bounds__(kRasterThreads, J3DG_RASTER_MINBLOCKS) k_raster(const FrameParams P) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t warp_g = (blockIdx.x * kRasterThreads + threadIdx.x) >> 5;
@@ -495,19 +497,34 @@ __global__ void __launch_bounds__(kRasterThreads, J3DG_RASTER_MINBLOCKS) k_raste
   float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na;
   uint32_t n_inst = 0, n_slot = 0;
   bool n_ok = false;
+  // kOne: the instance's matrix and padding in shared memory (broadcast reads)
+  __shared__ RasterInst R1;
+  if (kOne) {
+    if (threadIdx.x < sizeof(RasterInst) / 4)
+      reinterpret_cast<uint32_t*>(&R1)[threadIdx.x] = reinterpret_cast<const uint32_t*>(P.rinst)[threadIdx.x];
+    __syncthreads();
+  }
+  const float4* const tris1 = kOne ? P.inst[0].tris : nullptr;
   const auto fetch = [&](uint32_t chunk) {
     const uint32_t g = (chunk << 5) + lane;
     n_ok = false;
     if (chunk < n_chunks && g < P.raster_total) {
-      n_inst = raster_instance(P, g);
-      const RasterInst& R = P.rinst[n_inst];
-      n_slot = g - R.first;
-      if (n_slot < R.nt) {
-        const float4* tr = P.inst[n_inst].tris + 3 * (size_t)n_slot;
+      const float4* tr;
+      if (kOne) {
+        n_slot = g;
+        tr = tris1 + 3 * (size_t)g;
+        n_ok = g < R1.nt;
+      } else {
+        n_inst = raster_instance(P, g);
+        const RasterInst& R = P.rinst[n_inst];
+        n_slot = g - R.first;
+        tr = P.inst[n_inst].tris + 3 * (size_t)n_slot;
+        n_ok = n_slot < R.nt;
+      }
+      if (n_ok) {
         na = __ldg(tr);
         nb = __ldg(tr + 1);
         nc = __ldg(tr + 2);
-        n_ok = true;
       }
     }
   };
@@ -520,7 +537,7 @@ __global__ void __launch_bounds__(kRasterThreads, J3DG_RASTER_MINBLOCKS) k_raste
     uint32_t cnt = 0;
     int rx = 0, ry = 0, rw = 1;
     int x0, y0, x1, y1;
-    if (ok && raster_rect(P, P.rinst[inst], a, b, c, x0, y0, x1, y1)) {
+    if (ok && raster_rect(P, kOne ? R1 : P.rinst[inst], a, b, c, x0, y0, x1, y1)) {
       const uint64_t area = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
       if (area <= kRasterSmall) {
         cnt = (uint32_t)area;
@@ -551,11 +568,17 @@ __global__ void __launch_bounds__(kRasterThreads, J3DG_RASTER_MINBLOCKS) k_raste
     uint32_t qbase = 0;
     if (lane == 31) qbase = atomicAdd(stripe_count, total);
     qbase = __shfl_sync(0xffffffffu, qbase, 31);
-    for (uint32_t j = 0; j < cnt; ++j) {
-      const uint32_t q = qbase + incl - cnt + j;
-      if (q < cap)
-        queue[q] = make_uint2((uint32_t)(ry + (int)(j / (uint32_t)rw)) * P.w + (uint32_t)(rx + (int)(j % (uint32_t)rw)),
-                              raster_key_low(P, inst, slot));
+    {
+      const uint32_t key = raster_key_low(P, inst, slot);
+      uint32_t q = qbase + incl - cnt, pix = (uint32_t)ry * P.w + (uint32_t)rx;
+      int dx = 0;
+      for (uint32_t j = 0; j < cnt; ++j, ++q) {
+        if (q < cap) queue[q] = make_uint2(pix + (uint32_t)dx, key);
+        if (++dx == rw) {
+          dx = 0;
+          pix += P.w;
+        }
+      }
     }
     if (qbase + total <= cap) continue;
     for (uint32_t c0 = 0; c0 < total; c0 += 32) {
@@ -1100,14 +1123,17 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
     if (!blocks_s) {
       blocks_s = persistent_blocks(k_shadow);
       blocks_t = persistent_blocks(k_raster_test, kRasterThreads);
-      blocks_r = persistent_blocks(k_raster, kRasterThreads);
+      blocks_r = persistent_blocks(k_raster<false>, kRasterThreads);
     }
     e = cudaMemsetAsync(P.work, 0, 4 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(P.keys, 0xff, sizeof(unsigned long long) * (size_t)P.w * P.h, st);
     if (e != cudaSuccess) return e;
     k_raster_setup<<<1, 128, 0, st>>>(P);
     const uint32_t need = (P.raster_total + kRasterThreads - 1) / kRasterThreads;
-    k_raster<<<need < (uint32_t)blocks_r ? need : (uint32_t)blocks_r, kRasterThreads, 0, st>>>(P);
+    if (P.n_inst == 1)
+      k_raster<true><<<need < (uint32_t)blocks_r ? need : (uint32_t)blocks_r, kRasterThreads, 0, st>>>(P);
+    else
+      k_raster<false><<<need < (uint32_t)blocks_r ? need : (uint32_t)blocks_r, kRasterThreads, 0, st>>>(P);
     k_raster_large<<<dim3(16, 64), kRasterThreads, 0, st>>>(P);
     k_raster_test<<<blocks_t, kRasterThreads, 0, st>>>(P);
     k_resolve<<<(unsigned)(((size_t)rw * rh + kResolveThreads - 1) / kResolveThreads), kResolveThreads, 0, st>>>(P);

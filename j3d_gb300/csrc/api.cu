@@ -237,7 +237,6 @@ void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevI
   P.shading = cv->settings.shading;
   P.status = cv->ctx->d_status;
   P.work = cv->d_work;
-  P.queue = (float4*)cv->d_queue;
   CtxExtra& X = all(cv->ctx)->ex;
   P.counters = X.counting ? X.d_counters : nullptr;
 }
@@ -245,9 +244,10 @@ void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevI
 // Rasterised primary hits (FrameParams::raster) when the frame allows them:
 // every object's box in front of the camera (so no triangle's box reaches
 // the camera plane), keys that hold (object, triangle id), and room for the
-// tables in the canvas's 48-byte-per-pixel scratch; in the automatic mode
-// also at most kRasterTrisPerPixel triangles per pixel of the rectangle
-// (reading every triangle once then costs less than tracing every pixel).
+// tables in the canvas's 48-byte-per-pixel scratch. The automatic mode, if
+// kAutoRaster enabled it, would also want at most kRasterTrisPerPixel
+// triangles per pixel of the rectangle (reading every triangle once then
+// costs less than tracing every pixel).
 const double kRasterTrisPerPixel = 24.0;
 // the automatic mode traces: on the 28M-triangle torus at 1920x1080 the
 // rasterised frame measured slower than the traced one (with and without

@@ -11,7 +11,7 @@
 // rasteriser with a strict depth test gives. After each cloud a resolve pass
 // writes the winners' G-buffer fields and colours and marks them as canvas
 // (low bits all ones), so later clouds test against them. The keys live in
-// the canvas's shadow-ray queue, which is idle between frames.
+// the canvas's frame scratch, which is idle between frames.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -257,7 +257,7 @@ int j3dg_canvas_render_pointclouds(j3dg_canvas* cv, const j3dg_scene* s, const j
   if (n_pcs == 0 || npix == 0) return J3DG_OK;
   cudaSetDevice(c->device);
   j3dg::canvas_writable(cv);
-  // the shadow-ray queue (32 bytes per pixel) is idle between frames
+  // the canvas's frame scratch (48 bytes per pixel) is idle between frames
   unsigned long long* keys = (unsigned long long*)cv->d_queue;
   const unsigned pix_blocks = (unsigned)((npix + 255) / 256);
   k_zinit<<<pix_blocks, 256, 0, S(c)>>>((const j3dg_pixel*)cv->d_pixels, npix, keys);

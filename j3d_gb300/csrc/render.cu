@@ -304,18 +304,19 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
 // Primary hits without traversal. A ray can only pass the bounds gate of a
 // triangle if it passes through the triangle's box widened by the ray's
 // slab padding, so every pixel whose ray can accept a triangle has its
-// centre inside the screen rectangle of that widened box's eight projected
-// corners. Each triangle takes those pixels (the rectangle grown by
-// kRasterMargin pixels, far above the rounding of either the projection or
-// the pixel rays) as candidates and runs on each the traversal's own
-// Moller-Trumbore + gate with the pixel's own ray; accepted candidates go
-// into a per-pixel 64-bit atomicMin of (t, instance, triangle id). The
-// traversal's closest hit is the minimum of that same key over the same
-// accepted triangles, so the minima are equal; k_frame rebuilds the hit
-// record from the key. Triangles with more than kRasterSmall candidates
-// (and any whose box reaches the camera plane) go to a list that
-// k_raster_large covers pixel-parallel; if the list overflows, k_frame
-// traces the frame instead.
+// centre inside the screen rectangle of that widened box's projection
+// (bounded by interval arithmetic over the box). Each triangle takes those
+// pixels (the rectangle grown by kRasterMargin pixels, far above the
+// rounding of either the projection or the pixel rays) as candidates; each
+// candidate runs the traversal's own Moller-Trumbore + gate with the
+// pixel's own ray, and accepted ones go into a per-pixel 64-bit atomicMin of
+// (t, instance, triangle id). The traversal's closest hit is the minimum of
+// that same key over the same accepted triangles, so the minima are equal.
+// k_resolve rebuilds each hit from its key and runs the primary finish;
+// k_shadow traces the shadow rays it queued. Triangles with more than
+// kRasterSmall candidates (and any whose box reaches the camera plane) go
+// to a list that k_raster_large covers pixel-parallel; if the list
+// overflows, the raster kernels stand down and k_frame traces the frame.
 
 static const uint32_t kRasterSmall = 64;
 static const float kRasterMargin = 0.05f;

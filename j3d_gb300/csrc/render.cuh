@@ -45,8 +45,7 @@ struct FrameParams {
   uint32_t mw, mh, cavity;
   uint32_t shadow, textured, vertexcolors, shading;
   int shade_mode;  // 0: G-buffer only; 1: also plain shading into im (misses <- background)
-  uint32_t* work;   // [0] primary items taken, [1] shadow jobs queued, [2] shadow items taken
-  float4* queue;    // shadow jobs: (origin, pixel index bits), (direction, 0); w*h entries
+  uint32_t* work;   // [0] primary items taken; rasterised frames: [1] shadow jobs queued, [2] taken
   uint32_t* status;
   unsigned long long* counters;  // optional [node visits, triangle tests]
   // raster != 0: launch_render first fills keys[w*h] with the minimum of

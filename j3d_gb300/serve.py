@@ -60,8 +60,9 @@ class CanvasPool:
 
     @staticmethod
     def canvas_bytes(w: int, h: int) -> int:
-        # G-buffer 32 B + image 4 B + background 4 B + shadow queue 32 B per pixel
-        return w * h * 72
+        # per pixel: G-buffer 32 B + image 4 B + background 4 B + frame scratch
+        # 48 B; per canvas: 16 KB of scratch tables and 16 B of work counters
+        return w * h * 88 + 16384 + 16
 
     def take(self, res, settings):
         from .scene import Canvas
@@ -126,7 +127,7 @@ class RenderServer:
     def add_mesh(self, name: str, V, T, leaf_size: int = 2) -> bool:
         """Builds and keeps a mesh resident if its footprint fits the cap."""
         from .scene import Mesh
-        est = int(len(T)) * (48 + 16 + 12 + 40) + int(len(V)) * 12
+        est = int(len(T)) * (48 + 16 + 12 + 4 + 40) + int(len(V)) * 12
         if self.mesh_bytes + est > self.cap:
             return False
         m = Mesh(self.ctx, V, T, leaf_size)

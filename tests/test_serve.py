@@ -12,7 +12,7 @@ def test_poisson_requests_deterministic():
     assert [(r.mesh, r.resolution, r.arrival) for r in a] == [(r.mesh, r.resolution, r.arrival) for r in b]
     gaps = np.diff([r.arrival for r in a])
     assert (gaps > 0).all() and 0.5 / 400 < gaps.mean() < 2.0 / 400
-    assert CanvasPool.canvas_bytes(1920, 1080) == 1920 * 1080 * 72
+    assert CanvasPool.canvas_bytes(1920, 1080) == 1920 * 1080 * 88 + 16384 + 16
 
 
 def _server(ctx, cap, **kw):

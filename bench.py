@@ -113,91 +113,88 @@ class ClockSampler:
 
 
 class CpuRenderer:
-    """The oracle (port of j3d's CPU path: canvas::update_canvas + canvas_to_image
-    over a 4-wide binned-SAH BVH, row-parallel like pooled_parallel_for) on the
-    same mesh and cameras, timed on a bounded sample of rows."""
+    """The oracle (port of j3d's CPU path: canvas::render_scene's background
+    copy, update_canvas and canvas_to_image over a 4-wide binned-SAH BVH) on
+    the same mesh and cameras. Rows run on the oracle's persistent row pool
+    over all host cores, like pooled_parallel_for (canvas.cpp:765); frames
+    are whole 1920x1080 frames, timed as view.cpp:1263-1267 times them.
+    Inputs come from the oracle's own generators: this process never loads
+    the product library."""
 
-    def __init__(self, wl, n_threads: int):
+    def __init__(self, n_threads: int):
         import oracle.oracle as O
-        from j3d_gb300 import scene as S
-        self.O, self.wl, self.n_threads = O, wl, n_threads
-        self.m = O.Mesh(wl.vertices, wl.triangles, 4, n_threads)
+        import oracle.workloads as OW
+        self.O, self.n_threads = O, n_threads
+        V, T, self.poses, self.w, self.h = OW.config1(N_CAMERAS, W_, H_)
+        self.m = O.Mesh(V, T, 4, n_threads)
+        del V, T
         self.I16 = np.eye(4, dtype=np.float32).reshape(16)
-        mn, mx, self.diag = O.prepare_scene([(self.m.min_bb, self.m.max_bb)], [self.I16])
-        _, _, self.piv = O.unzoom(mn, mx, self.diag)
-        self.cam = O.camera_with_focal(S.lib().j3dg_focal_for_vfov(60.0, 0.768))
-        self.Pi = O.invert_projection_matrix(O.make_projection_matrix(self.cam, wl.width, wl.height))
+        mn, mx, diag = O.prepare_scene([(self.m.min_bb, self.m.max_bb)], [self.I16])
+        _, _, piv = O.unzoom(mn, mx, diag)
+        cam = O.camera_with_focal(OW.focal_for_vfov(60.0, 0.768))
+        Pi = O.invert_projection_matrix(O.make_projection_matrix(cam, self.w, self.h))
+        self.views = [O.view(p, O.invert_orthonormal(p), piv, diag, Pi, cam.near_clipping_plane) for p in self.poses]
         self.st = O.settings(shadow=True, edges=False)
         self.mc, self.cav = O.make_matcap(0)
+        self.bg = O.fill_background(self.w, self.h)
+        self.pix = O.fresh_pixels(self.w, self.h)
+        self.im = np.zeros((self.h, self.w), np.uint32)
 
-    def sample(self, cams, budget_s: float):
-        """Bands of 8 whole rows every 72 rows of each camera's frame, then the
-        bands shifted by 8 rows, ..., until the time budget is spent.
-        Returns (rays, seconds, node_visits, tri_tests, rows)."""
-        O, wl = self.O, self.wl
-        rays = visits = tests = rows_done = 0
-        secs = 0.0
-        views = []
-        for c in cams:
-            pose = wl.poses[c]
-            views.append(O.view(pose, O.invert_orthonormal(pose), self.piv, self.diag, self.Pi,
-                                self.cam.near_clipping_plane))
-        pix = O.fresh_pixels(wl.width, wl.height)
-        for shift in range(0, 72, 8):
-            for v in views:
-                for y0 in range(shift, wl.height, 72):
-                    y1 = min(wl.height - 1, y0 + 7)
-                    t0 = time.perf_counter()
-                    s = O.update_canvas(pix, [(self.m, self.I16, 1)], v, self.st, rect=(0, y0, wl.width - 1, y1),
-                                        n_threads=self.n_threads)
-                    band = np.ascontiguousarray(pix[y0:y1 + 1])
-                    im = np.zeros(band.shape, np.uint32)
-                    O.canvas_to_image(band, im, v, self.st, self.mc, self.cav)
-                    secs += time.perf_counter() - t0
-                    rays += s.rays
-                    visits += s.node_visits
-                    tests += s.tri_tests
-                    rows_done += y1 - y0 + 1
-                    if secs > budget_s:
-                        return rays, secs, visits, tests, rows_done
-        return rays, secs, visits, tests, rows_done
+    def frame(self, cam: int):
+        """One whole frame of camera `cam`: (rays, seconds, node visits, triangle tests)."""
+        O = self.O
+        self.pix[...] = O.fresh_pixels(self.w, self.h)
+        t0 = time.perf_counter()
+        _, _, s = O.render_frame(self.pix, self.im, self.bg, [(self.m, self.I16, 1)], self.views[cam], self.st,
+                                 self.mc, self.cav, n_threads=self.n_threads)
+        return s.rays, time.perf_counter() - t0, s.node_visits, s.tri_tests
+
+
+CPU_FRAMES_PER_STEP = 8  # 4 steps cover the 32 cameras once
 
 
 def run_reference(args):
-    """CPU arm: the oracle port of j3d's renderer on all host cores."""
+    """CPU arm: the oracle port of j3d's renderer on all host cores, whole
+    frames, CPU_FRAMES_PER_STEP cameras per step (step k renders cameras
+    8k .. 8k+7 mod 32, warm-up steps included in the count)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     import oracle.oracle as O
-    from j3d_gb300 import build as B, workloads as Wk
-    B.build()
     O.build()
-    wl = Wk.config1(N_CAMERAS, W_, H_)
     n_threads = os.cpu_count() or 1
-    cpu = CpuRenderer(wl, n_threads)
-    per_step = max(2.0, min(15.0, args.cpu_total / max(1, args.warmup + args.steps)))
-    vals = []
-    total_rays = total_visits = total_tests = 0
+    t0 = time.perf_counter()
+    cpu = CpuRenderer(n_threads)
+    setup_s = time.perf_counter() - t0
+    step_s, rays, visits, tests, frame_s = [], 0, 0, 0, []
     for i in range(args.warmup + args.steps):
-        r = cpu.sample(tuple((i + k) % N_CAMERAS for k in range(N_CAMERAS)), per_step)
+        cams = [(i * CPU_FRAMES_PER_STEP + k) % N_CAMERAS for k in range(CPU_FRAMES_PER_STEP)]
+        r = [cpu.frame(c) for c in cams]
         if i >= args.warmup:
-            vals.append(r[0] / r[1] / 1e6)
-            total_rays += r[0]
-            total_visits += r[2]
-            total_tests += r[3]
-    v = float(np.mean(vals))
+            step_s.append(sum(x[1] for x in r))
+            frame_s += [x[1] for x in r]
+            rays += sum(x[0] for x in r)
+            visits += sum(x[2] for x in r)
+            tests += sum(x[3] for x in r)
+    secs = float(np.sum(step_s))
+    v = rays / secs / 1e6
+    sample = (f"{CPU_FRAMES_PER_STEP} whole 1920x1080 frames per step (primary + shadow + plain shading, "
+              f"background copy included), cameras cycled over the 32; {args.steps} timed steps, {rays} rays in "
+              f"{secs:.2f} s on the oracle's persistent row pool over {n_threads} threads; the reference itself "
+              "cannot be built (jtk absent, SSE-only canvas)")
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / max(1, args.steps) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded displaced torus, no dataset)", "config": CONFIG,
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": n_threads, "kind": "port",
-                             "sample": f"per step up to {per_step:.1f} s of bands of 8 rows every 72 rows, "
-                                       "cycling over the 32 cameras' 1920x1080 frames (primary + shadow + "
-                                       f"shading), {total_rays} rays timed; the reference itself cannot be built "
-                                       "(jtk absent, SSE-only canvas)"},
+                             "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "bvh_build_s": round(cpu.m.build_seconds, 3),
-            "oracle_node_visits_per_ray": round(total_visits / max(1, total_rays), 4),
-            "oracle_tri_tests_per_ray": round(total_tests / max(1, total_rays), 4)}
+            "details": {"frame_ms_mean": round(float(np.mean(frame_s)) * 1e3, 2),
+                        "frame_ms_p50": round(float(np.median(frame_s)) * 1e3, 2),
+                        "oracle_bvh_build_s": round(cpu.m.build_seconds, 3),
+                        "setup_s": round(setup_s, 2),
+                        "oracle_node_visits_per_ray": round(visits / max(1, rays), 4),
+                        "oracle_tri_tests_per_ray": round(tests / max(1, rays), 4)}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -351,16 +348,15 @@ def run_own(args):
             torch.distributed.destroy_process_group()
         return 0
 
-    # CPU baseline (oracle port) on a bounded sample, in a fresh process (no
-    # CUDA context or torch threads beside it: measured in-process it reads
-    # about half as fast); it also gives the algorithmic bytes per ray of the
-    # 4-wide SAH BVH
+    # CPU baseline: the reference arm's own routine (the oracle port, whole
+    # frames on all host cores) in a fresh process, so that no CUDA context,
+    # torch threads or product library share the host with it; one warm-up
+    # step and four timed steps cover the 32 cameras once
     cpu = None
     if not args.no_cpu:
         env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-        rr = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
-                             "--warmup", "0", "--cpu-total", str(args.cpu_budget)], capture_output=True, text=True,
-                            env=env)
+        rr = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "4",
+                             "--warmup", "1"], capture_output=True, text=True, env=env)
         ref = json.loads(rr.stdout.strip().splitlines()[-1]) if rr.returncode == 0 else None
         if ref and "value" in ref:
             cpu = ref
@@ -385,7 +381,8 @@ def run_own(args):
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced torus, no dataset)",
-        "config": dict(CONFIG, parallelism="replicas" if ws > 1 else "single GPU",
+        "config": CONFIG,
+        "details": dict(parallelism="replicas" if ws > 1 else "single GPU",
                        frame_ms_mean=round(ms / N_CAMERAS, 4), frame_ms_p50=round(float(np.median(frame_ms)), 4),
                        raster_primary_frame_ms_mean=None if raster_frame_ms is None else round(raster_frame_ms, 4),
                        rays_per_step=rays_per_step, shadow_ray_fraction=round(sum(shadow_rays) / (prim * N_CAMERAS), 4),
@@ -417,7 +414,7 @@ def run_own(args):
     if cpu:
         line["cpu_baseline"] = dict(cpu["cpu_baseline"])
         line["cpu_baseline"]["sample"] = ("separate process: " + cpu["cpu_baseline"]["sample"] +
-                                          f"; oracle BVH build {cpu['bvh_build_s']:.2f} s")
+                                          f"; oracle BVH build {cpu['details']['oracle_bvh_build_s']:.2f} s")
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -846,8 +843,6 @@ def main():
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--leaf", type=int, default=2)
     ap.add_argument("--build", default="ploc", choices=["ploc", "lbvh"], help="BVH builder of the headline mesh")
-    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline sample (own arm)")
-    ap.add_argument("--cpu-total", type=float, default=90.0, help="seconds of CPU work over all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "

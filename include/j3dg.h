@@ -167,6 +167,12 @@ const char* j3dg_last_error(const j3dg_ctx* ctx);
    add their BVH node visits and triangle tests to two device counters. */
 int j3dg_ctx_set_counting(j3dg_ctx* ctx, int enable);
 int j3dg_ctx_read_counters(j3dg_ctx* ctx, uint64_t out[2], int reset);
+/* Device memory as the context sees it (no reference counterpart; the
+   reference has no device memory): out[0..1] free and total bytes of the
+   device (cudaMemGetInfo), out[2..3] bytes reserved and in use by the
+   context's canvas pool, out[4..5] the same for the device's default
+   stream-ordered pool (BVH build scratch). */
+int j3dg_ctx_memory(j3dg_ctx* ctx, uint64_t out[6]);
 /* How canvas frames (render_frame, update_canvas, render_scene) find the
    primary hits (no reference counterpart; the result is the same either
    way). TRACE walks the BVH per pixel. RASTER projects every triangle's box
@@ -240,10 +246,13 @@ int j3dg_voxelize(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32
    kept until the process exits. Grids larger than that are rejected with
    J3DG_ERR_INVALID_ARGUMENT and a message naming both sizes. The caller
    passes the mesh and the output (device or host memory, capacity >= the
-   dims product). The first call on each device looks the scratch up for
-   that device; make that first call before capturing any CUDA graph. All
-   calls share the one scratch array, which keeps the last call's contents
-   (the call clears what must start at zero): calls that overlap on the GPU,
+   dims product). j3dg_ctx_create looks the scratch's device address up
+   (cudaGetSymbolAddress, with the context's device current), which also
+   loads the array, so this function never allocates it; under CUDA's lazy
+   loading the driver may still load the kernels' code at their first
+   launch (CUDA_MODULE_LOADING=EAGER loads it at start). All calls
+   share the one scratch array, which keeps the last call's contents (the
+   call clears what must start at zero): calls that overlap on the GPU,
    from two contexts or two threads, race on it. */
 #define J3DG_NOALLOC_MAX_VOXELS (1u << 21)
 int j3dg_voxelize_noalloc(j3dg_ctx* ctx, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t dims[3],

@@ -106,6 +106,7 @@ SIGNATURES = {
     "j3dg_ctx_stream": (_P, [_P]),
     "j3dg_ctx_set_counting": (_I, [_P, _I]),
     "j3dg_ctx_read_counters": (_I, [_P, C.POINTER(C.c_uint64), _I]),
+    "j3dg_ctx_memory": (_I, [_P, C.POINTER(C.c_uint64)]),
     "j3dg_mesh_build": (_I, [_P, _P, _U, _P, _U, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_mesh_destroy": (_I, [_P]),
     "j3dg_mesh_get_info": (_I, [_P, C.POINTER(MeshInfo)]),

@@ -51,6 +51,11 @@ struct CtxExtra {
   // an HBM cap neither synchronizes the device (as cudaFree does) nor waits
   // for the driver to map memory again
   cudaMemPool_t canvas_pool = nullptr;
+  // device addresses of the no-allocation voxel grid's scratch (a file-scope
+  // array of the library), looked up once when the context is created
+  uint32_t* noalloc_keys = nullptr;
+  uint8_t* noalloc_staging = nullptr;
+  std::string noalloc_error;
 };
 
 int fail(j3dg_ctx* c, int code, const std::string& msg) {
@@ -472,6 +477,10 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
     j3dg_ctx_destroy(c);
     return J3DG_ERR_CUDA;
   }
+  // the no-allocation voxel grid's scratch: its address on this device, and
+  // the module holding it loaded now rather than in the first call; a failed
+  // lookup only disables j3dg_voxelize_noalloc (which then reports it)
+  j3dg::voxel_scratch(&A->ex.noalloc_keys, &A->ex.noalloc_staging, A->ex.noalloc_error);
   *out = c;
   return J3DG_OK;
 }
@@ -536,6 +545,27 @@ int j3dg_canvas_last_primary(const j3dg_canvas* cv) { return cv ? cv->last_prima
 int j3dg_ctx_set_batch_block(j3dg_ctx* c, int threads) {
   if (!c || (threads != 64 && threads != 128 && threads != 256)) return J3DG_ERR_INVALID_ARGUMENT;
   all(c)->ex.batch_threads = threads;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_memory(j3dg_ctx* c, uint64_t out[6]) {
+  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  size_t fr = 0, tot = 0;
+  CK(c, cudaMemGetInfo(&fr, &tot), "memory");
+  out[0] = fr;
+  out[1] = tot;
+  unsigned long long v = 0;
+  CK(c, cudaMemPoolGetAttribute(all(c)->ex.canvas_pool, cudaMemPoolAttrReservedMemCurrent, &v), "memory");
+  out[2] = v;
+  CK(c, cudaMemPoolGetAttribute(all(c)->ex.canvas_pool, cudaMemPoolAttrUsedMemCurrent, &v), "memory");
+  out[3] = v;
+  cudaMemPool_t dflt = nullptr;
+  CK(c, cudaDeviceGetDefaultMemPool(&dflt, c->device), "memory");
+  CK(c, cudaMemPoolGetAttribute(dflt, cudaMemPoolAttrReservedMemCurrent, &v), "memory");
+  out[4] = v;
+  CK(c, cudaMemPoolGetAttribute(dflt, cudaMemPoolAttrUsedMemCurrent, &v), "memory");
+  out[5] = v;
   return J3DG_OK;
 }
 
@@ -841,10 +871,9 @@ int j3dg_voxelize_noalloc(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, 
                     std::to_string(J3DG_NOALLOC_MAX_VOXELS) + " (use j3dg_voxelize or a smaller max_dim)");
   if (!voxels) return J3DG_OK;
   if (capacity < total) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: capacity below dims product");
-  uint32_t* keys = nullptr;
-  uint8_t* staging = nullptr;
-  std::string err;
-  if (int rc = j3dg::voxel_scratch(c->device, &keys, &staging, err)) return fail(c, rc, err);
+  uint32_t* keys = all(c)->ex.noalloc_keys;
+  uint8_t* staging = all(c)->ex.noalloc_staging;
+  if (!keys) return fail(c, J3DG_ERR_CUDA, all(c)->ex.noalloc_error);
   for (int d = 0; d < 3; ++d) V.rays[d] = V.dim[(d + 1) % 3] * V.dim[(d + 2) % 3];
   V.rays_total = V.rays[0] + V.rays[1] + V.rays[2];
   V.use_texture = mesh->d_uv && mesh->d_tex && mesh->tex_w && mesh->tex_h;

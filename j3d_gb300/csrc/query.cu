@@ -12,7 +12,6 @@
 #include <float.h>
 #include <stdint.h>
 
-#include <mutex>
 #include <string>
 
 #include "device_common.cuh"
@@ -287,31 +286,24 @@ cudaError_t launch_count_hits(const j3dg_pixel* G, size_t n, unsigned long long*
 // per voxel a 4-byte key, plus 1 byte of staging used when the caller's
 // output is in host memory. Host code cannot use the array's name as a
 // device address (it names a host-side stand-in); voxel_scratch() looks the
-// real address up once per device with cudaGetSymbolAddress.
+// real address up with cudaGetSymbolAddress on the current device. Contexts
+// call it once, when they are created, and keep the address for their life,
+// so the module holding the array is loaded then and a context created after
+// a device reset looks the address up again.
 namespace j3dg {
 
 static __device__ __align__(256) uint32_t g_voxel_scratch[J3DG_NOALLOC_MAX_VOXELS + J3DG_NOALLOC_MAX_VOXELS / 4];
 
-int voxel_scratch(int device, uint32_t** keys, uint8_t** staging, std::string& err) {
-  static std::mutex mu;
-  static void* addr[256] = {nullptr};
-  if (device < 0 || device >= 256) {
-    err = "voxelize_noalloc: device index out of range";
-    return J3DG_ERR_INVALID_ARGUMENT;
+int voxel_scratch(uint32_t** keys, uint8_t** staging, std::string& err) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_voxel_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    cudaGetLastError();
+    err = std::string("voxelize_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+    return J3DG_ERR_CUDA;
   }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[device]) {
-    // first call on this device (the device is current): resolve the symbol
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_voxel_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      err = std::string("voxelize_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
-      return J3DG_ERR_CUDA;
-    }
-    addr[device] = p;
-  }
-  *keys = static_cast<uint32_t*>(addr[device]);
-  *staging = reinterpret_cast<uint8_t*>(static_cast<uint32_t*>(addr[device]) + J3DG_NOALLOC_MAX_VOXELS);
+  *keys = static_cast<uint32_t*>(p);
+  *staging = reinterpret_cast<uint8_t*>(static_cast<uint32_t*>(p) + J3DG_NOALLOC_MAX_VOXELS);
   return J3DG_OK;
 }
 

@@ -25,10 +25,10 @@ cudaError_t launch_voxelize(const DevInst* inst, const VoxParams& V, uint32_t* k
                             cudaStream_t st);
 
 // Device addresses of the file-scope scratch of the no-allocation voxel grid
-// (keys: J3DG_NOALLOC_MAX_VOXELS words; staging: as many bytes), resolved
-// with cudaGetSymbolAddress on the first call for `device` (which must be
-// current).
-int voxel_scratch(int device, uint32_t** keys, uint8_t** staging, std::string& err);
+// (keys: J3DG_NOALLOC_MAX_VOXELS words; staging: as many bytes), looked up
+// with cudaGetSymbolAddress on the current device (contexts do this once,
+// when they are created).
+int voxel_scratch(uint32_t** keys, uint8_t** staging, std::string& err);
 
 cudaError_t launch_count_hits(const j3dg_pixel* G, size_t n, unsigned long long* out, cudaStream_t st);
 

@@ -90,6 +90,15 @@ class Context:
         pixel); the hits are the same."""
         _check(self.h, lib().j3dg_ctx_set_primary_mode(self.h, mode))
 
+    def memory(self) -> dict:
+        """Device free / total bytes and the reserved / used bytes of the
+        context's canvas pool and of the device's default pool."""
+        out = (C.c_uint64 * 6)()
+        _check(self.h, lib().j3dg_ctx_memory(self.h, out))
+        keys = ("device_free", "device_total", "canvas_pool_reserved", "canvas_pool_used",
+                "default_pool_reserved", "default_pool_used")
+        return {k: int(v) for k, v in zip(keys, out)}
+
     def read_counters(self, reset: bool = True) -> tuple[int, int]:
         out = (C.c_uint64 * 2)()
         _check(self.h, lib().j3dg_ctx_read_counters(self.h, out, 1 if reset else 0))

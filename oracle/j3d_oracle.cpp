@@ -48,10 +48,12 @@
 #include <cfloat>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -568,23 +570,83 @@ HitState find_closest(const Scene2& s, const float* orig, const float* dir, floa
   return hs;
 }
 
+// Row pool in the manner of pooled_parallel_for over jtk's thread_pool
+// (canvas.cpp:765, canvas.h:100): the workers start once, on first use, and
+// sleep between jobs; a job hands out items [y0, y1) one at a time through an
+// atomic counter, and the calling thread works on it too (slot 0). No thread
+// is created per call, so a frame's timing holds only the work.
+class RowPool {
+ public:
+  static RowPool& get() {
+    static RowPool* p = new RowPool();  // never destroyed: workers sleep until exit
+    return *p;
+  }
+  int capacity() const { return (int)workers_.size() + 1; }
+
+  void run(uint32_t y0, uint32_t y1, int n_threads, const std::function<void(uint32_t, int)>& f) {
+    std::lock_guard<std::mutex> job(job_mu_);
+    const int helpers = std::min(n_threads, capacity()) - 1;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &f;
+      next_.store(y0);
+      end_ = y1;
+      want_ = helpers;
+      pending_ = helpers;
+      ++generation_;
+    }
+    cv_.notify_all();
+    drain(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  RowPool() {
+    unsigned n = std::max(1u, std::thread::hardware_concurrency());
+    for (unsigned k = 1; k < n; ++k) workers_.emplace_back([this, k] { loop((int)k); });
+    for (auto& t : workers_) t.detach();
+  }
+  void drain(int slot) {
+    for (;;) {
+      uint32_t y = next_.fetch_add(1);
+      if (y >= end_) break;
+      (*fn_)(y, slot);
+    }
+  }
+  void loop(int slot) {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return generation_ != seen; });
+        seen = generation_;
+        if (slot > want_) continue;  // not part of this job
+      }
+      drain(slot);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_cv_.notify_all();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex job_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(uint32_t, int)>* fn_ = nullptr;
+  std::atomic<uint32_t> next_{0};
+  uint32_t end_ = 0;
+  int want_ = 0, pending_ = 0;
+  uint64_t generation_ = 0;
+};
+
 template <class F>
 void parallel_rows(uint32_t y0, uint32_t y1, int n_threads, F&& f) {
   if (n_threads <= 1 || y1 - y0 < 2) {
     for (uint32_t y = y0; y < y1; ++y) f(y, 0);
     return;
   }
-  std::atomic<uint32_t> next{y0};
-  std::vector<std::thread> th;
-  for (int t = 0; t < n_threads; ++t)
-    th.emplace_back([&, t] {
-      for (;;) {
-        uint32_t y = next.fetch_add(1);
-        if (y >= y1) break;
-        f(y, t);
-      }
-    });
-  for (auto& x : th) x.join();
+  const std::function<void(uint32_t, int)> fn = [&](uint32_t y, int t) { f(y, t); };
+  RowPool::get().run(y0, y1, n_threads, fn);
 }
 
 inline uint32_t make_color(uint32_t r, uint32_t g, uint32_t b) {

@@ -10,12 +10,12 @@ NO_ID = 0xFFFFFFFF
 
 def oracle_scene(O, V, T, poses, w, h, vfov=60.0, leaf=4, n_threads=None, cs_obj=None):
     """Oracle mesh + per-pose views (prepare_scene/unzoom pivot, 60 deg camera)."""
-    from j3d_gb300 import scene as S
+    from oracle.workloads import focal_for_vfov
     m = O.Mesh(V, T, leaf, n_threads)
     cs_obj = np.eye(4, dtype=np.float32).reshape(16) if cs_obj is None else cs_obj
     mn, mx, diag = O.prepare_scene([(m.min_bb, m.max_bb)], [cs_obj])
     _, _, piv = O.unzoom(mn, mx, diag)
-    cam = O.camera_with_focal(S.lib().j3dg_focal_for_vfov(vfov, 0.768))
+    cam = O.camera_with_focal(focal_for_vfov(vfov, 0.768))
     P = O.make_projection_matrix(cam, w, h)
     Pi = O.invert_projection_matrix(P)
     views = [O.view(p, O.invert_orthonormal(p), piv, diag, Pi, cam.near_clipping_plane) for p in poses]
@@ -60,3 +60,27 @@ def compare_rgba(a, b, lsb=1, where=""):
     d = np.abs(a8 - b8)
     assert d.max() <= lsb, f"{where}: RGBA differs by {d.max()} LSB at {np.flatnonzero(d.reshape(-1) > lsb)[:10]}"
     return int((a != b).sum())
+
+
+GBUFFER_FLOATS = ("depth", "u", "v", "barycentric_u", "barycentric_v")
+
+
+def frame_digests(pix, im):
+    """SHA-256 digests of one frame, so that a full-size frame can be compared
+    with the oracle's without storing it:
+      ids     object_id, db_id and mark of every pixel (must be bit-exact)
+      floats  the bits of depth, u, v and the barycentrics of the hit pixels
+      gbuffer every byte of the 32-byte records
+      rgba    the shaded RGBA8 image"""
+    import hashlib
+    p = pix.reshape(-1)
+    hit = p["object_id"] != NO_ID
+    ids = hashlib.sha256()
+    for f in ("object_id", "db_id", "mark"):
+        ids.update(np.ascontiguousarray(p[f]).tobytes())
+    fl = hashlib.sha256()
+    for f in GBUFFER_FLOATS:
+        fl.update(np.ascontiguousarray(p[f][hit]).tobytes())
+    return {"ids": ids.hexdigest(), "floats": fl.hexdigest(),
+            "gbuffer": hashlib.sha256(np.ascontiguousarray(p).view(np.uint8).tobytes()).hexdigest(),
+            "rgba": hashlib.sha256(np.ascontiguousarray(im).tobytes()).hexdigest()}

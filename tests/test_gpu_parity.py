@@ -362,43 +362,57 @@ def test_multi_object_textured_and_vertex_colours(gpu_ctx, oracle_mod, primary):
         compare_rgba(cv.get_image(), oi, 1 if kw.get("edges") else 0, "textured")
 
 
-def test_full_size_torus_rows_match_oracle(gpu_ctx, oracle_mod, primary):
-    """28.09M-triangle torus at 1920x1080, the 32 cameras of the benchmark:
-    hit and shadowed pixels of every frame equal the oracle's full-frame
-    counts (tests/golden/traffic.json, made by make_traffic.py), and so does
-    the ray total; on two cameras the GPU frame equals the oracle's on
-    sampled rows, with size-independent checks of every hit record."""
+def test_full_size_torus_frames_match_oracle(gpu_ctx, oracle_mod, primary):
+    """28.09M-triangle torus at 1920x1080, all 32 cameras of the benchmark,
+    primary + shadow + plain shading: every frame's G-buffer and RGBA image
+    equal the oracle's full frame (SHA-256 digests of triangle ids / db ids /
+    marks, of the hit records' float bits, of every G-buffer byte and of the
+    image, from tests/golden/traffic.json, made by make_traffic.py), and so
+    do the per-frame hit and shadowed pixel counts and the ray total. A frame
+    whose digests differ is rendered by the oracle and compared pixel by
+    pixel, which names the first differing pixels; float fields may then
+    differ within 1e-5 relative, nothing else may."""
+    import oracle.workloads as OW
+    from helpers import frame_digests
     from j3d_gb300 import workloads as W
     O = oracle_mod
     wl = W.config1()
     ref = json.loads((GOLDEN / "traffic.json").read_text())["config1"]
+    assert len(ref["digests"]) == len(wl.poses) == 32
+    assert np.array_equal(wl.poses.view(np.uint32), OW.cameras(32, W.SEED_BASE + 1 + (1 << 32), 2.5, 4.0).view(np.uint32))
     mesh, sc = gpu_scene(gpu_ctx, wl.vertices, wl.triangles, wl.poses[0])
     info = mesh.info()
     assert info.n_triangles == 28_090_000 and info.n_vertices == 14_045_000
-    hits, shadowed = [], []
-    for pose in wl.poses:
+    hits, shadowed, differ = [], [], []
+    for i, pose in enumerate(wl.poses):
         sc.set_pose(pose)
-        gp, _, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False), expect=primary)
+        gp, gi, cv, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False), expect=primary)
+        cv.close()
         hits.append(int((gp["object_id"] != NO_ID).sum()))
         shadowed.append(int(((gp["mark"] & 1) != 0).sum()))
+        if frame_digests(gp, gi) != ref["digests"][i]:
+            differ.append(i)
     assert hits == ref["hit_pixels"] and shadowed == ref["shadowed_pixels"]
     assert len(wl.poses) * wl.width * wl.height + sum(hits) == ref["rays"]
-    m, views, _ = oracle_scene(O, wl.vertices, wl.triangles, wl.poses[:2], wl.width, wl.height)
-    for i, pose in enumerate(wl.poses[:2]):
-        sc.set_pose(pose)
-        gp, gi, _, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
-        rows = list(range(3, wl.height, 67))
-        op = O.fresh_pixels(wl.width, wl.height)
-        for y in rows:
-            O.update_canvas(op, [(m, I16, 1)], views[i], O.settings(shadow=True, edges=False),
-                            rect=(0, y, wl.width - 1, y))
-        assert compare_gbuffers(gp[rows], op[rows], f"torus28M cam {i}") == 0
-        hit = gp["object_id"] != NO_ID
-        assert hit.mean() > 0.05
-        # depth is positive and finite on hits, FLT_MAX on misses
-        assert (gp["depth"][hit] > 0).all() and (gp["depth"][~hit] == FLT_MAX).all()
-        ids = gp["object_id"][hit]
-        assert ids.max() < 28_090_000
+    if differ:
+        # name the first differing pixels of up to two frames against the oracle's own frame
+        m, views, _ = oracle_scene(O, wl.vertices, wl.triangles, wl.poses[differ[:2]], wl.width, wl.height)
+        for k, i in enumerate(differ[:2]):
+            sc.set_pose(wl.poses[i])
+            gp, gi, cv, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
+            op, oi = oracle_frame(O, m, views[k], wl.width, wl.height, O.settings(shadow=True, edges=False))
+            assert frame_digests(op, oi) == ref["digests"][i], "oracle frame differs from its own digest"
+            compare_gbuffers(gp, op, f"torus28M cam {i}")
+            compare_rgba(gi, oi, 0, f"torus28M cam {i}")
+        for i in differ:
+            sc.set_pose(wl.poses[i])
+            gp, gi, cv, _ = gpu_frame(gpu_ctx, sc, wl.width, wl.height, gst(shadow=True, edges=False))
+            cv.close()
+            d = frame_digests(gp, gi)
+            assert d["ids"] == ref["digests"][i]["ids"], f"cam {i}: triangle / db ids or marks differ"
+            assert d["rgba"] == ref["digests"][i]["rgba"], f"cam {i}: RGBA differs"
+    print(f"torus28M ({primary}): {32 - len(differ)}/32 frames bit-identical to the oracle, "
+          f"{len(differ)} within tolerance")
 
 
 def test_async_download_overlaps_and_keeps_frame(gpu_ctx):

@@ -131,3 +131,27 @@ def test_normals_and_bbox_oracle_restatement(oracle_mod, product_lib):
     assert np.allclose(N, n, atol=1e-6)
     mn, mx = oracle_mod.compute_bb(V)
     assert np.array_equal(mn, V.min(axis=0)) and np.array_equal(mx, V.max(axis=0))
+
+
+def test_oracle_generators_equal_product_generators(product_lib):
+    """The oracle's numpy restatement of the seeded workloads (used by the CPU
+    baseline, which must not load the product library) gives the product's
+    bytes: icosphere subdivision order and displacement, torus grid, cameras,
+    and the 60-degree focal length."""
+    import oracle.workloads as OW
+    from j3d_gb300 import scene as S
+    from j3d_gb300 import workloads as W
+    for lvl in range(0, 6):
+        a, b = W.icosphere(lvl, W.SEED_BASE + 40 + lvl), OW.icosphere(lvl, W.SEED_BASE + 40 + lvl)
+        assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)) and np.array_equal(a[1], b[1]), lvl
+    for nu, nv, seed in ((3, 3, 1), (10, 7, 2), (301, 149, W.SEED_BASE + 1)):
+        a, b = W.torus(nu, nv, seed=seed), OW.torus(nu, nv, seed=seed)
+        assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)) and np.array_equal(a[1], b[1]), (nu, nv)
+    for n, seed, r0, r1 in ((32, W.SEED_BASE + 1 + (1 << 32), 2.5, 4.0), (300, 7, 2.0, 5.0)):
+        assert np.array_equal(W.cameras(n, seed, r0, r1).view(np.uint32), OW.cameras(n, seed, r0, r1).view(np.uint32))
+    for vfov in (60.0, 45.0, 31.0, 90.0, 1.0):
+        assert S.lib().j3dg_focal_for_vfov(vfov, 0.768) == OW.focal_for_vfov(vfov, 0.768)
+    c0 = W.config0()
+    V, T, poses, w, h = OW.config0()
+    assert np.array_equal(c0.vertices, V) and np.array_equal(c0.triangles, T) and np.array_equal(c0.poses, poses)
+    assert (c0.width, c0.height) == (w, h)

@@ -159,3 +159,27 @@ def test_render_region_and_empty_scene(oracle_mod, product_lib):
     empty["object_id"] = 7
     O.update_canvas(empty, [], views[0], st)
     assert (empty["object_id"] == NO_ID).all() and (empty["depth"] == FLT_MAX).all()
+
+
+def test_row_pool_gives_the_same_frame_at_any_thread_count(oracle_mod):
+    """The oracle's persistent row pool (workers started once, like
+    pooled_parallel_for's thread pool) renders the same G-buffer and image
+    with 1, 2, 3 or all threads, call after call."""
+    import os
+    import oracle.workloads as OW
+    O = oracle_mod
+    V, T = OW.icosphere(4, OW.SEED_BASE + 7)
+    m, views, _ = oracle_scene(O, V, T, OW.translation(0.1, 0.0, 2.6)[None], 160, 120)
+    mc, cav = O.make_matcap(0)
+    st = O.settings(shadow=True, edges=False)
+    frames = []
+    for nt in (1, 2, 3, os.cpu_count() or 1, 1, os.cpu_count() or 1):
+        pix = O.fresh_pixels(160, 120)
+        im = np.zeros((120, 160), np.uint32)
+        _, _, s = O.render_frame(pix, im, O.fill_background(160, 120), [(m, I16, 1)], views[0], st, mc, cav,
+                                 n_threads=nt)
+        frames.append((pix, im, s.rays, s.node_visits, s.tri_tests))
+    for f in frames[1:]:
+        assert np.array_equal(f[0].view(np.uint8), frames[0][0].view(np.uint8)) and np.array_equal(f[1], frames[0][1])
+        assert f[2:] == frames[0][2:]
+    assert (frames[0][0]["object_id"] != NO_ID).sum() > 1000

@@ -71,3 +71,39 @@ def test_noalloc_device_output_and_size_limit(product_lib, gpu_ctx):
     assert "scratch holds %d" % MAX_VOXELS in msg
     assert int(dims[0]) * int(dims[1]) * int(dims[2]) > MAX_VOXELS
     assert not big.any()
+
+
+def test_noalloc_calls_allocate_no_device_memory(product_lib, gpu_ctx):
+    """What the entry point exists for: once warm, calls with host and with
+    device output leave the device's free memory, the context's canvas pool
+    and the device's default stream-ordered pool exactly as they were
+    (cudaMemGetInfo and the pools' reserved / used bytes, read through
+    j3dg_ctx_memory), and every call still gives the allocating call's grid."""
+    import torch
+
+    from j3d_gb300 import Mesh, workloads as W
+    lib = product_lib
+    V, T = W.torus(120, 60, seed=W.SEED_BASE + 63)
+    m = Mesh(gpu_ctx, V, T)
+    want, _ = _grid(lib, gpu_ctx, m, 110, noalloc=False)
+    dev = torch.zeros(want.size, dtype=torch.uint8, device="cuda")
+    host = np.zeros(want.size, np.uint8)
+    _grid(lib, gpu_ctx, m, 110, noalloc=True)            # warm: the kernels' first launches
+    _grid(lib, gpu_ctx, m, 110, noalloc=True, out=dev)
+    gpu_ctx.synchronize()
+    torch.cuda.synchronize()
+    before = gpu_ctx.memory()
+    assert before["device_total"] > 0
+    dims = (C.c_uint32 * 3)()
+    for k in range(6):
+        if k % 2:
+            dev.zero_()
+            torch.cuda.synchronize()
+            assert lib.j3dg_voxelize_noalloc(gpu_ctx.h, m.h, 110, dims, dev.data_ptr(), dev.numel()) == 0
+            gpu_ctx.synchronize()
+            assert np.array_equal(dev.cpu().numpy(), want)
+        else:
+            host[:] = 0
+            assert lib.j3dg_voxelize_noalloc(gpu_ctx.h, m.h, 110, dims, host.ctypes.data, host.size) == 0
+            assert np.array_equal(host, want)
+        assert gpu_ctx.memory() == before, (k, before, gpu_ctx.memory())

@@ -189,7 +189,8 @@ def run_reference(args):
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": n_threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "details": {"frame_ms_mean": round(float(np.mean(frame_s)) * 1e3, 2),
+            "details": {"step_ms": [round(x * 1e3, 1) for x in step_s],
+                        "frame_ms_mean": round(float(np.mean(frame_s)) * 1e3, 2),
                         "frame_ms_p50": round(float(np.median(frame_s)) * 1e3, 2),
                         "oracle_bvh_build_s": round(cpu.m.build_seconds, 3),
                         "setup_s": round(setup_s, 2),
@@ -350,13 +351,13 @@ def run_own(args):
 
     # CPU baseline: the reference arm's own routine (the oracle port, whole
     # frames on all host cores) in a fresh process, so that no CUDA context,
-    # torch threads or product library share the host with it; one warm-up
-    # step and four timed steps cover the 32 cameras once
+    # torch threads or product library share the host with it; four warm-up
+    # steps cover the 32 cameras once, eight timed steps twice
     cpu = None
     if not args.no_cpu:
         env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-        rr = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "4",
-                             "--warmup", "1"], capture_output=True, text=True, env=env)
+        rr = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "8",
+                             "--warmup", "4"], capture_output=True, text=True, env=env)
         ref = json.loads(rr.stdout.strip().splitlines()[-1]) if rr.returncode == 0 else None
         if ref and "value" in ref:
             cpu = ref
@@ -762,6 +763,69 @@ def run_ingest(args):
     return 0
 
 
+def run_objects(args):
+    """Scenes of many objects (the two-level structure of canvas.cpp:762):
+    n instances of four meshes (icosphere L5, tori of 200k and 50k triangles,
+    icosphere L4) under seeded rigid transforms, 1920x1080 primary + shadow
+    + plain shading from 16 cameras, walked through the per-frame top-level
+    BVH and object after object (the same context, switched)."""
+    import torch
+
+    from j3d_gb300 import Canvas, Context, Matcap, Mesh, Scene, build as B, camera_for_vfov, settings, workloads as Wk
+    B.build()
+    ctx = Context(0)
+    rng = np.random.default_rng(Wk.SEED_BASE + 9)
+    meshes = [Mesh(ctx, *Wk.icosphere(5, Wk.SEED_BASE + 90)), Mesh(ctx, *Wk.torus(448, 224, seed=Wk.SEED_BASE + 91)),
+              Mesh(ctx, *Wk.torus(224, 112, seed=Wk.SEED_BASE + 92)), Mesh(ctx, *Wk.icosphere(4, Wk.SEED_BASE + 93))]
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {}
+    for n in (16, 256, 1024):
+        sc = Scene()
+        spread = 1.5 * n ** (1 / 3)
+        for k in range(n):
+            q = rng.normal(size=4)
+            q /= np.linalg.norm(q)
+            w, x, y, z = q
+            M = np.eye(4)
+            M[:3, :3] = [[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                         [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                         [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]]
+            M[:3, 3] = rng.uniform(-spread, spread, size=3)
+            sc.add_object(meshes[k % 4], M.T.reshape(16).astype(np.float32), 1 + k)
+        sc.prepare_scene()
+        sc.unzoom()
+        poses = Wk.cameras(16, Wk.SEED_BASE + 94, 2.2 * spread, 3.0 * spread)
+        cv = Canvas(ctx, W_, H_)
+        cv.set_camera(camera_for_vfov(60.0))
+        cv.set_background_color()
+        cv.update_settings(settings(shadow=True, edges=False))
+        mc = Matcap.make(ctx, 0)
+        res = {}
+        for top in (True, False):
+            ctx.set_top_level(top)
+            for p in poses[:4]:
+                sc.set_pose(p)
+                cv.render_frame(sc, mc)
+            ctx.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for p in poses:
+                sc.set_pose(p)
+                cv.render_frame(sc, mc)
+            e1.record(stream)
+            e1.synchronize()
+            ctx.synchronize()
+            res["top_level" if top else "object_loop"] = round(e0.elapsed_time(e1) / len(poses), 3)
+        ctx.set_top_level(True)
+        hits = int((cv.get_pixels()["object_id"] != 0xFFFFFFFF).sum())
+        out[n] = dict(res, last_frame_hit_pixels=hits)
+        cv.close()
+    print(json.dumps({"workload": "objects", "metric": "frame ms, 1920x1080 primary + shadow + shading",
+                      "frames_per_point": 16, "by_instances": out}), flush=True)
+    return 0
+
+
 def run_pointcloud(args):
     """Point-cloud splat after each headline frame: the 28.09M-triangle torus
     frame at 1920x1080 for each of the 32 cameras, then its 14.045M vertices
@@ -844,7 +908,8 @@ def main():
     ap.add_argument("--leaf", type=int, default=2)
     ap.add_argument("--build", default="ploc", choices=["ploc", "lbvh"], help="BVH builder of the headline mesh")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="torus", choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud"],
+    ap.add_argument("--workload", default="torus",
+                    choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
                          "serve: config-4 request serving")
     ap.add_argument("--serve-rate", type=float, default=400.0)
@@ -863,6 +928,8 @@ def main():
         return run_ingest(args)
     if args.workload == "pointcloud":
         return run_pointcloud(args)
+    if args.workload == "objects":
+        return run_objects(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

@@ -167,6 +167,12 @@ const char* j3dg_last_error(const j3dg_ctx* ctx);
    add their BVH node visits and triangle tests to two device counters. */
 int j3dg_ctx_set_counting(j3dg_ctx* ctx, int enable);
 int j3dg_ctx_read_counters(j3dg_ctx* ctx, uint64_t out[2], int reset);
+/* Scenes of two or more objects are walked through a per-frame top level,
+   a BVH4 over the objects' world boxes (the two-level structure of
+   qbvh_two_level_with_transformations, canvas.cpp:762, 786, 854). With
+   enable = 0 the kernels walk the objects one after the other instead (the
+   same results; for measurement). Default 1. */
+int j3dg_ctx_set_top_level(j3dg_ctx* ctx, int enable);
 /* Device memory as the context sees it (no reference counterpart; the
    reference has no device memory): out[0..1] free and total bytes of the
    device (cudaMemGetInfo), out[2..3] bytes reserved and in use by the
@@ -505,6 +511,15 @@ int j3dg_learned_set_params(j3dg_learned* l, const float* in);
 int j3dg_learned_loss_grad(j3dg_learned* l, const float* features, const int32_t* labels, uint32_t B, float* loss,
                            float* grads);
 /* Checkpoint (header + fp32 parameters). */
+/* A whole canvas frame (canvas::render_scene's update_canvas + canvas_to_image,
+   canvas.cpp:677-874, 582-670) whose primary hits come from the learned
+   path: the frame's primary rays go through the network and the exact
+   traversal it seeds, then the hit records, shadow rays and shading are the
+   plain path's. The G-buffer and image equal j3dg_canvas_render_frame's. The
+   scene must hold the network's mesh as its only object, with the identity
+   transform (the network works in the mesh's space). */
+int j3dg_learned_render_frame(j3dg_learned* l, j3dg_canvas* canvas, const j3dg_scene* scene,
+                              const j3dg_matcap* matcap);
 int j3dg_learned_save(j3dg_learned* l, const char* path);
 int j3dg_learned_load(j3dg_learned* l, const char* path);
 

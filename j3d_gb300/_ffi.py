@@ -107,6 +107,7 @@ SIGNATURES = {
     "j3dg_ctx_set_counting": (_I, [_P, _I]),
     "j3dg_ctx_read_counters": (_I, [_P, C.POINTER(C.c_uint64), _I]),
     "j3dg_ctx_memory": (_I, [_P, C.POINTER(C.c_uint64)]),
+    "j3dg_ctx_set_top_level": (_I, [_P, _I]),
     "j3dg_mesh_build": (_I, [_P, _P, _U, _P, _U, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_mesh_destroy": (_I, [_P]),
     "j3dg_mesh_get_info": (_I, [_P, C.POINTER(MeshInfo)]),
@@ -176,6 +177,7 @@ SIGNATURES = {
     "j3dg_learned_set_params": (_I, [_P, _P]),
     "j3dg_learned_loss_grad": (_I, [_P, _P, _P, _U, C.POINTER(_F), _P]),
     "j3dg_learned_save": (_I, [_P, C.c_char_p]),
+    "j3dg_learned_render_frame": (_I, [_P, _P, C.POINTER(Scene), _P]),
     "j3dg_learned_load": (_I, [_P, C.c_char_p]),
     "j3dg_make_default_camera": (None, [C.POINTER(Camera)]),
     "j3dg_make_projection_matrix": (None, [C.POINTER(Camera), _I, _I, _FP]),

@@ -15,6 +15,7 @@
 #include "../../include/j3dg.h"
 #include "device_common.cuh"
 #include "internal.h"
+#include "toplevel.h"
 #include "query.cuh"
 #include "render.cuh"
 
@@ -24,6 +25,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
 }
 
 using j3dg::DevInst;
+using j3dg::DevTop;
 using j3dg::FrameParams;
 
 namespace {
@@ -38,6 +40,7 @@ const size_t kQueueBytesPerPixel = 48, kQueueBytesFixed = 16384;
 struct CtxExtra {
   std::vector<DevInst> last;  // the table in the most recent slot
   int last_slot = -1;
+  bool last_top = false;      // whether that table's top level is walked
   uint32_t next_slot = 0;
   cudaEvent_t slot_ev[kInstSlots];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -46,6 +49,7 @@ struct CtxExtra {
   bool counting = false;
   int batch_threads = 128;            // block shape of batched launches
   int primary_mode = J3DG_PRIMARY_AUTO;
+  bool top_level = true;              // scenes of several objects walk a top level
   // canvas buffers: stream-ordered allocations from a pool that keeps freed
   // memory reserved, so a server that evicts and re-creates canvases under
   // an HBM cap neither synchronizes the device (as cudaFree does) nor waits
@@ -89,7 +93,7 @@ cudaStream_t S(j3dg_ctx* c) { return (cudaStream_t)c->stream; }
 struct CtxAll {
   j3dg_ctx ctx;
   CtxExtra ex;
-  DevInst* h_slots = nullptr;  // pinned, kInstSlots * inst_cap
+  char* h_slots = nullptr;  // pinned, kInstSlots tables of inst_cap objects
 };
 
 CtxAll* all(j3dg_ctx* c) { return reinterpret_cast<CtxAll*>(c); }
@@ -118,8 +122,57 @@ DevInst to_dev(const j3dg_instance& in) {
   return d;
 }
 
-// Uploads the instance table (skipped when unchanged); returns its device address.
-int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const DevInst** out) {
+// Instance table, on the device and in its pinned staging alike:
+// [DevTop][DevInst x cap][top-level BVH4 nodes x cap], 256-byte aligned. The
+// kernels receive &DevInst[0] and find the header just in front of it.
+size_t table_bytes(uint32_t cap) {
+  const size_t b = sizeof(DevTop) + sizeof(DevInst) * (size_t)cap + 128 * (size_t)std::max(cap, 1u);
+  return (b + 255) & ~size_t(255);
+}
+
+// Objects of a scene from which the kernels walk a top level (the two-level
+// structure of canvas.cpp:762); a single object is walked directly.
+const uint32_t kTopMinObjects = 2;
+
+// Writes the table of the n objects t / objs (capacity cap >= n) into the host
+// image h of a table whose device copy lives at d: the header, the objects
+// and the top level over their world boxes. Returns the device address of
+// DevInst[0]; top tells whether the kernels should walk the top level (it
+// exists, the scene has kTopMinObjects objects or more, and the deepest
+// object tree under it still fits the traversal stack).
+const DevInst* write_table(char* h, char* d, const DevInst* t, const j3dg_instance* objs, uint32_t n, uint32_t cap,
+                           bool& top, bool* fits = nullptr) {
+  DevTop* H = reinterpret_cast<DevTop*>(h);
+  DevInst* I = reinterpret_cast<DevInst*>(h + sizeof(DevTop));
+  const size_t off_nodes = sizeof(DevTop) + sizeof(DevInst) * (size_t)cap;
+  memcpy(I, t, sizeof(DevInst) * n);
+  std::vector<const float*> lo(n), hi(n), cs(n);
+  uint32_t deepest = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    lo[i] = objs[i].mesh->min_bb;
+    hi[i] = objs[i].mesh->max_bb;
+    cs[i] = objs[i].cs;
+    deepest = std::max(deepest, objs[i].mesh->max_depth);
+  }
+  const j3dg::TopLevel tl = j3dg::build_top_level(lo.data(), hi.data(), cs.data(), n,
+                                                  reinterpret_cast<float*>(h + off_nodes), std::max(cap, 1u));
+  memset(H, 0, sizeof(DevTop));
+  if (tl.ok) {
+    H->nodes = reinterpret_cast<const float4*>(d + off_nodes);
+    H->root = tl.root;
+    H->n_nodes = tl.n_nodes;
+    H->n_inst = n;
+    H->pad_scale = tl.pad_scale;
+  }
+  const bool walkable = tl.ok && tl.depth + deepest <= J3DG_MAX_DEPTH;
+  top = walkable && n >= kTopMinObjects;
+  if (fits) *fits = walkable;
+  return reinterpret_cast<const DevInst*>(d + sizeof(DevTop));
+}
+
+// Uploads the instance table (skipped when unchanged); returns its device
+// address and whether its top level is walked.
+int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const DevInst** out, bool* top = nullptr) {
   CtxAll* A = all(c);
   CtxExtra& X = A->ex;
   std::vector<DevInst> t(n);
@@ -128,6 +181,7 @@ int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const D
     if (objs[i].mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh belongs to another context");
     t[i] = to_dev(objs[i]);
   }
+  if (top) *top = false;
   if (n == 0) {
     *out = nullptr;
     return J3DG_OK;
@@ -137,9 +191,9 @@ int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const D
     CK(c, cudaStreamSynchronize(S(c)), "instance table");
     uint32_t cap = std::max(n, 2 * c->inst_cap);
     void* d = nullptr;
-    DevInst* h = nullptr;
-    CK(c, cudaMalloc(&d, sizeof(DevInst) * cap * kInstSlots), "instance table");
-    if (cudaMallocHost((void**)&h, sizeof(DevInst) * cap * kInstSlots) != cudaSuccess) {
+    char* h = nullptr;
+    CK(c, cudaMalloc(&d, table_bytes(cap) * kInstSlots), "instance table");
+    if (cudaMallocHost((void**)&h, table_bytes(cap) * kInstSlots) != cudaSuccess) {
       cudaFree(d);
       return fail(c, J3DG_ERR_OUT_OF_MEMORY, "instance table: pinned host allocation failed");
     }
@@ -151,21 +205,26 @@ int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const D
     X.last.clear();
     X.last_slot = -1;
   }
+  const size_t tb = table_bytes(c->inst_cap);
   if (X.last_slot >= 0 && X.last.size() == n && memcmp(X.last.data(), t.data(), sizeof(DevInst) * n) == 0) {
-    *out = (const DevInst*)c->d_inst + (size_t)X.last_slot * c->inst_cap;
+    *out = reinterpret_cast<const DevInst*>(static_cast<char*>(c->d_inst) + (size_t)X.last_slot * tb + sizeof(DevTop));
+    if (top) *top = X.last_top;
     return J3DG_OK;
   }
   uint32_t slot = X.next_slot;
   X.next_slot = (X.next_slot + 1) % kInstSlots;
   CK(c, cudaEventSynchronize(X.slot_ev[slot]), "instance table");
-  DevInst* h = A->h_slots + (size_t)slot * c->inst_cap;
-  memcpy(h, t.data(), sizeof(DevInst) * n);
-  DevInst* d = (DevInst*)c->d_inst + (size_t)slot * c->inst_cap;
-  CK(c, cudaMemcpyAsync(d, h, sizeof(DevInst) * n, cudaMemcpyHostToDevice, S(c)), "instance table");
+  char* h = A->h_slots + (size_t)slot * tb;
+  char* d = static_cast<char*>(c->d_inst) + (size_t)slot * tb;
+  bool walk_top = false;
+  *out = write_table(h, d, t.data(), objs, n, c->inst_cap, walk_top);
+  walk_top = walk_top && X.top_level;
+  CK(c, cudaMemcpyAsync(d, h, tb, cudaMemcpyHostToDevice, S(c)), "instance table");
   CK(c, cudaEventRecord(X.slot_ev[slot], S(c)), "instance table");
   X.last = t;
   X.last_slot = (int)slot;
-  *out = d;
+  X.last_top = walk_top;
+  if (top) *top = walk_top;
   return J3DG_OK;
 }
 
@@ -265,6 +324,29 @@ uint32_t bits_for(uint32_t v) {  // bits that hold 0..v
   return b;
 }
 
+// The canvas scratch as the raster stages use it: keys (8 B per pixel),
+// shadow jobs (32 B per pixel), the n objects' table, the large-triangle
+// list. Returns false if the scratch is too small.
+bool raster_layout(FrameParams& P, j3dg_canvas* cv, uint32_t n, uint32_t id_bits, uint32_t total) {
+  const size_t npx = (size_t)cv->w * cv->h, bytes = kQueueBytesPerPixel * npx + kQueueBytesFixed;
+  const size_t off_inst = (40 * npx + 255) & ~size_t(255);
+  const size_t off_list = (off_inst + sizeof(j3dg::RasterInst) * n + 255) & ~size_t(255);
+  const size_t min_entries = 16;
+  if (off_list + sizeof(uint32_t) * (j3dg::kRasterListHeader + min_entries * j3dg::kRasterEntryWords) > bytes)
+    return false;
+  const size_t cap = ((bytes - off_list) / sizeof(uint32_t) - j3dg::kRasterListHeader) / j3dg::kRasterEntryWords;
+  char* q = (char*)cv->d_queue;
+  P.raster = 1;
+  P.id_bits = id_bits;
+  P.raster_total = total;
+  P.rlist_cap = (uint32_t)std::min<size_t>(cap, 0xffffffffu);
+  memcpy(P.proj, cv->projection, sizeof(P.proj));
+  P.keys = (unsigned long long*)q;
+  P.rinst = (j3dg::RasterInst*)(q + off_inst);
+  P.rlist = (uint32_t*)(q + off_list);
+  return true;
+}
+
 void setup_raster(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s) {
   const int mode = all(cv->ctx)->ex.primary_mode;
   cv->last_primary = J3DG_PRIMARY_TRACE;
@@ -302,23 +384,7 @@ void setup_raster(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s) {
   }
   const uint64_t px = (uint64_t)(P.x1 - P.x0 + 1) * (uint64_t)(P.y1 - P.y0 + 1);
   if (mode == J3DG_PRIMARY_AUTO && (!kAutoRaster || (double)total > kRasterTrisPerPixel * (double)px)) return;
-  // keys (8 B per pixel), shadow jobs (32 B per pixel), instance table, list
-  const size_t npx = (size_t)cv->w * cv->h, bytes = kQueueBytesPerPixel * npx + kQueueBytesFixed;
-  const size_t off_inst = (40 * npx + 255) & ~size_t(255);
-  const size_t off_list = (off_inst + sizeof(j3dg::RasterInst) * n + 255) & ~size_t(255);
-  const size_t min_entries = 16;
-  if (off_list + sizeof(uint32_t) * (j3dg::kRasterListHeader + min_entries * j3dg::kRasterEntryWords) > bytes) return;
-  const size_t cap = ((bytes - off_list) / sizeof(uint32_t) - j3dg::kRasterListHeader) / j3dg::kRasterEntryWords;
-  char* q = (char*)cv->d_queue;
-  P.raster = 1;
-  P.id_bits = id_bits;
-  P.raster_total = (uint32_t)total;
-  P.rlist_cap = (uint32_t)std::min<size_t>(cap, 0xffffffffu);
-  memcpy(P.proj, cv->projection, sizeof(P.proj));
-  P.keys = (unsigned long long*)q;
-  P.rinst = (j3dg::RasterInst*)(q + off_inst);
-  P.rlist = (uint32_t*)(q + off_list);
-  cv->last_primary = J3DG_PRIMARY_RASTER;
+  if (raster_layout(P, cv, n, id_bits, (uint32_t)total)) cv->last_primary = J3DG_PRIMARY_RASTER;
 }
 
 }  // namespace
@@ -394,7 +460,7 @@ int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out) {
 int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits) {
   const DevInst* dinst = nullptr;
   if (int rc = mesh_devinst(c, mesh, &dinst)) return rc;
-  CK(c, launch_rays(dinst, 1, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, nullptr, S(c)),
+  CK(c, launch_rays(dinst, 1, false, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, nullptr, S(c)),
      "ray query");
   return J3DG_OK;
 }
@@ -469,8 +535,8 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
   for (uint32_t i = 0; ok && i < kInstSlots; ++i) ok = cudaEventCreateWithFlags(&A->ex.slot_ev[i], cudaEventDisableTiming) == cudaSuccess;
   if (ok) {
     c->inst_cap = 16;
-    ok = cudaMalloc(&c->d_inst, sizeof(DevInst) * c->inst_cap * kInstSlots) == cudaSuccess &&
-         cudaMallocHost((void**)&A->h_slots, sizeof(DevInst) * c->inst_cap * kInstSlots) == cudaSuccess;
+    ok = cudaMalloc(&c->d_inst, table_bytes(c->inst_cap) * kInstSlots) == cudaSuccess &&
+         cudaMallocHost((void**)&A->h_slots, table_bytes(c->inst_cap) * kInstSlots) == cudaSuccess;
   }
   if (!ok) {
     cudaGetLastError();
@@ -566,6 +632,13 @@ int j3dg_ctx_memory(j3dg_ctx* c, uint64_t out[6]) {
   out[4] = v;
   CK(c, cudaMemPoolGetAttribute(dflt, cudaMemPoolAttrUsedMemCurrent, &v), "memory");
   out[5] = v;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_set_top_level(j3dg_ctx* c, int enable) {
+  if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  all(c)->ex.top_level = enable != 0;
+  all(c)->ex.last_slot = -1;  // the next table is written afresh
   return J3DG_OK;
 }
 
@@ -724,7 +797,8 @@ static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, con
   if (!c || (n && (!rays || !hits)) || (n_obj && !objs)) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   const DevInst* dinst = nullptr;
-  int rc = upload_instances(c, objs, n_obj, &dinst);
+  bool top = false;
+  int rc = upload_instances(c, objs, n_obj, &dinst, &top);
   if (rc) return rc;
   if (n == 0) return J3DG_OK;
   const bool rays_dev = is_device_ptr(rays), hits_dev = is_device_ptr(hits);
@@ -735,7 +809,7 @@ static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, con
     CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "rays");
   }
   if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n, S(c)), "hits");
-  CK(c, j3dg::launch_rays(dinst, n_obj, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, j3dg::ctx_counters(c),
+  CK(c, j3dg::launch_rays(dinst, n_obj, top, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, j3dg::ctx_counters(c),
                           S(c)),
      "find");
   if (!hits_dev) {
@@ -1007,7 +1081,8 @@ int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, c
   cudaSetDevice(c->device);
   j3dg::canvas_writable(cv);
   const DevInst* dinst = nullptr;
-  if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
+  bool top = false;
+  if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst, &top)) return rc;
   // canvas.cpp:681-698: clamp the rectangle
   const int w = (int)cv->w, h = (int)cv->h;
   auto clampv = [](int v, int hi) { return v < 0 ? 0 : (v >= hi ? hi - 1 : v); };
@@ -1017,6 +1092,7 @@ int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, c
   y1 = clampv(y1, h);
   FrameParams P;
   fill_frame(P, cv, s, dinst, nullptr);
+  P.top = top ? 1u : 0u;
   P.x0 = x0;
   P.y0 = y0;
   P.x1 = x1;
@@ -1081,8 +1157,9 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   cudaSetDevice(c->device);
   j3dg::canvas_writable(cv);
   const DevInst* dinst = nullptr;
+  bool top = false;
   if (s)
-    if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst)) return rc;
+    if (int rc = upload_instances(c, s->objects, s->n_objects, &dinst, &top)) return rc;
   const int mode = shade_mode_of(cv->settings);
   if (!s) {
     const size_t n = (size_t)cv->w * cv->h;
@@ -1092,6 +1169,7 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   }
   FrameParams P;
   fill_frame(P, cv, s, dinst, m);
+  P.top = top ? 1u : 0u;
   setup_raster(P, cv, s);
   if (mode == 0) {
     P.shade_mode = 1;  // one kernel: G-buffer, shadow, plain shading, background
@@ -1104,21 +1182,83 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   return J3DG_OK;
 }
 
+// ------------------------------------------------------- learned frames
+
+namespace j3dg {
+int learned_hits_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits);
+const j3dg_mesh* learned_mesh(const j3dg_learned* l);
+j3dg_ctx* learned_ctx(const j3dg_learned* l);
+}  // namespace j3dg
+
+int j3dg_learned_render_frame(j3dg_learned* l, j3dg_canvas* cv, const j3dg_scene* s, const j3dg_matcap* m) {
+  if (!l || !cv || !s || !m) return J3DG_ERR_INVALID_ARGUMENT;
+  j3dg_ctx* c = cv->ctx;
+  if (int rc = scene_ok(c, s)) return rc;
+  if (j3dg::learned_ctx(l) != c || m->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned frame: objects of another context");
+  if (s->n_objects != 1 || s->objects[0].mesh != j3dg::learned_mesh(l))
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned frame: the scene must hold the network's mesh as its only object");
+  for (int i = 0; i < 16; ++i)
+    if (s->objects[0].cs[i] != ((i % 5 == 0) ? 1.f : 0.f))
+      return fail(c, J3DG_ERR_UNSUPPORTED, "learned frame: the network is trained in the mesh's space; its object "
+                                          "transform must be the identity");
+  if (cv->w == 0 || cv->h == 0) return J3DG_OK;
+  cudaSetDevice(c->device);
+  j3dg::canvas_writable(cv);
+  const DevInst* dinst = nullptr;
+  if (int rc = upload_instances(c, s->objects, 1, &dinst)) return rc;
+  FrameParams P;
+  fill_frame(P, cv, s, dinst, m);
+  if (!raster_layout(P, cv, 1, 32, s->objects[0].mesh->nt))
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned frame: canvas scratch too small");
+  cv->last_primary = J3DG_PRIMARY_TRACE;
+  const int mode = shade_mode_of(cv->settings);
+  P.shade_mode = mode == 0 ? 1 : 0;
+  const size_t n = (size_t)cv->w * cv->h;
+  if (n > 0xffffffffu) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "learned frame: canvas too large");
+  // rays and hits: stream-ordered scratch from the context's canvas pool,
+  // which keeps freed memory reserved (no device-wide synchronisation)
+  char* scratch = nullptr;
+  CK(c, cudaMallocFromPoolAsync((void**)&scratch, (sizeof(j3dg_ray) + sizeof(j3dg_hit)) * n, all(c)->ex.canvas_pool,
+                                S(c)),
+     "learned frame");
+  j3dg_ray* rays = reinterpret_cast<j3dg_ray*>(scratch);
+  j3dg_hit* hits = reinterpret_cast<j3dg_hit*>(scratch + sizeof(j3dg_ray) * n);
+  int rc = J3DG_OK;
+  cudaError_t e = j3dg::launch_primary_rays(P, rays, S(c));
+  if (e == cudaSuccess) {
+    rc = j3dg::learned_hits_device(l, rays, (uint32_t)n, hits);
+    if (rc == J3DG_OK) e = j3dg::launch_frame_from_hits(P, hits, S(c));
+    if (rc == J3DG_OK && e == cudaSuccess && mode != 0)
+      e = j3dg::launch_shade(P, (const j3dg_pixel*)cv->d_pixels, mode, 1, S(c));
+  }
+  cudaFreeAsync(scratch, S(c));
+  if (rc != J3DG_OK) return rc;
+  CK(c, e, "learned frame");
+  return J3DG_OK;
+}
+
 // ----------------------------------------------------------------- batches
 
 namespace {
 
-// Packed batch parameters: [FrameParams x n][offsets x (n+1), padded][DevInst x m]
+// Packed batch parameters: [FrameParams x n][offsets x (n+1), padded]
+// [instance table of frame 0][table of frame 1]... (frames without objects
+// take none); frame i's table holds caps[i] objects (table_bytes).
 struct BatchLayout {
-  size_t off_params = 0, off_offsets = 0, off_inst = 0, bytes = 0;
-  uint32_t n = 0, n_inst = 0;
-  void set(uint32_t frames, uint32_t inst) {
+  size_t off_params = 0, off_offsets = 0, bytes = 0;
+  std::vector<size_t> off_table;
+  uint32_t n = 0;
+  void set(uint32_t frames, const uint32_t* caps) {
     n = frames;
-    n_inst = inst;
     off_params = 0;
     off_offsets = (sizeof(FrameParams) * n + 255) & ~size_t(255);
-    off_inst = (off_offsets + sizeof(uint32_t) * (n + 1) + 255) & ~size_t(255);
-    bytes = off_inst + sizeof(DevInst) * (inst ? inst : 1);
+    size_t o = (off_offsets + sizeof(uint32_t) * (n + 1) + 255) & ~size_t(255);
+    off_table.assign(n, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+      off_table[i] = o;
+      if (caps[i]) o += table_bytes(caps[i]);
+    }
+    bytes = o;
   }
 };
 
@@ -1140,35 +1280,67 @@ int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_i
   return J3DG_OK;
 }
 
-// Fills host staging `h` for device base `d` (pointers inside point to `d`).
-// Frame i's objects take cap[i] instance slots (its object count if cap is null).
-// Returns the total primary items of the frames.
-uint32_t pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h, char* d,
-                     const uint32_t* cap = nullptr) {
+// Fills frame i of the host staging `h` for device base `d` (pointers
+// inside point to `d`): its parameters and its instance table (sized for
+// cap objects at creation). walk / fits: the frame's top level is worth
+// walking (two or more objects) / fits the traversal stack.
+void pack_frame(const j3dg_frame& f, uint32_t i, const BatchLayout& L, char* h, char* d, uint32_t cap, bool allow,
+                bool& walk, bool& fits) {
+  FrameParams* P = reinterpret_cast<FrameParams*>(h + L.off_params);
+  const j3dg_scene* s = f.scene;
+  const uint32_t ni = s ? s->n_objects : 0;
+  const DevInst* dI = nullptr;
+  walk = false;
+  fits = true;
+  if (ni) {
+    std::vector<DevInst> t(ni);
+    for (uint32_t j = 0; j < ni; ++j) t[j] = to_dev(s->objects[j]);
+    dI = write_table(h + L.off_table[i], d + L.off_table[i], t.data(), s->objects, ni, cap, walk, &fits);
+    walk = walk && allow;
+  }
+  fill_frame(P[i], f.canvas, s, dI, f.matcap);
+  P[i].shade_mode = shade_mode_of(f.canvas->settings) == 0 ? 1 : 0;
+}
+
+// The launch walks top levels when some frame has two or more objects and
+// every frame's top level fits the traversal stack (a frame with one object
+// has a one-leaf top level, which the walk enters directly).
+bool batch_top(const std::vector<char>& walk, const std::vector<char>& fits) {
+  bool any = false, all = true;
+  for (size_t i = 0; i < walk.size(); ++i) {
+    any = any || walk[i];
+    all = all && fits[i];
+  }
+  return any && all;
+}
+
+// Fills the whole staging; returns the total primary items of the frames.
+uint32_t pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* h, char* d, const uint32_t* cap,
+                     bool allow, std::vector<char>& walk, std::vector<char>& fits, bool& top) {
   FrameParams* P = reinterpret_cast<FrameParams*>(h + L.off_params);
   uint32_t* off = reinterpret_cast<uint32_t*>(h + L.off_offsets);
-  DevInst* I = reinterpret_cast<DevInst*>(h + L.off_inst);
-  DevInst* dI = reinterpret_cast<DevInst*>(d + L.off_inst);
-  uint32_t k = 0, items = 0;
+  uint32_t items = 0;
+  walk.assign(n, 0);
+  fits.assign(n, 1);
   for (uint32_t i = 0; i < n; ++i) {
-    const j3dg_scene* s = f[i].scene;
-    const uint32_t ni = s ? s->n_objects : 0;
-    for (uint32_t j = 0; j < ni; ++j) I[k + j] = to_dev(s->objects[j]);
-    fill_frame(P[i], f[i].canvas, s, ni ? dI + k : nullptr, f[i].matcap);
-    P[i].shade_mode = shade_mode_of(f[i].canvas->settings) == 0 ? 1 : 0;
-    k += cap ? cap[i] : ni;
+    bool w = false, ft = true;
+    pack_frame(f[i], i, L, h, d, cap[i], allow, w, ft);
+    walk[i] = w;
+    fits[i] = ft;
     off[i] = items;
     items += f[i].canvas->w && f[i].canvas->h ? j3dg::primary_items(P[i]) : 0u;
   }
   off[n] = items;
+  top = batch_top(walk, fits);
+  for (uint32_t i = 0; i < n; ++i) P[i].top = top ? 1u : 0u;
   return items;
 }
 
 int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* d, uint32_t items,
-                  uint32_t* work) {
+                  uint32_t* work, bool top) {
   const FrameParams* dP = reinterpret_cast<const FrameParams*>(d + L.off_params);
   const uint32_t* dOff = reinterpret_cast<const uint32_t*>(d + L.off_offsets);
-  CK(c, j3dg::launch_render_batch(dP, dOff, n, items, work, all(c)->ex.batch_threads, S(c)), "batch");
+  CK(c, j3dg::launch_render_batch(dP, dOff, n, items, work, all(c)->ex.batch_threads, top, S(c)), "batch");
   for (uint32_t i = 0; i < n; ++i) {
     const int mode = shade_mode_of(f[i].canvas->settings);
     if (mode != 0 && f[i].canvas->w && f[i].canvas->h) {
@@ -1190,6 +1362,8 @@ struct j3dg_batch {
   std::vector<j3dg_scene> scenes;
   std::vector<uint32_t> caps;  // instance slots of each frame (its object count at creation)
   BatchLayout L;
+  std::vector<char> walk, fits;  // per frame (pack_frame)
+  bool top = false;              // the captured launch walks top levels
   char* h = nullptr;  // pinned staging
   char* d = nullptr;  // device copy
   uint32_t* work = nullptr;
@@ -1205,17 +1379,21 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
   uint32_t total_inst = 0;
   if (int rc = check_frames(c, f, n, total_inst)) return rc;
   for (uint32_t i = 0; i < n; ++i) j3dg::canvas_writable(f[i].canvas);
+  std::vector<uint32_t> caps(n);
+  for (uint32_t i = 0; i < n; ++i) caps[i] = f[i].scene ? f[i].scene->n_objects : 0u;
   BatchLayout L;
-  L.set(n, total_inst);
+  L.set(n, caps.data());
   char* d = nullptr;
   uint32_t* work = nullptr;
   std::vector<char> h(L.bytes);
   CK(c, cudaMallocAsync((void**)&d, L.bytes + 256, S(c)), "render_batch");
   work = reinterpret_cast<uint32_t*>(d + L.bytes);
-  const uint32_t items = pack_frames(f, n, L, h.data(), d);
+  bool top = false;
+  std::vector<char> walk, fits;
+  const uint32_t items = pack_frames(f, n, L, h.data(), d, caps.data(), all(c)->ex.top_level, walk, fits, top);
   // pageable source: the copy is staged before the call returns
   CK(c, cudaMemcpyAsync(d, h.data(), L.bytes, cudaMemcpyHostToDevice, S(c)), "render_batch");
-  int rc = enqueue_batch(c, f, n, L, d, items, work);
+  int rc = enqueue_batch(c, f, n, L, d, items, work, top);
   cudaFreeAsync(d, S(c));
   return rc;
 }
@@ -1243,7 +1421,7 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
       b->frames[i].scene = &b->scenes[i];
     }
   }
-  b->L.set(n, total_inst);
+  b->L.set(n, b->caps.data());
   cudaError_t e = cudaMallocHost((void**)&b->h, b->L.bytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d, b->L.bytes + 256);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
@@ -1252,14 +1430,15 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
     return cuda_fail(c, e, "batch_create");
   }
   b->work = reinterpret_cast<uint32_t*>(b->d + b->L.bytes);
-  const uint32_t items = pack_frames(b->frames.data(), n, b->L, b->h, b->d);
+  const uint32_t items =
+      pack_frames(b->frames.data(), n, b->L, b->h, b->d, b->caps.data(), all(c)->ex.top_level, b->walk, b->fits, b->top);
   // capture: upload of the staged parameters, the launch and the shading passes
   cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   e = cudaStreamBeginCapture(S(c), mode);
   int rc = J3DG_OK;
   if (e == cudaSuccess) {
     e = cudaMemcpyAsync(b->d, b->h, b->L.bytes, cudaMemcpyHostToDevice, S(c));
-    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work);
+    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work, b->top);
     cudaError_t e2 = cudaStreamEndCapture(S(c), &b->graph);
     if (e == cudaSuccess) e = e2;
   }
@@ -1283,16 +1462,34 @@ int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* s) {
       return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_set_scene: bad scene object");
   cudaSetDevice(c->device);
   CK(c, cudaEventSynchronize(b->done), "batch_set_scene");  // the staging is read by the running launch
+  const std::vector<j3dg_instance> old_objects = b->objects[i];
+  const j3dg_scene old_scene = b->scenes[i];
   b->objects[i].assign(s->objects, s->objects + s->n_objects);
   b->scenes[i] = *s;
   b->scenes[i].objects = b->objects[i].data();
-  // frame k keeps the instance slots it had at creation
-  std::vector<uint32_t> caps(b->frames.size());
-  for (size_t k = 0; k < caps.size(); ++k) caps[k] = b->caps[k];
-  std::vector<j3dg_frame> fr = b->frames;
-  for (size_t k = 0; k < fr.size(); ++k)
-    if (fr[k].scene) fr[k].scene = &b->scenes[k];
-  pack_frames(fr.data(), (uint32_t)fr.size(), b->L, b->h, b->d, caps.data());
+  // frame i keeps the instance slots it had at creation; the captured
+  // launch keeps its top-level choice, so a scene that would change it is
+  // refused (and the frame keeps its previous scene)
+  j3dg_frame fr = b->frames[i];
+  fr.scene = &b->scenes[i];
+  const bool was_walk = b->walk[i], was_fits = b->fits[i];
+  bool w = false, ft = true;
+  pack_frame(fr, i, b->L, b->h, b->d, b->caps[i], all(c)->ex.top_level, w, ft);
+  b->walk[i] = w;
+  b->fits[i] = ft;
+  if (batch_top(b->walk, b->fits) != b->top) {
+    b->objects[i].assign(old_objects.begin(), old_objects.end());
+    b->scenes[i] = old_scene;
+    b->scenes[i].objects = b->objects[i].data();
+    fr.scene = &b->scenes[i];
+    pack_frame(fr, i, b->L, b->h, b->d, b->caps[i], all(c)->ex.top_level, w, ft);
+    b->walk[i] = was_walk;
+    b->fits[i] = was_fits;
+    reinterpret_cast<FrameParams*>(b->h + b->L.off_params)[i].top = b->top ? 1u : 0u;
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT,
+                "batch_set_scene: the new scene changes whether the batch walks top levels; create a new batch");
+  }
+  reinterpret_cast<FrameParams*>(b->h + b->L.off_params)[i].top = b->top ? 1u : 0u;
   return J3DG_OK;
 }
 

@@ -47,6 +47,32 @@ struct DevInst {
   float inv[16];
 };
 
+// Header of every instance table, just in front of its first DevInst (the
+// kernels receive &inst[0]): the per-frame top level over the objects' world
+// boxes (the two-level structure of canvas.cpp:762; built on the host,
+// toplevel.cpp), whose nodes follow the table. Leaves hold one object:
+// ref = J3DG_LEAF_BIT | object << 3.
+struct DevTop {
+  const float4* nodes;  // BVH4 nodes, or null when the table has no top level
+  uint32_t root;        // inner node 0, or the leaf of the only object
+  uint32_t n_nodes;
+  uint32_t n_inst;
+  float pad_scale;      // max |coordinate| of the padded object boxes
+  uint32_t reserved[2];
+};
+static_assert(sizeof(DevTop) % 16 == 0, "the instance table follows the header");
+static_assert(sizeof(DevInst) % 16 == 0, "top-level nodes follow the instance table");
+
+__device__ __forceinline__ const DevTop& top_of(const DevInst* insts) {
+  return reinterpret_cast<const DevTop*>(insts)[-1];
+}
+
+// inst while the walk is in the top level; stack entry that returns the walk
+// from an object to the top level (J3DG_LEAF_BIT with a first triangle beyond
+// J3DG_MAX_TRIANGLES: never a leaf of a mesh)
+static const uint32_t kTopInst = 0xffffffffu;
+static const uint32_t kPopTop = 0xfffffffeu;
+
 __device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
@@ -96,6 +122,24 @@ __device__ __forceinline__ void prep_axis(float o, float d, float pad, float& in
   float of = neg ? fa(o, pad) : fs(o, pad);
   nn = fm(-on, inv);
   nf = fm(-of, inv);
+}
+
+__device__ __forceinline__ Ray make_ray_pad(float ox, float oy, float oz, float dx, float dy, float dz, float t_near,
+                                            float pad) {
+  Ray r;
+  r.ox = ox;
+  r.oy = oy;
+  r.oz = oz;
+  r.dx = dx;
+  r.dy = dy;
+  r.dz = dz;
+  r.t_near = t_near;
+  bool nx, ny, nz;
+  prep_axis(ox, dx, pad, r.ix, r.nnx, r.nfx, nx);
+  prep_axis(oy, dy, pad, r.iy, r.nny, r.nfy, ny);
+  prep_axis(oz, dz, pad, r.iz, r.nnz, r.nfz, nz);
+  r.neg = (nx ? 1u : 0u) | (ny ? 2u : 0u) | (nz ? 4u : 0u);
+  return r;
 }
 
 __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float dx, float dy, float dz, float t_near,
@@ -230,12 +274,18 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
 }
 
 // Resumable traversal of one world ray over all objects of the scene
-// (qbvh_two_level_with_transformations::find_closest_triangle): the ray is
-// taken to each object's space (origin as a point, direction as a vector) and
-// that object's BVH4 is walked with a per-thread stack. run() advances by at
-// most `iters` node or leaf steps, so persistent warps can refill lanes whose
-// rays have finished. Corrupt trees raise status bits instead of trapping.
-template <int N>
+// (qbvh_two_level_with_transformations::find_closest_triangle): in an
+// object the ray is in that object's space (origin as a point, direction as
+// a vector) and the object's BVH4 is walked with a per-thread stack. With
+// TOP, the walk starts in the table's top level (a BVH4 over the objects'
+// world boxes) with the world ray; a top-level leaf pushes a kPopTop entry
+// (which carries the top level's remaining visit budget) and enters its
+// object; popping that entry takes the world ray back to the top level.
+// Without TOP the objects are walked one after the other. run() advances by
+// at most `iters` node or leaf steps, so persistent warps can refill lanes
+// whose rays have finished. Corrupt trees raise status bits instead of
+// trapping.
+template <int N, bool TOP = false>
 struct TracerT {
 #if J3DG_COLD_SMEM & 1
   // world ray: read only when an object's walk starts, kept in shared memory
@@ -245,14 +295,14 @@ struct TracerT {
   __device__ __forceinline__ float& wr(int k) { return wr_[k]; }
 #endif
   bool any;                             // stop at the first accepted triangle
-  Ray r;                                // object-space ray of object `inst`
+  Ray r;                                // object-space ray of object `inst` (world ray in the top level)
   BestT<N> b;
   const float4* nodes;
   const float4* tris;
   uint32_t n_nodes, nt;
   uint32_t cur;
   int sp;
-  uint32_t inst;
+  uint32_t inst;                        // kTopInst while in the top level
   uint32_t budget;
 
   __device__ __forceinline__ void start_object(const DevInst* __restrict__ insts) {
@@ -265,8 +315,23 @@ struct TracerT {
     n_nodes = I.n_nodes;
     nt = I.nt;
     cur = I.root_ref;
-    sp = 0;
     budget = n_nodes + 1;
+  }
+
+  // the top level with the world ray; its slab test is padded by
+  // (max|origin| + pad_scale) 2^-12 so that it never culls an object that
+  // holds an object-space hit (toplevel.cpp)
+  __device__ __forceinline__ void start_top(const DevInst* __restrict__ insts, uint32_t bud) {
+    const DevTop& H = top_of(insts);
+    const float ox = wr(0), oy = wr(1), oz = wr(2);
+    const float mo = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+    r = make_ray_pad(ox, oy, oz, wr(3), wr(4), wr(5), r.t_near, fm(fa(mo, H.pad_scale), 0x1p-12f));
+    nodes = H.nodes;
+    tris = nullptr;
+    n_nodes = H.n_nodes;
+    nt = H.n_inst;
+    inst = kTopInst;
+    budget = bud;
   }
 
   // Returns true if the ray is already finished (no objects).
@@ -286,9 +351,16 @@ struct TracerT {
     b.inst() = b.tri() = 0;
     b.u() = b.v() = 0.f;
     b.slot() = 0;
-    inst = 0;
+    sp = 0;
     if (n_inst == 0) return true;
-    start_object(insts);
+    if (TOP) {
+      const DevTop& H = top_of(insts);
+      start_top(insts, H.n_nodes + 1);
+      cur = H.root;
+    } else {
+      inst = 0;
+      start_object(insts);
+    }
     return false;
   }
 
@@ -304,8 +376,8 @@ struct TracerT {
     return false;
   }
 
-  // One traversal step: a pop, a leaf (its triangles) or a node. Returns
-  // true when the ray is finished.
+  // One traversal step: a pop, a leaf (its triangles, or with TOP an
+  // object entered) or a node. Returns true when the ray is finished.
   __device__ __forceinline__ bool step(const DevInst* __restrict__ insts, uint32_t n_inst, uint32_t* status,
                                        uint32_t& visits, uint32_t& tests, uint2* __restrict__ stack) {
     {
@@ -314,6 +386,10 @@ struct TracerT {
         while (sp > 0) {
           --sp;
           const uint2 e = stack[sp];
+          if (TOP && e.x == kPopTop) {  // the object is done: back to the top level
+            start_top(insts, e.y);
+            continue;
+          }
           if (__uint_as_float(e.y) <= b.t) {
             cur = e.x;
             got = true;
@@ -321,6 +397,7 @@ struct TracerT {
           }
         }
         if (!got) {
+          if (TOP) return true;
           if (++inst >= n_inst) return true;
           start_object(insts);
           return false;
@@ -331,6 +408,18 @@ struct TracerT {
         if (first + cnt > nt) {
           atomicOr(status, J3DG_DEV_BAD_INDEX);
           return true;
+        }
+        if (TOP && inst == kTopInst) {
+          // a top-level leaf: walk its object, then come back
+          if (cnt != 1u || sp + 1 > J3DG_STACK) {
+            atomicOr(status, cnt != 1u ? J3DG_DEV_BAD_INDEX : J3DG_DEV_STACK_OVERFLOW);
+            return true;
+          }
+          stack[sp] = make_uint2(kPopTop, budget);
+          ++sp;
+          inst = first;
+          start_object(insts);
+          return false;
         }
 #pragma unroll 1
         for (uint32_t k = 0; k < cnt; ++k) {
@@ -349,14 +438,14 @@ struct TracerT {
         return true;
       }
       ++visits;
-      const float4* N = nodes + 8 * (size_t)cur;
+      const float4* nd = nodes + 8 * (size_t)cur;
       // near / far planes by the ray's octant: the same values slab() selects,
       // picked by the load offsets instead of per-child selects
       const uint32_t ox = r.neg & 1u, oy = (r.neg >> 1) & 1u, oz = (r.neg >> 2) & 1u;
-      const float4 nx4 = __ldg(N + ox), fx4 = __ldg(N + (ox ^ 1u));
-      const float4 ny4 = __ldg(N + 2 + oy), fy4 = __ldg(N + 2 + (oy ^ 1u));
-      const float4 nz4 = __ldg(N + 4 + oz), fz4 = __ldg(N + 4 + (oz ^ 1u));
-      const float4 chf = __ldg(N + 6);
+      const float4 nx4 = __ldg(nd + ox), fx4 = __ldg(nd + (ox ^ 1u));
+      const float4 ny4 = __ldg(nd + 2 + oy), fy4 = __ldg(nd + 2 + (oy ^ 1u));
+      const float4 nz4 = __ldg(nd + 4 + oz), fz4 = __ldg(nd + 4 + (oz ^ 1u));
+      const float4 chf = __ldg(nd + 6);
       float tc[4];
       uint32_t rc[4] = {__float_as_uint(chf.x), __float_as_uint(chf.y), __float_as_uint(chf.z),
                         __float_as_uint(chf.w)};
@@ -400,7 +489,8 @@ struct TracerT {
 #if J3DG_PREFETCH
       // the next step starts with this child: its line is requested now, so
       // the fetch runs while the warp finishes the other lanes' branches
-      if (cur != J3DG_EMPTY_REF) {
+      // (not in the top level, whose leaves are objects, not triangles)
+      if (cur != J3DG_EMPTY_REF && !(TOP && inst == kTopInst)) {
         const bool leaf = (cur & J3DG_LEAF_BIT) != 0;
         const uint32_t first = (cur & 0x7fffffffu) >> 3;
         if (leaf ? first + (cur & 7u) + 1u <= nt : cur < n_nodes) {  // the checks the next step makes
@@ -420,11 +510,11 @@ struct TracerT {
 // (returns false when the item needs no tracing and was handled) and
 // finish(); ITERS node/leaf steps run between refills.
 // N: the kernel's block size.
-template <int ITERS, int N, class Src>
+template <int ITERS, int N, bool TOP, class Src>
 __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __restrict__ insts, uint32_t n_inst,
                                                  uint32_t* counter, uint32_t* status,
                                                  unsigned long long* counters) {
-  TracerT<N> T;
+  TracerT<N, TOP> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = src.count();

@@ -1118,6 +1118,37 @@ int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n,
   return rc;
 }
 
+}  // extern "C"
+
+namespace j3dg {
+
+// Learned closest hits of device rays into device hits, queued on the
+// context stream (no synchronisation): top-2 clusters by the fused network,
+// then the exact traversal seeded by them.
+int learned_hits_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits) {
+  if (n == 0) return J3DG_OK;
+  uint32_t* dt = nullptr;
+  LCK(cudaMallocAsync((void**)&dt, sizeof(uint32_t) * 2 * n, LS(l)), "learned hits");
+  int rc = predict_device(l, d_rays, n, dt);
+  const DevInst* dinst = nullptr;
+  if (rc == J3DG_OK) rc = mesh_devinst(l->ctx, l->mesh, &dinst);
+  if (rc == J3DG_OK) {
+    k_rays_learned<<<(n + 127) / 128, 128, 0, LS(l)>>>(dinst, d_rays, n, dt, l->d_roots, l->n_clusters, d_hits,
+                                                      l->ctx->d_status, ctx_counters(l->ctx), nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = ctx_fail(l->ctx, J3DG_ERR_CUDA, std::string("learned hits: ") + cudaGetErrorString(e));
+  }
+  cudaFreeAsync(dt, LS(l));
+  return rc;
+}
+
+const j3dg_mesh* learned_mesh(const j3dg_learned* l) { return l->mesh; }
+j3dg_ctx* learned_ctx(const j3dg_learned* l) { return l->ctx; }
+
+}  // namespace j3dg
+
+extern "C" {
+
 int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits) {
   return j3dg_learned_find_closest_stats(l, rays, n, hits, nullptr);
 }

@@ -742,17 +742,18 @@ struct ShadowSrc {
   }
 };
 
+template <bool TOP>
 __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_shadow(const FrameParams P) {
   if (P.rlist[1]) return;
   ShadowSrc src{&P, shadow_jobs(P), P.work[1], light_position(P)};
-  persistent_trace<kIters, kTraceThreads>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
+  persistent_trace<kIters, kTraceThreads, TOP>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
 }
 
-template <bool kThroughput>
+template <bool kThroughput, bool TOP>
 __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
     k_frame(const FrameParams P) {
   if (P.raster && P.rlist[1] == 0u) return;  // the raster kernels made this frame
-  TracerT<kTraceThreads> T;
+  TracerT<kTraceThreads, TOP> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
@@ -854,13 +855,13 @@ struct BatchSrc {
   }
 };
 
-template <bool ANY>
+template <bool ANY, bool TOP>
 __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restrict__ inst, uint32_t n_inst,
                                                         const j3dg_ray* __restrict__ rays, uint32_t n,
                                                         j3dg_hit* __restrict__ hits, uint32_t* counter,
                                                         uint32_t* status, unsigned long long* counters) {
   BatchSrc<ANY> src{rays, hits, n};
-  persistent_trace<kIters, kTraceThreads>(src, inst, n_inst, counter, status, counters);
+  persistent_trace<kIters, kTraceThreads, TOP>(src, inst, n_inst, counter, status, counters);
 }
 
 // Many frames (canvases, scenes, cameras, resolutions of uneven size) in one
@@ -875,11 +876,11 @@ struct MinBlocks {  // the same warps per SM as k_frame
   static const int value = TPB >= 256 ? per128 / 2 : (TPB >= 128 ? per128 : 2 * per128);
 };
 
-template <int TPB, bool kThroughput>
+template <int TPB, bool kThroughput, bool TOP>
 __global__ void __launch_bounds__(TPB, (MinBlocks<TPB, kThroughput>::value))
     k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
                   uint32_t* work) {
-  TracerT<TPB> T;
+  TracerT<TPB, TOP> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t total = offsets[n_frames];
@@ -966,6 +967,48 @@ __global__ void __launch_bounds__(TPB, (MinBlocks<TPB, kThroughput>::value))
     atomicAdd(counters + 0, (unsigned long long)visits);
     atomicAdd(counters + 1, (unsigned long long)tests);
   }
+}
+
+// --------------------------------------- primary hits from outside ----
+//
+// Frames whose primary hits another traversal found (the learned path):
+// k_primary_rays writes the frame's primary rays (row-major over the
+// rectangle, the same rays k_frame traces), the caller fills j3dg_hit per
+// ray, k_keys_from_hits turns them into the raster keys, and the raster
+// path's back half (k_resolve, k_shadow) makes the G-buffer records, the
+// shadow rays and the plain shading from there.
+
+__global__ void k_primary_rays(const FrameParams P, j3dg_ray* __restrict__ out) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rw * rh) return;
+  float4 o, d;
+  primary_ray(P, P.x0 + (int)(i % rw), P.y0 + (int)(i / rw), o, d);
+  float* f = reinterpret_cast<float*>(out + i);
+  f[0] = o.x;
+  f[1] = o.y;
+  f[2] = o.z;
+  f[3] = 1.f;
+  f[4] = d.x;
+  f[5] = d.y;
+  f[6] = d.z;
+  f[7] = 0.f;
+  f[8] = primary_t_near(P);
+  f[9] = FLT_MAX;
+}
+
+__global__ void k_keys_from_hits(const FrameParams P, const j3dg_hit* __restrict__ hits) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    P.rlist[1] = 0u;  // no overflow: k_resolve and k_shadow run
+    P.work[1] = P.work[2] = 0u;
+  }
+  if (i >= rw * rh) return;
+  const j3dg_hit h = hits[i];
+  const size_t pix = (size_t)(P.y0 + (int)(i / rw)) * P.w + (P.x0 + (int)(i % rw));
+  const uint32_t low = P.id_bits >= 32u ? h.object_id : ((h.two_level_index << P.id_bits) | h.object_id);
+  P.keys[pix] = h.found ? ((unsigned long long)__float_as_uint(h.distance) << 32 | low) : ~0ull;
 }
 
 template <class K>
@@ -1112,17 +1155,19 @@ __global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
   if (rw <= 0 || rh <= 0) return cudaSuccess;
-  static int blocks_t = 0, blocks_l = 0;
+  static int blocks_t = 0, blocks_l = 0, blocks_tt = 0, blocks_lt = 0;
   if (!blocks_t) {
-    blocks_t = persistent_blocks(k_frame<true>);
-    blocks_l = persistent_blocks(k_frame<false>);
+    blocks_t = persistent_blocks(k_frame<true, false>);
+    blocks_l = persistent_blocks(k_frame<false, false>);
+    blocks_tt = persistent_blocks(k_frame<true, true>);
+    blocks_lt = persistent_blocks(k_frame<false, true>);
   }
   cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (P.raster) {
     static int blocks_s = 0, blocks_t = 0, blocks_r = 0;
     if (!blocks_s) {
-      blocks_s = persistent_blocks(k_shadow);
+      blocks_s = persistent_blocks(k_shadow<false>);
       blocks_t = persistent_blocks(k_raster_test, kRasterThreads);
       blocks_r = persistent_blocks(k_raster<false>, kRasterThreads);
     }
@@ -1138,42 +1183,56 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
     k_raster_large<<<dim3(16, 64), kRasterThreads, 0, st>>>(P);
     k_raster_test<<<blocks_t, kRasterThreads, 0, st>>>(P);
     k_resolve<<<(unsigned)(((size_t)rw * rh + kResolveThreads - 1) / kResolveThreads), kResolveThreads, 0, st>>>(P);
-    k_shadow<<<blocks_s, kTraceThreads, 0, st>>>(P);
+    if (P.top)
+      k_shadow<true><<<blocks_s, kTraceThreads, 0, st>>>(P);
+    else
+      k_shadow<false><<<blocks_s, kTraceThreads, 0, st>>>(P);
     // k_frame below returns at once unless the large-triangle list overflowed
   }
-  if (primary_items(P) >= J3DG_THROUGHPUT_ITEMS)
-    k_frame<true><<<blocks_t, kTraceThreads, 0, st>>>(P);
-  else
-    k_frame<false><<<blocks_l, kTraceThreads, 0, st>>>(P);
+  const bool thr = primary_items(P) >= J3DG_THROUGHPUT_ITEMS;
+  if (P.top) {
+    if (thr)
+      k_frame<true, true><<<blocks_tt, kTraceThreads, 0, st>>>(P);
+    else
+      k_frame<false, true><<<blocks_lt, kTraceThreads, 0, st>>>(P);
+  } else {
+    if (thr)
+      k_frame<true, false><<<blocks_t, kTraceThreads, 0, st>>>(P);
+    else
+      k_frame<false, false><<<blocks_l, kTraceThreads, 0, st>>>(P);
+  }
   return cudaGetLastError();
 }
 
-template <bool kT>
+template <bool kT, bool TOP>
 static cudaError_t launch_batch_variant(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
                                         uint32_t* work, int block_threads, cudaStream_t st) {
   static int b64 = 0, b128 = 0, b256 = 0;
   if (!b64) {
-    b64 = persistent_blocks(k_frame_batch<64, kT>, 64);
-    b128 = persistent_blocks(k_frame_batch<128, kT>, 128);
-    b256 = persistent_blocks(k_frame_batch<256, kT>, 256);
+    b64 = persistent_blocks(k_frame_batch<64, kT, TOP>, 64);
+    b128 = persistent_blocks(k_frame_batch<128, kT, TOP>, 128);
+    b256 = persistent_blocks(k_frame_batch<256, kT, TOP>, 256);
   }
   if (block_threads == 64)
-    k_frame_batch<64, kT><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
+    k_frame_batch<64, kT, TOP><<<b64, 64, 0, st>>>(d_params, d_offsets, n_frames, work);
   else if (block_threads == 256)
-    k_frame_batch<256, kT><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
+    k_frame_batch<256, kT, TOP><<<b256, 256, 0, st>>>(d_params, d_offsets, n_frames, work);
   else
-    k_frame_batch<128, kT><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
+    k_frame_batch<128, kT, TOP><<<b128, 128, 0, st>>>(d_params, d_offsets, n_frames, work);
   return cudaGetLastError();
 }
 
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t total_items, uint32_t* work, int block_threads, cudaStream_t st) {
+                                uint32_t total_items, uint32_t* work, int block_threads, bool top, cudaStream_t st) {
   if (n_frames == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  return total_items >= J3DG_THROUGHPUT_ITEMS
-             ? launch_batch_variant<true>(d_params, d_offsets, n_frames, work, block_threads, st)
-             : launch_batch_variant<false>(d_params, d_offsets, n_frames, work, block_threads, st);
+  const bool thr = total_items >= J3DG_THROUGHPUT_ITEMS;
+  if (top)
+    return thr ? launch_batch_variant<true, true>(d_params, d_offsets, n_frames, work, block_threads, st)
+               : launch_batch_variant<false, true>(d_params, d_offsets, n_frames, work, block_threads, st);
+  return thr ? launch_batch_variant<true, false>(d_params, d_offsets, n_frames, work, block_threads, st)
+             : launch_batch_variant<false, false>(d_params, d_offsets, n_frames, work, block_threads, st);
 }
 
 uint32_t primary_items(const FrameParams& P) {
@@ -1205,20 +1264,49 @@ cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters, cudaStream_t st) {
+cudaError_t launch_primary_rays(const FrameParams& P, j3dg_ray* out, cudaStream_t st) {
+  const uint32_t n = (uint32_t)(P.x1 - P.x0 + 1) * (uint32_t)(P.y1 - P.y0 + 1);
+  if (n == 0) return cudaSuccess;
+  k_primary_rays<<<(n + 255) / 256, 256, 0, st>>>(P, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame_from_hits(const FrameParams& P, const j3dg_hit* hits, cudaStream_t st) {
+  const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
+  if (rw * rh == 0) return cudaSuccess;
+  static int blocks_s = 0;
+  if (!blocks_s) blocks_s = persistent_blocks(k_shadow<false>);
+  k_keys_from_hits<<<(rw * rh + 255) / 256, 256, 0, st>>>(P, hits);
+  k_resolve<<<(rw * rh + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(P);
+  if (P.top)
+    k_shadow<true><<<blocks_s, kTraceThreads, 0, st>>>(P);
+  else
+    k_shadow<false><<<blocks_s, kTraceThreads, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, const j3dg_ray* rays, uint32_t n,
+                        j3dg_hit* hits, bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters,
+                        cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   static int blocks_c = 0, blocks_a = 0;
   if (!blocks_c) {
-    blocks_c = persistent_blocks(k_rays<false>);
-    blocks_a = persistent_blocks(k_rays<true>);
+    blocks_c = persistent_blocks(k_rays<false, false>);
+    blocks_a = persistent_blocks(k_rays<true, false>);
   }
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  if (any)
-    k_rays<true><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
-  else
-    k_rays<false><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
+  if (top) {
+    if (any)
+      k_rays<true, true><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
+    else
+      k_rays<false, true><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
+  } else {
+    if (any)
+      k_rays<true, false><<<blocks_a, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
+    else
+      k_rays<false, false><<<blocks_c, kTraceThreads, 0, st>>>(inst, n_inst, rays, n, hits, counter, status, counters);
+  }
   return cudaGetLastError();
 }
 

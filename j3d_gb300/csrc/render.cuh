@@ -32,6 +32,7 @@ static const uint32_t kRasterEntryWords = 8;  // inst, slot, x0, y0, x1, y1, -, 
 struct FrameParams {
   const DevInst* inst;
   uint32_t n_inst;
+  uint32_t top;  // 1: the instance table carries a top level and the kernels walk it
   uint32_t w, h;
   int x0, y0, x1, y1;
   float cs[16], cs_inv[16], pinv[16];
@@ -66,14 +67,21 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
 // all frames in one persistent launch; offsets = prefix sums of primary_items
 // total_items = offsets[n_frames] (the sum of primary_items of the frames)
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t total_items, uint32_t* work, int block_threads, cudaStream_t st);
+                                uint32_t total_items, uint32_t* work, int block_threads, bool top, cudaStream_t st);
 uint32_t primary_items(const FrameParams& P);
 // mode: 0 plain, 1 edges, 2 wireframe, 3 one-bit
 cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st);
+// primary rays of the frame's rectangle, row-major (the rays k_frame traces)
+cudaError_t launch_primary_rays(const FrameParams& P, j3dg_ray* out, cudaStream_t st);
+// a frame from primary hits found elsewhere (one j3dg_hit per ray of
+// launch_primary_rays): hit records, shadow rays, plain shading; P needs the
+// raster scratch layout (keys, jobs, list) of its canvas
+cudaError_t launch_frame_from_hits(const FrameParams& P, const j3dg_hit* hits, cudaStream_t st);
 cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaStream_t st);
 cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st);
-cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits,
-                        bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, const j3dg_ray* rays, uint32_t n,
+                        j3dg_hit* hits, bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters,
+                        cudaStream_t st);
 
 }  // namespace j3dg

@@ -82,6 +82,13 @@ class Learned:
         _check(self.ctx.h, lib().j3dg_learned_find_closest_stats(self.h, vptr(rays), len(rays), vptr(hits), st))
         return hits, dict(zip(("cluster_visits", "cluster_tests", "exact_visits", "exact_tests"), list(st)))
 
+    def render_frame(self, canvas, scene, matcap) -> None:
+        """A canvas frame whose primary hits come from the learned path
+        (asynchronous on the context stream); equal to canvas.render_frame."""
+        s, keep = scene.as_c()
+        _check(self.ctx.h, lib().j3dg_learned_render_frame(self.h, canvas.h, C.byref(s), matcap.h))
+        del keep
+
     def get_params(self) -> np.ndarray:
         out = np.zeros(self.n_params, np.float32)
         _check(self.ctx.h, lib().j3dg_learned_get_params(self.h, vptr(out)))

@@ -90,6 +90,11 @@ class Context:
         pixel); the hits are the same."""
         _check(self.h, lib().j3dg_ctx_set_primary_mode(self.h, mode))
 
+    def set_top_level(self, on: bool) -> None:
+        """Walk scenes of several objects through a per-frame top-level BVH
+        (default) or object after object (for measurement)."""
+        _check(self.h, lib().j3dg_ctx_set_top_level(self.h, 1 if on else 0))
+
     def memory(self) -> dict:
         """Device free / total bytes and the reserved / used bytes of the
         context's canvas pool and of the device's default pool."""

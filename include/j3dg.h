@@ -489,9 +489,9 @@ int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, flo
    fused inference kernel (tcgen05, activations and logits kept on chip). */
 int j3dg_learned_predict(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2);
 /* The same with a choice of implementation: 1 the fused tcgen05 kernel, 0 the
-   layer-by-layer mma.sync GEMMs of training plus a top-2 pass over the
-   logits. Both round activations to bf16 at the same points; the fp32
-   accumulation order differs, so near-ties may rank differently. */
+   layer-by-layer tcgen05 GEMMs of training (fused epilogues) plus a top-2
+   pass over the logits. Both round activations to bf16 at the same points;
+   the fp32 accumulation order differs, so near-ties may rank differently. */
 int j3dg_learned_predict_impl(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, uint32_t* top2, int impl);
 /* Closest hits through the learned tmax (host or device arrays). */
 int j3dg_learned_find_closest(j3dg_learned* l, const j3dg_ray* rays, uint32_t n, j3dg_hit* hits);
@@ -510,7 +510,6 @@ int j3dg_learned_set_params(j3dg_learned* l, const float* in);
    multiple of 128) and labels (-1 = no hit), for gradient checks. */
 int j3dg_learned_loss_grad(j3dg_learned* l, const float* features, const int32_t* labels, uint32_t B, float* loss,
                            float* grads);
-/* Checkpoint (header + fp32 parameters). */
 /* A whole canvas frame (canvas::render_scene's update_canvas + canvas_to_image,
    canvas.cpp:677-874, 582-670) whose primary hits come from the learned
    path: the frame's primary rays go through the network and the exact
@@ -520,15 +519,17 @@ int j3dg_learned_loss_grad(j3dg_learned* l, const float* features, const int32_t
    transform (the network works in the mesh's space). */
 int j3dg_learned_render_frame(j3dg_learned* l, j3dg_canvas* canvas, const j3dg_scene* scene,
                               const j3dg_matcap* matcap);
+/* Checkpoint (header + fp32 parameters). */
 int j3dg_learned_save(j3dg_learned* l, const char* path);
 int j3dg_learned_load(j3dg_learned* l, const char* path);
 
-/* Diagnostics (no reference counterpart): the network's two bf16
-   tensor-core GEMMs, C[M x N] fp32 = A[M x K] . Bt[N x K]^T on device
-   arrays (A, Bt bf16 row-major). impl 0: mma.sync (M, N % 128, K % 32);
-   impl 1: tcgen05 with a TMEM accumulator (M, N % 128, K % 64); impl 2: the
-   tcgen05 kernel with its MMAs withheld, so that its bounded mbarrier wait
-   runs out (~0.25 s): the call must return J3DG_ERR_DEVICE_STATUS with
+/* Diagnostics (no reference counterpart): the network's bf16 tensor-core
+   GEMM (tcgen05, accumulator in tensor memory; M, N % 128, K % 64),
+   C[M x N] fp32 = A[M x K] . Bt[N x K]^T on device arrays (A, Bt bf16
+   row-major). impl 1: one CTA per output tile; impl 0: split-K, CTAs over
+   K ranges adding into C with atomics (the weight gradients' form); impl 2:
+   the kernel with its MMAs withheld, so that its bounded mbarrier wait runs
+   out (~0.25 s): the call must return J3DG_ERR_DEVICE_STATUS with
    J3DG_DEV_VISIT_CAP raised, and the context stays usable. Synchronous. */
 int j3dg_gemm_bf16(j3dg_ctx* ctx, const void* A, const void* Bt, float* C, uint32_t M, uint32_t N, uint32_t K,
                    int impl);

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-c
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
-CU_SOURCES = ["build.cu", "render.cu", "query.cu", "mlp_gemm.cu", "umma_gemm.cu", "learned.cu", "ingest.cu", "pointcloud.cu", "api.cu"]
+CU_SOURCES = ["build.cu", "render.cu", "query.cu", "umma_gemm.cu", "learned.cu", "ingest.cu", "pointcloud.cu", "api.cu"]
 CXX_SOURCES = ["host_math.cpp", "ingest_parse.cpp", "toplevel.cpp"]
 
 

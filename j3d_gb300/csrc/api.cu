@@ -1184,11 +1184,13 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
 
 // ------------------------------------------------------- learned frames
 
-namespace j3dg {
+extern "C++" {
+namespace j3dg {  // learned.cu
 int learned_hits_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits);
 const j3dg_mesh* learned_mesh(const j3dg_learned* l);
 j3dg_ctx* learned_ctx(const j3dg_learned* l);
 }  // namespace j3dg
+}
 
 int j3dg_learned_render_frame(j3dg_learned* l, j3dg_canvas* cv, const j3dg_scene* s, const j3dg_matcap* m) {
   if (!l || !cv || !s || !m) return J3DG_ERR_INVALID_ARGUMENT;

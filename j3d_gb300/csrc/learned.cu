@@ -3,8 +3,9 @@
 // A small network maps a ray (origin, direction) to a cluster of the mesh:
 // 16-band Fourier features of the 6 ray coordinates (192 values, padded to
 // 256), four 128-wide GELU layers, 4096 cluster logits; bf16 weights, fp32
-// accumulation (mma.sync tensor-core GEMMs of mlp_gemm.cu), trained with
-// softmax cross-entropy and Adam on rays traced by the plain method.
+// accumulation on the tcgen05 tensor cores (the GEMMs with fused epilogues
+// of umma_gemm.cu for training, one fused kernel for inference), trained
+// with softmax cross-entropy and Adam on rays traced by the plain method.
 // Clusters are the BVH4 subtrees at a fixed depth (depth 6: at most 4096),
 // which are Morton-ordered ranges of the mesh because the tree is an LBVH.
 //
@@ -175,6 +176,23 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   p[i] = pi;
   pb[i] = __float2bfloat16(pi);
+}
+
+// dst[c * ldd + r] = src[r * lds + c] for r < rows, c < cols (32 x 32 tiles
+// through shared memory, so both sides are read and written along rows)
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ src, int rows, int cols, int lds,
+                                 __nv_bfloat16* __restrict__ dst, int ldd) {
+  __shared__ __nv_bfloat16 t[32][34];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[i][threadIdx.x] = src[(size_t)r * lds + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(size_t)c * ldd + r] = t[threadIdx.x][i];
+  }
 }
 
 __global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ pb, size_t n) {
@@ -656,7 +674,6 @@ __global__ void __launch_bounds__(128) k_rays_learned(const DevInst* __restrict_
 // ------------------------------------------------------------------ host
 
 using j3dg::DevInst;
-using j3dg::GemmArgs;
 
 struct j3dg_learned {
   j3dg_ctx* ctx = nullptr;
@@ -675,6 +692,12 @@ struct j3dg_learned {
   uint32_t B = 0;
   __nv_bfloat16 *X = nullptr, *H[4] = {nullptr, nullptr, nullptr, nullptr}, *Z[4] = {nullptr, nullptr, nullptr, nullptr};
   __nv_bfloat16 *dZ5 = nullptr, *dA = nullptr, *dB = nullptr;
+  // transposed copies the tcgen05 GEMMs read K-major: of the features, the
+  // hidden activations and the gradients (weight gradients reduce over the
+  // batch), and of the bf16 weights (the forward pass)
+  __nv_bfloat16 *Xt = nullptr, *Ht[4] = {nullptr, nullptr, nullptr, nullptr};
+  __nv_bfloat16 *dZ5t = nullptr, *dAt = nullptr, *dBt = nullptr;
+  __nv_bfloat16* d_pbt = nullptr;
   float* logits = nullptr;
   int32_t* labels = nullptr;
   float* d_loss = nullptr;
@@ -707,6 +730,11 @@ int alloc_workspace(j3dg_learned* l, uint32_t B) {
   cudaFree(l->dZ5);
   cudaFree(l->dA);
   cudaFree(l->dB);
+  cudaFree(l->Xt);
+  for (int k = 0; k < 4; ++k) cudaFree(l->Ht[k]);
+  cudaFree(l->dZ5t);
+  cudaFree(l->dAt);
+  cudaFree(l->dBt);
   cudaFree(l->logits);
   cudaFree(l->labels);
   cudaFree(l->rays);
@@ -721,6 +749,11 @@ int alloc_workspace(j3dg_learned* l, uint32_t B) {
   LCK(cudaMalloc(&l->dZ5, sizeof(__nv_bfloat16) * B * j3dg::kOut), "learned workspace");
   LCK(cudaMalloc(&l->dA, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
   LCK(cudaMalloc(&l->dB, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  LCK(cudaMalloc(&l->Xt, sizeof(__nv_bfloat16) * B * j3dg::kIn), "learned workspace");
+  for (int k = 0; k < 4; ++k) LCK(cudaMalloc(&l->Ht[k], sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  LCK(cudaMalloc(&l->dZ5t, sizeof(__nv_bfloat16) * B * j3dg::kOut), "learned workspace");
+  LCK(cudaMalloc(&l->dAt, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
+  LCK(cudaMalloc(&l->dBt, sizeof(__nv_bfloat16) * B * j3dg::kHid), "learned workspace");
   LCK(cudaMalloc(&l->logits, sizeof(float) * B * j3dg::kOut), "learned workspace");
   LCK(cudaMalloc(&l->labels, sizeof(int32_t) * B), "learned workspace");
   LCK(cudaMalloc(&l->rays, sizeof(j3dg_ray) * B), "learned workspace");
@@ -730,56 +763,117 @@ int alloc_workspace(j3dg_learned* l, uint32_t B) {
 }
 
 __nv_bfloat16* W(j3dg_learned* l, int k) { return l->d_pb + l->L.w[k]; }
+__nv_bfloat16* Wt(j3dg_learned* l, int k) { return l->d_pbt + l->L.w[k]; }
 const float* Bias(j3dg_learned* l, int k) { return l->d_p + l->L.b[k]; }
 
-// forward over X (B rows): H1..H4, logits
-int forward(j3dg_learned* l, uint32_t B) {
-  const __nv_bfloat16* in = l->X;
-  int in_dim = j3dg::kIn;
-  for (int k = 0; k < 4; ++k) {
-    GemmArgs g{in, W(l, k), l->H[k], l->Z[k], Bias(l, k), (int)B, j3dg::kHid, in_dim, in_dim, j3dg::kHid, j3dg::kHid};
-    LCK(j3dg::gemm_bf16(g, false, false, j3dg::EPI_BIAS_GELU, LS(l)), "learned forward");
-    in = l->H[k];
-    in_dim = j3dg::kHid;
-  }
-  GemmArgs g{l->H[3], W(l, 4), l->logits, nullptr, Bias(l, 4), (int)B, j3dg::kOut, j3dg::kHid, j3dg::kHid, j3dg::kOut,
-             j3dg::kOut};
-  LCK(j3dg::gemm_bf16(g, false, false, j3dg::EPI_BIAS_F32, LS(l)), "learned forward");
+int transpose(j3dg_learned* l, const __nv_bfloat16* src, int rows, int cols, __nv_bfloat16* dst, const char* where) {
+  j3dg::k_transpose_bf16<<<dim3((cols + 31) / 32, (rows + 31) / 32), dim3(32, 8), 0, LS(l)>>>(src, rows, cols, cols,
+                                                                                             dst, rows);
+  LCK(cudaGetLastError(), where);
   return J3DG_OK;
 }
 
-// softmax CE + backward into l->d_g (all gradients overwritten)
+// the transposed bf16 weights Wt_k [out][in] the forward GEMMs read (after
+// every change of d_pb)
+int refresh_wt(j3dg_learned* l) {
+  for (int k = 0; k < 5; ++k)
+    if (int rc = transpose(l, W(l, k), l->L.in[k], l->L.out[k], Wt(l, k), "learned weights")) return rc;
+  return J3DG_OK;
+}
+
+int gemm(j3dg_learned* l, const j3dg::UmmaArgs& g, const char* where) {
+  cudaError_t e = j3dg::umma_gemm_bf16(g, l->ctx->d_status, LS(l));
+  if (e == cudaErrorInvalidValue) return j3dg::ctx_fail(l->ctx, J3DG_ERR_INVALID_ARGUMENT, std::string(where) + ": bad GEMM shape");
+  LCK(e, where);
+  return J3DG_OK;
+}
+
+j3dg::UmmaArgs umma(const __nv_bfloat16* A, const __nv_bfloat16* Bt, void* C, int M, int N, int K, int epi) {
+  j3dg::UmmaArgs g{};
+  g.A = A;
+  g.Bt = Bt;
+  g.C = C;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.lda = K;
+  g.ldb = K;
+  g.ldc = N;
+  g.epi = epi;
+  g.splits = 1;
+  return g;
+}
+
+// forward over X (B rows) on the tcgen05 GEMMs: H1..H4 (and with train,
+// their transposes for the weight gradients), logits
+int forward(j3dg_learned* l, uint32_t B, bool train = false) {
+  const __nv_bfloat16* in = l->X;
+  int in_dim = j3dg::kIn;
+  for (int k = 0; k < 4; ++k) {
+    j3dg::UmmaArgs g = umma(in, Wt(l, k), l->H[k], (int)B, j3dg::kHid, in_dim, j3dg::EPI_BIAS_GELU);
+    g.bias = Bias(l, k);
+    g.Z = l->Z[k];
+    if (train) {
+      g.Ct = l->Ht[k];
+      g.ldct = (int)B;
+    }
+    if (int rc = gemm(l, g, "learned forward")) return rc;
+    in = l->H[k];
+    in_dim = j3dg::kHid;
+  }
+  j3dg::UmmaArgs g = umma(l->H[3], Wt(l, 4), l->logits, (int)B, j3dg::kOut, j3dg::kHid, j3dg::EPI_BIAS_F32);
+  g.bias = Bias(l, 4);
+  return gemm(l, g, "learned forward");
+}
+
+// split-K of a weight gradient over the batch: about one CTA per SM
+int splits_for(j3dg_learned* l, int M, int N, uint32_t B) {
+  const int tiles = (M / 128) * (N % 256 == 0 ? N / 256 : N / 128);
+  const int want = std::max(1, l->ctx->sm_count / std::max(1, tiles));
+  return std::max(1, std::min(want, (int)(B / 256)));
+}
+
+// softmax CE + backward into l->d_g (all gradients overwritten), on the
+// tcgen05 GEMMs; forward(l, B, true) ran before
 int backward(j3dg_learned* l, uint32_t B, float inv_valid) {
   j3dg::k_softmax_ce<<<(B + 7) / 8, 256, 0, LS(l)>>>(l->logits, l->labels, B, l->n_clusters, inv_valid, l->dZ5,
                                                        l->d_loss, l->d_correct);
   LCK(cudaGetLastError(), "learned softmax");
+  if (int rc = transpose(l, l->dZ5, (int)B, j3dg::kOut, l->dZ5t, "learned backward")) return rc;
   float* g = l->d_g;
   // layer 5: dW5 = H4^T dZ5, db5 = colsum(dZ5), dZ4 = (dZ5 W5^T) * gelu'(Z4)
   {
-    GemmArgs a{l->H[3], l->dZ5, g + l->L.w[4], nullptr, nullptr, j3dg::kHid, j3dg::kOut, (int)B, j3dg::kHid, j3dg::kOut,
-               j3dg::kOut};
-    LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
+    j3dg::UmmaArgs a = umma(l->Ht[3], l->dZ5t, g + l->L.w[4], j3dg::kHid, j3dg::kOut, (int)B, j3dg::EPI_F32_ACCUM);
+    a.splits = splits_for(l, j3dg::kHid, j3dg::kOut, B);
+    LCK(cudaMemsetAsync(g + l->L.w[4], 0, sizeof(float) * j3dg::kHid * j3dg::kOut, LS(l)), "learned backward");
+    if (int rc = gemm(l, a, "learned backward")) return rc;
     LCK(cudaMemsetAsync(g + l->L.b[4], 0, sizeof(float) * j3dg::kOut, LS(l)), "learned backward");
     j3dg::k_colsum<<<dim3((j3dg::kOut + 255) / 256, (B + 127) / 128), 256, 0, LS(l)>>>(l->dZ5, B, j3dg::kOut,
                                                                                         g + l->L.b[4]);
-    GemmArgs d{l->dZ5, W(l, 4), l->dA, l->Z[3], nullptr, (int)B, j3dg::kHid, j3dg::kOut, j3dg::kOut, j3dg::kOut,
-               j3dg::kHid};
-    LCK(j3dg::gemm_bf16(d, false, true, j3dg::EPI_GELU_BWD, LS(l)), "learned backward");
+    j3dg::UmmaArgs d = umma(l->dZ5, W(l, 4), l->dA, (int)B, j3dg::kHid, j3dg::kOut, j3dg::EPI_GELU_BWD);
+    d.Z = l->Z[3];
+    d.Ct = l->dAt;
+    d.ldct = (int)B;
+    if (int rc = gemm(l, d, "learned backward")) return rc;
   }
-  __nv_bfloat16* dcur = l->dA;
-  __nv_bfloat16* dnext = l->dB;
+  __nv_bfloat16 *dcur = l->dA, *dcur_t = l->dAt, *dnext = l->dB, *dnext_t = l->dBt;
   for (int k = 3; k >= 0; --k) {
-    const __nv_bfloat16* in = k ? l->H[k - 1] : l->X;
+    const __nv_bfloat16* in_t = k ? l->Ht[k - 1] : l->Xt;
     const int in_dim = k ? j3dg::kHid : j3dg::kIn;
-    GemmArgs a{in, dcur, g + l->L.w[k], nullptr, nullptr, in_dim, j3dg::kHid, (int)B, in_dim, j3dg::kHid, j3dg::kHid};
-    LCK(j3dg::gemm_bf16(a, true, false, j3dg::EPI_F32, LS(l)), "learned backward");
+    j3dg::UmmaArgs a = umma(in_t, dcur_t, g + l->L.w[k], in_dim, j3dg::kHid, (int)B, j3dg::EPI_F32_ACCUM);
+    a.splits = splits_for(l, in_dim, j3dg::kHid, B);
+    LCK(cudaMemsetAsync(g + l->L.w[k], 0, sizeof(float) * in_dim * j3dg::kHid, LS(l)), "learned backward");
+    if (int rc = gemm(l, a, "learned backward")) return rc;
     LCK(cudaMemsetAsync(g + l->L.b[k], 0, sizeof(float) * j3dg::kHid, LS(l)), "learned backward");
     j3dg::k_colsum<<<dim3(1, (B + 127) / 128), 128, 0, LS(l)>>>(dcur, B, j3dg::kHid, g + l->L.b[k]);
     if (k > 0) {
-      GemmArgs d{dcur, W(l, k), dnext, l->Z[k - 1], nullptr, (int)B, j3dg::kHid, j3dg::kHid, j3dg::kHid, j3dg::kHid,
-                 j3dg::kHid};
-      LCK(j3dg::gemm_bf16(d, false, true, j3dg::EPI_GELU_BWD, LS(l)), "learned backward");
+      j3dg::UmmaArgs d = umma(dcur, W(l, k), dnext, (int)B, j3dg::kHid, j3dg::kHid, j3dg::EPI_GELU_BWD);
+      d.Z = l->Z[k - 1];
+      d.Ct = dnext_t;
+      d.ldct = (int)B;
+      if (int rc = gemm(l, d, "learned backward")) return rc;
       std::swap(dcur, dnext);
+      std::swap(dcur_t, dnext_t);
     }
   }
   LCK(cudaGetLastError(), "learned backward");
@@ -906,6 +1000,7 @@ int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_o
   if (e == cudaSuccess) e = cudaMalloc(&l->d_m, sizeof(float) * P);
   if (e == cudaSuccess) e = cudaMalloc(&l->d_v, sizeof(float) * P);
   if (e == cudaSuccess) e = cudaMalloc(&l->d_pb, sizeof(__nv_bfloat16) * P);
+  if (e == cudaSuccess) e = cudaMalloc(&l->d_pbt, sizeof(__nv_bfloat16) * P);
   if (e == cudaSuccess) e = cudaMalloc(&l->d_loss, sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&l->d_correct, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemcpyAsync(l->d_p, hp.data(), sizeof(float) * P, cudaMemcpyHostToDevice, LS(l));
@@ -915,6 +1010,7 @@ int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_o
     j3dg::k_to_bf16<<<(unsigned)((P + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_pb, P);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess && refresh_wt(l) != J3DG_OK) e = cudaErrorUnknown;
   if (e == cudaSuccess) e = cudaStreamSynchronize(LS(l));
   if (e != cudaSuccess) {
     j3dg_learned_destroy(l);
@@ -936,12 +1032,14 @@ int j3dg_learned_destroy(j3dg_learned* l) {
   if (!l) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(l->ctx->device);
   cudaStreamSynchronize(LS(l));
-  void* ptrs[] = {l->d_roots, l->d_cluster_of_tri, l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb, l->X, l->dZ5, l->dA, l->dB,
-                  l->logits, l->labels, l->d_loss, l->d_correct, l->rays, l->hits, l->top2, l->d_wpack};
+  void* ptrs[] = {l->d_roots, l->d_cluster_of_tri, l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb, l->d_pbt, l->X, l->dZ5,
+                  l->dA, l->dB, l->Xt, l->dZ5t, l->dAt, l->dBt, l->logits, l->labels, l->d_loss, l->d_correct,
+                  l->rays, l->hits, l->top2, l->d_wpack};
   for (void* p : ptrs) cudaFree(p);
   for (int k = 0; k < 4; ++k) {
     cudaFree(l->H[k]);
     cudaFree(l->Z[k]);
+    cudaFree(l->Ht[k]);
   }
   delete l;
   return J3DG_OK;
@@ -968,6 +1066,7 @@ int j3dg_learned_set_params(j3dg_learned* l, const float* in) {
   const size_t P = l->L.total;
   LCK(cudaMemcpyAsync(l->d_p, in, sizeof(float) * P, cudaMemcpyHostToDevice, LS(l)), "set_params");
   j3dg::k_to_bf16<<<(unsigned)((P + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_pb, P);
+  if (int rc = refresh_wt(l)) return rc;
   LCK(cudaStreamSynchronize(LS(l)), "set_params");
   return J3DG_OK;
 }
@@ -987,7 +1086,8 @@ int j3dg_learned_loss_grad(j3dg_learned* l, const float* feats, const int32_t* l
   LCK(cudaMemcpyAsync(l->labels, labels, sizeof(int32_t) * B, cudaMemcpyHostToDevice, LS(l)), "loss_grad");
   LCK(cudaMemsetAsync(l->d_loss, 0, sizeof(float), LS(l)), "loss_grad");
   LCK(cudaMemsetAsync(l->d_correct, 0, sizeof(uint32_t), LS(l)), "loss_grad");
-  if (int rc = forward(l, B)) return rc;
+  if (int rc = transpose(l, l->X, (int)B, j3dg::kIn, l->Xt, "loss_grad")) return rc;
+  if (int rc = forward(l, B, true)) return rc;
   if (int rc = backward(l, B, valid ? 1.f / (float)valid : 0.f)) return rc;
   float ls = 0.f;
   LCK(cudaMemcpyAsync(&ls, l->d_loss, sizeof(float), cudaMemcpyDeviceToHost, LS(l)), "loss_grad");
@@ -1018,7 +1118,8 @@ int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, flo
     if (int rc = features(l, l->rays, B, B)) return rc;
     LCK(cudaMemsetAsync(l->d_loss, 0, sizeof(float), LS(l)), "train");
     LCK(cudaMemsetAsync(l->d_correct, 0, sizeof(uint32_t), LS(l)), "train");
-    if (int rc = forward(l, B)) return rc;
+    if (int rc = transpose(l, l->X, (int)B, j3dg::kIn, l->Xt, "train")) return rc;
+    if (int rc = forward(l, B, true)) return rc;
     // hit fraction of the training rays is ~ constant; scale by the batch
     if (int rc = backward(l, B, 1.f / (float)B)) return rc;
     ++l->adam_t;
@@ -1026,6 +1127,7 @@ int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, flo
     j3dg::k_adam<<<(unsigned)((l->L.total + 255) / 256), 256, 0, LS(l)>>>(l->d_p, l->d_g, l->d_m, l->d_v, l->d_pb,
                                                                          l->L.total, l->opts.lr, b1, b2, 1e-8f, c1, c2);
     LCK(cudaGetLastError(), "adam");
+    if (int rc = refresh_wt(l)) return rc;
     if (s + 1 == steps || (s % 64) == 63) {
       float ls = 0.f;
       uint32_t corr = 0;
@@ -1080,7 +1182,7 @@ static int predict_fused(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, ui
 }
 
 // top-2 clusters per ray on device arrays: impl 1 fused tcgen05 kernel,
-// impl 0 layer-by-layer mma.sync GEMMs + a top-2 pass over the logits
+// impl 0 the layer-by-layer tcgen05 GEMMs + a top-2 pass over the logits
 static int predict_device(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2, int impl = 1) {
   if (impl == 1) return predict_fused(l, d_rays, n, d_top2);
   const uint32_t B = l->opts.batch;

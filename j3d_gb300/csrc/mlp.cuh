@@ -1,14 +1,6 @@
-// mlp.cuh -- bf16 tensor-core GEMM with fused epilogues for the ray ->
-// cluster network of the learned-tmax traversal.
-//
-//   C[m][n] = sum_k A(m, k) B(k, n), fp32 accumulation
-//   A(m, k) = AT ? A[k * lda + m] : A[m * lda + k]
-//   B(k, n) = BT ? B[n * ldb + k] : B[k * ldb + n]
-//
-// Tiles of 128 x 128 x 32 per block (8 warps, each 64 x 32), operands staged
-// k-contiguous in shared memory (double-buffered), fragments by ldmatrix,
-// products by mma.sync m16n8k16 bf16 -> f32. M, N, K must be multiples of
-// 128, 128, 32 (the callers pad).
+// mlp.cuh -- bf16 tensor-core GEMM (tcgen05, accumulator in tensor memory)
+// with fused epilogues for the ray -> cluster network of the learned-tmax
+// traversal (umma_gemm.cu), and the network's activation.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -18,31 +10,27 @@ namespace j3dg {
 
 enum Epilogue : int {
   EPI_F32 = 0,            // C (float) = acc
-  EPI_F32_ACCUM = 1,      // C (float) += acc
+  EPI_F32_ACCUM = 1,      // C (float) += acc (split-K over `splits` K ranges, atomics; C zeroed first)
   EPI_BIAS_GELU = 2,      // Z (bf16) = acc + bias; C (bf16) = gelu(Z)
   EPI_BIAS_F32 = 3,       // C (float) = acc + bias
   EPI_GELU_BWD = 4,       // C (bf16) = acc * gelu'(Z), Z given (bf16)
 };
 
-struct GemmArgs {
-  const __nv_bfloat16* A;
-  const __nv_bfloat16* B;
-  void* C;
-  __nv_bfloat16* Z;      // pre-activation out (EPI_BIAS_GELU) or in (EPI_GELU_BWD)
-  const float* bias;
-  int M, N, K, lda, ldb, ldc;
-};
-
-cudaError_t gemm_bf16(const GemmArgs& g, bool at, bool bt, int epi, cudaStream_t st);
-
-// C[M x N] fp32 = A[M x K] . Bt[N x K]^T on the tcgen05 tensor cores
-// (umma_gemm.cu). M % 128, N % 128, K % 64 == 0; lda, ldb multiples of 8;
-// 16-byte aligned pointers. A timed-out wait raises J3DG_DEV_VISIT_CAP.
+// C[M x N] = epilogue(A[M x K] . Bt[N x K]^T). M % 128, N % 128, K % 64 ==
+// 0; lda, ldb multiples of 8; 16-byte aligned pointers. Z has C's shape
+// and ldc. Ct (optional, bf16 epilogues): C also written transposed,
+// Ct[n * ldct + m]. A timed-out wait raises J3DG_DEV_VISIT_CAP.
 struct UmmaArgs {
   const __nv_bfloat16* A;
   const __nv_bfloat16* Bt;
-  float* C;
+  void* C;
   int M, N, K, lda, ldb, ldc;
+  int epi;
+  const float* bias;
+  __nv_bfloat16* Z;
+  __nv_bfloat16* Ct;
+  int ldct;
+  int splits;
 };
 // withhold != 0 issues no MMA and no commit, so the kernel's bounded wait runs
 // out (the failure path, exercised by a test)

@@ -1,6 +1,7 @@
 // umma_gemm.cu -- bf16 GEMM on the tcgen05 tensor cores with the
-// accumulator in tensor memory:
-//   C[M x N] (fp32) = A[M x K] . Bt[N x K]^T     (A and Bt row-major, K-major)
+// accumulator in tensor memory, and the fused epilogues the network's
+// training and layer-by-layer inference need:
+//   C[M x N] = epilogue(A[M x K] . Bt[N x K]^T)   (A and Bt row-major, K-major)
 // One CTA of 4 warps per 128 x BN tile. K advances in chunks of 64 through a
 // two-stage shared-memory ring: all threads copy the next chunk into the
 // canonical no-swizzle layout while the tensor core works on the previous
@@ -14,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../../include/j3dg.h"
@@ -51,11 +53,71 @@ __device__ __forceinline__ void copy_chunk(const __nv_bfloat16* __restrict__ src
   }
 }
 
-template <int BN>
-__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __restrict__ A,
-                                                      const __nv_bfloat16* __restrict__ Bt, float* __restrict__ C,
-                                                      int K, int lda, int ldb, int ldc, uint32_t* status,
-                                                      int withhold) {
+// The epilogue of thread `lane` of warp w: accumulator row m0 + 32 w + lane,
+// BN columns from n0, 16 per TMEM load.
+//   EPI_F32         C (float) = acc
+//   EPI_F32_ACCUM   C (float) += acc, with atomics (split-K: blockIdx.z
+//                   takes one K range; C starts at zero)
+//   EPI_BIAS_F32    C (float) = acc + bias
+//   EPI_BIAS_GELU   Z (bf16) = acc + bias; C (bf16) = gelu(Z)
+//   EPI_GELU_BWD    C (bf16) = acc * gelu'(Z), Z given
+// With Ct, the bf16 C is also written transposed (Ct[n][m], row stride
+// ldct): the next GEMMs read it K-major. Rounding is per element, bias ->
+// bf16 -> GELU -> bf16, as the inference kernel rounds.
+template <int BN, int EPI>
+__device__ __forceinline__ void epilogue(const UmmaArgs& g, uint32_t taddr, int m0, int n0, int warp, int lane) {
+  const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+  for (int j = 0; j < BN / 16; ++j) {
+    float v[16];
+    umma::ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * 16), v);
+    const int col = n0 + j * 16;
+    if (EPI == EPI_F32 || EPI == EPI_F32_ACCUM || EPI == EPI_BIAS_F32) {
+      float* c = static_cast<float*>(g.C) + (size_t)row * g.ldc + col;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float4 o = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        if (EPI == EPI_BIAS_F32) {
+          const float4 b = __ldg(reinterpret_cast<const float4*>(g.bias + col) + q);
+          o = make_float4(o.x + b.x, o.y + b.y, o.z + b.z, o.w + b.w);
+        }
+        if (EPI == EPI_F32_ACCUM)
+          atomicAdd(reinterpret_cast<float4*>(c) + q, o);
+        else
+          reinterpret_cast<float4*>(c)[q] = o;
+      }
+    } else {
+      __nv_bfloat16 out[16];
+      __nv_bfloat16* z = g.Z + (size_t)row * g.ldc + col;
+      if (EPI == EPI_BIAS_GELU) {
+        __nv_bfloat16 zz[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          zz[i] = __float2bfloat16_rn(v[i] + __ldg(g.bias + col + i));
+          out[i] = __float2bfloat16_rn(gelu_f(__bfloat162float(zz[i])));
+        }
+        reinterpret_cast<uint4*>(z)[0] = reinterpret_cast<const uint4*>(zz)[0];
+        reinterpret_cast<uint4*>(z)[1] = reinterpret_cast<const uint4*>(zz)[1];
+      } else {  // EPI_GELU_BWD
+        __nv_bfloat16 zz[16];
+        reinterpret_cast<uint4*>(zz)[0] = reinterpret_cast<const uint4*>(z)[0];
+        reinterpret_cast<uint4*>(zz)[1] = reinterpret_cast<const uint4*>(z)[1];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) out[i] = __float2bfloat16_rn(v[i] * gelu_grad_f(__bfloat162float(zz[i])));
+      }
+      __nv_bfloat16* c = static_cast<__nv_bfloat16*>(g.C) + (size_t)row * g.ldc + col;
+      reinterpret_cast<uint4*>(c)[0] = reinterpret_cast<const uint4*>(out)[0];
+      reinterpret_cast<uint4*>(c)[1] = reinterpret_cast<const uint4*>(out)[1];
+      if (g.Ct) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) g.Ct[(size_t)(col + i) * g.ldct + row] = out[i];
+      }
+    }
+  }
+}
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(128, 1) k_umma_gemm(const UmmaArgs g, uint32_t* status, int withhold) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t taddr_s;
@@ -80,19 +142,23 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
   const uint32_t taddr = taddr_s;
   constexpr uint32_t idesc = umma::idesc_bf16_f32(128, BN);
 
-  const int nk = K / kChunkK;
+  // this CTA's K range (split-K over blockIdx.z)
+  const int nk_all = g.K / kChunkK;
+  const int kc0 = (int)((long long)nk_all * blockIdx.z / gridDim.z);
+  const int kc1 = (int)((long long)nk_all * (blockIdx.z + 1) / gridDim.z);
+  const int nk = kc1 - kc0;
   bool ok = true;
-  for (int kc = 0; kc < nk; ++kc) {
-    const int s = kc & 1;
+  for (int it = 0; it < nk; ++it) {
+    const int s = it & 1;
     uint8_t* sA = sm + s * L::stage_bytes;
     uint8_t* sB = sA + L::a_bytes;
-    if (kc >= 2) ok = umma::mbar_wait(umma::smem_u32(&mbar[s]), ((kc - 2) >> 1) & 1, kWaitBudget);
+    if (it >= 2) ok = umma::mbar_wait(umma::smem_u32(&mbar[s]), ((it - 2) >> 1) & 1, kWaitBudget);
     if (!__syncthreads_and(ok)) {
       ok = false;
       break;
     }
-    copy_chunk(A, lda, m0, 128, kc * kChunkK, sA);
-    copy_chunk(Bt, ldb, n0, BN, kc * kChunkK, sB);
+    copy_chunk(g.A, g.lda, m0, 128, (kc0 + it) * kChunkK, sA);
+    copy_chunk(g.Bt, g.ldb, n0, BN, (kc0 + it) * kChunkK, sB);
     umma::fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0 && !withhold) {  // withhold: nothing completes the barrier (failure-path test)
@@ -101,25 +167,16 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
 #pragma unroll
       for (int k = 0; k < kChunkK / 16; ++k)
         umma::mma_bf16(taddr, umma::desc(a0 + k * 256, 128, (kChunkK / 8) * 128),
-                       umma::desc(b0 + k * 256, 128, (kChunkK / 8) * 128), idesc, (kc | k) != 0);
+                       umma::desc(b0 + k * 256, 128, (kChunkK / 8) * 128), idesc, (it | k) != 0);
       umma::commit(umma::smem_u32(&mbar[s]));
     }
   }
   if (ok && nk > 0) ok = umma::mbar_wait(umma::smem_u32(&mbar[(nk - 1) & 1]), ((nk - 1) >> 1) & 1, kWaitBudget);
   ok = __syncthreads_and(ok);
   umma::fence_after_sync();
-  if (ok) {
-    const int row = m0 + warp * 32 + lane;
-    float* c = C + (size_t)row * ldc + n0;
-#pragma unroll 1
-    for (int j = 0; j < BN / 16; ++j) {
-      float v[16];
-      umma::ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * 16), v);
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        reinterpret_cast<float4*>(c + j * 16)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-    }
-  } else if (threadIdx.x == 0) {
+  if (ok && nk > 0) {
+    epilogue<BN, EPI>(g, taddr, m0, n0, warp, lane);
+  } else if (!ok && threadIdx.x == 0) {
     atomicOr(status, J3DG_DEV_VISIT_CAP);
   }
   umma::fence_before_sync();
@@ -130,24 +187,40 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __nv_bfloat16* __res
   }
 }
 
-template <int BN>
+template <int BN, int EPI>
 cudaError_t launch(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold) {
   const uint32_t smem = GemmSmem<BN>::total;
-  cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_umma_gemm<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid(g.N / BN, g.M / 128);
-  k_umma_gemm<BN><<<grid, 128, smem, st>>>(g.A, g.Bt, g.C, g.K, g.lda, g.ldb, g.ldc, status, withhold);
+  dim3 grid(g.N / BN, g.M / 128, EPI == EPI_F32_ACCUM ? g.splits : 1);
+  k_umma_gemm<BN, EPI><<<grid, 128, smem, st>>>(g, status, withhold);
   return cudaGetLastError();
+}
+
+template <int BN>
+cudaError_t launch_epi(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold) {
+  switch (g.epi) {
+    case EPI_F32: return launch<BN, EPI_F32>(g, status, st, withhold);
+    case EPI_F32_ACCUM: return launch<BN, EPI_F32_ACCUM>(g, status, st, withhold);
+    case EPI_BIAS_F32: return launch<BN, EPI_BIAS_F32>(g, status, st, withhold);
+    case EPI_BIAS_GELU: return launch<BN, EPI_BIAS_GELU>(g, status, st, withhold);
+    case EPI_GELU_BWD: return launch<BN, EPI_GELU_BWD>(g, status, st, withhold);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace
 
 cudaError_t umma_gemm_bf16(const UmmaArgs& g, uint32_t* status, cudaStream_t st, int withhold) {
-  if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.M % 128 || g.K % kChunkK || g.lda % 8 || g.ldb % 8 || g.ldc % 4 ||
-      ((uintptr_t)g.A & 15) || ((uintptr_t)g.Bt & 15) || ((uintptr_t)g.C & 15))
+  const bool bf16_out = g.epi == EPI_BIAS_GELU || g.epi == EPI_GELU_BWD;
+  if (g.M <= 0 || g.N <= 0 || g.K <= 0 || g.M % 128 || g.K % kChunkK || g.lda % 8 || g.ldb % 8 ||
+      g.ldc % (bf16_out ? 16 : 4) || ((uintptr_t)g.A & 15) || ((uintptr_t)g.Bt & 15) || ((uintptr_t)g.C & 15) ||
+      (bf16_out && (!g.Z || ((uintptr_t)g.Z & 15))) || ((g.epi == EPI_BIAS_F32 || g.epi == EPI_BIAS_GELU) && !g.bias) ||
+      (g.epi == EPI_BIAS_F32 && ((uintptr_t)g.bias & 15)) || (g.Ct && (!bf16_out || g.ldct < g.M)) ||
+      (g.epi == EPI_F32_ACCUM && (g.splits < 1 || g.splits > g.K / kChunkK)))
     return cudaErrorInvalidValue;
-  if (g.N % 256 == 0) return launch<256>(g, status, st, withhold);
-  if (g.N % 128 == 0) return launch<128>(g, status, st, withhold);
+  if (g.N % 256 == 0) return launch_epi<256>(g, status, st, withhold);
+  if (g.N % 128 == 0) return launch_epi<128>(g, status, st, withhold);
   return cudaErrorInvalidValue;
 }
 
@@ -163,13 +236,25 @@ extern "C" int j3dg_gemm_bf16(j3dg_ctx* c, const void* A, const void* Bt, float*
   cudaSetDevice(c->device);
   cudaStream_t st = (cudaStream_t)c->stream;
   cudaError_t e;
-  if (impl == 0) {
-    j3dg::GemmArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, nullptr, nullptr, (int)M, (int)N, (int)K,
-                     (int)K, (int)K, (int)N};
-    e = j3dg::gemm_bf16(g, false, true, j3dg::EPI_F32, st);
-  } else if (impl == 1 || impl == 2) {
-    j3dg::UmmaArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)Bt, C, (int)M, (int)N, (int)K, (int)K, (int)K, (int)N};
-    e = j3dg::umma_gemm_bf16(g, c->d_status, st, impl == 2);
+  if (impl >= 0 && impl <= 2) {
+    j3dg::UmmaArgs g{};
+    g.A = (const __nv_bfloat16*)A;
+    g.Bt = (const __nv_bfloat16*)Bt;
+    g.C = C;
+    g.M = (int)M;
+    g.N = (int)N;
+    g.K = (int)K;
+    g.lda = g.ldb = (int)K;
+    g.ldc = (int)N;
+    g.epi = j3dg::EPI_F32;
+    if (impl == 0) {  // split-K into a zeroed C
+      g.epi = j3dg::EPI_F32_ACCUM;
+      g.splits = std::max(1, std::min(4, (int)K / 64));
+      e = cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, st);
+      if (e == cudaSuccess) e = j3dg::umma_gemm_bf16(g, c->d_status, st, 0);
+    } else {
+      e = j3dg::umma_gemm_bf16(g, c->d_status, st, impl == 2);
+    }
   } else {
     return j3dg::ctx_fail(c, J3DG_ERR_INVALID_ARGUMENT, "gemm_bf16: impl must be 0, 1 or 2");
   }

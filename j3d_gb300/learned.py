@@ -63,7 +63,7 @@ class Learned:
 
     def predict(self, rays, impl: int = 1) -> np.ndarray:
         """Top-2 clusters per ray: impl 1 the fused tcgen05 kernel, 0 the
-        layer-by-layer mma.sync GEMMs."""
+        layer-by-layer tcgen05 GEMMs of training."""
         out = np.zeros((len(rays), 2), np.uint32)
         _check(self.ctx.h, lib().j3dg_learned_predict_impl(self.h, vptr(rays), len(rays), vptr(out), impl))
         return out

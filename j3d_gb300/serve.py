@@ -12,6 +12,11 @@ batch a request lands in does not change its bytes (tests check alone == in
 the mix).
 
 Latency = completion (a CUDA event after the request's batch) - arrival.
+
+With learned networks attached (attach_learned), frames of those meshes find
+their primary hits through the learned path (j3dg_learned_render_frame:
+network, then the exact traversal it seeds); the admitted group is queued
+frame by frame, and the images are the plain path's (tests check it).
 """
 from __future__ import annotations
 
@@ -122,6 +127,7 @@ class RenderServer:
         self.peak_bytes = 0
         self.keep_images = keep_images
         self.images: dict[int, np.ndarray] = {}
+        self.learned: dict[str, object] = {}
 
     # ------------------------------------------------------------- meshes
     def add_mesh(self, name: str, V, T, leaf_size: int = 2) -> bool:
@@ -138,6 +144,13 @@ class RenderServer:
         self.meshes[name] = m
         self.mesh_bytes += real
         return True
+
+    def attach_learned(self, name: str, net) -> None:
+        """Frames of mesh `name` go through the learned network `net`
+        (a j3d_gb300.learned.Learned over that mesh)."""
+        if net.mesh is not self.meshes[name]:
+            raise ValueError("the network belongs to another mesh")
+        self.learned[name] = net
 
     def footprint(self) -> int:
         return self.mesh_bytes + self.pool.bytes
@@ -173,8 +186,12 @@ class RenderServer:
         for r in reqs:
             cv = self.pool.take(tuple(r.resolution), self.settings)
             r.slot = cv
-            frames.append((cv, self._scene(r), self.matcap))
-        render_batch(self.ctx, frames)
+            if r.mesh in self.learned:
+                self.learned[r.mesh].render_frame(cv, self._scene(r), self.matcap)
+            else:
+                frames.append((cv, self._scene(r), self.matcap))
+        if frames:
+            render_batch(self.ctx, frames)
         ev = torch.cuda.Event()
         ev.record(self.stream)
         self.in_flight.append((ev, reqs))

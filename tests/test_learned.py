@@ -144,7 +144,7 @@ def test_training_learns_and_learned_hits_are_exact(gpu_ctx, tmp_path):
 @pytest.mark.gpu
 def test_fused_inference_matches_layered(gpu_ctx):
     """The fused tcgen05 kernel (features, five layers, running top-2, all on
-    chip) against the layer-by-layer mma.sync GEMMs + top-2 pass, on random
+    chip) against the layer-by-layer tcgen05 GEMMs + top-2 pass, on random
     weights and rays (a ray count that leaves a partial 128-ray tile)."""
     from j3d_gb300 import Mesh, workloads as W
     from j3d_gb300.learned import Learned
@@ -161,3 +161,62 @@ def test_fused_inference_matches_layered(gpu_ctx):
     t1, t0 = net.predict(rays, impl=1), net.predict(rays, impl=0)
     assert (t1 < net.n_clusters).all() and (t1[:, 0] != t1[:, 1]).all()
     assert (t1[:, 0] == t0[:, 0]).mean() > 0.99, (t1[:, 0] == t0[:, 0]).mean()
+
+
+@pytest.mark.gpu
+def test_learned_frames_equal_plain_frames(gpu_ctx, oracle_mod):
+    """Whole canvas frames whose primary hits come from the learned path
+    (network + seeded exact traversal, then the plain hit records, shadow
+    rays and shading) equal the plain frames byte for byte and the oracle's
+    frames, in the plain and the edges mode; a scene that is not the
+    network's mesh alone, at the identity, is refused."""
+    from helpers import compare_gbuffers, gpu_scene, oracle_scene
+
+    from j3d_gb300 import Canvas, J3dgError, Matcap, Scene, camera_for_vfov, settings, workloads as W
+    from j3d_gb300.learned import Learned
+    O = oracle_mod
+    V, T = W.torus(300, 150, seed=W.SEED_BASE + 77)
+    poses = W.cameras(3, W.SEED_BASE + 78, 2.2, 3.5)
+    mesh, sc = gpu_scene(gpu_ctx, V, T, poses[0])
+    net = Learned(gpu_ctx, mesh, cluster_depth=4, batch=8192, seed=9)
+    net.train(8192 * 40)
+    mc = Matcap.make(gpu_ctx, 0)
+    w, h = 320, 200
+    m, views, _ = oracle_scene(O, V, T, poses, w, h)
+    mco, cav = O.make_matcap(0)
+    for kw in (dict(shadow=True, edges=False), dict(shadow=True, edges=True)):
+        for i, pose in enumerate(poses):
+            sc.set_pose(pose)
+            frames = []
+            for learned in (False, True):
+                cv = Canvas(gpu_ctx, w, h)
+                cv.set_camera(camera_for_vfov(60.0))
+                cv.set_background_color()
+                cv.update_settings(settings(**kw))
+                if learned:
+                    net.render_frame(cv, sc, mc)
+                else:
+                    cv.render_frame(sc, mc)
+                frames.append((cv.get_pixels(), cv.get_image()))
+                cv.close()
+            (gp, gi), (lp, li) = frames
+            assert np.array_equal(lp.view(np.uint8), gp.view(np.uint8)), f"pose {i} {kw}: G-buffer"
+            assert np.array_equal(li, gi), f"pose {i} {kw}: image"
+            op = O.fresh_pixels(w, h)
+            oi = np.zeros((h, w), np.uint32)
+            O.render_frame(op, oi, O.fill_background(w, h), [(m, np.eye(4, dtype=np.float32).reshape(16), 1)],
+                           views[i], O.settings(**kw), mco, cav)
+            assert compare_gbuffers(lp, op, f"learned pose {i}") == 0
+            assert (lp["object_id"] != 0xFFFFFFFF).mean() > 0.1
+    two = Scene()
+    two.add_object(mesh)
+    two.add_object(mesh, W.translation(2.0, 0.0, 0.0), 2)
+    two.prepare_scene()
+    two.unzoom()
+    cv = Canvas(gpu_ctx, 64, 48)
+    with pytest.raises(J3dgError):
+        net.render_frame(cv, two, mc)
+    moved = Scene()
+    moved.add_object(mesh, W.translation(0.5, 0.0, 0.0), 1)
+    with pytest.raises(J3dgError):
+        net.render_frame(cv, moved, mc)

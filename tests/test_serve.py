@@ -60,3 +60,22 @@ def test_admission_binds_under_a_low_cap(gpu_ctx):
     # a mesh larger than the cap is refused, nothing is allocated for it
     from j3d_gb300 import workloads as W
     assert not srv.add_mesh("big", *W.torus(400, 200))
+
+
+@pytest.mark.gpu
+def test_learned_requests_equal_plain_frames(gpu_ctx):
+    """With a learned network attached to a mesh, its requests render through
+    the learned path; every image equals the plain frame alone, and requests
+    of the other meshes still go through the batched plain path."""
+    from j3d_gb300.learned import Learned
+    srv = _server(gpu_ctx, 8 << 30, max_slots=8)
+    net = Learned(gpu_ctx, srv.meshes["m1"], cluster_depth=3, batch=4096, seed=3)
+    net.train(4096 * 20)
+    srv.attach_learned("m1", net)
+    reqs = poisson_requests(30, 3000.0, ["m0", "m1", "m2"], seed=12, resolutions=((64, 64), (128, 72)))
+    st = srv.run(reqs, realtime=True)
+    assert st.requests == 30 and any(r.mesh == "m1" for r in reqs)
+    for r in reqs:
+        assert np.array_equal(srv.images[r.rid], _alone(gpu_ctx, srv, r)), f"request {r.rid} ({r.mesh})"
+    with pytest.raises(ValueError):
+        srv.attach_learned("m0", net)

@@ -1,5 +1,6 @@
 """The network's bf16 tensor-core GEMMs against an fp32 reference:
-impl 0 = mma.sync, impl 1 = tcgen05 with the accumulator in tensor memory.
+impl 1 = tcgen05 with the accumulator in tensor memory, impl 0 = the same
+split over K ranges whose CTAs add into C (the weight gradients' form).
 C = A . Bt^T with A [M x K], Bt [N x K] bf16; the reference multiplies the
 same bf16 values in float64, and the tolerance is 1e-5 of the sum of |a b|
 (fp32 accumulation in another order)."""

@@ -34,16 +34,16 @@ NODE_BYTES = 128      # one BVH4 node: 4 child AABBs (96 B) + 4 refs, padded
 TRI_BYTES = 48        # 12 B index triple + 36 B of vertices per tested triangle
 RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # DRAM and L2 bytes of one k_frame launch on this workload (leaf size 2),
-# mean over the 32 launches of one step, from an ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum and lts__t_bytes.sum
-# (`ncu --metrics ... -k regex:k_frame -s 96 -c 32 python bench.py --steps 1
-# --warmup 3 --no-cpu [--build lbvh]`), per BVH builder:
-#   ploc: reads 427.8 MB, writes 70.0 MB, L2 2583.1 MB (SAH top levels +
-#         PLOC below 64 triangles, cost-optimal collapse, depth-first node
-#         order, parked finishes, 6 blocks per SM, next-node prefetch)
-#   lbvh: reads 463.2 MB, writes 70.7 MB, L2 1837.1 MB (level-order nodes,
-#         finishes in the tracing loop, 5 blocks per SM)
-FRAME_TRAFFIC = {"ploc": (427_842_504 + 69_961_168, 2_583_094_821),
+# mean of two launches (cameras 8 and 9) from an ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum and lts__t_sectors.sum x 32 B
+# (`ncu --set full -k regex:k_frame -s 40 -c 2 python bench.py --steps 2
+# --warmup 1 --no-cpu --no-side`), per BVH builder:
+#   ploc: DRAM 483.7 MB, L2 2401.3 MB (SAH top levels + PLOC below 64
+#         triangles, cost-optimal collapse, depth-first node order, parked
+#         finishes, 6 blocks per SM, next-node prefetch)
+#   lbvh: DRAM 533.9 MB, L2 1837.1 MB (level-order nodes, finishes in the
+#         tracing loop, 5 blocks per SM; an older capture)
+FRAME_TRAFFIC = {"ploc": (483_742_752, 2_401_349_440),
                  "lbvh": (463_159_392 + 70_692_880, 1_837_113_990)}
 
 
@@ -206,6 +206,127 @@ CONFIG = {"workload": "torus R=1 r=0.35 5300x2650 grid, 28,090,000 tris / 14,045
           "resolution": [W_, H_], "l2": "inputs larger than L2 (BVH + leaf triangles ~1.9 GB)"}
 
 
+def side_workloads(ctx, mesh, wl, args) -> dict:
+    """Short runs of the other configurations in the same process, so that one
+    bench run measures them beside the headline (each guarded: a failure is
+    reported in its entry and does not stop the headline line)."""
+    import torch
+
+    from j3d_gb300 import (Batch, Canvas, Matcap, Mesh, Scene, camera_for_vfov, settings, workloads as Wk)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {}
+
+    def ev_ms(fn, reps):
+        fn()
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # batched frames: 64 meshes (10k-2M tris) x 16 cameras, mixed resolutions,
+    # all 1024 frames in one graph-captured persistent launch
+    try:
+        t0 = time.perf_counter()
+        b = Wk.config2()
+        meshes = [Mesh(ctx, V, T) for V, T in b.meshes]
+        ctx.synchronize()
+        build_s = time.perf_counter() - t0
+        mc = Matcap.make(ctx, 0)
+        frames, k = [], 0
+        for i, m in enumerate(meshes):
+            for c in range(16):
+                sc = Scene()
+                sc.add_object(m, db_id=i + 1)
+                sc.prepare_scene()
+                sc.unzoom()
+                sc.set_pose(b.poses[i][c])
+                cv = Canvas(ctx, *b.resolutions[k])
+                cv.set_camera(camera_for_vfov(60.0))
+                cv.set_background_color()
+                cv.update_settings(settings(shadow=True, edges=False))
+                frames.append((cv, sc, mc))
+                k += 1
+        g = Batch(ctx, frames)
+        ms = ev_ms(g.launch, 3)
+        prim = sum(cv.width * cv.height for cv, _, _ in frames)
+        rays = prim + sum(cv.count_hits()[0] for cv, _, _ in frames)
+        out["batch_config2"] = {"frames": len(frames), "ms_per_launch": round(ms, 3),
+                                "mrays_s": round(rays / ms / 1e3, 1), "rays": rays,
+                                "triangles": int(sum(len(T) for _, T in b.meshes)),
+                                "setup_s_incl_64_builds": round(build_s, 2)}
+        g.close()
+        for cv, _, _ in frames:
+            cv.close()
+        for m in meshes:
+            m.close()
+    except Exception as e:  # noqa: BLE001
+        out["batch_config2"] = {"error": repr(e)[:300]}
+
+    # serving: 8 resident tori 200k..28.09M tris (the headline mesh is the
+    # 28M one), Poisson arrivals at 400/s, plain path
+    try:
+        from j3d_gb300.serve import RenderServer, poisson_requests
+        srv = RenderServer(ctx, 150 << 30, max_slots=64, max_in_flight=2)
+        for i, t in enumerate([200_000, 500_000, 1_000_000, 2_000_000, 5_000_000, 10_000_000, 20_000_000]):
+            assert srv.add_mesh(f"torus{t}", *Wk.torus(*Wk.torus_grid_for(t), seed=Wk.SEED_BASE + 4 + i))
+        srv.meshes["torus28090000"] = mesh  # resident already
+        srv.mesh_bytes += int(mesh.info().device_bytes)
+        names = list(srv.meshes)
+        srv.run(poisson_requests(64, 1600.0, names, seed=Wk.SEED_BASE + 40), realtime=True)
+        st = srv.run(poisson_requests(600, 400.0, names, seed=Wk.SEED_BASE + 41), realtime=True)
+        out["serve_config4_plain"] = {"requests": st.requests, "rate_per_s": 400, "p50_ms": round(st.p50_ms, 3),
+                                      "p99_ms": round(st.p99_ms, 3), "frames_per_s": round(st.frames_per_s, 1),
+                                      "mean_batch": round(st.mean_batch, 2),
+                                      "peak_hbm_gb": round(st.peak_bytes / 2**30, 2)}
+        for c in list(srv.pool.free.values()):
+            for cv in c:
+                cv.close()
+        for name, m in srv.meshes.items():
+            if m is not mesh:
+                m.close()
+    except Exception as e:  # noqa: BLE001
+        out["serve_config4_plain"] = {"error": repr(e)[:300]}
+
+    # learned tmax on the headline mesh: a 4096-cluster network trained on
+    # 16M rays, then one 1080p frame with learned vs plain primary hits
+    try:
+        from j3d_gb300.learned import Learned
+        net = Learned(ctx, mesh, cluster_depth=6, batch=16384, seed=Wk.SEED_BASE + 3)
+        loss, acc, train_s = net.train(16_000_000, 2.0, 5.0)
+        sc = Scene()
+        sc.add_object(mesh)
+        sc.prepare_scene()
+        sc.unzoom()
+        sc.set_pose(wl.poses[0])
+        mc = Matcap.make(ctx, 0)
+        cvs = []
+        for _ in range(2):
+            cv = Canvas(ctx, W_, H_)
+            cv.set_camera(camera_for_vfov(60.0))
+            cv.set_background_color()
+            cv.update_settings(settings(shadow=True, edges=False))
+            cvs.append(cv)
+        ms_plain = ev_ms(lambda: cvs[0].render_frame(sc, mc), 5)
+        ms_learned = ev_ms(lambda: net.render_frame(cvs[1], sc, mc), 3)
+        same = bool(np.array_equal(cvs[0].get_pixels().view(np.uint8), cvs[1].get_pixels().view(np.uint8)))
+        out["learned_config3"] = {"train_rays": 16_000_000, "train_s": round(train_s, 2),
+                                  "train_loss": round(loss, 4), "train_top1": round(acc, 4),
+                                  "frame_ms_plain": round(ms_plain, 3), "frame_ms_learned": round(ms_learned, 3),
+                                  "learned_over_plain": round(ms_plain / ms_learned, 4),
+                                  "frames_identical": same}
+        for cv in cvs:
+            cv.close()
+        net.close()
+    except Exception as e:  # noqa: BLE001
+        out["learned_config3"] = {"error": repr(e)[:300]}
+    return out
+
+
 def run_own(args):
     import torch
 
@@ -349,6 +470,8 @@ def run_own(args):
             torch.distributed.destroy_process_group()
         return 0
 
+    side = {} if args.no_side else side_workloads(ctx, mesh, wl, args)
+
     # CPU baseline: the reference arm's own routine (the oracle port, whole
     # frames on all host cores) in a fresh process, so that no CUDA context,
     # torch threads or product library share the host with it; four warm-up
@@ -409,6 +532,7 @@ def run_own(args):
                      "per_ray_model": "36 B per primary ray + node_visits*128 B + tri_tests*48 B (" + model_src + ")"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
+        "other_configs": side,
         "gpu_launches": N_CAMERAS * args.steps,  # one k_frame per frame
         "clocks": clk,
     }
@@ -927,6 +1051,7 @@ def main():
     ap.add_argument("--leaf", type=int, default=2)
     ap.add_argument("--build", default="ploc", choices=["ploc", "lbvh"], help="BVH builder of the headline mesh")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-side", action="store_true", help="skip the short runs of the other configurations")
     ap.add_argument("--workload", default="torus",
                     choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "

@@ -136,6 +136,13 @@ typedef struct j3dg_build_opts {
    build time (21 vs 36 ms for 28M triangles). The traversal results are the
    same for either tree. */
 #define J3DG_BUILD_LBVH 0x1u
+/* BVH width (children per node) of the default builder: 4 unless one of
+   these is set. The cost-optimal collapse of the binary tree is run for the
+   chosen width; results do not depend on it. Nodes are 64 B (2 children),
+   128 B (4) or 256 B (8). Meshes of one frame, batch or ray query must share
+   a width; all-hits queries, voxel grids and learned networks need width 4. */
+#define J3DG_BUILD_WIDTH2 0x2u
+#define J3DG_BUILD_WIDTH8 0x4u
 
 typedef struct j3dg_mesh_info {
   uint32_t n_vertices;
@@ -146,6 +153,7 @@ typedef struct j3dg_mesh_info {
   uint32_t max_depth;
   uint64_t device_bytes;
   float build_ms; /* device time of the last build, CUDA events */
+  uint32_t width; /* children per BVH node: 2, 4 or 8 */
 } j3dg_mesh_info;
 
 /* ---------------------------------------------------------------- context */

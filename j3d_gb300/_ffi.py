@@ -72,7 +72,7 @@ class BuildOpts(C.Structure):
 class MeshInfo(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("min_bb", C.c_float * 3),
                 ("max_bb", C.c_float * 3), ("n_nodes", C.c_uint32), ("max_depth", C.c_uint32),
-                ("device_bytes", C.c_uint64), ("build_ms", C.c_float)]
+                ("device_bytes", C.c_uint64), ("build_ms", C.c_float), ("width", C.c_uint32)]
 
 
 class GeometryInfo(C.Structure):

@@ -24,7 +24,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-c
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math"] + ARCH
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
-CU_SOURCES = ["build.cu", "render.cu", "query.cu", "umma_gemm.cu", "learned.cu", "ingest.cu", "pointcloud.cu", "api.cu"]
+CU_SOURCES = ["build.cu", "render_dispatch.cu", "query.cu", "umma_gemm.cu", "learned.cu", "ingest.cu", "pointcloud.cu",
+              "api.cu"]
+# render.cu once per BVH width (its kernels are templated on it; namespaces w2 / w4 / w8)
+RENDER_WIDTHS = (2, 4, 8)
 CXX_SOURCES = ["host_math.cpp", "ingest_parse.cpp", "toplevel.cpp"]
 
 
@@ -64,6 +67,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD_DIR / (src + ".o")
         objs.append(obj)
         jobs.append([nv, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)])
+    for w in RENDER_WIDTHS:
+        obj = BUILD_DIR / f"render_w{w}.cu.o"
+        objs.append(obj)
+        jobs.append([nv, *NVCC_FLAGS, f"-DJ3DG_W={w}", "-c", str(CSRC / "render.cu"), "-o", str(obj)])
     for src in CXX_SOURCES:
         obj = BUILD_DIR / (src + ".o")
         objs.append(obj)

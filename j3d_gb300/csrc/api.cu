@@ -117,6 +117,7 @@ DevInst to_dev(const j3dg_instance& in) {
   d.nt = m->nt;
   d.db_id = in.db_id;
   d.scale = m->scale;
+  d.width = m->width;
   memcpy(d.cs, in.cs, sizeof(d.cs));
   j3dg_invert_orthonormal(in.cs, d.inv);  // canvas.cpp:734
   return d;
@@ -126,7 +127,8 @@ DevInst to_dev(const j3dg_instance& in) {
 // [DevTop][DevInst x cap][top-level BVH4 nodes x cap], 256-byte aligned. The
 // kernels receive &DevInst[0] and find the header just in front of it.
 size_t table_bytes(uint32_t cap) {
-  const size_t b = sizeof(DevTop) + sizeof(DevInst) * (size_t)cap + 128 * (size_t)std::max(cap, 1u);
+  const size_t node = sizeof(float4) * J3DG_NODE_F4(8);  // the widest node
+  const size_t b = sizeof(DevTop) + sizeof(DevInst) * (size_t)cap + node * (size_t)std::max(cap, 1u);
   return (b + 255) & ~size_t(255);
 }
 
@@ -154,7 +156,8 @@ const DevInst* write_table(char* h, char* d, const DevInst* t, const j3dg_instan
     cs[i] = objs[i].cs;
     deepest = std::max(deepest, objs[i].mesh->max_depth);
   }
-  const j3dg::TopLevel tl = j3dg::build_top_level(lo.data(), hi.data(), cs.data(), n,
+  const uint32_t W = objs[0].mesh->width;
+  const j3dg::TopLevel tl = j3dg::build_top_level(lo.data(), hi.data(), cs.data(), n, W,
                                                   reinterpret_cast<float*>(h + off_nodes), std::max(cap, 1u));
   memset(H, 0, sizeof(DevTop));
   if (tl.ok) {
@@ -164,7 +167,7 @@ const DevInst* write_table(char* h, char* d, const DevInst* t, const j3dg_instan
     H->n_inst = n;
     H->pad_scale = tl.pad_scale;
   }
-  const bool walkable = tl.ok && tl.depth + deepest <= J3DG_MAX_DEPTH;
+  const bool walkable = tl.ok && tl.depth + deepest <= J3DG_MAX_DEPTH_W(W);
   top = walkable && n >= kTopMinObjects;
   if (fits) *fits = walkable;
   return reinterpret_cast<const DevInst*>(d + sizeof(DevTop));
@@ -179,6 +182,8 @@ int upload_instances(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n, const D
   for (uint32_t i = 0; i < n; ++i) {
     if (!objs[i].mesh) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "instance without a mesh");
     if (objs[i].mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh belongs to another context");
+    if (objs[i].mesh->width != objs[0].mesh->width)
+      return fail(c, J3DG_ERR_UNSUPPORTED, "the objects of one scene must share a BVH width");
     t[i] = to_dev(objs[i]);
   }
   if (top) *top = false;
@@ -272,6 +277,7 @@ void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevI
   memset(&P, 0, sizeof(P));
   P.inst = inst;
   P.n_inst = s ? s->n_objects : 0;
+  P.width = (s && s->n_objects && s->objects[0].mesh) ? s->objects[0].mesh->width : 4u;
   P.w = cv->w;
   P.h = cv->h;
   P.x0 = 0;
@@ -460,7 +466,8 @@ int mesh_devinst(j3dg_ctx* c, const j3dg_mesh* mesh, const DevInst** out) {
 int ray_query_device(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* d_rays, uint32_t n, j3dg_hit* d_hits) {
   const DevInst* dinst = nullptr;
   if (int rc = mesh_devinst(c, mesh, &dinst)) return rc;
-  CK(c, launch_rays(dinst, 1, false, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status, nullptr, S(c)),
+  CK(c, launch_rays(dinst, 1, false, (int)mesh->width, d_rays, n, d_hits, false, all(c)->ex.d_ray_counter, c->d_status,
+                    nullptr, S(c)),
      "ray query");
   return J3DG_OK;
 }
@@ -656,6 +663,20 @@ int j3dg_ctx_read_counters(j3dg_ctx* c, uint64_t out[2], int reset) {
 
 // ------------------------------------------------------------------ mesh
 
+// The BVH width from the build flags (J3DG_BUILD_WIDTH2 / 8, default 4);
+// the LBVH builder collapses to width 4 only.
+int set_width(j3dg_ctx* c, j3dg_mesh* m) {
+  const uint32_t f = m->build_flags;
+  if (f & ~(uint32_t)(J3DG_BUILD_LBVH | J3DG_BUILD_WIDTH2 | J3DG_BUILD_WIDTH8))
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: unknown build flags");
+  if ((f & J3DG_BUILD_WIDTH2) && (f & J3DG_BUILD_WIDTH8))
+    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: two BVH widths requested");
+  m->width = (f & J3DG_BUILD_WIDTH2) ? 2u : ((f & J3DG_BUILD_WIDTH8) ? 8u : 4u);
+  if (m->width != 4 && (f & J3DG_BUILD_LBVH))
+    return fail(c, J3DG_ERR_UNSUPPORTED, "mesh_build: the LBVH builder makes 4-wide trees only");
+  return J3DG_OK;
+}
+
 int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, uint32_t nt,
                     const j3dg_build_opts* opts, j3dg_mesh** out) {
   if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
@@ -673,9 +694,9 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   m->nt = nt;
   m->leaf_size = leaf;
   m->build_flags = opts ? opts->flags : 0u;
-  if (m->build_flags & ~(uint32_t)J3DG_BUILD_LBVH) {
+  if (int rc = set_width(c, m)) {
     delete m;
-    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: unknown build flags");
+    return rc;
   }
   CtxExtra& X = all(c)->ex;
   float* dV = nullptr;
@@ -739,6 +760,7 @@ int j3dg_mesh_get_info(const j3dg_mesh* m, j3dg_mesh_info* info) {
   info->max_depth = m->max_depth;
   info->device_bytes = m->device_bytes;
   info->build_ms = m->build_ms;
+  info->width = m->width;
   return J3DG_OK;
 }
 
@@ -809,7 +831,8 @@ static int ray_query(j3dg_ctx* c, const j3dg_instance* objs, uint32_t n_obj, con
     CK(c, cudaMemcpyAsync(dr, rays, sizeof(j3dg_ray) * (size_t)n, cudaMemcpyHostToDevice, S(c)), "rays");
   }
   if (!hits_dev) CK(c, cudaMallocAsync((void**)&dh, sizeof(j3dg_hit) * (size_t)n, S(c)), "hits");
-  CK(c, j3dg::launch_rays(dinst, n_obj, top, dr, n, dh, any, all(c)->ex.d_ray_counter, c->d_status, j3dg::ctx_counters(c),
+  CK(c, j3dg::launch_rays(dinst, n_obj, top, n_obj ? (int)objs[0].mesh->width : 4, dr, n, dh, any,
+                          all(c)->ex.d_ray_counter, c->d_status, j3dg::ctx_counters(c),
                           S(c)),
      "find");
   if (!hits_dev) {
@@ -834,6 +857,7 @@ int j3dg_find_all(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_ray* rays, uint
                   uint32_t* counts) {
   if (!c || !mesh || (n && (!rays || !counts || (cap && !hits)))) return J3DG_ERR_INVALID_ARGUMENT;
   if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "find_all: mesh of another context");
+  if (mesh->width != 4) return fail(c, J3DG_ERR_UNSUPPORTED, "find_all: needs a 4-wide BVH");
   cudaSetDevice(c->device);
   j3dg_instance one;
   one.mesh = mesh;
@@ -871,6 +895,7 @@ int j3dg_voxelize(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, uint32_t
   if (!c || !mesh || !dims) return J3DG_ERR_INVALID_ARGUMENT;
   if (max_dim == 0 || max_dim > 1024) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize: max_dim must be 1..1024");
   if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize: mesh of another context");
+  if (mesh->width != 4) return fail(c, J3DG_ERR_UNSUPPORTED, "voxelize: needs a 4-wide BVH");
   cudaSetDevice(c->device);
   // vox.cpp:286-299
   const float* mn = mesh->min_bb;
@@ -923,6 +948,7 @@ int j3dg_voxelize_noalloc(j3dg_ctx* c, const j3dg_mesh* mesh, uint32_t max_dim, 
   if (!c || !mesh || !dims) return J3DG_ERR_INVALID_ARGUMENT;
   if (max_dim == 0 || max_dim > 1024) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: max_dim must be 1..1024");
   if (mesh->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "voxelize_noalloc: mesh of another context");
+  if (mesh->width != 4) return fail(c, J3DG_ERR_UNSUPPORTED, "voxelize_noalloc: needs a 4-wide BVH");
   cudaSetDevice(c->device);
   const float* mn = mesh->min_bb;
   const float* mx = mesh->max_bb;
@@ -1264,8 +1290,9 @@ struct BatchLayout {
   }
 };
 
-int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_inst) {
+int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_inst, uint32_t* width = nullptr) {
   total_inst = 0;
+  uint32_t w = 0;
   for (uint32_t i = 0; i < n; ++i) {
     if (!f[i].canvas || !f[i].matcap) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: frame without canvas or matcap");
     if (f[i].canvas->ctx != c || f[i].matcap->ctx != c) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: object of another context");
@@ -1273,12 +1300,17 @@ int check_frames(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t& total_i
       if (f[j].canvas == f[i].canvas) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: a canvas appears twice");
     if (f[i].scene) {
       if (int rc = scene_ok(c, f[i].scene)) return rc;
-      for (uint32_t k = 0; k < f[i].scene->n_objects; ++k)
+      for (uint32_t k = 0; k < f[i].scene->n_objects; ++k) {
         if (!f[i].scene->objects[k].mesh || f[i].scene->objects[k].mesh->ctx != c)
           return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch: bad scene object");
+        const uint32_t mw = f[i].scene->objects[k].mesh->width;
+        if (w && mw != w) return fail(c, J3DG_ERR_UNSUPPORTED, "batch: the meshes of one batch must share a BVH width");
+        w = mw;
+      }
       total_inst += f[i].scene->n_objects;
     }
   }
+  if (width) *width = w ? w : 4u;
   return J3DG_OK;
 }
 
@@ -1339,10 +1371,11 @@ uint32_t pack_frames(const j3dg_frame* f, uint32_t n, const BatchLayout& L, char
 }
 
 int enqueue_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, const BatchLayout& L, char* d, uint32_t items,
-                  uint32_t* work, bool top) {
+                  uint32_t* work, bool top, uint32_t width) {
   const FrameParams* dP = reinterpret_cast<const FrameParams*>(d + L.off_params);
   const uint32_t* dOff = reinterpret_cast<const uint32_t*>(d + L.off_offsets);
-  CK(c, j3dg::launch_render_batch(dP, dOff, n, items, work, all(c)->ex.batch_threads, top, S(c)), "batch");
+  CK(c, j3dg::launch_render_batch(dP, dOff, n, items, work, all(c)->ex.batch_threads, top, (int)width, S(c)),
+     "batch");
   for (uint32_t i = 0; i < n; ++i) {
     const int mode = shade_mode_of(f[i].canvas->settings);
     if (mode != 0 && f[i].canvas->w && f[i].canvas->h) {
@@ -1366,6 +1399,7 @@ struct j3dg_batch {
   BatchLayout L;
   std::vector<char> walk, fits;  // per frame (pack_frame)
   bool top = false;              // the captured launch walks top levels
+  uint32_t width = 4;            // the BVH width of every mesh of the batch
   char* h = nullptr;  // pinned staging
   char* d = nullptr;  // device copy
   uint32_t* work = nullptr;
@@ -1378,8 +1412,8 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
   if (!c || (n && !f)) return J3DG_ERR_INVALID_ARGUMENT;
   if (n == 0) return J3DG_OK;
   cudaSetDevice(c->device);
-  uint32_t total_inst = 0;
-  if (int rc = check_frames(c, f, n, total_inst)) return rc;
+  uint32_t total_inst = 0, width = 4;
+  if (int rc = check_frames(c, f, n, total_inst, &width)) return rc;
   for (uint32_t i = 0; i < n; ++i) j3dg::canvas_writable(f[i].canvas);
   std::vector<uint32_t> caps(n);
   for (uint32_t i = 0; i < n; ++i) caps[i] = f[i].scene ? f[i].scene->n_objects : 0u;
@@ -1395,7 +1429,7 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
   const uint32_t items = pack_frames(f, n, L, h.data(), d, caps.data(), all(c)->ex.top_level, walk, fits, top);
   // pageable source: the copy is staged before the call returns
   CK(c, cudaMemcpyAsync(d, h.data(), L.bytes, cudaMemcpyHostToDevice, S(c)), "render_batch");
-  int rc = enqueue_batch(c, f, n, L, d, items, work, top);
+  int rc = enqueue_batch(c, f, n, L, d, items, work, top, width);
   cudaFreeAsync(d, S(c));
   return rc;
 }
@@ -1404,11 +1438,12 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
   if (!c || !out || n == 0 || !f) return J3DG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   cudaSetDevice(c->device);
-  uint32_t total_inst = 0;
-  if (int rc = check_frames(c, f, n, total_inst)) return rc;
+  uint32_t total_inst = 0, width = 4;
+  if (int rc = check_frames(c, f, n, total_inst, &width)) return rc;
   j3dg_batch* b = new (std::nothrow) j3dg_batch();
   if (!b) return J3DG_ERR_OUT_OF_MEMORY;
   b->ctx = c;
+  b->width = width;
   b->hold.attach(c);
   b->frames.assign(f, f + n);
   b->objects.resize(n);
@@ -1440,7 +1475,7 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
   int rc = J3DG_OK;
   if (e == cudaSuccess) {
     e = cudaMemcpyAsync(b->d, b->h, b->L.bytes, cudaMemcpyHostToDevice, S(c));
-    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work, b->top);
+    if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work, b->top, b->width);
     cudaError_t e2 = cudaStreamEndCapture(S(c), &b->graph);
     if (e == cudaSuccess) e = e2;
   }
@@ -1459,9 +1494,12 @@ int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* s) {
   if (int rc = scene_ok(c, s)) return rc;
   const uint32_t cap = b->caps[i];
   if (s->n_objects > cap) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_set_scene: more objects than at creation");
-  for (uint32_t k = 0; k < s->n_objects; ++k)
+  for (uint32_t k = 0; k < s->n_objects; ++k) {
     if (!s->objects[k].mesh || s->objects[k].mesh->ctx != c)
       return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_set_scene: bad scene object");
+    if (s->objects[k].mesh->width != b->width)
+      return fail(c, J3DG_ERR_UNSUPPORTED, "batch_set_scene: a mesh of another BVH width than the batch's");
+  }
   cudaSetDevice(c->device);
   CK(c, cudaEventSynchronize(b->done), "batch_set_scene");  // the staging is read by the running launch
   const std::vector<j3dg_instance> old_objects = b->objects[i];

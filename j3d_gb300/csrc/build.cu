@@ -585,45 +585,52 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
 
 __device__ __forceinline__ float half_area4(float4 lo, float4 hi);
 
-__device__ __forceinline__ void sub_costs(const float4* __restrict__ cost, const float4* __restrict__ tris, uint32_t r,
-                                          float c[5]) {
+// costs C(r, 1..W) of subtree r (a triangle: its area times c_t for any i)
+template <int W>
+__device__ __forceinline__ void sub_costs(const float* __restrict__ cost, const float4* __restrict__ tris, uint32_t r,
+                                          float (&c)[W + 1]) {
   if (r & 0x80000000u) {
     float4 lo, hi;
     leaf_box(tris, r & 0x7fffffffu, lo, hi);
-    c[1] = c[2] = c[3] = c[4] = half_area4(lo, hi) * J3DG_SAH_CTRI;
+    const float v = half_area4(lo, hi) * J3DG_SAH_CTRI;
+#pragma unroll
+    for (int i = 1; i <= W; ++i) c[i] = v;
   } else {
-    const float4 v = cost[r];
-    c[1] = v.x;
-    c[2] = v.y;
-    c[3] = v.z;
-    c[4] = v.w;
+#pragma unroll
+    for (int i = 1; i <= W; ++i) c[i] = cost[(size_t)r * W + i - 1];
   }
 }
 
+// cost: W floats per binary node (C(n, 1..W)); dec: W bytes per node
+// (dec[0] = the k of the node case | 0x80 when the leaf case is cheaper;
+// dec[i - 1], i = 2..W: 0 = as i - 1, else the k of the best split)
+template <int W>
 __global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* __restrict__ box,
                                 const uint32_t* __restrict__ count, const float4* __restrict__ tris, uint32_t lo,
-                                uint32_t hi, uint32_t leaf_size, float4* __restrict__ cost, uchar4* __restrict__ dec) {
+                                uint32_t hi, uint32_t leaf_size, float* __restrict__ cost, uint8_t* __restrict__ dec) {
   const uint32_t n = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= hi) return;
   const uint2 c = child[n];
-  float cl[5], cr[5], C[5];
-  sub_costs(cost, tris, c.x, cl);
-  sub_costs(cost, tris, c.y, cr);
+  float cl[W + 1], cr[W + 1], C[W + 1];
+  sub_costs<W>(cost, tris, c.x, cl);
+  sub_costs<W>(cost, tris, c.y, cr);
   const float A = half_area4(box[n].lo, box[n].hi);
   float best = FLT_MAX;
   uint32_t bk = 1;
-  for (uint32_t k = 1; k <= 3; ++k)
-    if (cl[k] + cr[4 - k] < best) {
-      best = cl[k] + cr[4 - k];
+#pragma unroll
+  for (uint32_t k = 1; k < (uint32_t)W; ++k)
+    if (cl[k] + cr[W - k] < best) {
+      best = cl[k] + cr[W - k];
       bk = k;
     }
   const float node = A + best;  // c_n = 1
   const uint32_t N = count[n];
   const float leaf = N <= leaf_size ? A * (float)N * J3DG_SAH_CTRI : FLT_MAX;
   C[1] = fminf(leaf, node);
-  uint8_t d[4];
+  uint8_t d[W];
   d[0] = (uint8_t)(bk | (leaf <= node ? 0x80u : 0u));
-  for (uint32_t i = 2; i <= 4; ++i) {
+#pragma unroll
+  for (uint32_t i = 2; i <= (uint32_t)W; ++i) {
     float v = C[i - 1];
     uint32_t dk = 0;
     for (uint32_t k = 1; k < i; ++k)
@@ -634,8 +641,11 @@ __global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* 
     C[i] = v;
     d[i - 1] = (uint8_t)dk;
   }
-  cost[n] = make_float4(C[1], C[2], C[3], C[4]);
-  dec[n] = make_uchar4(d[0], d[1], d[2], d[3]);
+#pragma unroll
+  for (int i = 1; i <= W; ++i) {
+    cost[(size_t)n * W + i - 1] = C[i];
+    dec[(size_t)n * W + i - 1] = d[i - 1];
+  }
 }
 
 struct PlaceItem {
@@ -648,17 +658,18 @@ struct PlaceItem {
 // The collapse of k_collapse over a tree whose subtrees are not ranges of the
 // sorted leaves: each slot carries its subtree's first position; leaves are
 // written to tris_out at those positions in depth-first order.
+template <int W>
 __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode* __restrict__ box,
                                  const uint32_t* __restrict__ count, const float4* __restrict__ tris,
                                  const PlaceItem* __restrict__ qin, uint32_t n_in, PlaceItem* __restrict__ qout,
                                  uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
                                  uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
-                                 uint32_t nt, uint32_t* status, const uchar4* __restrict__ dec) {
+                                 uint32_t nt, uint32_t* status, const uint8_t* __restrict__ dec) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_in) return;
   const PlaceItem it = qin[t];
-  uint32_t ref[4], cnt[4], start[4];
-  float4 lo[4], hi[4];
+  uint32_t ref[W], cnt[W], start[W];
+  float4 lo[W], hi[W];
   auto load = [&](uint32_t r, int s, uint32_t first) {
     ref[s] = r;
     start[s] = first;
@@ -674,25 +685,24 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
   const uint2 c = child[it.bin];
   int m = 0;
   if (dec) {
-    // the slots the cost decisions give: expand(left, k) then expand(right, 4 - k)
+    // the slots the cost decisions give: expand(left, k) then expand(right, W - k)
     struct Slot {
       uint32_t r, i, start;
     };
-    Slot stk[8];
+    Slot stk[2 * W];
     int sp = 0;
-    const uint32_t k = dec[it.bin].x & 0x7fu;
+    const uint32_t k = dec[(size_t)it.bin * W] & 0x7fu;
     const uint32_t nl = (c.x & 0x80000000u) ? 1u : count[c.x];
-    stk[sp++] = Slot{c.y, 4u - k, it.start + nl};
+    stk[sp++] = Slot{c.y, (uint32_t)W - k, it.start + nl};
     stk[sp++] = Slot{c.x, k, it.start};
-    while (sp > 0 && m < 4) {
+    while (sp > 0 && m < W) {
       const Slot e = stk[--sp];
       if ((e.r & 0x80000000u) || e.i <= 1u) {
         load(e.r, m++, e.start);
         continue;
       }
-      const uchar4 dd = dec[e.r];
-      const uint32_t d = e.i == 2u ? dd.y : (e.i == 3u ? dd.z : dd.w);
-      if (d == 0u || sp + 2 > 8) {
+      const uint32_t d = dec[(size_t)e.r * W + e.i - 1];
+      if (d == 0u || sp + 2 > 2 * W) {
         stk[sp++] = Slot{e.r, e.i - 1u, e.start};
         continue;
       }
@@ -706,7 +716,7 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     load(c.y, 1, it.start + cnt[0]);
     m = 2;
   }
-  while (!dec && m < 4) {
+  while (!dec && m < W) {
     int best = -1;
     float ba = -1.f;
     for (int s = 0; s < m; ++s)
@@ -724,20 +734,23 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     load(cc.y, m, s0 + cnt[best]);
     ++m;
   }
-  float4* W = wide + 8 * (size_t)it.wide;
-  float v[6][4];
-  uint32_t out_ref[4];
-  for (int s = 0; s < 4; ++s) {
+  // the node in the width-W layout: planes [6][W], refs [W], zero padding
+  float F[4 * J3DG_NODE_F4(W)];
+#pragma unroll
+  for (int k = 0; k < 4 * J3DG_NODE_F4(W); ++k) F[k] = 0.f;
+  for (int s = 0; s < W; ++s) {
+    uint32_t out_ref = J3DG_EMPTY_REF;
     if (s < m) {
-      v[0][s] = lo[s].x;
-      v[1][s] = hi[s].x;
-      v[2][s] = lo[s].y;
-      v[3][s] = hi[s].y;
-      v[4][s] = lo[s].z;
-      v[5][s] = hi[s].z;
-      const bool as_leaf = (ref[s] & 0x80000000u) || (dec ? (dec[ref[s]].x & 0x80u) != 0 : cnt[s] <= leaf_size);
+      F[0 * W + s] = lo[s].x;
+      F[1 * W + s] = hi[s].x;
+      F[2 * W + s] = lo[s].y;
+      F[3 * W + s] = hi[s].y;
+      F[4 * W + s] = lo[s].z;
+      F[5 * W + s] = hi[s].z;
+      const bool as_leaf = (ref[s] & 0x80000000u) ||
+                           (dec ? (dec[(size_t)ref[s] * W] & 0x80u) != 0 : cnt[s] <= leaf_size);
       if (as_leaf && cnt[s] <= J3DG_MAX_LEAF) {
-        out_ref[s] = J3DG_LEAF_BIT | (start[s] << 3) | (cnt[s] - 1u);
+        out_ref = J3DG_LEAF_BIT | (start[s] << 3) | (cnt[s] - 1u);
         uint32_t stk[J3DG_MAX_LEAF];
         int sp = 0;
         uint32_t k = 0;
@@ -766,18 +779,17 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
         const uint32_t w = atomicAdd(n_wide, 1u);
         const uint32_t q = atomicAdd(n_out, 1u);
         qout[q] = PlaceItem{ref[s], w, it.depth + 1, start[s]};
-        out_ref[s] = w;
+        out_ref = w;
       }
     } else {
-      v[0][s] = v[2][s] = v[4][s] = 3.4e38f;
-      v[1][s] = v[3][s] = v[5][s] = -3.4e38f;
-      out_ref[s] = J3DG_EMPTY_REF;
+      F[0 * W + s] = F[2 * W + s] = F[4 * W + s] = 3.4e38f;
+      F[1 * W + s] = F[3 * W + s] = F[5 * W + s] = -3.4e38f;
     }
+    F[6 * W + s] = __uint_as_float(out_ref);
   }
-  for (int k = 0; k < 6; ++k) W[k] = make_float4(v[k][0], v[k][1], v[k][2], v[k][3]);
-  W[6] = make_float4(__uint_as_float(out_ref[0]), __uint_as_float(out_ref[1]), __uint_as_float(out_ref[2]),
-                     __uint_as_float(out_ref[3]));
-  W[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4* Wn = wide + J3DG_NODE_F4(W) * (size_t)it.wide;
+#pragma unroll
+  for (int k = 0; k < J3DG_NODE_F4(W); ++k) Wn[k] = make_float4(F[4 * k], F[4 * k + 1], F[4 * k + 2], F[4 * k + 3]);
   atomicMax(max_depth, it.depth);
 }
 
@@ -796,84 +808,128 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
 #define J3DG_DFS_ORDER 1
 #endif
 
-__device__ __forceinline__ void child_refs(const float4* __restrict__ wide, uint32_t i, uint32_t r[4]) {
-  const float4 ch = wide[8 * (size_t)i + 6];
-  r[0] = __float_as_uint(ch.x);
-  r[1] = __float_as_uint(ch.y);
-  r[2] = __float_as_uint(ch.z);
-  r[3] = __float_as_uint(ch.w);
+template <int W>
+__device__ __forceinline__ void child_refs(const float4* __restrict__ wide, uint32_t i, uint32_t (&r)[W]) {
+  const float* f = reinterpret_cast<const float*>(wide + J3DG_NODE_F4(W) * (size_t)i) + 6 * W;
+#pragma unroll
+  for (int c = 0; c < W; ++c) r[c] = __float_as_uint(f[c]);
 }
 
 // size[i] = wide nodes in the subtree of i (children of level lo..hi are done)
+template <int W>
 __global__ void k_dfs_size(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, uint32_t* __restrict__ size) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
-  uint32_t r[4], s = 1;
-  child_refs(wide, i, r);
+  uint32_t r[W], s = 1;
+  child_refs<W>(wide, i, r);
 #pragma unroll
-  for (int c = 0; c < 4; ++c)
+  for (int c = 0; c < W; ++c)
     if (!(r[c] & J3DG_LEAF_BIT)) s += size[r[c]];  // the empty ref has the leaf bit
   size[i] = s;
 }
 
 // children of the level's nodes take consecutive ranges after their parent
+template <int W>
 __global__ void k_dfs_place(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ size,
                             uint32_t* __restrict__ pos) {
   const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= hi) return;
-  uint32_t r[4], next = pos[i] + 1;
-  child_refs(wide, i, r);
+  uint32_t r[W], next = pos[i] + 1;
+  child_refs<W>(wide, i, r);
 #pragma unroll
-  for (int c = 0; c < 4; ++c)
+  for (int c = 0; c < W; ++c)
     if (!(r[c] & J3DG_LEAF_BIT)) {
       pos[r[c]] = next;
       next += size[r[c]];
     }
 }
 
+template <int W>
 __global__ void k_dfs_permute(const float4* __restrict__ wide, uint32_t n, const uint32_t* __restrict__ pos,
                               float4* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float4* src = wide + 8 * (size_t)i;
-  float4* dst = out + 8 * (size_t)pos[i];
+  constexpr int F4 = J3DG_NODE_F4(W);
+  const float4* src = wide + F4 * (size_t)i;
+  float F[4 * F4];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) dst[k] = src[k];
-  uint32_t r[4];
-  child_refs(wide, i, r);
+  for (int k = 0; k < F4; ++k) {
+    const float4 v = src[k];
+    F[4 * k] = v.x, F[4 * k + 1] = v.y, F[4 * k + 2] = v.z, F[4 * k + 3] = v.w;
+  }
 #pragma unroll
-  for (int c = 0; c < 4; ++c)
-    if (!(r[c] & J3DG_LEAF_BIT)) r[c] = pos[r[c]];
-  dst[6] = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]), __uint_as_float(r[3]));
-  dst[7] = src[7];
+  for (int c = 0; c < W; ++c) {
+    const uint32_t r = __float_as_uint(F[6 * W + c]);
+    if (!(r & J3DG_LEAF_BIT)) F[6 * W + c] = __uint_as_float(pos[r]);
+  }
+  float4* dst = out + F4 * (size_t)pos[i];
+#pragma unroll
+  for (int k = 0; k < F4; ++k) dst[k] = make_float4(F[4 * k], F[4 * k + 1], F[4 * k + 2], F[4 * k + 3]);
 }
 
 // out = the n wide nodes of `wide` (root 0, level L = [level_end[L-1],
 // level_end[L]) with level_end[-1] = 0) in depth-first order; root stays 0.
-static cudaError_t dfs_order(const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end, float4* out,
-                             cudaStream_t st) {
+template <int W>
+static cudaError_t dfs_order_w(const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end, float4* out,
+                               cudaStream_t st) {
   uint32_t *size = nullptr, *pos = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&size, sizeof(uint32_t) * (size_t)n, st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&pos, sizeof(uint32_t) * (size_t)n, st);
   const size_t L = level_end.size();
   for (size_t l = L; e == cudaSuccess && l-- > 0;) {
     const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
-    if (hi > lo) k_dfs_size<<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size);
+    if (hi > lo) k_dfs_size<W><<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(pos, 0, sizeof(uint32_t), st);
   for (size_t l = 0; e == cudaSuccess && l < L; ++l) {
     const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
-    if (hi > lo) k_dfs_place<<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size, pos);
+    if (hi > lo) k_dfs_place<W><<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size, pos);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    k_dfs_permute<<<(n + 255) / 256, 256, 0, st>>>(wide, n, pos, out);
+    k_dfs_permute<W><<<(n + 255) / 256, 256, 0, st>>>(wide, n, pos, out);
     e = cudaGetLastError();
   }
   if (size) cudaFreeAsync(size, st);
   if (pos) cudaFreeAsync(pos, st);
   return e;
+}
+
+static cudaError_t dfs_order(uint32_t W, const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end,
+                             float4* out, cudaStream_t st) {
+  if (W == 2) return dfs_order_w<2>(wide, n, level_end, out, st);
+  if (W == 8) return dfs_order_w<8>(wide, n, level_end, out, st);
+  return dfs_order_w<4>(wide, n, level_end, out, st);
+}
+
+static void launch_collapse_cost(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
+                                 const float4* tris, uint32_t lo, uint32_t hi, uint32_t leaf_size, float* cost,
+                                 uint8_t* dec, cudaStream_t st) {
+  const uint32_t blocks = (hi - lo + 255) / 256;
+  if (W == 2)
+    k_collapse_cost<2><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+  else if (W == 8)
+    k_collapse_cost<8><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+  else
+    k_collapse_cost<4><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+}
+
+static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
+                                  const float4* tris, const PlaceItem* qin, uint32_t n_in, PlaceItem* qout,
+                                  uint32_t* n_out, uint32_t* n_wide, float4* wide, uint32_t leaf_size,
+                                  uint32_t* max_depth, float4* tris_out, uint32_t nt, uint32_t* status,
+                                  const uint8_t* dec, cudaStream_t st) {
+  const uint32_t blocks = (n_in + 127) / 128;
+  if (W == 2)
+    k_collapse_place<2><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+                                                max_depth, tris_out, nt, status, dec);
+  else if (W == 8)
+    k_collapse_place<8><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+                                                max_depth, tris_out, nt, status, dec);
+  else
+    k_collapse_place<4><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+                                                max_depth, tris_out, nt, status, dec);
 }
 
 // -------------------------------------------------- 5c. SAH top levels ----
@@ -1401,8 +1457,10 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   CollapseItem root_item;
   std::vector<uint32_t> level_end(1, 1u);  // wide nodes of level L end at level_end[L]
   std::vector<uint32_t> round_end;         // binary nodes of PLOC round r end at round_end[r]
-  float4* dp_cost = nullptr;
-  uchar4* dp_dec = nullptr;
+  float* dp_cost = nullptr;
+  uint8_t* dp_dec = nullptr;
+  const uint32_t W = m->width;
+  const size_t F4 = J3DG_NODE_F4(W);
 
   J3DG_CK(cudaMallocAsync((void**)&d_part, sizeof(float) * 6 * bbox_blocks, st));
   J3DG_CK(cudaMallocAsync((void**)&d_bb, sizeof(float) * 6, st));
@@ -1452,8 +1510,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
     m->n_nodes = 0;
     m->max_depth = 0;
-    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8));
-    J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * 8, st));
+    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * F4));
+    J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * F4, st));
     goto cleanup;
   }
 
@@ -1641,24 +1699,24 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_DROP(seg_scan);
     J3DG_DROP(ranges);
     if (J3DG_SAH_COLLAPSE) {
-      J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float4) * (nt - 1), st));
-      J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uchar4) * (nt - 1), st));
+      J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float) * W * (nt - 1), st));
+      J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uint8_t) * W * (nt - 1), st));
       // children before parents: the PLOC rounds in order, then the top levels deepest first
       uint32_t lo_n = n_top;
       for (uint32_t hi_n : round_end) {
-        k_collapse_cost<<<(hi_n - lo_n + 255) / 256, 256, 0, st>>>(child, box, count, (const float4*)m->d_tris, lo_n,
-                                                                     hi_n, m->leaf_size, dp_cost, dp_dec);
+        launch_collapse_cost(W, child, box, count, (const float4*)m->d_tris, lo_n, hi_n, m->leaf_size, dp_cost, dp_dec,
+                             st);
         lo_n = hi_n;
       }
       for (size_t k = top_end.size(); k-- > 0;) {
         const uint32_t lo_t = k ? top_end[k - 1] : 0u, hi_t = top_end[k];
-        k_collapse_cost<<<(hi_t - lo_t + 255) / 256, 256, 0, st>>>(child, box, count, (const float4*)m->d_tris, lo_t,
-                                                                     hi_t, m->leaf_size, dp_cost, dp_dec);
+        launch_collapse_cost(W, child, box, count, (const float4*)m->d_tris, lo_t, hi_t, m->leaf_size, dp_cost, dp_dec,
+                             st);
       }
       J3DG_CK(cudaGetLastError());
     }
     J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
-    J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * 8 * (size_t)nt, st));
+    J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * F4 * (size_t)nt, st));
     J3DG_CK(cudaMallocAsync((void**)&pa, sizeof(PlaceItem) * (size_t)nt, st));
     J3DG_CK(cudaMallocAsync((void**)&pb, sizeof(PlaceItem) * (size_t)nt, st));
     J3DG_CK(cudaMalloc((void**)&tris_out, sizeof(float4) * 3 * (size_t)nt));
@@ -1674,9 +1732,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     n_in = 1;
     while (n_in > 0) {
       J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
-      k_collapse_place<<<(n_in + 127) / 128, 128, 0, st>>>(child, box, count, (const float4*)m->d_tris, pa, n_in, pb,
-                                                          counters + 2, counters + 1, wide, m->leaf_size, counters + 3,
-                                                          tris_out, nt, d_status, dp_dec);
+      launch_collapse_place(W, child, box, count, (const float4*)m->d_tris, pa, n_in, pb, counters + 2, counters + 1,
+                            wide, m->leaf_size, counters + 3, tris_out, nt, d_status, dp_dec, st);
       J3DG_CK(cudaGetLastError());
       J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
       J3DG_CK(cudaStreamSynchronize(st));
@@ -1687,11 +1744,11 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->n_nodes = hc[1];
     m->max_depth = hc[3];
     m->root_ref = 0;
-    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
+    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * F4 * (size_t)m->n_nodes));
     if (J3DG_DFS_ORDER)
-      J3DG_CK(dfs_order(wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
+      J3DG_CK(dfs_order(W, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
     else
-      J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
+      J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * F4 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
     J3DG_CK(cudaStreamSynchronize(st));
     cudaFree(m->d_tris);  // the leaf-ordered triangles are the placed ones now
     m->d_tris = tris_out;
@@ -1739,7 +1796,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   m->root_ref = 0;
   J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
   if (J3DG_DFS_ORDER)
-    J3DG_CK(dfs_order(wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
+    J3DG_CK(dfs_order(4, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
   else
     J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
 
@@ -1796,11 +1853,11 @@ cleanup:
     }
   }
   if (rc != J3DG_OK) return rc;
-  if (m->max_depth > J3DG_MAX_DEPTH) {
-    err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack";
+  if (m->max_depth > J3DG_MAX_DEPTH_W(W)) {
+    err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack at width " + std::to_string(W);
     return J3DG_ERR_UNSUPPORTED;
   }
-  m->device_bytes = sizeof(float4) * 8 * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
+  m->device_bytes = sizeof(float4) * F4 * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
                     sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 4 * (uint64_t)nt;
   return J3DG_OK;
 }

@@ -42,7 +42,7 @@ struct DevInst {
   uint32_t nt;
   uint32_t db_id;
   float scale;
-  float pad_;
+  uint32_t width;          // children per BVH node (2, 4, 8)
   float cs[16];
   float inv[16];
 };
@@ -285,7 +285,72 @@ __device__ __forceinline__ bool tri_test(const Ray& r, const float4* __restrict_
 // at most `iters` node or leaf steps, so persistent warps can refill lanes
 // whose rays have finished. Corrupt trees raise status bits instead of
 // trapping.
-template <int N, bool TOP = false>
+// Child c's near / far planes of a width-W node for the ray's octant, and
+// its ref (the layout of J3DG_NODE_F4; the same values slab() selects).
+template <int W>
+struct NodeLoad {
+  float pnx[W], pfx[W], pny[W], pfy[W], pnz[W], pfz[W];
+  uint32_t rc[W];
+  __device__ __forceinline__ void load(const float4* __restrict__ nd, uint32_t neg) {
+    const uint32_t ox = neg & 1u, oy = (neg >> 1) & 1u, oz = (neg >> 2) & 1u;
+    if constexpr (W == 2) {
+      // [lo0 lo1 hi0 hi1] per axis, refs in float4 3
+      const float4 x = __ldg(nd), y = __ldg(nd + 1), z = __ldg(nd + 2), r = __ldg(nd + 3);
+      pnx[0] = ox ? x.z : x.x, pnx[1] = ox ? x.w : x.y, pfx[0] = ox ? x.x : x.z, pfx[1] = ox ? x.y : x.w;
+      pny[0] = oy ? y.z : y.x, pny[1] = oy ? y.w : y.y, pfy[0] = oy ? y.x : y.z, pfy[1] = oy ? y.y : y.w;
+      pnz[0] = oz ? z.z : z.x, pnz[1] = oz ? z.w : z.y, pfz[0] = oz ? z.x : z.z, pfz[1] = oz ? z.y : z.w;
+      rc[0] = __float_as_uint(r.x);
+      rc[1] = __float_as_uint(r.y);
+    } else {
+      // W / 4 float4 per plane; refs after the six planes
+      constexpr int Q = W / 4;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const float4 a = __ldg(nd + (0 * 2 + ox) * Q + q), b = __ldg(nd + (0 * 2 + (ox ^ 1u)) * Q + q);
+        const float4 c = __ldg(nd + (1 * 2 + oy) * Q + q), d = __ldg(nd + (1 * 2 + (oy ^ 1u)) * Q + q);
+        const float4 e = __ldg(nd + (2 * 2 + oz) * Q + q), f = __ldg(nd + (2 * 2 + (oz ^ 1u)) * Q + q);
+        const float4 r = __ldg(nd + 6 * Q + q);
+        pnx[4 * q] = a.x, pnx[4 * q + 1] = a.y, pnx[4 * q + 2] = a.z, pnx[4 * q + 3] = a.w;
+        pfx[4 * q] = b.x, pfx[4 * q + 1] = b.y, pfx[4 * q + 2] = b.z, pfx[4 * q + 3] = b.w;
+        pny[4 * q] = c.x, pny[4 * q + 1] = c.y, pny[4 * q + 2] = c.z, pny[4 * q + 3] = c.w;
+        pfy[4 * q] = d.x, pfy[4 * q + 1] = d.y, pfy[4 * q + 2] = d.z, pfy[4 * q + 3] = d.w;
+        pnz[4 * q] = e.x, pnz[4 * q + 1] = e.y, pnz[4 * q + 2] = e.z, pnz[4 * q + 3] = e.w;
+        pfz[4 * q] = f.x, pfz[4 * q + 1] = f.y, pfz[4 * q + 2] = f.z, pfz[4 * q + 3] = f.w;
+        rc[4 * q] = __float_as_uint(r.x), rc[4 * q + 1] = __float_as_uint(r.y);
+        rc[4 * q + 2] = __float_as_uint(r.z), rc[4 * q + 3] = __float_as_uint(r.w);
+      }
+    }
+  }
+};
+
+// ascending (t, ref) by a sorting network: 1, 5 or 19 compare-exchanges
+template <int W>
+__device__ __forceinline__ void sort_children(float (&tc)[W], uint32_t (&rc)[W]) {
+#define J3DG_CX(i, j)    \
+  if (tc[j] < tc[i]) {   \
+    float tt = tc[i];    \
+    tc[i] = tc[j];       \
+    tc[j] = tt;          \
+    uint32_t rr = rc[i]; \
+    rc[i] = rc[j];       \
+    rc[j] = rr;          \
+  }
+  if constexpr (W == 2) {
+    J3DG_CX(0, 1)
+  } else if constexpr (W == 4) {
+    J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(1, 2)
+  } else {
+    J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(4, 6) J3DG_CX(5, 7)
+    J3DG_CX(0, 4) J3DG_CX(1, 5) J3DG_CX(2, 6) J3DG_CX(3, 7)
+    J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(4, 5) J3DG_CX(6, 7)
+    J3DG_CX(2, 4) J3DG_CX(3, 5)
+    J3DG_CX(1, 4) J3DG_CX(3, 6)
+    J3DG_CX(1, 2) J3DG_CX(3, 4) J3DG_CX(5, 6)
+  }
+#undef J3DG_CX
+}
+
+template <int N, bool TOP = false, int W = 4>
 struct TracerT {
 #if J3DG_COLD_SMEM & 1
   // world ray: read only when an object's walk starts, kept in shared memory
@@ -307,6 +372,13 @@ struct TracerT {
 
   __device__ __forceinline__ void start_object(const DevInst* __restrict__ insts) {
     const DevInst& I = insts[inst];
+    if (I.width != (uint32_t)W) {  // a tree of another width: walk nothing (the host never launches that)
+      nodes = nullptr;
+      n_nodes = 0;
+      cur = J3DG_EMPTY_REF;
+      budget = 0;
+      return;
+    }
     float4 o = mat_vec(I.inv, wr(0), wr(1), wr(2), 1.f);
     float4 d = mat_vec(I.inv, wr(3), wr(4), wr(5), 0.f);
     r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, r.t_near, I.scale);
@@ -438,49 +510,32 @@ struct TracerT {
         return true;
       }
       ++visits;
-      const float4* nd = nodes + 8 * (size_t)cur;
+      const float4* nd = nodes + J3DG_NODE_F4(W) * (size_t)cur;
       // near / far planes by the ray's octant: the same values slab() selects,
       // picked by the load offsets instead of per-child selects
-      const uint32_t ox = r.neg & 1u, oy = (r.neg >> 1) & 1u, oz = (r.neg >> 2) & 1u;
-      const float4 nx4 = __ldg(nd + ox), fx4 = __ldg(nd + (ox ^ 1u));
-      const float4 ny4 = __ldg(nd + 2 + oy), fy4 = __ldg(nd + 2 + (oy ^ 1u));
-      const float4 nz4 = __ldg(nd + 4 + oz), fz4 = __ldg(nd + 4 + (oz ^ 1u));
-      const float4 chf = __ldg(nd + 6);
-      float tc[4];
-      uint32_t rc[4] = {__float_as_uint(chf.x), __float_as_uint(chf.y), __float_as_uint(chf.z),
-                        __float_as_uint(chf.w)};
-      const float pnx[4] = {nx4.x, nx4.y, nx4.z, nx4.w}, pfx[4] = {fx4.x, fx4.y, fx4.z, fx4.w};
-      const float pny[4] = {ny4.x, ny4.y, ny4.z, ny4.w}, pfy[4] = {fy4.x, fy4.y, fy4.z, fy4.w};
-      const float pnz[4] = {nz4.x, nz4.y, nz4.z, nz4.w}, pfz[4] = {fz4.x, fz4.y, fz4.z, fz4.w};
+      NodeLoad<W> L;
+      L.load(nd, r.neg);
+      float tc[W];
+      uint32_t rc[W];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
+      for (int c = 0; c < W; ++c) {
+        rc[c] = L.rc[c];
         // enter = max(tx, ty, tz, t_near), exit = min(tx, ty, tz, t_best)
-        const float a = max3f(__fmaf_rn(pnx[c], r.ix, r.nnx), __fmaf_rn(pny[c], r.iy, r.nny),
-                              fmaxf(__fmaf_rn(pnz[c], r.iz, r.nnz), r.t_near));
-        const float e = min3f(__fmaf_rn(pfx[c], r.ix, r.nfx), __fmaf_rn(pfy[c], r.iy, r.nfy),
-                              fminf(__fmaf_rn(pfz[c], r.iz, r.nfz), b.t));
+        const float a = max3f(__fmaf_rn(L.pnx[c], r.ix, r.nnx), __fmaf_rn(L.pny[c], r.iy, r.nny),
+                              fmaxf(__fmaf_rn(L.pnz[c], r.iz, r.nnz), r.t_near));
+        const float e = min3f(__fmaf_rn(L.pfx[c], r.ix, r.nfx), __fmaf_rn(L.pfy[c], r.iy, r.nfy),
+                              fminf(__fmaf_rn(L.pfz[c], r.iz, r.nfz), b.t));
         bool hit = (rc[c] != J3DG_EMPTY_REF) && (a <= e);
         tc[c] = hit ? a : __int_as_float(0x7f800000);
         if (!hit) rc[c] = J3DG_EMPTY_REF;
       }
-      // ascending (t, ref): 5 compare-exchanges
-#define J3DG_CX(i, j)  \
-  if (tc[j] < tc[i]) { \
-    float tt = tc[i];  \
-    tc[i] = tc[j];     \
-    tc[j] = tt;        \
-    uint32_t rr = rc[i]; \
-    rc[i] = rc[j];     \
-    rc[j] = rr;        \
-  }
-      J3DG_CX(0, 1) J3DG_CX(2, 3) J3DG_CX(0, 2) J3DG_CX(1, 3) J3DG_CX(1, 2)
-#undef J3DG_CX
-      if (sp + 3 > J3DG_STACK) {
+      sort_children<W>(tc, rc);
+      if (sp + (W - 1) > J3DG_STACK) {
         atomicOr(status, J3DG_DEV_STACK_OVERFLOW);
         return true;
       }
 #pragma unroll
-      for (int c = 3; c >= 1; --c)
+      for (int c = W - 1; c >= 1; --c)
         if (rc[c] != J3DG_EMPTY_REF) {
           stack[sp] = make_uint2(rc[c], __float_as_uint(tc[c]));
           ++sp;
@@ -494,7 +549,7 @@ struct TracerT {
         const bool leaf = (cur & J3DG_LEAF_BIT) != 0;
         const uint32_t first = (cur & 0x7fffffffu) >> 3;
         if (leaf ? first + (cur & 7u) + 1u <= nt : cur < n_nodes) {  // the checks the next step makes
-          const float4* line = leaf ? tris + 3 * (size_t)first : nodes + 8 * (size_t)cur;
+          const float4* line = leaf ? tris + 3 * (size_t)first : nodes + J3DG_NODE_F4(W) * (size_t)cur;
           asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
         }
       }
@@ -510,11 +565,11 @@ struct TracerT {
 // (returns false when the item needs no tracing and was handled) and
 // finish(); ITERS node/leaf steps run between refills.
 // N: the kernel's block size.
-template <int ITERS, int N, bool TOP, class Src>
+template <int ITERS, int N, bool TOP, int W, class Src>
 __device__ __forceinline__ void persistent_trace(Src& src, const DevInst* __restrict__ insts, uint32_t n_inst,
                                                  uint32_t* counter, uint32_t* status,
                                                  unsigned long long* counters) {
-  TracerT<N, TOP> T;
+  TracerT<N, TOP, W> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = src.count();

@@ -18,6 +18,13 @@
 // are refused at build time, so the device check never fires on valid BVHs.
 #define J3DG_STACK 96
 #define J3DG_MAX_DEPTH ((J3DG_STACK - 1) / 3)
+// Wide nodes of width W (2, 4 or 8 children): the child boxes as floats
+// [6][W] (planes lo.x, hi.x, lo.y, hi.y, lo.z, hi.z; child c of plane p at
+// p W + c), then the W child refs, padded to whole 64-byte lines: 64 B
+// (W = 2), 128 B (W = 4), 256 B (W = 8). A level pushes up to W - 1 stack
+// entries, so the deepest tree a width allows is J3DG_MAX_DEPTH_W(W).
+#define J3DG_NODE_F4(W) (((7 * (W)) + 15) / 16 * 4)
+#define J3DG_MAX_DEPTH_W(W) ((J3DG_STACK - 1) / ((W) - 1))
 
 struct j3dg_ctx {
   int device = 0;
@@ -56,6 +63,7 @@ struct j3dg_mesh {
   float min_bb[3] = {0, 0, 0}, max_bb[3] = {0, 0, 0};
   float scale = 0.f;  // max |coordinate| of the bbox corners
   uint32_t leaf_size = 4;
+  uint32_t width = 4;        // children per BVH node: 2, 4 or 8
   uint32_t build_flags = 0;  // j3dg_build_opts::flags
   uint32_t n_nodes = 0, max_depth = 0, root_ref = 0;
   float build_ms = 0.f;

@@ -896,6 +896,7 @@ extern "C" {
 int j3dg_learned_create(j3dg_ctx* c, const j3dg_mesh* mesh, const j3dg_learned_opts* opts, j3dg_learned** out) {
   if (!c || !mesh || !out) return J3DG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
+  if (mesh->width != 4) return j3dg::ctx_fail(c, J3DG_ERR_UNSUPPORTED, "learned: needs a 4-wide BVH");
   cudaSetDevice(c->device);
   j3dg_learned* l = new (std::nothrow) j3dg_learned();
   if (!l) return J3DG_ERR_OUT_OF_MEMORY;

@@ -15,7 +15,26 @@
 #include "device_common.cuh"
 #include "render.cuh"
 
+// This file is compiled once per BVH width (2, 4, 8): J3DG_W selects the
+// width its tracing kernels walk, and everything in it lives in namespace
+// j3dg::w<J3DG_W>; render_dispatch.cu calls the variant a frame's meshes
+// need (the width-independent launchers of the w4 build).
+#ifndef J3DG_W
+#define J3DG_W 4
+#endif
+#if J3DG_W == 2
+#define J3DG_WNS w2
+#elif J3DG_W == 4
+#define J3DG_WNS w4
+#elif J3DG_W == 8
+#define J3DG_WNS w8
+#else
+#error "J3DG_W must be 2, 4 or 8"
+#endif
+
 namespace j3dg {
+namespace J3DG_WNS {
+static const int kWidth = J3DG_W;
 
 // ------------------------------------------------------------ shading ----
 
@@ -687,7 +706,7 @@ __device__ __forceinline__ ShadowJob* shadow_jobs(const FrameParams& P) {
 // cast a shadow ray are queued for k_shadow.
 __global__ void __launch_bounds__(kResolveThreads) k_resolve(const FrameParams P) {
   if (P.rlist[1]) return;  // the list overflowed: k_frame traces the frame
-  TracerT<kResolveThreads> T;
+  TracerT<kResolveThreads, false, kWidth> T;
   const uint32_t rw = (uint32_t)(P.x1 - P.x0 + 1), rh = (uint32_t)(P.y1 - P.y0 + 1);
   const uint32_t i = blockIdx.x * kResolveThreads + threadIdx.x;
   bool queue = false;
@@ -746,14 +765,14 @@ template <bool TOP>
 __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_shadow(const FrameParams P) {
   if (P.rlist[1]) return;
   ShadowSrc src{&P, shadow_jobs(P), P.work[1], light_position(P)};
-  persistent_trace<kIters, kTraceThreads, TOP>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
+  persistent_trace<kIters, kTraceThreads, TOP, kWidth>(src, P.inst, P.n_inst, P.work + 2, P.status, P.counters);
 }
 
 template <bool kThroughput, bool TOP>
 __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
     k_frame(const FrameParams P) {
   if (P.raster && P.rlist[1] == 0u) return;  // the raster kernels made this frame
-  TracerT<kTraceThreads, TOP> T;
+  TracerT<kTraceThreads, TOP, kWidth> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
@@ -861,7 +880,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_rays(const DevInst* __restric
                                                         j3dg_hit* __restrict__ hits, uint32_t* counter,
                                                         uint32_t* status, unsigned long long* counters) {
   BatchSrc<ANY> src{rays, hits, n};
-  persistent_trace<kIters, kTraceThreads, TOP>(src, inst, n_inst, counter, status, counters);
+  persistent_trace<kIters, kTraceThreads, TOP, kWidth>(src, inst, n_inst, counter, status, counters);
 }
 
 // Many frames (canvases, scenes, cameras, resolutions of uneven size) in one
@@ -880,7 +899,7 @@ template <int TPB, bool kThroughput, bool TOP>
 __global__ void __launch_bounds__(TPB, (MinBlocks<TPB, kThroughput>::value))
     k_frame_batch(const FrameParams* __restrict__ params, const uint32_t* __restrict__ offsets, uint32_t n_frames,
                   uint32_t* work) {
-  TracerT<TPB, TOP> T;
+  TracerT<TPB, TOP, kWidth> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t total = offsets[n_frames];
@@ -1223,7 +1242,8 @@ static cudaError_t launch_batch_variant(const FrameParams* d_params, const uint3
 }
 
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t total_items, uint32_t* work, int block_threads, bool top, cudaStream_t st) {
+                                uint32_t total_items, uint32_t* work, int block_threads, bool top, int,
+                                cudaStream_t st) {
   if (n_frames == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
@@ -1285,7 +1305,7 @@ cudaError_t launch_frame_from_hits(const FrameParams& P, const j3dg_hit* hits, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, const j3dg_ray* rays, uint32_t n,
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, int, const j3dg_ray* rays, uint32_t n,
                         j3dg_hit* hits, bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters,
                         cudaStream_t st) {
   if (n == 0) return cudaSuccess;
@@ -1310,4 +1330,5 @@ cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, const j3
   return cudaGetLastError();
 }
 
+}  // namespace J3DG_WNS
 }  // namespace j3dg

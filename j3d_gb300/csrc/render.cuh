@@ -32,7 +32,8 @@ static const uint32_t kRasterEntryWords = 8;  // inst, slot, x0, y0, x1, y1, -, 
 struct FrameParams {
   const DevInst* inst;
   uint32_t n_inst;
-  uint32_t top;  // 1: the instance table carries a top level and the kernels walk it
+  uint32_t top;    // 1: the instance table carries a top level and the kernels walk it
+  uint32_t width;  // children per BVH node of the frame's meshes (2, 4, 8)
   uint32_t w, h;
   int x0, y0, x1, y1;
   float cs[16], cs_inv[16], pinv[16];
@@ -66,8 +67,10 @@ struct FrameParams {
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
 // all frames in one persistent launch; offsets = prefix sums of primary_items
 // total_items = offsets[n_frames] (the sum of primary_items of the frames)
+// (every frame's meshes have BVH width `width`)
 cudaError_t launch_render_batch(const FrameParams* d_params, const uint32_t* d_offsets, uint32_t n_frames,
-                                uint32_t total_items, uint32_t* work, int block_threads, bool top, cudaStream_t st);
+                                uint32_t total_items, uint32_t* work, int block_threads, bool top, int width,
+                                cudaStream_t st);
 uint32_t primary_items(const FrameParams& P);
 // mode: 0 plain, 1 edges, 2 wireframe, 3 one-bit
 cudaError_t launch_shade(const FrameParams& P, const j3dg_pixel* G, int mode, int fill_background, cudaStream_t st);
@@ -80,7 +83,7 @@ cudaError_t launch_frame_from_hits(const FrameParams& P, const j3dg_hit* hits, c
 cudaError_t launch_copy_u32(uint32_t* dst, const uint32_t* src, size_t n, cudaStream_t st);
 cudaError_t launch_clear_ids(j3dg_pixel* G, size_t n, cudaStream_t st);
 cudaError_t launch_init_pixels(j3dg_pixel* G, size_t n, cudaStream_t st);
-cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, const j3dg_ray* rays, uint32_t n,
+cudaError_t launch_rays(const DevInst* inst, uint32_t n_inst, bool top, int width, const j3dg_ray* rays, uint32_t n,
                         j3dg_hit* hits, bool any, uint32_t* counter, uint32_t* status, unsigned long long* counters,
                         cudaStream_t st);
 

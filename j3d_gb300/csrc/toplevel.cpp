@@ -3,13 +3,13 @@
 // qbvh_two_level_with_transformations (canvas.cpp:762) is built every frame
 // over all scene objects with their 4x4 transforms, and closest-hit and
 // shadow queries go through it (canvas.cpp:786, 854). Here the top level is
-// a small BVH4 over the objects' world-space boxes, built on the host when the
+// a small BVH over the objects' world-space boxes, built on the host when the
 // instance table is written (a few microseconds for hundreds of objects) and
 // uploaded with the table; the traversal kernels walk it with the world ray,
 // take an object's BVH with the object-space ray at a top-level leaf, and come
-// back. Node layout = the meshes' BVH4 nodes (8 float4: lo.x[4], hi.x[4],
-// lo.y[4], hi.y[4], lo.z[4], hi.z[4], refs[4], pad); a leaf holds one object:
-// ref = J3DG_LEAF_BIT | object << 3.
+// back. Node layout = the meshes' nodes of the same width W (J3DG_NODE_F4:
+// planes [6][W], refs [W]); a leaf holds one object: ref = J3DG_LEAF_BIT |
+// object << 3.
 //
 // Culling at the top level never changes a result: the boxes are padded
 // outward (relative 2^-20 of each box's magnitude plus outward rounding to
@@ -39,10 +39,11 @@ struct Box {
 struct Builder {
   const std::vector<Box>& box;
   std::vector<uint32_t> idx;
-  float* nodes;  // 32 floats per node
-  uint32_t cap, n_nodes = 0, depth = 0;
+  float* nodes;  // 4 J3DG_NODE_F4(W) floats per node
+  uint32_t W, cap, n_nodes = 0, depth = 0;
 
-  Builder(const std::vector<Box>& b, float* out, uint32_t node_cap) : box(b), nodes(out), cap(node_cap) {
+  Builder(const std::vector<Box>& b, uint32_t width, float* out, uint32_t node_cap)
+      : box(b), nodes(out), W(width), cap(node_cap) {
     idx.resize(b.size());
     std::iota(idx.begin(), idx.end(), 0u);
   }
@@ -85,42 +86,44 @@ struct Builder {
     return m;
   }
 
+  // splits [b, e) into up to `groups` ranges (a power of 2) by repeated
+  // median splits; g receives the range boundaries
+  void groups_of(uint32_t b, uint32_t e, uint32_t groups, std::vector<uint32_t>& g) {
+    if (groups == 1 || e - b < 2) {
+      g.push_back(b);
+      return;
+    }
+    const uint32_t m = split(b, e);
+    groups_of(b, m, groups / 2, g);
+    groups_of(m, e, groups / 2, g);
+  }
+
   // returns the ref of the subtree over idx[b, e)
   uint32_t build(uint32_t b, uint32_t e, uint32_t level) {
     if (e - b == 1) return J3DG_LEAF_BIT | (idx[b] << 3);
     const uint32_t node = n_nodes++;
     depth = std::max(depth, level + 1);
-    // up to four groups: halves, then halves of each half with more than one object
-    uint32_t g[5];
-    int ng = 0;
-    const uint32_t m = split(b, e);
-    const uint32_t parts[2][2] = {{b, m}, {m, e}};
-    for (const auto& p : parts) {
-      if (p[1] - p[0] >= 2) {
-        const uint32_t mm = split(p[0], p[1]);
-        g[ng++] = p[0];
-        g[ng++] = mm;
-      } else {
-        g[ng++] = p[0];
-      }
-    }
-    g[ng] = e;
-    float* N = nodes + 32 * (size_t)node;
-    for (int c = 0; c < 4; ++c) {
-      N[0 + c] = N[8 + c] = N[16 + c] = std::numeric_limits<float>::infinity();
-      N[4 + c] = N[12 + c] = N[20 + c] = -std::numeric_limits<float>::infinity();
-      uint32_t empty = J3DG_EMPTY_REF;
-      std::memcpy(N + 24 + c, &empty, 4);
-      N[28 + c] = 0.f;
+    std::vector<uint32_t> g;
+    groups_of(b, e, W, g);
+    g.push_back(e);
+    const int ng = (int)g.size() - 1;
+    const uint32_t F = 4 * J3DG_NODE_F4(W);
+    float* N = nodes + (size_t)F * node;
+    for (uint32_t k = 0; k < F; ++k) N[k] = 0.f;
+    for (uint32_t c = 0; c < W; ++c) {
+      N[0 * W + c] = N[2 * W + c] = N[4 * W + c] = std::numeric_limits<float>::infinity();
+      N[1 * W + c] = N[3 * W + c] = N[5 * W + c] = -std::numeric_limits<float>::infinity();
+      const uint32_t empty = J3DG_EMPTY_REF;
+      std::memcpy(N + 6 * W + c, &empty, 4);
     }
     for (int c = 0; c < ng; ++c) {
       const Box u = unite(box, idx.data() + g[c], idx.data() + g[c + 1]);
       const uint32_t ref = build(g[c], g[c + 1], level + 1);
       for (int a = 0; a < 3; ++a) {
-        N[8 * a + c] = (float)u.lo[a];      // already representable: boxes are rounded outward to float
-        N[8 * a + 4 + c] = (float)u.hi[a];
+        N[(2 * a) * W + c] = (float)u.lo[a];  // already representable: boxes are rounded outward to float
+        N[(2 * a + 1) * W + c] = (float)u.hi[a];
       }
-      std::memcpy(N + 24 + c, &ref, 4);
+      std::memcpy(N + 6 * W + c, &ref, 4);
     }
     return node;
   }
@@ -139,7 +142,7 @@ float up(double x) {
 }  // namespace
 
 TopLevel build_top_level(const float* const* mesh_lo, const float* const* mesh_hi, const float* const* cs, uint32_t n,
-                         float* nodes, uint32_t node_cap) {
+                         uint32_t W, float* nodes, uint32_t node_cap) {
   TopLevel t;
   t.n_inst = n;
   if (n == 0) return t;
@@ -170,8 +173,8 @@ TopLevel build_top_level(const float* const* mesh_lo, const float* const* mesh_h
   }
   t.pad_scale = up(scale);
   if (!std::isfinite(t.pad_scale)) return t;  // non-finite boxes: no top level (objects are walked in turn)
-  if (n > node_cap + 1 || n > (1u << 28)) return t;
-  Builder B(box, nodes, node_cap);
+  if (n > node_cap + 1 || n > (1u << 28) || (W != 2 && W != 4 && W != 8)) return t;
+  Builder B(box, W, nodes, node_cap);
   t.root = B.build(0, n, 0);
   t.n_nodes = B.n_nodes;
   t.depth = B.depth;

@@ -14,8 +14,10 @@ struct TopLevel {
   float pad_scale = 0.f;  // max |coordinate| of the padded object boxes
 };
 
-// nodes: room for node_cap BVH4 nodes (32 floats each); n objects need n - 1 at most.
+// A BVH of width W (2, 4, 8; the meshes' node layout, J3DG_NODE_F4) over the
+// n objects' padded world boxes. nodes: room for node_cap nodes; n objects
+// need n - 1 at most.
 TopLevel build_top_level(const float* const* mesh_lo, const float* const* mesh_hi, const float* const* cs, uint32_t n,
-                         float* nodes, uint32_t node_cap);
+                         uint32_t W, float* nodes, uint32_t node_cap);
 
 }  // namespace j3dg

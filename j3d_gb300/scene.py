@@ -114,15 +114,17 @@ class Mesh:
     """scene_object's mesh + qbvh (scene.h:10-25), resident on the device."""
 
     BUILDERS = {"ploc": 0, "lbvh": 1}
+    WIDTHS = {2: 0x2, 4: 0, 8: 0x4}  # J3DG_BUILD_WIDTH2 / (default) / J3DG_BUILD_WIDTH8
 
-    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2, build: str = "ploc"):
+    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2, build: str = "ploc", width: int = 4):
         """build: "ploc" (surface-area clustering, the default: fewer node
-        visits per ray) or "lbvh" (Morton splits, about half the build time)."""
+        visits per ray) or "lbvh" (Morton splits, about half the build time);
+        width: children per BVH node, 2, 4 (default) or 8."""
         self.ctx = ctx
         nv = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
         nt = int(triangles.shape[0]) if triangles.ndim > 1 else int(triangles.size // 3)
         h = C.c_void_p()
-        opts = BuildOpts(leaf_size, Mesh.BUILDERS[build])
+        opts = BuildOpts(leaf_size, Mesh.BUILDERS[build] | Mesh.WIDTHS[width])
         _check(ctx.h, lib().j3dg_mesh_build(ctx.h, vptr(vertices), nv, vptr(triangles), nt, C.byref(opts),
                                             C.byref(h)))
         self.h = h
@@ -257,12 +259,13 @@ class ScenePointCloud:
         self.db_id = db_id
 
 
-def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2, build: str = "ploc") -> Mesh:
+def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2, build: str = "ploc",
+                       width: int = 4) -> Mesh:
     """add_object's mesh built straight from device-resident geometry."""
     m = Mesh.__new__(Mesh)
     m.ctx = ctx
     h = C.c_void_p()
-    opts = BuildOpts(leaf_size, Mesh.BUILDERS[build])
+    opts = BuildOpts(leaf_size, Mesh.BUILDERS[build] | Mesh.WIDTHS[width])
     _check(ctx.h, lib().j3dg_mesh_build_geometry(ctx.h, geom.h, C.byref(opts), C.byref(h)))
     m.h = h
     ctx._own(m)

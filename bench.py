@@ -341,14 +341,14 @@ def run_own(args):
     wl = Wk.config1(N_CAMERAS, W_, H_)
     ctx = Context(local)
     t0 = time.perf_counter()
-    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build)
+    mesh = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build, args.width)
     build_wall = time.perf_counter() - t0
     info = mesh.info()
     # three more builds give the steady build time (their median: the level
     # loops synchronise with the host, so one build can catch host noise)
     build_samples = []
     for _ in range(3):
-        mesh2 = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build)
+        mesh2 = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, args.build, args.width)
         build_samples.append(mesh2.info().build_ms)
         mesh2.close()
     build_ms = float(np.median(build_samples))
@@ -513,7 +513,7 @@ def run_own(args):
                        bvh_build_ms=round(build_ms, 3), bvh_build_ms_samples=[round(b, 2) for b in build_samples],
                        bvh_first_build_wall_s=round(build_wall, 3),
                        bvh_nodes=info.n_nodes, bvh_depth=info.max_depth, leaf_size=args.leaf,
-                       bvh_builder=args.build,
+                       bvh_builder=args.build, bvh_width=args.width,
                        mesh_device_bytes=int(info.device_bytes),
                        bvh_build_mtris_per_s=round(28_090_000 / (build_ms / 1e3) / 1e6, 1),
                        # T (12 + 36) B read + T 24 B boxes + nodes x 128 B written, per build ms
@@ -522,8 +522,8 @@ def run_own(args):
                        gpu_tri_tests_per_ray=round(gtests / rays_per_step, 3)),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
-                     "traffic": FRAME_TRAFFIC[args.build][0] if args.leaf == 2 else None,
-                     "traffic_l2": FRAME_TRAFFIC[args.build][1] if args.leaf == 2 else None,
+                     "traffic": FRAME_TRAFFIC[args.build][0] if args.leaf == 2 and args.width == 4 else None,
+                     "traffic_l2": FRAME_TRAFFIC[args.build][1] if args.leaf == 2 and args.width == 4 else None,
                      "traffic_note": "bytes per k_frame launch (ncu, mean of the 32 cameras); the algorithmic "
                                      "bytes per launch are bytes_per_ray x rays_per_step / 32",
                      "kernel": "k_frame (primary + shadow + shading, one launch per frame)", "peak_kind": peak_kind,
@@ -571,8 +571,9 @@ def run_batch(args):
         weights[bucket_of(len(T))] += len(T)
     heavy = max(weights, key=weights.get)
     ctx.set_batch_block(tuner.table[heavy].block_threads)
+    width = tuner.table[heavy].width  # one width per batch: the heaviest bucket's
     t0 = time.perf_counter()
-    meshes = [Mesh(ctx, V, T, tuner.table[bucket_of(len(T))].leaf_size) for V, T in wl.meshes]
+    meshes = [Mesh(ctx, V, T, tuner.table[bucket_of(len(T))].leaf_size, "ploc", width) for V, T in wl.meshes]
     ctx.synchronize()
     build_s = time.perf_counter() - t0
     build_ms = sum(m.info().build_ms for m in meshes)
@@ -628,9 +629,10 @@ def run_batch(args):
                        "one_launch_mrays_s": round(rays / ms_batch / 1e3, 3),
                        "builds_ms_device": round(build_ms, 2), "builds_wall_s": round(build_s, 3),
                        "autotune_s": round(tune_s, 2),
-                       "autotune": {str(b): [c.leaf_size, c.block_threads, round(c.ms_per_frame, 4)]
+                       "autotune": {str(b): {"width": c.width, "leaf": c.leaf_size, "block": c.block_threads,
+                                             "ms_per_frame": round(c.ms_per_frame, 4)}
                                     for b, c in sorted(tuner.table.items())},
-                       "block_threads": tuner.table[heavy].block_threads}}
+                       "block_threads": tuner.table[heavy].block_threads, "bvh_width": width}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -969,6 +971,81 @@ def run_objects(args):
     return 0
 
 
+def run_config0(args):
+    """The small configuration: icosphere level 6 (81,920 triangles) at
+    1024x768, camera at distance 3, primary + shadow + plain shading; GPU
+    build and frame beside the CPU oracle's build and frame (all host
+    cores, persistent row pool), in one process (the CPU leg runs after the
+    GPU leg has finished)."""
+    import torch
+
+    import oracle.oracle as O
+    import oracle.workloads as OW
+    from j3d_gb300 import Canvas, Context, Matcap, Mesh, Scene, build as B, camera_for_vfov, settings
+    B.build()
+    O.build()
+    V, T, poses, w, h = OW.config0()
+    ctx = Context(0)
+    builds = []
+    for _ in range(4):
+        m = Mesh(ctx, V, T)
+        builds.append(m.info().build_ms)
+    sc = Scene()
+    sc.add_object(m)
+    sc.prepare_scene()
+    sc.unzoom()
+    sc.set_pose(poses[0])
+    cv = Canvas(ctx, w, h)
+    cv.set_camera(camera_for_vfov(60.0))
+    cv.set_background_color()
+    cv.update_settings(settings(shadow=True, edges=False))
+    mc = Matcap.make(ctx, 0)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        cv.render_frame(sc, mc)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        cv.render_frame(sc, mc)
+    e1.record(stream)
+    e1.synchronize()
+    gpu_ms = e0.elapsed_time(e1) / args.steps
+    hits = int((cv.get_pixels()["object_id"] != 0xFFFFFFFF).sum())
+    rays = w * h + hits
+    n_threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    om = O.Mesh(V, T, 4, n_threads)
+    cpu_build_s = time.perf_counter() - t0
+    mn, mx, diag = O.prepare_scene([(om.min_bb, om.max_bb)], [np.eye(4, dtype=np.float32).reshape(16)])
+    _, _, piv = O.unzoom(mn, mx, diag)
+    cam = O.camera_with_focal(OW.focal_for_vfov(60.0, 0.768))
+    Pi = O.invert_projection_matrix(O.make_projection_matrix(cam, w, h))
+    v = O.view(poses[0], O.invert_orthonormal(poses[0]), piv, diag, Pi, cam.near_clipping_plane)
+    st = O.settings(shadow=True, edges=False)
+    omc, cav = O.make_matcap(0)
+    bg = O.fill_background(w, h)
+    cpu_ms = []
+    for k in range(8):
+        pix = O.fresh_pixels(w, h)
+        im = np.zeros((h, w), np.uint32)
+        t0 = time.perf_counter()
+        O.render_frame(pix, im, bg, [(om, np.eye(4, dtype=np.float32).reshape(16), 1)], v, st, omc, cav,
+                       n_threads=n_threads)
+        if k >= 2:
+            cpu_ms.append((time.perf_counter() - t0) * 1e3)
+    same = bool(np.array_equal(pix.view(np.uint8), cv.get_pixels().view(np.uint8)))
+    line = {"workload": "config0", "metric": "Mrays/s & frame ms, icosphere L6 81,920 tris @1024x768, primary + shadow",
+            "gpu": {"frame_ms": round(gpu_ms, 4), "mrays_s": round(rays / gpu_ms / 1e3, 1),
+                    "build_ms_median_warm": round(float(np.median(builds[1:])), 3)},
+            "cpu_oracle": {"frame_ms": round(float(np.median(cpu_ms)), 2),
+                           "mrays_s": round(rays / float(np.median(cpu_ms)) / 1e3, 2),
+                           "build_s": round(cpu_build_s, 3), "cores": n_threads},
+            "rays_per_frame": rays, "gbuffer_identical": same}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_pointcloud(args):
     """Point-cloud splat after each headline frame: the 28.09M-triangle torus
     frame at 1920x1080 for each of the 32 cameras, then its 14.045M vertices
@@ -1049,11 +1126,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--leaf", type=int, default=2)
+    ap.add_argument("--width", type=int, default=4, choices=[2, 4, 8], help="BVH width of the headline mesh")
     ap.add_argument("--build", default="ploc", choices=["ploc", "lbvh"], help="BVH builder of the headline mesh")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-side", action="store_true", help="skip the short runs of the other configurations")
     ap.add_argument("--workload", default="torus",
-                    choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects"],
+                    choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects", "config0"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
                          "serve: config-4 request serving")
     ap.add_argument("--serve-rate", type=float, default=400.0)
@@ -1075,6 +1153,8 @@ def main():
         return run_pointcloud(args)
     if args.workload == "objects":
         return run_objects(args)
+    if args.workload == "config0":
+        return run_config0(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

@@ -1,11 +1,12 @@
 """Autotuner for the batched renderer: picks, per mesh-size bucket, the BVH
-leaf size and the block shape of the persistent launch by timing real frames.
+width, the leaf size and the block shape of the persistent launch by timing
+real frames.
 
-Search space: leaf size (max triangles per BVH4 leaf) 1, 2, 4, 8 and block
-shapes of 64, 128, 256 threads. The BVH width is fixed at 4: an 8-wide
-compressed layout was measured slower on this path (fewer node visits but
-more work per visit, in a kernel bound by issue rate rather than bandwidth).
-Results are kept per bucket of log2(triangle count) in a JSON cache.
+Search space: BVH width (children per node) 2, 4, 8; leaf size (max
+triangles per leaf) 1, 2, 4, 8; block shapes of 64, 128, 256 threads. A batch
+shares one width and one block shape (the kernels are specialised on both):
+the heaviest bucket's choice. Results are kept per bucket of log2(triangle
+count) in a JSON cache.
 """
 from __future__ import annotations
 
@@ -16,6 +17,7 @@ from pathlib import Path
 
 import numpy as np
 
+WIDTHS = (2, 4, 8)
 LEAF_SIZES = (1, 2, 4, 8)
 BLOCKS = (64, 128, 256)
 
@@ -26,6 +28,7 @@ class Choice:
     leaf_size: int
     block_threads: int
     ms_per_frame: float
+    width: int = 4
 
 
 def bucket_of(n_triangles: int) -> int:
@@ -49,8 +52,9 @@ class Autotuner:
     def lookup(self, n_triangles: int) -> Choice | None:
         return self.table.get(bucket_of(n_triangles))
 
-    def tune(self, vertices, triangles, poses, resolution=(512, 512), repeats: int = 3) -> Choice:
-        """Times frames of this mesh for every (leaf size, block shape) pair."""
+    def tune(self, vertices, triangles, poses, resolution=(512, 512), repeats: int = 3, widths=WIDTHS,
+             leaf_sizes=LEAF_SIZES, blocks=BLOCKS) -> Choice:
+        """Times frames of this mesh for every (width, leaf size, block shape)."""
         import torch
 
         from .scene import Canvas, Matcap, Mesh, Scene, camera_for_vfov, render_batch, settings
@@ -60,8 +64,12 @@ class Autotuner:
         mc = Matcap.make(self.ctx, 0)
         stream = torch.cuda.ExternalStream(self.ctx.stream())
         best = None
-        for leaf in LEAF_SIZES:
-            mesh = Mesh(self.ctx, vertices, triangles, leaf)
+        self.trials: list = []
+        for width, leaf in [(w, lf) for w in widths for lf in leaf_sizes]:
+            try:
+                mesh = Mesh(self.ctx, vertices, triangles, leaf, "ploc", width)
+            except Exception:  # noqa: BLE001  (a tree too deep for this width's stack is refused)
+                continue
             frames = []
             for p in poses:
                 sc = Scene()
@@ -73,7 +81,7 @@ class Autotuner:
                 cv.set_camera(camera_for_vfov(60.0))
                 cv.update_settings(settings(shadow=True, edges=False))
                 frames.append((cv, sc, mc))
-            for threads in BLOCKS:
+            for threads in blocks:
                 self.ctx.set_batch_block(threads)
                 render_batch(self.ctx, frames)  # warm-up
                 self.ctx.synchronize()
@@ -85,8 +93,9 @@ class Autotuner:
                 e1.record(stream)
                 e1.synchronize()
                 ms = e0.elapsed_time(e1) / (repeats * len(frames))
+                self.trials.append((width, leaf, threads, float(ms)))
                 if best is None or ms < best.ms_per_frame:
-                    best = Choice(b, leaf, threads, float(ms))
+                    best = Choice(b, leaf, threads, float(ms), width)
             for cv, _, _ in frames:
                 cv.close()
             mesh.close()

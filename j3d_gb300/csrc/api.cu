@@ -33,6 +33,9 @@ namespace {
 // ring of instance-table slots: host staging (pinned) -> device
 const uint32_t kInstSlots = 8;
 
+// bytes the device's default pool keeps reserved between calls (build scratch)
+const uint64_t kKeepReserved = 16ull << 30;
+
 // canvas scratch per pixel: raster keys, shadow jobs and tables during a
 // frame; the point-cloud splat's depth keys after it
 const size_t kQueueBytesPerPixel = 48, kQueueBytesFixed = 16384;
@@ -525,6 +528,17 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
     return J3DG_ERR_CUDA;
   }
   c->copy_stream = cst;
+  // the device's default stream-ordered pool (BVH build scratch, query
+  // buffers) keeps up to kKeepReserved bytes mapped between calls: a build
+  // then reuses the previous build's pages instead of mapping ~11 GB again
+  // (28M triangles) after every synchronisation released them
+  {
+    cudaMemPool_t dflt = nullptr;
+    uint64_t keep_bytes = kKeepReserved;
+    if (cudaDeviceGetDefaultMemPool(&dflt, device) == cudaSuccess)
+      cudaMemPoolSetAttribute(dflt, cudaMemPoolAttrReleaseThreshold, &keep_bytes);
+    cudaGetLastError();
+  }
   cudaMemPoolProps props;
   memset(&props, 0, sizeof(props));
   props.allocType = cudaMemAllocationTypePinned;

@@ -158,22 +158,52 @@ __global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, int 
   hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive scan helpers (three phases over chunks of 1024 elements)
-__global__ void k_scan_chunks(const uint32_t* in, uint32_t* out, uint32_t n,
-                              uint32_t* __restrict__ sums) {
-  __shared__ uint32_t s[1024];
-  uint32_t i = blockIdx.x * 1024 + threadIdx.x;
-  uint32_t v = i < n ? in[i] : 0;
-  s[threadIdx.x] = v;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    uint32_t t = threadIdx.x >= (uint32_t)o ? s[threadIdx.x - o] : 0;
-    __syncthreads();
-    s[threadIdx.x] += t;
-    __syncthreads();
+// exclusive scan helpers (three phases over chunks of 1024 elements):
+// k_scan_chunks scans each chunk (256 threads x 4 elements: a sequential
+// scan of the thread's uint4, a shuffle scan of the warp's totals, the
+// eight warp totals through shared memory) and writes the chunk total,
+// k_scan_sums scans the chunk totals, k_scan_add adds them back. in and out
+// are 16-byte aligned (device allocations); elements past n read as 0 and
+// are not written.
+__global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* in, uint32_t* out, uint32_t n,
+                                                     uint32_t* __restrict__ sums) {
+  __shared__ uint32_t wsum[8];
+  const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (base + 3 < n) {
+    v = *reinterpret_cast<const uint4*>(in + base);
+  } else {
+    if (base < n) v.x = in[base];
+    if (base + 1 < n) v.y = in[base + 1];
+    if (base + 2 < n) v.z = in[base + 2];
   }
-  if (i < n) out[i] = s[threadIdx.x] - v;
-  if (threadIdx.x == 1023) sums[blockIdx.x] = s[1023];
+  const uint32_t tot = v.x + v.y + v.z + v.w;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t inc = tot;  // inclusive scan of the thread totals within the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t woff = 0, all = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < 8; ++w) {
+    const uint32_t x = wsum[w];
+    woff += w < warp ? x : 0u;
+    all += x;
+  }
+  const uint32_t e = woff + inc - tot;  // exclusive prefix of this thread's first element
+  const uint4 o4 = make_uint4(e, e + v.x, e + v.x + v.y, e + v.x + v.y + v.z);
+  if (base + 3 < n) {
+    *reinterpret_cast<uint4*>(out + base) = o4;
+  } else {
+    if (base < n) out[base] = o4.x;
+    if (base + 1 < n) out[base + 1] = o4.y;
+    if (base + 2 < n) out[base + 2] = o4.z;
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = all;
 }
 
 __global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t n) {
@@ -202,9 +232,19 @@ __global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t n) {
   }
 }
 
-__global__ void k_scan_add(uint32_t* __restrict__ out, uint32_t n, const uint32_t* __restrict__ sums) {
-  uint32_t i = blockIdx.x * 1024 + threadIdx.x;
-  if (i < n) out[i] += sums[blockIdx.x];
+__global__ void __launch_bounds__(256) k_scan_add(uint32_t* __restrict__ out, uint32_t n,
+                                                  const uint32_t* __restrict__ sums) {
+  const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u, add = sums[blockIdx.x];
+  if (base + 3 < n) {
+    uint4 v = *reinterpret_cast<const uint4*>(out + base);
+    v.x += add;
+    v.y += add;
+    v.z += add;
+    v.w += add;
+    *reinterpret_cast<uint4*>(out + base) = v;
+  } else {
+    for (uint32_t k = base; k < n && k < base + 4u; ++k) out[k] += add;
+  }
 }
 
 __global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
@@ -1490,9 +1530,9 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   for (int pass = 0; pass < kRadixPasses; ++pass) {
     const int shift = 8 * pass;
     k_radix_hist<<<n_tiles, kSortThreads, 0, st>>>(k0, nt, shift, n_tiles, hist);
-    k_scan_chunks<<<scan_blocks, 1024, 0, st>>>(hist, hist, hist_n, sums);
+    k_scan_chunks<<<scan_blocks, 256, 0, st>>>(hist, hist, hist_n, sums);
     k_scan_sums<<<1, 1024, 0, st>>>(sums, scan_blocks);
-    k_scan_add<<<scan_blocks, 1024, 0, st>>>(hist, hist_n, sums);
+    k_scan_add<<<scan_blocks, 256, 0, st>>>(hist, hist_n, sums);
     k_radix_scatter<<<n_tiles, kSortThreads, 0, st>>>(k0, v0, k1, v1, nt, shift, n_tiles, hist, d_status);
     J3DG_CK(cudaGetLastError());
     std::swap(k0, k1);
@@ -1540,9 +1580,9 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     // exclusive scan of n words (n <= nt)
     const auto scan_u32 = [&](const uint32_t* in, uint32_t* out, uint32_t n) {
       const uint32_t sb = (n + 1023) / 1024;
-      k_scan_chunks<<<sb, 1024, 0, st>>>(in, out, n, pl_sums);
+      k_scan_chunks<<<sb, 256, 0, st>>>(in, out, n, pl_sums);
       k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
-      k_scan_add<<<sb, 1024, 0, st>>>(out, n, pl_sums);
+      k_scan_add<<<sb, 256, 0, st>>>(out, n, pl_sums);
     };
     top = J3DG_SAH_TOP > 0 && nt > J3DG_SAH_TOP;
     if (top) {
@@ -1641,12 +1681,12 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       const uint32_t blocks = (mcount + kPlocBlock - 1) / kPlocBlock, sb = (mcount + 1023) / 1024;
       k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, seg0, mcount, nn);
       k_ploc_flags<<<blocks, kPlocBlock, 0, st>>>(nn, mcount, create, survive);
-      k_scan_chunks<<<sb, 1024, 0, st>>>(create, cscan, mcount, pl_sums);
+      k_scan_chunks<<<sb, 256, 0, st>>>(create, cscan, mcount, pl_sums);
       k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
-      k_scan_add<<<sb, 1024, 0, st>>>(cscan, mcount, pl_sums);
-      k_scan_chunks<<<sb, 1024, 0, st>>>(survive, sscan, mcount, pl_sums);
+      k_scan_add<<<sb, 256, 0, st>>>(cscan, mcount, pl_sums);
+      k_scan_chunks<<<sb, 256, 0, st>>>(survive, sscan, mcount, pl_sums);
       k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
-      k_scan_add<<<sb, 1024, 0, st>>>(sscan, mcount, pl_sums);
+      k_scan_add<<<sb, 256, 0, st>>>(sscan, mcount, pl_sums);
       k_ploc_totals<<<1, 1, 0, st>>>(create, cscan, survive, sscan, mcount, tot);
       J3DG_CK(cudaGetLastError());
       J3DG_CK(cudaMemcpyAsync(htot, tot, sizeof(htot), cudaMemcpyDeviceToHost, st));

@@ -211,6 +211,20 @@ int j3dg_abi_version(void);
    device). The arrays are copied; the caller keeps them. */
 int j3dg_mesh_build(j3dg_ctx* ctx, const float* vertices, uint32_t n_vertices, const uint32_t* triangles,
                     uint32_t n_triangles, const j3dg_build_opts* opts, j3dg_mesh** out);
+/* No reference counterpart (add_object builds one mesh at a time): many
+   meshes built at once, up to max_concurrent (0: 8) at a time, each on its
+   own stream from its own host thread, so that one build's host round
+   trips overlap the others' device work. opts: one per mesh, or NULL for
+   the defaults. On failure every mesh of the call is destroyed and out[]
+   holds NULLs. The context stream's earlier work completes first. */
+typedef struct j3dg_mesh_source {
+  const float* vertices; /* n_vertices x 3, host or device */
+  uint32_t n_vertices;
+  uint32_t n_triangles;
+  const uint32_t* triangles; /* n_triangles x 3, host or device */
+} j3dg_mesh_source;
+int j3dg_mesh_build_many(j3dg_ctx* ctx, uint32_t n, const j3dg_mesh_source* sources, const j3dg_build_opts* opts,
+                         uint32_t max_concurrent, j3dg_mesh** out);
 int j3dg_mesh_destroy(j3dg_mesh* mesh);
 int j3dg_mesh_get_info(const j3dg_mesh* mesh, j3dg_mesh_info* info);
 /* scene_object::triangle_normals (scene.h:14): n_triangles x 3 floats out. */

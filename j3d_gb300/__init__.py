@@ -7,6 +7,6 @@ mirror of the reference's scene/canvas interface over that C-ABI.
 """
 from ._ffi import HIT_DTYPE, PIXEL_DTYPE, RAY_DTYPE, J3dgError, LIB_PATH, lib  # noqa: F401
 from ._ffi import PRIMARY_AUTO, PRIMARY_RASTER, PRIMARY_TRACE  # noqa: F401
-from .scene import (Batch, Canvas, Context, Geometry, Matcap, Mesh, PointCloud, mesh_from_geometry, Scene, SceneObject, camera_for_vfov, fill_background,  # noqa: F401
+from .scene import (Batch, Canvas, Context, Geometry, Matcap, Mesh, PointCloud, build_meshes, mesh_from_geometry, Scene, SceneObject, camera_for_vfov, fill_background,  # noqa: F401
                     find_all, find_closest, get_closest_vertex, get_world_position, invert_orthonormal, voxelize, invert_projection_matrix, make_default_camera, make_matcap,
                     make_projection_matrix, render_batch, settings)

@@ -69,6 +69,11 @@ class BuildOpts(C.Structure):
     _fields_ = [("leaf_size", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class MeshSource(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32),
+                ("triangles", C.c_void_p)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("min_bb", C.c_float * 3),
                 ("max_bb", C.c_float * 3), ("n_nodes", C.c_uint32), ("max_depth", C.c_uint32),
@@ -107,6 +112,7 @@ SIGNATURES = {
     "j3dg_ctx_set_counting": (_I, [_P, _I]),
     "j3dg_ctx_read_counters": (_I, [_P, C.POINTER(C.c_uint64), _I]),
     "j3dg_ctx_memory": (_I, [_P, C.POINTER(C.c_uint64)]),
+    "j3dg_mesh_build_many": (_I, [_P, _U, _P, _P, _U, _P]),
     "j3dg_ctx_set_top_level": (_I, [_P, _I]),
     "j3dg_mesh_build": (_I, [_P, _P, _U, _P, _U, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_mesh_destroy": (_I, [_P]),

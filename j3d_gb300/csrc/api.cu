@@ -11,6 +11,8 @@
 #include <new>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <thread>
 
 #include "../../include/j3dg.h"
 #include "device_common.cuh"
@@ -677,29 +679,29 @@ int j3dg_ctx_read_counters(j3dg_ctx* c, uint64_t out[2], int reset) {
 
 // ------------------------------------------------------------------ mesh
 
-// The BVH width from the build flags (J3DG_BUILD_WIDTH2 / 8, default 4);
-// the LBVH builder collapses to width 4 only.
-int set_width(j3dg_ctx* c, j3dg_mesh* m) {
-  const uint32_t f = m->build_flags;
-  if (f & ~(uint32_t)(J3DG_BUILD_LBVH | J3DG_BUILD_WIDTH2 | J3DG_BUILD_WIDTH8))
-    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: unknown build flags");
-  if ((f & J3DG_BUILD_WIDTH2) && (f & J3DG_BUILD_WIDTH8))
-    return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: two BVH widths requested");
-  m->width = (f & J3DG_BUILD_WIDTH2) ? 2u : ((f & J3DG_BUILD_WIDTH8) ? 8u : 4u);
-  if (m->width != 4 && (f & J3DG_BUILD_LBVH))
-    return fail(c, J3DG_ERR_UNSUPPORTED, "mesh_build: the LBVH builder makes 4-wide trees only");
-  return J3DG_OK;
-}
 
-int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, uint32_t nt,
-                    const j3dg_build_opts* opts, j3dg_mesh** out) {
-  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+namespace {
+
+// One mesh build on stream `st` with its own timing events (the body of
+// j3dg_mesh_build; j3dg_mesh_build_many runs several on their own streams).
+// The device status word is checked by the caller.
+int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, uint32_t nt,
+                  const j3dg_build_opts* opts, cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1, j3dg_mesh** out,
+                  std::string& msg) {
   *out = nullptr;
-  if (!V || !T || nv == 0 || nt == 0) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: empty mesh");
-  if (nt >= J3DG_MAX_TRIANGLES) return fail(c, J3DG_ERR_UNSUPPORTED, "mesh_build: more than 2^28 triangles");
+  if (!V || !T || nv == 0 || nt == 0) {
+    msg = "mesh_build: empty mesh";
+    return J3DG_ERR_INVALID_ARGUMENT;
+  }
+  if (nt >= J3DG_MAX_TRIANGLES) {
+    msg = "mesh_build: more than 2^28 triangles";
+    return J3DG_ERR_UNSUPPORTED;
+  }
   uint32_t leaf = opts && opts->leaf_size ? opts->leaf_size : 2u;
-  if (leaf < 1 || leaf > J3DG_MAX_LEAF) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "mesh_build: leaf_size must be 1..8");
-  cudaSetDevice(c->device);
+  if (leaf < 1 || leaf > J3DG_MAX_LEAF) {
+    msg = "mesh_build: leaf_size must be 1..8";
+    return J3DG_ERR_INVALID_ARGUMENT;
+  }
   j3dg_mesh* m = new (std::nothrow) j3dg_mesh();
   if (!m) return J3DG_ERR_OUT_OF_MEMORY;
   m->ctx = c;
@@ -708,40 +710,54 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   m->nt = nt;
   m->leaf_size = leaf;
   m->build_flags = opts ? opts->flags : 0u;
-  if (int rc = set_width(c, m)) {
-    delete m;
-    return rc;
+  {
+    const uint32_t f = m->build_flags;
+    if (f & ~(uint32_t)(J3DG_BUILD_LBVH | J3DG_BUILD_WIDTH2 | J3DG_BUILD_WIDTH8)) {
+      delete m;
+      msg = "mesh_build: unknown build flags";
+      return J3DG_ERR_INVALID_ARGUMENT;
+    }
+    if ((f & J3DG_BUILD_WIDTH2) && (f & J3DG_BUILD_WIDTH8)) {
+      delete m;
+      msg = "mesh_build: two BVH widths requested";
+      return J3DG_ERR_INVALID_ARGUMENT;
+    }
+    m->width = (f & J3DG_BUILD_WIDTH2) ? 2u : ((f & J3DG_BUILD_WIDTH8) ? 8u : 4u);
+    if (m->width != 4 && (f & J3DG_BUILD_LBVH)) {
+      delete m;
+      msg = "mesh_build: the LBVH builder makes 4-wide trees only";
+      return J3DG_ERR_UNSUPPORTED;
+    }
   }
-  CtxExtra& X = all(c)->ex;
   float* dV = nullptr;
   bool ownV = false;
   int rc = J3DG_OK;
-  std::string err;
   cudaError_t e = cudaMalloc(&m->d_index, sizeof(uint32_t) * 3 * (size_t)nt);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(m->d_index, T, sizeof(uint32_t) * 3 * (size_t)nt,
-                        is_device_ptr(T) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S(c));
+                        is_device_ptr(T) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     if (is_device_ptr(V)) {
       dV = const_cast<float*>(V);
     } else {
       ownV = true;
       e = cudaMalloc((void**)&dV, sizeof(float) * 3 * (size_t)nv);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(dV, V, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice, S(c));
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dV, V, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice, st);
     }
   }
-  if (e == cudaSuccess) e = cudaEventRecord(X.ev0, S(c));
+  if (e == cudaSuccess) e = cudaEventRecord(ev0, st);
   if (e != cudaSuccess) {
-    rc = cuda_fail(c, e, "mesh_build upload");
+    rc = e == cudaErrorMemoryAllocation ? J3DG_ERR_OUT_OF_MEMORY : J3DG_ERR_CUDA;
+    msg = std::string("mesh_build upload: ") + cudaGetErrorString(e);
   } else {
-    rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, S(c), c->d_status, err);
+    std::string err;
+    rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, st, c->d_status, err);
     if (rc == J3DG_OK) {
-      cudaEventRecord(X.ev1, S(c));
-      cudaEventSynchronize(X.ev1);
-      cudaEventElapsedTime(&m->build_ms, X.ev0, X.ev1);
-      rc = check_status(c);
+      cudaEventRecord(ev1, st);
+      cudaEventSynchronize(ev1);
+      cudaEventElapsedTime(&m->build_ms, ev0, ev1);
     } else {
-      fail(c, rc, "mesh_build: " + err);
+      msg = "mesh_build: " + err;
     }
   }
   if (ownV) cudaFree(dV);
@@ -752,6 +768,80 @@ int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T,
   }
   *out = m;
   return J3DG_OK;
+}
+
+}  // namespace
+
+int j3dg_mesh_build(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, uint32_t nt,
+                    const j3dg_build_opts* opts, j3dg_mesh** out) {
+  if (!c || !out) return J3DG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaSetDevice(c->device);
+  CtxExtra& X = all(c)->ex;
+  std::string msg;
+  j3dg_mesh* m = nullptr;
+  int rc = mesh_build_on(c, V, nv, T, nt, opts, S(c), X.ev0, X.ev1, &m, msg);
+  if (rc != J3DG_OK) return fail(c, rc, msg);
+  if ((rc = check_status(c)) != J3DG_OK) {
+    j3dg_mesh_destroy(m);
+    return rc;
+  }
+  *out = m;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_build_many(j3dg_ctx* c, uint32_t n, const j3dg_mesh_source* src, const j3dg_build_opts* opts,
+                         uint32_t max_concurrent, j3dg_mesh** out) {
+  if (!c || (n && (!src || !out))) return J3DG_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < n; ++i) out[i] = nullptr;
+  if (n == 0) return J3DG_OK;
+  cudaSetDevice(c->device);
+  // the work queued on the context stream before this call comes first
+  CK(c, cudaStreamSynchronize(S(c)), "mesh_build_many");
+  const uint32_t K = std::max(1u, std::min(n, max_concurrent ? max_concurrent : 8u));
+  std::vector<int> rcs(n, J3DG_OK);
+  std::vector<std::string> msgs(n);
+  std::atomic<uint32_t> next{0};
+  std::vector<std::thread> workers;
+  for (uint32_t k = 0; k < K; ++k)
+    workers.emplace_back([&, k] {
+      cudaSetDevice(c->device);
+      cudaStream_t st = nullptr;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      const bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+                      cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+      for (uint32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+        const j3dg_build_opts* o = opts ? opts + i : nullptr;
+        if (!ok) {
+          rcs[i] = J3DG_ERR_CUDA;
+          msgs[i] = "mesh_build_many: could not create a build stream";
+          continue;
+        }
+        rcs[i] = mesh_build_on(c, src[i].vertices, src[i].n_vertices, src[i].triangles, src[i].n_triangles, o, st,
+                               e0, e1, &out[i], msgs[i]);
+      }
+      if (st) cudaStreamSynchronize(st);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (st) cudaStreamDestroy(st);
+    });
+  for (auto& t : workers) t.join();
+  int rc = J3DG_OK;
+  std::string msg;
+  for (uint32_t i = 0; i < n && rc == J3DG_OK; ++i)
+    if (rcs[i] != J3DG_OK) {
+      rc = rcs[i];
+      msg = "mesh " + std::to_string(i) + ": " + msgs[i];
+    }
+  if (rc == J3DG_OK) rc = check_status(c);
+  else fail(c, rc, msg);
+  if (rc != J3DG_OK)
+    for (uint32_t i = 0; i < n; ++i)
+      if (out[i]) {
+        j3dg_mesh_destroy(out[i]);
+        out[i] = nullptr;
+      }
+  return rc;
 }
 
 int j3dg_mesh_destroy(j3dg_mesh* m) {

@@ -995,7 +995,11 @@ static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode*
 #define J3DG_SAH_TOP 64u
 #endif
 static const int kTopBins = 16;
-static const int kTopVals = 13;  // count, centroid lo/hi xyz, box lo/hi xyz (ordered-float encoded)
+// per bin: count, box lo / hi xyz (ordered-float encoded). The children's
+// centroid ranges (the next level's bin ranges) are their boxes: every
+// centroid lies in its triangle's box, and with triangles small against a
+// task the two ranges differ by about one triangle
+static const int kTopVals = 7;
 static const uint32_t kNoTask = 0xffffffffu;
 static const uint32_t kPendingRef = 0xfffffffeu;  // child slot filled by a segment root later
 
@@ -1095,23 +1099,22 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
     // task's global bins
     const uint32_t vm = __ballot_sync(0xffffffffu, valid);
     if (valid) {
-      const uint32_t v[12] = {f2o(c.x),  f2o(c.y),  f2o(c.z),  f2o(c.x),  f2o(c.y),  f2o(c.z),
-                              f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+      const uint32_t v[6] = {f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
       const int bins3[3] = {bx, by, bz};
       uint32_t* dst = st != kNoTask ? sb : bins + (size_t)t * 3 * kTopBins * kTopVals;
 #pragma unroll
       for (int ax = 0; ax < 3; ++ax) {
         const uint32_t g = __match_any_sync(vm, t * (uint32_t)kTopBins + (uint32_t)bins3[ax]);
         const uint32_t n_g = (uint32_t)__popc(g);
-        uint32_t r[12];
+        uint32_t r[6];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) r[k] = ((k % 6) < 3) ? __reduce_min_sync(g, v[k]) : __reduce_max_sync(g, v[k]);
+        for (int k = 0; k < 6; ++k) r[k] = k < 3 ? __reduce_min_sync(g, v[k]) : __reduce_max_sync(g, v[k]);
         if (lane == (uint32_t)(__ffs(g) - 1)) {
           uint32_t* b = dst + (ax * kTopBins + bins3[ax]) * kTopVals;
           atomicAdd(b, n_g);
 #pragma unroll
-          for (int k = 0; k < 12; ++k) {
-            if ((k % 6) < 3)
+          for (int k = 0; k < 6; ++k) {
+            if (k < 3)
               atomicMin(b + 1 + k, r[k]);
             else
               atomicMax(b + 1 + k, r[k]);
@@ -1158,15 +1161,14 @@ __global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict
     const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
     const int bins3[3] = {top_bin(c.x, T.clo.x, T.chi.x), top_bin(c.y, T.clo.y, T.chi.y),
                           top_bin(c.z, T.clo.z, T.chi.z)};
-    const uint32_t v[12] = {f2o(c.x),  f2o(c.y),  f2o(c.z),  f2o(c.x),  f2o(c.y),  f2o(c.z),
-                            f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
+    const uint32_t v[6] = {f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
       uint32_t* b = my + (ax * kTopBins + bins3[ax]) * kTopVals;
       atomicAdd(b, 1u);
 #pragma unroll
-      for (int k = 0; k < 12; ++k) {
-        if ((k % 6) < 3)
+      for (int k = 0; k < 6; ++k) {
+        if (k < 3)
           atomicMin(b + 1 + k, v[k]);
         else
           atomicMax(b + 1 + k, v[k]);
@@ -1204,8 +1206,8 @@ __global__ void k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks,
       const uint32_t* V = A + b * kTopVals;
       if (V[0]) {
         for (int k = 0; k < 3; ++k) {
-          l[k] = fminf(l[k], o2f(V[7 + k]));
-          h[k] = fmaxf(h[k], o2f(V[10 + k]));
+          l[k] = fminf(l[k], o2f(V[1 + k]));
+          h[k] = fmaxf(h[k], o2f(V[4 + k]));
         }
         cnt += V[0];
       }
@@ -1223,8 +1225,8 @@ __global__ void k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks,
       const uint32_t* V = A + b * kTopVals;
       if (V[0]) {
         for (int k = 0; k < 3; ++k) {
-          L[k] = fminf(L[k], o2f(V[7 + k]));
-          H[k] = fmaxf(H[k], o2f(V[10 + k]));
+          L[k] = fminf(L[k], o2f(V[1 + k]));
+          H[k] = fmaxf(H[k], o2f(V[4 + k]));
         }
         lc += V[0];
       }
@@ -1246,7 +1248,7 @@ __global__ void k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks,
   S.pad = 0;
   S.lclo = S.rclo = T.clo;
   S.lchi = S.rchi = T.chi;
-  if (ba < 3) {  // exact centroid bounds of both sides from the split axis's bins
+  if (ba < 3) {  // both sides' boxes from the split axis's bins: their centroid ranges
     const uint32_t* A = B + ba * kTopBins * kTopVals;
     float l0[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h0[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     float l1[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h1[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};

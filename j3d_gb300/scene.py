@@ -259,6 +259,40 @@ class ScenePointCloud:
         self.db_id = db_id
 
 
+def build_meshes(ctx: Context, meshes, leaf_sizes=None, width: int = 4, build: str = "ploc",
+                 max_concurrent: int = 8) -> list:
+    """Many meshes built at once (j3dg_mesh_build_many): [(vertices,
+    triangles)] -> [Mesh], up to max_concurrent builds in flight on their
+    own streams. leaf_sizes: one per mesh, or None for 2."""
+    n = len(meshes)
+    srcs = (_ffi.MeshSource * max(1, n))()
+    keep = []
+    for i, (V, T) in enumerate(meshes):
+        V = np.ascontiguousarray(V, np.float32)
+        T = np.ascontiguousarray(T, np.uint32)
+        keep += [V, T]
+        srcs[i].vertices = V.ctypes.data
+        srcs[i].n_vertices = int(V.size // 3)
+        srcs[i].triangles = T.ctypes.data
+        srcs[i].n_triangles = int(T.size // 3)
+    opts = (BuildOpts * max(1, n))()
+    for i in range(n):
+        opts[i] = BuildOpts(int(leaf_sizes[i]) if leaf_sizes is not None else 2,
+                            Mesh.BUILDERS[build] | Mesh.WIDTHS[width])
+    hs = (C.c_void_p * max(1, n))()
+    _check(ctx.h, lib().j3dg_mesh_build_many(ctx.h, n, C.cast(srcs, C.c_void_p), C.cast(opts, C.c_void_p),
+                                             max_concurrent, C.cast(hs, C.c_void_p)))
+    out = []
+    for i in range(n):
+        m = Mesh.__new__(Mesh)
+        m.ctx = ctx
+        m.h = C.c_void_p(hs[i])
+        ctx._own(m)
+        out.append(m)
+    del keep
+    return out
+
+
 def mesh_from_geometry(ctx: Context, geom: Geometry, leaf_size: int = 2, build: str = "ploc",
                        width: int = 4) -> Mesh:
     """add_object's mesh built straight from device-resident geometry."""

@@ -206,29 +206,49 @@ __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* in, uint32_
   if (threadIdx.x == 0) sums[blockIdx.x] = all;
 }
 
-__global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t n) {
-  // single block, sequential over per-thread strips
-  __shared__ uint32_t part[1024];
-  uint32_t per = (n + 1023) / 1024;
-  uint32_t b = threadIdx.x * per, e = min(n, b + per);
-  uint32_t acc = 0;
-  for (uint32_t i = b; i < e; ++i) acc += sums[i];
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (int t = 0; t < 1024; ++t) {
-      uint32_t x = part[t];
-      part[t] = run;
+__global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ sums_a, uint32_t* __restrict__ sums_b,
+                                                    uint32_t n, uint32_t* __restrict__ totals) {
+  // single block of 1024 threads, over one array of chunk totals (sums_b
+  // null) or two: each thread sums a strip of consecutive chunk totals, the
+  // strip sums are scanned by warp shuffles (within each warp, then the 32
+  // warp totals by warp 0), and each thread rewrites its strip as exclusive
+  // prefixes; totals (if not null) receives each array's grand total
+  __shared__ uint32_t wtot[32];
+  const uint32_t per = (n + 1023) / 1024;
+  const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (int q = 0; q < 2; ++q) {
+    uint32_t* sums = q ? sums_b : sums_a;
+    if (!sums) break;  // uniform over the block
+    uint32_t acc = 0;
+    for (uint32_t i = b; i < e; ++i) acc += sums[i];
+    uint32_t inc = acc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (uint32_t)o) inc += y;
+    }
+    if (lane == 31) wtot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t x = wtot[lane];
+      uint32_t xi = x;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+        if (lane >= (uint32_t)o) xi += y;
+      }
+      wtot[lane] = xi - x;
+      if (lane == 31 && totals) totals[q] = xi;
+    }
+    __syncthreads();
+    uint32_t run = wtot[warp] + inc - acc;
+    for (uint32_t i = b; i < e; ++i) {
+      const uint32_t x = sums[i];
+      sums[i] = run;
       run += x;
     }
-  }
-  __syncthreads();
-  acc = part[threadIdx.x];
-  for (uint32_t i = b; i < e; ++i) {
-    uint32_t x = sums[i];
-    sums[i] = acc;
-    acc += x;
+    __syncthreads();  // wtot is reused by the second array
   }
 }
 
@@ -249,12 +269,18 @@ __global__ void __launch_bounds__(256) k_scan_add(uint32_t* __restrict__ out, ui
 
 __global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                 uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n, int shift,
-                                uint32_t num_tiles, const uint32_t* __restrict__ offsets, uint32_t* status) {
+                                uint32_t num_tiles, const uint32_t* __restrict__ offsets,
+                                const uint32_t* __restrict__ chunk_offsets, uint32_t* status) {
   __shared__ uint32_t base[256];
   __shared__ uint32_t wc[kSortThreads / 32][257];
   __shared__ uint32_t total[256];
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  base[tid] = offsets[(size_t)tid * num_tiles + blockIdx.x];
+  {
+    // offsets: the digit histogram's scan within chunks of 1024 entries;
+    // chunk_offsets: the scanned chunk totals
+    const size_t h = (size_t)tid * num_tiles + blockIdx.x;
+    base[tid] = offsets[h] + chunk_offsets[h >> 10];
+  }
   size_t tile = (size_t)blockIdx.x * kSortTile;
   for (int j = 0; j < kSortItems; ++j) {
     for (int w = 0; w < kSortThreads / 32; ++w) wc[w][tid] = 0;
@@ -551,27 +577,78 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict
   nn[i] = bj;
 }
 
-__global__ void k_ploc_flags(const uint32_t* __restrict__ nn, uint32_t m, uint32_t* __restrict__ create,
-                             uint32_t* __restrict__ survive) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  const uint32_t j = nn[i];
-  const bool mutual = j < m && nn[j] == i;
-  create[i] = (mutual && i < j) ? 1u : 0u;
-  survive[i] = (!mutual || i < j) ? 1u : 0u;
-}
-
-// totals of the two exclusive scans: [creates, survivors]
-__global__ void k_ploc_totals(const uint32_t* create, const uint32_t* cscan, const uint32_t* survive,
-                              const uint32_t* sscan, uint32_t m, uint32_t* out) {
-  out[0] = cscan[m - 1] + create[m - 1];
-  out[1] = sscan[m - 1] + survive[m - 1];
+// a PLOC round's two compactions in one pass: position i creates a node if it
+// and its nearest neighbour j are mutual with i < j, and survives (keeps a
+// list slot) unless it is the j > i side of a mutual pair. Each chunk of 1024
+// positions (256 threads x 4) writes the exclusive scans of both flags
+// within the chunk (cps, sps) and its two totals (csum, ssum; scanned by
+// k_scan_sums, whose grand totals are the round's creates and survivors).
+__global__ void __launch_bounds__(256) k_ploc_flag_scan(const uint32_t* __restrict__ nn, uint32_t m,
+                                                        uint32_t* __restrict__ cps, uint32_t* __restrict__ sps,
+                                                        uint32_t* __restrict__ csum, uint32_t* __restrict__ ssum) {
+  __shared__ uint32_t wsum[2][8];
+  const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
+  uint32_t c[4] = {0u, 0u, 0u, 0u}, v[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t i = base + k;
+    if (i < m) {
+      const uint32_t j = nn[i];
+      const bool mutual = j < m && nn[j] == i;
+      c[k] = (mutual && i < j) ? 1u : 0u;
+      v[k] = (!mutual || i < j) ? 1u : 0u;
+    }
+  }
+  const uint32_t ct = c[0] + c[1] + c[2] + c[3], vt = v[0] + v[1] + v[2] + v[3];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t ci = ct, vi = vt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t yc = __shfl_up_sync(0xffffffffu, ci, o);
+    const uint32_t yv = __shfl_up_sync(0xffffffffu, vi, o);
+    if (lane >= (uint32_t)o) {
+      ci += yc;
+      vi += yv;
+    }
+  }
+  if (lane == 31) {
+    wsum[0][warp] = ci;
+    wsum[1][warp] = vi;
+  }
+  __syncthreads();
+  uint32_t co = 0, vo = 0, call = 0, vall = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < 8; ++w) {
+    const uint32_t xc = wsum[0][w], xv = wsum[1][w];
+    co += w < warp ? xc : 0u;
+    vo += w < warp ? xv : 0u;
+    call += xc;
+    vall += xv;
+  }
+  const uint32_t ec = co + ci - ct, ev = vo + vi - vt;
+  const uint4 oc = make_uint4(ec, ec + c[0], ec + c[0] + c[1], ec + c[0] + c[1] + c[2]);
+  const uint4 ov = make_uint4(ev, ev + v[0], ev + v[0] + v[1], ev + v[0] + v[1] + v[2]);
+  if (base + 3 < m) {
+    *reinterpret_cast<uint4*>(cps + base) = oc;
+    *reinterpret_cast<uint4*>(sps + base) = ov;
+  } else {
+    const uint32_t a4[4] = {oc.x, oc.y, oc.z, oc.w}, b4[4] = {ov.x, ov.y, ov.z, ov.w};
+    for (uint32_t k = 0; k < 4 && base + k < m; ++k) {
+      cps[base + k] = a4[k];
+      sps[base + k] = b4[k];
+    }
+  }
+  if (threadIdx.x == 0) {
+    csum[blockIdx.x] = call;
+    ssum[blockIdx.x] = vall;
+  }
 }
 
 __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
                              const float4* __restrict__ hi, const uint32_t* __restrict__ seg,
-                             const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cscan,
-                             const uint32_t* __restrict__ sscan, uint32_t m, uint32_t node_base,
+                             const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cps,
+                             const uint32_t* __restrict__ sps, const uint32_t* __restrict__ csum,
+                             const uint32_t* __restrict__ ssum, uint32_t m, uint32_t node_base,
                              uint32_t* __restrict__ C2, float4* __restrict__ lo2, float4* __restrict__ hi2,
                              uint32_t* __restrict__ seg2, uint2* __restrict__ child, BinNode* __restrict__ box,
                              uint32_t* __restrict__ count) {
@@ -580,7 +657,7 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
   const uint32_t j = nn[i];
   const bool mutual = j < m && nn[j] == i;
   if (mutual && i > j) return;  // merged into the node made at j
-  const uint32_t pos = sscan[i];
+  const uint32_t pos = sps[i] + ssum[i >> 10];  // survivors before i
   seg2[pos] = seg[i];
   if (!mutual) {
     C2[pos] = C[i];
@@ -588,7 +665,7 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
     hi2[pos] = hi[i];
     return;
   }
-  const uint32_t p = node_base + cscan[i];
+  const uint32_t p = node_base + cps[i] + csum[i >> 10];  // nodes made before i's
   const uint32_t a = C[i], b = C[j];
   const float4 l = make_float4(fminf(lo[i].x, lo[j].x), fminf(lo[i].y, lo[j].y), fminf(lo[i].z, lo[j].z), 0.f);
   const float4 h = make_float4(fmaxf(hi[i].x, hi[j].x), fmaxf(hi[i].y, hi[j].y), fmaxf(hi[i].z, hi[j].z), 0.f);
@@ -978,9 +1055,12 @@ static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode*
 // 2007, "On fast Construction of SAH-based Bounding Volume Hierarchies"):
 // per level, every task (a range of the triangle order `ord`) bins its
 // triangles' centroids into kTopBins bins per axis (per-block bins in shared
-// memory, then merged into the task's bins), one thread per task sweeps the
-// bins for the split of least A_L N_L + A_R N_R, and a stable partition
-// (flags, one exclusive scan) reorders the range. A stable partition of the
+// memory, then merged into the task's bins; tasks of at most kTopWarpTask
+// triangles are binned by one warp each), one warp per task finds the split
+// of least A_L N_L + A_R N_R from prefix and suffix unions of the bins
+// (shuffles, lanes = bins), and a stable partition
+// (flags from the bin codes that binning stored per position, one exclusive
+// scan) reorders the range. A stable partition of the
 // Morton-sorted order keeps every range in Morton order, so each range of at
 // most J3DG_SAH_TOP triangles (a segment) is then clustered by PLOC on its
 // own (neighbours searched within the segment only), and the segment roots
@@ -995,6 +1075,7 @@ static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode*
 #define J3DG_SAH_TOP 64u
 #endif
 static const int kTopBins = 16;
+static_assert(kTopBins <= 16, "bin codes keep 4 bits per axis");
 // per bin: count, box lo / hi xyz (ordered-float encoded). The children's
 // centroid ranges (the next level's bin ranges) are their boxes: every
 // centroid lies in its triangle's box, and with triangles small against a
@@ -1043,24 +1124,29 @@ __device__ __forceinline__ int top_bin(float c, float lo, float hi) {
   return b < 0 ? 0 : (b >= kTopBins ? kTopBins - 1 : b);
 }
 
-__global__ void k_top_bins_init(uint32_t* __restrict__ bins, uint32_t n_words) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_words) return;
-  const uint32_t v = i % kTopVals;
-  bins[i] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);  // lo fields: max code, hi fields: 0
-}
-
 static const int kTopChunk = 2048;
 // Tasks up to this size are binned by one warp each (k_top_bin_warp): at
 // that depth 32 neighbouring triangles span many bins, so grouping lanes by
 // bin (match + reductions per group) serialises; plain shared atomics do not.
 static const uint32_t kTopWarpTask = 2048;
 
+// global bins of the tasks larger than kTopWarpTask (k_top_bin's); the
+// smaller tasks keep their bins in shared memory
+__global__ void k_top_bins_init(uint32_t* __restrict__ bins, uint32_t n_words, const TopTask* __restrict__ tasks) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_words) return;
+  const TopTask& T = tasks[i / (3 * kTopBins * kTopVals)];
+  if (T.end - T.begin <= kTopWarpTask) return;
+  const uint32_t v = i % kTopVals;
+  bins[i] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);  // lo fields: max code, hi fields: 0
+}
+
+
 // bins of every active task: [task][axis][bin][kTopVals]
 __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
                                                  const float4* __restrict__ bhi, const uint32_t* __restrict__ task_of,
                                                  const TopTask* __restrict__ tasks, uint32_t n_tasks, uint32_t n,
-                                                 uint32_t* __restrict__ bins) {
+                                                 uint32_t* __restrict__ bins, uint16_t* __restrict__ code) {
   __shared__ uint32_t sb[3 * kTopBins * kTopVals];
   __shared__ uint32_t s_task;
   const uint32_t c0 = blockIdx.x * kTopChunk, c1 = min(n, c0 + kTopChunk);
@@ -1092,6 +1178,7 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
       bx = top_bin(c.x, T.clo.x, T.chi.x);
       by = top_bin(c.y, T.clo.y, T.chi.y);
       bz = top_bin(c.z, T.clo.z, T.chi.z);
+      code[p] = (uint16_t)(bx | (by << 4) | (bz << 8));
     }
     // neighbouring triangles (Morton order) mostly share a task and bins:
     // lanes of one (task, bin) reduce in registers and one lane updates the
@@ -1138,11 +1225,154 @@ __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ or
   }
 }
 
+__device__ __forceinline__ float box_half_area(float lx, float ly, float lz, float hx, float hy, float hz) {
+  const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// One warp: the split of least SAH cost A_L N_L + A_R N_R over the task's
+// bins B ([axis][bin][kTopVals], shared or global memory); writes the split,
+// the node's box and its triangle count. Lanes b and b + 16 hold bin b of
+// the axis in hand; prefix and suffix unions of the bins come from shuffles
+// within the 16 lanes. Among equal costs the lowest (axis, bin) wins, the
+// split a sweep over the axes and bins in order with a strict comparison
+// takes. Bins with no triangle carry no box (their encoded fields would
+// decode to NaN).
+__device__ void warp_top_split(const uint32_t* B, const TopTask& T, TopSplit* __restrict__ split,
+                               BinNode* __restrict__ box, uint32_t* __restrict__ count) {
+  const uint32_t lane = threadIdx.x & 31u, b = lane & 15u;
+  const uint32_t n = T.end - T.begin;
+  float best = FLT_MAX;
+  uint32_t best_idx = 0xffffffffu, best_lc = 0;
+  float bl[3], bh[3], rl_best[3], rh_best[3];
+  float nlo[3], nhi[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) bl[k] = bh[k] = rl_best[k] = rh_best[k] = nlo[k] = nhi[k] = 0.f;
+  for (int ax = 0; ax < 3; ++ax) {
+    const uint32_t* V = B + (ax * kTopBins + b) * kTopVals;
+    const uint32_t c = V[0];
+    float pl[3], ph[3], sl[3], sh[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      pl[k] = sl[k] = c ? o2f(V[1 + k]) : FLT_MAX;
+      ph[k] = sh[k] = c ? o2f(V[4 + k]) : -FLT_MAX;
+    }
+    uint32_t pc = c, sc = c;
+#pragma unroll
+    for (int o = 1; o < kTopBins; o <<= 1) {  // inclusive prefix (bins 0..b) and suffix (bins b..15)
+      const uint32_t yp = __shfl_up_sync(0xffffffffu, pc, o, kTopBins);
+      const uint32_t ys = __shfl_down_sync(0xffffffffu, sc, o, kTopBins);
+      float ypl[3], yph[3], ysl[3], ysh[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ypl[k] = __shfl_up_sync(0xffffffffu, pl[k], o, kTopBins);
+        yph[k] = __shfl_up_sync(0xffffffffu, ph[k], o, kTopBins);
+        ysl[k] = __shfl_down_sync(0xffffffffu, sl[k], o, kTopBins);
+        ysh[k] = __shfl_down_sync(0xffffffffu, sh[k], o, kTopBins);
+      }
+      if (b >= (uint32_t)o) {
+        pc += yp;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          pl[k] = fminf(pl[k], ypl[k]);
+          ph[k] = fmaxf(ph[k], yph[k]);
+        }
+      }
+      if (b + (uint32_t)o < (uint32_t)kTopBins) {
+        sc += ys;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          sl[k] = fminf(sl[k], ysl[k]);
+          sh[k] = fmaxf(sh[k], ysh[k]);
+        }
+      }
+    }
+    // the right side of a split after bin b: the suffix from bin b + 1
+    const uint32_t rc = __shfl_down_sync(0xffffffffu, sc, 1, kTopBins);
+    float rl[3], rh[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      rl[k] = __shfl_down_sync(0xffffffffu, sl[k], 1, kTopBins);
+      rh[k] = __shfl_down_sync(0xffffffffu, sh[k], 1, kTopBins);
+    }
+    if (ax == 0) {  // the node's box: the union of all bins of one axis
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        nlo[k] = __shfl_sync(0xffffffffu, sl[k], 0, kTopBins);
+        nhi[k] = __shfl_sync(0xffffffffu, sh[k], 0, kTopBins);
+      }
+    }
+    if (b + 1 < (uint32_t)kTopBins && pc != 0 && rc != 0) {
+      const float cost = box_half_area(pl[0], pl[1], pl[2], ph[0], ph[1], ph[2]) * (float)pc +
+                         box_half_area(rl[0], rl[1], rl[2], rh[0], rh[1], rh[2]) * (float)rc;
+      if (cost < best) {
+        best = cost;
+        best_idx = (uint32_t)ax * kTopBins + b;
+        best_lc = pc;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          bl[k] = pl[k];
+          bh[k] = ph[k];
+          rl_best[k] = rl[k];
+          rh_best[k] = rh[k];
+        }
+      }
+    }
+  }
+  // lowest (cost, axis, bin) over the warp
+  float wc = best;
+  uint32_t wi = best_idx;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oc = __shfl_xor_sync(0xffffffffu, wc, o);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, wi, o);
+    if (oc < wc || (oc == wc && oi < wi)) {
+      wc = oc;
+      wi = oi;
+    }
+  }
+  if (wi == 0xffffffffu) {  // no usable SAH split: split by position
+    if (lane == 0) {
+      TopSplit S;
+      S.axis = 3;
+      S.bin = 0;
+      S.nleft = n / 2;
+      S.pad = 0;
+      S.task[0] = S.task[1] = 0;
+      S.pad2[0] = S.pad2[1] = 0;
+      S.lclo = S.rclo = T.clo;
+      S.lchi = S.rchi = T.chi;
+      *split = S;
+    }
+  } else if (lane < (uint32_t)kTopBins && best_idx == wi) {
+    TopSplit S;
+    S.axis = wi / kTopBins;
+    S.bin = wi % kTopBins;
+    S.nleft = best_lc;
+    S.pad = 0;
+    S.task[0] = S.task[1] = 0;
+    S.pad2[0] = S.pad2[1] = 0;
+    S.lclo = make_float4(bl[0], bl[1], bl[2], 0.f);
+    S.lchi = make_float4(bh[0], bh[1], bh[2], 0.f);
+    S.rclo = make_float4(rl_best[0], rl_best[1], rl_best[2], 0.f);
+    S.rchi = make_float4(rh_best[0], rh_best[1], rh_best[2], 0.f);
+    *split = S;
+  }
+  if (lane == 0) {
+    box[T.node].lo = make_float4(nlo[0], nlo[1], nlo[2], 0.f);
+    box[T.node].hi = make_float4(nhi[0], nhi[1], nhi[2], 0.f);
+    count[T.node] = n;
+  }
+}
+
 // tasks of at most kTopWarpTask triangles: one warp bins a whole task into
-// its own shared-memory bins with per-lane shared atomics, then stores them
+// its own shared-memory bins with per-lane shared atomics, then splits it
+// from those bins (its bins never go to global memory)
 __global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
                                                       const float4* __restrict__ bhi, const TopTask* __restrict__ tasks,
-                                                      uint32_t n_tasks, uint32_t* __restrict__ bins) {
+                                                      uint32_t n_tasks, TopSplit* __restrict__ splits,
+                                                      BinNode* __restrict__ box, uint32_t* __restrict__ count,
+                                                      uint16_t* __restrict__ code) {
   __shared__ uint32_t sb[8][3 * kTopBins * kTopVals];
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint32_t t = blockIdx.x * 8u + warp;
@@ -1161,6 +1391,7 @@ __global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict
     const float4 c = make_float4(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z), 0.f);
     const int bins3[3] = {top_bin(c.x, T.clo.x, T.chi.x), top_bin(c.y, T.clo.y, T.chi.y),
                           top_bin(c.z, T.clo.z, T.chi.z)};
+    code[p] = (uint16_t)(bins3[0] | (bins3[1] << 4) | (bins3[2] << 8));
     const uint32_t v[6] = {f2o(lo.x), f2o(lo.y), f2o(lo.z), f2o(hi.x), f2o(hi.y), f2o(hi.z)};
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
@@ -1176,136 +1407,88 @@ __global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict
     }
   }
   __syncwarp();
-  uint32_t* g = bins + (size_t)t * 3 * kTopBins * kTopVals;
-  for (uint32_t k = lane; k < 3 * kTopBins * kTopVals; k += 32) g[k] = my[k];
+  warp_top_split(my, T, splits + t, box, count);
 }
 
-__device__ __forceinline__ float box_half_area(float lx, float ly, float lz, float hx, float hy, float hz) {
-  const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
-  return dx * dy + dy * dz + dz * dx;
-}
-
-// one thread per task: the split of least SAH cost; writes the node's box and count
-__global__ void k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks, const uint32_t* __restrict__ bins,
-                            TopSplit* __restrict__ splits, BinNode* __restrict__ box, uint32_t* __restrict__ count) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tasks) return;
+// one warp per task larger than kTopWarpTask (the smaller ones were split
+// by k_top_bin_warp from their shared-memory bins)
+__global__ void __launch_bounds__(128) k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks,
+                                                   const uint32_t* __restrict__ bins, TopSplit* __restrict__ splits,
+                                                   BinNode* __restrict__ box, uint32_t* __restrict__ count) {
+  const uint32_t t = blockIdx.x * 4u + (threadIdx.x >> 5);
+  if (t >= n_tasks) return;  // whole warps leave together
   const TopTask T = tasks[t];
-  const uint32_t* B = bins + (size_t)t * 3 * kTopBins * kTopVals;
-  const uint32_t n = T.end - T.begin;
-  float best = FLT_MAX;
-  uint32_t ba = 3, bb = 0, bl = n / 2;
-  float nlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, nhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  for (int ax = 0; ax < 3; ++ax) {
-    const uint32_t* A = B + ax * kTopBins * kTopVals;
-    float ra[kTopBins];  // area of bins b..15
-    uint32_t rn[kTopBins];
-    float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    uint32_t cnt = 0;
-    for (int b = kTopBins - 1; b >= 0; --b) {
-      const uint32_t* V = A + b * kTopVals;
-      if (V[0]) {
-        for (int k = 0; k < 3; ++k) {
-          l[k] = fminf(l[k], o2f(V[1 + k]));
-          h[k] = fmaxf(h[k], o2f(V[4 + k]));
-        }
-        cnt += V[0];
-      }
-      ra[b] = cnt ? box_half_area(l[0], l[1], l[2], h[0], h[1], h[2]) : 0.f;
-      rn[b] = cnt;
-    }
-    if (ax == 0)
-      for (int k = 0; k < 3; ++k) {
-        nlo[k] = l[k];
-        nhi[k] = h[k];
-      }
-    float L[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, H[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    uint32_t lc = 0;
-    for (int b = 0; b + 1 < kTopBins; ++b) {
-      const uint32_t* V = A + b * kTopVals;
-      if (V[0]) {
-        for (int k = 0; k < 3; ++k) {
-          L[k] = fminf(L[k], o2f(V[1 + k]));
-          H[k] = fmaxf(H[k], o2f(V[4 + k]));
-        }
-        lc += V[0];
-      }
-      const uint32_t rc = rn[b + 1];
-      if (lc == 0 || rc == 0) continue;
-      const float cost = box_half_area(L[0], L[1], L[2], H[0], H[1], H[2]) * (float)lc + ra[b + 1] * (float)rc;
-      if (cost < best) {
-        best = cost;
-        ba = (uint32_t)ax;
-        bb = (uint32_t)b;
-        bl = lc;
-      }
-    }
-  }
-  TopSplit S;
-  S.axis = ba;
-  S.bin = bb;
-  S.nleft = bl;
-  S.pad = 0;
-  S.lclo = S.rclo = T.clo;
-  S.lchi = S.rchi = T.chi;
-  if (ba < 3) {  // both sides' boxes from the split axis's bins: their centroid ranges
-    const uint32_t* A = B + ba * kTopBins * kTopVals;
-    float l0[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h0[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    float l1[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h1[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-    for (int b = 0; b < kTopBins; ++b) {
-      const uint32_t* V = A + b * kTopVals;
-      if (!V[0]) continue;
-      float* lo = b <= (int)bb ? l0 : l1;
-      float* hi = b <= (int)bb ? h0 : h1;
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = fminf(lo[k], o2f(V[1 + k]));
-        hi[k] = fmaxf(hi[k], o2f(V[4 + k]));
-      }
-    }
-    S.lclo = make_float4(l0[0], l0[1], l0[2], 0.f);
-    S.lchi = make_float4(h0[0], h0[1], h0[2], 0.f);
-    S.rclo = make_float4(l1[0], l1[1], l1[2], 0.f);
-    S.rchi = make_float4(h1[0], h1[1], h1[2], 0.f);
-  }
-  splits[t] = S;
-  box[T.node].lo = make_float4(nlo[0], nlo[1], nlo[2], 0.f);
-  box[T.node].hi = make_float4(nhi[0], nhi[1], nhi[2], 0.f);
-  count[T.node] = n;
+  if (T.end - T.begin <= kTopWarpTask) return;
+  warp_top_split(bins + (size_t)t * 3 * kTopBins * kTopVals, T, splits + t, box, count);
 }
 
-// flags[p] = 1 if position p of an active task goes left
-__global__ void k_top_flags(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
-                            const float4* __restrict__ bhi, const uint32_t* __restrict__ task_of,
-                            const TopTask* __restrict__ tasks, const TopSplit* __restrict__ splits, uint32_t n_tasks,
-                            uint32_t n, uint32_t* __restrict__ flags) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t t = task_of[p];
-  uint32_t f = 0;
-  if (t < n_tasks) {
-    const TopSplit S = splits[t];
-    const TopTask T = tasks[t];
-    if (S.axis < 3) {
-      const uint32_t tri = ord[p];
-      const float4 lo = blo[tri], hi = bhi[tri];
-      const float c = S.axis == 0 ? 0.5f * (lo.x + hi.x) : (S.axis == 1 ? 0.5f * (lo.y + hi.y) : 0.5f * (lo.z + hi.z));
-      const float clo = S.axis == 0 ? T.clo.x : (S.axis == 1 ? T.clo.y : T.clo.z);
-      const float chi = S.axis == 0 ? T.chi.x : (S.axis == 1 ? T.chi.y : T.chi.z);
-      f = top_bin(c, clo, chi) <= (int)S.bin ? 1u : 0u;
-    } else {
-      f = (p - T.begin) < S.nleft ? 1u : 0u;
-    }
-  }
-  flags[p] = f;
+// 1 if position p (of task t) goes left: its bin on the split axis (the
+// bin codes that binning wrote: 4 bits per axis) is at most the split bin,
+// or, for a split by position, it lies in the first nleft positions
+__device__ __forceinline__ uint32_t top_goes_left(uint32_t p, uint32_t code, const TopTask& T, const TopSplit& S) {
+  if (S.axis < 3) return ((code >> (4 * S.axis)) & 15u) <= S.bin ? 1u : 0u;
+  return (p - T.begin) < S.nleft ? 1u : 0u;
 }
 
-// stable partition of every active task's range (scan = exclusive scan of flags)
-// stable partition of every active task's range (scan = exclusive scan of
-// flags); task_of2 gets each position's task of the next level
+// the flags of the stable partition and the first phase of their exclusive
+// scan in one pass: each chunk of 1024 positions (256 threads x 4) scans its
+// flags into pscan and writes its total to sums (scanned by k_scan_sums;
+// k_top_scatter adds a chunk's offset itself)
+__global__ void __launch_bounds__(256) k_top_flag_scan(const uint32_t* __restrict__ task_of,
+                                                       const uint16_t* __restrict__ code,
+                                                       const TopTask* __restrict__ tasks,
+                                                       const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                                                       uint32_t n, uint32_t* __restrict__ pscan,
+                                                       uint32_t* __restrict__ sums) {
+  __shared__ uint32_t wsum[8];
+  const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
+  uint32_t f[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t p = base + k;
+    if (p < n) {
+      const uint32_t t = task_of[p];
+      if (t < n_tasks) f[k] = top_goes_left(p, code[p], tasks[t], splits[t]);
+    }
+  }
+  const uint32_t tot = f[0] + f[1] + f[2] + f[3];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t woff = 0, all = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < 8; ++w) {
+    const uint32_t x = wsum[w];
+    woff += w < warp ? x : 0u;
+    all += x;
+  }
+  const uint32_t e = woff + inc - tot;
+  const uint4 o4 = make_uint4(e, e + f[0], e + f[0] + f[1], e + f[0] + f[1] + f[2]);
+  if (base + 3 < n) {
+    *reinterpret_cast<uint4*>(pscan + base) = o4;
+  } else {
+    if (base < n) pscan[base] = o4.x;
+    if (base + 1 < n) pscan[base + 1] = o4.y;
+    if (base + 2 < n) pscan[base + 2] = o4.z;
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = all;
+}
+
+// stable partition of every active task's range: the lefts before p within
+// its task are the exclusive scan (chunk scan + chunk offset) at p minus that
+// at the task's first position; task_of2 gets each position's task of the
+// next level
 __global__ void k_top_scatter(const uint32_t* __restrict__ ord, uint32_t* __restrict__ ord2,
                               const uint32_t* __restrict__ task_of, uint32_t* __restrict__ task_of2,
-                              const TopTask* __restrict__ tasks, const TopSplit* __restrict__ splits, uint32_t n_tasks,
-                              const uint32_t* __restrict__ flags, const uint32_t* __restrict__ scan, uint32_t n,
+                              const uint16_t* __restrict__ code, const TopTask* __restrict__ tasks,
+                              const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                              const uint32_t* __restrict__ pscan, const uint32_t* __restrict__ sums, uint32_t n,
                               uint32_t* status) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -1314,9 +1497,10 @@ __global__ void k_top_scatter(const uint32_t* __restrict__ ord, uint32_t* __rest
   if (t < n_tasks) {
     const TopTask T = tasks[t];
     const TopSplit S = splits[t];
-    const uint32_t l = scan[p] - scan[T.begin];  // lefts before p within the task
-    d = flags[p] ? T.begin + l : T.begin + S.nleft + (p - T.begin - l);
-    next = S.task[flags[p] ? 0 : 1];
+    const uint32_t f = top_goes_left(p, code[p], T, S);
+    const uint32_t l = (pscan[p] + sums[p >> 10]) - (pscan[T.begin] + sums[T.begin >> 10]);
+    d = f ? T.begin + l : T.begin + S.nleft + (p - T.begin - l);
+    next = S.task[f ? 0 : 1];
     if (d < T.begin || d >= T.end) {
       atomicOr(status, J3DG_DEV_BAD_INDEX);
       return;
@@ -1475,14 +1659,15 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   CollapseItem *qa = nullptr, *qb = nullptr;
   float4* wide = nullptr;
   // PLOC
-  uint32_t *C0 = nullptr, *C1 = nullptr, *nn = nullptr, *create = nullptr, *survive = nullptr, *cscan = nullptr,
-           *sscan = nullptr, *pl_sums = nullptr, *count = nullptr, *tot = nullptr;
+  uint32_t *C0 = nullptr, *C1 = nullptr, *nn = nullptr, *cscan = nullptr,
+           *sscan = nullptr, *pl_sums = nullptr, *pl_sums2 = nullptr, *count = nullptr, *tot = nullptr;
   float4 *lo0 = nullptr, *hi0 = nullptr, *lo1 = nullptr, *hi1 = nullptr, *tris_out = nullptr;
   PlaceItem *pa = nullptr, *pb = nullptr;
   // SAH top levels
   uint32_t *ord_a = nullptr, *ord_b = nullptr, *task_of = nullptr, *task_of2 = nullptr, *seg0 = nullptr,
            *seg1 = nullptr, *seg_starts = nullptr, *seg_scan = nullptr, *top_bins = nullptr, *top_ctr = nullptr;
   float4 *tbox_lo = nullptr, *tbox_hi = nullptr;
+  uint16_t* codes = nullptr;  // per position: the centroid's bin on each axis (4 bits each)
   TopTask *tasks_a = nullptr, *tasks_b = nullptr;
   TopSplit* splits = nullptr;
   TopRange* ranges = nullptr;
@@ -1533,9 +1718,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     const int shift = 8 * pass;
     k_radix_hist<<<n_tiles, kSortThreads, 0, st>>>(k0, nt, shift, n_tiles, hist);
     k_scan_chunks<<<scan_blocks, 256, 0, st>>>(hist, hist, hist_n, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(sums, scan_blocks);
-    k_scan_add<<<scan_blocks, 256, 0, st>>>(hist, hist_n, sums);
-    k_radix_scatter<<<n_tiles, kSortThreads, 0, st>>>(k0, v0, k1, v1, nt, shift, n_tiles, hist, d_status);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, nullptr, scan_blocks, nullptr);
+    k_radix_scatter<<<n_tiles, kSortThreads, 0, st>>>(k0, v0, k1, v1, nt, shift, n_tiles, hist, sums, d_status);
     J3DG_CK(cudaGetLastError());
     std::swap(k0, k1);
     std::swap(v0, v1);
@@ -1567,11 +1751,10 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_CK(cudaMallocAsync((void**)&C0, sizeof(uint32_t) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&C1, sizeof(uint32_t) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&nn, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&create, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&survive, sizeof(uint32_t) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&cscan, sizeof(uint32_t) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&sscan, sizeof(uint32_t) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&pl_sums, sizeof(uint32_t) * (sblocks_max + 1), st));
+    J3DG_CK(cudaMallocAsync((void**)&pl_sums2, sizeof(uint32_t) * (sblocks_max + 1), st));
     J3DG_CK(cudaMallocAsync((void**)&tot, sizeof(uint32_t) * 2, st));
     J3DG_CK(cudaMallocAsync((void**)&lo0, sizeof(float4) * nt, st));
     J3DG_CK(cudaMallocAsync((void**)&hi0, sizeof(float4) * nt, st));
@@ -1583,7 +1766,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     const auto scan_u32 = [&](const uint32_t* in, uint32_t* out, uint32_t n) {
       const uint32_t sb = (n + 1023) / 1024;
       k_scan_chunks<<<sb, 256, 0, st>>>(in, out, n, pl_sums);
-      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
+      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, nullptr, sb, nullptr);
       k_scan_add<<<sb, 256, 0, st>>>(out, n, pl_sums);
     };
     top = J3DG_SAH_TOP > 0 && nt > J3DG_SAH_TOP;
@@ -1596,6 +1779,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       J3DG_CK(cudaMallocAsync((void**)&task_of2, sizeof(uint32_t) * nt, st));
       J3DG_CK(cudaMallocAsync((void**)&tbox_lo, sizeof(float4) * nt, st));
       J3DG_CK(cudaMallocAsync((void**)&tbox_hi, sizeof(float4) * nt, st));
+      J3DG_CK(cudaMallocAsync((void**)&codes, sizeof(uint16_t) * nt, st));
       k_top_boxes<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, tbox_lo, tbox_hi);
       J3DG_CK(cudaMallocAsync((void**)&seg_starts, sizeof(uint32_t) * nt, st));
       J3DG_CK(cudaMallocAsync((void**)&seg_scan, sizeof(uint32_t) * nt, st));
@@ -1624,20 +1808,20 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       uint32_t n_tasks = 1;
       while (n_tasks > 0) {
         const uint32_t words = n_tasks * 3 * kTopBins * kTopVals;
-        k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words);
+        k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words, tasks_a);
         k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
-                                                                     n_tasks, nt, top_bins);
-        k_top_bin_warp<<<(n_tasks + 7) / 8, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, tasks_a, n_tasks, top_bins);
-        k_top_split<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
+                                                                     n_tasks, nt, top_bins, codes);
+        k_top_bin_warp<<<(n_tasks + 7) / 8, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, tasks_a, n_tasks, splits, box,
+                                                          count, codes);
+        k_top_split<<<(n_tasks + 3) / 4, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
         J3DG_CK(cudaMemsetAsync(top_ctr + 1, 0, sizeof(uint32_t), st));
         k_top_children<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, splits, n_tasks, J3DG_SAH_TOP, top_ctr,
                                                                tasks_b, ranges, child, cap_tasks, nt, nt - 1,
                                                                d_status);
-        k_top_flags<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a, splits, n_tasks, nt,
-                                                      create);
-        scan_u32(create, cscan, nt);
-        k_top_scatter<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, tasks_a, splits, n_tasks,
-                                                        create, cscan, nt, d_status);
+        k_top_flag_scan<<<sblocks_max, 256, 0, st>>>(task_of, codes, tasks_a, splits, n_tasks, nt, cscan, pl_sums);
+        k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, nullptr, sblocks_max, nullptr);
+        k_top_scatter<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, codes, tasks_a, splits,
+                                                        n_tasks, cscan, pl_sums, nt, d_status);
         std::swap(ord_a, ord_b);
         std::swap(task_of, task_of2);
         J3DG_CK(cudaGetLastError());
@@ -1669,6 +1853,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       J3DG_DROP(task_of2);
       J3DG_DROP(tbox_lo);
       J3DG_DROP(tbox_hi);
+      J3DG_DROP(codes);
       J3DG_DROP(top_bins);
       J3DG_DROP(tasks_a);
       J3DG_DROP(tasks_b);
@@ -1682,14 +1867,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     while (mcount > n_seg) {
       const uint32_t blocks = (mcount + kPlocBlock - 1) / kPlocBlock, sb = (mcount + 1023) / 1024;
       k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, seg0, mcount, nn);
-      k_ploc_flags<<<blocks, kPlocBlock, 0, st>>>(nn, mcount, create, survive);
-      k_scan_chunks<<<sb, 256, 0, st>>>(create, cscan, mcount, pl_sums);
-      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
-      k_scan_add<<<sb, 256, 0, st>>>(cscan, mcount, pl_sums);
-      k_scan_chunks<<<sb, 256, 0, st>>>(survive, sscan, mcount, pl_sums);
-      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, sb);
-      k_scan_add<<<sb, 256, 0, st>>>(sscan, mcount, pl_sums);
-      k_ploc_totals<<<1, 1, 0, st>>>(create, cscan, survive, sscan, mcount, tot);
+      k_ploc_flag_scan<<<sb, 256, 0, st>>>(nn, mcount, cscan, sscan, pl_sums, pl_sums2);
+      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, pl_sums2, sb, tot);
       J3DG_CK(cudaGetLastError());
       J3DG_CK(cudaMemcpyAsync(htot, tot, sizeof(htot), cudaMemcpyDeviceToHost, st));
       J3DG_CK(cudaStreamSynchronize(st));
@@ -1698,8 +1877,8 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
         rc = J3DG_ERR_CUDA;
         goto cleanup;
       }
-      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, seg0, nn, cscan, sscan, mcount, node_base, C1, lo1,
-                                                 hi1, seg1, child, box, count);
+      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, seg0, nn, cscan, sscan, pl_sums, pl_sums2, mcount,
+                                                 node_base, C1, lo1, hi1, seg1, child, box, count);
       J3DG_CK(cudaGetLastError());
       node_base += htot[0];
       round_end.push_back(node_base);
@@ -1727,8 +1906,6 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_DROP(C0);
     J3DG_DROP(C1);
     J3DG_DROP(nn);
-    J3DG_DROP(create);
-    J3DG_DROP(survive);
     J3DG_DROP(cscan);
     J3DG_DROP(sscan);
     J3DG_DROP(lo0);
@@ -1873,6 +2050,7 @@ cleanup:
     if (q) cudaFreeAsync(q, st);
   if (tbox_lo) cudaFreeAsync(tbox_lo, st);
   if (tbox_hi) cudaFreeAsync(tbox_hi, st);
+  if (codes) cudaFreeAsync(codes, st);
   if (tasks_a) cudaFreeAsync(tasks_a, st);
   if (tasks_b) cudaFreeAsync(tasks_b, st);
   if (splits) cudaFreeAsync(splits, st);
@@ -1880,7 +2058,7 @@ cleanup:
   if (dp_dec) cudaFreeAsync(dp_dec, st);
   if (qa) cudaFreeAsync(qa, st);
   if (qb) cudaFreeAsync(qb, st);
-  for (uint32_t* p : {C0, C1, nn, create, survive, cscan, sscan, pl_sums, count, tot})
+  for (uint32_t* p : {C0, C1, nn, cscan, sscan, pl_sums, pl_sums2, count, tot})
     if (p) cudaFreeAsync(p, st);
   for (float4* p : {lo0, hi0, lo1, hi1})
     if (p) cudaFreeAsync(p, st);

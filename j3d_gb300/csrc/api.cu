@@ -259,6 +259,9 @@ int copy_out(j3dg_ctx* c, void* dst, const void* src, size_t n) {
 }
 
 void free_mesh_buffers(j3dg_mesh* m) {
+  // the BVH arrays come from the stream-ordered pool, whose cudaFree does not
+  // wait for the device: finish every stream's work on them first
+  cudaDeviceSynchronize();
   cudaFree(m->d_nodes);
   cudaFree(m->d_tris);
   cudaFree(m->d_normals);

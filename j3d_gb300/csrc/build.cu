@@ -1703,8 +1703,11 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   }
   for (int k = 0; k < 6; ++k) m->scale = std::max(m->scale, std::fabs(hbb[k]));
 
-  J3DG_CK(cudaMalloc(&m->d_normals, sizeof(float4) * (size_t)nt));
-  J3DG_CK(cudaMalloc(&m->d_tris, sizeof(float4) * 3 * (size_t)nt));
+  // the mesh's own arrays come from the stream-ordered pool too: a context
+  // keeps the pool's memory reserved between builds, so a warm build maps no
+  // new memory (mapping GBs takes milliseconds)
+  J3DG_CK(cudaMallocAsync(&m->d_normals, sizeof(float4) * (size_t)nt, st));
+  J3DG_CK(cudaMallocAsync(&m->d_tris, sizeof(float4) * 3 * (size_t)nt, st));
   J3DG_CK(cudaMallocAsync((void**)&k0, sizeof(uint64_t) * nt, st));
   J3DG_CK(cudaMallocAsync((void**)&k1, sizeof(uint64_t) * nt, st));
   J3DG_CK(cudaMallocAsync((void**)&v0, sizeof(uint32_t) * nt, st));
@@ -1736,7 +1739,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
     m->n_nodes = 0;
     m->max_depth = 0;
-    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * F4));
+    J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4, st));
     J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * F4, st));
     goto cleanup;
   }
@@ -1938,7 +1941,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * F4 * (size_t)nt, st));
     J3DG_CK(cudaMallocAsync((void**)&pa, sizeof(PlaceItem) * (size_t)nt, st));
     J3DG_CK(cudaMallocAsync((void**)&pb, sizeof(PlaceItem) * (size_t)nt, st));
-    J3DG_CK(cudaMalloc((void**)&tris_out, sizeof(float4) * 3 * (size_t)nt));
+    J3DG_CK(cudaMallocAsync((void**)&tris_out, sizeof(float4) * 3 * (size_t)nt, st));
     {
       const PlaceItem root_place{root, 0u, 1u, 0u};
       J3DG_CK(cudaMemcpyAsync(pa, &root_place, sizeof(root_place), cudaMemcpyHostToDevice, st));
@@ -1963,13 +1966,13 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->n_nodes = hc[1];
     m->max_depth = hc[3];
     m->root_ref = 0;
-    J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * F4 * (size_t)m->n_nodes));
+    J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4 * (size_t)m->n_nodes, st));
     if (J3DG_DFS_ORDER)
       J3DG_CK(dfs_order(W, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
     else
       J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * F4 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
     J3DG_CK(cudaStreamSynchronize(st));
-    cudaFree(m->d_tris);  // the leaf-ordered triangles are the placed ones now
+    cudaFreeAsync(m->d_tris, st);  // the leaf-ordered triangles are the placed ones now
     m->d_tris = tris_out;
     tris_out = nullptr;
     goto cleanup;
@@ -2013,7 +2016,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   m->n_nodes = hc[1];
   m->max_depth = hc[3];
   m->root_ref = 0;
-  J3DG_CK(cudaMalloc(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes));
+  J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes, st));
   if (J3DG_DFS_ORDER)
     J3DG_CK(dfs_order(4, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
   else
@@ -2021,7 +2024,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
 
 cleanup:
   if (rc == J3DG_OK && m->d_tris) {  // the inverse of the leaf order, for lookups by triangle id
-    cudaError_t e = cudaMalloc(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt);
+    cudaError_t e = cudaMallocAsync(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt, st);
     if (e == cudaSuccess) {
       k_slot_of<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, (uint32_t*)m->d_slot_of, d_status);
       e = cudaGetLastError();
@@ -2064,7 +2067,7 @@ cleanup:
     if (p) cudaFreeAsync(p, st);
   if (pa) cudaFreeAsync(pa, st);
   if (pb) cudaFreeAsync(pb, st);
-  if (tris_out) cudaFree(tris_out);
+  if (tris_out) cudaFreeAsync(tris_out, st);
   {
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == J3DG_OK && e != cudaSuccess) {

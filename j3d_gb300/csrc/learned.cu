@@ -82,12 +82,15 @@ __device__ __forceinline__ void ray_inputs(const j3dg_ray* ray, float cx, float 
   in6[5] = f[6] * dl;
 }
 
-// feature pair m = i * 16 + k (columns 2m: sin, 2m + 1: cos)
+// feature pair m = i * 16 + k (columns 2m: sin, 2m + 1: cos). The hardware
+// sine / cosine (__sincosf: absolute error ~1e-5 at the arguments here,
+// |x| < ~130) is far below the bf16 rounding the features get; training and
+// inference compute the features with this same function.
 __device__ __forceinline__ __nv_bfloat162 feature_pair(const float (&in6)[6], int m) {
   const int i = m / kBands, k = m % kBands;
   const float fr = 3.14159265f * exp2f(0.25f * (float)k);
   float s, c;
-  sincosf(fr * in6[i], &s, &c);
+  __sincosf(fr * in6[i], &s, &c);
   return __halves2bfloat162(__float2bfloat16(s), __float2bfloat16(c));
 }
 
@@ -253,48 +256,84 @@ __global__ void k_top2(const float* __restrict__ logits, uint32_t rows, uint32_t
 
 // ------------------------------------------- fused inference on tcgen05 ----
 //
-// One CTA of 8 warps per 128 rays runs the whole network on chip: the
-// features go to shared memory, every layer is a tcgen05 MMA chain (thread
-// 0 issues K / 16 MMAs of M = 128) into a TMEM accumulator, the hidden
-// epilogues (bias, bf16, GELU, bf16 -- as the layer-by-layer path rounds)
-// read TMEM with tcgen05.ld and write the next layer's operand back to
-// shared memory, and the 4096 logits are consumed in 16 chunks of 256
-// columns, alternating between two TMEM column ranges and two weight
-// buffers, by a per-row running top-2 (thread = row = TMEM lane). No
-// activation or logit leaves the SM. Weights are packed once per call into
-// the canonical K-major layout; thread 0 streams each layer / chunk into a
-// shared-memory buffer with cp.async.bulk as soon as the MMA that read the
-// buffer's previous contents has completed, so the copies run under the
-// epilogues.
+// One CTA runs the whole network on chip for 256 rays, as two tiles of 128
+// rows (A, B) that take turns on the tensor core: while the MMAs of one
+// tile's layer run, the other tile's epilogue runs on the CUDA cores, and
+// every weight chunk brought into shared memory serves both tiles (half the
+// weight traffic per ray of one tile per CTA).
+//
+// Warps 0-3 serve tile A and warps 4-7 tile B (thread = row = TMEM lane of
+// the tile's accumulator); warp 8 (one lane) is the producer: it streams
+// the weights with cp.async.bulk into two shared-memory buffers and issues
+// every MMA (tcgen05, M = 128, N = 128, fp32 accumulators in TMEM: tile A
+// columns 0-255, tile B 256-511, two 128-column buffers each). The network
+// runs as 36 stages per tile: layer 1 (K = 208: 192 Fourier features, the
+// two bias columns, zeros), layers 2-4 (K = 144) and 32 chunks of 128
+// logits (K = 144). Stage j of a tile writes TMEM buffer j % 2 and needs
+// the tile's epilogue of stage j - 1 (its operand rows, for the layers) or
+// j - 2 (the buffer, for the logits). Handshakes are mbarriers: MMA
+// completion per tile and buffer (tcgen05.commit), epilogue completion per
+// tile (128 arrivals), weights landed and weights consumed per buffer.
+// Hidden epilogues: bf16, GELU, bf16 (as the layer-by-layer path rounds)
+// back into the tile's operand rows; logit epilogues: a per-row running
+// top-2. No activation or logit leaves the SM. Every wait is bounded; a
+// CTA that times out raises the status word, lets its copies and MMAs
+// drain, frees its TMEM and ends.
+//
+// The biases ride in the MMAs: every operand row carries two columns of
+// ones (layer 1: columns 192, 193; layers 2-5: columns 128, 129 of a
+// 16-column block after the 128 activations), and the packed weights carry
+// each bias split into two bf16 parts (hi = bf16(b), lo = bf16(b - hi)) in
+// those rows, so the fp32 accumulator holds W x + b to ~16 bits of b.
+static const int kIn1 = 6 * kBands * 2 + 16;           // 208: K of layer 1
+static const int kHidB = kHid + 16;                     // 144: K of layers 2..5
+static const int kBiasIn = 2 * 6 * kBands;              // layer 1's bias columns: 192, 193
+static const int kChunkN = 128;                         // logits per stage
+static const int kChunks = kOut / kChunkN;              // 32
+static const int kStages = 4 + kChunks;                 // 36
+static const uint32_t kTileBytes = 128 * kIn1 * 2;      // 52 KB: a tile's operand rows (layer 1's are the widest)
+static const uint32_t kWBytes = 128 * kIn1 * 2;         // 52 KB: W1, or a layer / logit chunk of 128 x 144
+static const uint32_t kFusedSmem = 2 * kTileBytes + 2 * kWBytes + 1024;
+static const int kFusedThreads = 9 * 32;
+static const long long kFusedWait = 500000000ll;  // ~0.25 s at 2 GHz per wait
 
-static const uint32_t kFusedXBytes = 128 * kIn * 2;   // 64 KB: features, then hidden activations
-static const uint32_t kFusedWBytes = 256 * kHid * 2;  // 64 KB: W1 (128 x 256) or a 256-row W5 chunk
-static const uint32_t kFusedBiasBytes = (4 * kHid + kOut) * 4;
-static const uint32_t kFusedSmem = kFusedXBytes + 2 * kFusedWBytes + kFusedBiasBytes + 1024;
-static const long long kFusedWait = 500000000ll;      // ~0.25 s at 2 GHz per wait
-
-// W (fp32 row-major [K][N]) -> bf16 K-major operand Bt[N][K], canonical layout
-__global__ void k_pack_weights(const float* __restrict__ W, int K, int N, __nv_bfloat16* __restrict__ out) {
+// W (fp32 row-major [K][N]) and bias b -> the fused kernel's bf16 K-major
+// operand [N][Kp] (canonical layout): rows k < kb are W's, row kb the bias's
+// bf16 high part, row kb + 1 its low part, the rest zero; columns n >=
+// n_valid get a -inf bias (no cluster there)
+__global__ void k_pack_fused(const float* __restrict__ W, const float* __restrict__ b, int Kp, int kb, int N,
+                             uint32_t n_valid, __nv_bfloat16* __restrict__ out) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)K * N) return;
-  const int n = (int)(i / K), k = (int)(i % K);
-  out[umma::tile_offset(n, k, K / 8) / 2] = __float2bfloat16(W[(size_t)k * N + n]);
+  if (i >= (size_t)Kp * N) return;
+  const int n = (int)(i / Kp), k = (int)(i % Kp);
+  __nv_bfloat16 v = __float2bfloat16(0.f);
+  if (k < kb) {
+    v = __float2bfloat16(W[(size_t)k * N + n]);
+  } else if (k == kb || k == kb + 1) {
+    if ((uint32_t)n >= n_valid) {
+      v = __float2bfloat16(k == kb ? -INFINITY : 0.f);
+    } else {
+      const __nv_bfloat16 hi = __float2bfloat16(b[n]);
+      v = k == kb ? hi : __float2bfloat16(b[n] - __bfloat162float(hi));
+    }
+  }
+  out[umma::tile_offset(n, k, Kp / 8) / 2] = v;
 }
 
 struct FusedArgs {
   const j3dg_ray* rays;
   uint32_t n;
   float cx, cy, cz, inv_s;
-  const __nv_bfloat16* w[5];  // packed layers
-  const float* b[5];
+  const __nv_bfloat16* w[5];  // packed layers, biases included (k_pack_fused)
   uint32_t n_clusters;
+  uint32_t hint_back;  // rays between a CTA's first ray and the ray whose result picks its first chunk
   uint32_t* top2;
   uint32_t* status;
 };
 
 __device__ __forceinline__ uint32_t bits2(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
 
-// thread 0: D[tmem] = X[128 x K] . W^T, W given as N rows of K
+// D[tmem] = X[128 x K] . W^T, W given as N rows of K (one thread issues)
 __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* X, const uint8_t* W, int K, int N) {
   const uint32_t idesc = N == 256 ? umma::idesc_bf16_f32(128, 256) : umma::idesc_bf16_f32(128, 128);
   const uint32_t sbo = (uint32_t)(K / 8) * 128u, x0 = umma::smem_u32(X), w0 = umma::smem_u32(W);
@@ -302,223 +341,230 @@ __device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* X, c
     umma::mma_bf16(d_tmem, umma::desc(x0 + s * 256, 128, sbo), umma::desc(w0 + s * 256, 128, sbo), idesc, s > 0);
 }
 
-// bias, bf16, GELU, bf16 (EPI_BIAS_GELU) -> next operand rows in X (K = 128);
-// this thread's row and 64-column half h
-__device__ __forceinline__ void hidden_epilogue(uint32_t t_lane, const float* bias, uint8_t* X, int row, int h) {
-  {
-    float v[64];
-    umma::ld64(t_lane + (uint32_t)(h * 64), v);
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// the tanh-form GELU of the network, on the hardware tanh (relative error
+// ~2^-11, below the bf16 rounding of the result)
+__device__ __forceinline__ float gelu_hw(float x) {
+  const float k = 0.7978845608028654f;  // sqrt(2 / pi)
+  const float t = fmaf(k * 0.044715f, x * x, k);
+  const float hx = 0.5f * x;
+  return fmaf(hx, tanh_hw(x * t), hx);
+}
+
+// bf16, GELU, bf16 of 64 accumulator columns (the accumulator holds W x + b;
+// the layer-by-layer path rounds the pre-activation to bf16 as well) into
+// columns c0.. of this thread's operand row (K = 144)
+__device__ __forceinline__ void hidden_cols(uint32_t taddr, uint8_t* X, int row, int c0) {
+  float v[64];
+  umma::ld64(taddr, v);
 #pragma unroll
-    for (int g = 0; g < 8; ++g) {
-      uint32_t pk[4];
+  for (int g = 0; g < 8; ++g) {
+    uint32_t pk[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = g * 8 + 2 * q, c0 = h * 64 + i;
-        const __nv_bfloat16 z0 = __float2bfloat16(v[i] + bias[c0]);
-        const __nv_bfloat16 z1 = __float2bfloat16(v[i + 1] + bias[c0 + 1]);
-        pk[q] = bits2(__halves2bfloat162(__float2bfloat16(gelu_f(__bfloat162float(z0))),
-                                         __float2bfloat16(gelu_f(__bfloat162float(z1)))));
-      }
-      *reinterpret_cast<uint4*>(X + umma::tile_offset(row, h * 64 + g * 8, kHid / 8)) =
-          make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    for (int q = 0; q < 4; ++q) {
+      const int i = g * 8 + 2 * q;
+      const float z0 = __bfloat162float(__float2bfloat16(v[i]));
+      const float z1 = __bfloat162float(__float2bfloat16(v[i + 1]));
+      pk[q] = bits2(__floats2bfloat162_rn(gelu_hw(z0), gelu_hw(z1)));
     }
+    *reinterpret_cast<uint4*>(X + umma::tile_offset(row, c0 + g * 8, kHidB / 8)) =
+        make_uint4(pk[0], pk[1], pk[2], pk[3]);
   }
 }
 
-// 8 warps: warp w reads TMEM lane quarter w % 4 (rows 32 (w % 4) + lane)
-// and works on column half w / 4 of every epilogue.
-__global__ void __launch_bounds__(256, 1) k_learned_fused(const FusedArgs a) {
+__global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedArgs a) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t mma_bar[2];
-  __shared__ __align__(8) uint64_t load_bar[2];
-  __shared__ uint32_t taddr_s;
-  uint8_t* X = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* Wb[2] = {X + kFusedXBytes, X + kFusedXBytes + kFusedWBytes};
-  float* bias = reinterpret_cast<float*>(X + kFusedXBytes + 2 * kFusedWBytes);  // b1..b4, then b5 (-inf past n_clusters)
-  const int tid = threadIdx.x, warp = tid >> 5, row = tid & 127, half = tid >> 7;
-  const uint32_t r = blockIdx.x * 128u + (uint32_t)row;
-  bool ok = true;
-  float v1 = -FLT_MAX, v2 = -FLT_MAX;
-  uint32_t i1 = 0xffffffffu, i2 = 0xffffffffu, taddr = 0, t_lane = 0, mb[2] = {0, 0}, lb[2] = {0, 0};
-
-  // a CTA that timed out raised the status word: the rest of the grid stops
-  if (*reinterpret_cast<volatile uint32_t*>(a.status) & J3DG_DEV_VISIT_CAP) return;
+  __shared__ __align__(8) uint64_t bar_md[2][2];  // MMA of (tile, buffer) done
+  __shared__ __align__(8) uint64_t bar_cf[2][2];  // tile's epilogue done (128 arrivals), by epilogue parity
+  __shared__ __align__(8) uint64_t bar_wl[2];     // weights landed in buffer
+  __shared__ __align__(8) uint64_t bar_wf[2];     // MMAs reading buffer done
+  __shared__ uint32_t taddr_s, cs_s, stop_s;
+  uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) stop_s = *reinterpret_cast<volatile uint32_t*>(a.status) & J3DG_DEV_VISIT_CAP;
   if (warp == 0) {
     umma::tmem_alloc(umma::smem_u32(&taddr_s), 512);
     umma::tmem_relinquish();
   }
-  mb[0] = umma::smem_u32(&mma_bar[0]);
-  mb[1] = umma::smem_u32(&mma_bar[1]);
-  lb[0] = umma::smem_u32(&load_bar[0]);
-  lb[1] = umma::smem_u32(&load_bar[1]);
   if (tid == 0) {
-    for (int k = 0; k < 2; ++k) {
-      umma::mbar_init(mb[k], 1);
-      umma::mbar_init(lb[k], 1);
+    for (int i = 0; i < 2; ++i) {
+      for (int t = 0; t < 2; ++t) {
+        umma::mbar_init(umma::smem_u32(&bar_md[t][i]), 1);
+        umma::mbar_init(umma::smem_u32(&bar_cf[t][i]), 128);
+      }
+      umma::mbar_init(umma::smem_u32(&bar_wl[i]), 1);
+      umma::mbar_init(umma::smem_u32(&bar_wf[i]), 1);
     }
+    // The logit chunks are scanned starting from the chunk of the best
+    // cluster of a ray one wave of CTAs earlier (hint_back rays back; most
+    // likely written already, and a neighbour of these rays in the image),
+    // so that most rows meet their best clusters first and skip the other
+    // chunks' groups. Any value read here (even one still being written, or
+    // a previous call's) only picks the order: the top-2 does not depend on
+    // it.
+    uint32_t hint = 0;
+    if (blockIdx.x * 256u >= a.hint_back) hint = a.top2[2 * (size_t)(blockIdx.x * 256u - a.hint_back)];
+    cs_s = hint < a.n_clusters ? hint / kChunkN : 0u;
   }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
-  taddr = taddr_s;
-  t_lane = taddr + ((uint32_t)((warp & 3) * 32) << 16);
-  if (tid == 0) {  // W1 -> buffer 0, W2 -> buffer 1
-    umma::mbar_arrive_expect_tx(lb[0], kIn * kHid * 2);
-    umma::bulk_copy(umma::smem_u32(Wb[0]), a.w[0], kIn * kHid * 2, lb[0]);
-    umma::mbar_arrive_expect_tx(lb[1], kHid * kHid * 2);
-    umma::bulk_copy(umma::smem_u32(Wb[1]), a.w[1], kHid * kHid * 2, lb[1]);
-  }
+  const uint32_t taddr = taddr_s;
+  const int cs = (int)cs_s;
+  bool ok = stop_s == 0;  // a CTA that timed out raised the status word: the rest of the grid stops
 
-// all threads: wait for MMA barrier `bar` phase `parity` (bounded)
-#define J3DG_FUSED_WAIT(bar, parity)                                                   \
-  do {                                                                                 \
-    ok = __syncthreads_and(umma::mbar_wait(mb[bar], (parity), kFusedWait)) != 0;        \
-    if (!ok) goto done;                                                                \
-    umma::fence_after_sync();                                                          \
-  } while (0)
-// thread 0: refill weight buffer `buf` with `bytes` from `src` (its previous
-// MMA has completed: the caller waited for it)
-#define J3DG_FUSED_LOAD(buf, src, bytes)                                               \
-  do {                                                                                 \
-    if (tid == 0) {                                                                    \
-      umma::mbar_arrive_expect_tx(lb[buf], (bytes));                                   \
-      umma::bulk_copy(umma::smem_u32(Wb[buf]), (src), (bytes), lb[buf]);               \
-    }                                                                                  \
-  } while (0)
-// all threads publish their shared-memory writes and TMEM reads; thread 0
-// waits for the weights of buffer `buf` (load phase `lpar`) and issues
-#define J3DG_FUSED_ISSUE(dcol, buf, lpar, K, N)                                        \
-  do {                                                                                 \
-    umma::fence_async_smem();                                                          \
-    umma::fence_before_sync();                                                         \
-    __syncthreads();                                                                   \
-    if (tid == 0) {                                                                    \
-      const bool got = umma::mbar_wait(lb[buf], (lpar), kFusedWait);                   \
-      umma::fence_after_sync();                                                        \
-      if (got) issue_layer(taddr + (dcol), X, Wb[buf], (K), (N));                      \
-      else atomicOr(a.status, J3DG_DEV_VISIT_CAP);                                     \
-      umma::commit(mb[buf]);                                                           \
-    }                                                                                  \
-  } while (0)
-
-  for (int i = tid; i < 4 * kHid; i += 256) bias[i] = a.b[i / kHid][i % kHid];
-  for (int i = tid; i < kOut; i += 256) bias[4 * kHid + i] = (uint32_t)i < a.n_clusters ? a.b[4][i] : -INFINITY;
-  {  // features of ray r (zeros past n), K = 256 operand rows; this half's 16 core matrices
-    float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const bool live = r < a.n;
-    if (live) ray_inputs(a.rays + r, a.cx, a.cy, a.cz, a.inv_s, in6);
-    const __nv_bfloat162 zero = __halves2bfloat162(__float2bfloat16(0.f), __float2bfloat16(0.f));
-#pragma unroll 1
-    for (int kg = half * (kIn / 16); kg < (half + 1) * (kIn / 16); ++kg) {
-      uint32_t p[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int m = kg * 4 + q;
-        p[q] = bits2((live && m < 6 * kBands) ? feature_pair(in6, m) : zero);
+  if (warp == 8) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0 && ok) {
+      int loads = 0, issued = 0;  // stages whose weights were requested / whose MMAs were issued
+      auto load = [&](int j) {
+        const __nv_bfloat16* src;
+        uint32_t bytes;
+        if (j == 0) {
+          src = a.w[0];
+          bytes = 128 * kIn1 * 2;
+        } else if (j < 4) {
+          src = a.w[j];
+          bytes = 128 * kHidB * 2;
+        } else {
+          src = a.w[4] + (size_t)((cs + j - 4) & (kChunks - 1)) * kChunkN * kHidB;
+          bytes = kChunkN * kHidB * 2;
+        }
+        const uint32_t b = umma::smem_u32(&bar_wl[j & 1]);
+        umma::mbar_arrive_expect_tx(b, bytes);
+        umma::bulk_copy(umma::smem_u32(base + 2 * kTileBytes + (j & 1) * kWBytes), src, bytes, b);
+        loads = j + 1;
+      };
+      load(0);
+      load(1);
+      for (int j = 0; j < kStages && ok; ++j) {
+        const int b = j & 1;
+        ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[b]), (uint32_t)(j >> 1) & 1u, kFusedWait);
+        // the epilogue this stage needs: of stage j - 1 (operand rows) up to
+        // the last layer, of stage j - 2 (the TMEM buffer) for the logits;
+        // epilogue e counts as e + 1 (the features are epilogue 0)
+        const int e = j <= 4 ? j : j - 1;
+        for (int t = 0; t < 2 && ok; ++t) {
+          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_cf[t][e & 1]), (uint32_t)(e >> 1) & 1u, kFusedWait);
+          if (!ok) break;
+          umma::fence_after_sync();
+          issue_layer(taddr + (uint32_t)(t * 256 + b * 128), base + t * kTileBytes, base + 2 * kTileBytes + b * kWBytes,
+                      j == 0 ? kIn1 : kHidB, 128);
+          umma::commit(umma::smem_u32(&bar_md[t][b]));
+        }
+        if (!ok) break;
+        umma::commit(umma::smem_u32(&bar_wf[b]));
+        issued = j + 1;
+        if (j >= 1 && j + 1 < kStages) {  // stage j - 1's buffer is free once its MMAs are done: stage j + 1 goes there
+          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wf[(j - 1) & 1]), (uint32_t)((j - 1) >> 1) & 1u, kFusedWait);
+          if (ok) load(j + 1);
+        }
       }
-      *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kg * 8, kIn / 8)) = make_uint4(p[0], p[1], p[2], p[3]);
+      if (!ok) {
+        atomicOr(a.status, J3DG_DEV_VISIT_CAP);
+        // drain: the copies requested and the MMAs issued end before the
+        // CTA frees its TMEM and shared memory (bounded as well)
+        for (int j = issued; j < loads; ++j)
+          umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[j & 1]), (uint32_t)(j >> 1) & 1u, kFusedWait);
+        if (issued > 0)
+          umma::mbar_wait_sleep(umma::smem_u32(&bar_wf[(issued - 1) & 1]), (uint32_t)((issued - 1) >> 1) & 1u,
+                                kFusedWait);
+      }
     }
-  }
-  J3DG_FUSED_ISSUE(0, 0, 0, kIn, kHid);  // layer 1: W buffer 0, load phase 0, mma phase 0
-  J3DG_FUSED_WAIT(0, 0);
-  J3DG_FUSED_LOAD(0, a.w[2], kHid * kHid * 2);  // W3
-  hidden_epilogue(t_lane, bias, X, row, half);
-  J3DG_FUSED_ISSUE(0, 1, 0, kHid, kHid);  // layer 2
-  J3DG_FUSED_WAIT(1, 0);
-  J3DG_FUSED_LOAD(1, a.w[3], kHid * kHid * 2);  // W4
-  hidden_epilogue(t_lane, bias + kHid, X, row, half);
-  J3DG_FUSED_ISSUE(0, 0, 1, kHid, kHid);  // layer 3
-  J3DG_FUSED_WAIT(0, 1);
-  J3DG_FUSED_LOAD(0, a.w[4], kFusedWBytes);  // W5 chunk 0
-  hidden_epilogue(t_lane, bias + 2 * kHid, X, row, half);
-  J3DG_FUSED_ISSUE(0, 1, 1, kHid, kHid);  // layer 4
-  J3DG_FUSED_WAIT(1, 1);
-  J3DG_FUSED_LOAD(1, a.w[4] + 256 * kHid, kFusedWBytes);  // W5 chunk 1
-  hidden_epilogue(t_lane, bias + 3 * kHid, X, row, half);
-  J3DG_FUSED_ISSUE(0, 0, 0, kHid, 256);    // logits chunk 0 (load phase 2, mma phase 2)
-  J3DG_FUSED_ISSUE(256, 1, 0, kHid, 256);  // chunk 1
+  } else if (ok) {
+    // ------------------------------------------------------------ consumers
+    const int t = warp >> 2, row = (warp & 3) * 32 + lane;
+    uint8_t* X = base + t * kTileBytes;
+    const uint32_t r = blockIdx.x * 256u + (uint32_t)(t * 128 + row);
+    const uint32_t t_lane = taddr + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * 256);
+    float v1 = -FLT_MAX, v2 = -FLT_MAX;
+    uint32_t i1 = 0xffffffffu, i2 = 0xffffffffu;
+    {  // features of ray r (zeros past n; columns 192, 193 hold the ones of the bias rows), K = 208
+      float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      const bool live = r < a.n;
+      if (live) ray_inputs(a.rays + r, a.cx, a.cy, a.cz, a.inv_s, in6);
+      const __nv_bfloat162 zero = __floats2bfloat162_rn(0.f, 0.f), ones = __floats2bfloat162_rn(1.f, 1.f);
 #pragma unroll 1
-  for (int c = 0; c < kOut / 256; ++c) {
-    const int s = c & 1;
-    J3DG_FUSED_WAIT(s, (c >> 1) & 1);  // chunk c is commit 2 + c / 2 of its barriers
-    if (c + 2 < kOut / 256) J3DG_FUSED_LOAD(s, a.w[4] + (size_t)(c + 2) * 256 * kHid, kFusedWBytes);
-    const float* b5 = bias + 4 * kHid + c * 256;
-#pragma unroll 1
-    for (int h = 2 * half; h < 2 * half + 2; ++h) {
-      float v[64];
-      umma::ld64(t_lane + (uint32_t)(s * 256 + h * 64), v);
-      float m = -FLT_MAX;
+      for (int kg = 0; kg < kIn1 / 8; ++kg) {
+        uint32_t p[4];
 #pragma unroll
-      for (int q = 0; q < 64; ++q) {
-        v[q] += b5[h * 64 + q];
-        m = fmaxf(m, v[q]);
+        for (int q = 0; q < 4; ++q) {
+          const int m = kg * 4 + q;
+          p[q] = bits2((live && m < 6 * kBands) ? feature_pair(in6, m) : (m == kBiasIn / 2 ? ones : zero));
+        }
+        *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kg * 8, kIn1 / 8)) = make_uint4(p[0], p[1], p[2], p[3]);
       }
-      if (m > v2) {  // rare once the running top-2 is established
+    }
+    umma::fence_async_smem();
+    umma::mbar_arrive(umma::smem_u32(&bar_cf[t][0]));  // epilogue 0: the features
+#pragma unroll 1
+    for (int j = 0; j < kStages; ++j) {
+      const int b = j & 1;
+      ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_md[t][b]), (uint32_t)(j >> 1) & 1u, kFusedWait);
+      if (!ok) break;
+      umma::fence_after_sync();
+      const uint32_t tcol = t_lane + (uint32_t)(b * 128);
+      if (j < 4) {
+        hidden_cols(tcol, X, row, 0);
+        hidden_cols(tcol + 64, X, row, 64);
+        if (j == 0) {  // the bias block of layers 2..5: ones in columns 128, 129, zeros to 143
+          const uint32_t one2 = bits2(__floats2bfloat162_rn(1.f, 1.f));
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid, kHidB / 8)) = make_uint4(one2, 0u, 0u, 0u);
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid + 8, kHidB / 8)) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        umma::fence_async_smem();
+      } else {
+        const int c = (cs + j - 4) & (kChunks - 1);
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          float v[64];
+          umma::ld64(tcol + (uint32_t)(h * 64), v);  // the logits, biases included
+          float m = -FLT_MAX;
 #pragma unroll
-        for (int q = 0; q < 64; ++q) {
-          const float x = v[q];
-          if (x > v2) {
-            const uint32_t col = (uint32_t)(c * 256 + h * 64 + q);
-            if (x > v1) {
-              v2 = v1;
-              i2 = i1;
-              v1 = x;
-              i1 = col;
-            } else {
-              v2 = x;
-              i2 = col;
+          for (int q = 0; q < 64; q += 2) m = max3f(m, v[q], v[q + 1]);
+          if (m >= v2) {  // rare once the row's top-2 is established
+#pragma unroll
+            for (int q = 0; q < 64; ++q) {
+              // chunks come in a rotated order, so ties are broken by the
+              // index itself: (value desc, index asc)
+              const float x = v[q];
+              const uint32_t col = (uint32_t)(c * kChunkN + h * 64 + q);
+              if (x > v2 || (x == v2 && col < i2)) {
+                if (x > v1 || (x == v1 && col < i1)) {
+                  v2 = v1;
+                  i2 = i1;
+                  v1 = x;
+                  i1 = col;
+                } else {
+                  v2 = x;
+                  i2 = col;
+                }
+              }
             }
           }
         }
       }
+      umma::fence_before_sync();
+      umma::mbar_arrive(umma::smem_u32(&bar_cf[t][(j + 1) & 1]));  // epilogue j + 1
     }
-    // chunk c + 2 is load 2 + (c + 2) / 2 of buffer s
-    if (c + 2 < kOut / 256) J3DG_FUSED_ISSUE(s * 256, s, ((c >> 1) + 1) & 1, kHid, 256);
-  }
-  {  // merge the two halves' top-2 by (value desc, index asc) -- the order a
-     // sequential scan with strict comparisons keeps
-    float* pv = reinterpret_cast<float*>(Wb[0]);  // the weight buffers are idle now
-    uint32_t* pi = reinterpret_cast<uint32_t*>(Wb[0] + 1024);
-    if (half == 1) {
-      pv[2 * row] = v1;
-      pv[2 * row + 1] = v2;
-      pi[2 * row] = i1;
-      pi[2 * row + 1] = i2;
-    }
-    __syncthreads();
-    if (half == 0 && r < a.n) {
-      const float c[4] = {v1, v2, pv[2 * row], pv[2 * row + 1]};
-      const uint32_t ci[4] = {i1, i2, pi[2 * row], pi[2 * row + 1]};
-      float b1 = -FLT_MAX, b2 = -FLT_MAX;
-      uint32_t k1 = 0xffffffffu, k2 = 0xffffffffu;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (ci[q] == 0xffffffffu) continue;
-        if (c[q] > b1 || (c[q] == b1 && ci[q] < k1)) {
-          b2 = b1;
-          k2 = k1;
-          b1 = c[q];
-          k1 = ci[q];
-        } else if (c[q] > b2 || (c[q] == b2 && ci[q] < k2)) {
-          b2 = c[q];
-          k2 = ci[q];
-        }
-      }
-      a.top2[2 * (size_t)r] = k1;
-      a.top2[2 * (size_t)r + 1] = k2;
+    if (!ok) {
+      atomicOr(a.status, J3DG_DEV_VISIT_CAP);
+    } else if (r < a.n) {
+      a.top2[2 * (size_t)r] = i1;
+      a.top2[2 * (size_t)r + 1] = i2;
     }
   }
-done:
-  if (!ok && tid == 0) atomicOr(a.status, J3DG_DEV_VISIT_CAP);
   umma::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     umma::fence_after_sync();
     umma::tmem_dealloc(taddr, 512);
   }
-#undef J3DG_FUSED_WAIT
-#undef J3DG_FUSED_LOAD
-#undef J3DG_FUSED_ISSUE
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -1152,18 +1198,21 @@ int j3dg_learned_train(j3dg_learned* l, uint64_t n_rays, float r0, float r1, flo
 // top-2 clusters per ray on device arrays: the fused tcgen05 kernel
 static int predict_fused(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, uint32_t* d_top2) {
   const j3dg::Layout& L = l->L;
+  // packed operands with the bias rows: K = 208 for layer 1, 144 for layers 2..5
+  const int Kp[5] = {j3dg::kIn1, j3dg::kHidB, j3dg::kHidB, j3dg::kHidB, j3dg::kHidB};
+  const int kb[5] = {j3dg::kBiasIn, j3dg::kHid, j3dg::kHid, j3dg::kHid, j3dg::kHid};
   size_t total = 0;
-  for (int k = 0; k < 5; ++k) total += (size_t)L.in[k] * L.out[k];
+  for (int k = 0; k < 5; ++k) total += (size_t)Kp[k] * L.out[k];
   if (!l->d_wpack) LCK(cudaMalloc(&l->d_wpack, sizeof(__nv_bfloat16) * total), "learned pack");
   j3dg::FusedArgs a;
   size_t off = 0;
   for (int k = 0; k < 5; ++k) {
-    const size_t cnt = (size_t)L.in[k] * L.out[k];
-    j3dg::k_pack_weights<<<(unsigned)((cnt + 255) / 256), 256, 0, LS(l)>>>(l->d_p + L.w[k], L.in[k], L.out[k],
-                                                                            l->d_wpack + off);
+    const size_t cnt = (size_t)Kp[k] * L.out[k];
+    j3dg::k_pack_fused<<<(unsigned)((cnt + 255) / 256), 256, 0, LS(l)>>>(
+        l->d_p + L.w[k], l->d_p + L.b[k], Kp[k], kb[k], L.out[k], k == 4 ? l->n_clusters : (uint32_t)L.out[k],
+        l->d_wpack + off);
     LCK(cudaGetLastError(), "learned pack");
     a.w[k] = l->d_wpack + off;
-    a.b[k] = l->d_p + L.b[k];
     off += cnt;
   }
   a.rays = d_rays;
@@ -1173,11 +1222,12 @@ static int predict_fused(j3dg_learned* l, const j3dg_ray* d_rays, uint32_t n, ui
   a.cz = l->center[2];
   a.inv_s = l->inv_scale;
   a.n_clusters = l->n_clusters;
+  a.hint_back = 256u * (uint32_t)std::max(1, l->ctx->sm_count);  // one CTA per SM: one wave back
   a.top2 = d_top2;
   a.status = l->ctx->d_status;
   LCK(cudaFuncSetAttribute(j3dg::k_learned_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)j3dg::kFusedSmem),
       "learned fused");
-  j3dg::k_learned_fused<<<(n + 127) / 128, 256, j3dg::kFusedSmem, LS(l)>>>(a);
+  j3dg::k_learned_fused<<<(n + 255) / 256, j3dg::kFusedThreads, j3dg::kFusedSmem, LS(l)>>>(a);
   LCK(cudaGetLastError(), "learned fused");
   return J3DG_OK;
 }

@@ -141,6 +141,29 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long l
   }
 }
 
+// As mbar_wait, with mbarrier.try_wait: the thread is suspended in the
+// hardware while it waits (up to a system-dependent time per try), so
+// waiting warps take no issue slots from the working ones.
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t mbar, uint32_t parity, long long budget) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > budget) return false;
+  }
+}
+
+// One arrival on mbar (no transactions).
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
 // Byte offset of element (row, k) of a K-major bf16 tile in the canonical
 // layout with `kg` core matrices along K per 8-row group:
 //   core matrix (row / 8, k / 8) at ((row / 8) * kg + k / 8) * 128,

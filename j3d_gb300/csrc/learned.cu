@@ -82,32 +82,59 @@ __device__ __forceinline__ void ray_inputs(const j3dg_ray* ray, float cx, float 
   in6[5] = f[6] * dl;
 }
 
-// feature pair m = i * 16 + k (columns 2m: sin, 2m + 1: cos). The hardware
-// sine / cosine (__sincosf: absolute error ~1e-5 at the arguments here,
-// |x| < ~130) is far below the bf16 rounding the features get; training and
-// inference compute the features with this same function.
-__device__ __forceinline__ __nv_bfloat162 feature_pair(const float (&in6)[6], int m) {
-  const int i = m / kBands, k = m % kBands;
-  const float fr = 3.14159265f * exp2f(0.25f * (float)k);
-  float s, c;
-  __sincosf(fr * in6[i], &s, &c);
-  return __halves2bfloat162(__float2bfloat16(s), __float2bfloat16(c));
+__device__ __forceinline__ uint32_t bits2(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+
+// Frequencies pi 2^(q/4), q = 0..3, of the first octave of bands; band
+// k = 4 o + q has frequency 2^o times band q's, so its sine and cosine come
+// from band q's by o angle doublings (sin 2a = 2 sin a cos a, cos 2a =
+// (cos a - sin a)(cos a + sin a)). The first octave uses the hardware sine /
+// cosine (__sincosf: absolute error ~1e-5 at the arguments here), and the
+// doublings keep the error far below the bf16 rounding the features get.
+// Training and inference compute the features with these same functions.
+__device__ __forceinline__ void base_octave(float x, float (&s)[4], float (&c)[4]) {
+  const float fr[4] = {0x1.921fb6p+1f, 0x1.de3564p+1f, 0x1.1c5832p+2f, 0x1.5225p+2f};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) __sincosf(fr[q] * x, &s[q], &c[q]);
+}
+__device__ __forceinline__ void next_octave(float (&s)[4], float (&c)[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float s2 = 2.f * s[q] * c[q], c2 = (c[q] - s[q]) * (c[q] + s[q]);
+    s[q] = s2;
+    c[q] = c2;
+  }
+}
+// the 4 feature pairs (sin, cos as bf16) of one octave: 16 bytes of a row
+__device__ __forceinline__ uint4 octave_pairs(const float (&s)[4], const float (&c)[4]) {
+  return make_uint4(bits2(__floats2bfloat162_rn(s[0], c[0])), bits2(__floats2bfloat162_rn(s[1], c[1])),
+                    bits2(__floats2bfloat162_rn(s[2], c[2])), bits2(__floats2bfloat162_rn(s[3], c[3])));
 }
 
+// features of ray r: coordinate i, band k at pair i * 16 + k (columns: sin,
+// cos); zeros from column 192 to 255
 __global__ void k_features(const j3dg_ray* __restrict__ rays, uint32_t n, uint32_t n_pad, float cx, float cy,
                            float cz, float inv_s, __nv_bfloat16* __restrict__ X) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_pad) return;
-  __nv_bfloat162* x = reinterpret_cast<__nv_bfloat162*>(X + (size_t)r * kIn);
-  const __nv_bfloat162 zero = __halves2bfloat162(__float2bfloat16(0.f), __float2bfloat16(0.f));
+  uint4* x = reinterpret_cast<uint4*>(X + (size_t)r * kIn);
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
   if (r >= n) {
-    for (int j = 0; j < kIn / 2; ++j) x[j] = zero;
+    for (int j = 0; j < kIn / 8; ++j) x[j] = zero;
     return;
   }
   float in6[6];
   ray_inputs(rays + r, cx, cy, cz, inv_s, in6);
-  for (int m = 0; m < 6 * kBands; ++m) x[m] = feature_pair(in6, m);
-  for (int j = 6 * kBands; j < kIn / 2; ++j) x[j] = zero;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float sn[4], cn[4];
+    base_octave(in6[i], sn, cn);
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+      x[i * 4 + o] = octave_pairs(sn, cn);
+      if (o < 3) next_octave(sn, cn);
+    }
+  }
+  for (int j = 24; j < kIn / 8; ++j) x[j] = zero;
 }
 
 // Softmax cross-entropy over the first K logits of each row; rows with
@@ -258,27 +285,26 @@ __global__ void k_top2(const float* __restrict__ logits, uint32_t rows, uint32_t
 //
 // One CTA runs the whole network on chip for 256 rays, as two tiles of 128
 // rows (A, B) that take turns on the tensor core: while the MMAs of one
-// tile's layer run, the other tile's epilogue runs on the CUDA cores, and
-// every weight chunk brought into shared memory serves both tiles (half the
-// weight traffic per ray of one tile per CTA).
+// tile's stage run, the other tile's epilogue runs on the CUDA cores, and
+// every weight chunk brought into shared memory serves both tiles.
 //
 // Warps 0-3 serve tile A and warps 4-7 tile B (thread = row = TMEM lane of
 // the tile's accumulator); warp 8 (one lane) is the producer: it streams
 // the weights with cp.async.bulk into two shared-memory buffers and issues
-// every MMA (tcgen05, M = 128, N = 128, fp32 accumulators in TMEM: tile A
-// columns 0-255, tile B 256-511, two 128-column buffers each). The network
-// runs as 36 stages per tile: layer 1 (K = 208: 192 Fourier features, the
-// two bias columns, zeros), layers 2-4 (K = 144) and 32 chunks of 128
-// logits (K = 144). Stage j of a tile writes TMEM buffer j % 2 and needs
-// the tile's epilogue of stage j - 1 (its operand rows, for the layers) or
-// j - 2 (the buffer, for the logits). Handshakes are mbarriers: MMA
-// completion per tile and buffer (tcgen05.commit), epilogue completion per
-// tile (128 arrivals), weights landed and weights consumed per buffer.
-// Hidden epilogues: bf16, GELU, bf16 (as the layer-by-layer path rounds)
-// back into the tile's operand rows; logit epilogues: a per-row running
-// top-2. No activation or logit leaves the SM. Every wait is bounded; a
-// CTA that times out raises the status word, lets its copies and MMAs
-// drain, frees its TMEM and ends.
+// every MMA (tcgen05, M = 128, fp32 accumulators in TMEM: tile A columns
+// 0-255, tile B 256-511). Per tile the network is 21 stages: layer 1 in two
+// K parts (K = 208: 192 Fourier features, two bias columns, zeros; the
+// second part's operand columns are written once the first part's MMAs have
+// read theirs, so a tile's operand rows fit in 36 KB), layers 2-4 (K = 144,
+// N = 128) and 16 chunks of 256 logits (K = 144, N = 256). Stage j of a tile
+// needs the tile's epilogue of stage j - 1 (its operand rows and its TMEM
+// columns); handshakes are mbarriers: MMAs of a tile done (tcgen05.commit),
+// epilogue of a tile done (128 arrivals), weights landed and weights
+// consumed per buffer. Hidden epilogues: bf16, GELU, bf16 (as the
+// layer-by-layer path rounds) back into the tile's operand rows; logit
+// epilogues: a per-row running top-2. No activation or logit leaves the SM.
+// Every wait is bounded; a CTA that times out raises the status word, lets
+// its copies and MMAs drain, frees its TMEM and ends.
 //
 // The biases ride in the MMAs: every operand row carries two columns of
 // ones (layer 1: columns 192, 193; layers 2-5: columns 128, 129 of a
@@ -286,15 +312,18 @@ __global__ void k_top2(const float* __restrict__ logits, uint32_t rows, uint32_t
 // each bias split into two bf16 parts (hi = bf16(b), lo = bf16(b - hi)) in
 // those rows, so the fp32 accumulator holds W x + b to ~16 bits of b.
 static const int kIn1 = 6 * kBands * 2 + 16;           // 208: K of layer 1
+static const int kIn1a = 112;                           // layer 1's first K part (columns 0..111)
 static const int kHidB = kHid + 16;                     // 144: K of layers 2..5
 static const int kBiasIn = 2 * 6 * kBands;              // layer 1's bias columns: 192, 193
-static const int kChunkN = 128;                         // logits per stage
-static const int kChunks = kOut / kChunkN;              // 32
-static const int kStages = 4 + kChunks;                 // 36
-static const uint32_t kTileBytes = 128 * kIn1 * 2;      // 52 KB: a tile's operand rows (layer 1's are the widest)
-static const uint32_t kWBytes = 128 * kIn1 * 2;         // 52 KB: W1, or a layer / logit chunk of 128 x 144
+static const int kChunkN = 256;                         // logits per stage
+static const int kChunks = kOut / kChunkN;              // 16
+static const int kStages = 5 + kChunks;                 // 21
+static const int kWeights = 4 + kChunks;                // 20 weight loads (W1 serves stages 0 and 1)
+static const uint32_t kTileBytes = 128 * kHidB * 2;     // 36 KB: a tile's operand rows
+static const uint32_t kWBytes = kChunkN * kHidB * 2;    // 72 KB: a logit chunk (the largest weight block)
 static const uint32_t kFusedSmem = 2 * kTileBytes + 2 * kWBytes + 1024;
 static const int kFusedThreads = 9 * 32;
+static const int kLoadPieces = 8;  // bulk copies per weight block (every block's size is a multiple of 8 x 16 bytes)
 static const long long kFusedWait = 500000000ll;  // ~0.25 s at 2 GHz per wait
 
 // W (fp32 row-major [K][N]) and bias b -> the fused kernel's bf16 K-major
@@ -331,35 +360,17 @@ struct FusedArgs {
   uint32_t* status;
 };
 
-__device__ __forceinline__ uint32_t bits2(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
-
-// D[tmem] = X[128 x K] . W^T, W given as N rows of K (one thread issues)
-__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* X, const uint8_t* W, int K, int N) {
-  const uint32_t idesc = N == 256 ? umma::idesc_bf16_f32(128, 256) : umma::idesc_bf16_f32(128, 128);
-  const uint32_t sbo = (uint32_t)(K / 8) * 128u, x0 = umma::smem_u32(X), w0 = umma::smem_u32(W);
-  for (int s = 0; s < K / 16; ++s)
-    umma::mma_bf16(d_tmem, umma::desc(x0 + s * 256, 128, sbo), umma::desc(w0 + s * 256, 128, sbo), idesc, s > 0);
-}
-
 __device__ __forceinline__ float tanh_hw(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 
-// the tanh-form GELU of the network, on the hardware tanh (relative error
-// ~2^-11, below the bf16 rounding of the result)
-__device__ __forceinline__ float gelu_hw(float x) {
-  const float k = 0.7978845608028654f;  // sqrt(2 / pi)
-  const float t = fmaf(k * 0.044715f, x * x, k);
-  const float hx = 0.5f * x;
-  return fmaf(hx, tanh_hw(x * t), hx);
-}
-
-// bf16, GELU, bf16 of 64 accumulator columns (the accumulator holds W x + b;
-// the layer-by-layer path rounds the pre-activation to bf16 as well) into
-// columns c0.. of this thread's operand row (K = 144)
+// bf16, GELU (tanh form), bf16 of 64 accumulator columns (the accumulator
+// holds W x + b; the layer-by-layer path rounds the pre-activation to bf16
+// as well) into columns c0.. of this thread's operand row (K = 144)
 __device__ __forceinline__ void hidden_cols(uint32_t taddr, uint8_t* X, int row, int c0) {
+  const float k = 0.7978845608028654f;  // sqrt(2 / pi)
   float v[64];
   umma::ld64(taddr, v);
 #pragma unroll
@@ -370,21 +381,53 @@ __device__ __forceinline__ void hidden_cols(uint32_t taddr, uint8_t* X, int row,
       const int i = g * 8 + 2 * q;
       const float z0 = __bfloat162float(__float2bfloat16(v[i]));
       const float z1 = __bfloat162float(__float2bfloat16(v[i + 1]));
-      pk[q] = bits2(__floats2bfloat162_rn(gelu_hw(z0), gelu_hw(z1)));
+      // the hardware tanh (relative error ~2^-11, below the bf16 rounding of the result)
+      const float t0 = tanh_hw(z0 * fmaf(k * 0.044715f, z0 * z0, k)), t1 = tanh_hw(z1 * fmaf(k * 0.044715f, z1 * z1, k));
+      const float h0 = 0.5f * z0, h1 = 0.5f * z1;
+      pk[q] = bits2(__floats2bfloat162_rn(fmaf(h0, t0, h0), fmaf(h1, t1, h1)));
     }
     *reinterpret_cast<uint4*>(X + umma::tile_offset(row, c0 + g * 8, kHidB / 8)) =
         make_uint4(pk[0], pk[1], pk[2], pk[3]);
   }
 }
 
+// KS MMAs of one stage of one tile: D[tmem] (+)= A[128 x 16 KS] . B^T with
+// A the tile's operand rows and B the weight rows (both canonical K-major
+// layouts, kgA / kgB core matrices along K). Descriptors are built once; a
+// K step advances both start addresses by 256 bytes (16 in the descriptors'
+// address field).
+template <int KS>
+__device__ __forceinline__ void issue_mmas(uint32_t d_tmem, uint32_t xa, int kgA, uint32_t wb, int kgB, uint32_t idesc,
+                                           bool acc) {
+  const uint64_t da = umma::desc(xa, 128, (uint32_t)kgA * 128u), db = umma::desc(wb, 128, (uint32_t)kgB * 128u);
+#pragma unroll
+  for (int s = 0; s < KS; ++s)
+    umma::mma_bf16(d_tmem, da + 16u * (uint32_t)s, db + 16u * (uint32_t)s, idesc, (s > 0 || acc) ? 1u : 0u);
+}
+
+// stage j of one tile: layer 1's two K parts, layers 2-4 (N = 128), logit chunks (N = 256)
+__device__ __forceinline__ void issue_stage(int j, uint32_t d_tmem, uint32_t x0, uint32_t w0) {
+  if (j == 0)
+    issue_mmas<kIn1a / 16>(d_tmem, x0, kIn1a / 8, w0, kIn1 / 8, umma::idesc_bf16_f32(128, kHid), false);
+  else if (j == 1)
+    issue_mmas<(kIn1 - kIn1a) / 16>(d_tmem, x0, (kIn1 - kIn1a) / 8, w0 + (kIn1a / 16) * 256, kIn1 / 8,
+                                    umma::idesc_bf16_f32(128, kHid), true);
+  else if (j < 5)
+    issue_mmas<kHidB / 16>(d_tmem, x0, kHidB / 8, w0, kHidB / 8, umma::idesc_bf16_f32(128, kHid), false);
+  else
+    issue_mmas<kHidB / 16>(d_tmem, x0, kHidB / 8, w0, kHidB / 8, umma::idesc_bf16_f32(128, kChunkN), false);
+}
+
 __global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedArgs a) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t bar_md[2][2];  // MMA of (tile, buffer) done
-  __shared__ __align__(8) uint64_t bar_cf[2][2];  // tile's epilogue done (128 arrivals), by epilogue parity
-  __shared__ __align__(8) uint64_t bar_wl[2];     // weights landed in buffer
-  __shared__ __align__(8) uint64_t bar_wf[2];     // MMAs reading buffer done
+  __shared__ __align__(8) uint64_t bar_md[2];  // a tile's stage MMAs done
+  __shared__ __align__(8) uint64_t bar_cf[2];  // a tile's epilogue done (128 arrivals)
+  __shared__ __align__(8) uint64_t bar_wl[2];  // weights landed in buffer
+  __shared__ __align__(8) uint64_t bar_wf[2];  // MMAs reading buffer done
+  __shared__ __align__(8) uint64_t bar_dr;     // all issued MMAs done (the error path's drain)
   __shared__ uint32_t taddr_s, cs_s, stop_s;
   uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* wbuf = base + 2 * kTileBytes;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) stop_s = *reinterpret_cast<volatile uint32_t*>(a.status) & J3DG_DEV_VISIT_CAP;
   if (warp == 0) {
@@ -393,13 +436,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedA
   }
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
-      for (int t = 0; t < 2; ++t) {
-        umma::mbar_init(umma::smem_u32(&bar_md[t][i]), 1);
-        umma::mbar_init(umma::smem_u32(&bar_cf[t][i]), 128);
-      }
+      umma::mbar_init(umma::smem_u32(&bar_md[i]), 1);
+      umma::mbar_init(umma::smem_u32(&bar_cf[i]), 128);
       umma::mbar_init(umma::smem_u32(&bar_wl[i]), 1);
       umma::mbar_init(umma::smem_u32(&bar_wf[i]), 1);
     }
+    umma::mbar_init(umma::smem_u32(&bar_dr), 1);
     // The logit chunks are scanned starting from the chunk of the best
     // cluster of a ray one wave of CTAs earlier (hint_back rays back; most
     // likely written already, and a neighbour of these rays in the image),
@@ -421,59 +463,73 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedA
   if (warp == 8) {
     // ------------------------------------------------------------ producer
     if (lane == 0 && ok) {
-      int loads = 0, issued = 0;  // stages whose weights were requested / whose MMAs were issued
-      auto load = [&](int j) {
+      // weight block w (W1, W2, W3, W4, then the logit chunks in scan order)
+      // goes to buffer w % 2; stage j uses block j - 1 (stages 0, 1: W1)
+      int loads = 0, landed = 0;  // weight blocks requested / landed
+      bool any_mma = false;
+      auto load = [&](int w) {
         const __nv_bfloat16* src;
         uint32_t bytes;
-        if (j == 0) {
+        if (w == 0) {
           src = a.w[0];
           bytes = 128 * kIn1 * 2;
-        } else if (j < 4) {
-          src = a.w[j];
+        } else if (w < 4) {
+          src = a.w[w];
           bytes = 128 * kHidB * 2;
         } else {
-          src = a.w[4] + (size_t)((cs + j - 4) & (kChunks - 1)) * kChunkN * kHidB;
-          bytes = kChunkN * kHidB * 2;
+          src = a.w[4] + (size_t)((cs + w - 4) & (kChunks - 1)) * kChunkN * kHidB;
+          bytes = kWBytes;
         }
-        const uint32_t b = umma::smem_u32(&bar_wl[j & 1]);
+        const uint32_t b = umma::smem_u32(&bar_wl[w & 1]), dst = umma::smem_u32(wbuf + (w & 1) * kWBytes);
         umma::mbar_arrive_expect_tx(b, bytes);
-        umma::bulk_copy(umma::smem_u32(base + 2 * kTileBytes + (j & 1) * kWBytes), src, bytes, b);
-        loads = j + 1;
+        // in kLoadPieces copies (each a multiple of 16 bytes): several bulk
+        // copies in flight land a block sooner than one
+        for (int q = 0; q < kLoadPieces; ++q)
+          umma::bulk_copy(dst + q * (bytes / kLoadPieces), reinterpret_cast<const uint8_t*>(src) + q * (bytes / kLoadPieces),
+                          bytes / kLoadPieces, b);
+        loads = w + 1;
       };
       load(0);
       load(1);
       for (int j = 0; j < kStages && ok; ++j) {
-        const int b = j & 1;
-        ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[b]), (uint32_t)(j >> 1) & 1u, kFusedWait);
-        // the epilogue this stage needs: of stage j - 1 (operand rows) up to
-        // the last layer, of stage j - 2 (the TMEM buffer) for the logits;
-        // epilogue e counts as e + 1 (the features are epilogue 0)
-        const int e = j <= 4 ? j : j - 1;
+        const int w = j < 2 ? 0 : j - 1, b = w & 1;
+        if (j != 1) {
+          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[b]), (uint32_t)(w >> 1) & 1u, kFusedWait);
+          if (ok) landed = w + 1;
+        }
+        // each tile's epilogue of stage j - 1 (epilogue count j: the first
+        // feature part counts as epilogue 0)
         for (int t = 0; t < 2 && ok; ++t) {
-          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_cf[t][e & 1]), (uint32_t)(e >> 1) & 1u, kFusedWait);
+          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_cf[t]), (uint32_t)j & 1u, kFusedWait);
           if (!ok) break;
           umma::fence_after_sync();
-          issue_layer(taddr + (uint32_t)(t * 256 + b * 128), base + t * kTileBytes, base + 2 * kTileBytes + b * kWBytes,
-                      j == 0 ? kIn1 : kHidB, 128);
-          umma::commit(umma::smem_u32(&bar_md[t][b]));
+          issue_stage(j, taddr + (uint32_t)(t * 256), umma::smem_u32(base + t * kTileBytes),
+                      umma::smem_u32(wbuf + b * kWBytes));
+          umma::commit(umma::smem_u32(&bar_md[t]));
+          any_mma = true;
+          if (t == 0 && j >= 2 && w + 1 < kWeights) {
+            // block w - 1's MMAs ran before these: its buffer takes block w + 1
+            // now, while the tensor core works through this stage
+            ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wf[(w - 1) & 1]), (uint32_t)((w - 1) >> 1) & 1u,
+                                       kFusedWait);
+            if (ok) load(w + 1);
+          }
         }
         if (!ok) break;
-        umma::commit(umma::smem_u32(&bar_wf[b]));
-        issued = j + 1;
-        if (j >= 1 && j + 1 < kStages) {  // stage j - 1's buffer is free once its MMAs are done: stage j + 1 goes there
-          ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_wf[(j - 1) & 1]), (uint32_t)((j - 1) >> 1) & 1u, kFusedWait);
-          if (ok) load(j + 1);
-        }
+        if (j == 0) continue;      // W1 serves stage 1 too
+        umma::commit(umma::smem_u32(&bar_wf[b]));  // block w is consumed once these MMAs are done
       }
       if (!ok) {
         atomicOr(a.status, J3DG_DEV_VISIT_CAP);
         // drain: the copies requested and the MMAs issued end before the
         // CTA frees its TMEM and shared memory (bounded as well)
-        for (int j = issued; j < loads; ++j)
-          umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[j & 1]), (uint32_t)(j >> 1) & 1u, kFusedWait);
-        if (issued > 0)
-          umma::mbar_wait_sleep(umma::smem_u32(&bar_wf[(issued - 1) & 1]), (uint32_t)((issued - 1) >> 1) & 1u,
-                                kFusedWait);
+        // (at most one block per buffer is still in flight)
+        for (int w = landed; w < loads; ++w)
+          umma::mbar_wait_sleep(umma::smem_u32(&bar_wl[w & 1]), (uint32_t)(w >> 1) & 1u, kFusedWait);
+        if (any_mma) {
+          umma::commit(umma::smem_u32(&bar_dr));
+          umma::mbar_wait_sleep(umma::smem_u32(&bar_dr), 0u, kFusedWait);
+        }
       }
     }
   } else if (ok) {
@@ -481,47 +537,77 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedA
     const int t = warp >> 2, row = (warp & 3) * 32 + lane;
     uint8_t* X = base + t * kTileBytes;
     const uint32_t r = blockIdx.x * 256u + (uint32_t)(t * 128 + row);
-    const uint32_t t_lane = taddr + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * 256);
+    const uint32_t tcol = taddr + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(t * 256);
+    const uint32_t bar_m = umma::smem_u32(&bar_md[t]), bar_c = umma::smem_u32(&bar_cf[t]);
     float v1 = -FLT_MAX, v2 = -FLT_MAX;
     uint32_t i1 = 0xffffffffu, i2 = 0xffffffffu;
-    {  // features of ray r (zeros past n; columns 192, 193 hold the ones of the bias rows), K = 208
-      float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      const bool live = r < a.n;
-      if (live) ray_inputs(a.rays + r, a.cx, a.cy, a.cz, a.inv_s, in6);
-      const __nv_bfloat162 zero = __floats2bfloat162_rn(0.f, 0.f), ones = __floats2bfloat162_rn(1.f, 1.f);
-#pragma unroll 1
-      for (int kg = 0; kg < kIn1 / 8; ++kg) {
-        uint32_t p[4];
+    // features of ray r (zeros past n; columns 192, 193 hold the ones of the
+    // bias rows), in two K parts: coordinates 0-2 and the first half of
+    // coordinate 3 (columns 0..111), then the rest (112..207)
+    float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool live = r < a.n;
+    if (live) ray_inputs(a.rays + r, a.cx, a.cy, a.cz, a.inv_s, in6);
+    const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+    {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int m = kg * 4 + q;
-          p[q] = bits2((live && m < 6 * kBands) ? feature_pair(in6, m) : (m == kBiasIn / 2 ? ones : zero));
+      for (int i = 0; i < 4; ++i) {
+        float sn[4], cn[4];
+        base_octave(in6[i], sn, cn);
+#pragma unroll
+        for (int o = 0; o < (i < 3 ? 4 : 2); ++o) {
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, (i * 4 + o) * 8, kIn1a / 8)) =
+              live ? octave_pairs(sn, cn) : zero4;
+          next_octave(sn, cn);
         }
-        *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kg * 8, kIn1 / 8)) = make_uint4(p[0], p[1], p[2], p[3]);
       }
     }
+    uint4 fb[12];  // columns 112..207: coordinate 3's last two octaves, coordinates 4, 5, the ones, zeros
+    {
+      float sn[4], cn[4];
+      base_octave(in6[3], sn, cn);
+      next_octave(sn, cn);
+      next_octave(sn, cn);
+      fb[0] = octave_pairs(sn, cn);
+      next_octave(sn, cn);
+      fb[1] = octave_pairs(sn, cn);
+#pragma unroll
+      for (int i = 4; i < 6; ++i) {
+        base_octave(in6[i], sn, cn);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+          fb[2 + (i - 4) * 4 + o] = octave_pairs(sn, cn);
+          if (o < 3) next_octave(sn, cn);
+        }
+      }
+      if (!live)
+        for (int g = 0; g < 10; ++g) fb[g] = zero4;
+      fb[10] = make_uint4(bits2(__floats2bfloat162_rn(1.f, 1.f)), 0u, 0u, 0u);
+      fb[11] = zero4;
+    }
     umma::fence_async_smem();
-    umma::mbar_arrive(umma::smem_u32(&bar_cf[t][0]));  // epilogue 0: the features
+    umma::mbar_arrive(bar_c);  // epilogue 0: the first feature part
 #pragma unroll 1
     for (int j = 0; j < kStages; ++j) {
-      const int b = j & 1;
-      ok = umma::mbar_wait_sleep(umma::smem_u32(&bar_md[t][b]), (uint32_t)(j >> 1) & 1u, kFusedWait);
+      ok = umma::mbar_wait_sleep(bar_m, (uint32_t)j & 1u, kFusedWait);
       if (!ok) break;
       umma::fence_after_sync();
-      const uint32_t tcol = t_lane + (uint32_t)(b * 128);
-      if (j < 4) {
+      if (j == 0) {  // the first part's MMAs have read their columns: the second part
+#pragma unroll
+        for (int g = 0; g < 12; ++g)
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, g * 8, (kIn1 - kIn1a) / 8)) = fb[g];
+        umma::fence_async_smem();
+      } else if (j < 5) {
         hidden_cols(tcol, X, row, 0);
         hidden_cols(tcol + 64, X, row, 64);
-        if (j == 0) {  // the bias block of layers 2..5: ones in columns 128, 129, zeros to 143
-          const uint32_t one2 = bits2(__floats2bfloat162_rn(1.f, 1.f));
-          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid, kHidB / 8)) = make_uint4(one2, 0u, 0u, 0u);
-          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid + 8, kHidB / 8)) = make_uint4(0u, 0u, 0u, 0u);
+        if (j == 1) {  // the bias block of layers 2..5: ones in columns 128, 129, zeros to 143
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid, kHidB / 8)) = fb[10];
+          *reinterpret_cast<uint4*>(X + umma::tile_offset(row, kHid + 8, kHidB / 8)) = zero4;
         }
         umma::fence_async_smem();
       } else {
-        const int c = (cs + j - 4) & (kChunks - 1);
+        const int c = (cs + j - 5) & (kChunks - 1);
 #pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < kChunkN / 64; ++h) {
           float v[64];
           umma::ld64(tcol + (uint32_t)(h * 64), v);  // the logits, biases included
           float m = -FLT_MAX;
@@ -550,7 +636,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_learned_fused(const FusedA
         }
       }
       umma::fence_before_sync();
-      umma::mbar_arrive(umma::smem_u32(&bar_cf[t][(j + 1) & 1]));  // epilogue j + 1
+      umma::mbar_arrive(bar_c);  // epilogue j + 1
     }
     if (!ok) {
       atomicOr(a.status, J3DG_DEV_VISIT_CAP);

@@ -1442,15 +1442,21 @@ __global__ void __launch_bounds__(256) k_top_flag_scan(const uint32_t* __restric
                                                        uint32_t* __restrict__ sums) {
   __shared__ uint32_t wsum[8];
   const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
-  uint32_t f[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t p = base + k;
-    if (p < n) {
-      const uint32_t t = task_of[p];
-      if (t < n_tasks) f[k] = top_goes_left(p, code[p], tasks[t], splits[t]);
+  uint32_t f[4] = {0u, 0u, 0u, 0u}, tk[4] = {kNoTask, kNoTask, kNoTask, kNoTask}, cd[4] = {0u, 0u, 0u, 0u};
+  if (base + 3 < n) {  // task_of, code: 16- and 8-byte aligned groups of 4
+    const uint4 t4 = *reinterpret_cast<const uint4*>(task_of + base);
+    const uint2 c4 = *reinterpret_cast<const uint2*>(code + base);
+    tk[0] = t4.x, tk[1] = t4.y, tk[2] = t4.z, tk[3] = t4.w;
+    cd[0] = c4.x & 0xffffu, cd[1] = c4.x >> 16, cd[2] = c4.y & 0xffffu, cd[3] = c4.y >> 16;
+  } else {
+    for (uint32_t k = 0; k < 4 && base + k < n; ++k) {
+      tk[k] = task_of[base + k];
+      cd[k] = code[base + k];
     }
   }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (tk[k] < n_tasks) f[k] = top_goes_left(base + k, cd[k], tasks[tk[k]], splits[tk[k]]);
   const uint32_t tot = f[0] + f[1] + f[2] + f[3];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t inc = tot;
@@ -1484,30 +1490,58 @@ __global__ void __launch_bounds__(256) k_top_flag_scan(const uint32_t* __restric
 // its task are the exclusive scan (chunk scan + chunk offset) at p minus that
 // at the task's first position; task_of2 gets each position's task of the
 // next level
-__global__ void k_top_scatter(const uint32_t* __restrict__ ord, uint32_t* __restrict__ ord2,
-                              const uint32_t* __restrict__ task_of, uint32_t* __restrict__ task_of2,
-                              const uint16_t* __restrict__ code, const TopTask* __restrict__ tasks,
-                              const TopSplit* __restrict__ splits, uint32_t n_tasks,
-                              const uint32_t* __restrict__ pscan, const uint32_t* __restrict__ sums, uint32_t n,
-                              uint32_t* status) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t t = task_of[p];
-  uint32_t d = p, next = kNoTask;
-  if (t < n_tasks) {
-    const TopTask T = tasks[t];
-    const TopSplit S = splits[t];
-    const uint32_t f = top_goes_left(p, code[p], T, S);
-    const uint32_t l = (pscan[p] + sums[p >> 10]) - (pscan[T.begin] + sums[T.begin >> 10]);
-    d = f ? T.begin + l : T.begin + S.nleft + (p - T.begin - l);
-    next = S.task[f ? 0 : 1];
-    if (d < T.begin || d >= T.end) {
-      atomicOr(status, J3DG_DEV_BAD_INDEX);
-      return;
+__global__ void __launch_bounds__(256) k_top_scatter(const uint32_t* __restrict__ ord, uint32_t* __restrict__ ord2,
+                                                     const uint32_t* __restrict__ task_of,
+                                                     uint32_t* __restrict__ task_of2, const uint16_t* __restrict__ code,
+                                                     const TopTask* __restrict__ tasks,
+                                                     const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                                                     const uint32_t* __restrict__ pscan,
+                                                     const uint32_t* __restrict__ sums, uint32_t n, uint32_t* status) {
+  // 4 consecutive positions per thread (one chunk of the scan: base is a multiple of 4)
+  const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+  if (base >= n) return;
+  uint32_t tk[4] = {kNoTask, kNoTask, kNoTask, kNoTask}, cd[4] = {0u, 0u, 0u, 0u}, ps[4] = {0u, 0u, 0u, 0u},
+           od[4] = {0u, 0u, 0u, 0u};
+  const uint32_t m = min(4u, n - base);
+  if (m == 4) {
+    const uint4 t4 = *reinterpret_cast<const uint4*>(task_of + base);
+    const uint2 c4 = *reinterpret_cast<const uint2*>(code + base);
+    const uint4 p4 = *reinterpret_cast<const uint4*>(pscan + base);
+    const uint4 o4 = *reinterpret_cast<const uint4*>(ord + base);
+    tk[0] = t4.x, tk[1] = t4.y, tk[2] = t4.z, tk[3] = t4.w;
+    cd[0] = c4.x & 0xffffu, cd[1] = c4.x >> 16, cd[2] = c4.y & 0xffffu, cd[3] = c4.y >> 16;
+    ps[0] = p4.x, ps[1] = p4.y, ps[2] = p4.z, ps[3] = p4.w;
+    od[0] = o4.x, od[1] = o4.y, od[2] = o4.z, od[3] = o4.w;
+  } else {
+    for (uint32_t k = 0; k < m; ++k) {
+      tk[k] = task_of[base + k];
+      cd[k] = code[base + k];
+      ps[k] = pscan[base + k];
+      od[k] = ord[base + k];
     }
   }
-  ord2[d] = ord[p];
-  task_of2[d] = next;
+  const uint32_t chunk_off = sums[base >> 10];
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    if (k >= m) break;
+    const uint32_t p = base + k, t = tk[k];
+    uint32_t d = p, next = kNoTask;
+    if (t < n_tasks) {
+      const TopTask T = tasks[t];
+      const TopSplit S = splits[t];
+      const uint32_t f = top_goes_left(p, cd[k], T, S);
+      // lefts before p within its task: the exclusive scan at p minus that at the task's first position
+      const uint32_t l = (ps[k] + chunk_off) - (pscan[T.begin] + sums[T.begin >> 10]);
+      d = f ? T.begin + l : T.begin + S.nleft + (p - T.begin - l);
+      next = S.task[f ? 0 : 1];
+      if (d < T.begin || d >= T.end) {
+        atomicOr(status, J3DG_DEV_BAD_INDEX);
+        continue;
+      }
+    }
+    ord2[d] = od[k];
+    task_of2[d] = next;
+  }
 }
 
 // children of every task: a new task above J3DG_SAH_TOP triangles, else a
@@ -1516,7 +1550,7 @@ __global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __re
                                uint32_t n_tasks, uint32_t seg_max, uint32_t* __restrict__ counters,
                                TopTask* __restrict__ next, TopRange* __restrict__ ranges, uint2* __restrict__ child,
                                uint32_t cap_tasks, uint32_t cap_ranges, uint32_t max_nodes, uint32_t* status) {
-  // counters: [0] nodes allocated, [1] next tasks, [2] ranges
+  // counters: [0] nodes allocated, [1] next tasks, [2] ranges, [3] largest next task
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tasks) return;
   const TopTask T = tasks[t];
@@ -1542,6 +1576,7 @@ __global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __re
         ref[side] = kPendingRef;
         continue;
       }
+      atomicMax(counters + 3, e - b);  // the next level's largest task
       TopTask C;
       C.begin = b;
       C.end = e;
@@ -1672,7 +1707,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   TopSplit* splits = nullptr;
   TopRange* ranges = nullptr;
   std::vector<uint32_t> top_end;  // top nodes of level L end at top_end[L]
-  uint32_t n_top = 0, n_ranges = 0, n_seg = 1, hctr[3] = {0, 0, 0};
+  uint32_t n_top = 0, n_ranges = 0, n_seg = 1, hctr[4] = {0, 0, 0, 0};
   bool top = false;
   const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
   const uint32_t hist_n = 256 * n_tiles;
@@ -1787,7 +1822,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       J3DG_CK(cudaMallocAsync((void**)&seg_starts, sizeof(uint32_t) * nt, st));
       J3DG_CK(cudaMallocAsync((void**)&seg_scan, sizeof(uint32_t) * nt, st));
       J3DG_CK(cudaMallocAsync((void**)&top_bins, sizeof(uint32_t) * bin_words, st));
-      J3DG_CK(cudaMallocAsync((void**)&top_ctr, sizeof(uint32_t) * 3, st));
+      J3DG_CK(cudaMallocAsync((void**)&top_ctr, sizeof(uint32_t) * 4, st));
       J3DG_CK(cudaMallocAsync((void**)&tasks_a, sizeof(TopTask) * cap_tasks, st));
       J3DG_CK(cudaMallocAsync((void**)&tasks_b, sizeof(TopTask) * cap_tasks, st));
       J3DG_CK(cudaMallocAsync((void**)&splits, sizeof(TopSplit) * cap_tasks, st));
@@ -1804,27 +1839,34 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
       }
       hctr[0] = 1u;  // nodes allocated (the root)
       hctr[1] = hctr[2] = 0u;
+      hctr[3] = nt;  // the largest task: the root
       J3DG_CK(cudaMemcpyAsync(top_ctr, hctr, sizeof(hctr), cudaMemcpyHostToDevice, st));
       k_iota<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, nt);
       J3DG_CK(cudaMemsetAsync(task_of, 0, sizeof(uint32_t) * nt, st));
       top_end.push_back(1u);
       uint32_t n_tasks = 1;
       while (n_tasks > 0) {
-        const uint32_t words = n_tasks * 3 * kTopBins * kTopVals;
-        k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words, tasks_a);
-        k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
-                                                                     n_tasks, nt, top_bins, codes);
+        // levels whose tasks are all at most kTopWarpTask triangles need
+        // only the per-warp binning (which splits them too)
+        if (hctr[3] > kTopWarpTask) {
+          const uint32_t words = n_tasks * 3 * kTopBins * kTopVals;
+          k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words, tasks_a);
+          k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
+                                                                       n_tasks, nt, top_bins, codes);
+        }
         k_top_bin_warp<<<(n_tasks + 7) / 8, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, tasks_a, n_tasks, splits, box,
                                                           count, codes);
-        k_top_split<<<(n_tasks + 3) / 4, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
+        if (hctr[3] > kTopWarpTask)
+          k_top_split<<<(n_tasks + 3) / 4, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
         J3DG_CK(cudaMemsetAsync(top_ctr + 1, 0, sizeof(uint32_t), st));
+        J3DG_CK(cudaMemsetAsync(top_ctr + 3, 0, sizeof(uint32_t), st));
         k_top_children<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, splits, n_tasks, J3DG_SAH_TOP, top_ctr,
                                                                tasks_b, ranges, child, cap_tasks, nt, nt - 1,
                                                                d_status);
         k_top_flag_scan<<<sblocks_max, 256, 0, st>>>(task_of, codes, tasks_a, splits, n_tasks, nt, cscan, pl_sums);
         k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, nullptr, sblocks_max, nullptr);
-        k_top_scatter<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, codes, tasks_a, splits,
-                                                        n_tasks, cscan, pl_sums, nt, d_status);
+        k_top_scatter<<<(nt + 1023) / 1024, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, codes, tasks_a, splits,
+                                                          n_tasks, cscan, pl_sums, nt, d_status);
         std::swap(ord_a, ord_b);
         std::swap(task_of, task_of2);
         J3DG_CK(cudaGetLastError());

@@ -140,7 +140,7 @@ __global__ void k_tri_prep(const float* __restrict__ V, uint32_t nv, const uint3
 // ------------------------------------------------------ 3. radix sort ----
 
 static const int kSortThreads = 256;
-static const int kSortItems = 16;
+static const int kSortItems = 8;  // tiles of 2048 keys: the scatter's shared-memory reorder fits 34 KB
 static const int kSortTile = kSortThreads * kSortItems;
 
 __global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift, uint32_t num_tiles,
@@ -267,13 +267,25 @@ __global__ void __launch_bounds__(256) k_scan_add(uint32_t* __restrict__ out, ui
   }
 }
 
-__global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n, int shift,
-                                uint32_t num_tiles, const uint32_t* __restrict__ offsets,
-                                const uint32_t* __restrict__ chunk_offsets, uint32_t* status) {
-  __shared__ uint32_t base[256];
+// One tile of kSortTile keys per block: each key's rank among the tile's
+// keys of its digit comes from kSortItems rounds of 256 keys (warp
+// match_any ranks, per-warp digit counts scanned across the warps, a
+// running count per digit); the tile is then reordered by digit in shared
+// memory (stable) and written out so that consecutive threads write
+// consecutive positions of one digit's run (coalesced, instead of one
+// scattered 8-byte write per key).
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* __restrict__ kin,
+                                                                const uint32_t* __restrict__ vin,
+                                                                uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                                uint32_t n, int shift, uint32_t num_tiles,
+                                                                const uint32_t* __restrict__ offsets,
+                                                                const uint32_t* __restrict__ chunk_offsets,
+                                                                uint32_t* status) {
+  __shared__ uint32_t base[256];     // global position of the tile's first key of each digit
+  __shared__ uint32_t run[256];      // keys of each digit in the tile's earlier rounds, then the digit's local start
   __shared__ uint32_t wc[kSortThreads / 32][257];
-  __shared__ uint32_t total[256];
+  __shared__ uint64_t sk[kSortTile];
+  __shared__ uint32_t sv[kSortTile];
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   {
     // offsets: the digit histogram's scan within chunks of 1024 entries;
@@ -281,42 +293,79 @@ __global__ void k_radix_scatter(const uint64_t* __restrict__ kin, const uint32_t
     const size_t h = (size_t)tid * num_tiles + blockIdx.x;
     base[tid] = offsets[h] + chunk_offsets[h >> 10];
   }
-  size_t tile = (size_t)blockIdx.x * kSortTile;
+  run[tid] = 0;
+  const size_t tile = (size_t)blockIdx.x * kSortTile;
+  uint64_t key[kSortItems];
+  uint32_t rnk[kSortItems];  // digit (low 9 bits: 256 = no key) and rank within the tile's digit
+#pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
     for (int w = 0; w < kSortThreads / 32; ++w) wc[w][tid] = 0;
     if (tid == 0)
       for (int w = 0; w < kSortThreads / 32; ++w) wc[w][256] = 0;
     __syncthreads();
-    size_t idx = tile + (size_t)j * kSortThreads + tid;
-    bool valid = idx < n;
-    uint64_t k = valid ? kin[idx] : 0;
-    uint32_t d = valid ? (uint32_t)((k >> shift) & 255u) : 256u;
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
-    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    const size_t idx = tile + (size_t)j * kSortThreads + tid;
+    const bool valid = idx < n;
+    const uint64_t k = valid ? kin[idx] : 0;
+    const uint32_t d = valid ? (uint32_t)((k >> shift) & 255u) : 256u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
     if (rank == 0) wc[warp][d] = __popc(peers);
     __syncthreads();
+    uint32_t tot = 0;
     {
-      uint32_t run = 0;
+      uint32_t acc = 0;
       for (int w = 0; w < kSortThreads / 32; ++w) {
-        uint32_t c = wc[w][tid];
-        wc[w][tid] = run;
-        run += c;
+        const uint32_t c = wc[w][tid];
+        wc[w][tid] = acc;
+        acc += c;
       }
-      total[tid] = run;
+      tot = acc;
     }
     __syncthreads();
-    if (valid) {
-      uint32_t pos = base[d] + wc[warp][d] + rank;
-      if (pos < n) {
-        kout[pos] = k;
-        vout[pos] = vin[idx];
-      } else {
-        atomicOr(status, J3DG_DEV_BAD_INDEX);
-      }
+    key[j] = k;
+    rnk[j] = d | ((valid ? run[d] + wc[warp][d] + rank : 0u) << 9);
+    __syncthreads();
+    run[tid] += tot;
+  }
+  __syncthreads();
+  // the digits' starts within the tile: exclusive scan of the counts (run)
+  {
+    const uint32_t c = run[tid];
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
     }
+    if (lane == 31) wc[0][warp] = incl;
     __syncthreads();
-    base[tid] += total[tid];
+    uint32_t woff = 0;
+    for (uint32_t w = 0; w < warp; ++w) woff += wc[0][w];
     __syncthreads();
+    run[tid] = woff + incl - c;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    const uint32_t d = rnk[j] & 511u;
+    if (d < 256u) {
+      const uint32_t l = run[d] + (rnk[j] >> 9);
+      sk[l] = key[j];
+      sv[l] = vin[tile + (size_t)j * kSortThreads + tid];
+    }
+  }
+  __syncthreads();
+  const uint32_t tile_n = (uint32_t)min((size_t)kSortTile, (size_t)n - tile);
+  for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
+    const uint64_t k = sk[i];
+    const uint32_t d = (uint32_t)((k >> shift) & 255u);
+    const uint32_t pos = base[d] + (i - run[d]);
+    if (pos < n) {
+      kout[pos] = k;
+      vout[pos] = sv[i];
+    } else {
+      atomicOr(status, J3DG_DEV_BAD_INDEX);
+    }
   }
 }
 
@@ -779,12 +828,14 @@ template <int W>
 __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode* __restrict__ box,
                                  const uint32_t* __restrict__ count, const float4* __restrict__ tris,
                                  const PlaceItem* __restrict__ qin, uint32_t n_in, PlaceItem* __restrict__ qout,
-                                 uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
+                                 uint32_t* __restrict__ n_out, uint32_t wide_base, float4* __restrict__ wide,
                                  uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
                                  uint32_t nt, uint32_t* status, const uint8_t* __restrict__ dec) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_in) return;
-  const PlaceItem it = qin[t];
+  // whole warps stay to the end (the next level's slots are allocated per
+  // warp); lanes past n_in place nothing
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31u;
+  const bool valid = t < n_in;
+  const PlaceItem it = valid ? qin[t] : PlaceItem{0u, 0u, 0u, 0u};
   uint32_t ref[W], cnt[W], start[W];
   float4 lo[W], hi[W];
   auto load = [&](uint32_t r, int s, uint32_t first) {
@@ -799,9 +850,10 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
       cnt[s] = count[r];
     }
   };
-  const uint2 c = child[it.bin];
+  const uint2 c = valid ? child[it.bin] : make_uint2(0u, 0u);
   int m = 0;
-  if (dec) {
+  if (!valid) {
+  } else if (dec) {
     // the slots the cost decisions give: expand(left, k) then expand(right, W - k)
     struct Slot {
       uint32_t r, i, start;
@@ -833,7 +885,7 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     load(c.y, 1, it.start + cnt[0]);
     m = 2;
   }
-  while (!dec && m < W) {
+  while (valid && !dec && m < W) {
     int best = -1;
     float ba = -1.f;
     for (int s = 0; s < m; ++s)
@@ -851,6 +903,29 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     load(cc.y, m, s0 + cnt[best]);
     ++m;
   }
+  // slots placed as leaves, and the next level's queue slots for the rest:
+  // one atomic per warp (a warp-wide scan of the lanes' internal slots)
+  uint32_t leaf_mask = 0u, n_int = 0u;
+  for (int s = 0; s < m; ++s) {
+    const bool as_leaf = (ref[s] & 0x80000000u) ||
+                         (dec ? (dec[(size_t)ref[s] * W] & 0x80u) != 0 : cnt[s] <= leaf_size);
+    if (as_leaf && cnt[s] <= J3DG_MAX_LEAF)
+      leaf_mask |= 1u << s;
+    else
+      ++n_int;
+  }
+  uint32_t incl = n_int;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  uint32_t q_base = 0u;
+  if (lane == 31u && incl > 0u) q_base = atomicAdd(n_out, incl);
+  uint32_t q = __shfl_sync(0xffffffffu, q_base, 31) + incl - n_int;  // this lane's first queue slot
+  const uint32_t dmax = __reduce_max_sync(0xffffffffu, valid ? it.depth : 0u);
+  if (lane == 0u && dmax > 0u) atomicMax(max_depth, dmax);
+  if (!valid) return;
   // the node in the width-W layout: planes [6][W], refs [W], zero padding
   float F[4 * J3DG_NODE_F4(W)];
 #pragma unroll
@@ -864,9 +939,7 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
       F[3 * W + s] = hi[s].y;
       F[4 * W + s] = lo[s].z;
       F[5 * W + s] = hi[s].z;
-      const bool as_leaf = (ref[s] & 0x80000000u) ||
-                           (dec ? (dec[(size_t)ref[s] * W] & 0x80u) != 0 : cnt[s] <= leaf_size);
-      if (as_leaf && cnt[s] <= J3DG_MAX_LEAF) {
+      if (leaf_mask & (1u << s)) {
         out_ref = J3DG_LEAF_BIT | (start[s] << 3) | (cnt[s] - 1u);
         uint32_t stk[J3DG_MAX_LEAF];
         int sp = 0;
@@ -893,10 +966,10 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
           }
         }
       } else {
-        const uint32_t w = atomicAdd(n_wide, 1u);
-        const uint32_t q = atomicAdd(n_out, 1u);
-        qout[q] = PlaceItem{ref[s], w, it.depth + 1, start[s]};
-        out_ref = w;
+        // the next level's wide nodes follow this level's, in queue order
+        qout[q] = PlaceItem{ref[s], wide_base + q, it.depth + 1, start[s]};
+        out_ref = wide_base + q;
+        ++q;
       }
     } else {
       F[0 * W + s] = F[2 * W + s] = F[4 * W + s] = 3.4e38f;
@@ -907,7 +980,6 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
   float4* Wn = wide + J3DG_NODE_F4(W) * (size_t)it.wide;
 #pragma unroll
   for (int k = 0; k < J3DG_NODE_F4(W); ++k) Wn[k] = make_float4(F[4 * k], F[4 * k + 1], F[4 * k + 2], F[4 * k + 3]);
-  atomicMax(max_depth, it.depth);
 }
 
 // ------------------------------------------------ 7. depth-first order ----
@@ -1034,18 +1106,18 @@ static void launch_collapse_cost(uint32_t W, const uint2* child, const BinNode* 
 
 static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
                                   const float4* tris, const PlaceItem* qin, uint32_t n_in, PlaceItem* qout,
-                                  uint32_t* n_out, uint32_t* n_wide, float4* wide, uint32_t leaf_size,
+                                  uint32_t* n_out, uint32_t wide_base, float4* wide, uint32_t leaf_size,
                                   uint32_t* max_depth, float4* tris_out, uint32_t nt, uint32_t* status,
                                   const uint8_t* dec, cudaStream_t st) {
   const uint32_t blocks = (n_in + 127) / 128;
   if (W == 2)
-    k_collapse_place<2><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+    k_collapse_place<2><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
                                                 max_depth, tris_out, nt, status, dec);
   else if (W == 8)
-    k_collapse_place<8><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+    k_collapse_place<8><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
                                                 max_depth, tris_out, nt, status, dec);
   else
-    k_collapse_place<4><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, n_wide, wide, leaf_size,
+    k_collapse_place<4><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
                                                 max_depth, tris_out, nt, status, dec);
 }
 
@@ -1994,16 +2066,26 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     hc[3] = 0u;  // max depth
     J3DG_CK(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
     n_in = 1;
-    while (n_in > 0) {
-      J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
-      launch_collapse_place(W, child, box, count, (const float4*)m->d_tris, pa, n_in, pb, counters + 2, counters + 1,
-                            wide, m->leaf_size, counters + 3, tris_out, nt, d_status, dp_dec, st);
-      J3DG_CK(cudaGetLastError());
-      J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
-      J3DG_CK(cudaStreamSynchronize(st));
-      n_in = hc[2];
-      if (hc[1] > level_end.back()) level_end.push_back(hc[1]);
-      std::swap(pa, pb);
+    {
+      uint32_t n_wide = 1;  // wide nodes allocated (the root); a level's nodes follow the previous level's
+      while (n_in > 0) {
+        J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
+        launch_collapse_place(W, child, box, count, (const float4*)m->d_tris, pa, n_in, pb, counters + 2, n_wide, wide,
+                              m->leaf_size, counters + 3, tris_out, nt, d_status, dp_dec, st);
+        J3DG_CK(cudaGetLastError());
+        J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        J3DG_CK(cudaStreamSynchronize(st));
+        n_in = hc[2];
+        if (n_in > nt - n_wide) {
+          err = "BVH collapse overran its node bound";
+          rc = J3DG_ERR_CUDA;
+          goto cleanup;
+        }
+        n_wide += n_in;
+        if (n_wide > level_end.back()) level_end.push_back(n_wide);
+        std::swap(pa, pb);
+      }
+      hc[1] = n_wide;
     }
     m->n_nodes = hc[1];
     m->max_depth = hc[3];

@@ -36,7 +36,7 @@ namespace {
 const uint32_t kInstSlots = 8;
 
 // bytes the device's default pool keeps reserved between calls (build scratch)
-const uint64_t kKeepReserved = 16ull << 30;
+const uint64_t kKeepReserved = 24ull << 30;
 
 // canvas scratch per pixel: raster keys, shadow jobs and tables during a
 // frame; the point-cloud splat's depth keys after it
@@ -535,8 +535,8 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
   c->copy_stream = cst;
   // the device's default stream-ordered pool (BVH build scratch, query
   // buffers) keeps up to kKeepReserved bytes mapped between calls: a build
-  // then reuses the previous build's pages instead of mapping ~11 GB again
-  // (28M triangles) after every synchronisation released them
+  // then reuses the previous build's pages instead of mapping its scratch
+  // (~20 GB for 28M triangles) again after every synchronisation released them
   {
     cudaMemPool_t dflt = nullptr;
     uint64_t keep_bytes = kKeepReserved;

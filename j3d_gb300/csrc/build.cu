@@ -207,7 +207,11 @@ __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* in, uint32_
 }
 
 __global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ sums_a, uint32_t* __restrict__ sums_b,
-                                                    uint32_t n, uint32_t* __restrict__ totals) {
+                                                    uint32_t n, uint32_t* __restrict__ totals,
+                                                    const uint32_t* __restrict__ len_p = nullptr) {
+  // len_p (if given): the scanned list's length in device memory; the chunk
+  // totals to scan are then ceil(len / 1024)
+  if (len_p) n = (*len_p + 1023u) / 1024u;
   // single block of 1024 threads, over one array of chunk totals (sums_b
   // null) or two: each thread sums a strip of consecutive chunk totals, the
   // strip sums are scanned by warp shuffles (within each warp, then the 32
@@ -593,37 +597,44 @@ __device__ __forceinline__ float merged_area(float4 alo, float4 ahi, float4 blo,
 // list position, all 0 for one segment); a cluster alone in its segment gets
 // no neighbour (0xffffffff) and so never merges.
 __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict__ lo, const float4* __restrict__ hi,
-                                                       const uint32_t* __restrict__ seg, uint32_t m,
-                                                       uint32_t* __restrict__ nn) {
+                                                       const uint32_t* __restrict__ seg,
+                                                       const uint32_t* __restrict__ m_p,
+                                                       const uint32_t* __restrict__ n_seg_p, uint32_t* __restrict__ nn) {
   __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
   __shared__ uint32_t sseg[kPlocBlock + 2 * kPlocRadius];
-  const int base = (int)(blockIdx.x * kPlocBlock) - kPlocRadius;
-  for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += blockDim.x) {
-    const int j = base + k;
-    if (j >= 0 && j < (int)m) {
-      slo[k] = lo[j];
-      shi[k] = hi[j];
-      sseg[k] = seg[j];
+  const uint32_t m = *m_p;
+  if (m <= *n_seg_p) return;  // every segment is one cluster: no round
+  for (uint32_t tile = blockIdx.x; tile * kPlocBlock < m; tile += gridDim.x) {  // uniform over the block
+    const int base = (int)(tile * kPlocBlock) - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += blockDim.x) {
+      const int j = base + k;
+      if (j >= 0 && j < (int)m) {
+        slo[k] = lo[j];
+        shi[k] = hi[j];
+        sseg[k] = seg[j];
+      }
     }
-  }
-  __syncthreads();
-  const int i = (int)(blockIdx.x * kPlocBlock + threadIdx.x);
-  if (i >= (int)m) return;
-  const int si = threadIdx.x + kPlocRadius;
-  const float4 alo = slo[si], ahi = shi[si];
-  const uint32_t my = sseg[si];
-  float best = INFINITY;
-  uint32_t bj = 0xffffffffu;
-  for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
-    const int j = i + o;
-    if (o == 0 || j < 0 || j >= (int)m || sseg[si + o] != my) continue;
-    const float a = merged_area(alo, ahi, slo[si + o], shi[si + o]);
-    if (a < best) {  // increasing j: the first of equal areas is the smaller position
-      best = a;
-      bj = (uint32_t)j;
+    __syncthreads();
+    const int i = (int)(tile * kPlocBlock + threadIdx.x);
+    if (i < (int)m) {
+      const int si = threadIdx.x + kPlocRadius;
+      const float4 alo = slo[si], ahi = shi[si];
+      const uint32_t my = sseg[si];
+      float best = INFINITY;
+      uint32_t bj = 0xffffffffu;
+      for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
+        const int j = i + o;
+        if (o == 0 || j < 0 || j >= (int)m || sseg[si + o] != my) continue;
+        const float a = merged_area(alo, ahi, slo[si + o], shi[si + o]);
+        if (a < best) {  // increasing j: the first of equal areas is the smaller position
+          best = a;
+          bj = (uint32_t)j;
+        }
+      }
+      nn[i] = bj;
     }
+    __syncthreads();  // the tile's shared copies are read before the next tile overwrites them
   }
-  nn[i] = bj;
 }
 
 // a PLOC round's two compactions in one pass: position i creates a node if it
@@ -632,10 +643,13 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const float4* __restrict
 // positions (256 threads x 4) writes the exclusive scans of both flags
 // within the chunk (cps, sps) and its two totals (csum, ssum; scanned by
 // k_scan_sums, whose grand totals are the round's creates and survivors).
-__global__ void __launch_bounds__(256) k_ploc_flag_scan(const uint32_t* __restrict__ nn, uint32_t m,
+__global__ void __launch_bounds__(256) k_ploc_flag_scan(const uint32_t* __restrict__ nn, const uint32_t* __restrict__ m_p,
+                                                        const uint32_t* __restrict__ n_seg_p,
                                                         uint32_t* __restrict__ cps, uint32_t* __restrict__ sps,
                                                         uint32_t* __restrict__ csum, uint32_t* __restrict__ ssum) {
   __shared__ uint32_t wsum[2][8];
+  const uint32_t m = *m_p;
+  if (m <= *n_seg_p || blockIdx.x * 1024u >= m) return;  // no round, or past the list
   const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
   uint32_t c[4] = {0u, 0u, 0u, 0u}, v[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -693,16 +707,15 @@ __global__ void __launch_bounds__(256) k_ploc_flag_scan(const uint32_t* __restri
   }
 }
 
-__global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
-                             const float4* __restrict__ hi, const uint32_t* __restrict__ seg,
-                             const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cps,
-                             const uint32_t* __restrict__ sps, const uint32_t* __restrict__ csum,
-                             const uint32_t* __restrict__ ssum, uint32_t m, uint32_t node_base,
-                             uint32_t* __restrict__ C2, float4* __restrict__ lo2, float4* __restrict__ hi2,
-                             uint32_t* __restrict__ seg2, uint2* __restrict__ child, BinNode* __restrict__ box,
-                             uint32_t* __restrict__ count) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+__device__ __forceinline__ void ploc_merge_one(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
+                                               const float4* __restrict__ hi, const uint32_t* __restrict__ seg,
+                                               const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cps,
+                                               const uint32_t* __restrict__ sps, const uint32_t* __restrict__ csum,
+                                               const uint32_t* __restrict__ ssum, uint32_t i, uint32_t m,
+                                               uint32_t node_base, uint32_t* __restrict__ C2,
+                                               float4* __restrict__ lo2, float4* __restrict__ hi2,
+                                               uint32_t* __restrict__ seg2, uint2* __restrict__ child,
+                                               BinNode* __restrict__ box, uint32_t* __restrict__ count) {
   const uint32_t j = nn[i];
   const bool mutual = j < m && nn[j] == i;
   if (mutual && i > j) return;  // merged into the node made at j
@@ -725,6 +738,21 @@ __global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __res
   C2[pos] = p;
   lo2[pos] = l;
   hi2[pos] = h;
+}
+
+__global__ void k_ploc_merge(const uint32_t* __restrict__ C, const float4* __restrict__ lo,
+                             const float4* __restrict__ hi, const uint32_t* __restrict__ seg,
+                             const uint32_t* __restrict__ nn, const uint32_t* __restrict__ cps,
+                             const uint32_t* __restrict__ sps, const uint32_t* __restrict__ csum,
+                             const uint32_t* __restrict__ ssum, const uint32_t* __restrict__ m_p,
+                             const uint32_t* __restrict__ n_seg_p, const uint32_t* __restrict__ node_base_p,
+                             uint32_t* __restrict__ C2, float4* __restrict__ lo2, float4* __restrict__ hi2,
+                             uint32_t* __restrict__ seg2, uint2* __restrict__ child, BinNode* __restrict__ box,
+                             uint32_t* __restrict__ count) {
+  const uint32_t m = *m_p, node_base = *node_base_p;
+  if (m <= *n_seg_p) return;  // no round
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    ploc_merge_one(C, lo, hi, seg, nn, cps, sps, csum, ssum, i, m, node_base, C2, lo2, hi2, seg2, child, box, count);
 }
 
 // ------------------------------------------- 6b. cost-optimal collapse ----
@@ -771,11 +799,10 @@ __device__ __forceinline__ void sub_costs(const float* __restrict__ cost, const 
 // (dec[0] = the k of the node case | 0x80 when the leaf case is cheaper;
 // dec[i - 1], i = 2..W: 0 = as i - 1, else the k of the best split)
 template <int W>
-__global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* __restrict__ box,
-                                const uint32_t* __restrict__ count, const float4* __restrict__ tris, uint32_t lo,
-                                uint32_t hi, uint32_t leaf_size, float* __restrict__ cost, uint8_t* __restrict__ dec) {
-  const uint32_t n = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= hi) return;
+__device__ __forceinline__ void collapse_cost_one(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                                  const uint32_t* __restrict__ count, const float4* __restrict__ tris,
+                                                  uint32_t n, uint32_t leaf_size, float* __restrict__ cost,
+                                                  uint8_t* __restrict__ dec) {
   const uint2 c = child[n];
   float cl[W + 1], cr[W + 1], C[W + 1];
   sub_costs<W>(cost, tris, c.x, cl);
@@ -814,6 +841,17 @@ __global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* 
   }
 }
 
+template <int W>
+__global__ void k_collapse_cost(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                const uint32_t* __restrict__ count, const float4* __restrict__ tris,
+                                const uint32_t* __restrict__ lohi, uint32_t leaf_size, float* __restrict__ cost,
+                                uint8_t* __restrict__ dec) {
+  // the pass's binary nodes [lohi[0], lohi[1]) (device memory)
+  const uint32_t lo = lohi[0], hi = lohi[1];
+  for (uint32_t n = lo + blockIdx.x * blockDim.x + threadIdx.x; n < hi; n += gridDim.x * blockDim.x)
+    collapse_cost_one<W>(child, box, count, tris, n, leaf_size, cost, dec);
+}
+
 struct PlaceItem {
   uint32_t bin;    // binary node index
   uint32_t wide;   // wide node index to fill
@@ -825,15 +863,16 @@ struct PlaceItem {
 // sorted leaves: each slot carries its subtree's first position; leaves are
 // written to tris_out at those positions in depth-first order.
 template <int W>
-__global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode* __restrict__ box,
-                                 const uint32_t* __restrict__ count, const float4* __restrict__ tris,
-                                 const PlaceItem* __restrict__ qin, uint32_t n_in, PlaceItem* __restrict__ qout,
-                                 uint32_t* __restrict__ n_out, uint32_t wide_base, float4* __restrict__ wide,
-                                 uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
-                                 uint32_t nt, uint32_t* status, const uint8_t* __restrict__ dec) {
-  // whole warps stay to the end (the next level's slots are allocated per
+__device__ __forceinline__ void collapse_place_one(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                                   const uint32_t* __restrict__ count, const float4* __restrict__ tris,
+                                                   const PlaceItem* __restrict__ qin, uint32_t t, uint32_t n_in,
+                                                   PlaceItem* __restrict__ qout, uint32_t* __restrict__ n_out,
+                                                   uint32_t wide_base, float4* __restrict__ wide, uint32_t leaf_size,
+                                                   uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
+                                                   uint32_t nt, uint32_t* status, const uint8_t* __restrict__ dec) {
+  // whole warps come here together (the next level's slots are allocated per
   // warp); lanes past n_in place nothing
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31u;
+  const uint32_t lane = threadIdx.x & 31u;
   const bool valid = t < n_in;
   const PlaceItem it = valid ? qin[t] : PlaceItem{0u, 0u, 0u, 0u};
   uint32_t ref[W], cnt[W], start[W];
@@ -967,7 +1006,13 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
         }
       } else {
         // the next level's wide nodes follow this level's, in queue order
-        qout[q] = PlaceItem{ref[s], wide_base + q, it.depth + 1, start[s]};
+        // (the queue and the node array hold nt entries: a malformed tree
+        // is stopped here)
+        if (q < nt && wide_base + q < nt) {
+          qout[q] = PlaceItem{ref[s], wide_base + q, it.depth + 1, start[s]};
+        } else {
+          atomicOr(status, J3DG_DEV_BAD_INDEX);
+        }
         out_ref = wide_base + q;
         ++q;
       }
@@ -977,9 +1022,30 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
     }
     F[6 * W + s] = __uint_as_float(out_ref);
   }
+  if (it.wide >= nt) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    return;
+  }
   float4* Wn = wide + J3DG_NODE_F4(W) * (size_t)it.wide;
 #pragma unroll
   for (int k = 0; k < J3DG_NODE_F4(W); ++k) Wn[k] = make_float4(F[4 * k], F[4 * k + 1], F[4 * k + 2], F[4 * k + 3]);
+}
+
+// a level of the placement: the queue's n_in items (device memory) with
+// their wide nodes from wide_base on (device memory); warp-uniform strides
+template <int W>
+__global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                 const uint32_t* __restrict__ count, const float4* __restrict__ tris,
+                                 const PlaceItem* __restrict__ qin, const uint32_t* __restrict__ n_in_p,
+                                 PlaceItem* __restrict__ qout, uint32_t* __restrict__ n_out,
+                                 const uint32_t* __restrict__ wide_base_p, float4* __restrict__ wide,
+                                 uint32_t leaf_size, uint32_t* __restrict__ max_depth, float4* __restrict__ tris_out,
+                                 uint32_t nt, uint32_t* status, const uint8_t* __restrict__ dec) {
+  const uint32_t n_in = *n_in_p, wide_base = *wide_base_p;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t t0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); t0 < n_in; t0 += stride)
+    collapse_place_one<W>(child, box, count, tris, qin, t0 + (threadIdx.x & 31u), n_in, qout, n_out, wide_base, wide,
+                          leaf_size, max_depth, tris_out, nt, status, dec);
 }
 
 // ------------------------------------------------ 7. depth-first order ----
@@ -1006,38 +1072,41 @@ __device__ __forceinline__ void child_refs(const float4* __restrict__ wide, uint
 
 // size[i] = wide nodes in the subtree of i (children of level lo..hi are done)
 template <int W>
-__global__ void k_dfs_size(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, uint32_t* __restrict__ size) {
-  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
-  uint32_t r[W], s = 1;
-  child_refs<W>(wide, i, r);
+__global__ void k_dfs_size(const float4* __restrict__ wide, const uint32_t* __restrict__ lohi,
+                           uint32_t* __restrict__ size) {
+  const uint32_t lo = lohi[0], hi = lohi[1];  // the level's nodes (device memory)
+  for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+    uint32_t r[W], s = 1;
+    child_refs<W>(wide, i, r);
 #pragma unroll
-  for (int c = 0; c < W; ++c)
-    if (!(r[c] & J3DG_LEAF_BIT)) s += size[r[c]];  // the empty ref has the leaf bit
-  size[i] = s;
+    for (int c = 0; c < W; ++c)
+      if (!(r[c] & J3DG_LEAF_BIT)) s += size[r[c]];  // the empty ref has the leaf bit
+    size[i] = s;
+  }
 }
 
 // children of the level's nodes take consecutive ranges after their parent
 template <int W>
-__global__ void k_dfs_place(const float4* __restrict__ wide, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ size,
-                            uint32_t* __restrict__ pos) {
-  const uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= hi) return;
-  uint32_t r[W], next = pos[i] + 1;
-  child_refs<W>(wide, i, r);
+__global__ void k_dfs_place(const float4* __restrict__ wide, const uint32_t* __restrict__ lohi,
+                            const uint32_t* __restrict__ size, uint32_t* __restrict__ pos) {
+  const uint32_t lo = lohi[0], hi = lohi[1];  // the level's nodes (device memory)
+  for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+    uint32_t r[W], next = pos[i] + 1;
+    child_refs<W>(wide, i, r);
 #pragma unroll
-  for (int c = 0; c < W; ++c)
-    if (!(r[c] & J3DG_LEAF_BIT)) {
-      pos[r[c]] = next;
-      next += size[r[c]];
-    }
+    for (int c = 0; c < W; ++c)
+      if (!(r[c] & J3DG_LEAF_BIT)) {
+        pos[r[c]] = next;
+        next += size[r[c]];
+      }
+  }
 }
 
 template <int W>
-__global__ void k_dfs_permute(const float4* __restrict__ wide, uint32_t n, const uint32_t* __restrict__ pos,
-                              float4* __restrict__ out) {
+__global__ void k_dfs_permute(const float4* __restrict__ wide, const uint32_t* __restrict__ n_p,
+                              const uint32_t* __restrict__ pos, float4* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= *n_p) return;
   constexpr int F4 = J3DG_NODE_F4(W);
   const float4* src = wide + F4 * (size_t)i;
   float F[4 * F4];
@@ -1058,30 +1127,41 @@ __global__ void k_dfs_permute(const float4* __restrict__ wide, uint32_t n, const
 
 // out = the n wide nodes of `wide` (root 0, level L = [level_end[L-1],
 // level_end[L]) with level_end[-1] = 0) in depth-first order; root stays 0.
+// Host-driven (the LBVH builder's levels are known on the host): the
+// levels' node ranges go to the device once, the kernels read them there.
 template <int W>
 static cudaError_t dfs_order_w(const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end, float4* out,
                                cudaStream_t st) {
-  uint32_t *size = nullptr, *pos = nullptr;
+  const size_t L = level_end.size();
+  std::vector<uint32_t> h(2 * L + 1);
+  for (size_t l = 0; l < L; ++l) {
+    h[2 * l] = l ? level_end[l - 1] : 0u;
+    h[2 * l + 1] = level_end[l];
+  }
+  h[2 * L] = n;
+  uint32_t *size = nullptr, *pos = nullptr, *rng = nullptr;
   cudaError_t e = cudaMallocAsync((void**)&size, sizeof(uint32_t) * (size_t)n, st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&pos, sizeof(uint32_t) * (size_t)n, st);
-  const size_t L = level_end.size();
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&rng, sizeof(uint32_t) * h.size(), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rng, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice, st);
   for (size_t l = L; e == cudaSuccess && l-- > 0;) {
-    const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
-    if (hi > lo) k_dfs_size<W><<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size);
+    const uint32_t cnt = h[2 * l + 1] - h[2 * l];
+    if (cnt) k_dfs_size<W><<<(cnt + 255) / 256, 256, 0, st>>>(wide, rng + 2 * l, size);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(pos, 0, sizeof(uint32_t), st);
   for (size_t l = 0; e == cudaSuccess && l < L; ++l) {
-    const uint32_t lo = l ? level_end[l - 1] : 0u, hi = level_end[l];
-    if (hi > lo) k_dfs_place<W><<<(hi - lo + 255) / 256, 256, 0, st>>>(wide, lo, hi, size, pos);
+    const uint32_t cnt = h[2 * l + 1] - h[2 * l];
+    if (cnt) k_dfs_place<W><<<(cnt + 255) / 256, 256, 0, st>>>(wide, rng + 2 * l, size, pos);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    k_dfs_permute<W><<<(n + 255) / 256, 256, 0, st>>>(wide, n, pos, out);
+    k_dfs_permute<W><<<(n + 255) / 256, 256, 0, st>>>(wide, rng + 2 * L, pos, out);
     e = cudaGetLastError();
   }
   if (size) cudaFreeAsync(size, st);
   if (pos) cudaFreeAsync(pos, st);
+  if (rng) cudaFreeAsync(rng, st);
   return e;
 }
 
@@ -1092,33 +1172,34 @@ static cudaError_t dfs_order(uint32_t W, const float4* wide, uint32_t n, const s
   return dfs_order_w<4>(wide, n, level_end, out, st);
 }
 
+// the device-driven builder's fixed grids (grid-stride kernels)
+static const uint32_t kStrideBlocks = 2048;
+
 static void launch_collapse_cost(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
-                                 const float4* tris, uint32_t lo, uint32_t hi, uint32_t leaf_size, float* cost,
+                                 const float4* tris, const uint32_t* lohi, uint32_t leaf_size, float* cost,
                                  uint8_t* dec, cudaStream_t st) {
-  const uint32_t blocks = (hi - lo + 255) / 256;
   if (W == 2)
-    k_collapse_cost<2><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+    k_collapse_cost<2><<<kStrideBlocks, 256, 0, st>>>(child, box, count, tris, lohi, leaf_size, cost, dec);
   else if (W == 8)
-    k_collapse_cost<8><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+    k_collapse_cost<8><<<kStrideBlocks, 256, 0, st>>>(child, box, count, tris, lohi, leaf_size, cost, dec);
   else
-    k_collapse_cost<4><<<blocks, 256, 0, st>>>(child, box, count, tris, lo, hi, leaf_size, cost, dec);
+    k_collapse_cost<4><<<kStrideBlocks, 256, 0, st>>>(child, box, count, tris, lohi, leaf_size, cost, dec);
 }
 
 static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
-                                  const float4* tris, const PlaceItem* qin, uint32_t n_in, PlaceItem* qout,
-                                  uint32_t* n_out, uint32_t wide_base, float4* wide, uint32_t leaf_size,
+                                  const float4* tris, const PlaceItem* qin, const uint32_t* n_in, PlaceItem* qout,
+                                  uint32_t* n_out, const uint32_t* wide_base, float4* wide, uint32_t leaf_size,
                                   uint32_t* max_depth, float4* tris_out, uint32_t nt, uint32_t* status,
                                   const uint8_t* dec, cudaStream_t st) {
-  const uint32_t blocks = (n_in + 127) / 128;
   if (W == 2)
-    k_collapse_place<2><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
-                                                max_depth, tris_out, nt, status, dec);
+    k_collapse_place<2><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+                                                      leaf_size, max_depth, tris_out, nt, status, dec);
   else if (W == 8)
-    k_collapse_place<8><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
-                                                max_depth, tris_out, nt, status, dec);
+    k_collapse_place<8><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+                                                      leaf_size, max_depth, tris_out, nt, status, dec);
   else
-    k_collapse_place<4><<<blocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide, leaf_size,
-                                                max_depth, tris_out, nt, status, dec);
+    k_collapse_place<4><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+                                                      leaf_size, max_depth, tris_out, nt, status, dec);
 }
 
 // -------------------------------------------------- 5c. SAH top levels ----
@@ -1204,23 +1285,32 @@ static const uint32_t kTopWarpTask = 2048;
 
 // global bins of the tasks larger than kTopWarpTask (k_top_bin's); the
 // smaller tasks keep their bins in shared memory
-__global__ void k_top_bins_init(uint32_t* __restrict__ bins, uint32_t n_words, const TopTask* __restrict__ tasks) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_words) return;
-  const TopTask& T = tasks[i / (3 * kTopBins * kTopVals)];
-  if (T.end - T.begin <= kTopWarpTask) return;
-  const uint32_t v = i % kTopVals;
-  bins[i] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);  // lo fields: max code, hi fields: 0
+// (the level's task count and largest task are read from device memory;
+// levels with no task above kTopWarpTask have nothing to do here)
+__global__ void k_top_bins_init(uint32_t* __restrict__ bins, const uint32_t* __restrict__ n_tasks_p,
+                                const uint32_t* __restrict__ max_task_p, const TopTask* __restrict__ tasks) {
+  if (*max_task_p <= kTopWarpTask) return;
+  const uint32_t n_words = *n_tasks_p * 3 * kTopBins * kTopVals;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += gridDim.x * blockDim.x) {
+    const TopTask& T = tasks[i / (3 * kTopBins * kTopVals)];
+    if (T.end - T.begin <= kTopWarpTask) continue;
+    const uint32_t v = i % kTopVals;
+    bins[i] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);  // lo fields: max code, hi fields: 0
+  }
 }
 
 
 // bins of every active task: [task][axis][bin][kTopVals]
 __global__ void __launch_bounds__(256) k_top_bin(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
                                                  const float4* __restrict__ bhi, const uint32_t* __restrict__ task_of,
-                                                 const TopTask* __restrict__ tasks, uint32_t n_tasks, uint32_t n,
+                                                 const TopTask* __restrict__ tasks,
+                                                 const uint32_t* __restrict__ n_tasks_p,
+                                                 const uint32_t* __restrict__ max_task_p, uint32_t n,
                                                  uint32_t* __restrict__ bins, uint16_t* __restrict__ code) {
   __shared__ uint32_t sb[3 * kTopBins * kTopVals];
   __shared__ uint32_t s_task;
+  const uint32_t n_tasks = *n_tasks_p;
+  if (n_tasks == 0 || *max_task_p <= kTopWarpTask) return;  // k_top_bin_warp's level, or no level
   const uint32_t c0 = blockIdx.x * kTopChunk, c1 = min(n, c0 + kTopChunk);
   if (c0 >= n) return;
   if (threadIdx.x == 0) {
@@ -1437,21 +1527,12 @@ __device__ void warp_top_split(const uint32_t* B, const TopTask& T, TopSplit* __
   }
 }
 
-// tasks of at most kTopWarpTask triangles: one warp bins a whole task into
-// its own shared-memory bins with per-lane shared atomics, then splits it
-// from those bins (its bins never go to global memory)
-__global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
-                                                      const float4* __restrict__ bhi, const TopTask* __restrict__ tasks,
-                                                      uint32_t n_tasks, TopSplit* __restrict__ splits,
-                                                      BinNode* __restrict__ box, uint32_t* __restrict__ count,
-                                                      uint16_t* __restrict__ code) {
-  __shared__ uint32_t sb[8][3 * kTopBins * kTopVals];
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t t = blockIdx.x * 8u + warp;
-  if (t >= n_tasks) return;  // whole warps leave together
-  const TopTask T = tasks[t];
-  if (T.end - T.begin > kTopWarpTask) return;
-  uint32_t* my = sb[warp];
+// one warp bins task T (index t) into its shared bins `my` and splits it
+__device__ __forceinline__ void top_bin_warp_task(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
+                                                       const float4* __restrict__ bhi, const TopTask& T, uint32_t t,
+                                                       uint32_t* my, uint32_t lane, TopSplit* __restrict__ splits,
+                                                       BinNode* __restrict__ box, uint32_t* __restrict__ count,
+                                                       uint16_t* __restrict__ code) {
   for (uint32_t k = lane; k < 3 * kTopBins * kTopVals; k += 32) {
     const uint32_t v = k % kTopVals;
     my[k] = v == 0 ? 0u : (((v - 1) % 6) < 3 ? 0xffffffffu : 0u);
@@ -1480,18 +1561,42 @@ __global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict
   }
   __syncwarp();
   warp_top_split(my, T, splits + t, box, count);
+  __syncwarp();  // the split has read the bins before the warp's next task resets them
+}
+
+// tasks of at most kTopWarpTask triangles: one warp bins a whole task into
+// its own shared-memory bins with per-lane shared atomics, then splits it
+// from those bins (its bins never go to global memory)
+__global__ void __launch_bounds__(256) k_top_bin_warp(const uint32_t* __restrict__ ord, const float4* __restrict__ blo,
+                                                      const float4* __restrict__ bhi, const TopTask* __restrict__ tasks,
+                                                      const uint32_t* __restrict__ n_tasks_p,
+                                                      TopSplit* __restrict__ splits, BinNode* __restrict__ box,
+                                                      uint32_t* __restrict__ count, uint16_t* __restrict__ code) {
+  __shared__ uint32_t sb[8][3 * kTopBins * kTopVals];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t n_tasks = *n_tasks_p;
+  // whole warps take tasks together (a warp-stride loop over the level's tasks)
+  for (uint32_t t = blockIdx.x * 8u + warp; t < n_tasks; t += gridDim.x * 8u) {
+    const TopTask T = tasks[t];
+    if (T.end - T.begin > kTopWarpTask) continue;
+    top_bin_warp_task(ord, blo, bhi, T, t, sb[warp], lane, splits, box, count, code);
+  }
 }
 
 // one warp per task larger than kTopWarpTask (the smaller ones were split
 // by k_top_bin_warp from their shared-memory bins)
-__global__ void __launch_bounds__(128) k_top_split(const TopTask* __restrict__ tasks, uint32_t n_tasks,
+__global__ void __launch_bounds__(128) k_top_split(const TopTask* __restrict__ tasks,
+                                                   const uint32_t* __restrict__ n_tasks_p,
+                                                   const uint32_t* __restrict__ max_task_p,
                                                    const uint32_t* __restrict__ bins, TopSplit* __restrict__ splits,
                                                    BinNode* __restrict__ box, uint32_t* __restrict__ count) {
-  const uint32_t t = blockIdx.x * 4u + (threadIdx.x >> 5);
-  if (t >= n_tasks) return;  // whole warps leave together
-  const TopTask T = tasks[t];
-  if (T.end - T.begin <= kTopWarpTask) return;
-  warp_top_split(bins + (size_t)t * 3 * kTopBins * kTopVals, T, splits + t, box, count);
+  if (*max_task_p <= kTopWarpTask) return;
+  const uint32_t n_tasks = *n_tasks_p;
+  for (uint32_t t = blockIdx.x * 4u + (threadIdx.x >> 5); t < n_tasks; t += gridDim.x * 4u) {  // whole warps
+    const TopTask T = tasks[t];
+    if (T.end - T.begin <= kTopWarpTask) continue;
+    warp_top_split(bins + (size_t)t * 3 * kTopBins * kTopVals, T, splits + t, box, count);
+  }
 }
 
 // 1 if position p (of task t) goes left: its bin on the split axis (the
@@ -1509,10 +1614,12 @@ __device__ __forceinline__ uint32_t top_goes_left(uint32_t p, uint32_t code, con
 __global__ void __launch_bounds__(256) k_top_flag_scan(const uint32_t* __restrict__ task_of,
                                                        const uint16_t* __restrict__ code,
                                                        const TopTask* __restrict__ tasks,
-                                                       const TopSplit* __restrict__ splits, uint32_t n_tasks,
-                                                       uint32_t n, uint32_t* __restrict__ pscan,
-                                                       uint32_t* __restrict__ sums) {
+                                                       const TopSplit* __restrict__ splits,
+                                                       const uint32_t* __restrict__ n_tasks_p, uint32_t n,
+                                                       uint32_t* __restrict__ pscan, uint32_t* __restrict__ sums) {
   __shared__ uint32_t wsum[8];
+  const uint32_t n_tasks = *n_tasks_p;
+  if (n_tasks == 0) return;  // no level
   const uint32_t base = blockIdx.x * 1024u + threadIdx.x * 4u;
   uint32_t f[4] = {0u, 0u, 0u, 0u}, tk[4] = {kNoTask, kNoTask, kNoTask, kNoTask}, cd[4] = {0u, 0u, 0u, 0u};
   if (base + 3 < n) {  // task_of, code: 16- and 8-byte aligned groups of 4
@@ -1566,9 +1673,12 @@ __global__ void __launch_bounds__(256) k_top_scatter(const uint32_t* __restrict_
                                                      const uint32_t* __restrict__ task_of,
                                                      uint32_t* __restrict__ task_of2, const uint16_t* __restrict__ code,
                                                      const TopTask* __restrict__ tasks,
-                                                     const TopSplit* __restrict__ splits, uint32_t n_tasks,
+                                                     const TopSplit* __restrict__ splits,
+                                                     const uint32_t* __restrict__ n_tasks_p,
                                                      const uint32_t* __restrict__ pscan,
                                                      const uint32_t* __restrict__ sums, uint32_t n, uint32_t* status) {
+  const uint32_t n_tasks = *n_tasks_p;
+  if (n_tasks == 0) return;  // no level: the order stays where it is
   // 4 consecutive positions per thread (one chunk of the scan: base is a multiple of 4)
   const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
   if (base >= n) return;
@@ -1618,13 +1728,11 @@ __global__ void __launch_bounds__(256) k_top_scatter(const uint32_t* __restrict_
 
 // children of every task: a new task above J3DG_SAH_TOP triangles, else a
 // finished range (segment) whose root PLOC supplies later
-__global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __restrict__ splits,
-                               uint32_t n_tasks, uint32_t seg_max, uint32_t* __restrict__ counters,
-                               TopTask* __restrict__ next, TopRange* __restrict__ ranges, uint2* __restrict__ child,
-                               uint32_t cap_tasks, uint32_t cap_ranges, uint32_t max_nodes, uint32_t* status) {
-  // counters: [0] nodes allocated, [1] next tasks, [2] ranges, [3] largest next task
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tasks) return;
+__device__ __forceinline__ void top_children_of(const TopTask* __restrict__ tasks, TopSplit* __restrict__ splits,
+                                                uint32_t t, uint32_t seg_max, uint32_t* __restrict__ counters,
+                                                TopTask* __restrict__ next, TopRange* __restrict__ ranges,
+                                                uint2* __restrict__ child, uint32_t cap_tasks, uint32_t cap_ranges,
+                                                uint32_t max_nodes, uint32_t* status) {
   const TopTask T = tasks[t];
   TopSplit S = splits[t];
   const uint32_t n = T.end - T.begin;
@@ -1672,27 +1780,41 @@ __global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __re
   splits[t] = S;
 }
 
+__global__ void k_top_children(const TopTask* __restrict__ tasks, TopSplit* __restrict__ splits,
+                               const uint32_t* __restrict__ n_tasks_p, uint32_t seg_max,
+                               uint32_t* __restrict__ counters, TopTask* __restrict__ next,
+                               TopRange* __restrict__ ranges, uint2* __restrict__ child, uint32_t cap_tasks,
+                               uint32_t cap_ranges, uint32_t max_nodes, uint32_t* status) {
+  // counters: [0] nodes allocated, [1] next tasks, [2] ranges, [3] largest next task
+  const uint32_t n_tasks = *n_tasks_p;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tasks; t += gridDim.x * blockDim.x)
+    top_children_of(tasks, splits, t, seg_max, counters, next, ranges, child, cap_tasks, cap_ranges, max_nodes,
+                    status);
+}
+
 __global__ void k_iota(uint32_t* __restrict__ a, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) a[i] = i;
 }
 
 // segment starts: flags[begin] = 1 for every finished range
-__global__ void k_top_seg_starts(const TopRange* __restrict__ ranges, uint32_t n_ranges, uint32_t n,
-                                 uint32_t* __restrict__ flags) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < n_ranges && ranges[r].begin < n) flags[ranges[r].begin] = 1u;
+__global__ void k_top_seg_starts(const TopRange* __restrict__ ranges, const uint32_t* __restrict__ n_ranges_p,
+                                 uint32_t n, uint32_t* __restrict__ flags) {
+  const uint32_t n_ranges = *n_ranges_p;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_ranges; r += gridDim.x * blockDim.x)
+    if (ranges[r].begin < n) flags[ranges[r].begin] = 1u;
 }
 
 // PLOC's initial clusters in the order `ord`, with the segment of each position
 // (seg = inclusive scan of the starts - 1)
-__global__ void k_ploc_init_seg(const float4* __restrict__ tris, const uint32_t* __restrict__ ord, uint32_t n,
+__global__ void k_ploc_init_seg(const float4* __restrict__ tris, const uint32_t* __restrict__ ord_a,
+                                const uint32_t* __restrict__ ord_b, const uint32_t* __restrict__ parity, uint32_t n,
                                 const uint32_t* __restrict__ starts, const uint32_t* __restrict__ scan,
                                 uint32_t* __restrict__ C, float4* __restrict__ lo, float4* __restrict__ hi,
                                 uint32_t* __restrict__ seg) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint32_t t = ord[i];
+  const uint32_t t = (*parity ? ord_b : ord_a)[i];  // the final order is where the last level put it
   C[i] = 0x80000000u | t;
   leaf_box(tris, t, lo[i], hi[i]);
   seg[i] = scan[i] + starts[i] - 1u;
@@ -1700,21 +1822,26 @@ __global__ void k_ploc_init_seg(const float4* __restrict__ tris, const uint32_t*
 
 // the root of segment s (its one cluster left, at list position s) fills the
 // child slot of the top node that made the segment
-__global__ void k_top_link(const TopRange* __restrict__ ranges, uint32_t n_ranges, const uint32_t* __restrict__ starts,
-                           const uint32_t* __restrict__ scan, const uint32_t* __restrict__ C, uint32_t n_seg,
+// (the clusters are in C0 or C1, by the parity of the PLOC rounds run)
+__global__ void k_top_link(const TopRange* __restrict__ ranges, const uint32_t* __restrict__ n_ranges_p,
+                           const uint32_t* __restrict__ starts, const uint32_t* __restrict__ scan,
+                           const uint32_t* __restrict__ C0, const uint32_t* __restrict__ C1,
+                           const uint32_t* __restrict__ parity, const uint32_t* __restrict__ n_seg_p,
                            uint2* __restrict__ child, uint32_t* status) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_ranges) return;
-  const TopRange R = ranges[r];
-  const uint32_t s = scan[R.begin] + starts[R.begin] - 1u;
-  if (s >= n_seg) {
-    atomicOr(status, J3DG_DEV_BAD_INDEX);
-    return;
+  const uint32_t n_ranges = *n_ranges_p, n_seg = *n_seg_p;
+  const uint32_t* C = *parity ? C1 : C0;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_ranges; r += gridDim.x * blockDim.x) {
+    const TopRange R = ranges[r];
+    const uint32_t s = scan[R.begin] + starts[R.begin] - 1u;
+    if (s >= n_seg) {
+      atomicOr(status, J3DG_DEV_BAD_INDEX);
+      continue;
+    }
+    if (R.side)
+      child[R.parent].y = C[s];
+    else
+      child[R.parent].x = C[s];
   }
-  if (R.side)
-    child[R.parent].y = C[s];
-  else
-    child[R.parent].x = C[s];
 }
 
 // ------------------------------------------------------------- driver ----
@@ -1750,10 +1877,551 @@ __global__ void k_slot_of(const float4* __restrict__ tris, uint32_t nt, uint32_t
     p = nullptr;                 \
   } while (0)
 
+// ------------------------------------------------ device-driven build ----
+//
+// The default builder (binned-SAH top levels, PLOC below them, the
+// cost-optimal collapse, depth-first numbering) runs as one CUDA graph with
+// no host round trip: every level loop is a conditional while node whose
+// body ends in a one-thread step kernel, which advances the loop state kept
+// in device memory (BuildCtl) and sets the loop's condition. Kernels read
+// their sizes from BuildCtl and stride over them with fixed grids, so one
+// captured sequence serves every level. Loops whose levels alternate two
+// buffers run two levels per body (the second is a no-op when the first
+// ends the loop). enqueue_build only enqueues (it runs under a stream
+// capture): j3dg_mesh_build captures and launches it for one mesh, and a
+// batch captures it for all its meshes ahead of its frames.
+
+static const uint32_t kMaxTopLevels = 1024, kMaxRounds = 1024, kMaxPlaceLevels = 128;
+
+struct BuildCtl {
+  uint32_t top_ctr[4];  // k_top_children: [0] top nodes, [1] next level's tasks, [2] ranges, [3] largest next task
+  uint32_t n_tasks, max_task, ord_parity, top_levels;
+  uint32_t mcount, n_seg, node_base, c_parity, rounds, tot[2];
+  uint32_t lohi[2];  // the running pass's node range (collapse costs, depth-first levels)
+  uint32_t pass, n_pass;
+  uint32_t n_in, n_out, n_wide, place_levels, max_depth;
+  int32_t dfs_level;
+  uint32_t error;  // a loop overran its bound: 1 SAH levels, 2 PLOC, 4 placement
+  uint32_t top_end[kMaxTopLevels];     // top nodes of level L end at top_end[L]
+  uint32_t round_end[kMaxRounds];      // binary nodes of PLOC round r end at round_end[r]
+  uint32_t level_end[kMaxPlaceLevels]; // wide nodes of level L end at level_end[L]
+};
+
+__global__ void k_ctl_init(BuildCtl* __restrict__ c, TopTask* __restrict__ tasks, const float* __restrict__ bb,
+                           uint32_t nt, uint32_t top) {
+  if (top) {
+    TopTask r0;
+    r0.begin = 0;
+    r0.end = nt;
+    r0.node = 0;
+    r0.pad = 0;
+    r0.clo = make_float4(bb[0], bb[1], bb[2], 0.f);  // the vertex bbox holds every centroid
+    r0.chi = make_float4(bb[3], bb[4], bb[5], 0.f);
+    tasks[0] = r0;
+    c->top_ctr[0] = 1;  // the root node
+    c->n_tasks = 1;
+    c->max_task = nt;
+    c->top_levels = 1;
+    c->top_end[0] = 1;
+  }
+  c->mcount = nt;
+  c->n_seg = 1;
+  c->n_in = 1;  // the placement's root item
+  c->n_wide = 1;
+  c->place_levels = 1;
+  c->level_end[0] = 1;
+}
+
+__global__ void k_top_step(BuildCtl* __restrict__ c, uint32_t cap_tasks, uint32_t nt, cudaGraphConditionalHandle h,
+                           uint32_t set) {
+  if (c->n_tasks) {  // the level ran
+    uint32_t next = c->top_ctr[1];
+    if (next > cap_tasks || c->top_ctr[2] > nt || c->top_ctr[0] > nt - 1 || c->top_levels >= kMaxTopLevels) {
+      c->error |= 1u;
+      next = 0;
+    } else if (c->top_ctr[0] > c->top_end[c->top_levels - 1]) {
+      c->top_end[c->top_levels++] = c->top_ctr[0];
+    }
+    c->n_tasks = next;
+    c->max_task = c->top_ctr[3];
+    c->top_ctr[1] = 0;
+    c->top_ctr[3] = 0;
+    c->ord_parity ^= 1u;
+  }
+  if (set) cudaGraphSetConditional(h, c->n_tasks > 0 ? 1u : 0u);
+}
+
+__global__ void k_ploc_setup(BuildCtl* __restrict__ c) {  // after the SAH levels: one segment per range
+  c->n_seg = c->top_ctr[2];
+  c->node_base = c->top_ctr[0];
+}
+
+__global__ void k_ploc_step(BuildCtl* __restrict__ c, uint32_t nt, cudaGraphConditionalHandle h, uint32_t set) {
+  if (c->mcount > c->n_seg) {  // the round ran
+    const uint32_t creates = c->tot[0], surv = c->tot[1];
+    if (creates == 0 || surv >= c->mcount || c->node_base + creates > nt - 1 || c->rounds >= kMaxRounds) {
+      c->error |= 2u;  // no progress or past the node bound
+      c->mcount = c->n_seg;
+    } else {
+      c->node_base += creates;
+      c->round_end[c->rounds++] = c->node_base;
+      c->mcount = surv;
+      c->c_parity ^= 1u;
+    }
+  }
+  if (set) cudaGraphSetConditional(h, c->mcount > c->n_seg ? 1u : 0u);
+}
+
+// pass p of the cost programme: the PLOC rounds in order, then the top levels
+// deepest first (children before parents)
+__device__ __forceinline__ void cost_range(BuildCtl* c, uint32_t p, uint32_t top) {
+  uint32_t lo = 0, hi = 0;
+  if (p < c->rounds) {
+    lo = p ? c->round_end[p - 1] : (top ? c->top_ctr[0] : 0u);
+    hi = c->round_end[p];
+  } else if (p < c->n_pass) {
+    const uint32_t k = c->top_levels - 1 - (p - c->rounds);
+    lo = k ? c->top_end[k - 1] : 0u;
+    hi = c->top_end[k];
+  }
+  c->lohi[0] = lo;
+  c->lohi[1] = hi;
+}
+
+__global__ void k_ploc_done(BuildCtl* __restrict__ c, uint32_t nt, uint32_t top, const uint32_t* __restrict__ C0,
+                            const uint32_t* __restrict__ C1, PlaceItem* __restrict__ qa) {
+  const uint32_t root = top ? 0u : (c->c_parity ? C1 : C0)[0];
+  if (c->node_base != nt - 1 || (root & 0x80000000u)) c->error |= 2u;  // a malformed tree
+  qa[0] = PlaceItem{root, 0u, 1u, 0u};
+  c->n_pass = c->rounds + (top ? c->top_levels : 0u);
+  c->pass = 0;
+  cost_range(c, 0, top);
+}
+
+__global__ void k_cost_step(BuildCtl* __restrict__ c, uint32_t top, cudaGraphConditionalHandle h) {
+  ++c->pass;
+  cost_range(c, c->pass, top);
+  cudaGraphSetConditional(h, c->pass < c->n_pass ? 1u : 0u);
+}
+
+__global__ void k_place_step(BuildCtl* __restrict__ c, uint32_t nt, cudaGraphConditionalHandle h, uint32_t set) {
+  if (c->n_in) {  // the level ran
+    const uint32_t n_out = c->n_out;
+    c->n_wide += n_out;
+    if (c->n_wide > nt || c->place_levels >= kMaxPlaceLevels) {
+      c->error |= 4u;
+      c->n_in = 0;
+    } else {
+      if (n_out) c->level_end[c->place_levels++] = c->n_wide;
+      c->n_in = n_out;
+    }
+    c->n_out = 0;
+  }
+  if (set) cudaGraphSetConditional(h, c->n_in > 0 ? 1u : 0u);
+}
+
+__device__ __forceinline__ void level_range(BuildCtl* c, int32_t l) {
+  const bool ok = l >= 0 && l < (int32_t)c->place_levels;
+  c->lohi[0] = ok && l > 0 ? c->level_end[l - 1] : 0u;
+  c->lohi[1] = ok ? c->level_end[l] : 0u;
+}
+
+__global__ void k_dfs_setup(BuildCtl* __restrict__ c, uint32_t* __restrict__ pos, uint32_t up) {
+  if (!up) {  // subtree sizes, deepest level first
+    c->dfs_level = (int32_t)c->place_levels - 1;
+  } else {  // positions, root level first
+    c->dfs_level = 0;
+    pos[0] = 0;
+  }
+  level_range(c, c->dfs_level);
+}
+
+__global__ void k_dfs_step(BuildCtl* __restrict__ c, uint32_t up, cudaGraphConditionalHandle h) {
+  c->dfs_level += up ? 1 : -1;
+  level_range(c, c->dfs_level);
+  cudaGraphSetConditional(h, (c->dfs_level >= 0 && c->dfs_level < (int32_t)c->place_levels) ? 1u : 0u);
+}
+
+// Appends a while node (condition initially 1) to the graph that `st` is
+// capturing; `body(side, handle)` enqueues the loop body on `side`, which
+// captures it into the node's body graph.
+template <class Body>
+static cudaError_t capture_while(cudaStream_t st, cudaStream_t side, Body&& body) {
+  cudaStreamCaptureStatus cs;
+  unsigned long long id = 0;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  if (cs != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureUnsupported;
+  cudaGraphConditionalHandle h;
+  if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p)) != cudaSuccess) return e;
+  if ((e = cudaStreamBeginCaptureToGraph(side, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return e;
+  body(side, h);
+  const cudaError_t eb = cudaGetLastError();
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(side, &captured);
+  if (eb != cudaSuccess) return eb;
+  if (e != cudaSuccess) return e;
+  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// Every buffer of one build, sized by the triangle count alone (upper bounds
+// where the tree decides: the wide nodes, the queues).
+struct BuildPlan {
+  uint32_t nv = 0, nt = 0, W = 4, leaf = 2;
+  bool top = false;
+  // scratch
+  float* part = nullptr;
+  float* bb = nullptr;
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  uint32_t *v0 = nullptr, *v1 = nullptr, *hist = nullptr, *sums = nullptr;
+  uint32_t *ord_a = nullptr, *ord_b = nullptr, *task_of = nullptr, *task_of2 = nullptr, *seg_starts = nullptr,
+           *seg_scan = nullptr, *top_bins = nullptr;
+  float4 *tbox_lo = nullptr, *tbox_hi = nullptr;
+  uint16_t* codes = nullptr;
+  TopTask *tasks_a = nullptr, *tasks_b = nullptr;
+  TopSplit* splits = nullptr;
+  TopRange* ranges = nullptr;
+  uint2* child = nullptr;
+  BinNode* box = nullptr;
+  uint32_t *count = nullptr, *C0 = nullptr, *C1 = nullptr, *nn = nullptr, *cscan = nullptr, *sscan = nullptr,
+           *pl_sums = nullptr, *pl_sums2 = nullptr, *seg0 = nullptr, *seg1 = nullptr;
+  float4 *lo0 = nullptr, *hi0 = nullptr, *lo1 = nullptr, *hi1 = nullptr;
+  float* dp_cost = nullptr;
+  uint8_t* dp_dec = nullptr;
+  float4* wide = nullptr;
+  PlaceItem *pa = nullptr, *pb = nullptr;
+  uint32_t *dfs_size = nullptr, *dfs_pos = nullptr;
+  BuildCtl* ctl = nullptr;
+  // outputs (the mesh keeps them)
+  float4 *normals = nullptr, *soup = nullptr, *tris_out = nullptr, *nodes = nullptr;
+  uint32_t* slot_of = nullptr;
+  uint32_t cap_tasks() const { return nt / J3DG_SAH_TOP + 1; }  // tasks of one level are disjoint, each > J3DG_SAH_TOP
+  uint32_t n_tiles() const { return (nt + kSortTile - 1) / kSortTile; }
+  uint32_t hist_n() const { return 256 * n_tiles(); }
+  uint32_t scan_blocks() const { return (hist_n() + 1023) / 1024; }
+  uint32_t sblocks() const { return (nt + 1023) / 1024; }
+};
+
+static const int kBBoxBlocks = 1024;
+
+static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st) {
+  const size_t nt = P.nt, F4 = J3DG_NODE_F4(P.W);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](auto*& p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&p, bytes, st);
+  };
+  A(P.part, sizeof(float) * 6 * kBBoxBlocks);
+  A(P.bb, sizeof(float) * 6);
+  A(P.k0, sizeof(uint64_t) * nt);
+  A(P.k1, sizeof(uint64_t) * nt);
+  A(P.v0, sizeof(uint32_t) * nt);
+  A(P.v1, sizeof(uint32_t) * nt);
+  A(P.hist, sizeof(uint32_t) * P.hist_n());
+  A(P.sums, sizeof(uint32_t) * (P.scan_blocks() + 1));
+  if (P.top) {
+    A(P.ord_a, sizeof(uint32_t) * nt);
+    A(P.ord_b, sizeof(uint32_t) * nt);
+    A(P.task_of, sizeof(uint32_t) * nt);
+    A(P.task_of2, sizeof(uint32_t) * nt);
+    A(P.tbox_lo, sizeof(float4) * nt);
+    A(P.tbox_hi, sizeof(float4) * nt);
+    A(P.codes, sizeof(uint16_t) * nt);
+    A(P.seg_starts, sizeof(uint32_t) * nt);
+    A(P.seg_scan, sizeof(uint32_t) * nt);
+    A(P.top_bins, sizeof(uint32_t) * (size_t)P.cap_tasks() * 3 * kTopBins * kTopVals);
+    A(P.tasks_a, sizeof(TopTask) * P.cap_tasks());
+    A(P.tasks_b, sizeof(TopTask) * P.cap_tasks());
+    A(P.splits, sizeof(TopSplit) * P.cap_tasks());
+    A(P.ranges, sizeof(TopRange) * nt);  // at most one range per triangle
+  }
+  A(P.child, sizeof(uint2) * (nt - 1));
+  A(P.box, sizeof(BinNode) * (nt - 1));
+  A(P.count, sizeof(uint32_t) * (nt - 1));
+  A(P.C0, sizeof(uint32_t) * nt);
+  A(P.C1, sizeof(uint32_t) * nt);
+  A(P.nn, sizeof(uint32_t) * nt);
+  A(P.cscan, sizeof(uint32_t) * nt);
+  A(P.sscan, sizeof(uint32_t) * nt);
+  A(P.pl_sums, sizeof(uint32_t) * (P.sblocks() + 1));
+  A(P.pl_sums2, sizeof(uint32_t) * (P.sblocks() + 1));
+  A(P.seg0, sizeof(uint32_t) * nt);
+  A(P.seg1, sizeof(uint32_t) * nt);
+  A(P.lo0, sizeof(float4) * nt);
+  A(P.hi0, sizeof(float4) * nt);
+  A(P.lo1, sizeof(float4) * nt);
+  A(P.hi1, sizeof(float4) * nt);
+  A(P.dp_cost, sizeof(float) * P.W * (nt - 1));
+  A(P.dp_dec, sizeof(uint8_t) * P.W * (nt - 1));
+  A(P.wide, sizeof(float4) * F4 * nt);
+  A(P.pa, sizeof(PlaceItem) * nt);
+  A(P.pb, sizeof(PlaceItem) * nt);
+  A(P.dfs_size, sizeof(uint32_t) * nt);
+  A(P.dfs_pos, sizeof(uint32_t) * nt);
+  A(P.ctl, sizeof(BuildCtl));
+  A(P.normals, sizeof(float4) * nt);
+  A(P.soup, sizeof(float4) * 3 * nt);
+  A(P.tris_out, sizeof(float4) * 3 * nt);
+  A(P.nodes, sizeof(float4) * F4 * nt);  // the wide nodes are at most nt - 1
+  A(P.slot_of, sizeof(uint32_t) * nt);
+  return e;
+}
+
+// frees the scratch (outputs the caller took over are null)
+static void plan_free(BuildPlan& P, cudaStream_t st) {
+  void* ps[] = {P.part, P.bb, P.k0, P.k1, P.v0, P.v1, P.hist, P.sums, P.ord_a, P.ord_b, P.task_of, P.task_of2,
+                P.seg_starts, P.seg_scan, P.top_bins, P.tbox_lo, P.tbox_hi, P.codes, P.tasks_a, P.tasks_b, P.splits,
+                P.ranges, P.child, P.box, P.count, P.C0, P.C1, P.nn, P.cscan, P.sscan, P.pl_sums, P.pl_sums2, P.seg0,
+                P.seg1, P.lo0, P.hi0, P.lo1, P.hi1, P.dp_cost, P.dp_dec, P.wide, P.pa, P.pb, P.dfs_size, P.dfs_pos,
+                P.ctl, P.normals, P.soup, P.tris_out, P.nodes, P.slot_of};
+  for (void* p : ps)
+    if (p) cudaFreeAsync(p, st);
+  P = BuildPlan{};
+}
+
+// all of a build's work on `st` (capturing): no host synchronisation
+static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* dT, cudaStream_t st,
+                                 cudaStream_t side, uint32_t* d_status) {
+  const uint32_t nt = P.nt, nv = P.nv, W = P.W;
+  BuildCtl* c = P.ctl;
+  cudaError_t e = cudaSuccess;
+#define J3DG_EQ(x)                        \
+  do {                                    \
+    if (e == cudaSuccess) e = (x);        \
+    if (e == cudaSuccess) e = cudaGetLastError(); \
+  } while (0)
+  J3DG_EQ(cudaMemsetAsync(c, 0, sizeof(BuildCtl), st));
+  k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(dV, nv, P.part);
+  k_bbox_final<<<1, 32, 0, st>>>(P.part, kBBoxBlocks, P.bb);
+  k_ctl_init<<<1, 1, 0, st>>>(c, P.tasks_a, P.bb, nt, P.top ? 1u : 0u);
+  k_tri_prep<<<(nt + 255) / 256, 256, 0, st>>>(dV, nv, dT, nt, P.bb, P.normals, P.k0, P.v0, d_status);
+  J3DG_EQ(cudaSuccess);
+  {
+    uint64_t *ka = P.k0, *kb = P.k1;
+    uint32_t *va = P.v0, *vb = P.v1;
+    for (int pass = 0; pass < kRadixPasses; ++pass) {
+      const int shift = 8 * pass;
+      k_radix_hist<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, nt, shift, P.n_tiles(), P.hist);
+      k_scan_chunks<<<P.scan_blocks(), 256, 0, st>>>(P.hist, P.hist, P.hist_n(), P.sums);
+      k_scan_sums<<<1, 1024, 0, st>>>(P.sums, nullptr, P.scan_blocks(), nullptr);
+      k_radix_scatter<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, va, kb, vb, nt, shift, P.n_tiles(), P.hist, P.sums,
+                                                           d_status);
+      std::swap(ka, kb);
+      std::swap(va, vb);
+    }
+    k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, va, nt, nv, P.soup, d_status);
+  }
+  J3DG_EQ(cudaSuccess);
+  const float4* soup = P.soup;
+  if (P.top) {
+    k_top_boxes<<<(nt + 255) / 256, 256, 0, st>>>(soup, nt, P.tbox_lo, P.tbox_hi);
+    k_iota<<<(nt + 255) / 256, 256, 0, st>>>(P.ord_a, nt);
+    J3DG_EQ(cudaMemsetAsync(P.task_of, 0, sizeof(uint32_t) * nt, st));
+    // one SAH level: tasks ti, order oi, task of each position si -> the next level's
+    auto level = [&](cudaStream_t s, TopTask* ti, TopTask* to, uint32_t* oi, uint32_t* oo, uint32_t* si,
+                     uint32_t* so) {
+      k_top_bins_init<<<kStrideBlocks, 256, 0, s>>>(P.top_bins, &c->n_tasks, &c->max_task, ti);
+      k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, s>>>(oi, P.tbox_lo, P.tbox_hi, si, ti, &c->n_tasks,
+                                                                 &c->max_task, nt, P.top_bins, P.codes);
+      k_top_bin_warp<<<kStrideBlocks, 256, 0, s>>>(oi, P.tbox_lo, P.tbox_hi, ti, &c->n_tasks, P.splits, P.box,
+                                                   P.count, P.codes);
+      k_top_split<<<kStrideBlocks, 128, 0, s>>>(ti, &c->n_tasks, &c->max_task, P.top_bins, P.splits, P.box, P.count);
+      k_top_children<<<kStrideBlocks, 128, 0, s>>>(ti, P.splits, &c->n_tasks, J3DG_SAH_TOP, c->top_ctr, to, P.ranges,
+                                                   P.child, P.cap_tasks(), nt, nt - 1, d_status);
+      k_top_flag_scan<<<P.sblocks(), 256, 0, s>>>(si, P.codes, ti, P.splits, &c->n_tasks, nt, P.cscan, P.pl_sums);
+      k_scan_sums<<<1, 1024, 0, s>>>(P.pl_sums, nullptr, P.sblocks(), nullptr);
+      k_top_scatter<<<(nt + 1023) / 1024, 256, 0, s>>>(oi, oo, si, so, P.codes, ti, P.splits, &c->n_tasks, P.cscan,
+                                                       P.pl_sums, nt, d_status);
+    };
+    J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+      level(s, P.tasks_a, P.tasks_b, P.ord_a, P.ord_b, P.task_of, P.task_of2);
+      k_top_step<<<1, 1, 0, s>>>(c, P.cap_tasks(), nt, h, 0u);
+      level(s, P.tasks_b, P.tasks_a, P.ord_b, P.ord_a, P.task_of2, P.task_of);
+      k_top_step<<<1, 1, 0, s>>>(c, P.cap_tasks(), nt, h, 1u);
+    }));
+    k_ploc_setup<<<1, 1, 0, st>>>(c);
+    // segments numbered in position order: a flag at each range's start, one scan
+    J3DG_EQ(cudaMemsetAsync(P.seg_starts, 0, sizeof(uint32_t) * nt, st));
+    k_top_seg_starts<<<kStrideBlocks, 256, 0, st>>>(P.ranges, &c->top_ctr[2], nt, P.seg_starts);
+    k_scan_chunks<<<P.sblocks(), 256, 0, st>>>(P.seg_starts, P.seg_scan, nt, P.pl_sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(P.pl_sums, nullptr, P.sblocks(), nullptr);
+    k_scan_add<<<P.sblocks(), 256, 0, st>>>(P.seg_scan, nt, P.pl_sums);
+    k_ploc_init_seg<<<(nt + 255) / 256, 256, 0, st>>>(soup, P.ord_a, P.ord_b, &c->ord_parity, nt, P.seg_starts,
+                                                      P.seg_scan, P.C0, P.lo0, P.hi0, P.seg0);
+  } else {
+    k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>(soup, nt, P.C0, P.lo0, P.hi0);
+    J3DG_EQ(cudaMemsetAsync(P.seg0, 0, sizeof(uint32_t) * nt, st));
+  }
+  J3DG_EQ(cudaSuccess);
+  // PLOC rounds: clusters (C, lo, hi, seg) in -> out
+  auto round = [&](cudaStream_t s, const uint32_t* Ci, const float4* li, const float4* hi_, const uint32_t* si,
+                   uint32_t* Co, float4* lo_, float4* ho, uint32_t* so) {
+    k_ploc_nn<<<kStrideBlocks, kPlocBlock, 0, s>>>(li, hi_, si, &c->mcount, &c->n_seg, P.nn);
+    k_ploc_flag_scan<<<P.sblocks(), 256, 0, s>>>(P.nn, &c->mcount, &c->n_seg, P.cscan, P.sscan, P.pl_sums,
+                                                 P.pl_sums2);
+    k_scan_sums<<<1, 1024, 0, s>>>(P.pl_sums, P.pl_sums2, 0u, c->tot, &c->mcount);
+    k_ploc_merge<<<kStrideBlocks, 256, 0, s>>>(Ci, li, hi_, si, P.nn, P.cscan, P.sscan, P.pl_sums, P.pl_sums2,
+                                               &c->mcount, &c->n_seg, &c->node_base, Co, lo_, ho, so, P.child, P.box,
+                                               P.count);
+  };
+  J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+    round(s, P.C0, P.lo0, P.hi0, P.seg0, P.C1, P.lo1, P.hi1, P.seg1);
+    k_ploc_step<<<1, 1, 0, s>>>(c, nt, h, 0u);
+    round(s, P.C1, P.lo1, P.hi1, P.seg1, P.C0, P.lo0, P.hi0, P.seg0);
+    k_ploc_step<<<1, 1, 0, s>>>(c, nt, h, 1u);
+  }));
+  if (P.top)
+    k_top_link<<<kStrideBlocks, 256, 0, st>>>(P.ranges, &c->top_ctr[2], P.seg_starts, P.seg_scan, P.C0, P.C1,
+                                              &c->c_parity, &c->n_seg, P.child, d_status);
+  k_ploc_done<<<1, 1, 0, st>>>(c, nt, P.top ? 1u : 0u, P.C0, P.C1, P.pa);
+  J3DG_EQ(cudaSuccess);
+  // cost programme, children before parents
+  J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+    launch_collapse_cost(W, P.child, P.box, P.count, soup, c->lohi, P.leaf, P.dp_cost, P.dp_dec, s);
+    k_cost_step<<<1, 1, 0, s>>>(c, P.top ? 1u : 0u, h);
+  }));
+  // placement, level by level
+  J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+    launch_collapse_place(W, P.child, P.box, P.count, soup, P.pa, &c->n_in, P.pb, &c->n_out, &c->n_wide, P.wide,
+                          P.leaf, &c->max_depth, P.tris_out, nt, d_status, P.dp_dec, s);
+    k_place_step<<<1, 1, 0, s>>>(c, nt, h, 0u);
+    launch_collapse_place(W, P.child, P.box, P.count, soup, P.pb, &c->n_in, P.pa, &c->n_out, &c->n_wide, P.wide,
+                          P.leaf, &c->max_depth, P.tris_out, nt, d_status, P.dp_dec, s);
+    k_place_step<<<1, 1, 0, s>>>(c, nt, h, 1u);
+  }));
+  // depth-first numbering: subtree sizes bottom-up, positions top-down, permute
+  auto dfs = [&](auto Wc) {
+    constexpr int WW = decltype(Wc)::value;
+    k_dfs_setup<<<1, 1, 0, st>>>(c, P.dfs_pos, 0u);
+    J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+      k_dfs_size<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 0u, h);
+    }));
+    k_dfs_setup<<<1, 1, 0, st>>>(c, P.dfs_pos, 1u);
+    J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+      k_dfs_place<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size, P.dfs_pos);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 1u, h);
+    }));
+    k_dfs_permute<WW><<<(nt + 255) / 256, 256, 0, st>>>(P.wide, &c->n_wide, P.dfs_pos, P.nodes);
+  };
+  if (W == 2)
+    dfs(std::integral_constant<int, 2>());
+  else if (W == 8)
+    dfs(std::integral_constant<int, 8>());
+  else
+    dfs(std::integral_constant<int, 4>());
+  k_slot_of<<<(nt + 255) / 256, 256, 0, st>>>(P.tris_out, nt, P.slot_of, d_status);
+  J3DG_EQ(cudaSuccess);
+#undef J3DG_EQ
+  return e;
+}
+
+// The default build through the device-driven graph: allocate, capture,
+// launch, then take the tree's size from the device and keep an exactly
+// sized copy of the nodes.
+static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
+                           std::string& err) {
+  BuildPlan P;
+  P.nv = m->nv;
+  P.nt = m->nt;
+  P.W = m->width;
+  P.leaf = m->leaf_size;
+  P.top = J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
+  cudaStream_t side = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  BuildCtl h;
+  float hbb[6];
+  int rc = J3DG_OK;
+  cudaError_t e = plan_alloc(P, st);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    const cudaError_t eq = enqueue_build(P, dV, dT, st, side, d_status);
+    e = cudaStreamEndCapture(st, &g);
+    if (eq != cudaSuccess) e = eq;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(ex, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, P.ctl, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hbb, P.bb, sizeof(hbb), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    err = std::string("build: ") + cudaGetErrorString(e);
+    rc = e == cudaErrorMemoryAllocation ? J3DG_ERR_OUT_OF_MEMORY : J3DG_ERR_CUDA;
+  } else if (h.error) {
+    err = (h.error & 1u) ? "SAH top levels overran their bounds"
+                         : ((h.error & 2u) ? "PLOC clustering ended with a malformed tree"
+                                           : "BVH collapse overran its node bound");
+    rc = J3DG_ERR_CUDA;
+  }
+  if (rc == J3DG_OK) {
+    m->scale = 0.f;
+    for (int k = 0; k < 3; ++k) {
+      m->min_bb[k] = hbb[k];
+      m->max_bb[k] = hbb[3 + k];
+    }
+    for (int k = 0; k < 6; ++k) m->scale = std::max(m->scale, std::fabs(hbb[k]));
+    m->n_nodes = h.n_wide;
+    m->max_depth = h.max_depth;
+    m->root_ref = 0;
+    const size_t bytes = sizeof(float4) * J3DG_NODE_F4(P.W) * (size_t)m->n_nodes;
+    e = cudaMallocAsync(&m->d_nodes, bytes, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m->d_nodes, P.nodes, bytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+      m->d_normals = P.normals;
+      m->d_tris = P.tris_out;
+      m->d_slot_of = P.slot_of;
+      P.normals = nullptr;
+      P.tris_out = nullptr;
+      P.slot_of = nullptr;
+    } else {
+      err = std::string("build: ") + cudaGetErrorString(e);
+      rc = e == cudaErrorMemoryAllocation ? J3DG_ERR_OUT_OF_MEMORY : J3DG_ERR_CUDA;
+    }
+  }
+  plan_free(P, st);
+  if (ex) cudaGraphExecDestroy(ex);
+  if (g) cudaGraphDestroy(g);
+  if (side) cudaStreamDestroy(side);
+  {
+    const cudaError_t es = cudaStreamSynchronize(st);
+    if (rc == J3DG_OK && es != cudaSuccess) {
+      err = std::string("build: ") + cudaGetErrorString(es);
+      rc = J3DG_ERR_CUDA;
+    }
+  }
+  if (rc != J3DG_OK) return rc;
+  const uint32_t W = m->width;
+  if (m->max_depth > J3DG_MAX_DEPTH_W(W)) {
+    err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack at width " + std::to_string(W);
+    return J3DG_ERR_UNSUPPORTED;
+  }
+  m->device_bytes = sizeof(float4) * J3DG_NODE_F4(W) * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
+                    sizeof(float4) * 4 * (uint64_t)m->nt + sizeof(uint32_t) * 4 * (uint64_t)m->nt;
+  return J3DG_OK;
+}
+
 // Builds the device BVH. dV and dT are device arrays. On success fills the
-// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals).
+// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals). The
+// default builder goes through build_bvh_graph; this host-driven path builds
+// with the LBVH builder and handles meshes of at most one leaf.
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
               std::string& err) {
+  // the default builder runs device-driven; the LBVH builder and tiny meshes here
+  if (!(m->build_flags & J3DG_BUILD_LBVH) && m->nt > m->leaf_size)
+    return build_bvh_graph(m, dV, dT, st, d_status, err);
   int rc = J3DG_OK;
   const uint32_t nv = m->nv, nt = m->nt;
   float* d_part = nullptr;
@@ -1765,22 +2433,6 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   uint32_t *other = nullptr, *counters = nullptr;
   CollapseItem *qa = nullptr, *qb = nullptr;
   float4* wide = nullptr;
-  // PLOC
-  uint32_t *C0 = nullptr, *C1 = nullptr, *nn = nullptr, *cscan = nullptr,
-           *sscan = nullptr, *pl_sums = nullptr, *pl_sums2 = nullptr, *count = nullptr, *tot = nullptr;
-  float4 *lo0 = nullptr, *hi0 = nullptr, *lo1 = nullptr, *hi1 = nullptr, *tris_out = nullptr;
-  PlaceItem *pa = nullptr, *pb = nullptr;
-  // SAH top levels
-  uint32_t *ord_a = nullptr, *ord_b = nullptr, *task_of = nullptr, *task_of2 = nullptr, *seg0 = nullptr,
-           *seg1 = nullptr, *seg_starts = nullptr, *seg_scan = nullptr, *top_bins = nullptr, *top_ctr = nullptr;
-  float4 *tbox_lo = nullptr, *tbox_hi = nullptr;
-  uint16_t* codes = nullptr;  // per position: the centroid's bin on each axis (4 bits each)
-  TopTask *tasks_a = nullptr, *tasks_b = nullptr;
-  TopSplit* splits = nullptr;
-  TopRange* ranges = nullptr;
-  std::vector<uint32_t> top_end;  // top nodes of level L end at top_end[L]
-  uint32_t n_top = 0, n_ranges = 0, n_seg = 1, hctr[4] = {0, 0, 0, 0};
-  bool top = false;
   const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
   const uint32_t hist_n = 256 * n_tiles;
   const uint32_t scan_blocks = (hist_n + 1023) / 1024;
@@ -1790,9 +2442,6 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   uint32_t n_in = 0;
   CollapseItem root_item;
   std::vector<uint32_t> level_end(1, 1u);  // wide nodes of level L end at level_end[L]
-  std::vector<uint32_t> round_end;         // binary nodes of PLOC round r end at round_end[r]
-  float* dp_cost = nullptr;
-  uint8_t* dp_dec = nullptr;
   const uint32_t W = m->width;
   const size_t F4 = J3DG_NODE_F4(W);
 
@@ -1848,257 +2497,6 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
     m->max_depth = 0;
     J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4, st));
     J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * F4, st));
-    goto cleanup;
-  }
-
-  if (!(m->build_flags & J3DG_BUILD_LBVH)) {
-    uint32_t mcount = nt, node_base = 0, iters = 0, htot[2] = {0, 0}, root = 0;
-    const uint32_t sblocks_max = (nt + 1023) / 1024;
-    J3DG_DROP(k0);
-    J3DG_CK(cudaMallocAsync((void**)&child, sizeof(uint2) * (nt - 1), st));
-    J3DG_CK(cudaMallocAsync((void**)&box, sizeof(BinNode) * (nt - 1), st));
-    J3DG_CK(cudaMallocAsync((void**)&count, sizeof(uint32_t) * (nt - 1), st));
-    J3DG_CK(cudaMallocAsync((void**)&C0, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&C1, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&nn, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&cscan, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&sscan, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&pl_sums, sizeof(uint32_t) * (sblocks_max + 1), st));
-    J3DG_CK(cudaMallocAsync((void**)&pl_sums2, sizeof(uint32_t) * (sblocks_max + 1), st));
-    J3DG_CK(cudaMallocAsync((void**)&tot, sizeof(uint32_t) * 2, st));
-    J3DG_CK(cudaMallocAsync((void**)&lo0, sizeof(float4) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&hi0, sizeof(float4) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&lo1, sizeof(float4) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&hi1, sizeof(float4) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&seg0, sizeof(uint32_t) * nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&seg1, sizeof(uint32_t) * nt, st));
-    // exclusive scan of n words (n <= nt)
-    const auto scan_u32 = [&](const uint32_t* in, uint32_t* out, uint32_t n) {
-      const uint32_t sb = (n + 1023) / 1024;
-      k_scan_chunks<<<sb, 256, 0, st>>>(in, out, n, pl_sums);
-      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, nullptr, sb, nullptr);
-      k_scan_add<<<sb, 256, 0, st>>>(out, n, pl_sums);
-    };
-    top = J3DG_SAH_TOP > 0 && nt > J3DG_SAH_TOP;
-    if (top) {
-      const uint32_t cap_tasks = nt / J3DG_SAH_TOP + 1;  // tasks of one level are disjoint, each > J3DG_SAH_TOP
-      const size_t bin_words = (size_t)cap_tasks * 3 * kTopBins * kTopVals;
-      J3DG_CK(cudaMallocAsync((void**)&ord_a, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&ord_b, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&task_of, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&task_of2, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&tbox_lo, sizeof(float4) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&tbox_hi, sizeof(float4) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&codes, sizeof(uint16_t) * nt, st));
-      k_top_boxes<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, tbox_lo, tbox_hi);
-      J3DG_CK(cudaMallocAsync((void**)&seg_starts, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&seg_scan, sizeof(uint32_t) * nt, st));
-      J3DG_CK(cudaMallocAsync((void**)&top_bins, sizeof(uint32_t) * bin_words, st));
-      J3DG_CK(cudaMallocAsync((void**)&top_ctr, sizeof(uint32_t) * 4, st));
-      J3DG_CK(cudaMallocAsync((void**)&tasks_a, sizeof(TopTask) * cap_tasks, st));
-      J3DG_CK(cudaMallocAsync((void**)&tasks_b, sizeof(TopTask) * cap_tasks, st));
-      J3DG_CK(cudaMallocAsync((void**)&splits, sizeof(TopSplit) * cap_tasks, st));
-      J3DG_CK(cudaMallocAsync((void**)&ranges, sizeof(TopRange) * nt, st));  // at most one range per triangle
-      {
-        TopTask r0;
-        r0.begin = 0;
-        r0.end = nt;
-        r0.node = 0;
-        r0.pad = 0;
-        r0.clo = make_float4(hbb[0], hbb[1], hbb[2], 0.f);  // the vertex bbox holds every centroid
-        r0.chi = make_float4(hbb[3], hbb[4], hbb[5], 0.f);
-        J3DG_CK(cudaMemcpyAsync(tasks_a, &r0, sizeof(r0), cudaMemcpyHostToDevice, st));
-      }
-      hctr[0] = 1u;  // nodes allocated (the root)
-      hctr[1] = hctr[2] = 0u;
-      hctr[3] = nt;  // the largest task: the root
-      J3DG_CK(cudaMemcpyAsync(top_ctr, hctr, sizeof(hctr), cudaMemcpyHostToDevice, st));
-      k_iota<<<(nt + 255) / 256, 256, 0, st>>>(ord_a, nt);
-      J3DG_CK(cudaMemsetAsync(task_of, 0, sizeof(uint32_t) * nt, st));
-      top_end.push_back(1u);
-      uint32_t n_tasks = 1;
-      while (n_tasks > 0) {
-        // levels whose tasks are all at most kTopWarpTask triangles need
-        // only the per-warp binning (which splits them too)
-        if (hctr[3] > kTopWarpTask) {
-          const uint32_t words = n_tasks * 3 * kTopBins * kTopVals;
-          k_top_bins_init<<<(words + 255) / 256, 256, 0, st>>>(top_bins, words, tasks_a);
-          k_top_bin<<<(nt + kTopChunk - 1) / kTopChunk, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, task_of, tasks_a,
-                                                                       n_tasks, nt, top_bins, codes);
-        }
-        k_top_bin_warp<<<(n_tasks + 7) / 8, 256, 0, st>>>(ord_a, tbox_lo, tbox_hi, tasks_a, n_tasks, splits, box,
-                                                          count, codes);
-        if (hctr[3] > kTopWarpTask)
-          k_top_split<<<(n_tasks + 3) / 4, 128, 0, st>>>(tasks_a, n_tasks, top_bins, splits, box, count);
-        J3DG_CK(cudaMemsetAsync(top_ctr + 1, 0, sizeof(uint32_t), st));
-        J3DG_CK(cudaMemsetAsync(top_ctr + 3, 0, sizeof(uint32_t), st));
-        k_top_children<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks_a, splits, n_tasks, J3DG_SAH_TOP, top_ctr,
-                                                               tasks_b, ranges, child, cap_tasks, nt, nt - 1,
-                                                               d_status);
-        k_top_flag_scan<<<sblocks_max, 256, 0, st>>>(task_of, codes, tasks_a, splits, n_tasks, nt, cscan, pl_sums);
-        k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, nullptr, sblocks_max, nullptr);
-        k_top_scatter<<<(nt + 1023) / 1024, 256, 0, st>>>(ord_a, ord_b, task_of, task_of2, codes, tasks_a, splits,
-                                                          n_tasks, cscan, pl_sums, nt, d_status);
-        std::swap(ord_a, ord_b);
-        std::swap(task_of, task_of2);
-        J3DG_CK(cudaGetLastError());
-        J3DG_CK(cudaMemcpyAsync(hctr, top_ctr, sizeof(hctr), cudaMemcpyDeviceToHost, st));
-        J3DG_CK(cudaStreamSynchronize(st));
-        if (hctr[1] > cap_tasks || hctr[2] > nt || hctr[0] > nt - 1 || ++iters > 100000) {
-          err = "SAH top levels overran their bounds";
-          rc = J3DG_ERR_CUDA;
-          goto cleanup;
-        }
-        n_tasks = hctr[1];
-        if (hctr[0] > top_end.back()) top_end.push_back(hctr[0]);
-        std::swap(tasks_a, tasks_b);
-      }
-      iters = 0;
-      n_top = hctr[0];
-      n_ranges = hctr[2];
-      node_base = n_top;
-      // segments numbered in position order: a flag at each range's start, one scan
-      J3DG_CK(cudaMemsetAsync(seg_starts, 0, sizeof(uint32_t) * nt, st));
-      k_top_seg_starts<<<(n_ranges + 255) / 256, 256, 0, st>>>(ranges, n_ranges, nt, seg_starts);
-      scan_u32(seg_starts, seg_scan, nt);
-      k_ploc_init_seg<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, ord_a, nt, seg_starts, seg_scan, C0,
-                                                        lo0, hi0, seg0);
-      n_seg = n_ranges;
-      J3DG_DROP(ord_a);
-      J3DG_DROP(ord_b);
-      J3DG_DROP(task_of);
-      J3DG_DROP(task_of2);
-      J3DG_DROP(tbox_lo);
-      J3DG_DROP(tbox_hi);
-      J3DG_DROP(codes);
-      J3DG_DROP(top_bins);
-      J3DG_DROP(tasks_a);
-      J3DG_DROP(tasks_b);
-      J3DG_DROP(splits);
-    } else {
-      k_ploc_init<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, C0, lo0, hi0);
-      J3DG_CK(cudaMemsetAsync(seg0, 0, sizeof(uint32_t) * nt, st));
-      n_seg = 1;
-    }
-    J3DG_CK(cudaGetLastError());
-    while (mcount > n_seg) {
-      const uint32_t blocks = (mcount + kPlocBlock - 1) / kPlocBlock, sb = (mcount + 1023) / 1024;
-      k_ploc_nn<<<blocks, kPlocBlock, 0, st>>>(lo0, hi0, seg0, mcount, nn);
-      k_ploc_flag_scan<<<sb, 256, 0, st>>>(nn, mcount, cscan, sscan, pl_sums, pl_sums2);
-      k_scan_sums<<<1, 1024, 0, st>>>(pl_sums, pl_sums2, sb, tot);
-      J3DG_CK(cudaGetLastError());
-      J3DG_CK(cudaMemcpyAsync(htot, tot, sizeof(htot), cudaMemcpyDeviceToHost, st));
-      J3DG_CK(cudaStreamSynchronize(st));
-      if (htot[0] == 0 || htot[1] >= mcount || node_base + htot[0] > nt - 1 || ++iters > 100000) {
-        err = "PLOC clustering made no progress";
-        rc = J3DG_ERR_CUDA;
-        goto cleanup;
-      }
-      k_ploc_merge<<<blocks, kPlocBlock, 0, st>>>(C0, lo0, hi0, seg0, nn, cscan, sscan, pl_sums, pl_sums2, mcount,
-                                                 node_base, C1, lo1, hi1, seg1, child, box, count);
-      J3DG_CK(cudaGetLastError());
-      node_base += htot[0];
-      round_end.push_back(node_base);
-      mcount = htot[1];
-      std::swap(C0, C1);
-      std::swap(lo0, lo1);
-      std::swap(hi0, hi1);
-      std::swap(seg0, seg1);
-    }
-    if (top) {
-      k_top_link<<<(n_ranges + 255) / 256, 256, 0, st>>>(ranges, n_ranges, seg_starts, seg_scan, C0, n_seg, child,
-                                                         d_status);
-      J3DG_CK(cudaGetLastError());
-      root = 0;
-    } else {
-      J3DG_CK(cudaMemcpyAsync(&root, C0, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    }
-    J3DG_CK(cudaStreamSynchronize(st));
-    if (node_base != nt - 1 || (root & 0x80000000u)) {
-      err = "PLOC clustering ended with a malformed tree";
-      rc = J3DG_ERR_CUDA;
-      goto cleanup;
-    }
-    // the binary tree (child, box, count) is all the collapse needs
-    J3DG_DROP(C0);
-    J3DG_DROP(C1);
-    J3DG_DROP(nn);
-    J3DG_DROP(cscan);
-    J3DG_DROP(sscan);
-    J3DG_DROP(lo0);
-    J3DG_DROP(hi0);
-    J3DG_DROP(lo1);
-    J3DG_DROP(hi1);
-    J3DG_DROP(seg0);
-    J3DG_DROP(seg1);
-    J3DG_DROP(seg_starts);
-    J3DG_DROP(seg_scan);
-    J3DG_DROP(ranges);
-    if (J3DG_SAH_COLLAPSE) {
-      J3DG_CK(cudaMallocAsync((void**)&dp_cost, sizeof(float) * W * (nt - 1), st));
-      J3DG_CK(cudaMallocAsync((void**)&dp_dec, sizeof(uint8_t) * W * (nt - 1), st));
-      // children before parents: the PLOC rounds in order, then the top levels deepest first
-      uint32_t lo_n = n_top;
-      for (uint32_t hi_n : round_end) {
-        launch_collapse_cost(W, child, box, count, (const float4*)m->d_tris, lo_n, hi_n, m->leaf_size, dp_cost, dp_dec,
-                             st);
-        lo_n = hi_n;
-      }
-      for (size_t k = top_end.size(); k-- > 0;) {
-        const uint32_t lo_t = k ? top_end[k - 1] : 0u, hi_t = top_end[k];
-        launch_collapse_cost(W, child, box, count, (const float4*)m->d_tris, lo_t, hi_t, m->leaf_size, dp_cost, dp_dec,
-                             st);
-      }
-      J3DG_CK(cudaGetLastError());
-    }
-    J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
-    J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * F4 * (size_t)nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&pa, sizeof(PlaceItem) * (size_t)nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&pb, sizeof(PlaceItem) * (size_t)nt, st));
-    J3DG_CK(cudaMallocAsync((void**)&tris_out, sizeof(float4) * 3 * (size_t)nt, st));
-    {
-      const PlaceItem root_place{root, 0u, 1u, 0u};
-      J3DG_CK(cudaMemcpyAsync(pa, &root_place, sizeof(root_place), cudaMemcpyHostToDevice, st));
-    }
-    hc[0] = 0u;
-    hc[1] = 1u;  // wide nodes allocated (the root)
-    hc[2] = 0u;  // queue out
-    hc[3] = 0u;  // max depth
-    J3DG_CK(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
-    n_in = 1;
-    {
-      uint32_t n_wide = 1;  // wide nodes allocated (the root); a level's nodes follow the previous level's
-      while (n_in > 0) {
-        J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
-        launch_collapse_place(W, child, box, count, (const float4*)m->d_tris, pa, n_in, pb, counters + 2, n_wide, wide,
-                              m->leaf_size, counters + 3, tris_out, nt, d_status, dp_dec, st);
-        J3DG_CK(cudaGetLastError());
-        J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
-        J3DG_CK(cudaStreamSynchronize(st));
-        n_in = hc[2];
-        if (n_in > nt - n_wide) {
-          err = "BVH collapse overran its node bound";
-          rc = J3DG_ERR_CUDA;
-          goto cleanup;
-        }
-        n_wide += n_in;
-        if (n_wide > level_end.back()) level_end.push_back(n_wide);
-        std::swap(pa, pb);
-      }
-      hc[1] = n_wide;
-    }
-    m->n_nodes = hc[1];
-    m->max_depth = hc[3];
-    m->root_ref = 0;
-    J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4 * (size_t)m->n_nodes, st));
-    if (J3DG_DFS_ORDER)
-      J3DG_CK(dfs_order(W, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
-    else
-      J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * F4 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
-    J3DG_CK(cudaStreamSynchronize(st));
-    cudaFreeAsync(m->d_tris, st);  // the leaf-ordered triangles are the placed ones now
-    m->d_tris = tris_out;
-    tris_out = nullptr;
     goto cleanup;
   }
 
@@ -2172,26 +2570,8 @@ cleanup:
   if (other) cudaFreeAsync(other, st);
   if (counters) cudaFreeAsync(counters, st);
   if (wide) cudaFreeAsync(wide, st);
-  if (dp_cost) cudaFreeAsync(dp_cost, st);
-  for (uint32_t* q : {ord_a, ord_b, task_of, task_of2, seg0, seg1, seg_starts, seg_scan, top_bins, top_ctr})
-    if (q) cudaFreeAsync(q, st);
-  if (tbox_lo) cudaFreeAsync(tbox_lo, st);
-  if (tbox_hi) cudaFreeAsync(tbox_hi, st);
-  if (codes) cudaFreeAsync(codes, st);
-  if (tasks_a) cudaFreeAsync(tasks_a, st);
-  if (tasks_b) cudaFreeAsync(tasks_b, st);
-  if (splits) cudaFreeAsync(splits, st);
-  if (ranges) cudaFreeAsync(ranges, st);
-  if (dp_dec) cudaFreeAsync(dp_dec, st);
   if (qa) cudaFreeAsync(qa, st);
   if (qb) cudaFreeAsync(qb, st);
-  for (uint32_t* p : {C0, C1, nn, cscan, sscan, pl_sums, pl_sums2, count, tot})
-    if (p) cudaFreeAsync(p, st);
-  for (float4* p : {lo0, hi0, lo1, hi1})
-    if (p) cudaFreeAsync(p, st);
-  if (pa) cudaFreeAsync(pa, st);
-  if (pb) cudaFreeAsync(pb, st);
-  if (tris_out) cudaFreeAsync(tris_out, st);
   {
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == J3DG_OK && e != cudaSuccess) {

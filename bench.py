@@ -234,7 +234,7 @@ def side_workloads(ctx, mesh, wl, args) -> dict:
         from j3d_gb300 import build_meshes
         b = Wk.config2()
         t0 = time.perf_counter()
-        meshes = build_meshes(ctx, b.meshes)  # concurrently, 8 builds in flight
+        meshes = build_meshes(ctx, b.meshes, rebuildable=True)  # concurrently, 8 builds in flight
         ctx.synchronize()
         build_s = time.perf_counter() - t0
         mc = Matcap.make(ctx, 0)
@@ -256,10 +256,16 @@ def side_workloads(ctx, mesh, wl, args) -> dict:
         ms = ev_ms(g.launch, 3)
         prim = sum(cv.width * cv.height for cv, _, _ in frames)
         rays = prim + sum(cv.count_hits()[0] for cv, _, _ in frames)
+        g.close()
+        # all 64 builds, then all 1024 frames, in one graph launch
+        g = Batch(ctx, frames, rebuild=True)
+        ms_rb = ev_ms(g.launch, 3)
         out["batch_config2"] = {"frames": len(frames), "ms_per_launch": round(ms, 3),
                                 "mrays_s": round(rays / ms / 1e3, 1), "rays": rays,
                                 "triangles": int(sum(len(T) for _, T in b.meshes)),
-                                "builds_64_wall_s": round(build_s, 3)}
+                                "builds_64_wall_s": round(build_s, 3),
+                                "builds_and_frames_one_graph_ms": round(ms_rb, 3),
+                                "builds_in_graph_ms": round(ms_rb - ms, 3)}
         g.close()
         for cv, _, _ in frames:
             cv.close()
@@ -581,7 +587,8 @@ def run_batch(args):
     for m in serial:
         m.close()
     t0 = time.perf_counter()
-    meshes = build_meshes(ctx, wl.meshes, [tuner.table[bucket_of(len(T))].leaf_size for _, T in wl.meshes], width)
+    meshes = build_meshes(ctx, wl.meshes, [tuner.table[bucket_of(len(T))].leaf_size for _, T in wl.meshes], width,
+                          rebuildable=True)
     ctx.synchronize()
     build_s = time.perf_counter() - t0
     build_ms = sum(m.info().build_ms for m in meshes)
@@ -626,6 +633,11 @@ def run_batch(args):
     ms_batch = timed(lambda: render_batch(ctx, frames), args.steps)
     g = Batch(ctx, frames)
     ms_graph = timed(g.launch, args.steps)
+    g.close()
+    # the configuration as specified: all builds, then all frames, one graph launch
+    g = Batch(ctx, frames, rebuild=True)
+    ms_rebuild = timed(g.launch, args.steps)
+    g.close()
     line = {"metric": "Mrays/s, batched frames (config 2)", "value": round(rays / (ms_graph / 1e3) / 1e6, 3),
             "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms_graph, 3), "higher_is_better": True, "dtype": "f32",
@@ -636,6 +648,8 @@ def run_batch(args):
                        "graph_ms": round(ms_graph, 3), "per_frame_launches_mrays_s": round(rays / ms_single / 1e3, 3),
                        "one_launch_mrays_s": round(rays / ms_batch / 1e3, 3),
                        "builds_ms_device": round(build_ms, 2), "builds_wall_s": round(build_s, 3),
+                       "builds_and_frames_one_graph_ms": round(ms_rebuild, 3),
+                       "builds_in_graph_ms": round(ms_rebuild - ms_graph, 3),
                        "builds_one_by_one_wall_s": round(serial_s, 3),
                        "autotune_s": round(tune_s, 2),
                        "autotune": {str(b): {"width": c.width, "leaf": c.leaf_size, "block": c.block_threads,

@@ -143,6 +143,11 @@ typedef struct j3dg_build_opts {
    a width; all-hits queries, voxel grids and learned networks need width 4. */
 #define J3DG_BUILD_WIDTH2 0x2u
 #define J3DG_BUILD_WIDTH8 0x4u
+/* A mesh that a batch can rebuild inside its graph (j3dg_batch_create2 with
+   J3DG_BATCH_REBUILD): it keeps a device copy of its vertices and its node
+   array at the size bound (nt - 1 nodes), so the rebuild writes in place.
+   Default builder only (not LBVH). No reference counterpart. */
+#define J3DG_BUILD_REBUILDABLE 0x8u
 
 typedef struct j3dg_mesh_info {
   uint32_t n_vertices;
@@ -227,6 +232,11 @@ int j3dg_mesh_build_many(j3dg_ctx* ctx, uint32_t n, const j3dg_mesh_source* sour
                          uint32_t max_concurrent, j3dg_mesh** out);
 int j3dg_mesh_destroy(j3dg_mesh* mesh);
 int j3dg_mesh_get_info(const j3dg_mesh* mesh, j3dg_mesh_info* info);
+/* Copies the first `bytes` of the mesh's BVH node array (n_nodes nodes of
+   16, 32 or 64 floats by the width: planes [6][W], refs [W], padding) to
+   host memory; for tools that export or check a tree. No reference
+   counterpart. */
+int j3dg_mesh_get_nodes(const j3dg_mesh* mesh, void* dst, uint64_t bytes);
 /* scene_object::triangle_normals (scene.h:14): n_triangles x 3 floats out. */
 int j3dg_mesh_get_triangle_normals(const j3dg_mesh* mesh, float* normals);
 /* Optional per-mesh data for the textured / vertex-colour branches of
@@ -477,6 +487,17 @@ int j3dg_batch_create(j3dg_ctx* ctx, const j3dg_frame* frames, uint32_t n, j3dg_
 /* Replaces frame i's scene (camera pose, objects) for the next launches; the
    number of objects must not exceed the one given at creation. Waits for
    the previous launch of this batch. */
+/* As j3dg_batch_create, with flags. J3DG_BATCH_REBUILD: every launch first
+   rebuilds the BVH of every mesh of the batch's scenes from the mesh's kept
+   vertices and triangles (all built with J3DG_BUILD_REBUILDABLE, default
+   builder), then renders the frames: builds and frames are one graph launch
+   (builds of up to 8 meshes at a time on forked capture streams, each
+   build's level loops device-driven). A rebuild gives the mesh the same tree
+   as its first build. Other work must not use these meshes while a launch
+   runs. No reference counterpart (the reference builds on the host, one
+   mesh at a time). */
+#define J3DG_BATCH_REBUILD 0x1u
+int j3dg_batch_create2(j3dg_ctx* ctx, const j3dg_frame* frames, uint32_t n, uint32_t flags, j3dg_batch** out);
 int j3dg_batch_set_scene(j3dg_batch* b, uint32_t i, const j3dg_scene* scene);
 int j3dg_batch_launch(j3dg_batch* b);
 int j3dg_batch_destroy(j3dg_batch* b);

@@ -117,6 +117,7 @@ SIGNATURES = {
     "j3dg_mesh_build": (_I, [_P, _P, _U, _P, _U, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_mesh_destroy": (_I, [_P]),
     "j3dg_mesh_get_info": (_I, [_P, C.POINTER(MeshInfo)]),
+    "j3dg_mesh_get_nodes": (_I, [_P, _P, C.c_uint64]),
     "j3dg_mesh_get_triangle_normals": (_I, [_P, _P]),
     "j3dg_mesh_set_vertex_colors": (_I, [_P, _P]),
     "j3dg_mesh_set_uv": (_I, [_P, _P]),
@@ -167,6 +168,7 @@ SIGNATURES = {
     "j3dg_ctx_set_primary_mode": (_I, [_P, _I]),
     "j3dg_canvas_last_primary": (_I, [_P]),
     "j3dg_batch_create": (_I, [_P, C.POINTER(Frame), _U, C.POINTER(_P)]),
+    "j3dg_batch_create2": (_I, [_P, C.POINTER(Frame), _U, _U, C.POINTER(_P)]),
     "j3dg_batch_set_scene": (_I, [_P, _U, C.POINTER(Scene)]),
     "j3dg_batch_launch": (_I, [_P]),
     "j3dg_batch_destroy": (_I, [_P]),

@@ -24,6 +24,11 @@
 namespace j3dg {
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
               std::string& err);
+struct RebuildLane;
+int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, cudaStream_t st, RebuildLane** out,
+                       std::string& err);
+void rebuild_lane_free(RebuildLane* L, cudaStream_t st);
+cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st, cudaStream_t side, uint32_t* d_status);
 }
 
 using j3dg::DevInst;
@@ -270,7 +275,9 @@ void free_mesh_buffers(j3dg_mesh* m) {
   cudaFree(m->d_colors);
   cudaFree(m->d_uv);
   cudaFree(m->d_tex);
+  cudaFree(m->d_verts);
   m->d_nodes = m->d_tris = m->d_normals = m->d_slot_of = m->d_index = m->d_colors = m->d_uv = m->d_tex = nullptr;
+  m->d_verts = nullptr;
 }
 
 int shade_mode_of(const j3dg_canvas_settings& s) {
@@ -715,7 +722,7 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
   m->build_flags = opts ? opts->flags : 0u;
   {
     const uint32_t f = m->build_flags;
-    if (f & ~(uint32_t)(J3DG_BUILD_LBVH | J3DG_BUILD_WIDTH2 | J3DG_BUILD_WIDTH8)) {
+    if (f & ~(uint32_t)(J3DG_BUILD_LBVH | J3DG_BUILD_WIDTH2 | J3DG_BUILD_WIDTH8 | J3DG_BUILD_REBUILDABLE)) {
       delete m;
       msg = "mesh_build: unknown build flags";
       return J3DG_ERR_INVALID_ARGUMENT;
@@ -729,6 +736,11 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
     if (m->width != 4 && (f & J3DG_BUILD_LBVH)) {
       delete m;
       msg = "mesh_build: the LBVH builder makes 4-wide trees only";
+      return J3DG_ERR_UNSUPPORTED;
+    }
+    if ((f & J3DG_BUILD_REBUILDABLE) && (f & J3DG_BUILD_LBVH)) {
+      delete m;
+      msg = "mesh_build: rebuildable meshes use the default builder";
       return J3DG_ERR_UNSUPPORTED;
     }
   }
@@ -755,6 +767,15 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
   } else {
     std::string err;
     rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, st, c->d_status, err);
+    if (rc == J3DG_OK && (m->build_flags & J3DG_BUILD_REBUILDABLE)) {  // the vertices a batch rebuilds from
+      cudaError_t ev = cudaMalloc(&m->d_verts, sizeof(float) * 3 * (size_t)nv);
+      if (ev == cudaSuccess)
+        ev = cudaMemcpyAsync(m->d_verts, dV, sizeof(float) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, st);
+      if (ev != cudaSuccess) {
+        rc = ev == cudaErrorMemoryAllocation ? J3DG_ERR_OUT_OF_MEMORY : J3DG_ERR_CUDA;
+        err = std::string("keeping the vertices: ") + cudaGetErrorString(ev);
+      }
+    }
     if (rc == J3DG_OK) {
       cudaEventRecord(ev1, st);
       cudaEventSynchronize(ev1);
@@ -854,6 +875,17 @@ int j3dg_mesh_destroy(j3dg_mesh* m) {
   all(m->ctx)->ex.last_slot = -1;  // the cached instance table may name this mesh
   free_mesh_buffers(m);
   delete m;
+  return J3DG_OK;
+}
+
+int j3dg_mesh_get_nodes(const j3dg_mesh* m, void* dst, uint64_t bytes) {
+  if (!m || (!dst && bytes)) return J3DG_ERR_INVALID_ARGUMENT;
+  const uint64_t have = sizeof(float4) * J3DG_NODE_F4(m->width) * (uint64_t)m->n_nodes;
+  if (bytes > have) return fail(m->ctx, J3DG_ERR_INVALID_ARGUMENT, "mesh_get_nodes: more bytes than the node array");
+  if (!bytes) return J3DG_OK;
+  cudaSetDevice(m->ctx->device);
+  CK(m->ctx, cudaStreamSynchronize(S(m->ctx)), "mesh_get_nodes");
+  CK(m->ctx, cudaMemcpy(dst, m->d_nodes, bytes, cudaMemcpyDeviceToHost), "mesh_get_nodes");
   return J3DG_OK;
 }
 
@@ -1513,6 +1545,12 @@ struct j3dg_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t done = nullptr;
+  // J3DG_BATCH_REBUILD: the meshes rebuilt ahead of the frames, by lane
+  std::vector<j3dg::RebuildLane*> lanes;
+  std::vector<std::vector<const j3dg_mesh*>> lane_meshes;
+  std::vector<cudaStream_t> lane_streams;
+  std::vector<cudaEvent_t> lane_events;  // [0]: the fork, then one join per lane
+  cudaStream_t side = nullptr;           // captures the builds' loop bodies
 };
 
 int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
@@ -1542,7 +1580,36 @@ int j3dg_render_batch(j3dg_ctx* c, const j3dg_frame* f, uint32_t n) {
 }
 
 int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch** out) {
+  return j3dg_batch_create2(c, f, n, 0u, out);
+}
+
+namespace {
+
+// the distinct meshes of the frames' scenes, split into up to 8 lanes of
+// about equal triangle counts (largest first, each to the lightest lane)
+void rebuild_lanes(const j3dg_frame* f, uint32_t n, std::vector<std::vector<const j3dg_mesh*>>& lanes) {
+  std::vector<const j3dg_mesh*> ms;
+  for (uint32_t i = 0; i < n; ++i)
+    if (f[i].scene)
+      for (uint32_t k = 0; k < f[i].scene->n_objects; ++k) ms.push_back(f[i].scene->objects[k].mesh);
+  std::sort(ms.begin(), ms.end());
+  ms.erase(std::unique(ms.begin(), ms.end()), ms.end());
+  std::stable_sort(ms.begin(), ms.end(), [](const j3dg_mesh* a, const j3dg_mesh* b) { return a->nt > b->nt; });
+  const size_t K = std::min<size_t>(8, ms.size());
+  lanes.assign(K, {});
+  std::vector<uint64_t> load(K, 0);
+  for (const j3dg_mesh* m : ms) {
+    const size_t k = std::min_element(load.begin(), load.end()) - load.begin();
+    lanes[k].push_back(m);
+    load[k] += m->nt;
+  }
+}
+
+}  // namespace
+
+int j3dg_batch_create2(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t flags, j3dg_batch** out) {
   if (!c || !out || n == 0 || !f) return J3DG_ERR_INVALID_ARGUMENT;
+  if (flags & ~J3DG_BATCH_REBUILD) return fail(c, J3DG_ERR_INVALID_ARGUMENT, "batch_create2: unknown flags");
   *out = nullptr;
   cudaSetDevice(c->device);
   uint32_t total_inst = 0, width = 4;
@@ -1574,12 +1641,64 @@ int j3dg_batch_create(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, j3dg_batch**
     return cuda_fail(c, e, "batch_create");
   }
   b->work = reinterpret_cast<uint32_t*>(b->d + b->L.bytes);
+  int rc = J3DG_OK;
+  if (flags & J3DG_BATCH_REBUILD) {
+    rebuild_lanes(b->frames.data(), n, b->lane_meshes);
+    for (const auto& lane : b->lane_meshes)
+      for (const j3dg_mesh* m : lane)
+        if (!m->d_verts && m->nt > m->leaf_size) {
+          j3dg_batch_destroy(b);
+          return fail(c, J3DG_ERR_UNSUPPORTED, "batch_create2: rebuilt meshes must be built with J3DG_BUILD_REBUILDABLE");
+        }
+    std::string err;
+    for (const auto& lane : b->lane_meshes) {
+      uint32_t nt_max = 2, nv_max = 3;
+      for (const j3dg_mesh* m : lane) {
+        nt_max = std::max(nt_max, m->nt);
+        nv_max = std::max(nv_max, m->nv);
+      }
+      j3dg::RebuildLane* L = nullptr;
+      rc = j3dg::rebuild_lane_alloc(nt_max, nv_max, width, S(c), &L, err);
+      if (rc != J3DG_OK) {
+        j3dg_batch_destroy(b);
+        return fail(c, rc, "batch_create2: " + err);
+      }
+      b->lanes.push_back(L);
+      cudaStream_t ls = nullptr;
+      e = cudaStreamCreateWithFlags(&ls, cudaStreamNonBlocking);
+      if (e == cudaSuccess) b->lane_streams.push_back(ls);
+      cudaEvent_t ev = nullptr;
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) b->lane_events.push_back(ev);
+      if (e != cudaSuccess) break;
+    }
+    cudaEvent_t fork = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->lane_events.insert(b->lane_events.begin(), fork);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S(c));  // the scratch is allocated before the capture
+    if (e != cudaSuccess) {
+      j3dg_batch_destroy(b);
+      return cuda_fail(c, e, "batch_create2");
+    }
+  }
   const uint32_t items =
       pack_frames(b->frames.data(), n, b->L, b->h, b->d, b->caps.data(), all(c)->ex.top_level, b->walk, b->fits, b->top);
-  // capture: upload of the staged parameters, the launch and the shading passes
+  // capture: the rebuilds (forked lanes, joined before the frames), the
+  // upload of the staged parameters, the launch and the shading passes
   cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   e = cudaStreamBeginCapture(S(c), mode);
-  int rc = J3DG_OK;
+  if (e == cudaSuccess && !b->lanes.empty()) {
+    e = cudaEventRecord(b->lane_events[0], S(c));
+    for (size_t k = 0; e == cudaSuccess && k < b->lanes.size(); ++k) {
+      cudaStream_t ls = b->lane_streams[k];
+      e = cudaStreamWaitEvent(ls, b->lane_events[0], 0);
+      for (size_t i = 0; e == cudaSuccess && i < b->lane_meshes[k].size(); ++i)
+        e = j3dg::rebuild_enqueue(b->lanes[k], b->lane_meshes[k][i], ls, b->side, c->d_status);
+      if (e == cudaSuccess) e = cudaEventRecord(b->lane_events[k + 1], ls);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(S(c), b->lane_events[k + 1], 0);
+    }
+  }
   if (e == cudaSuccess) {
     e = cudaMemcpyAsync(b->d, b->h, b->L.bytes, cudaMemcpyHostToDevice, S(c));
     if (e == cudaSuccess) rc = enqueue_batch(c, b->frames.data(), n, b->L, b->d, items, b->work, b->top, b->width);
@@ -1656,6 +1775,11 @@ int j3dg_batch_destroy(j3dg_batch* b) {
   cudaStreamSynchronize(S(b->ctx));
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  for (j3dg::RebuildLane* L : b->lanes) j3dg::rebuild_lane_free(L, S(b->ctx));
+  cudaStreamSynchronize(S(b->ctx));
+  for (cudaStream_t ls : b->lane_streams) cudaStreamDestroy(ls);
+  for (cudaEvent_t ev : b->lane_events) cudaEventDestroy(ev);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->done) cudaEventDestroy(b->done);
   cudaFree(b->d);
   if (b->h) cudaFreeHost(b->h);

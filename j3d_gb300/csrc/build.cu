@@ -2116,7 +2116,7 @@ struct BuildPlan {
 
 static const int kBBoxBlocks = 1024;
 
-static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st) {
+static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st, bool outputs = true) {
   const size_t nt = P.nt, F4 = J3DG_NODE_F4(P.W);
   cudaError_t e = cudaSuccess;
   auto A = [&](auto*& p, size_t bytes) {
@@ -2170,11 +2170,13 @@ static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st) {
   A(P.dfs_size, sizeof(uint32_t) * nt);
   A(P.dfs_pos, sizeof(uint32_t) * nt);
   A(P.ctl, sizeof(BuildCtl));
-  A(P.normals, sizeof(float4) * nt);
   A(P.soup, sizeof(float4) * 3 * nt);
-  A(P.tris_out, sizeof(float4) * 3 * nt);
-  A(P.nodes, sizeof(float4) * F4 * nt);  // the wide nodes are at most nt - 1
-  A(P.slot_of, sizeof(uint32_t) * nt);
+  if (outputs) {  // else the mesh's own arrays (a rebuild in place)
+    A(P.normals, sizeof(float4) * nt);
+    A(P.tris_out, sizeof(float4) * 3 * nt);
+    A(P.nodes, sizeof(float4) * F4 * nt);  // the wide nodes are at most nt - 1
+    A(P.slot_of, sizeof(uint32_t) * nt);
+  }
   return e;
 }
 
@@ -2377,8 +2379,13 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
     m->max_depth = h.max_depth;
     m->root_ref = 0;
     const size_t bytes = sizeof(float4) * J3DG_NODE_F4(P.W) * (size_t)m->n_nodes;
-    e = cudaMallocAsync(&m->d_nodes, bytes, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(m->d_nodes, P.nodes, bytes, cudaMemcpyDeviceToDevice, st);
+    if (m->build_flags & J3DG_BUILD_REBUILDABLE) {  // the node array stays at the size bound: rebuilds write in place
+      m->d_nodes = P.nodes;
+      P.nodes = nullptr;
+    } else {
+      e = cudaMallocAsync(&m->d_nodes, bytes, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(m->d_nodes, P.nodes, bytes, cudaMemcpyDeviceToDevice, st);
+    }
     if (e == cudaSuccess) {
       m->d_normals = P.normals;
       m->d_tris = P.tris_out;
@@ -2408,9 +2415,60 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
     err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack at width " + std::to_string(W);
     return J3DG_ERR_UNSUPPORTED;
   }
-  m->device_bytes = sizeof(float4) * J3DG_NODE_F4(W) * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
+  m->device_bytes = sizeof(float4) * J3DG_NODE_F4(W) *
+                        (uint64_t)((m->build_flags & J3DG_BUILD_REBUILDABLE) ? m->nt : (m->n_nodes ? m->n_nodes : 1)) +
                     sizeof(float4) * 4 * (uint64_t)m->nt + sizeof(uint32_t) * 4 * (uint64_t)m->nt;
   return J3DG_OK;
+}
+
+// ---------------------------------------------------- batch rebuilds ----
+//
+// A batch's graph rebuilds its meshes in place: each lane (a forked capture
+// stream) owns one build's scratch, sized for its largest mesh, and builds
+// its meshes one after another into their own arrays.
+
+struct RebuildLane {
+  BuildPlan P;  // scratch only; nt = the lane's largest mesh
+};
+
+int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, cudaStream_t st, RebuildLane** out,
+                       std::string& err) {
+  RebuildLane* L = new (std::nothrow) RebuildLane();
+  if (!L) return J3DG_ERR_OUT_OF_MEMORY;
+  L->P.nt = nt_max;
+  L->P.nv = nv_max;
+  L->P.W = W;
+  L->P.top = J3DG_SAH_TOP > 0 && nt_max > J3DG_SAH_TOP;
+  const cudaError_t e = plan_alloc(L->P, st, false);
+  if (e != cudaSuccess) {
+    plan_free(L->P, st);
+    delete L;
+    err = std::string("batch rebuild scratch: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? J3DG_ERR_OUT_OF_MEMORY : J3DG_ERR_CUDA;
+  }
+  *out = L;
+  return J3DG_OK;
+}
+
+void rebuild_lane_free(RebuildLane* L, cudaStream_t st) {
+  if (!L) return;
+  plan_free(L->P, st);
+  delete L;
+}
+
+// enqueues (under a capture) the rebuild of mesh m into its own arrays
+cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st, cudaStream_t side, uint32_t* d_status) {
+  if (m->nt <= m->leaf_size) return cudaSuccess;  // one leaf: nothing to rebuild
+  BuildPlan Pm = L->P;  // the lane's scratch, this mesh's sizes and arrays
+  Pm.nt = m->nt;
+  Pm.nv = m->nv;
+  Pm.leaf = m->leaf_size;
+  Pm.top = J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
+  Pm.normals = (float4*)m->d_normals;
+  Pm.tris_out = (float4*)m->d_tris;
+  Pm.nodes = (float4*)m->d_nodes;
+  Pm.slot_of = (uint32_t*)m->d_slot_of;
+  return enqueue_build(Pm, (const float*)m->d_verts, (const uint32_t*)m->d_index, st, side, d_status);
 }
 
 // Builds the device BVH. dV and dT are device arrays. On success fills the

@@ -73,6 +73,7 @@ struct j3dg_mesh {
   void* d_normals = nullptr;  // float4[nt], by triangle id
   void* d_slot_of = nullptr;  // uint32[nt]: leaf-order position of each triangle id
   void* d_index = nullptr;    // uint32[3 * nt], the caller's triangles
+  void* d_verts = nullptr;    // float[3 * nv], kept by rebuildable meshes (J3DG_BUILD_REBUILDABLE)
   void* d_colors = nullptr;   // float[3 * nv] or null
   void* d_uv = nullptr;       // float[6 * nt] or null
   void* d_tex = nullptr;      // uint32[tex_w * tex_h] or null

@@ -115,16 +115,19 @@ class Mesh:
 
     BUILDERS = {"ploc": 0, "lbvh": 1}
     WIDTHS = {2: 0x2, 4: 0, 8: 0x4}  # J3DG_BUILD_WIDTH2 / (default) / J3DG_BUILD_WIDTH8
+    REBUILDABLE = 0x8  # J3DG_BUILD_REBUILDABLE
 
-    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2, build: str = "ploc", width: int = 4):
+    def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2, build: str = "ploc", width: int = 4,
+                 rebuildable: bool = False):
         """build: "ploc" (surface-area clustering, the default: fewer node
         visits per ray) or "lbvh" (Morton splits, about half the build time);
-        width: children per BVH node, 2, 4 (default) or 8."""
+        width: children per BVH node, 2, 4 (default) or 8; rebuildable: keep
+        what a Batch(rebuild=True) rebuilds the BVH from, inside its graph."""
         self.ctx = ctx
         nv = int(vertices.shape[0]) if vertices.ndim > 1 else int(vertices.size // 3)
         nt = int(triangles.shape[0]) if triangles.ndim > 1 else int(triangles.size // 3)
         h = C.c_void_p()
-        opts = BuildOpts(leaf_size, Mesh.BUILDERS[build] | Mesh.WIDTHS[width])
+        opts = BuildOpts(leaf_size, Mesh.BUILDERS[build] | Mesh.WIDTHS[width] | (Mesh.REBUILDABLE if rebuildable else 0))
         _check(ctx.h, lib().j3dg_mesh_build(ctx.h, vptr(vertices), nv, vptr(triangles), nt, C.byref(opts),
                                             C.byref(h)))
         self.h = h
@@ -145,6 +148,15 @@ class Mesh:
         i = MeshInfo()
         _check(self.ctx.h, lib().j3dg_mesh_get_info(self.h, C.byref(i)))
         return i
+
+    def nodes(self) -> np.ndarray:
+        """The BVH node array (n_nodes x 4 * width float32 words: planes
+        [6][W], refs [W], padding) as host bytes."""
+        i = self.info()
+        words = {2: 16, 4: 32, 8: 64}[i.width]
+        out = np.empty((i.n_nodes, words), np.float32)
+        _check(self.ctx.h, lib().j3dg_mesh_get_nodes(self.h, vptr(out), out.nbytes))
+        return out
 
     def triangle_normals(self) -> np.ndarray:
         i = self.info()
@@ -260,10 +272,11 @@ class ScenePointCloud:
 
 
 def build_meshes(ctx: Context, meshes, leaf_sizes=None, width: int = 4, build: str = "ploc",
-                 max_concurrent: int = 8) -> list:
+                 max_concurrent: int = 8, rebuildable: bool = False) -> list:
     """Many meshes built at once (j3dg_mesh_build_many): [(vertices,
     triangles)] -> [Mesh], up to max_concurrent builds in flight on their
-    own streams. leaf_sizes: one per mesh, or None for 2."""
+    own streams. leaf_sizes: one per mesh, or None for 2; rebuildable: as
+    for Mesh."""
     n = len(meshes)
     srcs = (_ffi.MeshSource * max(1, n))()
     keep = []
@@ -278,7 +291,7 @@ def build_meshes(ctx: Context, meshes, leaf_sizes=None, width: int = 4, build: s
     opts = (BuildOpts * max(1, n))()
     for i in range(n):
         opts[i] = BuildOpts(int(leaf_sizes[i]) if leaf_sizes is not None else 2,
-                            Mesh.BUILDERS[build] | Mesh.WIDTHS[width])
+                            Mesh.BUILDERS[build] | Mesh.WIDTHS[width] | (Mesh.REBUILDABLE if rebuildable else 0))
     hs = (C.c_void_p * max(1, n))()
     _check(ctx.h, lib().j3dg_mesh_build_many(ctx.h, n, C.cast(srcs, C.c_void_p), C.cast(opts, C.c_void_p),
                                              max_concurrent, C.cast(hs, C.c_void_p)))
@@ -589,14 +602,16 @@ def render_batch(ctx: Context, frames) -> None:
 
 
 class Batch:
-    """A fixed set of frames captured as a CUDA graph; set_scene() moves cameras."""
+    """A fixed set of frames captured as a CUDA graph; set_scene() moves cameras.
+    rebuild=True: every launch first rebuilds the BVHs of the scenes' meshes
+    (built rebuildable) inside the same graph (J3DG_BATCH_REBUILD)."""
 
-    def __init__(self, ctx: Context, frames):
+    def __init__(self, ctx: Context, frames, rebuild: bool = False):
         self.ctx = ctx
         self.frames = list(frames)
         arr, keep = _frames(self.frames)
         h = C.c_void_p()
-        _check(ctx.h, lib().j3dg_batch_create(ctx.h, arr, len(self.frames), C.byref(h)))
+        _check(ctx.h, lib().j3dg_batch_create2(ctx.h, arr, len(self.frames), 0x1 if rebuild else 0, C.byref(h)))
         self.h = h
         ctx._own(self)
         del keep

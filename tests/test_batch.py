@@ -159,3 +159,71 @@ def test_build_many_equals_single_builds(gpu_ctx):
     bad = [srcs[0], (srcs[1][0], np.zeros((0, 3), np.uint32))]
     with pytest.raises(J3dgError):
         build_meshes(gpu_ctx, bad)
+
+
+def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod):
+    """Batch(rebuild=True): every launch first rebuilds the BVHs of its
+    scenes' meshes (built rebuildable) inside the graph, on forked capture
+    streams with device-driven level loops, then renders. After two launches
+    every mesh's node array equals the one its standalone build made, byte
+    for byte (the rebuild is the same build), and one frame of every mesh
+    equals the oracle's. Meshes from 2 triangles (a single leaf) to 80k, on
+    both sides of the SAH / PLOC split, 12 of them so that lanes rebuild
+    several meshes in turn."""
+    from helpers import compare_gbuffers, oracle_scene
+
+    from j3d_gb300 import Batch, Canvas, J3dgError, Matcap, Mesh, Scene, camera_for_vfov, settings, workloads as W
+    O = oracle_mod
+    quad_V = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], np.float32)
+    quad_T = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    srcs = [(quad_V, quad_T)]
+    srcs += [W.icosphere(k, W.SEED_BASE + 90 + k) for k in (1, 2, 3, 4, 5, 6)]
+    srcs += [W.torus(nu, nv, seed=W.SEED_BASE + 100 + nu) for nu, nv in ((8, 4), (40, 20), (120, 60), (200, 100),
+                                                                           (282, 141))]
+    meshes = [Mesh(gpu_ctx, V, T, rebuildable=True) for V, T in srcs]
+    nodes0 = [m.nodes() for m in meshes]
+    mc = Matcap.make(gpu_ctx, 0)
+    poses = W.cameras(len(meshes), W.SEED_BASE + 110, 2.5, 3.5)
+    frames, sizes = [], []
+    for i, m in enumerate(meshes):
+        sc = Scene()
+        sc.add_object(m, db_id=i + 1)
+        sc.prepare_scene()
+        sc.unzoom()
+        sc.set_pose(poses[i])
+        w, h = (320, 240) if i % 2 else (256, 256)
+        cv = Canvas(gpu_ctx, w, h)
+        cv.set_camera(camera_for_vfov(60.0))
+        cv.set_background_color()
+        cv.update_settings(settings(shadow=True, edges=False))
+        frames.append((cv, sc, mc))
+        sizes.append((w, h))
+    g = Batch(gpu_ctx, frames, rebuild=True)
+    for _ in range(2):
+        g.launch()
+    gpu_ctx.synchronize()
+    for i, m in enumerate(meshes):
+        assert np.array_equal(m.nodes().view(np.uint32), nodes0[i].view(np.uint32)), f"mesh {i}: rebuilt nodes"
+    mco, cav = O.make_matcap(0)
+    for i, (V, T) in enumerate(srcs):
+        cv, sc, _ = frames[i]
+        w, h = sizes[i]
+        om, views, _ = oracle_scene(O, V, T, poses[i:i + 1], w, h)
+        op = O.fresh_pixels(w, h)
+        oi = np.zeros((h, w), np.uint32)
+        O.render_frame(op, oi, O.fill_background(w, h), [(om, np.eye(4, dtype=np.float32).reshape(16), i + 1)],
+                       views[0], O.settings(shadow=True, edges=False), mco, cav)
+        assert compare_gbuffers(cv.get_pixels(), op, f"rebuild batch, mesh {i} ({len(T)} tris)") == 0
+        assert np.array_equal(cv.get_image(), oi), f"rebuild batch, mesh {i}: RGBA"
+    g.close()
+    # a mesh built without the flag cannot be rebuilt
+    plain = Mesh(gpu_ctx, *srcs[3])
+    sc = Scene()
+    sc.add_object(plain)
+    sc.prepare_scene()
+    sc.unzoom()
+    sc.set_pose(poses[3])
+    with pytest.raises(J3dgError):
+        Batch(gpu_ctx, [(frames[0][0], sc, mc)], rebuild=True)
+    for cv, _, _ in frames:
+        cv.close()

@@ -740,6 +740,38 @@ def primary_rays(pose, pinv, w, h, near, t_near):
     return rays
 
 
+def run_build(args):
+    """The config-1 mesh's BVH builds alone: warm builds of the 28.09M-triangle
+    torus with the default builder (one CUDA graph with device-driven level
+    loops) and with the LBVH builder, CUDA-event times from the library."""
+    from j3d_gb300 import Context, Mesh, build as B, workloads as Wk
+    B.build()
+    wl = Wk.config1(N_CAMERAS, W_, H_)
+    ctx = Context(0)
+    out = {}
+    for name in ("ploc", "lbvh"):
+        ms = []
+        for k in range(args.warmup + args.steps):
+            m = Mesh(ctx, wl.vertices, wl.triangles, args.leaf, name, args.width)
+            if k >= args.warmup:
+                ms.append(m.info().build_ms)
+            info = m.info()
+            m.close()
+        out[name] = {"ms_median": round(float(np.median(ms)), 3), "ms": [round(x, 2) for x in ms],
+                     "nodes": int(info.n_nodes), "depth": int(info.max_depth)}
+    nt = len(wl.triangles)
+    med = out["ploc"]["ms_median"]
+    line = {"metric": "BVH build ms, 28.09M-triangle torus (config 1)", "value": med, "unit": "ms", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": med, "higher_is_better": False,
+            "dtype": "f32", "data": "synthetic (seeded displaced torus)",
+            "config": {"workload": "torus R=1 r=0.35 5300x2650 grid, 28,090,000 tris", "leaf": args.leaf,
+                       "width": args.width, "default_builder": out["ploc"], "lbvh_builder": out["lbvh"],
+                       "mtris_per_s": round(nt / (med / 1e3) / 1e6, 1),
+                       "alg_gbs": round((nt * (48 + 24) + out["ploc"]["nodes"] * 128) / (med / 1e3) / 1e9, 1)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned(args):
     """Learned tmax (config 3): the 4096-cluster network trained on 50M rays
     of the 28.09M-triangle torus, then learned vs plain closest hit on the
@@ -751,6 +783,8 @@ def run_learned(args):
     from j3d_gb300.learned import Learned
     B.build()
     wl = Wk.config1(N_CAMERAS, W_, H_)
+    if args.learned_mesh == "icosphere":  # a small case of the same kernels (profiling)
+        wl.vertices, wl.triangles = Wk.icosphere(7, Wk.SEED_BASE + 76)
     ctx = Context(0)
     # the LBVH: its depth-6 subtrees are Morton-ordered ranges of the mesh,
     # the "4096 spatial clusters (Morton order)" of this configuration
@@ -1154,13 +1188,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-side", action="store_true", help="skip the short runs of the other configurations")
     ap.add_argument("--workload", default="torus",
-                    choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects", "config0"],
+                    choices=["torus", "batch", "serve", "learned", "ingest", "pointcloud", "objects", "config0", "build"],
                     help="torus: the headline 28M-triangle frames; batch: config-2 batched frames; "
                          "serve: config-4 request serving")
     ap.add_argument("--serve-rate", type=float, default=400.0)
     ap.add_argument("--serve-requests", type=int, default=1200)
     ap.add_argument("--serve-train-rays", type=int, default=4_000_000, help="training rays per mesh (learned serving)")
     ap.add_argument("--learned-rays", type=int, default=50_000_000)
+    ap.add_argument("--learned-mesh", default="torus", choices=["torus", "icosphere"],
+                    help="icosphere: a 327,680-triangle mesh instead of the 28M torus (a small case of the same "
+                         "kernels, for profiling)")
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--batch-cameras", type=int, default=16)
     args = ap.parse_args()
@@ -1178,6 +1215,8 @@ def main():
         return run_objects(args)
     if args.workload == "config0":
         return run_config0(args)
+    if args.workload == "build":
+        return run_build(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_own(args)

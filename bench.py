@@ -531,8 +531,9 @@ def run_own(args):
                      "frac": round(achieved / peak, 4),
                      "traffic": FRAME_TRAFFIC[args.build][0] if args.leaf == 2 and args.width == 4 else None,
                      "traffic_l2": FRAME_TRAFFIC[args.build][1] if args.leaf == 2 and args.width == 4 else None,
-                     "traffic_note": "bytes per k_frame launch (ncu, mean of the 32 cameras); the algorithmic "
-                                     "bytes per launch are bytes_per_ray x rays_per_step / 32",
+                     "traffic_note": "DRAM (and L2) bytes per k_frame launch: mean of two launches (cameras 8 "
+                                     "and 9) of one ncu capture; the algorithmic bytes per launch are bytes_per_ray "
+                                     "x rays_per_step / 32",
                      "kernel": "k_frame (primary + shadow + shading, one launch per frame)", "peak_kind": peak_kind,
                      "bytes_per_ray": round(alg_bytes / rays_per_step, 1),
                      "node_visits_per_ray": round(node_per_ray, 3), "tri_tests_per_ray": round(tri_per_ray, 3),

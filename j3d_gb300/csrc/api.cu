@@ -25,8 +25,8 @@ namespace j3dg {
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
               std::string& err);
 struct RebuildLane;
-int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, cudaStream_t st, RebuildLane** out,
-                       std::string& err);
+int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, bool ploc, bool lbvh, cudaStream_t st,
+                       RebuildLane** out, std::string& err);
 void rebuild_lane_free(RebuildLane* L, cudaStream_t st);
 cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st, cudaStream_t side, uint32_t* d_status);
 }
@@ -736,11 +736,6 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
     if (m->width != 4 && (f & J3DG_BUILD_LBVH)) {
       delete m;
       msg = "mesh_build: the LBVH builder makes 4-wide trees only";
-      return J3DG_ERR_UNSUPPORTED;
-    }
-    if ((f & J3DG_BUILD_REBUILDABLE) && (f & J3DG_BUILD_LBVH)) {
-      delete m;
-      msg = "mesh_build: rebuildable meshes use the default builder";
       return J3DG_ERR_UNSUPPORTED;
     }
   }
@@ -1653,12 +1648,14 @@ int j3dg_batch_create2(j3dg_ctx* c, const j3dg_frame* f, uint32_t n, uint32_t fl
     std::string err;
     for (const auto& lane : b->lane_meshes) {
       uint32_t nt_max = 2, nv_max = 3;
+      bool ploc = false, lbvh = false;  // the builders the lane's meshes use
       for (const j3dg_mesh* m : lane) {
         nt_max = std::max(nt_max, m->nt);
         nv_max = std::max(nv_max, m->nv);
+        if (m->nt > m->leaf_size) ((m->build_flags & J3DG_BUILD_LBVH) ? lbvh : ploc) = true;
       }
       j3dg::RebuildLane* L = nullptr;
-      rc = j3dg::rebuild_lane_alloc(nt_max, nv_max, width, S(c), &L, err);
+      rc = j3dg::rebuild_lane_alloc(nt_max, nv_max, width, ploc || !lbvh, lbvh, S(c), &L, err);
       if (rc != J3DG_OK) {
         j3dg_batch_destroy(b);
         return fail(c, rc, "batch_create2: " + err);

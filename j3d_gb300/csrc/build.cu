@@ -479,14 +479,22 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 }
 __device__ __forceinline__ float half_area4(float4 lo, float4 hi) { return half_area(lo, hi); }
 
-__global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __restrict__ box,
-                           const uint2* __restrict__ range, const float4* __restrict__ tris,
-                           const CollapseItem* __restrict__ qin, uint32_t n_in, CollapseItem* __restrict__ qout,
-                           uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide, float4* __restrict__ wide,
-                           uint32_t leaf_size, uint32_t* __restrict__ max_depth) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_in) return;
-  CollapseItem it = qin[t];
+// One binary node of the LBVH's 4-wide collapse: it becomes wide node
+// it.wide, whose slots are its children, the largest-area child opened until
+// four slots are filled (or every slot is small enough to be a leaf); the
+// slots that stay internal get wide nodes (n_wide) and are queued for the
+// next level (n_out). bound: the wide array's and the queue's size; an index
+// past it raises J3DG_DEV_BAD_INDEX and is not written.
+__device__ __forceinline__ void collapse_one(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                                             const uint2* __restrict__ range, const float4* __restrict__ tris,
+                                             const CollapseItem it, CollapseItem* __restrict__ qout,
+                                             uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide,
+                                             float4* __restrict__ wide, uint32_t bound, uint32_t leaf_size,
+                                             uint32_t* __restrict__ max_depth, uint32_t* __restrict__ status) {
+  if (it.wide >= bound) {
+    atomicOr(status, J3DG_DEV_BAD_INDEX);
+    return;
+  }
   uint32_t ref[4];
   float4 lo[4], hi[4];
   uint32_t cnt[4];
@@ -539,9 +547,13 @@ __global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __res
         uint32_t first = (ref[s] & 0x80000000u) ? (ref[s] & 0x7fffffffu) : range[ref[s]].x;
         out_ref[s] = J3DG_LEAF_BIT | (first << 3) | (cnt[s] - 1u);
       } else {
-        uint32_t w = atomicAdd(n_wide, 1u);
-        uint32_t q = atomicAdd(n_out, 1u);
-        qout[q] = CollapseItem{ref[s], w, it.depth + 1};
+        const uint32_t w = atomicAdd(n_wide, 1u);
+        const uint32_t q = atomicAdd(n_out, 1u);
+        if (w < bound && q < bound) {
+          qout[q] = CollapseItem{ref[s], w, it.depth + 1};
+        } else {
+          atomicOr(status, J3DG_DEV_BAD_INDEX);
+        }
         out_ref[s] = w;
       }
     } else {
@@ -555,6 +567,19 @@ __global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __res
                      __uint_as_float(out_ref[3]));
   W[7] = make_float4(0.f, 0.f, 0.f, 0.f);
   atomicMax(max_depth, it.depth);
+}
+
+// One level of the collapse: the level's item count is read from the device
+// (n_in_p) and the grid strides over it.
+__global__ void k_collapse(const uint2* __restrict__ child, const BinNode* __restrict__ box,
+                           const uint2* __restrict__ range, const float4* __restrict__ tris,
+                           const CollapseItem* __restrict__ qin, const uint32_t* __restrict__ n_in_p,
+                           CollapseItem* __restrict__ qout, uint32_t* __restrict__ n_out, uint32_t* __restrict__ n_wide,
+                           float4* __restrict__ wide, uint32_t bound, uint32_t leaf_size, uint32_t* __restrict__ max_depth,
+                           uint32_t* __restrict__ status) {
+  const uint32_t n_in = *n_in_p;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_in; t += gridDim.x * blockDim.x)
+    collapse_one(child, box, range, tris, qin[t], qout, n_out, n_wide, wide, bound, leaf_size, max_depth, status);
 }
 
 // -------------------------------------------------------- 5b. PLOC ----
@@ -1059,10 +1084,6 @@ __global__ void k_collapse_place(const uint2* __restrict__ child, const BinNode*
 // next level), so subtree sizes go bottom-up and new positions top-down, one
 // launch per level.
 
-#ifndef J3DG_DFS_ORDER
-#define J3DG_DFS_ORDER 1
-#endif
-
 template <int W>
 __device__ __forceinline__ void child_refs(const float4* __restrict__ wide, uint32_t i, uint32_t (&r)[W]) {
   const float* f = reinterpret_cast<const float*>(wide + J3DG_NODE_F4(W) * (size_t)i) + 6 * W;
@@ -1125,55 +1146,21 @@ __global__ void k_dfs_permute(const float4* __restrict__ wide, const uint32_t* _
   for (int k = 0; k < F4; ++k) dst[k] = make_float4(F[4 * k], F[4 * k + 1], F[4 * k + 2], F[4 * k + 3]);
 }
 
-// out = the n wide nodes of `wide` (root 0, level L = [level_end[L-1],
-// level_end[L]) with level_end[-1] = 0) in depth-first order; root stays 0.
-// Host-driven (the LBVH builder's levels are known on the host): the
-// levels' node ranges go to the device once, the kernels read them there.
-template <int W>
-static cudaError_t dfs_order_w(const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end, float4* out,
-                               cudaStream_t st) {
-  const size_t L = level_end.size();
-  std::vector<uint32_t> h(2 * L + 1);
-  for (size_t l = 0; l < L; ++l) {
-    h[2 * l] = l ? level_end[l - 1] : 0u;
-    h[2 * l + 1] = level_end[l];
-  }
-  h[2 * L] = n;
-  uint32_t *size = nullptr, *pos = nullptr, *rng = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&size, sizeof(uint32_t) * (size_t)n, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&pos, sizeof(uint32_t) * (size_t)n, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&rng, sizeof(uint32_t) * h.size(), st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(rng, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice, st);
-  for (size_t l = L; e == cudaSuccess && l-- > 0;) {
-    const uint32_t cnt = h[2 * l + 1] - h[2 * l];
-    if (cnt) k_dfs_size<W><<<(cnt + 255) / 256, 256, 0, st>>>(wide, rng + 2 * l, size);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaMemsetAsync(pos, 0, sizeof(uint32_t), st);
-  for (size_t l = 0; e == cudaSuccess && l < L; ++l) {
-    const uint32_t cnt = h[2 * l + 1] - h[2 * l];
-    if (cnt) k_dfs_place<W><<<(cnt + 255) / 256, 256, 0, st>>>(wide, rng + 2 * l, size, pos);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) {
-    k_dfs_permute<W><<<(n + 255) / 256, 256, 0, st>>>(wide, rng + 2 * L, pos, out);
-    e = cudaGetLastError();
-  }
-  if (size) cudaFreeAsync(size, st);
-  if (pos) cudaFreeAsync(pos, st);
-  if (rng) cudaFreeAsync(rng, st);
-  return e;
-}
-
-static cudaError_t dfs_order(uint32_t W, const float4* wide, uint32_t n, const std::vector<uint32_t>& level_end,
-                             float4* out, cudaStream_t st) {
-  if (W == 2) return dfs_order_w<2>(wide, n, level_end, out, st);
-  if (W == 8) return dfs_order_w<8>(wide, n, level_end, out, st);
-  return dfs_order_w<4>(wide, n, level_end, out, st);
-}
-
 // the device-driven builder's fixed grids (grid-stride kernels)
 static const uint32_t kStrideBlocks = 2048;
+
+// one full wave of 128-thread blocks (16 per SM): the collapse kernels are
+// chains of dependent loads per item, so every resident thread slot is used
+static uint32_t wave_blocks128() {
+  static uint32_t blocks = 0;
+  if (!blocks) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    blocks = sms > 0 ? 16u * (uint32_t)sms : kStrideBlocks;
+  }
+  return blocks;
+}
 
 static void launch_collapse_cost(uint32_t W, const uint2* child, const BinNode* box, const uint32_t* count,
                                  const float4* tris, const uint32_t* lohi, uint32_t leaf_size, float* cost,
@@ -1192,13 +1179,13 @@ static void launch_collapse_place(uint32_t W, const uint2* child, const BinNode*
                                   uint32_t* max_depth, float4* tris_out, uint32_t nt, uint32_t* status,
                                   const uint8_t* dec, cudaStream_t st) {
   if (W == 2)
-    k_collapse_place<2><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+    k_collapse_place<2><<<wave_blocks128(), 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
                                                       leaf_size, max_depth, tris_out, nt, status, dec);
   else if (W == 8)
-    k_collapse_place<8><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+    k_collapse_place<8><<<wave_blocks128(), 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
                                                       leaf_size, max_depth, tris_out, nt, status, dec);
   else
-    k_collapse_place<4><<<kStrideBlocks, 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
+    k_collapse_place<4><<<wave_blocks128(), 128, 0, st>>>(child, box, count, tris, qin, n_in, qout, n_out, wide_base, wide,
                                                       leaf_size, max_depth, tris_out, nt, status, dec);
 }
 
@@ -1879,9 +1866,10 @@ __global__ void k_slot_of(const float4* __restrict__ tris, uint32_t nt, uint32_t
 
 // ------------------------------------------------ device-driven build ----
 //
-// The default builder (binned-SAH top levels, PLOC below them, the
-// cost-optimal collapse, depth-first numbering) runs as one CUDA graph with
-// no host round trip: every level loop is a conditional while node whose
+// A build (the default: binned-SAH top levels, PLOC below them, the
+// cost-optimal collapse; or the LBVH: the one-pass tree and its collapse;
+// then the depth-first numbering) runs as one CUDA graph with no host round
+// trip: every level loop is a conditional while node whose
 // body ends in a one-thread step kernel, which advances the loop state kept
 // in device memory (BuildCtl) and sets the loop's condition. Kernels read
 // their sizes from BuildCtl and stride over them with fixed grids, so one
@@ -1895,13 +1883,14 @@ static const uint32_t kMaxTopLevels = 1024, kMaxRounds = 1024, kMaxPlaceLevels =
 
 struct BuildCtl {
   uint32_t top_ctr[4];  // k_top_children: [0] top nodes, [1] next level's tasks, [2] ranges, [3] largest next task
+                        // (LBVH: [0] the root that k_lbvh found)
   uint32_t n_tasks, max_task, ord_parity, top_levels;
   uint32_t mcount, n_seg, node_base, c_parity, rounds, tot[2];
   uint32_t lohi[2];  // the running pass's node range (collapse costs, depth-first levels)
   uint32_t pass, n_pass;
   uint32_t n_in, n_out, n_wide, place_levels, max_depth;
   int32_t dfs_level;
-  uint32_t error;  // a loop overran its bound: 1 SAH levels, 2 PLOC, 4 placement
+  uint32_t error;  // a loop overran its bound: 1 SAH levels, 2 PLOC, 4 placement / collapse
   uint32_t top_end[kMaxTopLevels];     // top nodes of level L end at top_end[L]
   uint32_t round_end[kMaxRounds];      // binary nodes of PLOC round r end at round_end[r]
   uint32_t level_end[kMaxPlaceLevels]; // wide nodes of level L end at level_end[L]
@@ -2042,6 +2031,26 @@ __global__ void k_dfs_step(BuildCtl* __restrict__ c, uint32_t up, cudaGraphCondi
   cudaGraphSetConditional(h, (c->dfs_level >= 0 && c->dfs_level < (int32_t)c->place_levels) ? 1u : 0u);
 }
 
+// the LBVH's collapse starts at the root that k_lbvh left in top_ctr[0]
+__global__ void k_lbvh_root(BuildCtl* __restrict__ c, CollapseItem* __restrict__ qa) {
+  qa[0] = CollapseItem{c->top_ctr[0], 0u, 1u};
+}
+
+// after an LBVH collapse level: k_collapse allocated its wide nodes itself
+__global__ void k_lbvh_step(BuildCtl* __restrict__ c, uint32_t nt, cudaGraphConditionalHandle h, uint32_t set) {
+  if (c->n_in) {  // the level ran
+    if (c->n_wide > nt || c->n_out > nt || c->place_levels >= kMaxPlaceLevels) {
+      c->error |= 4u;
+      c->n_in = 0;
+    } else {
+      if (c->n_wide > c->level_end[c->place_levels - 1]) c->level_end[c->place_levels++] = c->n_wide;
+      c->n_in = c->n_out;
+    }
+    c->n_out = 0;
+  }
+  if (set) cudaGraphSetConditional(h, c->n_in > 0 ? 1u : 0u);
+}
+
 // Appends a while node (condition initially 1) to the graph that `st` is
 // capturing; `body(side, handle)` enqueues the loop body on `side`, which
 // captures it into the node's body graph.
@@ -2080,7 +2089,11 @@ static cudaError_t capture_while(cudaStream_t st, cudaStream_t side, Body&& body
 // where the tree decides: the wide nodes, the queues).
 struct BuildPlan {
   uint32_t nv = 0, nt = 0, W = 4, leaf = 2;
-  bool top = false;
+  bool top = false;   // binned-SAH top levels (the default builder, large meshes)
+  bool lbvh = false;  // this build is an LBVH (J3DG_BUILD_LBVH)
+  // the builders the scratch serves: PLOC (the default) and / or LBVH (a
+  // batch's rebuild lane may serve both)
+  bool need_ploc = true, need_lbvh = false;
   // scratch
   float* part = nullptr;
   float* bb = nullptr;
@@ -2102,6 +2115,8 @@ struct BuildPlan {
   uint8_t* dp_dec = nullptr;
   float4* wide = nullptr;
   PlaceItem *pa = nullptr, *pb = nullptr;
+  uint2* range = nullptr;  // LBVH: each binary node's leaf range
+  CollapseItem *qa = nullptr, *qb = nullptr;
   uint32_t *dfs_size = nullptr, *dfs_pos = nullptr;
   BuildCtl* ctl = nullptr;
   // outputs (the mesh keeps them)
@@ -2148,29 +2163,36 @@ static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st, bool outputs = true
   }
   A(P.child, sizeof(uint2) * (nt - 1));
   A(P.box, sizeof(BinNode) * (nt - 1));
-  A(P.count, sizeof(uint32_t) * (nt - 1));
-  A(P.C0, sizeof(uint32_t) * nt);
-  A(P.C1, sizeof(uint32_t) * nt);
-  A(P.nn, sizeof(uint32_t) * nt);
-  A(P.cscan, sizeof(uint32_t) * nt);
-  A(P.sscan, sizeof(uint32_t) * nt);
-  A(P.pl_sums, sizeof(uint32_t) * (P.sblocks() + 1));
-  A(P.pl_sums2, sizeof(uint32_t) * (P.sblocks() + 1));
-  A(P.seg0, sizeof(uint32_t) * nt);
-  A(P.seg1, sizeof(uint32_t) * nt);
-  A(P.lo0, sizeof(float4) * nt);
-  A(P.hi0, sizeof(float4) * nt);
-  A(P.lo1, sizeof(float4) * nt);
-  A(P.hi1, sizeof(float4) * nt);
-  A(P.dp_cost, sizeof(float) * P.W * (nt - 1));
-  A(P.dp_dec, sizeof(uint8_t) * P.W * (nt - 1));
+  A(P.count, sizeof(uint32_t) * (nt - 1));  // LBVH: the sibling handshake of k_lbvh
+  if (P.need_ploc) {
+    A(P.C0, sizeof(uint32_t) * nt);
+    A(P.C1, sizeof(uint32_t) * nt);
+    A(P.nn, sizeof(uint32_t) * nt);
+    A(P.cscan, sizeof(uint32_t) * nt);
+    A(P.sscan, sizeof(uint32_t) * nt);
+    A(P.pl_sums, sizeof(uint32_t) * (P.sblocks() + 1));
+    A(P.pl_sums2, sizeof(uint32_t) * (P.sblocks() + 1));
+    A(P.seg0, sizeof(uint32_t) * nt);
+    A(P.seg1, sizeof(uint32_t) * nt);
+    A(P.lo0, sizeof(float4) * nt);
+    A(P.hi0, sizeof(float4) * nt);
+    A(P.lo1, sizeof(float4) * nt);
+    A(P.hi1, sizeof(float4) * nt);
+    A(P.dp_cost, sizeof(float) * P.W * (nt - 1));
+    A(P.dp_dec, sizeof(uint8_t) * P.W * (nt - 1));
+    A(P.pa, sizeof(PlaceItem) * nt);
+    A(P.pb, sizeof(PlaceItem) * nt);
+    A(P.soup, sizeof(float4) * 3 * nt);  // the LBVH gathers straight into the leaf order
+  }
+  if (P.need_lbvh) {
+    A(P.range, sizeof(uint2) * (nt - 1));
+    A(P.qa, sizeof(CollapseItem) * nt);
+    A(P.qb, sizeof(CollapseItem) * nt);
+  }
   A(P.wide, sizeof(float4) * F4 * nt);
-  A(P.pa, sizeof(PlaceItem) * nt);
-  A(P.pb, sizeof(PlaceItem) * nt);
   A(P.dfs_size, sizeof(uint32_t) * nt);
   A(P.dfs_pos, sizeof(uint32_t) * nt);
   A(P.ctl, sizeof(BuildCtl));
-  A(P.soup, sizeof(float4) * 3 * nt);
   if (outputs) {  // else the mesh's own arrays (a rebuild in place)
     A(P.normals, sizeof(float4) * nt);
     A(P.tris_out, sizeof(float4) * 3 * nt);
@@ -2185,46 +2207,26 @@ static void plan_free(BuildPlan& P, cudaStream_t st) {
   void* ps[] = {P.part, P.bb, P.k0, P.k1, P.v0, P.v1, P.hist, P.sums, P.ord_a, P.ord_b, P.task_of, P.task_of2,
                 P.seg_starts, P.seg_scan, P.top_bins, P.tbox_lo, P.tbox_hi, P.codes, P.tasks_a, P.tasks_b, P.splits,
                 P.ranges, P.child, P.box, P.count, P.C0, P.C1, P.nn, P.cscan, P.sscan, P.pl_sums, P.pl_sums2, P.seg0,
-                P.seg1, P.lo0, P.hi0, P.lo1, P.hi1, P.dp_cost, P.dp_dec, P.wide, P.pa, P.pb, P.dfs_size, P.dfs_pos,
-                P.ctl, P.normals, P.soup, P.tris_out, P.nodes, P.slot_of};
+                P.seg1, P.lo0, P.hi0, P.lo1, P.hi1, P.dp_cost, P.dp_dec, P.wide, P.pa, P.pb, P.range, P.qa, P.qb,
+                P.dfs_size, P.dfs_pos, P.ctl, P.normals, P.soup, P.tris_out, P.nodes, P.slot_of};
   for (void* p : ps)
     if (p) cudaFreeAsync(p, st);
   P = BuildPlan{};
 }
 
-// all of a build's work on `st` (capturing): no host synchronisation
-static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* dT, cudaStream_t st,
-                                 cudaStream_t side, uint32_t* d_status) {
-  const uint32_t nt = P.nt, nv = P.nv, W = P.W;
-  BuildCtl* c = P.ctl;
-  cudaError_t e = cudaSuccess;
-#define J3DG_EQ(x)                        \
-  do {                                    \
-    if (e == cudaSuccess) e = (x);        \
+#define J3DG_EQ(x)                                \
+  do {                                            \
+    if (e == cudaSuccess) e = (x);                \
     if (e == cudaSuccess) e = cudaGetLastError(); \
   } while (0)
-  J3DG_EQ(cudaMemsetAsync(c, 0, sizeof(BuildCtl), st));
-  k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(dV, nv, P.part);
-  k_bbox_final<<<1, 32, 0, st>>>(P.part, kBBoxBlocks, P.bb);
-  k_ctl_init<<<1, 1, 0, st>>>(c, P.tasks_a, P.bb, nt, P.top ? 1u : 0u);
-  k_tri_prep<<<(nt + 255) / 256, 256, 0, st>>>(dV, nv, dT, nt, P.bb, P.normals, P.k0, P.v0, d_status);
-  J3DG_EQ(cudaSuccess);
-  {
-    uint64_t *ka = P.k0, *kb = P.k1;
-    uint32_t *va = P.v0, *vb = P.v1;
-    for (int pass = 0; pass < kRadixPasses; ++pass) {
-      const int shift = 8 * pass;
-      k_radix_hist<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, nt, shift, P.n_tiles(), P.hist);
-      k_scan_chunks<<<P.scan_blocks(), 256, 0, st>>>(P.hist, P.hist, P.hist_n(), P.sums);
-      k_scan_sums<<<1, 1024, 0, st>>>(P.sums, nullptr, P.scan_blocks(), nullptr);
-      k_radix_scatter<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, va, kb, vb, nt, shift, P.n_tiles(), P.hist, P.sums,
-                                                           d_status);
-      std::swap(ka, kb);
-      std::swap(va, vb);
-    }
-    k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, va, nt, nv, P.soup, d_status);
-  }
-  J3DG_EQ(cudaSuccess);
+
+// the default builder's binary tree and wide nodes (P.wide, level ranges in
+// c->level_end): binned-SAH top levels over PLOC ranges (or PLOC alone), the
+// cost programme, the placement; the leaf-ordered triangles go to P.tris_out
+static cudaError_t enqueue_tree_ploc(BuildPlan& P, cudaStream_t st, cudaStream_t side, uint32_t* d_status) {
+  const uint32_t nt = P.nt, W = P.W;
+  BuildCtl* c = P.ctl;
+  cudaError_t e = cudaSuccess;
   const float4* soup = P.soup;
   if (P.top) {
     k_top_boxes<<<(nt + 255) / 256, 256, 0, st>>>(soup, nt, P.tbox_lo, P.tbox_hi);
@@ -2302,6 +2304,77 @@ static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* 
                           P.leaf, &c->max_depth, P.tris_out, nt, d_status, P.dp_dec, s);
     k_place_step<<<1, 1, 0, s>>>(c, nt, h, 1u);
   }));
+  return e;
+}
+
+// the LBVH (J3DG_BUILD_LBVH): Apetrei's one-pass binary tree over the sorted
+// Morton codes, then the 4-wide collapse level by level; the triangles are
+// already in leaf order (P.tris_out)
+static cudaError_t enqueue_tree_lbvh(BuildPlan& P, const uint64_t* keys, cudaStream_t st, cudaStream_t side,
+                                     uint32_t* d_status) {
+  const uint32_t nt = P.nt;
+  BuildCtl* c = P.ctl;
+  cudaError_t e = cudaSuccess;
+  J3DG_EQ(cudaMemsetAsync(P.count, 0xff, sizeof(uint32_t) * (nt - 1), st));
+  k_lbvh<<<(nt + 255) / 256, 256, 0, st>>>(keys, P.tris_out, nt, P.child, P.box, P.range, P.count, &c->top_ctr[0]);
+  k_lbvh_root<<<1, 1, 0, st>>>(c, P.qa);
+  J3DG_EQ(cudaSuccess);
+  J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
+    k_collapse<<<wave_blocks128(), 128, 0, s>>>(P.child, P.box, P.range, P.tris_out, P.qa, &c->n_in, P.qb, &c->n_out,
+                                             &c->n_wide, P.wide, nt, P.leaf, &c->max_depth, d_status);
+    k_lbvh_step<<<1, 1, 0, s>>>(c, nt, h, 0u);
+    k_collapse<<<wave_blocks128(), 128, 0, s>>>(P.child, P.box, P.range, P.tris_out, P.qb, &c->n_in, P.qa, &c->n_out,
+                                             &c->n_wide, P.wide, nt, P.leaf, &c->max_depth, d_status);
+    k_lbvh_step<<<1, 1, 0, s>>>(c, nt, h, 1u);
+  }));
+  return e;
+}
+
+// the sorted Morton codes after the radix passes (they alternate k0 / k1)
+static const uint64_t* sorted_keys(const BuildPlan& P) { return (kRadixPasses & 1) ? P.k1 : P.k0; }
+
+// A build's first part, whose launches do not depend on the tree: the loop
+// state reset, the bounding box, normals and Morton codes, the radix sort
+// and the gather into Morton order. No host synchronisation.
+static cudaError_t enqueue_prefix(BuildPlan& P, const float* dV, const uint32_t* dT, cudaStream_t st,
+                                  uint32_t* d_status) {
+  const uint32_t nt = P.nt, nv = P.nv;
+  BuildCtl* c = P.ctl;
+  cudaError_t e = cudaSuccess;
+  J3DG_EQ(cudaMemsetAsync(c, 0, sizeof(BuildCtl), st));
+  k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(dV, nv, P.part);
+  k_bbox_final<<<1, 32, 0, st>>>(P.part, kBBoxBlocks, P.bb);
+  k_ctl_init<<<1, 1, 0, st>>>(c, P.tasks_a, P.bb, nt, P.top ? 1u : 0u);
+  k_tri_prep<<<(nt + 255) / 256, 256, 0, st>>>(dV, nv, dT, nt, P.bb, P.normals, P.k0, P.v0, d_status);
+  J3DG_EQ(cudaSuccess);
+  {
+    uint64_t *ka = P.k0, *kb = P.k1;
+    uint32_t *va = P.v0, *vb = P.v1;
+    for (int pass = 0; pass < kRadixPasses; ++pass) {
+      const int shift = 8 * pass;
+      k_radix_hist<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, nt, shift, P.n_tiles(), P.hist);
+      k_scan_chunks<<<P.scan_blocks(), 256, 0, st>>>(P.hist, P.hist, P.hist_n(), P.sums);
+      k_scan_sums<<<1, 1024, 0, st>>>(P.sums, nullptr, P.scan_blocks(), nullptr);
+      k_radix_scatter<<<P.n_tiles(), kSortThreads, 0, st>>>(ka, va, kb, vb, nt, shift, P.n_tiles(), P.hist, P.sums,
+                                                           d_status);
+      std::swap(ka, kb);
+      std::swap(va, vb);
+    }
+    k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, va, nt, nv, P.lbvh ? P.tris_out : P.soup, d_status);
+  }
+  J3DG_EQ(cudaSuccess);
+  return e;
+}
+
+// The rest: the tree, its wide nodes, the depth-first numbering and the
+// triangles' slots; its level loops are conditional while nodes, so `st`
+// must be capturing.
+static cudaError_t enqueue_tree(BuildPlan& P, cudaStream_t st, cudaStream_t side, uint32_t* d_status) {
+  const uint32_t nt = P.nt, W = P.W;
+  BuildCtl* c = P.ctl;
+  cudaError_t e = cudaSuccess;
+  J3DG_EQ(P.lbvh ? enqueue_tree_lbvh(P, sorted_keys(P), st, side, d_status)
+                 : enqueue_tree_ploc(P, st, side, d_status));
   // depth-first numbering: subtree sizes bottom-up, positions top-down, permute
   auto dfs = [&](auto Wc) {
     constexpr int WW = decltype(Wc)::value;
@@ -2325,13 +2398,23 @@ static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* 
     dfs(std::integral_constant<int, 4>());
   k_slot_of<<<(nt + 255) / 256, 256, 0, st>>>(P.tris_out, nt, P.slot_of, d_status);
   J3DG_EQ(cudaSuccess);
-#undef J3DG_EQ
   return e;
 }
 
-// The default build through the device-driven graph: allocate, capture,
-// launch, then take the tree's size from the device and keep an exactly
-// sized copy of the nodes.
+// all of a build's work on `st` (capturing)
+static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* dT, cudaStream_t st,
+                                 cudaStream_t side, uint32_t* d_status) {
+  cudaError_t e = cudaSuccess;
+  J3DG_EQ(enqueue_prefix(P, dV, dT, st, d_status));
+  J3DG_EQ(enqueue_tree(P, st, side, d_status));
+  return e;
+}
+#undef J3DG_EQ
+
+// A build through the device-driven graph: allocate, enqueue the prefix
+// (the GPU sorts while the host captures and instantiates the rest), capture
+// the tree's part, launch it, then take the tree's size from the device and
+// keep an exactly sized copy of the nodes.
 static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
                            std::string& err) {
   BuildPlan P;
@@ -2339,7 +2422,10 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
   P.nt = m->nt;
   P.W = m->width;
   P.leaf = m->leaf_size;
-  P.top = J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
+  P.lbvh = (m->build_flags & J3DG_BUILD_LBVH) != 0;
+  P.need_ploc = !P.lbvh;
+  P.need_lbvh = P.lbvh;
+  P.top = !P.lbvh && J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
   cudaStream_t side = nullptr;
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ex = nullptr;
@@ -2348,9 +2434,10 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
   int rc = J3DG_OK;
   cudaError_t e = plan_alloc(P, st);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = enqueue_prefix(P, dV, dT, st, d_status);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    const cudaError_t eq = enqueue_build(P, dV, dT, st, side, d_status);
+    const cudaError_t eq = enqueue_tree(P, st, side, d_status);
     e = cudaStreamEndCapture(st, &g);
     if (eq != cudaSuccess) e = eq;
   }
@@ -2431,14 +2518,16 @@ struct RebuildLane {
   BuildPlan P;  // scratch only; nt = the lane's largest mesh
 };
 
-int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, cudaStream_t st, RebuildLane** out,
-                       std::string& err) {
+int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, bool ploc, bool lbvh, cudaStream_t st,
+                       RebuildLane** out, std::string& err) {
   RebuildLane* L = new (std::nothrow) RebuildLane();
   if (!L) return J3DG_ERR_OUT_OF_MEMORY;
   L->P.nt = nt_max;
   L->P.nv = nv_max;
   L->P.W = W;
-  L->P.top = J3DG_SAH_TOP > 0 && nt_max > J3DG_SAH_TOP;
+  L->P.need_ploc = ploc;
+  L->P.need_lbvh = lbvh;
+  L->P.top = ploc && J3DG_SAH_TOP > 0 && nt_max > J3DG_SAH_TOP;
   const cudaError_t e = plan_alloc(L->P, st, false);
   if (e != cudaSuccess) {
     plan_free(L->P, st);
@@ -2463,7 +2552,9 @@ cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st,
   Pm.nt = m->nt;
   Pm.nv = m->nv;
   Pm.leaf = m->leaf_size;
-  Pm.top = J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
+  Pm.lbvh = (m->build_flags & J3DG_BUILD_LBVH) != 0;
+  Pm.top = !Pm.lbvh && J3DG_SAH_TOP > 0 && m->nt > J3DG_SAH_TOP;
+  if (Pm.lbvh ? !Pm.need_lbvh : !Pm.need_ploc) return cudaErrorInvalidValue;  // the lane has no scratch for it
   Pm.normals = (float4*)m->d_normals;
   Pm.tris_out = (float4*)m->d_tris;
   Pm.nodes = (float4*)m->d_nodes;
@@ -2472,34 +2563,20 @@ cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st,
 }
 
 // Builds the device BVH. dV and dT are device arrays. On success fills the
-// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals). The
-// default builder goes through build_bvh_graph; this host-driven path builds
-// with the LBVH builder and handles meshes of at most one leaf.
+// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals). Both
+// builders go through build_bvh_graph; a mesh of at most one leaf is built
+// here.
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
               std::string& err) {
-  // the default builder runs device-driven; the LBVH builder and tiny meshes here
-  if (!(m->build_flags & J3DG_BUILD_LBVH) && m->nt > m->leaf_size)
-    return build_bvh_graph(m, dV, dT, st, d_status, err);
+  if (m->nt > m->leaf_size) return build_bvh_graph(m, dV, dT, st, d_status, err);
   int rc = J3DG_OK;
   const uint32_t nv = m->nv, nt = m->nt;
   float* d_part = nullptr;
   float* d_bb = nullptr;
-  uint64_t *k0 = nullptr, *k1 = nullptr;
-  uint32_t *v0 = nullptr, *v1 = nullptr, *hist = nullptr, *sums = nullptr;
-  uint2 *child = nullptr, *range = nullptr;
-  BinNode* box = nullptr;
-  uint32_t *other = nullptr, *counters = nullptr;
-  CollapseItem *qa = nullptr, *qb = nullptr;
-  float4* wide = nullptr;
-  const uint32_t n_tiles = (nt + kSortTile - 1) / kSortTile;
-  const uint32_t hist_n = 256 * n_tiles;
-  const uint32_t scan_blocks = (hist_n + 1023) / 1024;
+  uint64_t* k0 = nullptr;
+  uint32_t* v0 = nullptr;
   const int bbox_blocks = 1024;
   float hbb[6];
-  uint32_t hc[4] = {0, 0, 0, 0};
-  uint32_t n_in = 0;
-  CollapseItem root_item;
-  std::vector<uint32_t> level_end(1, 1u);  // wide nodes of level L end at level_end[L]
   const uint32_t W = m->width;
   const size_t F4 = J3DG_NODE_F4(W);
 
@@ -2517,119 +2594,29 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   }
   for (int k = 0; k < 6; ++k) m->scale = std::max(m->scale, std::fabs(hbb[k]));
 
-  // the mesh's own arrays come from the stream-ordered pool too: a context
-  // keeps the pool's memory reserved between builds, so a warm build maps no
-  // new memory (mapping GBs takes milliseconds)
+  // the triangles in input order (a single leaf), their normals; the root
+  // is the leaf and the node array one empty node
   J3DG_CK(cudaMallocAsync(&m->d_normals, sizeof(float4) * (size_t)nt, st));
   J3DG_CK(cudaMallocAsync(&m->d_tris, sizeof(float4) * 3 * (size_t)nt, st));
   J3DG_CK(cudaMallocAsync((void**)&k0, sizeof(uint64_t) * nt, st));
-  J3DG_CK(cudaMallocAsync((void**)&k1, sizeof(uint64_t) * nt, st));
   J3DG_CK(cudaMallocAsync((void**)&v0, sizeof(uint32_t) * nt, st));
-  J3DG_CK(cudaMallocAsync((void**)&v1, sizeof(uint32_t) * nt, st));
-  k_tri_prep<<<(nt + 255) / 256, 256, 0, st>>>(dV, nv, dT, nt, d_bb, (float4*)m->d_normals, k0, v0, d_status);
+  k_tri_prep<<<1, 256, 0, st>>>(dV, nv, dT, nt, d_bb, (float4*)m->d_normals, k0, v0, d_status);  // v0[i] = i
+  k_soup<<<1, 256, 0, st>>>(dV, dT, v0, nt, nv, (float4*)m->d_tris, d_status);
   J3DG_CK(cudaGetLastError());
-
-  J3DG_CK(cudaMallocAsync((void**)&hist, sizeof(uint32_t) * hist_n, st));
-  J3DG_CK(cudaMallocAsync((void**)&sums, sizeof(uint32_t) * (scan_blocks + 1), st));
-  for (int pass = 0; pass < kRadixPasses; ++pass) {
-    const int shift = 8 * pass;
-    k_radix_hist<<<n_tiles, kSortThreads, 0, st>>>(k0, nt, shift, n_tiles, hist);
-    k_scan_chunks<<<scan_blocks, 256, 0, st>>>(hist, hist, hist_n, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(sums, nullptr, scan_blocks, nullptr);
-    k_radix_scatter<<<n_tiles, kSortThreads, 0, st>>>(k0, v0, k1, v1, nt, shift, n_tiles, hist, sums, d_status);
-    J3DG_CK(cudaGetLastError());
-    std::swap(k0, k1);
-    std::swap(v0, v1);
-  }
-  k_soup<<<(nt + 255) / 256, 256, 0, st>>>(dV, dT, v0, nt, nv, (float4*)m->d_tris, d_status);
+  m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
+  m->n_nodes = 0;
+  m->max_depth = 0;
+  J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4, st));
+  J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * F4, st));
+  J3DG_CK(cudaMallocAsync(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt, st));
+  k_slot_of<<<1, 256, 0, st>>>((const float4*)m->d_tris, nt, (uint32_t*)m->d_slot_of, d_status);
   J3DG_CK(cudaGetLastError());
-  J3DG_DROP(k1);  // the sorted codes (k0) stay for the LBVH
-  J3DG_DROP(v0);
-  J3DG_DROP(v1);
-  J3DG_DROP(hist);
-  J3DG_DROP(sums);
-
-  if (nt <= m->leaf_size) {  // tiny mesh: the root is one leaf
-    m->root_ref = J3DG_LEAF_BIT | (nt - 1u);
-    m->n_nodes = 0;
-    m->max_depth = 0;
-    J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * F4, st));
-    J3DG_CK(cudaMemsetAsync(m->d_nodes, 0, sizeof(float4) * F4, st));
-    goto cleanup;
-  }
-
-  J3DG_CK(cudaMallocAsync((void**)&child, sizeof(uint2) * (nt - 1), st));
-  J3DG_CK(cudaMallocAsync((void**)&range, sizeof(uint2) * (nt - 1), st));
-  J3DG_CK(cudaMallocAsync((void**)&box, sizeof(BinNode) * (nt - 1), st));
-  J3DG_CK(cudaMallocAsync((void**)&other, sizeof(uint32_t) * (nt - 1), st));
-  J3DG_CK(cudaMallocAsync((void**)&counters, sizeof(uint32_t) * 4, st));
-  J3DG_CK(cudaMemsetAsync(other, 0xff, sizeof(uint32_t) * (nt - 1), st));
-  J3DG_CK(cudaMemsetAsync(counters, 0, sizeof(uint32_t) * 4, st));
-  k_lbvh<<<(nt + 255) / 256, 256, 0, st>>>(k0, (const float4*)m->d_tris, nt, child, box, range, other, counters);
-  J3DG_CK(cudaGetLastError());
-
-  // every wide node has >= 2 children, so there are at most nt - 1 of them
-  J3DG_CK(cudaMallocAsync((void**)&wide, sizeof(float4) * 8 * (size_t)nt, st));
-  J3DG_CK(cudaMallocAsync((void**)&qa, sizeof(CollapseItem) * (size_t)nt, st));
-  J3DG_CK(cudaMallocAsync((void**)&qb, sizeof(CollapseItem) * (size_t)nt, st));
-  J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  J3DG_CK(cudaStreamSynchronize(st));
-  root_item = CollapseItem{hc[0], 0u, 1u};
-  J3DG_CK(cudaMemcpyAsync(qa, &root_item, sizeof(root_item), cudaMemcpyHostToDevice, st));
-  hc[0] = 0u;  // unused
-  hc[1] = 1u;  // wide nodes allocated (the root)
-  hc[2] = 0u;  // queue out
-  hc[3] = 0u;  // max depth
-  J3DG_CK(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
-  n_in = 1;
-  while (n_in > 0) {
-    J3DG_CK(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
-    k_collapse<<<(n_in + 127) / 128, 128, 0, st>>>(child, box, range, (const float4*)m->d_tris, qa, n_in, qb,
-                                                   counters + 2, counters + 1, wide, m->leaf_size, counters + 3);
-    J3DG_CK(cudaGetLastError());
-    J3DG_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
-    J3DG_CK(cudaStreamSynchronize(st));
-    n_in = hc[2];
-    if (hc[1] > level_end.back()) level_end.push_back(hc[1]);
-    std::swap(qa, qb);
-  }
-  m->n_nodes = hc[1];
-  m->max_depth = hc[3];
-  m->root_ref = 0;
-  J3DG_CK(cudaMallocAsync(&m->d_nodes, sizeof(float4) * 8 * (size_t)m->n_nodes, st));
-  if (J3DG_DFS_ORDER)
-    J3DG_CK(dfs_order(4, wide, m->n_nodes, level_end, (float4*)m->d_nodes, st));
-  else
-    J3DG_CK(cudaMemcpyAsync(m->d_nodes, wide, sizeof(float4) * 8 * (size_t)m->n_nodes, cudaMemcpyDeviceToDevice, st));
 
 cleanup:
-  if (rc == J3DG_OK && m->d_tris) {  // the inverse of the leaf order, for lookups by triangle id
-    cudaError_t e = cudaMallocAsync(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt, st);
-    if (e == cudaSuccess) {
-      k_slot_of<<<(nt + 255) / 256, 256, 0, st>>>((const float4*)m->d_tris, nt, (uint32_t*)m->d_slot_of, d_status);
-      e = cudaGetLastError();
-    }
-    if (e != cudaSuccess) {
-      err = std::string("build: ") + cudaGetErrorString(e);
-      rc = J3DG_ERR_CUDA;
-    }
-  }
   if (d_part) cudaFreeAsync(d_part, st);
   if (d_bb) cudaFreeAsync(d_bb, st);
   if (k0) cudaFreeAsync(k0, st);
-  if (k1) cudaFreeAsync(k1, st);
   if (v0) cudaFreeAsync(v0, st);
-  if (v1) cudaFreeAsync(v1, st);
-  if (hist) cudaFreeAsync(hist, st);
-  if (sums) cudaFreeAsync(sums, st);
-  if (child) cudaFreeAsync(child, st);
-  if (range) cudaFreeAsync(range, st);
-  if (box) cudaFreeAsync(box, st);
-  if (other) cudaFreeAsync(other, st);
-  if (counters) cudaFreeAsync(counters, st);
-  if (wide) cudaFreeAsync(wide, st);
-  if (qa) cudaFreeAsync(qa, st);
-  if (qb) cudaFreeAsync(qb, st);
   {
     cudaError_t e = cudaStreamSynchronize(st);
     if (rc == J3DG_OK && e != cudaSuccess) {
@@ -2638,12 +2625,7 @@ cleanup:
     }
   }
   if (rc != J3DG_OK) return rc;
-  if (m->max_depth > J3DG_MAX_DEPTH_W(W)) {
-    err = "BVH depth " + std::to_string(m->max_depth) + " exceeds the traversal stack at width " + std::to_string(W);
-    return J3DG_ERR_UNSUPPORTED;
-  }
-  m->device_bytes = sizeof(float4) * F4 * (uint64_t)(m->n_nodes ? m->n_nodes : 1) +
-                    sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 4 * (uint64_t)nt;
+  m->device_bytes = sizeof(float4) * F4 + sizeof(float4) * 4 * (uint64_t)nt + sizeof(uint32_t) * 4 * (uint64_t)nt;
   return J3DG_OK;
 }
 

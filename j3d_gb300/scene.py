@@ -119,8 +119,9 @@ class Mesh:
 
     def __init__(self, ctx: Context, vertices, triangles, leaf_size: int = 2, build: str = "ploc", width: int = 4,
                  rebuildable: bool = False):
-        """build: "ploc" (surface-area clustering, the default: fewer node
-        visits per ray) or "lbvh" (Morton splits, about half the build time);
+        """build: "ploc" (binned-SAH top levels over surface-area
+        clustering, the default: fewer node visits per ray) or "lbvh" (Morton
+        splits, 4-wide only, about a third of the build time);
         width: children per BVH node, 2, 4 (default) or 8; rebuildable: keep
         what a Batch(rebuild=True) rebuilds the BVH from, inside its graph."""
         self.ctx = ctx

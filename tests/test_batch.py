@@ -161,7 +161,8 @@ def test_build_many_equals_single_builds(gpu_ctx):
         build_meshes(gpu_ctx, bad)
 
 
-def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod):
+@pytest.mark.parametrize("width,mixed", [(2, False), (4, False), (8, False), (4, True)])
+def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod, width, mixed):
     """Batch(rebuild=True): every launch first rebuilds the BVHs of its
     scenes' meshes (built rebuildable) inside the graph, on forked capture
     streams with device-driven level loops, then renders. After two launches
@@ -169,10 +170,14 @@ def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod):
     for byte (the rebuild is the same build), and one frame of every mesh
     equals the oracle's. Meshes from 2 triangles (a single leaf) to 80k, on
     both sides of the SAH / PLOC split, 12 of them so that lanes rebuild
-    several meshes in turn."""
+    several meshes in turn; half built one by one, half by build_meshes (the
+    concurrent builds); BVH widths 2, 4 and 8, and at width 4 the two
+    builders mixed (LBVH meshes among default ones, so that lanes keep
+    scratch for both)."""
     from helpers import compare_gbuffers, oracle_scene
 
-    from j3d_gb300 import Batch, Canvas, J3dgError, Matcap, Mesh, Scene, camera_for_vfov, settings, workloads as W
+    from j3d_gb300 import (Batch, Canvas, J3dgError, Matcap, Mesh, Scene, build_meshes, camera_for_vfov, settings,
+                           workloads as W)
     O = oracle_mod
     quad_V = np.array([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], np.float32)
     quad_T = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
@@ -180,7 +185,9 @@ def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod):
     srcs += [W.icosphere(k, W.SEED_BASE + 90 + k) for k in (1, 2, 3, 4, 5, 6)]
     srcs += [W.torus(nu, nv, seed=W.SEED_BASE + 100 + nu) for nu, nv in ((8, 4), (40, 20), (120, 60), (200, 100),
                                                                            (282, 141))]
-    meshes = [Mesh(gpu_ctx, V, T, rebuildable=True) for V, T in srcs]
+    meshes = [Mesh(gpu_ctx, V, T, width=width, build="lbvh" if mixed and k % 2 else "ploc", rebuildable=True)
+              for k, (V, T) in enumerate(srcs[:6])]
+    meshes += build_meshes(gpu_ctx, srcs[6:], width=width, build="lbvh" if mixed else "ploc", rebuildable=True)
     nodes0 = [m.nodes() for m in meshes]
     mc = Matcap.make(gpu_ctx, 0)
     poses = W.cameras(len(meshes), W.SEED_BASE + 110, 2.5, 3.5)
@@ -217,7 +224,7 @@ def test_batch_rebuilds_its_meshes_in_the_graph(gpu_ctx, oracle_mod):
         assert np.array_equal(cv.get_image(), oi), f"rebuild batch, mesh {i}: RGBA"
     g.close()
     # a mesh built without the flag cannot be rebuilt
-    plain = Mesh(gpu_ctx, *srcs[3])
+    plain = Mesh(gpu_ctx, *srcs[3], width=width)
     sc = Scene()
     sc.add_object(plain)
     sc.prepare_scene()

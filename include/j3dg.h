@@ -43,6 +43,7 @@ typedef enum j3dg_status {
 #define J3DG_DEV_VISIT_CAP 0x2u
 #define J3DG_DEV_BAD_INDEX 0x4u
 #define J3DG_DEV_HIT_OVERFLOW 0x8u /* more than 64 hits on one voxelization ray */
+#define J3DG_DEV_WAIT_TIMEOUT 0x10u /* a frame waited too long for its canvas's previous frame */
 
 typedef struct j3dg_ctx j3dg_ctx;
 typedef struct j3dg_mesh j3dg_mesh;
@@ -188,6 +189,21 @@ int j3dg_ctx_read_counters(j3dg_ctx* ctx, uint64_t out[2], int reset);
    enable = 0 the kernels walk the objects one after the other instead (the
    same results; for measurement). Default 1. */
 int j3dg_ctx_set_top_level(j3dg_ctx* ctx, int enable);
+/* Overlapped frames (no reference counterpart): a traced frame of a canvas
+   (j3dg_canvas_render_frame) is launched so that it may start while the
+   canvas's previous frame finishes its last pixels; each pixel carries the
+   number of the frame that last wrote it, and a frame writes a pixel only
+   once the previous frame's number is there, so results are those of
+   frames run one after the other. Frames after other writes to the canvas
+   (rectangles, rasterised or learned frames, batches, shading) do not
+   overlap. enable = 0 runs every frame after the previous one has ended
+   (for measurement). Default 1. */
+int j3dg_ctx_set_frame_overlap(j3dg_ctx* ctx, int enable);
+/* Diagnostics: the canvas's next traced frame waits for every pixel to carry
+   frame number seq. A number no frame wrote makes the waits run out (half a
+   second): the frame raises J3DG_DEV_WAIT_TIMEOUT (J3DG_ERR_DEVICE_STATUS at
+   the next synchronising call) and the context stays usable. */
+int j3dg_canvas_expect_frame(j3dg_canvas* cv, uint32_t seq);
 /* Device memory as the context sees it (no reference counterpart; the
    reference has no device memory): out[0..1] free and total bytes of the
    device (cudaMemGetInfo), out[2..3] bytes reserved and in use by the

@@ -114,6 +114,8 @@ SIGNATURES = {
     "j3dg_ctx_memory": (_I, [_P, C.POINTER(C.c_uint64)]),
     "j3dg_mesh_build_many": (_I, [_P, _U, _P, _P, _U, _P]),
     "j3dg_ctx_set_top_level": (_I, [_P, _I]),
+    "j3dg_ctx_set_frame_overlap": (_I, [_P, _I]),
+    "j3dg_canvas_expect_frame": (_I, [_P, _U]),
     "j3dg_mesh_build": (_I, [_P, _P, _U, _P, _U, C.POINTER(BuildOpts), C.POINTER(_P)]),
     "j3dg_mesh_destroy": (_I, [_P]),
     "j3dg_mesh_get_info": (_I, [_P, C.POINTER(MeshInfo)]),

@@ -60,6 +60,8 @@ struct CtxExtra {
   int batch_threads = 128;            // block shape of batched launches
   int primary_mode = J3DG_PRIMARY_AUTO;
   bool top_level = true;              // scenes of several objects walk a top level
+  bool frame_overlap = true;          // a canvas's traced frame may start while its previous one finishes
+  uint64_t frame_ops = ~0ull;         // stream_ops right after the last traced frame was launched
   // canvas buffers: stream-ordered allocations from a pool that keeps freed
   // memory reserved, so a server that evicts and re-creates canvases under
   // an HBM cap neither synchronizes the device (as cudaFree does) nor waits
@@ -97,7 +99,10 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-cudaStream_t S(j3dg_ctx* c) { return (cudaStream_t)c->stream; }
+cudaStream_t S(j3dg_ctx* c) {
+  ++c->stream_ops;
+  return (cudaStream_t)c->stream;
+}
 
 // Context layout: the opaque j3dg_ctx plus CtxExtra allocated together.
 struct CtxAll {
@@ -251,7 +256,8 @@ int check_status(j3dg_ctx* c) {
     CK(c, cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), S(c)), "status");
     CK(c, cudaStreamSynchronize(S(c)), "status");
     return fail(c, J3DG_ERR_DEVICE_STATUS, "device status word 0x" + std::to_string(st) +
-                                               " (1 stack overflow, 2 visit cap, 4 bad index)");
+                                               " (1 stack overflow, 2 visit cap, 4 bad index, 8 hit overflow, "
+                                               "16 frame wait timeout)");
   }
   return J3DG_OK;
 }
@@ -286,6 +292,12 @@ int shade_mode_of(const j3dg_canvas_settings& s) {
   if (s.wireframe) return 2;
   if (s.edges) return 1;
   return 0;
+}
+
+// the number of the canvas's next traced frame (never 0)
+uint32_t next_frame_seq(j3dg_canvas* cv) {
+  if (++cv->seq == 0u) ++cv->seq;
+  return cv->seq;
 }
 
 void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevInst* inst, const j3dg_matcap* m) {
@@ -419,11 +431,12 @@ namespace {
 void canvas_release(j3dg_canvas* cv) {
   j3dg_ctx* c = cv->ctx;
   j3dg::canvas_writable(cv);
-  void* bufs[5] = {cv->d_pixels, cv->d_image, cv->d_background, cv->d_queue, cv->d_work};
+  void* bufs[6] = {cv->d_pixels, cv->d_image, cv->d_background, cv->d_queue, cv->d_work, cv->d_stamps};
   for (void* b : bufs)
     if (b) cudaFreeAsync(b, S(c));
   cv->d_pixels = cv->d_queue = nullptr;
-  cv->d_image = cv->d_background = cv->d_work = nullptr;
+  cv->d_image = cv->d_background = cv->d_work = cv->d_stamps = nullptr;
+  cv->stamp_seq = 0;
 }
 
 int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
@@ -438,7 +451,11 @@ int canvas_alloc(j3dg_canvas* cv, uint32_t w, uint32_t h) {
     CK(c, cudaMallocFromPoolAsync((void**)&cv->d_image, sizeof(uint32_t) * n, pool, S(c)), "canvas");
     CK(c, cudaMallocFromPoolAsync((void**)&cv->d_background, sizeof(uint32_t) * n, pool, S(c)), "canvas");
     CK(c, cudaMallocFromPoolAsync(&cv->d_queue, kQueueBytesPerPixel * n + kQueueBytesFixed, pool, S(c)), "canvas");
-    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_work, 4 * sizeof(uint32_t), pool, S(c)), "canvas");
+    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_work, j3dg::kCanvasWorkWords * sizeof(uint32_t), pool, S(c)),
+       "canvas");
+    CK(c, cudaMallocFromPoolAsync((void**)&cv->d_stamps, sizeof(uint32_t) * n, pool, S(c)), "canvas");
+    CK(c, cudaMemsetAsync(cv->d_work, 0, j3dg::kCanvasWorkWords * sizeof(uint32_t), S(c)), "canvas");
+    CK(c, cudaMemsetAsync(cv->d_stamps, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_image, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, cudaMemsetAsync(cv->d_background, 0, sizeof(uint32_t) * n, S(c)), "canvas");
     CK(c, j3dg::launch_init_pixels((j3dg_pixel*)cv->d_pixels, n, S(c)), "canvas");
@@ -458,6 +475,7 @@ int ctx_fail(j3dg_ctx* c, int code, const std::string& msg) { return fail(c, cod
 // Before work that writes the canvas: the context stream waits (on the
 // device) for a download of the canvas still running on the copy stream.
 void canvas_writable(j3dg_canvas* cv) {
+  cv->stamp_seq = 0;  // a write without stamps: the next traced frame does not overlap
   if (!cv->copy_pending) return;
   cudaStreamWaitEvent(S(cv->ctx), (cudaEvent_t)cv->ev_copied, 0);
   cv->copy_pending = false;
@@ -1253,6 +1271,7 @@ int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, c
   FrameParams P;
   fill_frame(P, cv, s, dinst, nullptr);
   P.top = top ? 1u : 0u;
+  P.seq = next_frame_seq(cv);  // its counters; a rectangle writes no stamps and does not overlap
   P.x0 = x0;
   P.y0 = y0;
   P.x1 = x1;
@@ -1315,6 +1334,11 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   if (int rc = scene_ok(c, s)) return rc;
   if (cv->w == 0 || cv->h == 0) return J3DG_OK;
   cudaSetDevice(c->device);
+  const uint32_t prev_frame = cv->stamp_seq;  // every pixel carries it (0: unknown)
+  CtxExtra& X = all(c)->ex;
+  // the stream's last work is a traced frame (or a diagnostic asks for the wait)
+  const bool after_frame = c->stream_ops == X.frame_ops || cv->expect_stamps;
+  cv->expect_stamps = false;
   j3dg::canvas_writable(cv);
   const DevInst* dinst = nullptr;
   bool top = false;
@@ -1331,6 +1355,14 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   fill_frame(P, cv, s, dinst, m);
   P.top = top ? 1u : 0u;
   setup_raster(P, cv, s);
+  P.seq = next_frame_seq(cv);
+  // a traced frame in one kernel (plain shading) stamps its pixels and may
+  // overlap the frame before it on the stream
+  const bool single = !P.raster && mode == 0;
+  if (single) {
+    P.stamps = cv->d_stamps;
+    P.wait_seq = X.frame_overlap && after_frame ? prev_frame : 0u;
+  }
   if (mode == 0) {
     P.shade_mode = 1;  // one kernel: G-buffer, shadow, plain shading, background
     CK(c, j3dg::launch_render(P, S(c)), "render_frame");
@@ -1339,6 +1371,21 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
     CK(c, j3dg::launch_render(P, S(c)), "render_frame");
     CK(c, j3dg::launch_shade(P, (const j3dg_pixel*)cv->d_pixels, mode, 1, S(c)), "render_frame");
   }
+  cv->stamp_seq = single ? P.seq : 0u;
+  X.frame_ops = single ? c->stream_ops : ~0ull;
+  return J3DG_OK;
+}
+
+int j3dg_ctx_set_frame_overlap(j3dg_ctx* c, int enable) {
+  if (!c) return J3DG_ERR_INVALID_ARGUMENT;
+  all(c)->ex.frame_overlap = enable != 0;
+  return J3DG_OK;
+}
+
+int j3dg_canvas_expect_frame(j3dg_canvas* cv, uint32_t seq) {
+  if (!cv) return J3DG_ERR_INVALID_ARGUMENT;
+  cv->stamp_seq = seq;
+  cv->expect_stamps = true;
   return J3DG_OK;
 }
 
@@ -1806,7 +1853,9 @@ int j3dg_canvas_download_async(j3dg_canvas* cv, j3dg_pixel* pixels, uint32_t* im
     CK(c, cudaEventCreateWithFlags((cudaEvent_t*)&cv->ev_copied, cudaEventDisableTiming), "download_async");
   }
   const size_t n = (size_t)cv->w * cv->h;
-  CK(c, cudaEventRecord((cudaEvent_t)cv->ev_ready, S(c)), "download_async");
+  // an event record writes nothing: the stream's last work stays what it
+  // was, so the next traced frame may still overlap the previous one
+  CK(c, cudaEventRecord((cudaEvent_t)cv->ev_ready, (cudaStream_t)c->stream), "download_async");
   CK(c, cudaStreamWaitEvent(cs, (cudaEvent_t)cv->ev_ready, 0), "download_async");
   if (pixels && n)
     CK(c, cudaMemcpyAsync(pixels, cv->d_pixels, sizeof(j3dg_pixel) * n,
@@ -1826,6 +1875,7 @@ int j3dg_canvas_download_wait(j3dg_canvas* cv) {
   if (!cv->ev_copied) return J3DG_OK;
   cudaSetDevice(cv->ctx->device);
   CK(cv->ctx, cudaEventSynchronize((cudaEvent_t)cv->ev_copied), "download_wait");
+  cv->copy_pending = false;  // the copy has ended: the next write need not wait for it on the device
   return J3DG_OK;
 }
 

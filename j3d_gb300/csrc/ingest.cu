@@ -258,7 +258,10 @@ __global__ void k_colors_to_float(const uint32_t* c, uint64_t n, float* out) {
 
 // ------------------------------------------------------------------ host
 
-cudaStream_t S(j3dg_ctx* c) { return (cudaStream_t)c->stream; }
+cudaStream_t S(j3dg_ctx* c) {
+  ++c->stream_ops;
+  return (cudaStream_t)c->stream;
+}
 
 int fail(j3dg_ctx* c, int code, const std::string& msg) { return j3dg::ctx_fail(c, code, msg); }
 

@@ -35,6 +35,9 @@ struct j3dg_ctx {
   uint32_t inst_cap = 0;
   void* h_inst = nullptr;        // pinned staging for the instance table
   int sm_count = 0;
+  // library calls that took the context stream: a frame overlaps the kernel
+  // before it only when that kernel is the previous frame (nothing between)
+  uint64_t stream_ops = 0;
   std::string last_error;
   std::atomic<uint32_t> live{0};  // meshes, canvases, ... made from this context and not destroyed
 };
@@ -98,7 +101,11 @@ struct j3dg_canvas {
   uint32_t* d_image = nullptr;   // w*h
   uint32_t* d_background = nullptr;
   void* d_queue = nullptr;       // 48 B per pixel: raster keys, jobs and tables during a frame, splat keys after
-  uint32_t* d_work = nullptr;    // per-frame work counters
+  uint32_t* d_work = nullptr;    // per-frame work counters (kCanvasWorkWords)
+  uint32_t* d_stamps = nullptr;  // w*h: number of the traced frame that last wrote each pixel
+  uint32_t seq = 0;              // traced frames launched on this canvas
+  uint32_t stamp_seq = 0;        // every pixel carries this frame number (0: not known, no overlap)
+  bool expect_stamps = false;    // the next traced frame waits for stamp_seq (j3dg_canvas_expect_frame)
   int last_primary = 1;          // J3DG_PRIMARY_TRACE or J3DG_PRIMARY_RASTER
   // asynchronous download: ev_ready marks the work queued before it, ev_copied its end
   void* ev_ready = nullptr;

@@ -843,7 +843,10 @@ struct j3dg_learned {
 
 namespace {
 
-cudaStream_t LS(j3dg_learned* l) { return (cudaStream_t)l->ctx->stream; }
+cudaStream_t LS(j3dg_learned* l) {
+  ++l->ctx->stream_ops;
+  return (cudaStream_t)l->ctx->stream;
+}
 
 #define LCK(x, where)                                                                              \
   do {                                                                                             \

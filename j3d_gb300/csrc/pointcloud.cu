@@ -35,7 +35,10 @@ using j3dg::fa;
 using j3dg::fm;
 using j3dg::mat_vec;
 
-cudaStream_t S(j3dg_ctx* c) { return (cudaStream_t)c->stream; }
+cudaStream_t S(j3dg_ctx* c) {
+  ++c->stream_ops;
+  return (cudaStream_t)c->stream;
+}
 
 int fail(j3dg_ctx* c, int code, const std::string& msg) { return j3dg::ctx_fail(c, code, msg); }
 

@@ -130,6 +130,59 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
   if (P.shade_mode == 1) P.im[pix] = P.background ? __ldg(P.background + pix) : P.im[pix];
 }
 
+// ------------------------------------------- overlapped frames ----
+//
+// The kernel of a canvas's frame is launched as a programmatic dependent of
+// the previous kernel on the stream, so it starts while that kernel's last
+// rays finish (a frame's tail otherwise leaves most of the GPU idle). Each
+// warp, once the frame's items are all taken, waits until the previous
+// kernel has completed (griddepcontrol.wait) and then lets the next frame
+// start (griddepcontrol.launch_dependents): at most two frames are in
+// flight. A pixel's writes keep frame order through the canvas's stamps: the
+// previous frame stores its number with release order after its last write
+// of the pixel, and this frame, before its first write, waits (acquire) until
+// the pixel carries that number. The wait is bounded (half a second by the
+// global timer, and an iteration cap): when it runs out it raises
+// J3DG_DEV_WAIT_TIMEOUT and the frame stops waiting.
+static const uint64_t kAwaitNs = 500000000ull;
+static const uint32_t kAwaitSpins = 1u << 26;
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void await_pixel(const FrameParams& P, size_t pix) {
+  if (P.wait_seq == 0u) return;
+  const uint32_t* a = P.stamps + pix;
+  if (ld_acquire(a) == P.wait_seq) return;
+  const uint64_t t0 = global_ns();
+  for (uint32_t k = 0; k < kAwaitSpins; ++k) {
+    if (*reinterpret_cast<volatile const uint32_t*>(P.status) & J3DG_DEV_WAIT_TIMEOUT) return;  // one ran out
+    __nanosleep(256);
+    if (ld_acquire(a) == P.wait_seq) return;
+    if (global_ns() - t0 > kAwaitNs) break;
+  }
+  atomicOr(P.status, J3DG_DEV_WAIT_TIMEOUT);
+}
+
+__device__ __forceinline__ void stamp_pixel(const FrameParams& P, size_t pix) {
+  if (P.stamps) asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(P.stamps + pix), "r"(P.seq) : "memory");
+}
+
+// the previous kernel on the stream has completed; the next may start
+__device__ __forceinline__ void frame_handover() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // A frame in one persistent kernel: each lane runs primary ray -> (shadow ray)
 // -> next pixel, refilled from the tile-ordered pixel list by warp-aggregated
 // atomics (Aila and Laine 2009 dynamic fetch), so shadow rays overlap other
@@ -175,6 +228,15 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 #endif
 static const int kTraceThreads = J3DG_TRACE_THREADS;
 static const int kIters = J3DG_TRACE_ITERS;
+// k_frame runs one warp per block, with the warps per SM of the builds
+// above: when a frame's last rays keep a few warps busy, every warp that is
+// done frees its slot for the canvas's next frame (overlapped frames, below)
+#ifndef J3DG_FRAME_THREADS
+#define J3DG_FRAME_THREADS 32
+#endif
+static const int kFrameThreads = J3DG_FRAME_THREADS;
+static const int kFrameBlocksT = J3DG_TRACE_MINBLOCKS * 128 / kFrameThreads;
+static const int kFrameBlocksL = J3DG_LATENCY_MINBLOCKS * 128 / kFrameThreads;
 
 // Pixel and colour state of a lane: read only at a pixel's start and
 // finish. The throughput build keeps it in a per-block shared array
@@ -230,9 +292,11 @@ __device__ __forceinline__ float4 light_position(const FrameParams& P) {
 template <class Tracer>
 __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, size_t pix, uint32_t& w0, float& su,
                                                float& sv) {
+  await_pixel(P, pix);
   const auto b = T.b;
   if (!b.found) {
     write_miss(P, pix);
+    stamp_pixel(P, pix);
     return false;
   }
   j3dg_pixel* rec = P.gbuf + pix;
@@ -289,6 +353,7 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   sv = n.y;
   if (!P.shadow) {
     if (P.shade_mode == 1) P.im[pix] = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
+    stamp_pixel(P, pix);
     return false;
   }
   // canvas.cpp:836-853: from the hit point towards the light
@@ -316,6 +381,7 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
   }
   if (P.shade_mode == 1)
     P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
+  stamp_pixel(P, pix);
 }
 
 // ------------------------------------------------------- rasterisation ----
@@ -769,17 +835,18 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_shadow(
 }
 
 template <bool kThroughput, bool TOP>
-__global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLOCKS : J3DG_LATENCY_MINBLOCKS)
+__global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : kFrameBlocksL)
     k_frame(const FrameParams P) {
   if (P.raster && P.rlist[1] == 0u) return;  // the raster kernels made this frame
-  TracerT<kTraceThreads, TOP, kWidth> T;
+  TracerT<kFrameThreads, TOP, kWidth> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
+  uint32_t* const taken = P.work + 4 + (P.seq & 1u);
   int phase = 0;  // 0 idle, 1 primary, 2 shadow, 3 / 4 primary / shadow finished (parked)
-  bool exhausted = false;
+  bool exhausted = false, handed_over = false;
   PixState local;
-  PixState& ps = pix_state<kThroughput && (J3DG_COLD_SMEM & 4) != 0, kTraceThreads>(local);
+  PixState& ps = pix_state<kThroughput && (J3DG_COLD_SMEM & 4) != 0, kFrameThreads>(local);
   ps = PixState{0, 0u, 0u, 0.f, 0.f};
   size_t& pix = ps.pix;
   uint32_t& w0 = ps.w0;
@@ -799,7 +866,7 @@ __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLO
     if (m) {
       const int leader = __ffs(m) - 1;
       uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(P.work, (uint32_t)__popc(m));
+      if ((int)lane == leader) base = atomicAdd(taken, (uint32_t)__popc(m));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (need) {
         const uint32_t my = base + __popc(m & ((1u << lane) - 1u));
@@ -809,13 +876,19 @@ __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLO
         } else if (item_pixel(P, my, x, y)) {
           pix = (size_t)y * P.w + x;
           if (P.n_inst == 0) {
+            await_pixel(P, pix);
             write_miss(P, pix);
+            stamp_pixel(P, pix);
           } else {
             primary_begin(P, T, x, y);
             phase = 1;
           }
         }
       }
+    }
+    if (!handed_over && __any_sync(0xffffffffu, exhausted)) {  // the frame's items are all taken
+      handed_over = true;
+      frame_handover();
     }
     if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
     // all lanes step together; leave to refill once enough lanes are idle
@@ -840,6 +913,15 @@ __global__ void __launch_bounds__(kTraceThreads, kThroughput ? J3DG_TRACE_MINBLO
   if (P.counters) {
     atomicAdd(P.counters + 0, (unsigned long long)visits);
     atomicAdd(P.counters + 1, (unsigned long long)tests);
+  }
+  // the frame's last warp zeroes its counters for the frame two later
+  if (lane == 0) {
+    uint32_t* const done = P.work + 6 + (P.seq & 1u);
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    if (atomicAdd(done, 1u) == warps - 1u) {
+      atomicExch(taken, 0u);
+      atomicExch(done, 0u);
+    }
   }
 }
 
@@ -1171,17 +1253,39 @@ __global__ void k_init_pixels(j3dg_pixel* __restrict__ G, size_t n) {
 
 // ------------------------------------------------------------ launchers ----
 
+// k_frame, as a programmatic dependent of the previous kernel on the stream
+// when the frame overlaps its canvas's previous frame
+template <bool kT, bool TOP>
+static cudaError_t launch_frame(int blocks, const FrameParams& P, bool overlap, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3((unsigned)kFrameThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = overlap ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_frame<kT, TOP>, P);
+}
+
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const int rw = P.x1 - P.x0 + 1, rh = P.y1 - P.y0 + 1;
   if (rw <= 0 || rh <= 0) return cudaSuccess;
   static int blocks_t = 0, blocks_l = 0, blocks_tt = 0, blocks_lt = 0;
   if (!blocks_t) {
-    blocks_t = persistent_blocks(k_frame<true, false>);
-    blocks_l = persistent_blocks(k_frame<false, false>);
-    blocks_tt = persistent_blocks(k_frame<true, true>);
-    blocks_lt = persistent_blocks(k_frame<false, true>);
+    blocks_t = persistent_blocks(k_frame<true, false>, kFrameThreads);
+    blocks_l = persistent_blocks(k_frame<false, false>, kFrameThreads);
+    blocks_tt = persistent_blocks(k_frame<true, true>, kFrameThreads);
+    blocks_lt = persistent_blocks(k_frame<false, true>, kFrameThreads);
   }
-  cudaError_t e = cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
+  // an overlapped frame finds its counters zeroed by the frame two before
+  // (which completed before the previous frame let this one start); any
+  // other frame zeroes them here
+  const bool overlap = P.wait_seq != 0u && !P.raster;
+  cudaError_t e = cudaSuccess;
+  if (!overlap) e = cudaMemsetAsync(P.work + 4, 0, 4 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (P.raster) {
     static int blocks_s = 0, blocks_t = 0, blocks_r = 0;
@@ -1211,16 +1315,16 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
   const bool thr = primary_items(P) >= J3DG_THROUGHPUT_ITEMS;
   if (P.top) {
     if (thr)
-      k_frame<true, true><<<blocks_tt, kTraceThreads, 0, st>>>(P);
+      e = launch_frame<true, true>(blocks_tt, P, overlap, st);
     else
-      k_frame<false, true><<<blocks_lt, kTraceThreads, 0, st>>>(P);
+      e = launch_frame<false, true>(blocks_lt, P, overlap, st);
   } else {
     if (thr)
-      k_frame<true, false><<<blocks_t, kTraceThreads, 0, st>>>(P);
+      e = launch_frame<true, false>(blocks_t, P, overlap, st);
     else
-      k_frame<false, false><<<blocks_l, kTraceThreads, 0, st>>>(P);
+      e = launch_frame<false, false>(blocks_l, P, overlap, st);
   }
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <bool kT, bool TOP>

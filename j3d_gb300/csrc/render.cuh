@@ -47,7 +47,10 @@ struct FrameParams {
   uint32_t mw, mh, cavity;
   uint32_t shadow, textured, vertexcolors, shading;
   int shade_mode;  // 0: G-buffer only; 1: also plain shading into im (misses <- background)
-  uint32_t* work;   // [0] primary items taken; rasterised frames: [1] shadow jobs queued, [2] taken
+  // [0..3] rasterised frames: [0] primary items taken, [1] shadow jobs queued,
+  // [2] taken; k_frame: [4 + (seq & 1)] items taken, [6 + (seq & 1)] warps
+  // done (the frame's last warp zeroes both)
+  uint32_t* work;
   uint32_t* status;
   unsigned long long* counters;  // optional [node visits, triangle tests]
   // raster != 0: launch_render first fills keys[w*h] with the minimum of
@@ -62,7 +65,16 @@ struct FrameParams {
   unsigned long long* keys;
   RasterInst* rinst;      // n_inst entries
   uint32_t* rlist;        // counters, then the large-triangle entries (kRasterListHeader)
+  // Frames of one canvas may overlap (k_frame launched as a programmatic
+  // dependent of the canvas's previous frame): seq is the frame's number
+  // (>= 1), stamps (w*h, or null: not written) the number of the frame that
+  // last wrote each pixel, stored after the pixel's last write, and a frame
+  // with wait_seq != 0 waits before its first write of a pixel until the
+  // pixel carries wait_seq, so that every pixel's writes stay in frame order.
+  uint32_t* stamps;
+  uint32_t seq, wait_seq;
 };
+static const uint32_t kCanvasWorkWords = 8;  // FrameParams::work
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
 // all frames in one persistent launch; offsets = prefix sums of primary_items

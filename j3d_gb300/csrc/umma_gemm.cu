@@ -234,6 +234,7 @@ extern "C" int j3dg_gemm_bf16(j3dg_ctx* c, const void* A, const void* Bt, float*
                               int impl) {
   if (!c || !A || !Bt || !C) return J3DG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
+  ++c->stream_ops;
   cudaStream_t st = (cudaStream_t)c->stream;
   cudaError_t e;
   if (impl >= 0 && impl <= 2) {

@@ -95,6 +95,12 @@ class Context:
         (default) or object after object (for measurement)."""
         _check(self.h, lib().j3dg_ctx_set_top_level(self.h, 1 if on else 0))
 
+    def set_frame_overlap(self, on: bool) -> None:
+        """Let a canvas's traced frame start while its previous frame
+        finishes (default; the same results) or run frames strictly one
+        after the other (for measurement)."""
+        _check(self.h, lib().j3dg_ctx_set_frame_overlap(self.h, 1 if on else 0))
+
     def memory(self) -> dict:
         """Device free / total bytes and the reserved / used bytes of the
         context's canvas pool and of the device's default pool."""
@@ -472,6 +478,11 @@ class Canvas:
         if self.h:
             lib().j3dg_canvas_destroy(self.h)
             self.h = None
+
+    def expect_frame(self, seq: int) -> None:
+        """Diagnostics: the next traced frame waits for every pixel to carry
+        frame number seq (a number no frame wrote makes its waits run out)."""
+        _check(self.ctx.h, lib().j3dg_canvas_expect_frame(self.h, seq))
 
     def __del__(self):
         try:

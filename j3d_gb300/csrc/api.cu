@@ -1357,11 +1357,11 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   setup_raster(P, cv, s);
   P.seq = next_frame_seq(cv);
   // a traced frame in one kernel (plain shading) stamps its pixels and may
-  // overlap the frame before it on the stream
-  const bool single = !P.raster && mode == 0;
+  // overlap the frame before it on the stream (with overlap on)
+  const bool single = !P.raster && mode == 0 && X.frame_overlap;
   if (single) {
     P.stamps = cv->d_stamps;
-    P.wait_seq = X.frame_overlap && after_frame ? prev_frame : 0u;
+    P.wait_seq = after_frame ? prev_frame : 0u;
   }
   if (mode == 0) {
     P.shade_mode = 1;  // one kernel: G-buffer, shadow, plain shading, background

@@ -228,11 +228,12 @@ __device__ __forceinline__ void frame_handover() {
 #endif
 static const int kTraceThreads = J3DG_TRACE_THREADS;
 static const int kIters = J3DG_TRACE_ITERS;
-// k_frame runs one warp per block, with the warps per SM of the builds
-// above: when a frame's last rays keep a few warps busy, every warp that is
-// done frees its slot for the canvas's next frame (overlapped frames, below)
+// k_frame runs two warps per block, with the warps per SM of the builds
+// above: when a frame's last rays keep a few warps busy, every block that is
+// done frees its slot for the canvas's next frame (overlapped frames, below;
+// 32 / 64 / 128 threads measured 0.610 / 0.591 / 0.594 ms per headline frame)
 #ifndef J3DG_FRAME_THREADS
-#define J3DG_FRAME_THREADS 32
+#define J3DG_FRAME_THREADS 64
 #endif
 static const int kFrameThreads = J3DG_FRAME_THREADS;
 static const int kFrameBlocksT = J3DG_TRACE_MINBLOCKS * 128 / kFrameThreads;
@@ -296,7 +297,6 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   const auto b = T.b;
   if (!b.found) {
     write_miss(P, pix);
-    stamp_pixel(P, pix);
     return false;
   }
   j3dg_pixel* rec = P.gbuf + pix;
@@ -353,7 +353,6 @@ __device__ __forceinline__ bool primary_finish(const FrameParams& P, Tracer& T, 
   sv = n.y;
   if (!P.shadow) {
     if (P.shade_mode == 1) P.im[pix] = pixel_color(P, mark, pr, pg, pb, n.x, n.y);
-    stamp_pixel(P, pix);
     return false;
   }
   // canvas.cpp:836-853: from the hit point towards the light
@@ -381,7 +380,6 @@ __device__ __forceinline__ void shadow_finish(const FrameParams& P, const Tracer
   }
   if (P.shade_mode == 1)
     P.im[pix] = pixel_color(P, mark, (w0 >> 8) & 0xffu, (w0 >> 16) & 0xffu, (w0 >> 24) & 0xffu, su, sv);
-  stamp_pixel(P, pix);
 }
 
 // ------------------------------------------------------- rasterisation ----
@@ -852,14 +850,23 @@ __global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : k
   uint32_t& w0 = ps.w0;
   float &su = ps.su, &sv = ps.sv;
   uint32_t visits = 0, tests = 0;
-#pragma unroll 1
-  for (;;) {
-    if (phase == 3) {
+  // a finished ray's finish code (parked: phase 3 / 4, or in-line: 1 / 2);
+  // the pixel's stamp follows its last write, one store site for all paths
+  auto finish = [&](int ph) {
+    bool last;
+    if (ph == 1 || ph == 3) {
       phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
-    } else if (phase == 4) {
+      last = phase == 0;
+    } else {
       shadow_finish(P, T, pix, w0, su, sv);
       phase = 0;
+      last = true;
     }
+    if (last) stamp_pixel(P, pix);
+  };
+#pragma unroll 1
+  for (;;) {
+    if (phase >= 3) finish(phase);
     // refill: every idle lane takes the next pixel; one atomic per warp
     const bool need = phase == 0 && !exhausted;
     const uint32_t m = __ballot_sync(0xffffffffu, need);
@@ -898,12 +905,7 @@ __global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : k
 #if J3DG_DEFER_FINISH
         phase += 2;
 #else
-        if (phase == 1) {
-          phase = primary_finish(P, T, pix, w0, su, sv) ? 2 : 0;
-        } else {
-          shadow_finish(P, T, pix, w0, su, sv);
-          phase = 0;
-        }
+        finish(phase);
 #endif
       }
       if (__all_sync(0xffffffffu, phase != 1 && phase != 2)) break;

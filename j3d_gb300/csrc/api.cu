@@ -62,6 +62,8 @@ struct CtxExtra {
   bool top_level = true;              // scenes of several objects walk a top level
   bool frame_overlap = true;          // a canvas's traced frame may start while its previous one finishes
   uint64_t frame_ops = ~0ull;         // stream_ops right after the last traced frame was launched
+  uint32_t* d_frame_ring = nullptr;   // FrameParams::ring (kFrameDepth words)
+  uint32_t frame_launches = 0;        // frame kernels launched (FrameParams::launch)
   // canvas buffers: stream-ordered allocations from a pool that keeps freed
   // memory reserved, so a server that evicts and re-creates canvases under
   // an HBM cap neither synchronizes the device (as cudaFree does) nor waits
@@ -294,10 +296,15 @@ int shade_mode_of(const j3dg_canvas_settings& s) {
   return 0;
 }
 
-// the number of the canvas's next traced frame (never 0)
-uint32_t next_frame_seq(j3dg_canvas* cv) {
+// the numbers of the canvas's next traced frame (never 0) and of the
+// context's next frame kernel (never 0)
+void next_frame_seq(FrameParams& P, j3dg_canvas* cv) {
   if (++cv->seq == 0u) ++cv->seq;
-  return cv->seq;
+  P.seq = cv->seq;
+  CtxExtra& X = all(cv->ctx)->ex;
+  if (++X.frame_launches == 0u) ++X.frame_launches;
+  P.launch = X.frame_launches;
+  P.ring = X.d_frame_ring;
 }
 
 void fill_frame(FrameParams& P, j3dg_canvas* cv, const j3dg_scene* s, const DevInst* inst, const j3dg_matcap* m) {
@@ -581,6 +588,8 @@ int j3dg_ctx_create(int device, j3dg_ctx** out) {
             cudaMemset(c->d_status, 0, sizeof(uint32_t)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMalloc((void**)&A->ex.d_ray_counter, sizeof(uint32_t)) == cudaSuccess &&
+            cudaMalloc((void**)&A->ex.d_frame_ring, j3dg::kFrameDepth * sizeof(uint32_t)) == cudaSuccess &&
+            cudaMemset(A->ex.d_frame_ring, 0, j3dg::kFrameDepth * sizeof(uint32_t)) == cudaSuccess &&
             cudaMemset(A->ex.d_counters, 0, 2 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaEventCreate(&A->ex.ev0) == cudaSuccess && cudaEventCreate(&A->ex.ev1) == cudaSuccess;
   for (uint32_t i = 0; ok && i < kInstSlots; ++i) ok = cudaEventCreateWithFlags(&A->ex.slot_ev[i], cudaEventDisableTiming) == cudaSuccess;
@@ -615,6 +624,7 @@ int j3dg_ctx_destroy(j3dg_ctx* c) {
   cudaFree(c->d_inst);
   cudaFree(A->ex.d_counters);
   cudaFree(A->ex.d_ray_counter);
+  cudaFree(A->ex.d_frame_ring);
   if (A->h_slots) cudaFreeHost(A->h_slots);
   for (uint32_t i = 0; i < kInstSlots; ++i)
     if (A->ex.slot_ev[i]) cudaEventDestroy(A->ex.slot_ev[i]);
@@ -1271,7 +1281,7 @@ int j3dg_canvas_update_canvas(j3dg_canvas* cv, int x0, int y0, int x1, int y1, c
   FrameParams P;
   fill_frame(P, cv, s, dinst, nullptr);
   P.top = top ? 1u : 0u;
-  P.seq = next_frame_seq(cv);  // its counters; a rectangle writes no stamps and does not overlap
+  next_frame_seq(P, cv);  // its counters; a rectangle writes no stamps and does not overlap
   P.x0 = x0;
   P.y0 = y0;
   P.x1 = x1;
@@ -1355,7 +1365,7 @@ int j3dg_canvas_render_frame(j3dg_canvas* cv, const j3dg_scene* s, const j3dg_ma
   fill_frame(P, cv, s, dinst, m);
   P.top = top ? 1u : 0u;
   setup_raster(P, cv, s);
-  P.seq = next_frame_seq(cv);
+  next_frame_seq(P, cv);
   // a traced frame in one kernel (plain shading) stamps its pixels and may
   // overlap the frame before it on the stream (with overlap on)
   const bool single = !P.raster && mode == 0 && X.frame_overlap;

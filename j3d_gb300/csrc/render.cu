@@ -134,16 +134,26 @@ __device__ __forceinline__ void write_miss(const FrameParams& P, size_t pix) {
 //
 // The kernel of a canvas's frame is launched as a programmatic dependent of
 // the previous kernel on the stream, so it starts while that kernel's last
-// rays finish (a frame's tail otherwise leaves most of the GPU idle). Each
-// warp, once the frame's items are all taken, waits until the previous
-// kernel has completed (griddepcontrol.wait) and then lets the next frame
-// start (griddepcontrol.launch_dependents): at most two frames are in
-// flight. A pixel's writes keep frame order through the canvas's stamps: the
-// previous frame stores its number with release order after its last write
-// of the pixel, and this frame, before its first write, waits (acquire) until
-// the pixel carries that number. The wait is bounded (half a second by the
-// global timer, and an iteration cap): when it runs out it raises
-// J3DG_DEV_WAIT_TIMEOUT and the frame stops waiting.
+// rays finish (a frame's tail otherwise leaves most of the GPU idle).
+//
+// Hand-over: each warp, once the frame's items are all taken, lets the next
+// frame start (griddepcontrol.launch_dependents) if the frame kFrameDepth - 1
+// launches before this one has released its ring entry; nothing waits
+// there, so at most kFrameDepth frames are in flight. A frame's last warp to
+// finish zeroes the frame's counter slot, waits until the kernel before it
+// has completed (griddepcontrol.wait) and then releases the frame's ring
+// entry: a frame completes only after every frame before it, and a released
+// entry means every frame up to it has completed. A warp that never handed
+// over waits likewise before it exits (its block's exit then counts as the
+// hand-over). A canvas's frames use counter slots seq % kFrameDepth, so a
+// slot's previous user has completed before the slot is used again.
+//
+// Pixel order: the previous frame stores its number into the pixel's stamp
+// with release order after its last write of the pixel, and this frame,
+// before its first write, waits (acquire) until the pixel carries that
+// number. The wait is bounded (half a second by the global timer, and an
+// iteration cap): when it runs out it raises J3DG_DEV_WAIT_TIMEOUT and the
+// frame stops waiting.
 static const uint64_t kAwaitNs = 500000000ull;
 static const uint32_t kAwaitSpins = 1u << 26;
 
@@ -177,10 +187,32 @@ __device__ __forceinline__ void stamp_pixel(const FrameParams& P, size_t pix) {
   if (P.stamps) asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(P.stamps + pix), "r"(P.seq) : "memory");
 }
 
-// the previous kernel on the stream has completed; the next may start
-__device__ __forceinline__ void frame_handover() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+// warp-uniform: the next frame may start (the frame kFrameDepth - 1
+// launches before this one has released its ring entry)
+__device__ __forceinline__ bool handover_allowed(const FrameParams& P) {
+  uint32_t rel = 0;
+  if ((threadIdx.x & 31u) == 0) rel = ld_acquire(P.ring + ((P.launch + 1u) % kFrameDepth));
+  rel = __shfl_sync(0xffffffffu, rel, 0);
+  return rel + (kFrameDepth - 1u) >= P.launch;
+}
+
+// the frame's end for one warp (all lanes): the last warp zeroes the
+// frame's counter slot, waits for the kernel before it and releases the
+// frame's ring entry
+__device__ __forceinline__ void frame_exit(const FrameParams& P, bool handed_over) {
+  if (!handed_over) asm volatile("griddepcontrol.wait;" ::: "memory");
+  if ((threadIdx.x & 31u) == 0) {
+    const uint32_t slot = P.seq % kFrameDepth;
+    uint32_t* const done = P.work + 4 + kFrameDepth + slot;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    if (atomicAdd(done, 1u) == warps - 1u) {
+      atomicExch(P.work + 4 + slot, 0u);
+      atomicExch(done, 0u);
+      asm volatile("griddepcontrol.wait;" ::: "memory");
+      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(P.ring + P.launch % kFrameDepth), "r"(P.launch)
+                   : "memory");
+    }
+  }
 }
 
 // A frame in one persistent kernel: each lane runs primary ray -> (shadow ray)
@@ -835,14 +867,14 @@ __global__ void __launch_bounds__(kTraceThreads, J3DG_TRACE_MINBLOCKS) k_shadow(
 template <bool kThroughput, bool TOP>
 __global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : kFrameBlocksL)
     k_frame(const FrameParams P) {
-  if (P.raster && P.rlist[1] == 0u) return;  // the raster kernels made this frame
   TracerT<kFrameThreads, TOP, kWidth> T;
   uint2 stack[J3DG_STACK];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t n = primary_count(P);
-  uint32_t* const taken = P.work + 4 + (P.seq & 1u);
+  uint32_t* const taken = P.work + 4 + P.seq % kFrameDepth;
   int phase = 0;  // 0 idle, 1 primary, 2 shadow, 3 / 4 primary / shadow finished (parked)
-  bool exhausted = false, handed_over = false;
+  // the raster kernels made this frame: nothing to take (the exit still runs)
+  bool exhausted = P.raster && P.rlist[1] == 0u, handed_over = false;
   PixState local;
   PixState& ps = pix_state<kThroughput && (J3DG_COLD_SMEM & 4) != 0, kFrameThreads>(local);
   ps = PixState{0, 0u, 0u, 0.f, 0.f};
@@ -893,9 +925,9 @@ __global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : k
         }
       }
     }
-    if (!handed_over && __any_sync(0xffffffffu, exhausted)) {  // the frame's items are all taken
+    if (!handed_over && __any_sync(0xffffffffu, exhausted) && handover_allowed(P)) {  // items all taken
       handed_over = true;
-      frame_handover();
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     }
     if (__all_sync(0xffffffffu, phase == 0 && exhausted)) break;
     // all lanes step together; leave to refill once enough lanes are idle
@@ -916,15 +948,7 @@ __global__ void __launch_bounds__(kFrameThreads, kThroughput ? kFrameBlocksT : k
     atomicAdd(P.counters + 0, (unsigned long long)visits);
     atomicAdd(P.counters + 1, (unsigned long long)tests);
   }
-  // the frame's last warp zeroes its counters for the frame two later
-  if (lane == 0) {
-    uint32_t* const done = P.work + 6 + (P.seq & 1u);
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    if (atomicAdd(done, 1u) == warps - 1u) {
-      atomicExch(taken, 0u);
-      atomicExch(done, 0u);
-    }
-  }
+  frame_exit(P, handed_over);
 }
 
 // j3dg_ray batches (find_closest / find_any through the C-ABI)
@@ -1282,12 +1306,12 @@ cudaError_t launch_render(const FrameParams& P, cudaStream_t st) {
     blocks_tt = persistent_blocks(k_frame<true, true>, kFrameThreads);
     blocks_lt = persistent_blocks(k_frame<false, true>, kFrameThreads);
   }
-  // an overlapped frame finds its counters zeroed by the frame two before
-  // (which completed before the previous frame let this one start); any
-  // other frame zeroes them here
+  // an overlapped frame finds its counter slot zeroed by the slot's
+  // previous user (completed before this frame could start); any other
+  // frame zeroes the canvas's slots here
   const bool overlap = P.wait_seq != 0u && !P.raster;
   cudaError_t e = cudaSuccess;
-  if (!overlap) e = cudaMemsetAsync(P.work + 4, 0, 4 * sizeof(uint32_t), st);
+  if (!overlap) e = cudaMemsetAsync(P.work + 4, 0, 2 * kFrameDepth * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (P.raster) {
     static int blocks_s = 0, blocks_t = 0, blocks_r = 0;

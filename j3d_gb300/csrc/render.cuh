@@ -48,8 +48,9 @@ struct FrameParams {
   uint32_t shadow, textured, vertexcolors, shading;
   int shade_mode;  // 0: G-buffer only; 1: also plain shading into im (misses <- background)
   // [0..3] rasterised frames: [0] primary items taken, [1] shadow jobs queued,
-  // [2] taken; k_frame: [4 + (seq & 1)] items taken, [6 + (seq & 1)] warps
-  // done (the frame's last warp zeroes both)
+  // [2] taken; k_frame: [4 + seq % kFrameDepth] items taken,
+  // [4 + kFrameDepth + seq % kFrameDepth] warps done (the frame's last warp
+  // zeroes both)
   uint32_t* work;
   uint32_t* status;
   unsigned long long* counters;  // optional [node visits, triangle tests]
@@ -73,8 +74,15 @@ struct FrameParams {
   // pixel carries wait_seq, so that every pixel's writes stay in frame order.
   uint32_t* stamps;
   uint32_t seq, wait_seq;
+  // frame kernels of the context, in launch order: launch is this one's
+  // number (>= 1), ring[launch % kFrameDepth] the number of the last frame
+  // kernel that released that entry (at its end, once every frame before it
+  // had completed)
+  uint32_t* ring;
+  uint32_t launch;
 };
-static const uint32_t kCanvasWorkWords = 8;  // FrameParams::work
+static const uint32_t kFrameDepth = 4;                     // frame kernels in flight at most
+static const uint32_t kCanvasWorkWords = 4 + 2 * kFrameDepth;  // FrameParams::work
 
 cudaError_t launch_render(const FrameParams& P, cudaStream_t st);
 // all frames in one persistent launch; offsets = prefix sums of primary_items

@@ -15,6 +15,7 @@ j3d's canvas + qbvh, all threads) on a bounded sample of the same frames.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -40,7 +41,10 @@ RECORD_BYTES = 32 + 4  # G-buffer record + RGBA8 per primary ray
 # --warmup 1 --no-cpu --no-side`), per BVH builder:
 #   ploc: DRAM 483.7 MB, L2 2401.3 MB (SAH top levels + PLOC below 64
 #         triangles, cost-optimal collapse, depth-first node order, parked
-#         finishes, 6 blocks per SM, next-node prefetch)
+#         finishes, 6 blocks per SM, next-node prefetch; captured before
+#         frames overlapped, with the same traversal: on the overlapped
+#         build that multi-pass capture ended in an Xid 31 during ncu's
+#         memory save and restore, and it was not repeated)
 #   lbvh: DRAM 533.9 MB, L2 1837.1 MB (level-order nodes, finishes in the
 #         tracing loop, 5 blocks per SM; an older capture)
 FRAME_TRAFFIC = {"ploc": (483_742_752, 2_401_349_440),
@@ -285,7 +289,15 @@ def side_workloads(ctx, mesh, wl, args) -> dict:
         srv.mesh_bytes += int(mesh.info().device_bytes)
         names = list(srv.meshes)
         srv.run(poisson_requests(64, 1600.0, names, seed=Wk.SEED_BASE + 40), realtime=True)
+        # this process holds the headline's multi-GB arrays and their Python
+        # objects: collect once and freeze the heap, as a server process
+        # would, so that a collection pausing the host loop does not land in
+        # the latency tail (the dedicated serving run measures p99 1.8 ms;
+        # here, with the heap unfrozen, 8.6-26.9 ms)
+        gc.collect()
+        gc.freeze()
         st = srv.run(poisson_requests(600, 400.0, names, seed=Wk.SEED_BASE + 41), realtime=True)
+        gc.unfreeze()
         out["serve_config4_plain"] = {"requests": st.requests, "rate_per_s": 400, "p50_ms": round(st.p50_ms, 3),
                                       "p99_ms": round(st.p99_ms, 3), "frames_per_s": round(st.frames_per_s, 1),
                                       "mean_batch": round(st.mean_batch, 2),

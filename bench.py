@@ -547,6 +547,7 @@ def run_own(args):
         "config": CONFIG,
         "details": dict(parallelism="replicas" if ws > 1 else "single GPU",
                        frame_ms_mean=round(ms / N_CAMERAS, 4), frame_ms_p50=round(float(np.median(frame_ms)), 4),
+                       frame_ms_p50_note="per-frame timing events between the frames keep them from overlapping",
                        frame_ms_without_overlap=round(serial_frame_ms, 4),
                        raster_primary_frame_ms_mean=None if raster_frame_ms is None else round(raster_frame_ms, 4),
                        rays_per_step=rays_per_step, shadow_ray_fraction=round(sum(shadow_rays) / (prim * N_CAMERAS), 4),

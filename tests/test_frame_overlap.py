@@ -226,3 +226,78 @@ def test_downloads_of_overlapped_frames(gpu_ctx):
     for k, (a, b) in enumerate(zip(*runs)):
         assert np.array_equal(a[0], b[0]), f"downloaded frame {k}: G-buffer differs"
         assert np.array_equal(a[1], b[1]), f"downloaded frame {k}: image differs"
+
+
+def test_mixed_sequences_overlap_equal_serial(gpu_ctx):
+    """A seeded random sequence of 60 calls over three canvases of different
+    sizes and two scenes: plain frames (which may overlap), edges-mode frames,
+    rectangles (update_canvas), rasterised frames, render_scene +
+    canvas_to_image, asynchronous downloads and synchronous reads in
+    between. Run with overlap on and off: every read and every final canvas
+    is identical."""
+    torch = pytest.importorskip("torch")
+    from j3d_gb300 import (PRIMARY_AUTO, PRIMARY_RASTER, Matcap, Mesh, Scene, settings, workloads as W)
+    rng = np.random.default_rng(2024)
+    V1, T1 = W.torus(400, 200, seed=W.SEED_BASE + 130)
+    V2, T2 = W.icosphere(5, W.SEED_BASE + 131)
+    m1, m2 = Mesh(gpu_ctx, V1, T1), Mesh(gpu_ctx, V2, T2)
+    scenes = []
+    for m in (m1, m2):
+        sc = Scene()
+        sc.add_object(m, db_id=len(scenes) + 1)
+        sc.prepare_scene()
+        sc.unzoom()
+        scenes.append(sc)
+    poses = W.cameras(16, W.SEED_BASE + 132, 2.2, 3.8)
+    sizes = [(640, 480), (800, 600), (320, 240)]
+    ops = []
+    for _ in range(60):
+        ops.append((int(rng.integers(0, 100)), int(rng.integers(0, 3)), int(rng.integers(0, 2)),
+                    int(rng.integers(0, 16)), rng.uniform(size=4)))
+    mc = Matcap.make(gpu_ctx, 0)
+    runs = []
+    for on in (True, False):
+        gpu_ctx.set_frame_overlap(on)
+        cvs = [_canvas(gpu_ctx, w, h) for w, h in sizes]
+        bufs = [(torch.zeros(h * w * 32, dtype=torch.uint8, pin_memory=True),
+                 torch.zeros(h * w * 4, dtype=torch.uint8, pin_memory=True)) for w, h in sizes]
+        reads = []
+        for kind, ci, si, pi, u in ops:
+            cv, sc = cvs[ci], scenes[si]
+            w, h = sizes[ci]
+            sc.set_pose(poses[pi])
+            if kind < 55:  # plain frame
+                cv.render_frame(sc, mc)
+            elif kind < 63:  # edges mode (a shading kernel after the frame)
+                cv.update_settings(settings(shadow=True, edges=True))
+                cv.render_frame(sc, mc)
+                cv.update_settings(settings(shadow=True, edges=False))
+            elif kind < 71:  # a rectangle
+                x0, x1 = sorted((int(u[0] * w), int(u[1] * w)))
+                y0, y1 = sorted((int(u[2] * h), int(u[3] * h)))
+                cv.update_canvas(x0, y0, x1, y1, sc)
+            elif kind < 77:  # rasterised primary hits
+                gpu_ctx.set_primary_mode(PRIMARY_RASTER)
+                cv.render_frame(sc, mc)
+                gpu_ctx.set_primary_mode(PRIMARY_AUTO)
+            elif kind < 82:  # render_scene + canvas_to_image
+                cv.render_scene(sc)
+                cv.canvas_to_image(mc)
+            elif kind < 92:  # asynchronous download, read at the next wait
+                cv.download_wait()
+                cv.download_async(bufs[ci][0].numpy(), bufs[ci][1].numpy())
+            else:  # synchronous read
+                reads.append((cv.get_pixels(), cv.get_image()))
+        for ci, cv in enumerate(cvs):
+            cv.download_wait()
+            reads.append((bufs[ci][0].numpy().copy(), bufs[ci][1].numpy().copy()))
+            reads.append((cv.get_pixels(), cv.get_image()))
+            cv.close()
+        runs.append(reads)
+    gpu_ctx.set_frame_overlap(True)
+    gpu_ctx.set_primary_mode(PRIMARY_AUTO)
+    assert gpu_ctx.device_status() == 0
+    assert len(runs[0]) == len(runs[1])
+    for k, (a, b) in enumerate(zip(*runs)):
+        assert np.array_equal(np.asarray(a[0]).view(np.uint8), np.asarray(b[0]).view(np.uint8)), f"read {k}: G-buffer"
+        assert np.array_equal(np.asarray(a[1]).view(np.uint8), np.asarray(b[1]).view(np.uint8)), f"read {k}: image"

@@ -190,6 +190,7 @@ __device__ __forceinline__ void stamp_pixel(const FrameParams& P, size_t pix) {
 // warp-uniform: the next frame may start (the frame kFrameDepth - 1
 // launches before this one has released its ring entry)
 __device__ __forceinline__ bool handover_allowed(const FrameParams& P) {
+  if (!P.ring) return false;  // no ring: the block's exit hands over
   uint32_t rel = 0;
   if ((threadIdx.x & 31u) == 0) rel = ld_acquire(P.ring + ((P.launch + 1u) % kFrameDepth));
   rel = __shfl_sync(0xffffffffu, rel, 0);
@@ -209,8 +210,9 @@ __device__ __forceinline__ void frame_exit(const FrameParams& P, bool handed_ove
       atomicExch(P.work + 4 + slot, 0u);
       atomicExch(done, 0u);
       asm volatile("griddepcontrol.wait;" ::: "memory");
-      asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(P.ring + P.launch % kFrameDepth), "r"(P.launch)
-                   : "memory");
+      if (P.ring)
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(P.ring + P.launch % kFrameDepth), "r"(P.launch)
+                     : "memory");
     }
   }
 }

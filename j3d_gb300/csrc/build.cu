@@ -1987,10 +1987,10 @@ __global__ void k_ploc_done(BuildCtl* __restrict__ c, uint32_t nt, uint32_t top,
   cost_range(c, 0, top);
 }
 
-__global__ void k_cost_step(BuildCtl* __restrict__ c, uint32_t top, cudaGraphConditionalHandle h) {
+__global__ void k_cost_step(BuildCtl* __restrict__ c, uint32_t top, cudaGraphConditionalHandle h, uint32_t set) {
   ++c->pass;
-  cost_range(c, c->pass, top);
-  cudaGraphSetConditional(h, c->pass < c->n_pass ? 1u : 0u);
+  cost_range(c, c->pass, top);  // past the last pass: an empty range
+  if (set) cudaGraphSetConditional(h, c->pass < c->n_pass ? 1u : 0u);
 }
 
 __global__ void k_place_step(BuildCtl* __restrict__ c, uint32_t nt, cudaGraphConditionalHandle h, uint32_t set) {
@@ -2025,10 +2025,10 @@ __global__ void k_dfs_setup(BuildCtl* __restrict__ c, uint32_t* __restrict__ pos
   level_range(c, c->dfs_level);
 }
 
-__global__ void k_dfs_step(BuildCtl* __restrict__ c, uint32_t up, cudaGraphConditionalHandle h) {
+__global__ void k_dfs_step(BuildCtl* __restrict__ c, uint32_t up, cudaGraphConditionalHandle h, uint32_t set) {
   c->dfs_level += up ? 1 : -1;
-  level_range(c, c->dfs_level);
-  cudaGraphSetConditional(h, (c->dfs_level >= 0 && c->dfs_level < (int32_t)c->place_levels) ? 1u : 0u);
+  level_range(c, c->dfs_level);  // past the last level: an empty range
+  if (set) cudaGraphSetConditional(h, (c->dfs_level >= 0 && c->dfs_level < (int32_t)c->place_levels) ? 1u : 0u);
 }
 
 // the LBVH's collapse starts at the root that k_lbvh left in top_ctr[0]
@@ -2293,7 +2293,9 @@ static cudaError_t enqueue_tree_ploc(BuildPlan& P, cudaStream_t st, cudaStream_t
   // cost programme, children before parents
   J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
     launch_collapse_cost(W, P.child, P.box, P.count, soup, c->lohi, P.leaf, P.dp_cost, P.dp_dec, s);
-    k_cost_step<<<1, 1, 0, s>>>(c, P.top ? 1u : 0u, h);
+    k_cost_step<<<1, 1, 0, s>>>(c, P.top ? 1u : 0u, h, 0u);
+    launch_collapse_cost(W, P.child, P.box, P.count, soup, c->lohi, P.leaf, P.dp_cost, P.dp_dec, s);
+    k_cost_step<<<1, 1, 0, s>>>(c, P.top ? 1u : 0u, h, 1u);
   }));
   // placement, level by level
   J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
@@ -2381,12 +2383,16 @@ static cudaError_t enqueue_tree(BuildPlan& P, cudaStream_t st, cudaStream_t side
     k_dfs_setup<<<1, 1, 0, st>>>(c, P.dfs_pos, 0u);
     J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
       k_dfs_size<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size);
-      k_dfs_step<<<1, 1, 0, s>>>(c, 0u, h);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 0u, h, 0u);
+      k_dfs_size<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 0u, h, 1u);
     }));
     k_dfs_setup<<<1, 1, 0, st>>>(c, P.dfs_pos, 1u);
     J3DG_EQ(capture_while(st, side, [&](cudaStream_t s, cudaGraphConditionalHandle h) {
       k_dfs_place<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size, P.dfs_pos);
-      k_dfs_step<<<1, 1, 0, s>>>(c, 1u, h);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 1u, h, 0u);
+      k_dfs_place<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size, P.dfs_pos);
+      k_dfs_step<<<1, 1, 0, s>>>(c, 1u, h, 1u);
     }));
     k_dfs_permute<WW><<<(nt + 255) / 256, 256, 0, st>>>(P.wide, &c->n_wide, P.dfs_pos, P.nodes);
   };

@@ -23,7 +23,7 @@
 
 namespace j3dg {
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
-              std::string& err);
+              cudaEvent_t done, std::string& err);
 struct RebuildLane;
 int rebuild_lane_alloc(uint32_t nt_max, uint32_t nv_max, uint32_t W, bool ploc, bool lbvh, cudaStream_t st,
                        RebuildLane** out, std::string& err);
@@ -789,7 +789,7 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
     msg = std::string("mesh_build upload: ") + cudaGetErrorString(e);
   } else {
     std::string err;
-    rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, st, c->d_status, err);
+    rc = j3dg::build_bvh(m, dV, (const uint32_t*)m->d_index, st, c->d_status, ev1, err);  // ev1: the BVH is ready
     if (rc == J3DG_OK && (m->build_flags & J3DG_BUILD_REBUILDABLE)) {  // the vertices a batch rebuilds from
       cudaError_t ev = cudaMalloc(&m->d_verts, sizeof(float) * 3 * (size_t)nv);
       if (ev == cudaSuccess)
@@ -800,7 +800,6 @@ int mesh_build_on(j3dg_ctx* c, const float* V, uint32_t nv, const uint32_t* T, u
       }
     }
     if (rc == J3DG_OK) {
-      cudaEventRecord(ev1, st);
       cudaEventSynchronize(ev1);
       cudaEventElapsedTime(&m->build_ms, ev0, ev1);
     } else {

@@ -2422,7 +2422,7 @@ static cudaError_t enqueue_build(BuildPlan& P, const float* dV, const uint32_t* 
 // the tree's part, launch it, then take the tree's size from the device and
 // keep an exactly sized copy of the nodes.
 static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
-                           std::string& err) {
+                           cudaEvent_t done, std::string& err) {
   BuildPlan P;
   P.nv = m->nv;
   P.nt = m->nt;
@@ -2479,6 +2479,7 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
       e = cudaMallocAsync(&m->d_nodes, bytes, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(m->d_nodes, P.nodes, bytes, cudaMemcpyDeviceToDevice, st);
     }
+    if (e == cudaSuccess && done) e = cudaEventRecord(done, st);  // the BVH is ready; the rest is clean-up
     if (e == cudaSuccess) {
       m->d_normals = P.normals;
       m->d_tris = P.tris_out;
@@ -2569,12 +2570,13 @@ cudaError_t rebuild_enqueue(RebuildLane* L, const j3dg_mesh* m, cudaStream_t st,
 }
 
 // Builds the device BVH. dV and dT are device arrays. On success fills the
-// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals). Both
-// builders go through build_bvh_graph; a mesh of at most one leaf is built
-// here.
+// mesh fields (bbox, scale, nodes, leaf-ordered triangles, normals); `done`
+// (may be null) is recorded on st once the BVH is ready, before the host's
+// clean-up (the build time is taken up to it). Both builders go through
+// build_bvh_graph; a mesh of at most one leaf is built here.
 int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st, uint32_t* d_status,
-              std::string& err) {
-  if (m->nt > m->leaf_size) return build_bvh_graph(m, dV, dT, st, d_status, err);
+              cudaEvent_t done, std::string& err) {
+  if (m->nt > m->leaf_size) return build_bvh_graph(m, dV, dT, st, d_status, done, err);
   int rc = J3DG_OK;
   const uint32_t nv = m->nv, nt = m->nt;
   float* d_part = nullptr;
@@ -2617,6 +2619,7 @@ int build_bvh(j3dg_mesh* m, const float* dV, const uint32_t* dT, cudaStream_t st
   J3DG_CK(cudaMallocAsync(&m->d_slot_of, sizeof(uint32_t) * (size_t)nt, st));
   k_slot_of<<<1, 256, 0, st>>>((const float4*)m->d_tris, nt, (uint32_t*)m->d_slot_of, d_status);
   J3DG_CK(cudaGetLastError());
+  if (done) J3DG_CK(cudaEventRecord(done, st));
 
 cleanup:
   if (d_part) cudaFreeAsync(d_part, st);

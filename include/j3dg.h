@@ -134,7 +134,7 @@ typedef struct j3dg_build_opts {
    triangles and parallel locally-ordered clustering (Meister and Bittner
    2018) within them, collapsed by a cost-optimal programme: the fewest node
    visits per ray. J3DG_BUILD_LBVH splits at Morton prefixes instead (4-wide
-   only): about 40 % of the build time (12.2 vs 30.7 ms for 28M triangles),
+   only): about 40 % of the build time (12.0 vs 30.6 ms for 28M triangles),
    about 19 % more node visits per ray. Either build is one CUDA
    graph with device-driven level loops. The traversal results are the same
    for either tree. */

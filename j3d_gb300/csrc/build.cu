@@ -2131,7 +2131,10 @@ struct BuildPlan {
 
 static const int kBBoxBlocks = 1024;
 
-static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st, bool outputs = true) {
+// outputs: the mesh's arrays too (else the mesh's own: a rebuild in place);
+// node_bound: with them, a node array at the size bound (rebuildable meshes;
+// other builds write the nodes into an array of the tree's size at the end)
+static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st, bool outputs = true, bool node_bound = true) {
   const size_t nt = P.nt, F4 = J3DG_NODE_F4(P.W);
   cudaError_t e = cudaSuccess;
   auto A = [&](auto*& p, size_t bytes) {
@@ -2196,7 +2199,7 @@ static cudaError_t plan_alloc(BuildPlan& P, cudaStream_t st, bool outputs = true
   if (outputs) {  // else the mesh's own arrays (a rebuild in place)
     A(P.normals, sizeof(float4) * nt);
     A(P.tris_out, sizeof(float4) * 3 * nt);
-    A(P.nodes, sizeof(float4) * F4 * nt);  // the wide nodes are at most nt - 1
+    if (node_bound) A(P.nodes, sizeof(float4) * F4 * nt);  // the wide nodes are at most nt - 1
     A(P.slot_of, sizeof(uint32_t) * nt);
   }
   return e;
@@ -2368,10 +2371,12 @@ static cudaError_t enqueue_prefix(BuildPlan& P, const float* dV, const uint32_t*
   return e;
 }
 
-// The rest: the tree, its wide nodes, the depth-first numbering and the
+// The rest: the tree, its wide nodes, the depth-first numbering (and, with
+// `permute`, the nodes written in that order into P.nodes) and the
 // triangles' slots; its level loops are conditional while nodes, so `st`
 // must be capturing.
-static cudaError_t enqueue_tree(BuildPlan& P, cudaStream_t st, cudaStream_t side, uint32_t* d_status) {
+static cudaError_t enqueue_tree(BuildPlan& P, cudaStream_t st, cudaStream_t side, uint32_t* d_status,
+                                bool permute = true) {
   const uint32_t nt = P.nt, W = P.W;
   BuildCtl* c = P.ctl;
   cudaError_t e = cudaSuccess;
@@ -2394,7 +2399,7 @@ static cudaError_t enqueue_tree(BuildPlan& P, cudaStream_t st, cudaStream_t side
       k_dfs_place<WW><<<kStrideBlocks, 256, 0, s>>>(P.wide, c->lohi, P.dfs_size, P.dfs_pos);
       k_dfs_step<<<1, 1, 0, s>>>(c, 1u, h, 1u);
     }));
-    k_dfs_permute<WW><<<(nt + 255) / 256, 256, 0, st>>>(P.wide, &c->n_wide, P.dfs_pos, P.nodes);
+    if (permute) k_dfs_permute<WW><<<(nt + 255) / 256, 256, 0, st>>>(P.wide, &c->n_wide, P.dfs_pos, P.nodes);
   };
   if (W == 2)
     dfs(std::integral_constant<int, 2>());
@@ -2438,12 +2443,12 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
   BuildCtl h;
   float hbb[6];
   int rc = J3DG_OK;
-  cudaError_t e = plan_alloc(P, st);
+  cudaError_t e = plan_alloc(P, st, true, (m->build_flags & J3DG_BUILD_REBUILDABLE) != 0);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = enqueue_prefix(P, dV, dT, st, d_status);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    const cudaError_t eq = enqueue_tree(P, st, side, d_status);
+    const cudaError_t eq = enqueue_tree(P, st, side, d_status, false);
     e = cudaStreamEndCapture(st, &g);
     if (eq != cudaSuccess) e = eq;
   }
@@ -2471,13 +2476,28 @@ static int build_bvh_graph(j3dg_mesh* m, const float* dV, const uint32_t* dT, cu
     m->n_nodes = h.n_wide;
     m->max_depth = h.max_depth;
     m->root_ref = 0;
+    // the nodes in depth-first order into an array of the tree's size (a
+    // rebuildable mesh keeps the array at the size bound: rebuilds write in
+    // place)
     const size_t bytes = sizeof(float4) * J3DG_NODE_F4(P.W) * (size_t)m->n_nodes;
-    if (m->build_flags & J3DG_BUILD_REBUILDABLE) {  // the node array stays at the size bound: rebuilds write in place
+    if (m->build_flags & J3DG_BUILD_REBUILDABLE) {
       m->d_nodes = P.nodes;
       P.nodes = nullptr;
     } else {
-      e = cudaMallocAsync(&m->d_nodes, bytes, st);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(m->d_nodes, P.nodes, bytes, cudaMemcpyDeviceToDevice, st);
+      e = cudaMallocAsync(&m->d_nodes, bytes ? bytes : sizeof(float4) * J3DG_NODE_F4(P.W), st);
+    }
+    if (e == cudaSuccess) {
+      float4* out = (float4*)m->d_nodes;
+      const uint32_t grid = (m->n_nodes + 255) / 256;
+      if (grid) {
+        if (P.W == 2)
+          k_dfs_permute<2><<<grid, 256, 0, st>>>(P.wide, &P.ctl->n_wide, P.dfs_pos, out);
+        else if (P.W == 8)
+          k_dfs_permute<8><<<grid, 256, 0, st>>>(P.wide, &P.ctl->n_wide, P.dfs_pos, out);
+        else
+          k_dfs_permute<4><<<grid, 256, 0, st>>>(P.wide, &P.ctl->n_wide, P.dfs_pos, out);
+        e = cudaGetLastError();
+      }
     }
     if (e == cudaSuccess && done) e = cudaEventRecord(done, st);  // the BVH is ready; the rest is clean-up
     if (e == cudaSuccess) {
